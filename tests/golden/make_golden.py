@@ -1,0 +1,130 @@
+"""Regenerates the golden fixtures in this directory from the reference itself.
+
+Each case writes a synthetic (or the reference's own test) mesh as SU2, runs
+the reference's code on it (oracle/_ref/ref_driver, built by
+oracle/build_ref.sh from the reference sources against the Eigen API shim) and
+stores every dumped array plus the case configuration in ``<case>.npz``.
+
+Runs only where the reference sources exist (the development container):
+
+    oracle/build_ref.sh && python tests/golden/make_golden.py
+
+The arrays are the reference's own outputs: element order is the reference
+parser's (hash-set) order, so the fixtures also carry the element
+connectivity the reference used.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from nonlocal_gb300.meshgen import BILINEAR, SERENDIPITY, structured_quad_mesh, write_su2  # noqa: E402
+
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+REFERENCE = os.environ.get("NONLOCAL_REFERENCE", "/root/reference")
+REF_MESHES = os.path.join(REFERENCE, "tests", "solvers_2d", "meshes")
+
+# name -> (mesh spec, driver arguments)
+CASES = {
+    # config-2 shape, scaled: bilinear, fast polynomial bell, left T=0, right flux 1
+    "b12_fastpoly": ({"nx": 12, "ny": 12, "element": BILINEAR},
+                     {"mode": "stationary2d", "influence": "fast_polynomial", "radius": 0.2, "local_weight": 0.5,
+                      "conductivity": "1", "bc.left": "temperature:0", "bc.right": "flux:1", "tolerance": 1e-14}),
+    # config-3 shape, scaled: jittered 8-node serendipity, normal kernel, orthotropic
+    "s6_exp_ortho_jitter": ({"nx": 6, "ny": 6, "element": SERENDIPITY, "jitter": 0.2, "seed": 0},
+                            {"mode": "stationary2d", "influence": "exponential", "n": 2, "p": 2, "q": 0.5,
+                             "radius": 0.3, "local_weight": 0.3, "conductivity": "1,0.1",
+                             "bc.up": "temperature:1", "bc.down": "temperature:0", "tolerance": 1e-14}),
+    # general polynomial kernel, no radius widening, source term, anisotropic conductivity
+    "b10_poly_no_aniso": ({"nx": 10, "ny": 8, "element": BILINEAR, "height": 0.8, "jitter": 0.15, "seed": 3},
+                          {"mode": "stationary2d", "influence": "polynomial", "n": 2, "p": 4, "q": 2,
+                           "radius": 0.25, "local_weight": 0.4, "conductivity": "2,1,0.5", "strategy": "NO",
+                           "source": 1.5, "bc.down": "temperature:0", "bc.left": "temperature:0.5",
+                           "bc.up": "flux:-1", "tolerance": 1e-14}),
+    # constant kernel on serendipity, flux on two sides
+    "s5_const": ({"nx": 5, "ny": 5, "element": SERENDIPITY},
+                 {"mode": "stationary2d", "influence": "constant", "n": 2, "radius": 0.35, "local_weight": 0.6,
+                  "conductivity": "1", "bc.left": "temperature:0", "bc.right": "flux:1", "bc.up": "flux:0.5",
+                  "tolerance": 1e-14}),
+    # reference's own known-answer tests (local limit)
+    "ref_square16_manufactured": ({"su2": "square_1x1_16el_uniform_mesh.su2"},
+                                  {"mode": "stationary2d", "local_weight": 1, "conductivity": "10,10,0",
+                                   "source": "manufactured", "bc.Left": "temperature:manufactured",
+                                   "bc.Right": "temperature:manufactured", "bc.Top": "temperature:manufactured",
+                                   "bc.Bottom": "temperature:manufactured", "tolerance": 1e-14}),
+    "ref_solid_ring": ({"su2": "solid_ring.su2"},
+                       {"mode": "stationary2d", "local_weight": 1, "conductivity": "1",
+                        "bc.Inner": "temperature:0", "bc.Outer": "temperature:1", "tolerance": 1e-14}),
+    # nonstationary 2D: left T = sin(10 t), identity-preconditioned CG per step
+    "b8_nonstationary": ({"nx": 8, "ny": 8, "element": BILINEAR},
+                         {"mode": "nonstationary2d", "influence": "fast_polynomial", "radius": 0.3,
+                          "local_weight": 0.5, "conductivity": "1", "dt": 1e-3, "steps": 5, "omega": 10,
+                          "dirichlet_group": "left"}),
+    # 1D stationary, the full 1000-element quadratic configuration and a small linear one
+    "d1_quadratic_1000": ({"none": True},
+                          {"mode": "stationary1d", "elements": 1000, "order": 2, "radius": 0.1, "local_weight": 0.5,
+                           "influence": "bell", "conductivity": 1, "left_temperature": 0, "right_flux": 1,
+                           "source": "sin"}),
+    "d1_linear_40_triangle": ({"none": True},
+                              {"mode": "stationary1d", "elements": 40, "order": 1, "quadrature": 2, "radius": 0.1,
+                               "local_weight": 0.3, "influence": "triangle", "conductivity": 2,
+                               "left_temperature": 1, "right_flux": 0.5, "source": "sin"}),
+}
+
+
+def load_dump(path: str) -> dict[str, np.ndarray]:
+    out = {}
+    with open(os.path.join(path, "manifest.txt")) as f:
+        for line in f:
+            name, dt, shape = line.split()
+            arr = np.fromfile(os.path.join(path, name + ".bin"), dtype=np.dtype(dt))
+            out[name] = arr.reshape([int(s) for s in shape.split(",")])
+    gfile = os.path.join(path, "groups_1d.txt")
+    if os.path.exists(gfile):
+        with open(gfile) as f:
+            out["groups_1d"] = np.array([g.strip() for g in f if g.strip()])
+    return out
+
+
+def run_case(name: str, mesh_spec: dict, args: dict, tmp: str) -> None:
+    args = dict(args)
+    if "su2" in mesh_spec:
+        args["mesh"] = os.path.join(REF_MESHES, mesh_spec["su2"])
+    elif "nx" in mesh_spec:
+        spec = dict(mesh_spec)
+        m = structured_quad_mesh(spec.pop("nx"), spec.pop("ny"), spec.pop("element"), **spec)
+        args["mesh"] = os.path.join(tmp, name + ".su2")
+        write_su2(m, args["mesh"])
+    out = os.path.join(tmp, name)
+    cmd = [DRIVER] + [f"{k}={v}" for k, v in args.items()] + [f"out={out}"]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    data = load_dump(out)
+    for k in [k for k in data if k.startswith("t_")]:
+        data.pop(k)   # wall times are not golden
+    cfg = {k: v for k, v in args.items() if k != "mesh"}
+    cfg["mesh_spec"] = mesh_spec
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), config=json.dumps(cfg), **data)
+    print(f"{name}: {sorted(data)}")
+
+
+def main() -> None:
+    if not os.path.exists(DRIVER):
+        raise SystemExit("build oracle/_ref/ref_driver first (oracle/build_ref.sh)")
+    only = set(sys.argv[1:])
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (spec, args) in CASES.items():
+            if not only or name in only:
+                run_case(name, spec, args, tmp)
+
+
+if __name__ == "__main__":
+    main()
