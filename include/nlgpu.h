@@ -1,0 +1,226 @@
+/*
+ * nlgpu: GB300 (sm_103a) implementation of NonLocFEM's nonlocal thermal hot
+ * path behind a plain C ABI.
+ *
+ * Every entry point takes plain host pointers and sizes (no C++ or CUDA types
+ * in the signatures) and returns an nlgpu_status.  A context (nlgpu_ctx) owns
+ * the device copies of one problem: mesh, neighbour lists, matrices,
+ * preconditioner and solver vectors.  One context per host thread; calls on
+ * one context are serialised on the context's CUDA stream.
+ *
+ * Index conventions follow the reference application: node and element
+ * numbers are int64 on the boundary (mesh_2d<T, I> with I = int64_t in the
+ * reference's tests), matrix row pointers and column indices are int64
+ * (Eigen::SparseMatrix<T, RowMajor, J> with J = int64_t, NonLocFEM/main.cpp:15).
+ * Matrices cross the boundary in the reference's storage: the upper triangle
+ * of the symmetric "inner" part, full rows of the "bound" part, CSR with
+ * sorted columns (conductivity_matrix_2d.hpp:39-72).
+ */
+#ifndef NLGPU_H
+#define NLGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nlgpu_ctx nlgpu_ctx;
+
+/* Status codes.  The reference throws std::domain_error / std::logic_error;
+ * across the C ABI those become NLGPU_ERR_ARG / NLGPU_ERR_STATE. */
+enum {
+    NLGPU_OK = 0,
+    NLGPU_ERR_ARG = 1,          /* invalid argument (sizes, indices, kinds) */
+    NLGPU_ERR_CUDA = 2,         /* a CUDA runtime call failed (no device, launch error, ...) */
+    NLGPU_ERR_UNSUPPORTED = 3,  /* valid input outside what this build implements */
+    NLGPU_ERR_STATE = 4,        /* call order violated (e.g. solve before assembly) */
+    NLGPU_ERR_NUMERICAL = 5,    /* factorisation breakdown after all diagonal shifts */
+    NLGPU_ERR_NO_CONVERGENCE = 6, /* iteration limit reached before the tolerance */
+    NLGPU_ERR_OUT_OF_MEMORY = 7,
+    NLGPU_ERR_TIMEOUT = 8       /* a bounded device-side wait gave up */
+};
+
+/* element_2d_t numbering (libraries/mesh/mesh_2d/elements_set.hpp:231-237) */
+enum { NLGPU_BILINEAR = 2, NLGPU_QUADRATIC_SERENDIPITY = 3 };
+
+/* influence kinds (libraries/solvers/solver_2d/influence_functions_2d.hpp:39-148) */
+enum { NLGPU_INFLUENCE_CONSTANT = 0, NLGPU_INFLUENCE_POLYNOMIAL = 1,
+       NLGPU_INFLUENCE_EXPONENTIAL = 2, NLGPU_INFLUENCE_FAST_POLYNOMIAL = 3 };
+
+/* conductivity kinds (libraries/solvers/solver_2d/thermal/thermal_parameters_2d.hpp:176-192);
+ * anisotropic components are ordered XX, YY, XY (libraries/constants/nonlocal_constants.hpp:262) */
+enum { NLGPU_CONDUCTIVITY_ISOTROPIC = 0, NLGPU_CONDUCTIVITY_ORTHOTROPIC = 1, NLGPU_CONDUCTIVITY_ANISOTROPIC = 2 };
+
+/* diameter_expanding_strategy (libraries/mesh/mesh_2d/find_neighbours.hpp:357) */
+enum { NLGPU_EXPAND_NO = 0, NLGPU_EXPAND_MAX = 1, NLGPU_EXPAND_MIN = 2, NLGPU_EXPAND_MEAN = 3 };
+
+/* assemble_part (libraries/solvers/solver_2d/base/matrix_assembler_2d.hpp:301-305) */
+enum { NLGPU_PART_LOCAL = 0, NLGPU_PART_FULL = 2 };
+
+/* boundary condition kinds (thermal_boundary_conditions_2d.hpp:271-301) */
+enum { NLGPU_BC_TEMPERATURE = 0, NLGPU_BC_FLUX = 1 };
+
+/* matrices that can be copied out */
+enum { NLGPU_MATRIX_INNER = 0, NLGPU_MATRIX_BOUND = 1, NLGPU_MATRIX_LOCAL = 2 };
+
+/* preconditioners of the conjugate gradient */
+enum { NLGPU_PRECONDITIONER_IDENTITY = 0, NLGPU_PRECONDITIONER_ILLT = 1 };
+
+/* precision of the solve */
+enum { NLGPU_PRECISION_FP64 = 0, NLGPU_PRECISION_MIXED = 1 };
+
+/* Nonlocal model of one material: model_parameters<2, T> (equation_parameters.hpp:251-257)
+ * plus its influence function and constant conductivity (parameter_2d). */
+typedef struct nlgpu_model_2d {
+    int influence;            /* NLGPU_INFLUENCE_* */
+    int n;                    /* powered-distance exponent (2 = Euclidean) */
+    int p;                    /* polynomial / exponential exponent */
+    double q;                 /* polynomial power or exponential rate */
+    double radius[2];         /* nonlocal radii r1, r2 */
+    double local_weight;      /* p1; the model is nonlocal when p1 < 0.999 */
+    int conductivity_kind;    /* NLGPU_CONDUCTIVITY_* */
+    double conductivity[3];   /* lambda | (lx, ly) | (xx, yy, xy) */
+} nlgpu_model_2d;
+
+typedef struct nlgpu_solve_options {
+    double tolerance;         /* relative residual target (|b - Ax| / |b|) */
+    int64_t max_iterations;
+    int preconditioner;       /* NLGPU_PRECONDITIONER_* */
+    int precision;            /* NLGPU_PRECISION_* */
+} nlgpu_solve_options;
+
+typedef struct nlgpu_solve_report {
+    int64_t iterations;       /* CG iterations */
+    double residual;          /* final |b - Ax| / |b| (FP64, recomputed) */
+    double reference_residual;/* sqrt(r.z) / |b|, the reference's stopping measure */
+    int preconditioner_ok;    /* 0 if ILLT failed and identity was used */
+    int preconditioner_shifts;/* diagonal-shift attempts used by the factorisation */
+    int64_t nnz_inner;        /* stored entries of the upper inner matrix */
+    int64_t nnz_solver;       /* stored entries of the matrix the SpMV reads */
+    int64_t element_pairs;    /* sum over elements of the neighbour count */
+    double seconds_neighbours, seconds_pattern, seconds_assembly, seconds_boundary,
+           seconds_preconditioner, seconds_solve, seconds_total;
+} nlgpu_solve_report;
+
+/* ---- library ------------------------------------------------------------ */
+const char* nlgpu_status_string(int status);
+/* Message of the last failed call on the calling thread ("" if none). */
+const char* nlgpu_last_error(void);
+/* Device count seen by the CUDA runtime (0 when no GPU is visible). */
+int nlgpu_device_count(int* count);
+/* Number of kernels this library launched in the calling process so far. */
+int64_t nlgpu_kernel_launches(void);
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates a context on the current device.  `stream` is a cudaStream_t to run
+ * on, or NULL for a stream the context creates and owns. */
+int nlgpu_create(nlgpu_ctx** ctx, void* stream);
+int nlgpu_destroy(nlgpu_ctx* ctx);
+int nlgpu_synchronize(nlgpu_ctx* ctx);
+
+/* ---- mesh: mesh_2d<T, I>::mesh_2d + init (libraries/mesh/mesh_2d/mesh_2d.hpp:83-108)
+ * nodes: n_nodes x 2 (x, y); elements: n_elements x nodes_per_element in the
+ * reference's local node order; one element type per mesh. */
+int nlgpu_mesh_2d(nlgpu_ctx* ctx, int element_type, int64_t n_nodes, const double* nodes,
+                  int64_t n_elements, const int64_t* elements);
+/* Quadrature data as mesh_2d stores it: coordinates [e][q][2], |J| [e][q],
+ * derivatives dN.adj(J) [e][i][q][2] (mesh_container_2d_utils.hpp:385-408).
+ * Any pointer may be NULL. */
+int nlgpu_get_quadrature(nlgpu_ctx* ctx, double* qcoords, double* jacobians, double* derivatives);
+/* Element basis tables: qN, qNxi, qNeta [i][q], weights [q], N_i(0,0) [i]
+ * (element_2d_integrate.hpp:69-106).  sizes: nodes_per_element, qnodes. */
+int nlgpu_get_basis(nlgpu_ctx* ctx, int* nodes_per_element, int* qnodes, double* qN, double* qNxi,
+                    double* qNeta, double* weights, double* centre);
+
+/* ---- model ---------------------------------------------------------------- */
+int nlgpu_set_model_2d(nlgpu_ctx* ctx, const nlgpu_model_2d* model);
+/* Spatially varying isotropic conductivity, one value per quadrature point
+ * [e][q] (evaluate_conductivity.hpp:9-48).  With a nonlocal model this makes
+ * the problem non-symmetric (problem_settings.hpp:252-254). */
+int nlgpu_set_conductivity_field(nlgpu_ctx* ctx, const double* values);
+/* Heat capacity and density for the nonstationary solver (parameter_2d). */
+int nlgpu_set_capacity(nlgpu_ctx* ctx, double capacity, double density);
+
+/* ---- neighbours: mesh::find_neighbours (find_neighbours.hpp:469-510) ------- */
+/* Runs the bucketed centre-distance search with the widened radius.  Outputs
+ * (may be NULL): the widened radii [2] and the total number of pairs. */
+int nlgpu_find_neighbours(nlgpu_ctx* ctx, int strategy, double* search_radius, int64_t* pairs);
+/* Neighbour lists in the reference's order: offsets [n_elements + 1], list [pairs]. */
+int nlgpu_get_neighbours(nlgpu_ctx* ctx, int64_t* offsets, int64_t* list);
+
+/* ---- boundary conditions and right-hand side ------------------------------- */
+/* One boundary group: n_edges line elements of nodes_per_edge (2 or 3) nodes,
+ * local order (end, [middle,] end).  kind NLGPU_BC_TEMPERATURE with a constant
+ * value (node_values may give one value per listed node instead), or
+ * NLGPU_BC_FLUX with a constant flux (thermal_boundary_conditions_2d.hpp:271-301).
+ * Groups apply in the order added; a node in two temperature groups keeps the
+ * first non-zero value (boundary_condition_first_kind_2d.hpp:16-26). */
+int nlgpu_add_boundary_2d(nlgpu_ctx* ctx, int kind, int64_t n_edges, int nodes_per_edge,
+                          const int64_t* edges, double value, const double* node_values);
+/* Volume source: constant value, or one value per quadrature point [e][q] when
+ * per_qnode is not NULL (right_part_2d.hpp:10-35). */
+int nlgpu_set_source(nlgpu_ctx* ctx, double value, const double* per_qnode);
+/* Overrides the Dirichlet value of each Dirichlet node (values [n_nodes]). */
+int nlgpu_set_dirichlet_values(nlgpu_ctx* ctx, const double* values);
+int nlgpu_clear_boundaries(nlgpu_ctx* ctx);
+
+/* ---- assembly: conductivity_matrix_2d::compute (conductivity_matrix_2d.hpp:166-193)
+ * part NLGPU_PART_FULL assembles p1*K_local + (1-p1)*K_nonlocal into the
+ * inner/bound pair; NLGPU_PART_LOCAL assembles p1*K_local (the matrix the
+ * ILLT preconditioner is built from).  Dirichlet rows get a unit diagonal. */
+int nlgpu_conductivity_matrix_2d(nlgpu_ctx* ctx, int part, int64_t* nnz_inner, int64_t* nnz_bound);
+/* Copies a matrix out in the reference's CSR storage (see top of file). */
+int nlgpu_get_matrix(nlgpu_ctx* ctx, int which, int64_t* rowptr, int64_t* col, double* val);
+/* Right-hand side after boundary conditions: flux and source integrals,
+ * f -= K_bound x_D, f[D] = x_D (boundary_condition_first_kind_2d.hpp:50-59).
+ * rhs_init (may be NULL) receives the vector before the first-kind step. */
+int nlgpu_get_rhs(nlgpu_ctx* ctx, double* rhs, double* rhs_init);
+
+/* ---- solve: stationary_heat_equation_solver_2d (stationary_heat_equation_solver_2d.hpp:46-120)
+ * Runs neighbours (if not yet run), both assemblies, boundary conditions,
+ * ILLT(p1 K_local) and preconditioned CG; writes the nodal temperature
+ * [n_nodes].  report may be NULL. */
+int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* temperature,
+                        nlgpu_solve_report* report);
+/* Only the solve stage on the already assembled system (for timing it alone). */
+int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* temperature,
+                          nlgpu_solve_report* report);
+
+/* ---- slae::conjugate_gradient on caller matrices (conjugate_gradient.hpp:15-79)
+ * A: upper CSR of a symmetric matrix with the diagonal first in each row;
+ * optional ILLT preconditioner built from P (upper CSR, same size), the
+ * eigen_ILLT_preconditioner of eigen_preconditioner.hpp:136-137.
+ * x0 may be NULL (zero start).  Stops when |b - Ax| / |b| <= tolerance. */
+int nlgpu_cg_solve(nlgpu_ctx* ctx, int64_t n, const int64_t* a_rowptr, const int64_t* a_col,
+                   const double* a_val, const int64_t* p_rowptr, const int64_t* p_col,
+                   const double* p_val, const double* b, const double* x0, double tolerance,
+                   int64_t max_iterations, double* x, nlgpu_solve_report* report);
+
+/* ---- nonstationary_heat_equation_solver_2d (nonstationary_heat_equation_solver_2d.hpp:16-106)
+ * compute: assembles dt*K + C (unit Dirichlet diagonal) for the current mesh,
+ * model and boundary groups; initial temperature [n_nodes] or NULL (zero).
+ * step: one implicit Euler step with the Dirichlet nodes set to
+ * dirichlet_value (or per-node dirichlet_values when not NULL), CG with the
+ * identity preconditioner and x0 = previous temperature. */
+int nlgpu_nonstationary_2d_compute(nlgpu_ctx* ctx, double time_step, const double* initial);
+int nlgpu_nonstationary_2d_step(nlgpu_ctx* ctx, double dirichlet_value, const double* dirichlet_values,
+                                double tolerance, int64_t max_iterations, double* temperature,
+                                int64_t* iterations);
+
+/* ---- stationary_heat_equation_solver_1d (stationary_heat_equation_solver_1d.hpp:43-122)
+ * One segment [0, length] of `elements` Lagrange elements of `order` 1
+ * (Gauss-2) or 2 (Gauss-3), constant conductivity, influence kind
+ * 0 = polynomial_1d<2,1>, 1 = polynomial_1d<1,1>, 2 = normal, 3 = constant
+ * (influence_functions_1d.hpp:10-75), temperature t_left at x = 0, flux
+ * q_right at x = length, source sin(pi x) when sin_source != 0.  Writes the
+ * nodal temperature [elements * order + 1]. */
+int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double length, double radius,
+                        double local_weight, int influence, double conductivity, double t_left,
+                        double q_right, int sin_source, double* temperature);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NLGPU_H */

@@ -1,0 +1,137 @@
+"""Loads libnlgpu.so (the sm_103a CUDA library behind include/nlgpu.h) with ctypes.
+
+There is no CPU implementation behind this module: when the library is
+missing or cannot be loaded every call raises, and compute calls need a CUDA
+device.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libnlgpu.so")
+
+c_i64, c_d, c_p, c_int = ctypes.c_int64, ctypes.c_double, ctypes.c_void_p, ctypes.c_int
+
+OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "unsupported", 4: "call order violated",
+          5: "numerical breakdown", 6: "no convergence", 7: "out of device memory", 8: "device wait timed out"}
+
+BILINEAR, QUADRATIC_SERENDIPITY = 2, 3
+INFLUENCE = {"constant": 0, "polynomial": 1, "exponential": 2, "fast_polynomial": 3}
+CONDUCTIVITY_KIND = {1: 0, 2: 1, 3: 2}
+EXPAND = {"NO": 0, "MAX": 1, "MIN": 2, "MEAN": 3}
+PART_LOCAL, PART_FULL = 0, 2
+BC_TEMPERATURE, BC_FLUX = 0, 1
+MATRIX_INNER, MATRIX_BOUND, MATRIX_LOCAL = 0, 1, 2
+PRECONDITIONER = {"identity": 0, "illt": 1}
+PRECISION = {"fp64": 0, "mixed": 1}
+
+
+class NlgpuError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class Model2D(ctypes.Structure):
+    _fields_ = [("influence", c_int), ("n", c_int), ("p", c_int), ("q", c_d), ("radius", c_d * 2),
+                ("local_weight", c_d), ("conductivity_kind", c_int), ("conductivity", c_d * 3)]
+
+
+class SolveOptions(ctypes.Structure):
+    _fields_ = [("tolerance", c_d), ("max_iterations", c_i64), ("preconditioner", c_int), ("precision", c_int)]
+
+
+class SolveReport(ctypes.Structure):
+    _fields_ = [("iterations", c_i64), ("residual", c_d), ("reference_residual", c_d), ("preconditioner_ok", c_int),
+                ("preconditioner_shifts", c_int), ("nnz_inner", c_i64), ("nnz_solver", c_i64),
+                ("element_pairs", c_i64), ("seconds_neighbours", c_d), ("seconds_pattern", c_d),
+                ("seconds_assembly", c_d), ("seconds_boundary", c_d), ("seconds_preconditioner", c_d),
+                ("seconds_solve", c_d), ("seconds_total", c_d)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# name -> (restype, argtypes); every function declared in include/nlgpu.h
+SIGNATURES = {
+    "nlgpu_status_string": (ctypes.c_char_p, [c_int]),
+    "nlgpu_last_error": (ctypes.c_char_p, []),
+    "nlgpu_device_count": (c_int, [ctypes.POINTER(c_int)]),
+    "nlgpu_kernel_launches": (c_i64, []),
+    "nlgpu_create": (c_int, [ctypes.POINTER(c_p), c_p]),
+    "nlgpu_destroy": (c_int, [c_p]),
+    "nlgpu_synchronize": (c_int, [c_p]),
+    "nlgpu_mesh_2d": (c_int, [c_p, c_int, c_i64, c_p, c_i64, c_p]),
+    "nlgpu_get_quadrature": (c_int, [c_p, c_p, c_p, c_p]),
+    "nlgpu_get_basis": (c_int, [c_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), c_p, c_p, c_p, c_p, c_p]),
+    "nlgpu_set_model_2d": (c_int, [c_p, ctypes.POINTER(Model2D)]),
+    "nlgpu_set_conductivity_field": (c_int, [c_p, c_p]),
+    "nlgpu_set_capacity": (c_int, [c_p, c_d, c_d]),
+    "nlgpu_find_neighbours": (c_int, [c_p, c_int, c_p, ctypes.POINTER(c_i64)]),
+    "nlgpu_get_neighbours": (c_int, [c_p, c_p, c_p]),
+    "nlgpu_add_boundary_2d": (c_int, [c_p, c_int, c_i64, c_int, c_p, c_d, c_p]),
+    "nlgpu_set_source": (c_int, [c_p, c_d, c_p]),
+    "nlgpu_set_dirichlet_values": (c_int, [c_p, c_p]),
+    "nlgpu_clear_boundaries": (c_int, [c_p]),
+    "nlgpu_conductivity_matrix_2d": (c_int, [c_p, c_int, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)]),
+    "nlgpu_get_matrix": (c_int, [c_p, c_int, c_p, c_p, c_p]),
+    "nlgpu_get_rhs": (c_int, [c_p, c_p, c_p]),
+    "nlgpu_stationary_2d": (c_int, [c_p, ctypes.POINTER(SolveOptions), c_p, ctypes.POINTER(SolveReport)]),
+    "nlgpu_solve_assembled": (c_int, [c_p, ctypes.POINTER(SolveOptions), c_p, ctypes.POINTER(SolveReport)]),
+    "nlgpu_cg_solve": (c_int, [c_p, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_d, c_i64, c_p,
+                               ctypes.POINTER(SolveReport)]),
+    "nlgpu_nonstationary_2d_compute": (c_int, [c_p, c_d, c_p]),
+    "nlgpu_nonstationary_2d_step": (c_int, [c_p, c_d, c_p, c_d, c_i64, c_p, ctypes.POINTER(c_i64)]),
+    "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads the library (raising if it is missing) and sets every signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with nonlocal_gb300/build.py (nvcc, sm_103a)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        msg = load().nlgpu_last_error()
+        raise NlgpuError(status, msg.decode() if msg else "")
+
+
+def ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
+
+
+def f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def device_count() -> int:
+    n = c_int(0)
+    check(load().nlgpu_device_count(ctypes.byref(n)))
+    return n.value
+
+
+def kernel_launches() -> int:
+    return int(load().nlgpu_kernel_launches())

@@ -1,0 +1,630 @@
+// C ABI of the library (include/nlgpu.h): argument checks, call order,
+// host <-> device copies, and the stationary / nonstationary drivers.
+#include "common.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numbers>
+
+using namespace nlgpu;
+
+struct nlgpu_ctx : Ctx {};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template<class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return NLGPU_OK;
+    } catch (const nlgpu::error& e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return NLGPU_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return NLGPU_ERR_ARG;
+    }
+}
+
+double ipow_host(double x, int n) {
+    double r = 1.0;
+    while (n > 0) { if (n & 1) { r *= x; --n; } else { x *= x; n >>= 1; } }
+    return r;
+}
+
+double seconds(std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+}
+
+void reset_from_model(Ctx& c) {
+    c.neighbours_ready = false;
+    c.inner_ready = c.local_ready = c.nonstationary_ready = false;
+}
+
+void reset_from_boundary(Ctx& c) {
+    c.bc_ready = false;
+    c.inner_ready = c.local_ready = c.nonstationary_ready = false;
+}
+
+void ensure_neighbours(Ctx& c) {
+    if (!c.neighbours_ready) find_neighbours(c, c.strategy);
+}
+
+void ensure_boundary(Ctx& c) {
+    if (!c.bc_ready) boundary_vectors(c);
+}
+
+// conductivity_matrix_2d::compute(FULL) into inner/bound, and the solver's full rows
+void build_inner(Ctx& c) {
+    NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "mesh and model must be set before assembly");
+    ensure_boundary(c);
+    c.symmetric = !(c.model.nonlocal() && c.cond_field.n);   // problem_settings::is_symmetric (problem_settings.hpp:252-254)
+    if (c.model.nonlocal()) ensure_neighbours(c);
+    build_patterns(c, !c.model.nonlocal(), c.symmetric, c.inner, &c.bound, &c.full, &c.full_from_upper);
+    assemble_full(c);
+    fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
+    c.rhs.resize(size_t(c.n_nodes));
+    apply_first_kind(c, c.bound, c.rhs_init.p, c.rhs.p, c.x_dirichlet.p);
+    c.inner_ready = true;
+}
+
+// p1 * K_local with the reference's LOCAL theories (stationary_heat_equation_solver_2d.hpp:91-93)
+void build_local(Ctx& c) {
+    ensure_boundary(c);
+    build_patterns(c, true, true, c.local, nullptr, nullptr, nullptr);
+    assemble_local(c, c.local, c.model.p1, 0);
+    c.local_ready = true;
+}
+
+void download_csr(Ctx& c, const Csr& m, int64_t* rowptr, int64_t* col, double* val) {
+    if (rowptr) m.rowptr.download(rowptr, size_t(m.rows + 1), c.stream);
+    std::vector<int32_t> tmp;
+    if (col) { tmp.resize(size_t(m.nnz)); m.col.download(tmp.data(), tmp.size(), c.stream); }
+    if (val) m.val.download(val, size_t(m.nnz), c.stream);
+    NL_CUDA(cudaStreamSynchronize(c.stream));
+    if (col) for (size_t k = 0; k < tmp.size(); ++k) col[k] = tmp[k];
+}
+
+void fill_report(Ctx& c, nlgpu_solve_report* rep, const CgResult& r) {
+    if (!rep) return;
+    rep->iterations = r.iterations;
+    rep->residual = r.residual;
+    rep->reference_residual = r.reference_residual;
+    rep->preconditioner_ok = c.ilt.ok ? 1 : 0;
+    rep->preconditioner_shifts = c.ilt.attempts;
+    rep->nnz_inner = c.inner.nnz;
+    rep->nnz_solver = c.full.nnz;
+    rep->element_pairs = c.pairs;
+}
+
+CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep) {
+    NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "the system must be assembled first");
+    NL_REQUIRE(c.symmetric, NLGPU_ERR_UNSUPPORTED, "non-symmetric systems (variable conductivity with a nonlocal model) need BiCGSTAB");
+    const IncompleteCholesky* M = nullptr;
+    auto t0 = std::chrono::steady_clock::now();
+    if (o.preconditioner == NLGPU_PRECONDITIONER_ILLT) {
+        if (!c.local_ready) build_local(c);
+        ilt_build(c, c.local, c.ilt);
+        if (c.ilt.ok) M = &c.ilt;   // identity fallback (stationary_heat_equation_solver_2d.hpp:97-101)
+    } else {
+        c.ilt.ok = false;
+    }
+    NL_CUDA(cudaStreamSynchronize(c.stream));
+    if (rep) rep->seconds_preconditioner = seconds(t0);
+    t0 = std::chrono::steady_clock::now();
+    c.temperature.resize(size_t(c.n_nodes));
+    const CgResult r = cg_solve(c, c.full, M, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations, false);
+    if (rep) rep->seconds_solve = seconds(t0);
+    fill_report(c, rep, r);
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* nlgpu_status_string(int status) {
+    switch (status) {
+    case NLGPU_OK: return "ok";
+    case NLGPU_ERR_ARG: return "invalid argument";
+    case NLGPU_ERR_CUDA: return "CUDA error";
+    case NLGPU_ERR_UNSUPPORTED: return "unsupported";
+    case NLGPU_ERR_STATE: return "call order violated";
+    case NLGPU_ERR_NUMERICAL: return "numerical breakdown";
+    case NLGPU_ERR_NO_CONVERGENCE: return "no convergence";
+    case NLGPU_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case NLGPU_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+    }
+}
+
+const char* nlgpu_last_error(void) { return g_last_error.c_str(); }
+
+int nlgpu_device_count(int* count) {
+    if (!count) return NLGPU_ERR_ARG;
+    int n = 0;
+    const cudaError_t e = cudaGetDeviceCount(&n);
+    *count = e == cudaSuccess ? n : 0;
+    if (e != cudaSuccess) cudaGetLastError();
+    return NLGPU_OK;
+}
+
+int64_t nlgpu_kernel_launches(void) { return g_launches.load(); }
+
+int nlgpu_create(nlgpu_ctx** ctx, void* stream) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        int n = 0;
+        NL_CUDA(cudaGetDeviceCount(&n));
+        NL_REQUIRE(n > 0, NLGPU_ERR_CUDA, "no CUDA device");
+        auto* c = new nlgpu_ctx{};
+        if (stream) c->stream = static_cast<cudaStream_t>(stream);
+        else {
+            if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; NL_CUDA(cudaGetLastError()); }
+            c->own_stream = true;
+        }
+        *ctx = c;
+    });
+}
+
+int nlgpu_destroy(nlgpu_ctx* ctx) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        cudaStreamSynchronize(ctx->stream);
+        const bool own = ctx->own_stream;
+        cudaStream_t s = ctx->stream;
+        delete ctx;
+        if (own) cudaStreamDestroy(s);
+    });
+}
+
+int nlgpu_synchronize(nlgpu_ctx* ctx) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] { NL_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+int nlgpu_mesh_2d(nlgpu_ctx* ctx, int element_type, int64_t n_nodes, const double* nodes, int64_t n_elements,
+                  const int64_t* elements) {
+    if (!ctx || !nodes || !elements || n_nodes <= 0 || n_elements <= 0) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        c.basis = make_basis(element_type);
+        NL_REQUIRE(n_nodes < (int64_t(1) << 31) && n_elements * c.basis.nen < (int64_t(1) << 40), NLGPU_ERR_UNSUPPORTED,
+                   "mesh too large for 32-bit node numbers");
+        std::vector<int32_t> el(size_t(n_elements * c.basis.nen));
+        for (size_t k = 0; k < el.size(); ++k) {
+            NL_REQUIRE(elements[k] >= 0 && elements[k] < n_nodes, NLGPU_ERR_ARG, "element node out of range");
+            el[k] = int32_t(elements[k]);
+        }
+        c.element_type = element_type;
+        c.n_nodes = n_nodes; c.n_elems = n_elements;
+        c.nodes.upload(nodes, size_t(2 * n_nodes), c.stream);
+        c.elems.upload(el.data(), el.size(), c.stream);
+        mesh_init(c);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        c.cond_field.release(); c.source_q.release(); c.dirichlet_override.release();
+        c.groups.clear();
+        reset_from_model(c);
+        reset_from_boundary(c);
+    });
+}
+
+int nlgpu_get_quadrature(nlgpu_ctx* ctx, double* qcoords, double* jacobians, double* derivatives) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        if (qcoords) c.qcoord.download(qcoords, c.qcoord.n, c.stream);
+        if (jacobians) c.jac.download(jacobians, c.jac.n, c.stream);
+        if (derivatives) c.deriv.download(derivatives, c.deriv.n, c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int nlgpu_get_basis(nlgpu_ctx* ctx, int* nodes_per_element, int* qnodes, double* qN, double* qNxi, double* qNeta,
+                    double* weights, double* centre) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        const Basis& b = ctx->basis;
+        NL_REQUIRE(ctx->mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        if (nodes_per_element) *nodes_per_element = b.nen;
+        if (qnodes) *qnodes = b.nq;
+        const size_t m = size_t(b.nen * b.nq);
+        if (qN) std::memcpy(qN, b.qN, m * sizeof(double));
+        if (qNxi) std::memcpy(qNxi, b.qNxi, m * sizeof(double));
+        if (qNeta) std::memcpy(qNeta, b.qNeta, m * sizeof(double));
+        if (weights) std::memcpy(weights, b.w, size_t(b.nq) * sizeof(double));
+        if (centre) std::memcpy(centre, b.centre, size_t(b.nen) * sizeof(double));
+    });
+}
+
+int nlgpu_set_model_2d(nlgpu_ctx* ctx, const nlgpu_model_2d* model) {
+    if (!ctx || !model) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        ctx->model = make_model(*model);
+        ctx->model_ready = true;
+        reset_from_model(*ctx);
+    });
+}
+
+int nlgpu_set_conductivity_field(nlgpu_ctx* ctx, const double* values) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        if (values) c.cond_field.upload(values, size_t(c.n_elems * c.basis.nq), c.stream);
+        else c.cond_field.release();
+        c.inner_ready = c.local_ready = c.nonstationary_ready = false;
+    });
+}
+
+int nlgpu_set_capacity(nlgpu_ctx* ctx, double capacity, double density) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    ctx->capacity = capacity; ctx->density = density; ctx->nonstationary_ready = false;
+    return NLGPU_OK;
+}
+
+int nlgpu_find_neighbours(nlgpu_ctx* ctx, int strategy, double* search_radius, int64_t* pairs) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        find_neighbours(*ctx, strategy);
+        if (search_radius) { search_radius[0] = ctx->search_r[0]; search_radius[1] = ctx->search_r[1]; }
+        if (pairs) *pairs = ctx->pairs;
+        ctx->inner_ready = ctx->nonstationary_ready = false;
+    });
+}
+
+int nlgpu_get_neighbours(nlgpu_ctx* ctx, int64_t* offsets, int64_t* list) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.neighbours_ready, NLGPU_ERR_STATE, "no neighbour search yet");
+        if (offsets) c.noff.download(offsets, size_t(c.n_elems + 1), c.stream);
+        std::vector<int32_t> tmp(static_cast<size_t>(c.pairs));
+        if (list) c.nlist.download(tmp.data(), tmp.size(), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        if (list) for (size_t k = 0; k < tmp.size(); ++k) list[k] = tmp[k];
+    });
+}
+
+int nlgpu_add_boundary_2d(nlgpu_ctx* ctx, int kind, int64_t n_edges, int nodes_per_edge, const int64_t* edges,
+                          double value, const double* node_values) {
+    if (!ctx || !edges || n_edges < 0) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        NL_REQUIRE(kind == NLGPU_BC_TEMPERATURE || kind == NLGPU_BC_FLUX, NLGPU_ERR_ARG, "unknown boundary kind");
+        NL_REQUIRE(nodes_per_edge == 2 || nodes_per_edge == 3, NLGPU_ERR_UNSUPPORTED, "boundary edges have 2 or 3 nodes");
+        BoundaryGroup g;
+        g.kind = kind; g.nen = nodes_per_edge; g.n_edges = n_edges; g.value = value;
+        std::vector<int32_t> e(size_t(n_edges * nodes_per_edge));
+        for (size_t k = 0; k < e.size(); ++k) {
+            NL_REQUIRE(edges[k] >= 0 && edges[k] < c.n_nodes, NLGPU_ERR_ARG, "boundary node out of range");
+            e[k] = int32_t(edges[k]);
+        }
+        g.edges.upload(e.data(), e.size(), c.stream);
+        if (node_values) g.node_values.upload(node_values, e.size(), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        c.groups.push_back(std::move(g));
+        reset_from_boundary(c);
+    });
+}
+
+int nlgpu_set_source(nlgpu_ctx* ctx, double value, const double* per_qnode) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        c.source = value;
+        if (per_qnode) c.source_q.upload(per_qnode, size_t(c.n_elems * c.basis.nq), c.stream);
+        else c.source_q.release();
+        reset_from_boundary(c);
+    });
+}
+
+int nlgpu_set_dirichlet_values(nlgpu_ctx* ctx, const double* values) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        if (values) c.dirichlet_override.upload(values, size_t(c.n_nodes), c.stream);
+        else c.dirichlet_override.release();
+        reset_from_boundary(c);
+    });
+}
+
+int nlgpu_clear_boundaries(nlgpu_ctx* ctx) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    ctx->groups.clear();
+    ctx->source = 0.0;
+    ctx->source_q.release();
+    ctx->dirichlet_override.release();
+    reset_from_boundary(*ctx);
+    return NLGPU_OK;
+}
+
+int nlgpu_conductivity_matrix_2d(nlgpu_ctx* ctx, int part, int64_t* nnz_inner, int64_t* nnz_bound) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(part == NLGPU_PART_FULL || part == NLGPU_PART_LOCAL, NLGPU_ERR_ARG, "part is LOCAL or FULL");
+        NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "mesh and model must be set before assembly");
+        if (part == NLGPU_PART_FULL) {
+            build_inner(c);
+            if (nnz_inner) *nnz_inner = c.inner.nnz;
+            if (nnz_bound) *nnz_bound = c.bound.nnz;
+        } else {
+            build_local(c);
+            if (nnz_inner) *nnz_inner = c.local.nnz;
+            if (nnz_bound) *nnz_bound = 0;
+        }
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int nlgpu_get_matrix(nlgpu_ctx* ctx, int which, int64_t* rowptr, int64_t* col, double* val) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        if (which == NLGPU_MATRIX_INNER || which == NLGPU_MATRIX_BOUND) {
+            NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "FULL part not assembled");
+            download_csr(c, which == NLGPU_MATRIX_INNER ? c.inner : c.bound, rowptr, col, val);
+        } else if (which == NLGPU_MATRIX_LOCAL) {
+            NL_REQUIRE(c.local_ready, NLGPU_ERR_STATE, "LOCAL part not assembled");
+            download_csr(c, c.local, rowptr, col, val);
+        } else {
+            throw nlgpu::error{NLGPU_ERR_ARG, "unknown matrix"};
+        }
+    });
+}
+
+int nlgpu_get_rhs(nlgpu_ctx* ctx, double* rhs, double* rhs_init) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "FULL part not assembled");
+        if (rhs) c.rhs.download(rhs, size_t(c.n_nodes), c.stream);
+        if (rhs_init) c.rhs_init.download(rhs_init, size_t(c.n_nodes), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* temperature,
+                          nlgpu_solve_report* report) {
+    if (!ctx || !options || !temperature) return NLGPU_ERR_ARG;
+    int conv_status = NLGPU_OK;
+    const int rc = guarded([&] {
+        Ctx& c = *ctx;
+        const auto t0 = std::chrono::steady_clock::now();
+        const CgResult r = solve_system(c, *options, report);
+        c.temperature.download(temperature, size_t(c.n_nodes), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        if (report) report->seconds_total = seconds(t0);
+        if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
+    });
+    return rc != NLGPU_OK ? rc : conv_status;
+}
+
+int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* temperature,
+                        nlgpu_solve_report* report) {
+    if (!ctx || !options || !temperature) return NLGPU_ERR_ARG;
+    int conv_status = NLGPU_OK;
+    const int rc = guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "mesh and model must be set");
+        nlgpu_solve_report local_rep{};
+        nlgpu_solve_report* rep = report ? report : &local_rep;
+        std::memset(rep, 0, sizeof *rep);
+        const auto t_all = std::chrono::steady_clock::now();
+        auto t0 = t_all;
+        ensure_boundary(c);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        rep->seconds_boundary = seconds(t0);
+        t0 = std::chrono::steady_clock::now();
+        if (c.model.nonlocal()) ensure_neighbours(c);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        rep->seconds_neighbours = seconds(t0);
+        t0 = std::chrono::steady_clock::now();
+        c.symmetric = !(c.model.nonlocal() && c.cond_field.n);
+        build_patterns(c, !c.model.nonlocal(), c.symmetric, c.inner, &c.bound, &c.full, &c.full_from_upper);
+        build_patterns(c, true, true, c.local, nullptr, nullptr, nullptr);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        rep->seconds_pattern = seconds(t0);
+        t0 = std::chrono::steady_clock::now();
+        assemble_full(c);
+        fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
+        assemble_local(c, c.local, c.model.p1, 0);
+        c.local_ready = true;
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        rep->seconds_assembly = seconds(t0);
+        t0 = std::chrono::steady_clock::now();
+        c.rhs.resize(size_t(c.n_nodes));
+        apply_first_kind(c, c.bound, c.rhs_init.p, c.rhs.p, c.x_dirichlet.p);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        rep->seconds_boundary += seconds(t0);
+        c.inner_ready = true;
+        const CgResult r = solve_system(c, *options, rep);
+        c.temperature.download(temperature, size_t(c.n_nodes), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        rep->seconds_total = seconds(t_all);
+        if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
+    });
+    return rc != NLGPU_OK ? rc : conv_status;
+}
+
+int nlgpu_cg_solve(nlgpu_ctx* ctx, int64_t n, const int64_t* a_rowptr, const int64_t* a_col, const double* a_val,
+                   const int64_t* p_rowptr, const int64_t* p_col, const double* p_val, const double* b, const double* x0,
+                   double tolerance, int64_t max_iterations, double* x, nlgpu_solve_report* report) {
+    if (!ctx || n <= 0 || !a_rowptr || !a_col || !a_val || !b || !x) return NLGPU_ERR_ARG;
+    int conv_status = NLGPU_OK;
+    const int rc = guarded([&] {
+        Ctx& c = *ctx;
+        const auto t0 = std::chrono::steady_clock::now();
+        // full padded rows from the upper storage (both triangles)
+        std::vector<std::vector<std::pair<int32_t, double>>> rows(static_cast<size_t>(n));
+        for (int64_t r = 0; r < n; ++r)
+            for (int64_t k = a_rowptr[r]; k < a_rowptr[r + 1]; ++k) {
+                const int64_t cc = a_col[k];
+                NL_REQUIRE(cc >= r && cc < n, NLGPU_ERR_ARG, "A must be the upper triangle with columns in range");
+                rows[size_t(r)].push_back({int32_t(cc), a_val[k]});
+                if (cc != r) rows[size_t(cc)].push_back({int32_t(r), a_val[k]});
+            }
+        std::vector<i64> rp(size_t(n + 1), 0);
+        std::vector<int32_t> col;
+        std::vector<double> val;
+        for (int64_t r = 0; r < n; ++r) {
+            auto& row = rows[size_t(r)];
+            std::sort(row.begin(), row.end(), [](const auto& u, const auto& v) { return u.first < v.first; });
+            for (const auto& [cc, v] : row) { col.push_back(cc); val.push_back(v); }
+            while (col.size() % 4) { col.push_back(int32_t(r)); val.push_back(0.0); }
+            rp[size_t(r) + 1] = i64(col.size());
+        }
+        rows.clear();
+        Csr A;
+        A.rows = n; A.nnz = i64(col.size());
+        A.rowptr.upload(rp.data(), rp.size(), c.stream);
+        A.col.upload(col.data(), col.size(), c.stream);
+        A.val.upload(val.data(), val.size(), c.stream);
+        dbuf<double> db, dx;
+        db.upload(b, size_t(n), c.stream);
+        dx.resize(size_t(n));
+        if (x0) dx.upload(x0, size_t(n), c.stream);
+        const IncompleteCholesky* M = nullptr;
+        IncompleteCholesky ic;
+        if (p_rowptr && p_col && p_val) {
+            Csr P;
+            P.rows = n; P.nnz = p_rowptr[n];
+            std::vector<int32_t> pc(static_cast<size_t>(P.nnz));
+            for (int64_t k = 0; k < P.nnz; ++k) {
+                NL_REQUIRE(p_col[k] >= 0 && p_col[k] < n, NLGPU_ERR_ARG, "P column out of range");
+                pc[size_t(k)] = int32_t(p_col[k]);
+            }
+            std::vector<i64> prp(p_rowptr, p_rowptr + n + 1);
+            P.rowptr.upload(prp.data(), prp.size(), c.stream);
+            P.col.upload(pc.data(), pc.size(), c.stream);
+            P.val.upload(p_val, size_t(P.nnz), c.stream);
+            ilt_build(c, P, ic);
+            if (ic.ok) M = &ic;
+        }
+        const CgResult r = cg_solve(c, A, M, db.p, dx.p, tolerance, max_iterations, x0 != nullptr);
+        dx.download(x, size_t(n), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        if (report) {
+            std::memset(report, 0, sizeof *report);
+            report->iterations = r.iterations;
+            report->residual = r.residual;
+            report->reference_residual = r.reference_residual;
+            report->preconditioner_ok = M ? 1 : 0;
+            report->preconditioner_shifts = ic.attempts;
+            report->nnz_solver = A.nnz;
+            report->seconds_total = seconds(t0);
+        }
+        if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
+    });
+    return rc != NLGPU_OK ? rc : conv_status;
+}
+
+int nlgpu_nonstationary_2d_compute(nlgpu_ctx* ctx, double time_step, const double* initial) {
+    if (!ctx || !(time_step > 0.0)) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "mesh and model must be set");
+        // nonstationary_heat_equation_solver_2d::compute (nonstationary_heat_equation_solver_2d.hpp:63-88)
+        NL_REQUIRE(!(c.model.nonlocal() && c.cond_field.n), NLGPU_ERR_UNSUPPORTED, "variable conductivity with a nonlocal model");
+        ensure_boundary(c);
+        c.symmetric = true;
+        if (c.model.nonlocal()) ensure_neighbours(c);
+        build_patterns(c, !c.model.nonlocal(), true, c.inner, &c.bound, &c.full, &c.full_from_upper);
+        assemble_full(c);
+        build_patterns(c, true, true, c.capacity_m, nullptr, &c.capacity_full, &c.capacity_map);
+        assemble_local(c, c.capacity_m, c.capacity * c.density, 1);
+        fill_full_from_upper(c, c.capacity_m, c.capacity_full, c.capacity_map);
+        c.time_step = time_step;
+        combine_nonstationary(c, time_step);   // K <- dt K + C, unit Dirichlet diagonal, bound <- dt bound
+        fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
+        c.temperature.resize(size_t(c.n_nodes));
+        if (initial) c.temperature.upload(initial, size_t(c.n_nodes), c.stream);
+        else c.temperature.zero(c.stream);
+        c.rhs.resize(size_t(c.n_nodes));
+        c.step_tmp.resize(size_t(c.n_nodes));
+        c.step_xd.resize(size_t(c.n_nodes));
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        c.inner_ready = false;   // inner now holds dt K + C
+        c.nonstationary_ready = true;
+    });
+}
+
+int nlgpu_nonstationary_2d_step(nlgpu_ctx* ctx, double dirichlet_value, const double* dirichlet_values,
+                                double tolerance, int64_t max_iterations, double* temperature, int64_t* iterations) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    int conv_status = NLGPU_OK;
+    const int rc = guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.nonstationary_ready, NLGPU_ERR_STATE, "nonstationary_2d_compute must run first");
+        // calc_step (nonstationary_heat_equation_solver_2d.hpp:90-106):
+        // f = dt * (flux + source) + C T_prev; f -= dt K_bound x_D; f[D] = x_D; CG from T_prev
+        if (dirichlet_values) c.step_xd.upload(dirichlet_values, size_t(c.n_nodes), c.stream);
+        nonstationary_rhs(c, dirichlet_value, dirichlet_values != nullptr);
+        const CgResult r = cg_solve(c, c.full, nullptr, c.rhs.p, c.temperature.p, tolerance, max_iterations, true);
+        if (temperature) c.temperature.download(temperature, size_t(c.n_nodes), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        if (iterations) *iterations = r.iterations;
+        if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
+    });
+    return rc != NLGPU_OK ? rc : conv_status;
+}
+
+int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double length, double radius, double local_weight,
+                        int influence, double conductivity, double t_left, double q_right, int sin_source,
+                        double* temperature) {
+    if (!ctx || elements <= 0 || (order != 1 && order != 2) || !(length > 0.0) || !temperature) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        stationary_1d(*ctx, elements, order, length, radius, local_weight, influence, conductivity, t_left, q_right,
+                      sin_source != 0, temperature);
+    });
+}
+
+}  // extern "C"
+
+namespace nlgpu {
+
+Model make_model(const nlgpu_model_2d& m) {
+    NL_REQUIRE(m.influence >= NLGPU_INFLUENCE_CONSTANT && m.influence <= NLGPU_INFLUENCE_FAST_POLYNOMIAL, NLGPU_ERR_ARG,
+               "unknown influence kind");
+    NL_REQUIRE(m.conductivity_kind >= 0 && m.conductivity_kind <= 2, NLGPU_ERR_ARG, "unknown conductivity kind");
+    NL_REQUIRE(m.n >= 1, NLGPU_ERR_ARG, "powered-distance exponent must be positive");
+    Model o{};
+    o.influence = m.influence; o.n = m.n; o.p = m.p; o.q = m.q;
+    o.r[0] = m.radius[0]; o.r[1] = m.radius[1];
+    o.p1 = m.local_weight;
+    o.cond_kind = m.conductivity_kind;
+    for (int k = 0; k < 3; ++k) o.cond[k] = m.conductivity[k];
+    if (o.nonlocal()) {
+        NL_REQUIRE(o.r[0] > 0.0 && o.r[1] > 0.0, NLGPU_ERR_ARG, "nonlocal radii must be positive");
+        o.inv_r[0] = 1.0 / o.r[0]; o.inv_r[1] = 1.0 / o.r[1];
+        const double n = m.n;
+        switch (m.influence) {   // normalisations of influence_functions_2d.hpp:44-142
+        case NLGPU_INFLUENCE_FAST_POLYNOMIAL:
+            o.norm = 2.0 / (std::numbers::pi * o.r[0] * o.r[1]); break;
+        case NLGPU_INFLUENCE_POLYNOMIAL:
+            NL_REQUIRE(m.p > 0 && m.q >= 1.0 && m.q == std::floor(m.q), NLGPU_ERR_UNSUPPORTED, "polynomial: integer q >= 1");
+            o.norm = n * m.p / (4 * o.r[0] * o.r[1] * std::beta(1 / n, 1 / n) * std::beta(2.0 / m.p, m.q + 1)); break;
+        case NLGPU_INFLUENCE_EXPONENTIAL:
+            NL_REQUIRE(m.p > 0 && m.q > 0.0, NLGPU_ERR_ARG, "exponential: p > 0, q > 0");
+            o.norm = (n * m.p * std::pow(4.0, 1 / n) * std::pow(m.q, 2.0 / m.p)) /
+                     (8 * o.r[0] * o.r[1] * std::tgamma(2.0 / m.p) * std::beta(0.5, 1 / n)); break;
+        default:
+            o.norm = std::tgamma(1 + 2 / n) / (4 * o.r[0] * o.r[1] * ipow_host(std::tgamma(1 + 1 / n), 2)); break;
+        }
+    }
+    return o;
+}
+
+}  // namespace nlgpu

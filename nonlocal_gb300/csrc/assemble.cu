@@ -1,0 +1,438 @@
+// Values of the conductivity (and capacity) matrices.
+//
+// Reference: conductivity_matrix_2d::compute (conductivity_matrix_2d.hpp:166-193)
+// runs integrator::operator() (integrator.hpp:62-91) for every
+// (row node, eL containing it, eNL in neighbours(eL), jNL), recomputing
+//   K_ij += (1 - p1) * sum_qL w_qL G_i(qL) . sum_qNL w_qNL phi(x_qL, x_qNL) Lambda(qNL) G_j(qNL)
+//         + p1 * [eL == eNL] * sum_q w_q G_i(q) . Lambda(q) G_j(q) / |J(q)|
+// (integrate_nonlocal :132-164, integrate_local :106-130) for each entry.
+//
+// Here the work is organised by element pair.  A CTA owns element eL: the CSR
+// segments of its node rows (column numbers and value accumulators) sit in
+// shared memory.  Each warp takes one neighbour eNL at a time, stages eNL's
+// quadrature data in shared memory and evaluates the pair's whole block once,
+// factorised as
+//   Phi[qL][qNL] = w_qNL phi(x_qL, x_qNL)                  (nq^2 kernel values)
+//   H[qL][j]     = sum_qNL Phi[qL][qNL] Lambda G_j(qNL)     (nq^2 * nen * 2 FMA)
+//   K[i][j]      = sum_qL w_qL G_i(qL) . H[qL][j]            (nen^2 * nq * 2 FMA)
+// then adds every entry the reference keeps (matrix_separator_base::part) to
+// the shared accumulators; BOUND entries go straight to global memory.  When
+// the CTA is done its accumulators are added to the global values (several
+// elements share a node row).  Rows too long for shared memory fall back to
+// global atomics with a binary search of the column.
+#include "common.cuh"
+
+namespace nlgpu {
+
+namespace {
+
+constexpr int AS_THREADS = 256;
+constexpr int AS_WARPS = AS_THREADS / 32;
+
+struct AssembleArgs {
+    i64 E;
+    const int32_t* elems;
+    const double* qcoord;     // [e][q][2]
+    const double* jac;        // [e][q]
+    const double* deriv;      // [e][i][q][2]
+    const i64* noff;
+    const int32_t* nlist;
+    const uint8_t* is_inner;
+    const double* cond_field; // isotropic conductivity per quadrature point, or null
+    const i64* in_rp; const int32_t* in_col; double* in_val;
+    const i64* bd_rp; const int32_t* bd_col; double* bd_val;
+    bool symmetric;
+    int cap;                  // accumulator entries in shared memory
+    int* error;               // set when an entry is missing from its pattern
+};
+
+__device__ __forceinline__ double ipow(double x, int n) {   // power(T, integral) of metamath/functions/power.hpp:232-247
+    double r = 1.0;
+    while (n > 0) { if (n & 1) { r *= x; --n; } else { x *= x; n >>= 1; } }
+    return r;
+}
+
+// influence functions (influence_functions_2d.hpp:39-148) with the powered
+// distance of search_function.hpp:569-579; radii enter as multiplications by
+// their inverses.
+template<int INF>
+__device__ __forceinline__ double influence(const Model& m, double ax, double ay, double bx, double by) {
+    const double z0 = (ax - bx) * m.inv_r[0], z1 = (ay - by) * m.inv_r[1];
+    double d;
+    if (m.n == 2) d = z0 * z0 + z1 * z1;
+    else if (m.n == 1) d = fabs(z0) + fabs(z1);
+    else d = ipow(fabs(z0), m.n) + ipow(fabs(z1), m.n);
+    if constexpr (INF == NLGPU_INFLUENCE_FAST_POLYNOMIAL) {
+        return d < 1.0 ? m.norm * (1.0 - d) : 0.0;
+    } else if constexpr (INF == NLGPU_INFLUENCE_CONSTANT) {
+        return d <= 1.0 ? m.norm : 0.0;
+    } else {
+        const bool integral = (m.p % m.n) == 0;
+        const double dp = integral ? ipow(d, m.p / m.n) : pow(d, double(m.p) / double(m.n));
+        if constexpr (INF == NLGPU_INFLUENCE_POLYNOMIAL) {
+            return d < 1.0 ? m.norm * ipow(1.0 - dp, int(m.q)) : 0.0;
+        } else {
+            return m.norm * exp(-m.q * dp);
+        }
+    }
+}
+
+__device__ __forceinline__ i64 find_col(const int32_t* col, i64 lo, i64 hi, int32_t c) {
+    while (lo < hi) {
+        const i64 mid = (lo + hi) >> 1;
+        if (col[mid] < c) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+template<int NEN, int NQ>
+struct PairSmem {
+    double qx[NQ], qy[NQ];
+    double gx[NEN * NQ], gy[NEN * NQ];
+    double phi[NQ * NQ];
+    double hx[NQ * NEN], hy[NQ * NEN];
+    double lam[NQ];           // conductivity at eNL's points (field case)
+    int32_t nodes[NEN];
+};
+
+template<int NEN, int NQ, int INF>
+__global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, Model m, Basis b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double eqx[NQ], eqy[NQ], egx[NEN * NQ], egy[NEN * NQ], ejac[NQ], elam[NQ];
+    __shared__ int32_t enodes[NEN];
+    __shared__ i64 row_start[NEN];
+    __shared__ int row_len[NEN], row_off[NEN + 1];
+    __shared__ int use_smem;
+
+    auto* pairs = reinterpret_cast<PairSmem<NEN, NQ>*>(smem_raw);
+    double* acc = reinterpret_cast<double*>(smem_raw + sizeof(PairSmem<NEN, NQ>) * AS_WARPS);
+    int32_t* cols = reinterpret_cast<int32_t*>(acc + a.cap);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    PairSmem<NEN, NQ>& ps = pairs[warp];
+    const double nl_weight = 1.0 - m.p1, l_weight = m.p1;
+
+    for (i64 eL = blockIdx.x; eL < a.E; eL += gridDim.x) {
+        // ---- element eL: quadrature data and its node rows
+        for (int t = threadIdx.x; t < NEN * NQ; t += AS_THREADS) {
+            egx[t] = a.deriv[2 * (eL * NEN * NQ + t)];
+            egy[t] = a.deriv[2 * (eL * NEN * NQ + t) + 1];
+        }
+        for (int t = threadIdx.x; t < NQ; t += AS_THREADS) {
+            eqx[t] = a.qcoord[2 * (eL * NQ + t)];
+            eqy[t] = a.qcoord[2 * (eL * NQ + t) + 1];
+            ejac[t] = a.jac[eL * NQ + t];
+            elam[t] = a.cond_field ? a.cond_field[eL * NQ + t] : m.cond[0];
+        }
+        if (threadIdx.x < NEN) {
+            const int32_t r = a.elems[eL * NEN + threadIdx.x];
+            enodes[threadIdx.x] = r;
+            row_start[threadIdx.x] = a.in_rp[r];
+            row_len[threadIdx.x] = a.is_inner[r] ? int(a.in_rp[r + 1] - a.in_rp[r]) : 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int off = 0;
+            for (int i = 0; i < NEN; ++i) { row_off[i] = off; off += row_len[i]; }
+            row_off[NEN] = off;
+            use_smem = off <= a.cap;
+        }
+        __syncthreads();
+        const bool smem_rows = use_smem;
+        if (smem_rows) {
+            for (int i = 0; i < NEN; ++i)
+                for (int t = threadIdx.x; t < row_len[i]; t += AS_THREADS) {
+                    cols[row_off[i] + t] = a.in_col[row_start[i] + t];
+                    acc[row_off[i] + t] = 0.0;
+                }
+        }
+        __syncthreads();
+
+        // ---- pairs (eL, eNL): one warp each
+        const i64 kb = a.noff[eL], ke = a.noff[eL + 1];
+        for (i64 k = kb + warp; k < ke; k += AS_WARPS) {
+            const int32_t eNL = a.nlist[k];
+            for (int t = lane; t < NEN * NQ; t += 32) {
+                ps.gx[t] = a.deriv[2 * (i64(eNL) * NEN * NQ + t)];
+                ps.gy[t] = a.deriv[2 * (i64(eNL) * NEN * NQ + t) + 1];
+            }
+            if (lane < NQ) {
+                ps.qx[lane] = a.qcoord[2 * (i64(eNL) * NQ + lane)];
+                ps.qy[lane] = a.qcoord[2 * (i64(eNL) * NQ + lane) + 1];
+                ps.lam[lane] = a.cond_field ? a.cond_field[i64(eNL) * NQ + lane] : m.cond[0];
+            }
+            if (lane < NEN) ps.nodes[lane] = a.elems[i64(eNL) * NEN + lane];
+            __syncwarp();
+            for (int t = lane; t < NQ * NQ; t += 32) {
+                const int qL = t / NQ, qNL = t % NQ;
+                ps.phi[t] = b.w[qNL] * influence<INF>(m, eqx[qL], eqy[qL], ps.qx[qNL], ps.qy[qNL]);
+            }
+            __syncwarp();
+            for (int t = lane; t < NQ * NEN; t += 32) {
+                const int qL = t / NEN, j = t % NEN;
+                double h0 = 0.0, h1 = 0.0;
+                #pragma unroll
+                for (int qNL = 0; qNL < NQ; ++qNL) {
+                    const double f = ps.phi[qL * NQ + qNL];
+                    const double gx = ps.gx[j * NQ + qNL], gy = ps.gy[j * NQ + qNL];
+                    if (m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC) {
+                        const double s = f * ps.lam[qNL];
+                        h0 += s * gx; h1 += s * gy;
+                    } else if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) {
+                        h0 += f * m.cond[0] * gx; h1 += f * m.cond[1] * gy;
+                    } else {
+                        h0 += f * (m.cond[0] * gx + m.cond[2] * gy);
+                        h1 += f * (m.cond[2] * gx + m.cond[1] * gy);
+                    }
+                }
+                ps.hx[t] = h0; ps.hy[t] = h1;
+            }
+            __syncwarp();
+            for (int t = lane; t < NEN * NEN; t += 32) {
+                const int i = t / NEN, j = t % NEN;
+                const int32_t r = enodes[i], c = ps.nodes[j];
+                const bool c_inner = a.is_inner[c];
+                const bool keep_inner = c_inner && a.is_inner[r] && (!a.symmetric || r <= c);
+                const bool keep_bound = !c_inner && r != c;
+                if (!keep_inner && !keep_bound) continue;
+                double v = 0.0;
+                #pragma unroll
+                for (int qL = 0; qL < NQ; ++qL)
+                    v += b.w[qL] * (egx[i * NQ + qL] * ps.hx[qL * NEN + j] + egy[i * NQ + qL] * ps.hy[qL * NEN + j]);
+                v *= nl_weight;
+                if (eNL == int32_t(eL)) {
+                    double loc = 0.0;
+                    #pragma unroll
+                    for (int q = 0; q < NQ; ++q) {
+                        const double ax = egx[i * NQ + q], ay = egy[i * NQ + q];
+                        const double bx = egx[j * NQ + q], by = egy[j * NQ + q];
+                        double val;
+                        if (m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC) val = elam[q] * (ax * bx + ay * by);
+                        else if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) val = m.cond[0] * ax * bx + m.cond[1] * ay * by;
+                        else val = ax * (m.cond[0] * bx + m.cond[2] * by) + ay * (m.cond[2] * bx + m.cond[1] * by);
+                        loc += b.w[q] * val / ejac[q];
+                    }
+                    v += l_weight * loc;
+                }
+                // the patterns hold every kept entry; a miss is recorded, never written
+                if (keep_inner) {
+                    if (smem_rows) {
+                        const i64 pos = find_col(cols, row_off[i], row_off[i + 1], c);
+                        if (pos < row_off[i + 1] && cols[pos] == c) atomicAdd(acc + pos, v);
+                        else atomicExch(a.error, 1);
+                    } else {
+                        const i64 pos = find_col(a.in_col, a.in_rp[r], a.in_rp[r + 1], c);
+                        if (pos < a.in_rp[r + 1] && a.in_col[pos] == c) atomicAdd(a.in_val + pos, v);
+                        else atomicExch(a.error, 1);
+                    }
+                } else {
+                    const i64 pos = find_col(a.bd_col, a.bd_rp[r], a.bd_rp[r + 1], c);
+                    if (pos < a.bd_rp[r + 1] && a.bd_col[pos] == c) atomicAdd(a.bd_val + pos, v);
+                    else atomicExch(a.error, 1);
+                }
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        if (smem_rows)
+            for (int i = 0; i < NEN; ++i)
+                for (int t = threadIdx.x; t < row_len[i]; t += AS_THREADS) {
+                    const double v = acc[row_off[i] + t];
+                    if (v != 0.0) atomicAdd(a.in_val + row_start[i] + t, v);
+                }
+        __syncthreads();
+    }
+}
+
+// Local integrands, one thread per (e, i, j): conductivity
+// (integrate_local, conductivity_matrix_2d.hpp:106-130) or capacity
+// (integrate_basic_pair, heat_capacity_matrix_2d.hpp:137-144).
+__global__ void k_assemble_local(i64 E, int nen, int nq, const int32_t* __restrict__ elems,
+                                 const double* __restrict__ jac, const double* __restrict__ deriv,
+                                 const uint8_t* __restrict__ is_inner, const double* __restrict__ cond_field,
+                                 Model m, Basis b, int integrand, double weight, bool symmetric,
+                                 const i64* __restrict__ rp, const int32_t* __restrict__ col, double* __restrict__ val,
+                                 const i64* __restrict__ bd_rp, const int32_t* __restrict__ bd_col, double* __restrict__ bd_val) {
+    for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < E * nen * nen; t += i64(gridDim.x) * blockDim.x) {
+        const i64 e = t / (nen * nen);
+        const int i = int((t / nen) % nen), j = int(t % nen);
+        const int32_t r = elems[e * nen + i], c = elems[e * nen + j];
+        const bool keep_inner = is_inner[c] && is_inner[r] && (!symmetric || r <= c);
+        const bool keep_bound = !is_inner[c] && r != c && bd_rp != nullptr;
+        if (!keep_inner && !keep_bound) continue;
+        double integral = 0.0;
+        for (int q = 0; q < nq; ++q) {
+            if (integrand == 1) {
+                integral += b.w[q] * b.qN[i * nq + q] * b.qN[j * nq + q] * jac[e * nq + q];
+            } else {
+                const double* di = deriv + 2 * ((e * nen + i) * nq + q);
+                const double* dj = deriv + 2 * ((e * nen + j) * nq + q);
+                double v;
+                if (m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC)
+                    v = (cond_field ? cond_field[e * nq + q] : m.cond[0]) * (di[0] * dj[0] + di[1] * dj[1]);
+                else if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) v = m.cond[0] * di[0] * dj[0] + m.cond[1] * di[1] * dj[1];
+                else v = di[0] * (m.cond[0] * dj[0] + m.cond[2] * dj[1]) + di[1] * (m.cond[2] * dj[0] + m.cond[1] * dj[1]);
+                integral += b.w[q] * v / jac[e * nq + q];
+            }
+        }
+        integral *= weight;
+        if (keep_inner) {
+            const i64 pos = find_col(col, rp[r], rp[r + 1], c);
+            if (pos < rp[r + 1] && col[pos] == c) atomicAdd(val + pos, integral);
+        } else {
+            const i64 pos = find_col(bd_col, bd_rp[r], bd_rp[r + 1], c);
+            if (pos < bd_rp[r + 1] && bd_col[pos] == c) atomicAdd(bd_val + pos, integral);
+        }
+    }
+}
+
+__global__ void k_dirichlet_diagonal(i64 n, const uint8_t* __restrict__ is_inner, const i64* __restrict__ rp,
+                                     double* __restrict__ val, double value) {
+    for (i64 r = blockIdx.x * i64(blockDim.x) + threadIdx.x; r < n; r += i64(gridDim.x) * blockDim.x)
+        if (!is_inner[r]) val[rp[r]] = value;
+}
+
+__global__ void k_gather_full(i64 nnz, const i64* __restrict__ map, const double* __restrict__ upper,
+                              double* __restrict__ full, float* __restrict__ full32) {
+    for (i64 k = blockIdx.x * i64(blockDim.x) + threadIdx.x; k < nnz; k += i64(gridDim.x) * blockDim.x) {
+        const i64 s = map[k];
+        const double v = s >= 0 ? upper[s] : 0.0;
+        full[k] = v;
+        if (full32) full32[k] = float(v);
+    }
+}
+
+template<int NEN, int NQ, int INF>
+void launch_pairs(Ctx& ctx, const AssembleArgs& a) {
+    const size_t fixed = sizeof(PairSmem<NEN, NQ>) * AS_WARPS;
+    const size_t dyn = fixed + size_t(a.cap) * (sizeof(double) + sizeof(int32_t));
+    auto kernel = k_assemble_pairs<NEN, NQ, INF>;
+    NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
+    const unsigned grid = unsigned(std::min<i64>(a.E, 152 * 16));
+    NL_LAUNCH(kernel, grid, AS_THREADS, dyn, ctx.stream, a, ctx.model, ctx.basis);
+}
+
+template<int NEN, int NQ>
+void dispatch_influence(Ctx& ctx, const AssembleArgs& a) {
+    switch (ctx.model.influence) {
+    case NLGPU_INFLUENCE_FAST_POLYNOMIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_FAST_POLYNOMIAL>(ctx, a); break;
+    case NLGPU_INFLUENCE_POLYNOMIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_POLYNOMIAL>(ctx, a); break;
+    case NLGPU_INFLUENCE_EXPONENTIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_EXPONENTIAL>(ctx, a); break;
+    default: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_CONSTANT>(ctx, a); break;
+    }
+}
+
+}  // namespace
+
+// Assembles p1*K_local + (1-p1)*K_nonlocal (or p1*K_local for a local model)
+// into ctx.inner / ctx.bound, whose patterns are already built.
+void assemble_full(Ctx& ctx) {
+    ctx.inner.val.zero(ctx.stream);
+    ctx.bound.val.zero(ctx.stream);
+    const Model& m = ctx.model;
+    if (!m.nonlocal()) {
+        assemble_local(ctx, ctx.inner, m.p1, 0);
+        return;
+    }
+    AssembleArgs a{};
+    a.E = ctx.n_elems; a.elems = ctx.elems.p; a.qcoord = ctx.qcoord.p; a.jac = ctx.jac.p; a.deriv = ctx.deriv.p;
+    a.noff = ctx.noff.p; a.nlist = ctx.nlist.p; a.is_inner = ctx.is_inner.p;
+    a.cond_field = ctx.cond_field.n ? ctx.cond_field.p : nullptr;
+    a.in_rp = ctx.inner.rowptr.p; a.in_col = ctx.inner.col.p; a.in_val = ctx.inner.val.p;
+    a.bd_rp = ctx.bound.rowptr.p; a.bd_col = ctx.bound.col.p; a.bd_val = ctx.bound.val.p;
+    a.symmetric = ctx.symmetric;
+    dbuf<int> err;
+    err.resize(1);
+    err.zero(ctx.stream);
+    a.error = err.p;
+    if (ctx.basis.nen == 4) {
+        a.cap = int((200 * 1024 - sizeof(PairSmem<4, 4>) * AS_WARPS) / 12);
+        dispatch_influence<4, 4>(ctx, a);
+    } else {
+        a.cap = int((200 * 1024 - sizeof(PairSmem<8, 9>) * AS_WARPS) / 12);
+        dispatch_influence<8, 9>(ctx, a);
+    }
+    set_dirichlet_diagonal(ctx, ctx.inner, 1.0);
+    int herr = 0;
+    NL_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof herr, cudaMemcpyDeviceToHost, ctx.stream));
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+    NL_REQUIRE(herr == 0, NLGPU_ERR_STATE, "assembly met an entry outside the sparsity pattern");
+}
+
+void assemble_local(Ctx& ctx, Csr& mtx, double weight, int integrand) {
+    const int nen = ctx.basis.nen, nq = ctx.basis.nq;
+    const i64 work = ctx.n_elems * nen * nen;
+    const bool with_bound = &mtx == &ctx.inner;
+    NL_LAUNCH(k_assemble_local, grid_for(work, 256), 256, 0, ctx.stream, ctx.n_elems, nen, nq, ctx.elems.p, ctx.jac.p,
+              ctx.deriv.p, ctx.is_inner.p, ctx.cond_field.n ? ctx.cond_field.p : nullptr, ctx.model, ctx.basis,
+              integrand, weight, ctx.symmetric || integrand == 1, mtx.rowptr.p, mtx.col.p, mtx.val.p,
+              with_bound ? ctx.bound.rowptr.p : nullptr, with_bound ? ctx.bound.col.p : nullptr,
+              with_bound ? ctx.bound.val.p : nullptr);
+    set_dirichlet_diagonal(ctx, mtx, 1.0);
+}
+
+void set_dirichlet_diagonal(Ctx& ctx, Csr& mtx, double value) {
+    NL_LAUNCH(k_dirichlet_diagonal, grid_for(mtx.rows, 256), 256, 0, ctx.stream, mtx.rows, ctx.is_inner.p,
+              mtx.rowptr.p, mtx.val.p, value);
+}
+
+void fill_full_from_upper(Ctx& ctx, const Csr& upper, Csr& full, const dbuf<i64>& map) {
+    full.val.resize(size_t(full.nnz));
+    NL_LAUNCH(k_gather_full, grid_for(full.nnz, 256), 256, 0, ctx.stream, full.nnz, map.p, upper.val.p, full.val.p,
+              full.val32.n ? full.val32.p : nullptr);
+}
+
+}  // namespace nlgpu
+
+// ---------------------------------------------------------------- nonstationary
+namespace nlgpu {
+
+namespace {
+
+// K <- dt K + C row by row (C's pattern is contained in K's), unit Dirichlet
+// diagonal; bound <- dt bound (nonstationary_heat_equation_solver_2d.hpp:77-82).
+__global__ void k_combine(i64 n, double dt, const uint8_t* __restrict__ is_inner, const i64* __restrict__ krp,
+                          const int32_t* __restrict__ kcol, double* __restrict__ kval, const i64* __restrict__ crp,
+                          const int32_t* __restrict__ ccol, const double* __restrict__ cval, const i64* __restrict__ brp,
+                          double* __restrict__ bval) {
+    for (i64 r = blockIdx.x * i64(blockDim.x) + threadIdx.x; r < n; r += i64(gridDim.x) * blockDim.x) {
+        for (i64 k = krp[r]; k < krp[r + 1]; ++k) kval[k] *= dt;
+        for (i64 k = brp[r]; k < brp[r + 1]; ++k) bval[k] *= dt;
+        i64 k = krp[r];
+        for (i64 s = crp[r]; s < crp[r + 1]; ++s) {
+            while (k < krp[r + 1] && kcol[k] != ccol[s]) ++k;
+            if (k < krp[r + 1]) kval[k] += cval[s];
+        }
+        if (!is_inner[r]) kval[krp[r]] = 1.0;
+    }
+}
+
+// Dirichlet vector of a step: value on every Dirichlet node (or the uploaded per-node values)
+__global__ void k_step_dirichlet(i64 n, const uint8_t* __restrict__ is_inner, double value, bool per_node,
+                                 double* __restrict__ xd) {
+    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
+        xd[i] = is_inner[i] ? 0.0 : (per_node ? xd[i] : value);
+}
+
+__global__ void k_axpy_into(i64 n, double a, const double* __restrict__ x, double* __restrict__ y) {
+    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) y[i] += a * x[i];
+}
+
+}  // namespace
+
+void combine_nonstationary(Ctx& ctx, double dt) {
+    NL_LAUNCH(k_combine, grid_for(ctx.n_nodes, 256), 256, 0, ctx.stream, ctx.n_nodes, dt, ctx.is_inner.p,
+              ctx.inner.rowptr.p, ctx.inner.col.p, ctx.inner.val.p, ctx.capacity_m.rowptr.p, ctx.capacity_m.col.p,
+              ctx.capacity_m.val.p, ctx.bound.rowptr.p, ctx.bound.val.p);
+}
+
+// rhs = dt * rhs_init + C T_prev, then the first-kind step with the step's Dirichlet values
+void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values) {
+    const i64 n = ctx.n_nodes;
+    NL_LAUNCH(k_step_dirichlet, grid_for(n, 256), 256, 0, ctx.stream, n, ctx.is_inner.p, dirichlet_value,
+              per_node_values, ctx.step_xd.p);
+    spmv_full(ctx, ctx.capacity_full, ctx.temperature.p, ctx.step_tmp.p);
+    NL_LAUNCH(k_axpy_into, grid_for(n, 256), 256, 0, ctx.stream, n, ctx.time_step, ctx.rhs_init.p, ctx.step_tmp.p);
+    apply_first_kind(ctx, ctx.bound, ctx.step_tmp.p, ctx.rhs.p, ctx.step_xd.p);
+}
+
+}  // namespace nlgpu

@@ -1,0 +1,277 @@
+// Shared definitions of the nlgpu library: error handling, device buffers,
+// element tables, the per-problem context and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/nlgpu.h"
+
+namespace nlgpu {
+
+using i64 = int64_t;
+
+// ------------------------------------------------------------------ errors
+struct error : std::runtime_error {
+    int code;
+    error(int c, const std::string& what) : std::runtime_error{what}, code{c} {}
+};
+
+[[noreturn]] inline void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    const int code = e == cudaErrorMemoryAllocation ? NLGPU_ERR_OUT_OF_MEMORY : NLGPU_ERR_CUDA;
+    throw error{code, std::string{what} + ": " + cudaGetErrorString(e) + " (" + file + ":" + std::to_string(line) + ")"};
+}
+
+#define NL_CUDA(call)                                                          \
+    do {                                                                       \
+        const cudaError_t nl_e_ = (call);                                      \
+        if (nl_e_ != cudaSuccess) ::nlgpu::cuda_fail(nl_e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define NL_REQUIRE(cond, code, msg)                                            \
+    do {                                                                       \
+        if (!(cond)) throw ::nlgpu::error{(code), (msg)};                      \
+    } while (0)
+
+extern std::atomic<int64_t> g_launches;
+
+#define NL_LAUNCH(kernel, grid, block, smem, stream, ...)                      \
+    do {                                                                       \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);            \
+        ::nlgpu::g_launches.fetch_add(1, std::memory_order_relaxed);           \
+        NL_CUDA(cudaGetLastError());                                           \
+    } while (0)
+
+inline unsigned grid_for(i64 n, int block, i64 cap = 152 * 32) {
+    i64 g = (n + block - 1) / block;
+    if (g > cap) g = cap;
+    return unsigned(g < 1 ? 1 : g);
+}
+
+// --------------------------------------------------------- device buffers
+template<class T>
+struct dbuf {
+    T* p = nullptr;
+    size_t n = 0;
+    dbuf() = default;
+    dbuf(const dbuf&) = delete;
+    dbuf& operator=(const dbuf&) = delete;
+    dbuf(dbuf&& o) noexcept : p{o.p}, n{o.n} { o.p = nullptr; o.n = 0; }
+    dbuf& operator=(dbuf&& o) noexcept { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; return *this; }
+    ~dbuf() { release(); }
+    void release() noexcept { if (p) cudaFree(p); p = nullptr; n = 0; }
+    void resize(size_t count) {
+        if (count == n && p) return;
+        release();
+        if (count) NL_CUDA(cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T)));
+        n = count;
+    }
+    // grows only; keeps the allocation when it is already large enough
+    void reserve(size_t count) { if (count > n) resize(count); }
+    void zero(cudaStream_t s) { if (n) NL_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s)); }
+    void upload(const T* host, size_t count, cudaStream_t s) {
+        resize(count);
+        if (count) NL_CUDA(cudaMemcpyAsync(p, host, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void download(T* host, size_t count, cudaStream_t s) const {
+        if (count) NL_CUDA(cudaMemcpyAsync(host, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+    size_t bytes() const noexcept { return n * sizeof(T); }
+};
+
+// ------------------------------------------------------ element tables
+constexpr int MAX_NEN = 8;
+constexpr int MAX_NQ = 9;
+
+// Shape functions and derivatives at the Gauss points of the reference
+// element, q = ix * ny + iy (element_2d_integrate.hpp:69-106), and N_i(0,0).
+struct Basis {
+    int type = 0, nen = 0, nq = 0;
+    double qN[MAX_NEN * MAX_NQ], qNxi[MAX_NEN * MAX_NQ], qNeta[MAX_NEN * MAX_NQ];
+    double w[MAX_NQ];
+    double centre[MAX_NEN];
+};
+Basis make_basis(int element_type);
+
+// Line elements of boundary groups: 2 nodes / Gauss-1, 3 nodes / Gauss-2
+// (vtk_elements_set.hpp:354-363).
+struct Basis1d {
+    int nen = 0, nq = 0;
+    double qN[3 * 2], qNxi[3 * 2], w[2];
+};
+Basis1d make_basis_1d(int nodes);
+
+// Nonlocal model with the influence normalisation precomputed on the host.
+struct Model {
+    int influence = NLGPU_INFLUENCE_FAST_POLYNOMIAL, n = 2, p = 2;
+    double q = 1.0, r[2] = {0.1, 0.1}, inv_r[2] = {10.0, 10.0}, p1 = 1.0, norm = 1.0;
+    int cond_kind = NLGPU_CONDUCTIVITY_ISOTROPIC;
+    double cond[3] = {1.0, 0.0, 0.0};
+    bool nonlocal() const noexcept { return p1 < 0.999; }   // nonlocal_constants.hpp:274-280
+};
+Model make_model(const nlgpu_model_2d& m);
+
+// CSR on the device: int64 row pointers, int32 columns.
+struct Csr {
+    i64 rows = 0, nnz = 0;
+    dbuf<i64> rowptr;
+    dbuf<int32_t> col;
+    dbuf<double> val;
+    dbuf<float> val32;
+};
+
+struct BoundaryGroup {
+    int kind = NLGPU_BC_TEMPERATURE, nen = 2;
+    i64 n_edges = 0;
+    double value = 0.0;
+    dbuf<int32_t> edges;
+    dbuf<double> node_values;   // optional, per listed node
+};
+
+// One triangular sweep, level scheduled: rows grouped by level, each level's
+// off-diagonal entries in a column-major (ELL) slab so that consecutive
+// threads read consecutive entries; padding points at the zero slot n.
+struct TriSlab {
+    i64 n_levels = 0, entries = 0;
+    dbuf<i64> lev_ptr;           // [n_levels + 1] positions in `rows`
+    dbuf<i64> slab_base;         // [n_levels]
+    dbuf<int32_t> width;         // [n_levels]
+    dbuf<int32_t> rows;          // row of each level position
+    dbuf<int32_t> col;           // slab columns
+    dbuf<i64> src;               // slab entry -> factor value (-1: padding)
+    dbuf<i64> diag_src;          // level position -> factor diagonal value
+    dbuf<double> val, inv_diag;
+    dbuf<float> val32, inv_diag32;
+};
+
+// ILLT preconditioner: IC(0) of S A S + alpha I on the pattern of A's upper part.
+struct IncompleteCholesky {
+    i64 n = 0, nnz = 0;
+    dbuf<i64> rp;                // upper pattern (diagonal first)
+    dbuf<int32_t> col;
+    dbuf<double> a_scaled, u;    // S A S and the factor values
+    dbuf<i64> lrp, l_to_u;       // U^T as lower CSR (diagonal last) and its U positions
+    dbuf<int32_t> lcol;
+    dbuf<i64> ic_lev_ptr;        // forward levels for the factorisation
+    dbuf<int32_t> ic_rows;
+    i64 ic_levels = 0;
+    dbuf<double> scale;          // S
+    dbuf<float> scale32;
+    TriSlab fwd, bwd;
+    dbuf<double> y, w;           // sweep buffers, n + 1 entries
+    dbuf<float> y32, w32;
+    bool ok = false;
+    int attempts = 0;
+    double shift = 0.0;
+};
+
+// Persistent device state of CG.
+struct CgWork {
+    i64 n = 0;
+    dbuf<double> r, z, p, q, x, tmp;
+    dbuf<double> partial;        // block partial sums
+    dbuf<double> scalars;        // see solver.cu
+    dbuf<int> flags;
+};
+
+struct Ctx {
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // mesh
+    int element_type = 0;
+    Basis basis{};
+    i64 n_nodes = 0, n_elems = 0;
+    dbuf<double> nodes;          // [n][2]
+    dbuf<int32_t> elems;         // [e][nen]
+    dbuf<double> qcoord, jac, deriv, centres;
+    dbuf<i64> ne_off;            // node -> elements CSR
+    dbuf<int32_t> ne_elem;
+    dbuf<int8_t> ne_local;
+    bool mesh_ready = false;
+    // model
+    Model model{};
+    bool model_ready = false;
+    dbuf<double> cond_field;     // optional isotropic conductivity [e][q]
+    double capacity = 1.0, density = 1.0;
+    // neighbours
+    bool neighbours_ready = false;
+    int strategy = NLGPU_EXPAND_MAX;
+    double search_r[2] = {0, 0};
+    i64 pairs = 0;
+    dbuf<i64> noff;
+    dbuf<int32_t> nlist;
+    // boundary
+    std::vector<BoundaryGroup> groups;
+    double source = 0.0;
+    dbuf<double> source_q;
+    dbuf<double> dirichlet_override;
+    dbuf<uint8_t> is_inner;
+    dbuf<double> x_dirichlet, rhs_init, rhs;
+    bool bc_ready = false;
+    // matrices (reference storage) and the solver's full-row copy
+    bool symmetric = true;
+    Csr inner, bound, local, full;
+    dbuf<i64> full_from_upper;   // full entry -> upper entry (lower part via transpose)
+    bool inner_ready = false, local_ready = false;
+    IncompleteCholesky ilt;
+    CgWork cg;
+    // nonstationary
+    Csr capacity_m, capacity_full;
+    dbuf<i64> capacity_map;
+    dbuf<double> step_tmp, step_xd;
+    double time_step = 0.0;
+    dbuf<double> temperature;
+    bool nonstationary_ready = false;
+    // scratch
+    dbuf<unsigned char> scratch;
+    dbuf<i64> i64_scratch_a, i64_scratch_b;
+    unsigned char* scratch_bytes(size_t bytes) { scratch.reserve(bytes); return scratch.p; }
+};
+
+// ------------------------------------------------------------ utilities
+// Exclusive prefix sum of n int64 values (in may alias out); writes the total
+// to *total_host when not null (synchronises the stream).
+void exclusive_scan(Ctx& ctx, const i64* in, i64* out, i64 n, i64* total_host);
+i64 device_read_i64(Ctx& ctx, const i64* p);
+
+// mesh.cu
+void mesh_init(Ctx& ctx);
+// neighbours.cu
+void find_neighbours(Ctx& ctx, int strategy);
+// boundary.cu
+void boundary_vectors(Ctx& ctx);
+void apply_first_kind(Ctx& ctx, const Csr& bound, const double* rhs_in, double* rhs_out, const double* x_dirichlet);
+// pattern.cu
+void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* bound, Csr* full,
+                    dbuf<i64>* full_from_upper);
+// assemble.cu
+void assemble_full(Ctx& ctx);
+void assemble_local(Ctx& ctx, Csr& m, double weight, int integrand);   // integrand 0 conductivity, 1 capacity
+void fill_full_from_upper(Ctx& ctx, const Csr& upper, Csr& full, const dbuf<i64>& map);
+void set_dirichlet_diagonal(Ctx& ctx, Csr& m, double value);
+void combine_nonstationary(Ctx& ctx, double dt);
+void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values);
+// solver.cu
+void spmv_full(Ctx& ctx, const Csr& A, const double* x, double* y);
+void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic);
+void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* z);
+struct CgResult { i64 iterations = 0; double residual = 0, reference_residual = 0; bool converged = false; };
+CgResult cg_solve(Ctx& ctx, const Csr& A_full, const IncompleteCholesky* M, const double* b, double* x,
+                  double tolerance, i64 max_iterations, bool x_is_initial_guess);
+// onedim.cu
+void stationary_1d(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight, int influence,
+                   double conductivity, double t_left, double q_right, bool sin_source, double* temperature);
+
+// device helpers --------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace nlgpu

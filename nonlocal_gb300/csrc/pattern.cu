@@ -1,0 +1,268 @@
+// Sparsity patterns of the assembled matrices.
+//
+// The reference builds them in two mesh_run sweeps (shift_initializer counts
+// distinct columns per row, matrix_index_initializer writes them, then
+// sort_indices; matrix_assembler_2d.hpp:430-461, conductivity_matrix_2d.hpp:39-72)
+// with the split of matrix_separator_base::part (matrix_separator_base.hpp:51-58):
+//   INNER  column and row inner, and row <= column when symmetric;
+//   BOUND  column Dirichlet and row != column (full rows);
+//   NO     otherwise; a Dirichlet row holds only its unit diagonal.
+// The candidate columns of row r are the nodes of every neighbour eNL of every
+// element eL containing r (nodes of eL itself for the local part).
+//
+// Here one CTA owns a row.  Candidates are OR-ed into shared-memory bitmaps
+// over a window of node numbers (windows repeat when the row spans more
+// nodes than a window holds, so any numbering works), then the set bits are
+// emitted in increasing order with popcounts and a block scan: the result is
+// the reference's sorted column list without any sort.  Three bitmaps are
+// filled at once: the inner part (upper or full), the bound part, and the
+// full-row inner pattern the solver's SpMV reads (rows padded to a multiple
+// of 4 entries for 16-byte vector loads).
+#include "common.cuh"
+
+namespace nlgpu {
+
+namespace {
+
+constexpr int PT_THREADS = 256;
+constexpr int PT_WORDS = 3840;                 // 122880 node numbers per window (3 bitmaps < 48 KB)
+constexpr i64 PT_WINDOW = i64(PT_WORDS) * 32;
+constexpr int PT_MAX_ELEMS = 16;               // elements sharing one node
+
+struct PatternArgs {
+    i64 n;
+    int nen;
+    bool local_only, symmetric;
+    const int32_t* elems;
+    const i64* ne_off;
+    const int32_t* ne_elem;
+    const i64* noff;
+    const int32_t* nlist;
+    const uint8_t* is_inner;
+    // count pass outputs
+    i64* cnt_inner;
+    i64* cnt_bound;
+    i64* cnt_full;
+    // fill pass outputs (null in the count pass)
+    const i64* rp_inner;
+    const i64* rp_bound;
+    const i64* rp_full;
+    int32_t* col_inner;
+    int32_t* col_bound;
+    int32_t* col_full;
+    int* error;
+};
+
+__device__ __forceinline__ i64 block_scan_excl(i64 v, i64* sh, i64* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    i64 incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const i64 t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) sh[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        i64 s = lane < PT_THREADS / 32 ? sh[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const i64 t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        if (lane < PT_THREADS / 32) sh[lane] = s;
+    }
+    __syncthreads();
+    const i64 off = warp ? sh[warp - 1] : 0;
+    *total = sh[PT_THREADS / 32 - 1];
+    __syncthreads();
+    return off + incl - v;
+}
+
+__global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
+    __shared__ uint32_t bm_inner[PT_WORDS], bm_bound[PT_WORDS], bm_full[PT_WORDS];
+    __shared__ i64 seg_end[PT_MAX_ELEMS];     // cumulative candidate counts per element of the row
+    __shared__ int32_t seg_elem[PT_MAX_ELEMS];
+    __shared__ i64 seg_noff[PT_MAX_ELEMS];
+    __shared__ i64 sh_scan[PT_THREADS / 32];
+    __shared__ int red_min[PT_THREADS / 32], red_max[PT_THREADS / 32];
+    const bool fill = a.col_inner != nullptr;
+
+    for (i64 r = blockIdx.x; r < a.n; r += gridDim.x) {
+        const i64 eb = a.ne_off[r], ee = a.ne_off[r + 1];
+        const int ne = int(ee - eb);
+        if (ne > PT_MAX_ELEMS) { if (threadIdx.x == 0) atomicExch(a.error, 1); continue; }
+        if (threadIdx.x == 0) {
+            i64 acc = 0;
+            for (int s = 0; s < ne; ++s) {
+                const int32_t e = a.ne_elem[eb + s];
+                const i64 len = a.local_only ? 1 : a.noff[e + 1] - a.noff[e];
+                seg_elem[s] = e;
+                seg_noff[s] = a.local_only ? 0 : a.noff[e];
+                acc += len * a.nen;
+                seg_end[s] = acc;
+            }
+        }
+        __syncthreads();
+        const i64 total_cand = ne ? seg_end[ne - 1] : 0;
+        const bool row_inner = a.is_inner[r];
+
+        // candidate flat index -> node number
+        auto candidate = [&](i64 t) -> int32_t {
+            int s = 0;
+            while (s < ne - 1 && t >= seg_end[s]) ++s;
+            const i64 local = t - (s ? seg_end[s - 1] : 0);
+            const i64 k = local / a.nen;
+            const int j = int(local % a.nen);
+            const int32_t eNL = a.local_only ? seg_elem[s] : a.nlist[seg_noff[s] + k];
+            return a.elems[i64(eNL) * a.nen + j];
+        };
+
+        // node range of the candidates
+        int lo = 0x7fffffff, hi = -1;
+        for (i64 t = threadIdx.x; t < total_cand; t += PT_THREADS) {
+            const int32_t c = candidate(t);
+            lo = min(lo, c); hi = max(hi, c);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if ((threadIdx.x & 31) == 0) { red_min[threadIdx.x >> 5] = lo; red_max[threadIdx.x >> 5] = hi; }
+        __syncthreads();
+        lo = red_min[0]; hi = red_max[0];
+        for (int w = 1; w < PT_THREADS / 32; ++w) { lo = min(lo, red_min[w]); hi = max(hi, red_max[w]); }
+        __syncthreads();
+
+        i64 n_inner = 0, n_bound = 0, n_full = 0;
+        if (!row_inner) {   // Dirichlet row: unit diagonal only in the inner parts
+            n_inner = 1; n_full = 1;
+            if (fill && threadIdx.x == 0) { a.col_inner[a.rp_inner[r]] = int32_t(r); a.col_full[a.rp_full[r]] = int32_t(r); }
+        }
+        for (i64 base = lo; hi >= 0 && base <= hi; base += PT_WINDOW) {
+            for (int w = threadIdx.x; w < PT_WORDS; w += PT_THREADS) { bm_inner[w] = 0u; bm_bound[w] = 0u; bm_full[w] = 0u; }
+            __syncthreads();
+            for (i64 t = threadIdx.x; t < total_cand; t += PT_THREADS) {
+                const int32_t c = candidate(t);
+                const i64 off = i64(c) - base;
+                if (off < 0 || off >= PT_WINDOW) continue;
+                const uint32_t bit = 1u << (off & 31);
+                const int word = int(off >> 5);
+                if (a.is_inner[c]) {
+                    if (row_inner) {
+                        atomicOr(&bm_full[word], bit);
+                        if (!a.symmetric || r <= c) atomicOr(&bm_inner[word], bit);
+                    }
+                } else if (c != r) {
+                    atomicOr(&bm_bound[word], bit);
+                }
+            }
+            __syncthreads();
+            const i64 span = min(i64(hi) - base + 1, PT_WINDOW);
+            const int words = int((span + 31) >> 5);
+            const int per = (words + PT_THREADS - 1) / PT_THREADS;
+            const int w0 = threadIdx.x * per, w1 = min(words, w0 + per);
+            i64 ci = 0, cb = 0, cf = 0;
+            for (int w = w0; w < w1; ++w) { ci += __popc(bm_inner[w]); cb += __popc(bm_bound[w]); cf += __popc(bm_full[w]); }
+            i64 ti, tb, tf;
+            const i64 oi = block_scan_excl(ci, sh_scan, &ti);
+            const i64 ob = block_scan_excl(cb, sh_scan, &tb);
+            const i64 of = block_scan_excl(cf, sh_scan, &tf);
+            if (fill) {
+                i64 pi = a.rp_inner[r] + n_inner + oi, pb = a.rp_bound[r] + n_bound + ob, pf = a.rp_full[r] + n_full + of;
+                for (int w = w0; w < w1; ++w) {
+                    for (uint32_t m = bm_inner[w]; m; m &= m - 1) a.col_inner[pi++] = int32_t(base + i64(w) * 32 + __ffs(m) - 1);
+                    for (uint32_t m = bm_bound[w]; m; m &= m - 1) a.col_bound[pb++] = int32_t(base + i64(w) * 32 + __ffs(m) - 1);
+                    for (uint32_t m = bm_full[w]; m; m &= m - 1) a.col_full[pf++] = int32_t(base + i64(w) * 32 + __ffs(m) - 1);
+                }
+            }
+            n_inner += ti; n_bound += tb; n_full += tf;
+            __syncthreads();
+        }
+        if (!fill) {
+            if (threadIdx.x == 0) { a.cnt_inner[r] = n_inner; a.cnt_bound[r] = n_bound; a.cnt_full[r] = (n_full + 3) & ~i64(3); }
+        } else {   // pad the solver row to a multiple of 4 with (r, 0) entries
+            const i64 end = a.rp_full[r + 1];
+            for (i64 k = a.rp_full[r] + n_full + threadIdx.x; k < end; k += PT_THREADS) a.col_full[k] = int32_t(r);
+        }
+        __syncthreads();
+    }
+}
+
+// full-row entry -> index of the same value in the upper storage (or -1 for padding)
+__global__ void k_full_map(i64 n, const i64* __restrict__ up_rp, const int32_t* __restrict__ up_col,
+                           const i64* __restrict__ full_rp, const int32_t* __restrict__ full_col,
+                           const uint8_t* __restrict__ is_inner, bool symmetric, i64* __restrict__ map) {
+    const int lane = threadIdx.x & 31;
+    const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
+    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
+        const i64 fb = full_rp[r], fe = full_rp[r + 1];
+        const i64 ub = up_rp[r], ue = up_rp[r + 1];
+        for (i64 k = fb + lane; k < fe; k += 32) {
+            const int32_t c = full_col[k];
+            i64 target = -1;
+            // real entries are strictly increasing; padding (col r) breaks the order
+            if (k > fb && c <= full_col[k - 1]) target = -1;
+            else if (!symmetric || c >= int32_t(r)) {
+                i64 lo = ub, hi = ue;   // search c in row r
+                while (lo < hi) { const i64 mid = (lo + hi) >> 1; if (up_col[mid] < c) lo = mid + 1; else hi = mid; }
+                target = (lo < ue && up_col[lo] == c) ? lo : -1;
+            } else {
+                i64 lo = up_rp[c], hi = up_rp[c + 1];   // transpose: search r in row c
+                while (lo < hi) { const i64 mid = (lo + hi) >> 1; if (up_col[mid] < int32_t(r)) lo = mid + 1; else hi = mid; }
+                target = (lo < up_rp[c + 1] && up_col[lo] == int32_t(r)) ? lo : -1;
+            }
+            map[k] = target;
+        }
+        (void)is_inner;
+    }
+}
+
+}  // namespace
+
+void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* bound, Csr* full,
+                    dbuf<i64>* full_from_upper) {
+    const i64 n = ctx.n_nodes;
+    NL_REQUIRE(local_only || ctx.neighbours_ready, NLGPU_ERR_STATE, "neighbour search must run before a nonlocal assembly");
+    dbuf<i64> ci, cb, cf;
+    ci.resize(size_t(n + 1)); cb.resize(size_t(n + 1)); cf.resize(size_t(n + 1));
+    ci.zero(ctx.stream); cb.zero(ctx.stream); cf.zero(ctx.stream);
+    dbuf<int> err;
+    err.resize(1); err.zero(ctx.stream);
+    PatternArgs a{};
+    a.n = n; a.nen = ctx.basis.nen; a.local_only = local_only; a.symmetric = symmetric;
+    a.elems = ctx.elems.p; a.ne_off = ctx.ne_off.p; a.ne_elem = ctx.ne_elem.p;
+    a.noff = local_only ? nullptr : ctx.noff.p; a.nlist = local_only ? nullptr : ctx.nlist.p;
+    a.is_inner = ctx.is_inner.p;
+    a.cnt_inner = ci.p; a.cnt_bound = cb.p; a.cnt_full = cf.p; a.error = err.p;
+    const unsigned grid = unsigned(std::min<i64>(n, 152 * 8));
+    NL_LAUNCH(k_pattern, grid, PT_THREADS, 0, ctx.stream, a);
+    int herr = 0;
+    NL_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof herr, cudaMemcpyDeviceToHost, ctx.stream));
+    i64 nnz_i = 0, nnz_b = 0, nnz_f = 0;
+    inner.rows = n; inner.rowptr.resize(size_t(n + 1));
+    exclusive_scan(ctx, ci.p, inner.rowptr.p, n + 1, &nnz_i);
+    NL_REQUIRE(herr == 0, NLGPU_ERR_UNSUPPORTED, "a node belongs to more than 16 elements");
+    Csr tmp_bound, tmp_full;
+    Csr& B = bound ? *bound : tmp_bound;
+    Csr& F = full ? *full : tmp_full;
+    B.rows = n; B.rowptr.resize(size_t(n + 1));
+    F.rows = n; F.rowptr.resize(size_t(n + 1));
+    exclusive_scan(ctx, cb.p, B.rowptr.p, n + 1, &nnz_b);
+    exclusive_scan(ctx, cf.p, F.rowptr.p, n + 1, &nnz_f);
+    inner.nnz = nnz_i; B.nnz = nnz_b; F.nnz = nnz_f;
+    inner.col.resize(size_t(nnz_i)); B.col.resize(size_t(nnz_b)); F.col.resize(size_t(nnz_f));
+    a.rp_inner = inner.rowptr.p; a.rp_bound = B.rowptr.p; a.rp_full = F.rowptr.p;
+    a.col_inner = inner.col.p; a.col_bound = B.col.p; a.col_full = F.col.p;
+    // count pointers stay set but are not written in the fill pass
+    NL_LAUNCH(k_pattern, grid, PT_THREADS, 0, ctx.stream, a);
+    inner.val.resize(size_t(nnz_i)); inner.val.zero(ctx.stream);
+    B.val.resize(size_t(nnz_b)); B.val.zero(ctx.stream);
+    if (full && full_from_upper) {
+        full_from_upper->resize(size_t(nnz_f));
+        NL_LAUNCH(k_full_map, grid_for(n * 32, 256, 152 * 64), 256, 0, ctx.stream, n, inner.rowptr.p, inner.col.p,
+                  F.rowptr.p, F.col.p, ctx.is_inner.p, symmetric, full_from_upper->p);
+        F.val.resize(size_t(nnz_f));
+    }
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+}  // namespace nlgpu

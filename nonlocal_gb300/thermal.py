@@ -1,0 +1,317 @@
+"""Host-side mirror of NonLocFEM's thermal solver API over the nlgpu C ABI.
+
+Names and argument meaning follow the reference:
+
+* ``Problem2D`` holds what the reference spreads over ``mesh::mesh_2d``,
+  ``parameters_2d`` and ``thermal_boundaries_conditions_2d``: one device
+  context (``nlgpu_ctx``) per problem;
+* ``find_neighbours`` -- ``mesh::find_neighbours`` (find_neighbours.hpp:469-510);
+* ``Problem2D.conductivity_matrix`` -- ``conductivity_matrix_2d::compute``
+  (conductivity_matrix_2d.hpp:166-193);
+* ``stationary_heat_equation_solver_2d`` (stationary_heat_equation_solver_2d.hpp:46-120);
+* ``NonstationaryHeatEquationSolver2D`` (nonstationary_heat_equation_solver_2d.hpp:16-106);
+* ``conjugate_gradient`` -- ``slae::conjugate_gradient`` with the ILLT
+  preconditioner (conjugate_gradient.hpp:15-79, eigen_preconditioner.hpp:136-137);
+* ``stationary_heat_equation_solver_1d`` (stationary_heat_equation_solver_1d.hpp:43-122).
+
+Errors raise ``NlgpuError`` (the reference throws std::domain_error /
+std::logic_error); every compute call runs on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from .meshgen import BILINEAR, SERENDIPITY, QuadMesh
+
+ELEMENT_TYPE = {BILINEAR: L.BILINEAR, SERENDIPITY: L.QUADRATIC_SERENDIPITY}
+
+
+@dataclass
+class Model2D:
+    """model_parameters<2, T> with its influence function and constant conductivity."""
+
+    influence: str = "fast_polynomial"      # constant | polynomial | exponential | fast_polynomial
+    radius: tuple[float, float] = (0.1, 0.1)
+    local_weight: float = 1.0               # p1
+    n: int = 2                              # powered-distance exponent
+    p: int = 2
+    q: float | None = None                  # default 1 (polynomial) / 0.5 (exponential)
+    conductivity: tuple[float, ...] = (1.0,)  # (l,) | (lx, ly) | (xx, yy, xy)
+
+    def to_c(self) -> L.Model2D:
+        m = L.Model2D()
+        m.influence = L.INFLUENCE[self.influence]
+        m.n, m.p = int(self.n), int(self.p)
+        m.q = float(self.q if self.q is not None else (0.5 if self.influence == "exponential" else 1.0))
+        m.radius[0], m.radius[1] = float(self.radius[0]), float(self.radius[1])
+        m.local_weight = float(self.local_weight)
+        c = tuple(float(v) for v in self.conductivity)
+        m.conductivity_kind = L.CONDUCTIVITY_KIND[len(c)]
+        for k, v in enumerate(c):
+            m.conductivity[k] = v
+        return m
+
+
+@dataclass
+class Boundary:
+    """A boundary group: ``kind`` 'temperature' or 'flux', constant value or per-node values."""
+
+    edges: np.ndarray
+    kind: str = "temperature"
+    value: float = 0.0
+    node_values: np.ndarray | None = None
+
+
+@dataclass
+class SolveReport:
+    values: dict = field(default_factory=dict)
+
+    def __getattr__(self, name):
+        try:
+            return self.values[name]
+        except KeyError as e:
+            raise AttributeError(name) from e
+
+
+class Context:
+    """An nlgpu_ctx: device state of one problem on one CUDA stream."""
+
+    def __init__(self, stream: int | None = None):
+        self._lib = L.load()
+        self._h = ctypes.c_void_p()
+        L.check(self._lib.nlgpu_create(ctypes.byref(self._h), stream))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.nlgpu_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def synchronize(self) -> None:
+        L.check(self._lib.nlgpu_synchronize(self._h))
+
+
+class Problem2D(Context):
+    """One 2D thermal problem held on the GPU."""
+
+    def __init__(self, element: str | int, nodes, elements, stream: int | None = None):
+        super().__init__(stream)
+        et = ELEMENT_TYPE.get(element, element)
+        self.nodes = L.f64(nodes)
+        self.elements = L.i64(elements)
+        L.check(self._lib.nlgpu_mesh_2d(self._h, int(et), self.nodes.shape[0], L.ptr(self.nodes),
+                                        self.elements.shape[0], L.ptr(self.elements)))
+        self.n_nodes = int(self.nodes.shape[0])
+        self.n_elements = int(self.elements.shape[0])
+        self.nodes_per_element = int(self.elements.shape[1])
+        self.qnodes = 4 if self.nodes_per_element == 4 else 9
+
+    @classmethod
+    def from_mesh(cls, mesh: QuadMesh, **kw) -> "Problem2D":
+        return cls(mesh.element, mesh.nodes, mesh.elements, **kw)
+
+    # ---- model, boundaries ------------------------------------------------
+    def set_model(self, model: Model2D) -> None:
+        m = model.to_c()
+        L.check(self._lib.nlgpu_set_model_2d(self._h, ctypes.byref(m)))
+        self.model = model
+
+    def set_conductivity_field(self, values: np.ndarray | None) -> None:
+        self._cond = None if values is None else L.f64(values).reshape(-1)
+        L.check(self._lib.nlgpu_set_conductivity_field(self._h, L.ptr(self._cond)))
+
+    def set_capacity(self, capacity: float = 1.0, density: float = 1.0) -> None:
+        L.check(self._lib.nlgpu_set_capacity(self._h, capacity, density))
+
+    def add_boundary(self, b: Boundary) -> None:
+        edges = L.i64(b.edges)
+        nv = None if b.node_values is None else L.f64(b.node_values)
+        kind = L.BC_TEMPERATURE if b.kind == "temperature" else L.BC_FLUX
+        L.check(self._lib.nlgpu_add_boundary_2d(self._h, kind, edges.shape[0], edges.shape[1], L.ptr(edges),
+                                                float(b.value), L.ptr(nv)))
+
+    def clear_boundaries(self) -> None:
+        L.check(self._lib.nlgpu_clear_boundaries(self._h))
+
+    def set_source(self, value: float = 0.0, per_qnode: np.ndarray | None = None) -> None:
+        self._src = None if per_qnode is None else L.f64(per_qnode).reshape(-1)
+        L.check(self._lib.nlgpu_set_source(self._h, float(value), L.ptr(self._src)))
+
+    def set_dirichlet_values(self, values: np.ndarray | None) -> None:
+        self._dv = None if values is None else L.f64(values)
+        L.check(self._lib.nlgpu_set_dirichlet_values(self._h, L.ptr(self._dv)))
+
+    # ---- mesh data ------------------------------------------------------------
+    def quadrature(self):
+        E, nq, nen = self.n_elements, self.qnodes, self.nodes_per_element
+        qc, jac, der = np.empty((E, nq, 2)), np.empty((E, nq)), np.empty((E, nen, nq, 2))
+        L.check(self._lib.nlgpu_get_quadrature(self._h, L.ptr(qc), L.ptr(jac), L.ptr(der)))
+        return qc, jac, der
+
+    def basis(self) -> dict:
+        nen, nq = ctypes.c_int(), ctypes.c_int()
+        L.check(self._lib.nlgpu_get_basis(self._h, ctypes.byref(nen), ctypes.byref(nq), None, None, None, None, None))
+        qN, qNxi, qNeta = (np.empty(nen.value * nq.value) for _ in range(3))
+        w, c = np.empty(nq.value), np.empty(nen.value)
+        L.check(self._lib.nlgpu_get_basis(self._h, None, None, L.ptr(qN), L.ptr(qNxi), L.ptr(qNeta), L.ptr(w), L.ptr(c)))
+        return {"basis_qN": qN, "basis_qNxi": qNxi, "basis_qNeta": qNeta, "basis_weights": w, "basis_centre": c}
+
+    # ---- neighbours -----------------------------------------------------------
+    def find_neighbours(self, strategy: str = "MAX") -> tuple[np.ndarray, int]:
+        r = np.empty(2)
+        pairs = ctypes.c_int64()
+        L.check(self._lib.nlgpu_find_neighbours(self._h, L.EXPAND[strategy], L.ptr(r), ctypes.byref(pairs)))
+        self.pairs = int(pairs.value)
+        return r, self.pairs
+
+    def neighbours(self) -> tuple[np.ndarray, np.ndarray]:
+        off = np.empty(self.n_elements + 1, dtype=np.int64)
+        L.check(self._lib.nlgpu_get_neighbours(self._h, L.ptr(off), None))
+        lst = np.empty(int(off[-1]), dtype=np.int64)
+        L.check(self._lib.nlgpu_get_neighbours(self._h, None, L.ptr(lst)))
+        return off, lst
+
+    # ---- assembly -------------------------------------------------------------
+    def conductivity_matrix(self, part: str = "FULL") -> tuple[int, int]:
+        ni, nb = ctypes.c_int64(), ctypes.c_int64()
+        L.check(self._lib.nlgpu_conductivity_matrix_2d(self._h, L.PART_FULL if part == "FULL" else L.PART_LOCAL,
+                                                       ctypes.byref(ni), ctypes.byref(nb)))
+        self._nnz = {"FULL": (int(ni.value), int(nb.value))} if part == "FULL" else {"LOCAL": (int(ni.value), 0)}
+        if part == "FULL":
+            self.nnz_inner, self.nnz_bound = int(ni.value), int(nb.value)
+        else:
+            self.nnz_local = int(ni.value)
+        return int(ni.value), int(nb.value)
+
+    def matrix(self, which: str = "inner") -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        code = {"inner": L.MATRIX_INNER, "bound": L.MATRIX_BOUND, "local": L.MATRIX_LOCAL}[which]
+        rp = np.empty(self.n_nodes + 1, dtype=np.int64)
+        L.check(self._lib.nlgpu_get_matrix(self._h, code, L.ptr(rp), None, None))
+        col = np.empty(int(rp[-1]), dtype=np.int64)
+        val = np.empty(int(rp[-1]))
+        L.check(self._lib.nlgpu_get_matrix(self._h, code, None, L.ptr(col), L.ptr(val)))
+        return rp, col, val
+
+    def rhs(self) -> tuple[np.ndarray, np.ndarray]:
+        f, f0 = np.empty(self.n_nodes), np.empty(self.n_nodes)
+        L.check(self._lib.nlgpu_get_rhs(self._h, L.ptr(f), L.ptr(f0)))
+        return f, f0
+
+    # ---- solves -----------------------------------------------------------------
+    @staticmethod
+    def _options(tolerance, max_iterations, preconditioner, precision) -> L.SolveOptions:
+        o = L.SolveOptions()
+        o.tolerance, o.max_iterations = float(tolerance), int(max_iterations)
+        o.preconditioner, o.precision = L.PRECONDITIONER[preconditioner], L.PRECISION[precision]
+        return o
+
+    def stationary(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64",
+                   check_convergence=True):
+        o = self._options(tolerance, max_iterations, preconditioner, precision)
+        t = np.empty(self.n_nodes)
+        rep = L.SolveReport()
+        rc = self._lib.nlgpu_stationary_2d(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep))
+        if rc != L.OK and (check_convergence or rc != 6):
+            L.check(rc)
+        return t, SolveReport(rep.as_dict())
+
+    def solve_assembled(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64"):
+        o = self._options(tolerance, max_iterations, preconditioner, precision)
+        t = np.empty(self.n_nodes)
+        rep = L.SolveReport()
+        L.check(self._lib.nlgpu_solve_assembled(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep)))
+        return t, SolveReport(rep.as_dict())
+
+
+def find_neighbours(problem: Problem2D, strategy: str = "MAX"):
+    """mesh::find_neighbours: widened radii, offsets, lists (reference order)."""
+    r, _ = problem.find_neighbours(strategy)
+    off, lst = problem.neighbours()
+    return r, off, lst
+
+
+def stationary_heat_equation_solver_2d(problem: Problem2D, model: Model2D, boundaries: list[Boundary],
+                                       source: float = 0.0, tolerance: float = 1e-10, max_iterations: int = 10000,
+                                       preconditioner: str = "illt", precision: str = "fp64"):
+    problem.set_model(model)
+    problem.clear_boundaries()
+    for b in boundaries:
+        problem.add_boundary(b)
+    if source:
+        problem.set_source(source)
+    return problem.stationary(tolerance, max_iterations, preconditioner, precision)
+
+
+class NonstationaryHeatEquationSolver2D:
+    """Implicit Euler in time: (C + dt K) T^{k+1} = C T^k + dt f, identity-preconditioned CG."""
+
+    def __init__(self, problem: Problem2D, time_step: float):
+        self.problem, self.time_step = problem, float(time_step)
+        self.temperature = np.zeros(problem.n_nodes)
+        self.iterations: list[int] = []
+
+    def compute(self, initial: np.ndarray | None = None) -> None:
+        init = None if initial is None else L.f64(initial)
+        L.check(self.problem._lib.nlgpu_nonstationary_2d_compute(self.problem.handle, self.time_step, L.ptr(init)))
+        if init is not None:
+            self.temperature = init.copy()
+
+    def calc_step(self, dirichlet_value: float = 0.0, dirichlet_values: np.ndarray | None = None,
+                  tolerance: float = 1e-15, max_iterations: int = 10000) -> np.ndarray:
+        dv = None if dirichlet_values is None else L.f64(dirichlet_values)
+        it = ctypes.c_int64()
+        t = np.empty(self.problem.n_nodes)
+        rc = self.problem._lib.nlgpu_nonstationary_2d_step(self.problem.handle, float(dirichlet_value), L.ptr(dv),
+                                                           float(tolerance), int(max_iterations), L.ptr(t),
+                                                           ctypes.byref(it))
+        if rc not in (L.OK, 6):   # the reference loops to its iteration cap without raising
+            L.check(rc)
+        self.iterations.append(int(it.value))
+        self.temperature = t
+        return t
+
+
+def conjugate_gradient(problem: Problem2D, a_csr, b, x0=None, preconditioner_csr=None, tolerance=1e-10,
+                       max_iterations=10000):
+    """slae::conjugate_gradient on an upper-stored symmetric CSR (diagonal first in each row)."""
+    rp, col, val = (L.i64(a_csr[0]), L.i64(a_csr[1]), L.f64(a_csr[2]))
+    b = L.f64(b)
+    n = b.shape[0]
+    x = np.empty(n)
+    x0 = None if x0 is None else L.f64(x0)
+    if preconditioner_csr is not None:
+        prp, pcol, pval = (L.i64(preconditioner_csr[0]), L.i64(preconditioner_csr[1]), L.f64(preconditioner_csr[2]))
+    else:
+        prp = pcol = pval = None
+    rep = L.SolveReport()
+    rc = problem._lib.nlgpu_cg_solve(problem.handle, n, L.ptr(rp), L.ptr(col), L.ptr(val), L.ptr(prp), L.ptr(pcol),
+                                     L.ptr(pval), L.ptr(b), L.ptr(x0), float(tolerance), int(max_iterations), L.ptr(x),
+                                     ctypes.byref(rep))
+    L.check(rc)
+    return x, SolveReport(rep.as_dict())
+
+
+def stationary_heat_equation_solver_1d(context: Context | None = None, elements: int = 1000, order: int = 2, length: float = 1.0,
+                                       radius: float = 0.1, local_weight: float = 0.5, influence: str = "bell",
+                                       conductivity: float = 1.0, t_left: float = 0.0, q_right: float = 1.0,
+                                       sin_source: bool = True) -> np.ndarray:
+    kinds = {"bell": 0, "triangle": 1, "normal": 2, "constant": 3}
+    ctx = context if context is not None else Context()
+    t = np.empty(elements * order + 1)
+    L.check(ctx._lib.nlgpu_stationary_1d(ctx.handle, int(elements), int(order), float(length), float(radius),
+                                             float(local_weight), kinds[influence], float(conductivity), float(t_left),
+                                             float(q_right), int(bool(sin_source)), L.ptr(t)))
+    return t

@@ -1,0 +1,243 @@
+"""Parity of the CUDA path (through the C ABI) with the reference.
+
+* golden fixtures: the reference's own outputs on the same inputs
+  (tests/golden, made by tests/golden/make_golden.py): neighbour lists and
+  sparsity patterns bit-exact, matrix values and right-hand sides within
+  1e-12 relative (max-norm scaled), nodal temperature within 1e-10 relative L2;
+* the oracle (CPU restatement pinned to those fixtures) on larger cases of the
+  benchmark shapes with the same r/h;
+* size-independent properties at the full benchmark sizes.
+"""
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+MATRIX_RTOL = 1e-12
+SOLUTION_RTOL = 1e-10
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="session")
+def lib():
+    from nonlocal_gb300 import _lib, build
+    build.build()
+    _lib.load()
+    if _lib.device_count() == 0:
+        pytest.fail("no CUDA device visible to the nlgpu library")
+    return _lib
+
+
+def gpu_problem(fx):
+    from nonlocal_gb300 import thermal as T
+    cfg = fx["config"]
+    pb = T.Problem2D(gc.element_type(fx), fx["nodes"], fx["elements"])
+    m = gc.model(cfg)
+    kind, cond = m["cond_kind"], m["cond"]
+    pb.set_model(T.Model2D(influence={v: k for k, v in gc.INFLUENCE.items()}[m["influence"]], radius=m["radius"],
+                           local_weight=m["local_weight"], n=m["n"], p=m["p"], q=m["q"],
+                           conductivity=cond[:kind + 1]))
+    for kind_, edges, value in gc.boundaries(fx):
+        pb.add_boundary(T.Boundary(edges=edges, kind="temperature" if kind_ == 0 else "flux", value=value))
+    if cfg.get("source") == "manufactured":
+        pb.set_source(0.0, fx["source_q"])
+    elif "source" in cfg:
+        pb.set_source(float(cfg["source"]))
+    if "dirichlet_values" in fx:
+        pb.set_dirichlet_values(fx["dirichlet_values"])
+    return pb
+
+
+def assert_csr_equal(got, fx, name):
+    rp, col, val = got
+    assert np.array_equal(rp, fx[name + "_rowptr"]), f"{name}: row pointers"
+    assert np.array_equal(col, fx[name + "_col"]), f"{name}: columns"
+    ref = fx[name + "_val"]
+    scale = np.abs(ref).max() if ref.size else 1.0
+    np.testing.assert_allclose(val, ref, rtol=MATRIX_RTOL, atol=MATRIX_RTOL * scale, err_msg=name)
+
+
+@pytest.fixture(scope="module", params=gc.STATIONARY_2D)
+def golden(request, lib):
+    fx = gc.load(request.param)
+    pb = gpu_problem(fx)
+    return request.param, fx, pb
+
+
+def test_basis_and_quadrature(golden):
+    _, fx, pb = golden
+    b = pb.basis()
+    for k, v in b.items():
+        np.testing.assert_allclose(v, fx[k].reshape(-1), rtol=0, atol=2e-15, err_msg=k)
+    qc, jac, der = pb.quadrature()
+    for got, key in [(qc, "qcoords"), (jac, "jacobians"), (der, "derivatives")]:
+        ref = fx[key].reshape(-1)
+        np.testing.assert_allclose(got.reshape(-1), ref, rtol=1e-13, atol=1e-14 * np.abs(ref).max(), err_msg=key)
+
+
+def test_neighbours_bit_exact(golden):
+    name, fx, pb = golden
+    if fx["config"].get("local_weight", 1) >= 0.999:
+        pytest.skip("local model")
+    r, pairs = pb.find_neighbours(fx["config"].get("strategy", "MAX"))
+    off, lst = pb.neighbours()
+    assert r[0] == pytest.approx(float(fx["search_radius"][0]), rel=1e-15)
+    assert np.array_equal(off, fx["neigh_offsets"])
+    assert np.array_equal(lst, fx["neigh_list"])
+
+
+def test_matrices_and_rhs(golden):
+    _, fx, pb = golden
+    if fx["config"].get("local_weight", 1) < 0.999:
+        pb.find_neighbours(fx["config"].get("strategy", "MAX"))
+    pb.conductivity_matrix("FULL")
+    assert_csr_equal(pb.matrix("inner"), fx, "K_inner")
+    assert_csr_equal(pb.matrix("bound"), fx, "K_bound")
+    f, f0 = pb.rhs()
+    for got, key in [(f0, "rhs_init"), (f, "rhs")]:
+        np.testing.assert_allclose(got, fx[key], rtol=MATRIX_RTOL, atol=MATRIX_RTOL * max(np.abs(fx[key]).max(), 1.0))
+    pb.conductivity_matrix("LOCAL")
+    assert_csr_equal(pb.matrix("local"), fx, "K_local")
+
+
+def test_stationary_solution(golden):
+    _, fx, pb = golden
+    if fx["config"].get("local_weight", 1) < 0.999:
+        pb.find_neighbours(fx["config"].get("strategy", "MAX"))
+    t, rep = pb.stationary(tolerance=1e-13, max_iterations=20000)
+    assert rep.preconditioner_ok == 1
+    assert rep.residual <= 1e-13
+    assert rel(t, fx["temperature"]) < SOLUTION_RTOL
+
+
+def test_known_answers(lib):
+    fx = gc.load("ref_square16_manufactured")
+    t, _ = gpu_problem(fx).stationary(tolerance=1e-13)
+    ex = fx["exact_solution"]
+    assert ((t - ex) ** 2).sum() / (ex ** 2).sum() < 1e-3                # boundary_conditions_2d.cpp:111
+    fx = gc.load("ref_solid_ring")
+    t, _ = gpu_problem(fx).stationary(tolerance=1e-13)
+    x = fx["nodes"]
+    exact = 1.0 + np.log(np.hypot(x[:, 0], x[:, 1])) / np.log(2.0)
+    assert np.abs(t - exact).max() / np.abs(exact).max() < 1.4e-3        # isotropic_solid_ring.cpp:43-45
+
+
+def test_cg_on_reference_matrices(lib):
+    """slae::conjugate_gradient with ILLT(p1 K_local) on the reference's own matrices."""
+    from nonlocal_gb300 import thermal as T
+    fx = gc.load("s6_exp_ortho_jitter")
+    ctx = gpu_problem(fx)
+    a = (fx["K_inner_rowptr"], fx["K_inner_col"], fx["K_inner_val"])
+    p = (fx["K_local_rowptr"], fx["K_local_col"], fx["K_local_val"])
+    x, rep = T.conjugate_gradient(ctx, a, fx["rhs"], preconditioner_csr=p, tolerance=1e-13)
+    assert rep.preconditioner_ok == 1
+    assert rel(x, fx["temperature"]) < SOLUTION_RTOL
+    x2, rep2 = T.conjugate_gradient(ctx, a, fx["rhs"], tolerance=1e-13)     # identity preconditioner
+    assert rel(x2, fx["temperature"]) < SOLUTION_RTOL
+    assert rep2.iterations > rep.iterations
+
+
+def test_nonstationary_history(lib):
+    from nonlocal_gb300 import thermal as T
+    fx = gc.load("b8_nonstationary")
+    cfg = fx["config"]
+    pb = T.Problem2D(gc.element_type(fx), fx["nodes"], fx["elements"])
+    m = gc.model(cfg)
+    pb.set_model(T.Model2D(influence="fast_polynomial", radius=m["radius"], local_weight=m["local_weight"]))
+    pb.add_boundary(T.Boundary(edges=fx["bnd_" + cfg["dirichlet_group"]], kind="temperature", value=0.0))
+    dt, steps, omega = float(cfg["dt"]), int(cfg["steps"]), float(cfg["omega"])
+    solver = T.NonstationaryHeatEquationSolver2D(pb, dt)
+    solver.compute()
+    for s in range(1, steps + 1):
+        t = solver.calc_step(np.sin(omega * s * dt), tolerance=1e-15, max_iterations=10000)
+        assert rel(t, fx["temperature_history"][s - 1]) < SOLUTION_RTOL, s
+
+
+@pytest.mark.parametrize("name", ["d1_quadratic_1000", "d1_linear_40_triangle"])
+def test_stationary_1d(lib, name):
+    from nonlocal_gb300 import thermal as T
+    fx = gc.load(name)
+    cfg = fx["config"]
+    t = T.stationary_heat_equation_solver_1d(elements=int(cfg["elements"]), order=int(cfg["order"]),
+                                             radius=float(cfg["radius"]), local_weight=float(cfg["local_weight"]),
+                                             influence=cfg["influence"], conductivity=float(cfg["conductivity"]),
+                                             t_left=float(cfg["left_temperature"]), q_right=float(cfg["right_flux"]),
+                                             sin_source=cfg["source"] == "sin")
+    assert rel(t, fx["temperature"]) < SOLUTION_RTOL
+
+
+# ---------------------------------------------------------------- oracle, larger cases
+def oracle_and_gpu(mesh, model_kw, bcs, lib):
+    import oracle
+    from nonlocal_gb300 import thermal as T
+    et = 2 if mesh.element == "bilinear" else 3
+    prob = oracle.Problem(et, mesh.nodes, mesh.elements)
+    kind = {1: 0, 2: 1, 3: 2}[len(model_kw["conductivity"])]
+    prob.set_model(influence=gc.INFLUENCE[model_kw["influence"]], n=2, p=model_kw.get("p", 2),
+                   q=model_kw.get("q", 0.5 if model_kw["influence"] == "exponential" else 1.0),
+                   radius=model_kw["radius"], local_weight=model_kw["local_weight"], cond_kind=kind,
+                   cond=tuple(model_kw["conductivity"]) + (0.0,) * (3 - len(model_kw["conductivity"])))
+    pb = T.Problem2D.from_mesh(mesh)
+    pb.set_model(T.Model2D(**model_kw))
+    for group, kind_, value in bcs:
+        prob.add_boundary(0 if kind_ == "temperature" else 1, mesh.boundaries[group], value)
+        pb.add_boundary(T.Boundary(edges=mesh.boundaries[group], kind=kind_, value=value))
+    return prob, pb
+
+
+@pytest.mark.parametrize("case", ["config2_scaled_40", "config3_scaled_20"])
+def test_against_oracle_scaled(lib, case):
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    if case == "config2_scaled_40":
+        mesh = structured_quad_mesh(40, 40, "bilinear")
+        model = dict(influence="fast_polynomial", radius=(0.25, 0.25), local_weight=0.5, conductivity=(1.0,))
+        bcs = [("left", "temperature", 0.0), ("right", "flux", 1.0)]
+    else:
+        mesh = structured_quad_mesh(20, 20, "serendipity", jitter=0.2, seed=0)
+        model = dict(influence="exponential", radius=(0.15, 0.15), local_weight=0.3, conductivity=(1.0, 0.1))
+        bcs = [("up", "temperature", 1.0), ("down", "temperature", 0.0)]
+    prob, pb = oracle_and_gpu(mesh, model, bcs, lib)
+    prob.find_neighbours()
+    prob.assemble()
+    prob.assemble_local()
+    prob.solve(variant=1, tol=1e-13)
+    pb.find_neighbours()
+    off, lst = pb.neighbours()
+    assert np.array_equal(off, prob.get("neigh_offsets"))
+    assert np.array_equal(lst, prob.get("neigh_list"))
+    pb.conductivity_matrix("FULL")
+    rp, col, val = pb.matrix("inner")
+    orp, ocol, oval = prob.csr("K_inner")
+    assert np.array_equal(rp, orp) and np.array_equal(col, ocol)
+    np.testing.assert_allclose(val, oval, rtol=MATRIX_RTOL, atol=MATRIX_RTOL * np.abs(oval).max())
+    t, rep = pb.stationary(tolerance=1e-13)
+    assert rel(t, prob.get("solution")) < SOLUTION_RTOL
+    # same preconditioner (fixed-pattern IC(0) on the scaled, shifted local matrix): iteration counts agree
+    assert abs(rep.iterations - prob.scalar("iterations")) <= 2
+
+
+def test_operator_annihilates_constants_full_size(lib):
+    """Without boundary conditions every row of K sums to zero (sum_j grad N_j = 0),
+    at the full 200x200 benchmark size; the assembled upper part is symmetric by construction."""
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    mesh = structured_quad_mesh(200, 200, "bilinear")
+    pb = T.Problem2D.from_mesh(mesh)
+    pb.set_model(T.Model2D(influence="fast_polynomial", radius=(0.05, 0.05), local_weight=0.5))
+    r, pairs = pb.find_neighbours()
+    assert r[0] == pytest.approx(0.05 + 0.005 * np.sqrt(2), rel=1e-12)
+    off, _ = pb.neighbours()
+    counts = np.diff(off).reshape(200, 200)
+    assert counts[100, 100] == 421          # lattice points with |d| <= 10 + sqrt(2)
+    pb.conductivity_matrix("FULL")
+    rp, col, val = pb.matrix("inner")
+    n = pb.n_nodes
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    off_diag = col != rows
+    sums = np.bincount(rows, weights=val, minlength=n) + np.bincount(col[off_diag], weights=val[off_diag], minlength=n)
+    assert np.abs(sums).max() < 1e-12 * np.abs(val).max() * 50
