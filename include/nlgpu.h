@@ -111,6 +111,8 @@ const char* nlgpu_last_error(void);
 int nlgpu_device_count(int* count);
 /* Number of kernels this library launched in the calling process so far. */
 int64_t nlgpu_kernel_launches(void);
+/* Selects the CUDA device of the calling thread for contexts created after it. */
+int nlgpu_set_device(int device);
 
 /* ---- context ------------------------------------------------------------ */
 /* Creates a context on the current device.  `stream` is a cudaStream_t to run

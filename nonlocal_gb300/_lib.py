@@ -63,6 +63,7 @@ SIGNATURES = {
     "nlgpu_last_error": (ctypes.c_char_p, []),
     "nlgpu_device_count": (c_int, [ctypes.POINTER(c_int)]),
     "nlgpu_kernel_launches": (c_i64, []),
+    "nlgpu_set_device": (c_int, [c_int]),
     "nlgpu_create": (c_int, [ctypes.POINTER(c_p), c_p]),
     "nlgpu_destroy": (c_int, [c_p]),
     "nlgpu_synchronize": (c_int, [c_p]),

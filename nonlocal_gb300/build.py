@@ -71,7 +71,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
     tmp = LIB + ".tmp"
-    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    # the CUDA runtime is linked statically: the library needs no libcudart at run time
+    cmd = [cc, "-shared", "-cudart", "static", "-o", tmp] + objs + ARCH
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

@@ -158,6 +158,10 @@ int nlgpu_device_count(int* count) {
 
 int64_t nlgpu_kernel_launches(void) { return g_launches.load(); }
 
+int nlgpu_set_device(int device) {
+    return guarded([&] { NL_CUDA(cudaSetDevice(device)); });
+}
+
 int nlgpu_create(nlgpu_ctx** ctx, void* stream) {
     if (!ctx) return NLGPU_ERR_ARG;
     return guarded([&] {
