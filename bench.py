@@ -1,0 +1,380 @@
+#!/usr/bin/env python3
+"""Benchmark of the nonlocal thermal hot path on GB300.
+
+Workload (default ``config2``): unit square, 200x200 bilinear elements, 2x2
+Gauss, isotropic conductivity 1, p1 = 0.5, polynomial-bell (fast_polynomial)
+influence r = 0.05 (search radius widened to r + h*sqrt(2)), T = 0 on the
+left edge, unit flux on the right edge, no source; ILLT-preconditioned CG to
+relative residual |b - Ax| / |b| <= 1e-10 in FP64.  Synthetic structured
+mesh, deterministic.
+
+One step = one stationary solve from the resident mesh: neighbour search,
+sparsity patterns, nonlocal + local assembly, boundary conditions, ILLT
+factorisation and CG.  value = device time per solve (CUDA events on the
+library's stream), L2 flushed between steps.  e2e = the same solve through
+the C ABI from host buffers (mesh upload and temperature download included).
+
+--impl reference times the reference algorithm on the host cores instead
+(the CPU restatement in oracle/, all threads), same workload and metric.
+Multi-GPU (torchrun): independent replicas, one per rank (the path does not
+shard); the time is the maximum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to 1e-10 relative residual, nonlocal stationary 2D solve (plain FP64 ILLT-CG, full pipeline)"
+
+WORKLOADS = {
+    "config2": dict(name="200x200 bilinear, fast_polynomial r=0.05, p1=0.5, left T=0 / right flux 1, FP64 ILLT-CG 1e-10",
+                    nx=200, ny=200, element="bilinear", jitter=0.0,
+                    model=dict(influence="fast_polynomial", radius=(0.05, 0.05), local_weight=0.5, conductivity=(1.0,)),
+                    bcs=[("left", "temperature", 0.0), ("right", "flux", 1.0)], tolerance=1e-10),
+    "config3": dict(name="300x300 8-node serendipity jittered 0.2h, normal kernel r=0.05, p1=0.3, ortho (1,0.1), "
+                         "top T=1 / bottom T=0, FP64 ILLT-CG 1e-10",
+                    nx=300, ny=300, element="serendipity", jitter=0.2,
+                    model=dict(influence="exponential", radius=(0.05, 0.05), local_weight=0.3, conductivity=(1.0, 0.1)),
+                    bcs=[("up", "temperature", 1.0), ("down", "temperature", 0.0)], tolerance=1e-10),
+}
+# algorithmic FLOPs of one element pair: 2 D (nq^2 nen + nen nq nen), D = 2
+PAIR_FLOPS = {"bilinear": 2 * 2 * (4 * 4 * 4 + 4 * 4 * 4), "serendipity": 2 * 2 * (9 * 9 * 8 + 8 * 9 * 8)}
+PAIR_QUAD = {"bilinear": 16, "serendipity": 81}
+L2_FLUSH_BYTES = 256 << 20
+
+
+def peaks() -> tuple[dict, str]:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic() -> dict:
+    """DRAM bytes per launch from the committed ncu summaries (profiles/roofline_traffic.txt)."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    if os.path.exists(path):
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 3 and not line.startswith("#"):
+                out[(parts[0], parts[1])] = float(parts[2])
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        self.file = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.file.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, value: float) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_problem(w, T, mesh):
+    pb = T.Problem2D.from_mesh(mesh)
+    pb.set_model(T.Model2D(**w["model"]))
+    for group, kind, value in w["bcs"]:
+        pb.add_boundary(T.Boundary(edges=mesh.boundaries[group], kind=kind, value=value))
+    return pb
+
+
+def cpu_solve(w, mesh) -> tuple[float, dict]:
+    """One full solve of the workload by the CPU restatement; returns seconds and details."""
+    import oracle
+    et = oracle.BILINEAR if w["element"] == "bilinear" else oracle.SERENDIPITY
+    inf = {"fast_polynomial": oracle.INF_FAST_POLYNOMIAL, "exponential": oracle.INF_EXPONENTIAL}[w["model"]["influence"]]
+    cond = tuple(w["model"]["conductivity"])
+    t0 = time.perf_counter()
+    p = oracle.Problem(et, mesh.nodes, mesh.elements)
+    p.set_model(influence=inf, radius=w["model"]["radius"], local_weight=w["model"]["local_weight"],
+                cond_kind=len(cond) - 1, cond=cond + (0.0,) * (3 - len(cond)))
+    for group, kind, value in w["bcs"]:
+        p.add_boundary(oracle.BC_TEMPERATURE if kind == "temperature" else oracle.BC_FLUX, mesh.boundaries[group], value)
+    p.find_neighbours()
+    p.assemble()
+    p.assemble_local()
+    p.solve(variant=0, tol=w["tolerance"])
+    dt = time.perf_counter() - t0
+    return dt, {"solution": p.get("solution"), "iterations": int(p.scalar("iterations")),
+                "neighbours_s": p.scalar("neighbours"),
+                "assembly_s": p.scalar("assembly"), "ilt_s": p.scalar("ilt"), "cg_s": p.scalar("cg"),
+                "true_residual": p.scalar("true_residual"), "threads": int(p.scalar("threads"))}
+
+
+def run_reference(args, w, mesh, world, rank, dist):
+    """Reference arm: the reference algorithm on the host cores (CPU restatement, all threads)."""
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    for _ in range(args.warmup):
+        cpu_solve(w, mesh)
+    times, det = [], {}
+    for _ in range(args.steps):
+        t, det = cpu_solve(w, mesh)
+        times.append(t)
+    value = sum(times) / len(times)
+    line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": w["name"], "mesh": f"{w['nx']}x{w['ny']} {w['element']}"},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": det.get("threads", cores), "kind": "port",
+                             "sample": "one full solve of the workload per step (neighbours, assembly, local "
+                                       "assembly, ILLT, CG to 1e-10) by the CPU restatement"},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "details": {k: v for k, v in det.items() if k != "solution"}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args, w, mesh, world, rank, local, dist):
+    from nonlocal_gb300 import _lib as L
+    from nonlocal_gb300 import build as nbuild
+    from nonlocal_gb300 import thermal as T
+    import ctypes
+    nbuild.build()
+    lib = L.load()
+    L.check(lib.nlgpu_set_device(local))
+    pb = make_problem(w, T, mesh)
+    h = pb.handle
+    tol = w["tolerance"]
+
+    def step():
+        pb.find_neighbours()
+        return pb.stationary(tolerance=tol, max_iterations=100000)
+
+    for _ in range(args.warmup):
+        temp, rep = step()
+    # -------- timed region: device time per solve, L2 flushed between solves
+    sampler = ClockSampler(local)
+    launches0 = L.kernel_launches()
+    barrier(dist)
+    L.check(lib.nlgpu_synchronize(h))
+    sampler.start()
+    ms_steps = []
+    reports = []
+    for k in range(args.steps):
+        L.check(lib.nlgpu_flush_l2(h, L2_FLUSH_BYTES))
+        L.check(lib.nlgpu_event_record(h, 0))
+        temp, rep = step()
+        L.check(lib.nlgpu_event_record(h, 1))
+        ms = ctypes.c_double()
+        L.check(lib.nlgpu_event_elapsed(h, 0, 1, ctypes.byref(ms)))
+        ms_steps.append(ms.value)
+        reports.append(rep)
+    L.check(lib.nlgpu_synchronize(h))
+    clocks = sampler.stop()
+    launches = L.kernel_launches() - launches0
+    barrier(dist)
+    mean_ms = max_over_ranks(dist, sum(ms_steps) / len(ms_steps))
+    seconds = mean_ms / 1e3
+    rep = reports[-1]
+    pairs = rep.element_pairs
+    iters = rep.iterations
+
+    # -------- stage timings for the roofline (device events, this problem)
+    stage_ms = {}
+    for stage, name, reps in [(0, "spmv", 50), (2, "illt_apply", 20), (1, "pair_assembly", 3)]:
+        v = ctypes.c_double()
+        L.check(lib.nlgpu_time_stage(h, stage, reps, ctypes.byref(v)))
+        stage_ms[name] = v.value
+    n = pb.n_nodes
+    nnz_solver = rep.nnz_solver
+    spmv_bytes = nnz_solver * (8 + 4) + (n + 1) * 8 + 2 * n * 8
+    per_solve_ms = {"spmv": stage_ms["spmv"] * (iters + 2), "illt_apply": stage_ms["illt_apply"] * (iters + 1),
+                    "pair_assembly": stage_ms["pair_assembly"]}
+    dominant = max(per_solve_ms, key=per_solve_ms.get)
+    pk, pk_kind = peaks()
+    traffic = profile_traffic()
+    if dominant == "pair_assembly":
+        flops = pairs * PAIR_FLOPS[w["element"]]
+        achieved = flops / (stage_ms["pair_assembly"] * 1e-3) / 1e12
+        fp64_peak = 1.25   # nominal GB300 FP64 TFLOP/s (not in the measured peaks file)
+        roof = {"kernel": "k_assemble_pairs", "bound": "fp64", "achieved": achieved, "peak": fp64_peak,
+                "peak_kind": "nominal FP64 (no measured FP64 peak on this pool)", "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak, "traffic": traffic.get(("k_assemble_pairs", args.workload))}
+    elif dominant == "spmv":
+        achieved = spmv_bytes / (stage_ms["spmv"] * 1e-3) / 1e9
+        roof = {"kernel": "k_spmv", "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                "peak_kind": pk_kind, "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                "traffic": traffic.get(("k_spmv", args.workload))}
+    else:
+        # both sweeps read each off-diagonal factor entry (value 8 B + column 4 B)
+        # once, per row its number and inverse diagonal (4 + 8 B) once, r and S
+        # (16 B) once, and write y, w and z (24 B)
+        ilt_bytes = factor_offdiag_entries(lib, h, n) * 12 + n * (4 + 8) * 2 + n * 8 * 5
+        achieved = ilt_bytes / (stage_ms["illt_apply"] * 1e-3) / 1e9
+        roof = {"kernel": "k_trisolve", "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                "peak_kind": pk_kind, "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                "traffic": traffic.get(("k_trisolve", args.workload)),
+                "note": "level-scheduled sweeps: latency bound (one dependency level per step), not bandwidth bound"}
+    roof["algorithmic_per_launch"] = {"spmv_bytes": spmv_bytes,
+                                      "pair_assembly_flops": pairs * PAIR_FLOPS[w["element"]]}
+
+    # -------- end to end through the C ABI from host buffers
+    e2e_s = []
+    import numpy as np
+    h2d = mesh.nodes.nbytes + mesh.n_elements * mesh.nodes_per_element * 8 + sum(
+        mesh.boundaries[g].size * 8 for g, _, _ in w["bcs"])
+    d2h = n * 8
+    for k in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        pe = make_problem(w, T, mesh)
+        pe.find_neighbours()
+        te, _ = pe.stationary(tolerance=tol, max_iterations=100000)
+        e2e_s.append(time.perf_counter() - t0)
+        pe.close()
+    e2e = max_over_ranks(dist, sum(e2e_s) / len(e2e_s))
+
+    # -------- CPU baseline (rank 0, N=1): the CPU restatement on the host cores
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle
+        oracle.build.build()
+        oracle.set_threads(os.cpu_count() or 1)
+        t_cpu, det = cpu_solve(w, mesh)
+        err = float(np.linalg.norm(temp - det["solution"]) / np.linalg.norm(det["solution"]))
+        cpu = {"value": t_cpu, "unit": "s", "cores": det["threads"], "kind": "port",
+               "sample": "one full solve of the same workload (neighbours, assembly, local assembly, ILLT, CG to "
+                         "1e-10) by the CPU restatement of the reference (oracle/), all host threads",
+               "iterations": det["iterations"], "true_residual": det["true_residual"],
+               "gpu_vs_cpu_temperature_rel_l2": err}
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": seconds, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mean_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": w["name"], "mesh": f"{w['nx']}x{w['ny']} {w['element']}",
+                   "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",
+                   "parallelism": f"replicas x{world}"},
+        "throughput": {"element_pairs_per_s": pairs / seconds,
+                       "pair_quadrature_contributions_per_s": pairs * PAIR_QUAD[w["element"]] / seconds,
+                       "cg_iterations_per_s": iters / seconds},
+        "solve": {"element_pairs": pairs, "nnz_inner_upper": rep.nnz_inner, "nnz_solver_full_padded": nnz_solver,
+                  "cg_iterations": iters, "residual": rep.residual, "reference_residual": rep.reference_residual,
+                  "phases_s": {k: getattr(rep, "seconds_" + k) for k in
+                               ["neighbours", "pattern", "assembly", "boundary", "preconditioner", "solve"]},
+                  "stage_ms": stage_ms, "per_solve_ms": per_solve_ms},
+        "clocks": clocks,
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def factor_offdiag_entries(lib, h, n: int) -> int:
+    """Off-diagonal entries read by both triangular sweeps: the factor has the
+    pattern of the upper local matrix, each sweep reads it once."""
+    import numpy as np
+    from nonlocal_gb300 import _lib as L
+    rp = np.empty(n + 1, dtype=np.int64)
+    L.check(lib.nlgpu_get_matrix(h, L.MATRIX_LOCAL, L.ptr(rp), None, None))
+    return int(2 * (rp[-1] - n))
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["nlgpu", "reference"], default="nlgpu")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    w = WORKLOADS[args.workload]
+    mesh = structured_quad_mesh(w["nx"], w["ny"], w["element"], jitter=w["jitter"], seed=0)
+    world, rank, local, dist = dist_setup()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, w, mesh, world, rank, dist)
+        return run_gpu(args, w, mesh, world, rank, local, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

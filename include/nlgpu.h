@@ -221,6 +221,17 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
                         double local_weight, int influence, double conductivity, double t_left,
                         double q_right, int sin_source, double* temperature);
 
+/* ---- measurement utilities (no counterpart in the reference) ---------------
+ * Events recorded on the context's stream (slots 0..63) and the device time
+ * between two of them; an L2 flush (writes `bytes` of scratch memory); and the
+ * average device time of one kernel stage over `reps` launches on the current
+ * problem: 0 SpMV of the solver matrix, 1 pair assembly (FULL part),
+ * 2 ILLT application (both triangular sweeps), 3 neighbour search. */
+int nlgpu_event_record(nlgpu_ctx* ctx, int slot);
+int nlgpu_event_elapsed(nlgpu_ctx* ctx, int start_slot, int stop_slot, double* milliseconds);
+int nlgpu_flush_l2(nlgpu_ctx* ctx, int64_t bytes);
+int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* milliseconds);
+
 #ifdef __cplusplus
 }
 #endif

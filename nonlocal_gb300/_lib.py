@@ -89,6 +89,10 @@ SIGNATURES = {
     "nlgpu_nonstationary_2d_compute": (c_int, [c_p, c_d, c_p]),
     "nlgpu_nonstationary_2d_step": (c_int, [c_p, c_d, c_p, c_d, c_i64, c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),
+    "nlgpu_event_record": (c_int, [c_p, c_int]),
+    "nlgpu_event_elapsed": (c_int, [c_p, c_int, c_int, ctypes.POINTER(c_d)]),
+    "nlgpu_flush_l2": (c_int, [c_p, c_i64]),
+    "nlgpu_time_stage": (c_int, [c_p, c_int, c_int, ctypes.POINTER(c_d)]),
 }
 
 _lib = None

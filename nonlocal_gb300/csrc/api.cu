@@ -595,6 +595,70 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
     });
 }
 
+int nlgpu_event_record(nlgpu_ctx* ctx, int slot) {
+    if (!ctx || slot < 0 || slot >= 64) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        if (!c.events[slot]) NL_CUDA(cudaEventCreate(&c.events[slot]));
+        NL_CUDA(cudaEventRecord(c.events[slot], c.stream));
+    });
+}
+
+int nlgpu_event_elapsed(nlgpu_ctx* ctx, int a, int b, double* ms) {
+    if (!ctx || !ms || a < 0 || b < 0 || a >= 64 || b >= 64) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.events[a] && c.events[b], NLGPU_ERR_STATE, "event slot not recorded");
+        NL_CUDA(cudaEventSynchronize(c.events[b]));
+        float f = 0.0f;
+        NL_CUDA(cudaEventElapsedTime(&f, c.events[a], c.events[b]));
+        *ms = double(f);
+    });
+}
+
+int nlgpu_flush_l2(nlgpu_ctx* ctx, int64_t bytes) {
+    if (!ctx || bytes <= 0) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        c.flush.reserve(size_t(bytes));
+        NL_CUDA(cudaMemsetAsync(c.flush.p, int(c.flush_value++ & 0xff), size_t(bytes), c.stream));
+    });
+}
+
+int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
+    if (!ctx || !ms || reps <= 0) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        cudaEvent_t e0, e1;
+        NL_CUDA(cudaEventCreate(&e0));
+        NL_CUDA(cudaEventCreate(&e1));
+        dbuf<double> x, y;
+        if (stage == 0 || stage == 2) {
+            NL_REQUIRE(c.full.nnz > 0, NLGPU_ERR_STATE, "assemble the system first");
+            x.resize(size_t(c.n_nodes)); y.resize(size_t(c.n_nodes));
+            NL_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), c.stream));
+            if (stage == 2) NL_REQUIRE(c.ilt.ok, NLGPU_ERR_STATE, "no ILLT factor");
+        }
+        if (stage == 1) NL_REQUIRE(c.inner.nnz > 0 && c.model.nonlocal(), NLGPU_ERR_STATE, "no nonlocal pattern");
+        if (stage == 3) NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "no mesh/model");
+        NL_CUDA(cudaEventRecord(e0, c.stream));
+        for (int k = 0; k < reps; ++k) {
+            if (stage == 0) spmv_full(c, c.full, x.p, y.p);
+            else if (stage == 1) assemble_full(c);
+            else if (stage == 2) ilt_apply(c, c.ilt, x.p, y.p);
+            else if (stage == 3) find_neighbours(c, c.strategy);
+            else throw nlgpu::error{NLGPU_ERR_ARG, "unknown stage"};
+        }
+        NL_CUDA(cudaEventRecord(e1, c.stream));
+        NL_CUDA(cudaEventSynchronize(e1));
+        float f = 0.0f;
+        NL_CUDA(cudaEventElapsedTime(&f, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *ms = double(f) / reps;
+    });
+}
+
 }  // extern "C"
 
 namespace nlgpu {

@@ -228,6 +228,11 @@ struct Ctx {
     double time_step = 0.0;
     dbuf<double> temperature;
     bool nonstationary_ready = false;
+    // measurement
+    cudaEvent_t events[64] = {};
+    dbuf<unsigned char> flush;
+    unsigned flush_value = 0;
+    ~Ctx() { for (cudaEvent_t& e : events) if (e) cudaEventDestroy(e); }
     // scratch
     dbuf<unsigned char> scratch;
     dbuf<i64> i64_scratch_a, i64_scratch_b;
