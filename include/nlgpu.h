@@ -227,6 +227,11 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
  * average device time of one kernel stage over `reps` launches on the current
  * problem: 0 SpMV of the solver matrix, 1 pair assembly (FULL part),
  * 2 ILLT application (both triangular sweeps), 3 neighbour search. */
+/* Options of a context: NLGPU_OPTION_GLOBAL_SWEEPS = 1 makes the ILLT
+ * triangular sweeps read and write their values in global memory instead of
+ * the TMA-fed shared-memory ring (same arithmetic; for comparison). */
+enum { NLGPU_OPTION_GLOBAL_SWEEPS = 0 };
+int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value);
 int nlgpu_event_record(nlgpu_ctx* ctx, int slot);
 int nlgpu_event_elapsed(nlgpu_ctx* ctx, int start_slot, int stop_slot, double* milliseconds);
 int nlgpu_flush_l2(nlgpu_ctx* ctx, int64_t bytes);

@@ -89,6 +89,7 @@ SIGNATURES = {
     "nlgpu_nonstationary_2d_compute": (c_int, [c_p, c_d, c_p]),
     "nlgpu_nonstationary_2d_step": (c_int, [c_p, c_d, c_p, c_d, c_i64, c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),
+    "nlgpu_set_option": (c_int, [c_p, c_int, c_int]),
     "nlgpu_event_record": (c_int, [c_p, c_int]),
     "nlgpu_event_elapsed": (c_int, [c_p, c_int, c_int, ctypes.POINTER(c_d)]),
     "nlgpu_flush_l2": (c_int, [c_p, c_i64]),

@@ -122,6 +122,12 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     c.temperature.resize(size_t(c.n_nodes));
     const CgResult r = cg_solve(c, c.full, M, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations, false);
     if (rep) rep->seconds_solve = seconds(t0);
+    if (M && c.sweep_error.n) {
+        int err = 0;
+        NL_CUDA(cudaMemcpyAsync(&err, c.sweep_error.p, sizeof err, cudaMemcpyDeviceToHost, c.stream));
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        NL_REQUIRE(err == 0, NLGPU_ERR_TIMEOUT, "a triangular sweep stage wait gave up");
+    }
     fill_report(c, rep, r);
     return r;
 }
@@ -593,6 +599,12 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
         stationary_1d(*ctx, elements, order, length, radius, local_weight, influence, conductivity, t_left, q_right,
                       sin_source != 0, temperature);
     });
+}
+
+int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    if (option == NLGPU_OPTION_GLOBAL_SWEEPS) { ctx->force_global_sweeps = value != 0; return NLGPU_OK; }
+    return NLGPU_ERR_ARG;
 }
 
 int nlgpu_event_record(nlgpu_ctx* ctx, int slot) {

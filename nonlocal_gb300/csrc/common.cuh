@@ -150,8 +150,29 @@ struct TriSlab {
     dbuf<float> val32, inv_diag32;
 };
 
+// Triangular sweep fed by TMA bulk copies with a shared-memory ring (sweep.cu).
+struct SweepPlan {
+    bool ok = false;
+    i64 n_levels = 0, P = 0;     // levels, padded positions
+    int stage_bytes = 0;
+    size_t smem_bytes = 0;
+    dbuf<int32_t> cnt, cntp, width;
+    dbuf<i64> ppos, block_off;
+    dbuf<unsigned char> blocks;  // per level: values, inverse diagonal, ring slots
+    dbuf<int32_t> row_of;        // padded position -> row (-1 padding)
+    dbuf<int32_t> ppos_of_row;
+    dbuf<i64> val_dst, val_src, inv_dst, inv_src;   // factor value -> block byte offset
+    dbuf<double> in, out;        // right-hand side / solution in padded level order
+};
+
+// CG reduction layout shared by the solver kernels
+constexpr int RED_BLOCKS = 152 * 4;   // blocks of every reducing kernel (one partial each)
+enum { S_BB = 0, S_RZ0 = 1, S_DONE = 2, S_ITERS = 3, S_RR_FINAL = 4 };   // scalar slots
+enum { P_PQ = 0, P_RR = 1, P_RZ_A = 2, P_RZ_B = 3, P_BB = 4, P_COUNT = 5 };   // partial buffers
+
 // ILLT preconditioner: IC(0) of S A S + alpha I on the pattern of A's upper part.
 struct IncompleteCholesky {
+    SweepPlan fwd_plan, bwd_plan;
     i64 n = 0, nnz = 0;
     dbuf<i64> rp;                // upper pattern (diagonal first)
     dbuf<int32_t> col;
@@ -228,6 +249,8 @@ struct Ctx {
     double time_step = 0.0;
     dbuf<double> temperature;
     bool nonstationary_ready = false;
+    dbuf<int> sweep_error;
+    bool force_global_sweeps = false;   // use the global-memory sweeps (for comparison)
     // measurement
     cudaEvent_t events[64] = {};
     dbuf<unsigned char> flush;
@@ -269,6 +292,13 @@ void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* 
 struct CgResult { i64 iterations = 0; double residual = 0, reference_residual = 0; bool converged = false; };
 CgResult cg_solve(Ctx& ctx, const Csr& A_full, const IncompleteCholesky* M, const double* b, double* x,
                   double tolerance, i64 max_iterations, bool x_is_initial_guess);
+// sweep.cu
+bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vector<int32_t>& rows,
+                      const std::vector<i64>& rp, const std::vector<int32_t>& col, const std::vector<i64>& val_index,
+                      const std::vector<i64>& diag_pos, SweepPlan& plan);
+void sweep_plan_fill(Ctx& ctx, SweepPlan& plan, const double* u);
+void sweep_apply(Ctx& ctx, IncompleteCholesky& ic, const double* r, double* z, const double* partials,
+                 const double* flags, double tol2);
 // onedim.cu
 void stationary_1d(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight, int influence,
                    double conductivity, double t_left, double q_right, bool sin_source, double* temperature);

@@ -34,15 +34,9 @@ namespace nlgpu {
 
 namespace {
 
-constexpr int RED_BLOCKS = 152 * 4;   // blocks of every reducing kernel
 constexpr int RED_THREADS = 256;
 constexpr int GRAPH_ITERS = 16;
 constexpr int TRI_THREADS = 1024;
-
-// scalar slots
-enum { S_BB = 0, S_RZ0 = 1, S_DONE = 2, S_ITERS = 3, S_RR_FINAL = 4 };
-// partial buffers, RED_BLOCKS each
-enum { P_PQ = 0, P_RR = 1, P_RZ_A = 2, P_RZ_B = 3, P_BB = 4, P_COUNT = 5 };
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
     v = warp_sum(v);
@@ -405,6 +399,10 @@ void finalize_scalar(Ctx& ctx, const double* partials, double* dst) {
 void precondition(Ctx& ctx, const IncompleteCholesky* M, const double* r, double* z, const double* partials,
                   const double* flags, double tol2) {
     const i64 n = ctx.cg.n;
+    if (M && M->fwd_plan.ok && M->bwd_plan.ok && !ctx.force_global_sweeps) {
+        sweep_apply(ctx, const_cast<IncompleteCholesky&>(*M), r, z, partials, flags, tol2);
+        return;
+    }
     if (!M) {
         if (flags) NL_LAUNCH(k_copy_if_running, RED_BLOCKS, RED_THREADS, 0, ctx.stream, n, r, z, partials, flags, tol2);
         else NL_LAUNCH(k_copy, grid_for(n, 256), 256, 0, ctx.stream, n, r, z);
@@ -457,10 +455,17 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     std::vector<i64> ident(static_cast<size_t>(nnz)), u_diag(static_cast<size_t>(n)), l_diag(static_cast<size_t>(n));
     std::iota(ident.begin(), ident.end(), i64(0));
     for (i64 r = 0; r < n; ++r) { u_diag[size_t(r)] = rp[size_t(r)]; l_diag[size_t(r)] = lrp[size_t(r) + 1] - 1; }
-    std::vector<i64> ic_lev_ptr;
-    std::vector<int32_t> ic_rows;
+    std::vector<i64> ic_lev_ptr, bwd_lev_ptr;
+    std::vector<int32_t> ic_rows, bwd_rows;
     build_slab(ctx, lrp, lcol, l_to_u, l_diag, true, ic.fwd, &ic_lev_ptr, &ic_rows);
-    build_slab(ctx, rp, col, ident, u_diag, false, ic.bwd, nullptr, nullptr);
+    build_slab(ctx, rp, col, ident, u_diag, false, ic.bwd, &bwd_lev_ptr, &bwd_rows);
+    // TMA-fed shared-memory sweeps when every dependency fits the ring
+    ctx.sweep_error.resize(1);
+    ctx.sweep_error.zero(ctx.stream);
+    ic.fwd_plan = SweepPlan{};
+    ic.bwd_plan = SweepPlan{};
+    if (sweep_plan_build(ctx, ic_lev_ptr, ic_rows, lrp, lcol, l_to_u, l_diag, ic.fwd_plan))
+        sweep_plan_build(ctx, bwd_lev_ptr, bwd_rows, rp, col, ident, u_diag, ic.bwd_plan);
     ic.ic_levels = i64(ic_lev_ptr.size()) - 1;
     ic.ic_lev_ptr.upload(ic_lev_ptr.data(), ic_lev_ptr.size(), ctx.stream);
     ic.ic_rows.upload(ic_rows.data(), ic_rows.size(), ctx.stream);
@@ -506,6 +511,10 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     }
     ic.shift = shift;
     if (!ic.ok) return;
+    if (ic.fwd_plan.ok && ic.bwd_plan.ok) {
+        sweep_plan_fill(ctx, ic.fwd_plan, ic.u.p);
+        sweep_plan_fill(ctx, ic.bwd_plan, ic.u.p);
+    }
     for (TriSlab* s : {&ic.fwd, &ic.bwd}) {
         if (s->entries)
             NL_LAUNCH(k_slab_values, grid_for(s->entries, 256), 256, 0, ctx.stream, s->entries, s->src.p, ic.u.p,

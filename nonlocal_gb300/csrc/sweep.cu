@@ -1,0 +1,326 @@
+// Level-scheduled triangular sweep fed by TMA bulk copies, with the solved
+// values kept in a shared-memory ring.
+//
+// A sweep solves y[row] = (in[row] - sum_k L[row][k] y[k]) / L[row][row] level
+// by level (rows of one level depend only on earlier levels).  Everything the
+// sweep reads is laid out per level, contiguously, in level order:
+//   * a "level block": off-diagonal values [w][cntp], inverse diagonal [cntp]
+//     and dependency slots [w][cntp] (int16), padded to 16 bytes;
+//   * the right-hand side, pre-gathered into level order (padded positions).
+// One CTA walks the levels.  Thread 0 keeps STAGES levels in flight with
+// cp.async.bulk (one copy per block, one per right-hand-side chunk) completing
+// on an mbarrier per stage; the other threads wait on the stage's barrier
+// (bounded spin), solve their row and put the value into a ring of RING
+// doubles in shared memory at (padded position mod RING).  The dependency slot
+// of an entry is that ring index, valid because every dependency lies fewer
+// than RING positions back (checked when the plan is built; otherwise the
+// global-memory sweep of solver.cu is used).  Results also stream to global
+// memory in level order; small gather/scatter kernels convert between level
+// order and node order before and after the sweeps.
+#include "common.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace nlgpu {
+
+namespace {
+
+constexpr int SW_THREADS = 256;
+constexpr int SW_STAGES = 6;
+constexpr int SW_RING = 4096;
+constexpr int SW_ZERO = SW_RING;          // ring slot holding 0 (padding)
+constexpr unsigned long long SW_WAIT_LIMIT_NS = 2000000000ull;   // a stage wait gives up after 2 s
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+template<class T>
+struct SweepArgs {
+    i64 n_levels;
+    const i64* block_off;     // [L] byte offset of the level block
+    const int32_t* cnt;       // [L] rows
+    const int32_t* cntp;      // [L] padded rows (multiple of 8)
+    const int32_t* width;     // [L]
+    const i64* ppos;          // [L + 1] padded position of the level's first row
+    const unsigned char* blocks;
+    const T* in;              // right-hand side in padded level order
+    T* out;                   // solution in padded level order
+    int stage_bytes;          // bytes of one stage (block + rhs chunk)
+    int* error;
+    const double* partials;   // optional CG state: skip after convergence
+    const double* flags;
+    double tol2;
+};
+
+template<class T>
+__global__ void __launch_bounds__(SW_THREADS) k_sweep_tma(SweepArgs<T> a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    T* ring = reinterpret_cast<T*>(smem);
+    unsigned char* stage_base = smem + ((sizeof(T) * (SW_RING + 1) + 127) / 128) * 128;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(stage_base + size_t(a.stage_bytes) * SW_STAGES);
+    __shared__ double sh[40];
+    __shared__ int skip;
+    if (a.flags) {
+        // converged CG state: every thread takes the same early return
+        double v = 0.0;
+        for (int k = threadIdx.x; k < RED_BLOCKS; k += blockDim.x) v += a.partials[P_RR * RED_BLOCKS + k];
+        v = warp_sum(v);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double rr = 0.0;
+            for (int w = 0; w < int(blockDim.x >> 5); ++w) rr += sh[w];
+            skip = (a.flags[S_DONE] != 0.0) || (rr <= a.tol2 * a.flags[S_BB]);
+        }
+        __syncthreads();
+        if (skip) return;
+    }
+    for (int k = threadIdx.x; k <= SW_RING; k += blockDim.x) ring[k] = T(0);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < SW_STAGES; ++s) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](i64 l) {
+        const int s = int(l % SW_STAGES);
+        unsigned char* dst = stage_base + size_t(s) * a.stage_bytes;
+        const int cp = a.cntp[l], w = a.width[l];
+        const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 2) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
+        const uint32_t rhs_bytes = uint32_t(size_t(cp) * sizeof(T));
+        mbar_expect_tx(&bars[s], block_bytes + rhs_bytes);
+        bulk_g2s(dst, a.blocks + a.block_off[l], block_bytes, &bars[s]);
+        bulk_g2s(dst + block_bytes, a.in + a.ppos[l], rhs_bytes, &bars[s]);
+    };
+    if (threadIdx.x == 0)
+        for (i64 l = 0; l < a.n_levels && l < SW_STAGES; ++l) issue(l);
+    for (i64 l = 0; l < a.n_levels; ++l) {
+        const int s = int(l % SW_STAGES);
+        const uint32_t parity = uint32_t((l / SW_STAGES) & 1);
+        if (!mbar_try_wait(&bars[s], parity)) {
+            const unsigned long long t0 = globaltimer_ns();
+            while (!mbar_try_wait(&bars[s], parity)) {
+                if (globaltimer_ns() - t0 > SW_WAIT_LIMIT_NS) { atomicExch(a.error, 1); return; }
+            }
+        }
+        const int c = a.cnt[l], cp = a.cntp[l], w = a.width[l];
+        const unsigned char* blk = stage_base + size_t(s) * a.stage_bytes;
+        const T* vals = reinterpret_cast<const T*>(blk);
+        const T* inv = vals + size_t(w) * cp;
+        const int16_t* dep = reinterpret_cast<const int16_t*>(inv + cp);
+        const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 2) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
+        const T* rhs = reinterpret_cast<const T*>(blk + block_bytes);
+        const i64 p0 = a.ppos[l];
+        for (int t = threadIdx.x; t < c; t += blockDim.x) {
+            T acc = rhs[t];
+            for (int k = 0; k < w; ++k) acc -= vals[k * cp + t] * ring[dep[k * cp + t]];
+            const T v = acc * inv[t];
+            ring[(p0 + t) & (SW_RING - 1)] = v;
+            a.out[p0 + t] = v;
+        }
+        __syncthreads();   // stage s is consumed and the level's ring values are visible
+        if (threadIdx.x == 0 && l + SW_STAGES < a.n_levels) issue(l + SW_STAGES);
+    }
+}
+
+// level order <-> node order
+template<class T>
+__global__ void k_gather_scaled(i64 P, const int32_t* __restrict__ row_of, const double* __restrict__ scale,
+                                const double* __restrict__ r, T* __restrict__ out, const double* __restrict__ partials,
+                                const double* __restrict__ flags, double tol2) {
+    for (i64 p = blockIdx.x * i64(blockDim.x) + threadIdx.x; p < P; p += i64(gridDim.x) * blockDim.x) {
+        const int32_t row = row_of[p];
+        out[p] = row >= 0 ? T(scale[row] * r[row]) : T(0);
+    }
+    (void)partials; (void)flags; (void)tol2;
+}
+
+template<class T>
+__global__ void k_transfer(i64 P, const int32_t* __restrict__ row_of_b, const int32_t* __restrict__ ppos_of_row_f,
+                           const T* __restrict__ in_f, T* __restrict__ out_b) {
+    for (i64 p = blockIdx.x * i64(blockDim.x) + threadIdx.x; p < P; p += i64(gridDim.x) * blockDim.x) {
+        const int32_t row = row_of_b[p];
+        out_b[p] = row >= 0 ? in_f[ppos_of_row_f[row]] : T(0);
+    }
+}
+
+template<class T>
+__global__ void k_scatter_scaled(i64 P, const int32_t* __restrict__ row_of, const double* __restrict__ scale,
+                                 const T* __restrict__ in, double* __restrict__ z) {
+    for (i64 p = blockIdx.x * i64(blockDim.x) + threadIdx.x; p < P; p += i64(gridDim.x) * blockDim.x) {
+        const int32_t row = row_of[p];
+        if (row >= 0) z[row] = scale[row] * double(in[p]);
+    }
+}
+
+__global__ void k_fill_blocks_f64(i64 count, const i64* __restrict__ dst_off, const i64* __restrict__ src,
+                                  const double* __restrict__ u, bool invert, unsigned char* __restrict__ blocks) {
+    for (i64 k = blockIdx.x * i64(blockDim.x) + threadIdx.x; k < count; k += i64(gridDim.x) * blockDim.x) {
+        double v = src[k] >= 0 ? u[src[k]] : 0.0;
+        if (invert) v = src[k] >= 0 ? 1.0 / v : 0.0;
+        *reinterpret_cast<double*>(blocks + dst_off[k]) = v;
+    }
+}
+
+}  // namespace
+
+// Host construction of a sweep plan from the level structure of a triangular
+// matrix (rows by level, entries with their factor value indices).
+bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vector<int32_t>& rows,
+                      const std::vector<i64>& rp, const std::vector<int32_t>& col, const std::vector<i64>& val_index,
+                      const std::vector<i64>& diag_pos, SweepPlan& plan) {
+    const i64 L = i64(lev_ptr.size()) - 1;
+    const i64 n = i64(rows.size());
+    std::vector<int32_t> cnt(static_cast<size_t>(L)), cntp(static_cast<size_t>(L)), width(static_cast<size_t>(L));
+    std::vector<i64> ppos(static_cast<size_t>(L + 1), 0), block_off(static_cast<size_t>(L));
+    std::vector<int32_t> ppos_of_row(static_cast<size_t>(n));
+    i64 bytes = 0;
+    int max_stage = 0;
+    for (i64 l = 0; l < L; ++l) {
+        const int c = int(lev_ptr[size_t(l) + 1] - lev_ptr[size_t(l)]);
+        int w = 0;
+        for (i64 t = lev_ptr[size_t(l)]; t < lev_ptr[size_t(l) + 1]; ++t) {
+            const int32_t r = rows[size_t(t)];
+            w = std::max(w, int(rp[size_t(r) + 1] - rp[size_t(r)] - 1));
+        }
+        cnt[size_t(l)] = c;
+        cntp[size_t(l)] = (c + 7) / 8 * 8;
+        width[size_t(l)] = w;
+        ppos[size_t(l) + 1] = ppos[size_t(l)] + cntp[size_t(l)];
+        for (int t = 0; t < c; ++t) ppos_of_row[size_t(rows[size_t(lev_ptr[size_t(l)] + t)])] = int32_t(ppos[size_t(l)] + t);
+        const i64 blk = (i64(w) * cntp[size_t(l)] * (8 + 2) + i64(cntp[size_t(l)]) * 8 + 15) / 16 * 16;
+        block_off[size_t(l)] = bytes;
+        bytes += blk;
+        max_stage = std::max<int>(max_stage, int(blk + i64(cntp[size_t(l)]) * 8));
+    }
+    const i64 P = ppos[size_t(L)];
+    // dependency distances must fit the ring, stages must fit shared memory
+    std::vector<int16_t> dep_all;
+    std::vector<i64> val_dst, val_src, inv_dst, inv_src;
+    std::vector<unsigned char> dep_bytes(static_cast<size_t>(bytes), 0);
+    i64 max_dist = 0;
+    for (i64 l = 0; l < L; ++l) {
+        const int c = cnt[size_t(l)], cp = cntp[size_t(l)], w = width[size_t(l)];
+        const i64 vbase = block_off[size_t(l)];
+        const i64 ibase = vbase + i64(w) * cp * 8;
+        const i64 dbase = ibase + i64(cp) * 8;
+        for (int t = 0; t < cp; ++t) {
+            const bool real = t < c;
+            const int32_t r = real ? rows[size_t(lev_ptr[size_t(l)] + t)] : -1;
+            inv_dst.push_back(ibase + i64(t) * 8);
+            inv_src.push_back(real ? val_index[size_t(diag_pos[size_t(r)])] : -1);
+            int k = 0;
+            if (real)
+                for (i64 s = rp[size_t(r)]; s < rp[size_t(r) + 1]; ++s) {
+                    if (s == diag_pos[size_t(r)]) continue;
+                    const i64 dp = ppos_of_row[size_t(col[size_t(s)])];
+                    max_dist = std::max(max_dist, ppos[size_t(l) + 1] - dp);
+                    const int16_t slot = int16_t(dp & (SW_RING - 1));
+                    std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 2)], &slot, 2);
+                    val_dst.push_back(vbase + (i64(k) * cp + t) * 8);
+                    val_src.push_back(val_index[size_t(s)]);
+                    ++k;
+                }
+            for (; k < w; ++k) {
+                const int16_t slot = int16_t(SW_ZERO);
+                std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 2)], &slot, 2);
+                val_dst.push_back(vbase + (i64(k) * cp + t) * 8);
+                val_src.push_back(-1);
+            }
+        }
+    }
+    const size_t smem = ((sizeof(double) * (SW_RING + 1) + 127) / 128) * 128 + size_t(max_stage) * SW_STAGES +
+                        SW_STAGES * sizeof(uint64_t);
+    plan.ok = max_dist <= SW_RING && smem <= 220 * 1024 && n < (i64(1) << 31);
+    if (!plan.ok) return false;
+    std::vector<int32_t> row_of(static_cast<size_t>(P), -1);
+    for (i64 l = 0; l < L; ++l)
+        for (int t = 0; t < cnt[size_t(l)]; ++t) row_of[size_t(ppos[size_t(l)] + t)] = rows[size_t(lev_ptr[size_t(l)] + t)];
+    plan.n_levels = L;
+    plan.P = P;
+    plan.stage_bytes = max_stage;
+    plan.smem_bytes = smem;
+    plan.cnt.upload(cnt.data(), cnt.size(), ctx.stream);
+    plan.cntp.upload(cntp.data(), cntp.size(), ctx.stream);
+    plan.width.upload(width.data(), width.size(), ctx.stream);
+    plan.ppos.upload(ppos.data(), ppos.size(), ctx.stream);
+    plan.block_off.upload(block_off.data(), block_off.size(), ctx.stream);
+    plan.blocks.upload(dep_bytes.data(), dep_bytes.size(), ctx.stream);   // dependency slots; values filled later
+    plan.row_of.upload(row_of.data(), row_of.size(), ctx.stream);
+    plan.ppos_of_row.upload(ppos_of_row.data(), ppos_of_row.size(), ctx.stream);
+    plan.val_dst.upload(val_dst.data(), val_dst.size(), ctx.stream);
+    plan.val_src.upload(val_src.data(), val_src.size(), ctx.stream);
+    plan.inv_dst.upload(inv_dst.data(), inv_dst.size(), ctx.stream);
+    plan.inv_src.upload(inv_src.data(), inv_src.size(), ctx.stream);
+    plan.in.resize(size_t(P)); plan.out.resize(size_t(P));
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+    return true;
+}
+
+void sweep_plan_fill(Ctx& ctx, SweepPlan& plan, const double* u) {
+    const i64 nv = i64(plan.val_src.n), ni = i64(plan.inv_src.n);
+    if (nv) NL_LAUNCH(k_fill_blocks_f64, grid_for(nv, 256), 256, 0, ctx.stream, nv, plan.val_dst.p, plan.val_src.p, u, false,
+                      plan.blocks.p);
+    NL_LAUNCH(k_fill_blocks_f64, grid_for(ni, 256), 256, 0, ctx.stream, ni, plan.inv_dst.p, plan.inv_src.p, u, true,
+              plan.blocks.p);
+}
+
+static void run_sweep(Ctx& ctx, SweepPlan& plan, const double* partials, const double* flags, double tol2) {
+    SweepArgs<double> a{};
+    a.n_levels = plan.n_levels; a.block_off = plan.block_off.p; a.cnt = plan.cnt.p; a.cntp = plan.cntp.p;
+    a.width = plan.width.p; a.ppos = plan.ppos.p; a.blocks = plan.blocks.p; a.in = plan.in.p; a.out = plan.out.p;
+    a.stage_bytes = plan.stage_bytes; a.partials = partials; a.flags = flags; a.tol2 = tol2;
+    ctx.sweep_error.reserve(1);
+    a.error = ctx.sweep_error.p;
+    static bool attr_set = false;
+    if (!attr_set) {
+        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        attr_set = true;
+    }
+    NL_LAUNCH(k_sweep_tma<double>, 1, SW_THREADS, plan.smem_bytes, ctx.stream, a);
+}
+
+// z = S U^-1 U^-T S r with the TMA sweeps (forward plan on U^T, backward on U)
+void sweep_apply(Ctx& ctx, IncompleteCholesky& ic, const double* r, double* z, const double* partials,
+                 const double* flags, double tol2) {
+    SweepPlan& F = ic.fwd_plan;
+    SweepPlan& B = ic.bwd_plan;
+    NL_LAUNCH(k_gather_scaled<double>, grid_for(F.P, 256), 256, 0, ctx.stream, F.P, F.row_of.p, ic.scale.p, r, F.in.p,
+              partials, flags, tol2);
+    run_sweep(ctx, F, partials, flags, tol2);
+    NL_LAUNCH(k_transfer<double>, grid_for(B.P, 256), 256, 0, ctx.stream, B.P, B.row_of.p, F.ppos_of_row.p, F.out.p, B.in.p);
+    run_sweep(ctx, B, partials, flags, tol2);
+    NL_LAUNCH(k_scatter_scaled<double>, grid_for(B.P, 256), 256, 0, ctx.stream, B.P, B.row_of.p, ic.scale.p, B.out.p, z);
+}
+
+}  // namespace nlgpu
