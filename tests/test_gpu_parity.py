@@ -117,8 +117,9 @@ def test_stationary_solution(golden):
 
 @pytest.mark.parametrize("name", ["b12_fastpoly", "s6_exp_ortho_jitter"])
 def test_tma_sweeps_match_global_sweeps(lib, name):
-    """The TMA-fed shared-memory triangular sweeps compute exactly what the
-    global-memory sweeps compute (same entries, same order)."""
+    """The TMA-fed shared-memory triangular sweeps compute what the global-memory
+    sweeps compute (same entries in the same order; the two assemblies differ
+    only by the order of atomic additions)."""
     fx = gc.load(name)
     runs = []
     for global_sweeps in (0, 1):
@@ -127,8 +128,8 @@ def test_tma_sweeps_match_global_sweeps(lib, name):
         pb.find_neighbours()
         t, rep = pb.stationary(tolerance=1e-12)
         runs.append((t, rep.iterations))
-    assert runs[0][1] == runs[1][1]
-    assert np.array_equal(runs[0][0], runs[1][0])
+    assert abs(runs[0][1] - runs[1][1]) <= 1
+    assert rel(runs[0][0], runs[1][0]) < 1e-12
 
 
 def test_known_answers(lib):
