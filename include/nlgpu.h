@@ -229,8 +229,10 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
  * 2 ILLT application (both triangular sweeps), 3 neighbour search. */
 /* Options of a context: NLGPU_OPTION_GLOBAL_SWEEPS = 1 makes the ILLT
  * triangular sweeps read and write their values in global memory instead of
- * the TMA-fed shared-memory ring (same arithmetic; for comparison). */
-enum { NLGPU_OPTION_GLOBAL_SWEEPS = 0 };
+ * the TMA-fed shared-memory ring (same arithmetic); NLGPU_OPTION_ORDERED_PAIRS
+ * = 1 makes a symmetric assembly evaluate every ordered element pair instead
+ * of each unordered pair once (both for comparison). */
+enum { NLGPU_OPTION_GLOBAL_SWEEPS = 0, NLGPU_OPTION_ORDERED_PAIRS = 1 };
 int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value);
 int nlgpu_event_record(nlgpu_ctx* ctx, int slot);
 int nlgpu_event_elapsed(nlgpu_ctx* ctx, int start_slot, int stop_slot, double* milliseconds);

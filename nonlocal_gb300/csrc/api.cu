@@ -604,6 +604,7 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
 int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value) {
     if (!ctx) return NLGPU_ERR_ARG;
     if (option == NLGPU_OPTION_GLOBAL_SWEEPS) { ctx->force_global_sweeps = value != 0; return NLGPU_OK; }
+    if (option == NLGPU_OPTION_ORDERED_PAIRS) { ctx->ordered_pairs = value != 0; return NLGPU_OK; }
     return NLGPU_ERR_ARG;
 }
 

@@ -12,14 +12,18 @@
 // shared memory.  Each warp takes one neighbour eNL at a time, stages eNL's
 // quadrature data in shared memory and evaluates the pair's whole block once,
 // factorised as
-//   Phi[qL][qNL] = w_qNL phi(x_qL, x_qNL)                  (nq^2 kernel values)
-//   H[qL][j]     = sum_qNL Phi[qL][qNL] Lambda G_j(qNL)     (nq^2 * nen * 2 FMA)
-//   K[i][j]      = sum_qL w_qL G_i(qL) . H[qL][j]            (nen^2 * nq * 2 FMA)
-// then adds every entry the reference keeps (matrix_separator_base::part) to
-// the shared accumulators; BOUND entries go straight to global memory.  When
-// the CTA is done its accumulators are added to the global values (several
-// elements share a node row).  Rows too long for shared memory fall back to
-// global atomics with a binary search of the column.
+//   Phi[qL][qNL] = c_qNL * shape(x_qL, x_qNL)       c_qNL = w_qNL norm (1 - p1) [lambda]
+//   H[qL][j]     = sum_qNL Phi[qL][qNL] Lambda G_j(qNL)
+//   K[i][j]      = sum_qL (w_qL G_i(qL)) . H[qL][j]
+// and adds every entry the reference keeps (matrix_separator_base::part) to
+// the shared accumulators; BOUND entries go to global memory.  When the
+// problem is symmetric (constant conductivity) each unordered pair is
+// evaluated once: the CTA of the element with the smaller (first node, number)
+// key takes it, and the block's transposed entries -- which the reference
+// computes from the swapped pair, the same value mathematically -- go to the
+// other element's rows through global atomics (few with a banded numbering).
+// When the CTA is done its accumulators are added to the global values.  Rows
+// too long for shared memory fall back to global atomics with a binary search.
 #include "common.cuh"
 
 namespace nlgpu {
@@ -37,6 +41,7 @@ struct AssembleArgs {
     const double* deriv;      // [e][i][q][2]
     const i64* noff;
     const int32_t* nlist;
+    const int32_t* minnode;
     const uint8_t* is_inner;
     const double* cond_field; // isotropic conductivity per quadrature point, or null
     const i64* in_rp; const int32_t* in_col; double* in_val;
@@ -52,28 +57,25 @@ __device__ __forceinline__ double ipow(double x, int n) {   // power(T, integral
     return r;
 }
 
-// influence functions (influence_functions_2d.hpp:39-148) with the powered
-// distance of search_function.hpp:569-579; radii enter as multiplications by
-// their inverses.
+// Influence function without its normalisation (influence_functions_2d.hpp:39-148),
+// over the powered distance of search_function.hpp:569-579 with the radii as
+// inverse multipliers.
 template<int INF>
-__device__ __forceinline__ double influence(const Model& m, double ax, double ay, double bx, double by) {
-    const double z0 = (ax - bx) * m.inv_r[0], z1 = (ay - by) * m.inv_r[1];
+__device__ __forceinline__ double shape(const Model& m, double dx, double dy) {
+    const double z0 = dx * m.inv_r[0], z1 = dy * m.inv_r[1];
     double d;
     if (m.n == 2) d = z0 * z0 + z1 * z1;
     else if (m.n == 1) d = fabs(z0) + fabs(z1);
     else d = ipow(fabs(z0), m.n) + ipow(fabs(z1), m.n);
     if constexpr (INF == NLGPU_INFLUENCE_FAST_POLYNOMIAL) {
-        return d < 1.0 ? m.norm * (1.0 - d) : 0.0;
+        return d < 1.0 ? 1.0 - d : 0.0;
     } else if constexpr (INF == NLGPU_INFLUENCE_CONSTANT) {
-        return d <= 1.0 ? m.norm : 0.0;
+        return d <= 1.0 ? 1.0 : 0.0;
     } else {
         const bool integral = (m.p % m.n) == 0;
         const double dp = integral ? ipow(d, m.p / m.n) : pow(d, double(m.p) / double(m.n));
-        if constexpr (INF == NLGPU_INFLUENCE_POLYNOMIAL) {
-            return d < 1.0 ? m.norm * ipow(1.0 - dp, int(m.q)) : 0.0;
-        } else {
-            return m.norm * exp(-m.q * dp);
-        }
+        if constexpr (INF == NLGPU_INFLUENCE_POLYNOMIAL) return d < 1.0 ? ipow(1.0 - dp, int(m.q)) : 0.0;
+        else return exp(-m.q * dp);
     }
 }
 
@@ -85,20 +87,27 @@ __device__ __forceinline__ i64 find_col(const int32_t* col, i64 lo, i64 hi, int3
     return lo;
 }
 
+__device__ __forceinline__ void add_global(const i64* rp, const int32_t* col, double* val, int32_t r, int32_t c, double v,
+                                           int* error) {
+    const i64 pos = find_col(col, rp[r], rp[r + 1], c);
+    if (pos < rp[r + 1] && col[pos] == c) atomicAdd(val + pos, v);
+    else atomicExch(error, 1);
+}
+
 template<int NEN, int NQ>
 struct PairSmem {
     double qx[NQ], qy[NQ];
     double gx[NEN * NQ], gy[NEN * NQ];
     double phi[NQ * NQ];
     double hx[NQ * NEN], hy[NQ * NEN];
-    double lam[NQ];           // conductivity at eNL's points (field case)
+    double c[NQ];             // c_qNL
     int32_t nodes[NEN];
 };
 
-template<int NEN, int NQ, int INF>
+template<int NEN, int NQ, int INF, bool SYM>
 __global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, Model m, Basis b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double eqx[NQ], eqy[NQ], egx[NEN * NQ], egy[NEN * NQ], ejac[NQ], elam[NQ];
+    __shared__ double eqx[NQ], eqy[NQ], egx[NEN * NQ], egy[NEN * NQ], ewx[NEN * NQ], ewy[NEN * NQ], ejac[NQ], elam[NQ];
     __shared__ int32_t enodes[NEN];
     __shared__ i64 row_start[NEN];
     __shared__ int row_len[NEN], row_off[NEN + 1];
@@ -109,13 +118,15 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, M
     int32_t* cols = reinterpret_cast<int32_t*>(acc + a.cap);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     PairSmem<NEN, NQ>& ps = pairs[warp];
-    const double nl_weight = 1.0 - m.p1, l_weight = m.p1;
+    const double cnl = m.norm * (1.0 - m.p1);
+    const bool iso = m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC;
 
     for (i64 eL = blockIdx.x; eL < a.E; eL += gridDim.x) {
-        // ---- element eL: quadrature data and its node rows
+        // ---- element eL: quadrature data, weighted gradients and its node rows
         for (int t = threadIdx.x; t < NEN * NQ; t += AS_THREADS) {
-            egx[t] = a.deriv[2 * (eL * NEN * NQ + t)];
-            egy[t] = a.deriv[2 * (eL * NEN * NQ + t) + 1];
+            const double gx = a.deriv[2 * (eL * NEN * NQ + t)], gy = a.deriv[2 * (eL * NEN * NQ + t) + 1];
+            egx[t] = gx; egy[t] = gy;
+            ewx[t] = b.w[t % NQ] * gx; ewy[t] = b.w[t % NQ] * gy;
         }
         for (int t = threadIdx.x; t < NQ; t += AS_THREADS) {
             eqx[t] = a.qcoord[2 * (eL * NQ + t)];
@@ -146,11 +157,16 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, M
                 }
         }
         __syncthreads();
+        const int32_t key_l = SYM ? a.minnode[eL] : 0;
 
         // ---- pairs (eL, eNL): one warp each
         const i64 kb = a.noff[eL], ke = a.noff[eL + 1];
         for (i64 k = kb + warp; k < ke; k += AS_WARPS) {
             const int32_t eNL = a.nlist[k];
+            if constexpr (SYM) {   // the pair belongs to the element with the smaller key
+                const int32_t key_n = a.minnode[eNL];
+                if (key_n < key_l || (key_n == key_l && eNL < int32_t(eL))) continue;
+            }
             for (int t = lane; t < NEN * NQ; t += 32) {
                 ps.gx[t] = a.deriv[2 * (i64(eNL) * NEN * NQ + t)];
                 ps.gy[t] = a.deriv[2 * (i64(eNL) * NEN * NQ + t) + 1];
@@ -158,13 +174,14 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, M
             if (lane < NQ) {
                 ps.qx[lane] = a.qcoord[2 * (i64(eNL) * NQ + lane)];
                 ps.qy[lane] = a.qcoord[2 * (i64(eNL) * NQ + lane) + 1];
-                ps.lam[lane] = a.cond_field ? a.cond_field[i64(eNL) * NQ + lane] : m.cond[0];
+                const double lam = a.cond_field ? a.cond_field[i64(eNL) * NQ + lane] : m.cond[0];
+                ps.c[lane] = b.w[lane] * cnl * (iso ? lam : 1.0);
             }
             if (lane < NEN) ps.nodes[lane] = a.elems[i64(eNL) * NEN + lane];
             __syncwarp();
             for (int t = lane; t < NQ * NQ; t += 32) {
                 const int qL = t / NQ, qNL = t % NQ;
-                ps.phi[t] = b.w[qNL] * influence<INF>(m, eqx[qL], eqy[qL], ps.qx[qNL], ps.qy[qNL]);
+                ps.phi[t] = ps.c[qNL] * shape<INF>(m, eqx[qL] - ps.qx[qNL], eqy[qL] - ps.qy[qNL]);
             }
             __syncwarp();
             for (int t = lane; t < NQ * NEN; t += 32) {
@@ -174,61 +191,55 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, M
                 for (int qNL = 0; qNL < NQ; ++qNL) {
                     const double f = ps.phi[qL * NQ + qNL];
                     const double gx = ps.gx[j * NQ + qNL], gy = ps.gy[j * NQ + qNL];
-                    if (m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC) {
-                        const double s = f * ps.lam[qNL];
-                        h0 += s * gx; h1 += s * gy;
-                    } else if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) {
-                        h0 += f * m.cond[0] * gx; h1 += f * m.cond[1] * gy;
-                    } else {
-                        h0 += f * (m.cond[0] * gx + m.cond[2] * gy);
-                        h1 += f * (m.cond[2] * gx + m.cond[1] * gy);
-                    }
+                    if (m.cond_kind != NLGPU_CONDUCTIVITY_ANISOTROPIC) { h0 += f * gx; h1 += f * gy; }
+                    else { h0 += f * (m.cond[0] * gx + m.cond[2] * gy); h1 += f * (m.cond[2] * gx + m.cond[1] * gy); }
                 }
+                if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) { h0 *= m.cond[0]; h1 *= m.cond[1]; }
                 ps.hx[t] = h0; ps.hy[t] = h1;
             }
             __syncwarp();
+            const bool self = eNL == int32_t(eL);
             for (int t = lane; t < NEN * NEN; t += 32) {
                 const int i = t / NEN, j = t % NEN;
                 const int32_t r = enodes[i], c = ps.nodes[j];
-                const bool c_inner = a.is_inner[c];
-                const bool keep_inner = c_inner && a.is_inner[r] && (!a.symmetric || r <= c);
-                const bool keep_bound = !c_inner && r != c;
-                if (!keep_inner && !keep_bound) continue;
+                const bool r_in = a.is_inner[r], c_in = a.is_inner[c];
+                // (r, c) from this pair; (c, r) from the swapped pair when it is folded into this one
+                const bool fwd_inner = c_in && r_in && (!a.symmetric || r <= c);
+                const bool fwd_bound = !c_in && r != c;
+                const bool tr = SYM && !self;
+                const bool bwd_inner = tr && c_in && r_in && c <= r;
+                const bool bwd_bound = tr && !r_in && c != r;
+                if (!fwd_inner && !fwd_bound && !bwd_inner && !bwd_bound) continue;
                 double v = 0.0;
                 #pragma unroll
                 for (int qL = 0; qL < NQ; ++qL)
-                    v += b.w[qL] * (egx[i * NQ + qL] * ps.hx[qL * NEN + j] + egy[i * NQ + qL] * ps.hy[qL * NEN + j]);
-                v *= nl_weight;
-                if (eNL == int32_t(eL)) {
+                    v += ewx[i * NQ + qL] * ps.hx[qL * NEN + j] + ewy[i * NQ + qL] * ps.hy[qL * NEN + j];
+                if (self) {
                     double loc = 0.0;
                     #pragma unroll
                     for (int q = 0; q < NQ; ++q) {
                         const double ax = egx[i * NQ + q], ay = egy[i * NQ + q];
                         const double bx = egx[j * NQ + q], by = egy[j * NQ + q];
                         double val;
-                        if (m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC) val = elam[q] * (ax * bx + ay * by);
+                        if (iso) val = elam[q] * (ax * bx + ay * by);
                         else if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) val = m.cond[0] * ax * bx + m.cond[1] * ay * by;
                         else val = ax * (m.cond[0] * bx + m.cond[2] * by) + ay * (m.cond[2] * bx + m.cond[1] * by);
                         loc += b.w[q] * val / ejac[q];
                     }
-                    v += l_weight * loc;
+                    v += m.p1 * loc;
                 }
-                // the patterns hold every kept entry; a miss is recorded, never written
-                if (keep_inner) {
+                if (fwd_inner) {
                     if (smem_rows) {
                         const i64 pos = find_col(cols, row_off[i], row_off[i + 1], c);
                         if (pos < row_off[i + 1] && cols[pos] == c) atomicAdd(acc + pos, v);
                         else atomicExch(a.error, 1);
                     } else {
-                        const i64 pos = find_col(a.in_col, a.in_rp[r], a.in_rp[r + 1], c);
-                        if (pos < a.in_rp[r + 1] && a.in_col[pos] == c) atomicAdd(a.in_val + pos, v);
-                        else atomicExch(a.error, 1);
+                        add_global(a.in_rp, a.in_col, a.in_val, r, c, v, a.error);
                     }
-                } else {
-                    const i64 pos = find_col(a.bd_col, a.bd_rp[r], a.bd_rp[r + 1], c);
-                    if (pos < a.bd_rp[r + 1] && a.bd_col[pos] == c) atomicAdd(a.bd_val + pos, v);
-                    else atomicExch(a.error, 1);
                 }
+                if (fwd_bound) add_global(a.bd_rp, a.bd_col, a.bd_val, r, c, v, a.error);
+                if (bwd_inner) add_global(a.in_rp, a.in_col, a.in_val, c, r, v, a.error);
+                if (bwd_bound) add_global(a.bd_rp, a.bd_col, a.bd_val, c, r, v, a.error);
             }
             __syncwarp();
         }
@@ -302,22 +313,28 @@ __global__ void k_gather_full(i64 nnz, const i64* __restrict__ map, const double
 }
 
 template<int NEN, int NQ, int INF>
-void launch_pairs(Ctx& ctx, const AssembleArgs& a) {
+void launch_pairs(Ctx& ctx, const AssembleArgs& a, bool sym) {
     const size_t fixed = sizeof(PairSmem<NEN, NQ>) * AS_WARPS;
     const size_t dyn = fixed + size_t(a.cap) * (sizeof(double) + sizeof(int32_t));
-    auto kernel = k_assemble_pairs<NEN, NQ, INF>;
-    NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
     const unsigned grid = unsigned(std::min<i64>(a.E, 152 * 16));
-    NL_LAUNCH(kernel, grid, AS_THREADS, dyn, ctx.stream, a, ctx.model, ctx.basis);
+    if (sym) {
+        auto kernel = k_assemble_pairs<NEN, NQ, INF, true>;
+        NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
+        NL_LAUNCH(kernel, grid, AS_THREADS, dyn, ctx.stream, a, ctx.model, ctx.basis);
+    } else {
+        auto kernel = k_assemble_pairs<NEN, NQ, INF, false>;
+        NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
+        NL_LAUNCH(kernel, grid, AS_THREADS, dyn, ctx.stream, a, ctx.model, ctx.basis);
+    }
 }
 
 template<int NEN, int NQ>
-void dispatch_influence(Ctx& ctx, const AssembleArgs& a) {
+void dispatch_influence(Ctx& ctx, const AssembleArgs& a, bool sym) {
     switch (ctx.model.influence) {
-    case NLGPU_INFLUENCE_FAST_POLYNOMIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_FAST_POLYNOMIAL>(ctx, a); break;
-    case NLGPU_INFLUENCE_POLYNOMIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_POLYNOMIAL>(ctx, a); break;
-    case NLGPU_INFLUENCE_EXPONENTIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_EXPONENTIAL>(ctx, a); break;
-    default: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_CONSTANT>(ctx, a); break;
+    case NLGPU_INFLUENCE_FAST_POLYNOMIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_FAST_POLYNOMIAL>(ctx, a, sym); break;
+    case NLGPU_INFLUENCE_POLYNOMIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_POLYNOMIAL>(ctx, a, sym); break;
+    case NLGPU_INFLUENCE_EXPONENTIAL: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_EXPONENTIAL>(ctx, a, sym); break;
+    default: launch_pairs<NEN, NQ, NLGPU_INFLUENCE_CONSTANT>(ctx, a, sym); break;
     }
 }
 
@@ -335,7 +352,7 @@ void assemble_full(Ctx& ctx) {
     }
     AssembleArgs a{};
     a.E = ctx.n_elems; a.elems = ctx.elems.p; a.qcoord = ctx.qcoord.p; a.jac = ctx.jac.p; a.deriv = ctx.deriv.p;
-    a.noff = ctx.noff.p; a.nlist = ctx.nlist.p; a.is_inner = ctx.is_inner.p;
+    a.noff = ctx.noff.p; a.nlist = ctx.nlist.p; a.minnode = ctx.elem_minnode.p; a.is_inner = ctx.is_inner.p;
     a.cond_field = ctx.cond_field.n ? ctx.cond_field.p : nullptr;
     a.in_rp = ctx.inner.rowptr.p; a.in_col = ctx.inner.col.p; a.in_val = ctx.inner.val.p;
     a.bd_rp = ctx.bound.rowptr.p; a.bd_col = ctx.bound.col.p; a.bd_val = ctx.bound.val.p;
@@ -344,12 +361,14 @@ void assemble_full(Ctx& ctx) {
     err.resize(1);
     err.zero(ctx.stream);
     a.error = err.p;
+    // unordered pairs need a symmetric influence and constant conductivity
+    const bool sym = ctx.symmetric && !ctx.cond_field.n && !ctx.ordered_pairs;
     if (ctx.basis.nen == 4) {
         a.cap = int((200 * 1024 - sizeof(PairSmem<4, 4>) * AS_WARPS) / 12);
-        dispatch_influence<4, 4>(ctx, a);
+        dispatch_influence<4, 4>(ctx, a, sym);
     } else {
         a.cap = int((200 * 1024 - sizeof(PairSmem<8, 9>) * AS_WARPS) / 12);
-        dispatch_influence<8, 9>(ctx, a);
+        dispatch_influence<8, 9>(ctx, a, sym);
     }
     set_dirichlet_diagonal(ctx, ctx.inner, 1.0);
     int herr = 0;
@@ -381,11 +400,7 @@ void fill_full_from_upper(Ctx& ctx, const Csr& upper, Csr& full, const dbuf<i64>
               full.val32.n ? full.val32.p : nullptr);
 }
 
-}  // namespace nlgpu
-
 // ---------------------------------------------------------------- nonstationary
-namespace nlgpu {
-
 namespace {
 
 // K <- dt K + C row by row (C's pattern is contained in K's), unit Dirichlet

@@ -157,6 +157,7 @@ struct SweepPlan {
     int stage_bytes = 0;
     size_t smem_bytes = 0;
     dbuf<int32_t> cnt, cntp, width;
+    dbuf<ushort4> meta;          // per level: rows, padded rows, width
     dbuf<i64> ppos, block_off;
     dbuf<unsigned char> blocks;  // per level: values, inverse diagonal, ring slots
     dbuf<int32_t> row_of;        // padded position -> row (-1 padding)
@@ -214,6 +215,7 @@ struct Ctx {
     dbuf<i64> ne_off;            // node -> elements CSR
     dbuf<int32_t> ne_elem;
     dbuf<int8_t> ne_local;
+    dbuf<int32_t> elem_minnode;  // smallest node number per element
     bool mesh_ready = false;
     // model
     Model model{};
@@ -251,6 +253,7 @@ struct Ctx {
     bool nonstationary_ready = false;
     dbuf<int> sweep_error;
     bool force_global_sweeps = false;   // use the global-memory sweeps (for comparison)
+    bool ordered_pairs = false;         // evaluate every ordered element pair (for comparison)
     // measurement
     cudaEvent_t events[64] = {};
     dbuf<unsigned char> flush;

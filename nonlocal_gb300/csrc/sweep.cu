@@ -67,11 +67,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 template<class T>
 struct SweepArgs {
     i64 n_levels;
-    const i64* block_off;     // [L] byte offset of the level block
-    const int32_t* cnt;       // [L] rows
-    const int32_t* cntp;      // [L] padded rows (multiple of 8)
-    const int32_t* width;     // [L]
-    const i64* ppos;          // [L + 1] padded position of the level's first row
+    const ushort4* meta;      // [L] rows, padded rows (multiple of 8), width, 0
     const unsigned char* blocks;
     const T* in;              // right-hand side in padded level order
     T* out;                   // solution in padded level order
@@ -105,6 +101,9 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_tma(SweepArgs<T> a) {
         __syncthreads();
         if (skip) return;
     }
+    // per-level (rows, padded rows, width) for every level, read once
+    ushort4* meta = reinterpret_cast<ushort4*>(bars + SW_STAGES);
+    for (i64 l = threadIdx.x; l < a.n_levels; l += blockDim.x) meta[l] = a.meta[l];
     for (int k = threadIdx.x; k <= SW_RING; k += blockDim.x) ring[k] = T(0);
     if (threadIdx.x == 0) {
         for (int s = 0; s < SW_STAGES; ++s) mbar_init(&bars[s], 1);
@@ -112,18 +111,23 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_tma(SweepArgs<T> a) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
+    // the issuing thread walks the level blocks and right-hand-side chunks in order
+    i64 issue_block = 0, issue_pos = 0;
     auto issue = [&](i64 l) {
         const int s = int(l % SW_STAGES);
         unsigned char* dst = stage_base + size_t(s) * a.stage_bytes;
-        const int cp = a.cntp[l], w = a.width[l];
+        const int cp = meta[l].y, w = meta[l].z;
         const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 2) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
         const uint32_t rhs_bytes = uint32_t(size_t(cp) * sizeof(T));
         mbar_expect_tx(&bars[s], block_bytes + rhs_bytes);
-        bulk_g2s(dst, a.blocks + a.block_off[l], block_bytes, &bars[s]);
-        bulk_g2s(dst + block_bytes, a.in + a.ppos[l], rhs_bytes, &bars[s]);
+        bulk_g2s(dst, a.blocks + issue_block, block_bytes, &bars[s]);
+        bulk_g2s(dst + block_bytes, a.in + issue_pos, rhs_bytes, &bars[s]);
+        issue_block += block_bytes;
+        issue_pos += cp;
     };
     if (threadIdx.x == 0)
         for (i64 l = 0; l < a.n_levels && l < SW_STAGES; ++l) issue(l);
+    i64 p0 = 0;
     for (i64 l = 0; l < a.n_levels; ++l) {
         const int s = int(l % SW_STAGES);
         const uint32_t parity = uint32_t((l / SW_STAGES) & 1);
@@ -133,14 +137,13 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_tma(SweepArgs<T> a) {
                 if (globaltimer_ns() - t0 > SW_WAIT_LIMIT_NS) { atomicExch(a.error, 1); return; }
             }
         }
-        const int c = a.cnt[l], cp = a.cntp[l], w = a.width[l];
+        const int c = meta[l].x, cp = meta[l].y, w = meta[l].z;
         const unsigned char* blk = stage_base + size_t(s) * a.stage_bytes;
         const T* vals = reinterpret_cast<const T*>(blk);
         const T* inv = vals + size_t(w) * cp;
         const int16_t* dep = reinterpret_cast<const int16_t*>(inv + cp);
         const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 2) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
         const T* rhs = reinterpret_cast<const T*>(blk + block_bytes);
-        const i64 p0 = a.ppos[l];
         for (int t = threadIdx.x; t < c; t += blockDim.x) {
             T acc = rhs[t];
             for (int k = 0; k < w; ++k) acc -= vals[k * cp + t] * ring[dep[k * cp + t]];
@@ -148,6 +151,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_tma(SweepArgs<T> a) {
             ring[(p0 + t) & (SW_RING - 1)] = v;
             a.out[p0 + t] = v;
         }
+        p0 += cp;
         __syncthreads();   // stage s is consumed and the level's ring values are visible
         if (threadIdx.x == 0 && l + SW_STAGES < a.n_levels) issue(l + SW_STAGES);
     }
@@ -260,9 +264,16 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
         }
     }
     const size_t smem = ((sizeof(double) * (SW_RING + 1) + 127) / 128) * 128 + size_t(max_stage) * SW_STAGES +
-                        SW_STAGES * sizeof(uint64_t);
-    plan.ok = max_dist <= SW_RING && smem <= 220 * 1024 && n < (i64(1) << 31);
+                        SW_STAGES * sizeof(uint64_t) + size_t(L) * sizeof(ushort4);
+    std::vector<ushort4> meta(static_cast<size_t>(L));
+    bool small = true;
+    for (i64 l = 0; l < L; ++l) {
+        small = small && cntp[size_t(l)] < 65536 && width[size_t(l)] < 65536;
+        meta[size_t(l)] = make_ushort4(uint16_t(cnt[size_t(l)]), uint16_t(cntp[size_t(l)]), uint16_t(width[size_t(l)]), 0);
+    }
+    plan.ok = small && max_dist <= SW_RING && smem <= 220 * 1024 && n < (i64(1) << 31);
     if (!plan.ok) return false;
+    plan.meta.upload(meta.data(), meta.size(), ctx.stream);
     std::vector<int32_t> row_of(static_cast<size_t>(P), -1);
     for (i64 l = 0; l < L; ++l)
         for (int t = 0; t < cnt[size_t(l)]; ++t) row_of[size_t(ppos[size_t(l)] + t)] = rows[size_t(lev_ptr[size_t(l)] + t)];
@@ -297,8 +308,8 @@ void sweep_plan_fill(Ctx& ctx, SweepPlan& plan, const double* u) {
 
 static void run_sweep(Ctx& ctx, SweepPlan& plan, const double* partials, const double* flags, double tol2) {
     SweepArgs<double> a{};
-    a.n_levels = plan.n_levels; a.block_off = plan.block_off.p; a.cnt = plan.cnt.p; a.cntp = plan.cntp.p;
-    a.width = plan.width.p; a.ppos = plan.ppos.p; a.blocks = plan.blocks.p; a.in = plan.in.p; a.out = plan.out.p;
+    a.n_levels = plan.n_levels; a.meta = plan.meta.p;
+    a.blocks = plan.blocks.p; a.in = plan.in.p; a.out = plan.out.p;
     a.stage_bytes = plan.stage_bytes; a.partials = partials; a.flags = flags; a.tol2 = tol2;
     ctx.sweep_error.reserve(1);
     a.error = ctx.sweep_error.p;
