@@ -199,6 +199,19 @@ int nlgpu_cg_solve(nlgpu_ctx* ctx, int64_t n, const int64_t* a_rowptr, const int
                    const double* p_val, const double* b, const double* x0, double tolerance,
                    int64_t max_iterations, double* x, nlgpu_solve_report* report);
 
+/* ---- ILLT behind slae::preconditioner_base (preconditioner_base.hpp:8-15),
+ * the GPU counterpart of eigen_preconditioner<T, I, Eigen::IncompleteCholesky<
+ * T, Eigen::Upper, Eigen::NaturalOrdering<I>>> (eigen_preconditioner.hpp:9-57).
+ * compute: factorises an upper-stored symmetric CSR (row pointers [n + 1],
+ * sorted columns with the diagonal first, values; the reference's RowMajor
+ * int64 storage) and writes computation_info as Eigen::ComputationInfo
+ * (0 Success, 1 NumericalIssue when every diagonal shift failed; the
+ * reference then falls back to the identity).  The factor stays in the
+ * context until the next compute.  solve: y = M^-1 x for host vectors [n]. */
+int nlgpu_illt_compute(nlgpu_ctx* ctx, int64_t n, const int64_t* rowptr, const int64_t* col, const double* val,
+                       int* computation_info);
+int nlgpu_illt_solve(nlgpu_ctx* ctx, int64_t n, const double* x, double* y);
+
 /* ---- nonstationary_heat_equation_solver_2d (nonstationary_heat_equation_solver_2d.hpp:16-106)
  * compute: assembles dt*K + C (unit Dirichlet diagonal) for the current mesh,
  * model and boundary groups; initial temperature [n_nodes] or NULL (zero).

@@ -86,6 +86,8 @@ SIGNATURES = {
     "nlgpu_solve_assembled": (c_int, [c_p, ctypes.POINTER(SolveOptions), c_p, ctypes.POINTER(SolveReport)]),
     "nlgpu_cg_solve": (c_int, [c_p, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_d, c_i64, c_p,
                                ctypes.POINTER(SolveReport)]),
+    "nlgpu_illt_compute": (c_int, [c_p, c_i64, c_p, c_p, c_p, ctypes.POINTER(c_int)]),
+    "nlgpu_illt_solve": (c_int, [c_p, c_i64, c_p, c_p]),
     "nlgpu_nonstationary_2d_compute": (c_int, [c_p, c_d, c_p]),
     "nlgpu_nonstationary_2d_step": (c_int, [c_p, c_d, c_p, c_d, c_i64, c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),

@@ -541,6 +541,53 @@ int nlgpu_cg_solve(nlgpu_ctx* ctx, int64_t n, const int64_t* a_rowptr, const int
     return rc != NLGPU_OK ? rc : conv_status;
 }
 
+int nlgpu_illt_compute(nlgpu_ctx* ctx, int64_t n, const int64_t* rowptr, const int64_t* col, const double* val,
+                       int* computation_info) {
+    if (!ctx || n <= 0 || n >= (int64_t(1) << 31) || !rowptr || !col || !val || !computation_info) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        c.plugin_ilt_ready = false;
+        NL_REQUIRE(rowptr[0] == 0 && rowptr[n] >= n, NLGPU_ERR_ARG, "row pointers must start at 0 and hold a diagonal per row");
+        Csr P;
+        P.rows = n; P.nnz = rowptr[n];
+        std::vector<int32_t> pc(static_cast<size_t>(P.nnz));
+        for (int64_t r = 0; r < n; ++r) {
+            NL_REQUIRE(rowptr[r + 1] > rowptr[r], NLGPU_ERR_ARG, "every row needs its diagonal");
+            for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+                NL_REQUIRE(col[k] >= r && col[k] < n && (k == rowptr[r] || col[k] > col[k - 1]), NLGPU_ERR_ARG,
+                           "columns must be upper, sorted and in range");
+                pc[size_t(k)] = int32_t(col[k]);
+            }
+        }
+        std::vector<i64> prp(rowptr, rowptr + n + 1);
+        P.rowptr.upload(prp.data(), prp.size(), c.stream);
+        P.col.upload(pc.data(), pc.size(), c.stream);
+        P.val.upload(val, size_t(P.nnz), c.stream);
+        ilt_build(c, P, c.plugin_ilt);
+        c.plugin_ilt_ready = c.plugin_ilt.ok;
+        *computation_info = c.plugin_ilt.ok ? 0 : 1;
+    });
+}
+
+int nlgpu_illt_solve(nlgpu_ctx* ctx, int64_t n, const double* x, double* y) {
+    if (!ctx || !x || !y) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.plugin_ilt_ready, NLGPU_ERR_STATE, "nlgpu_illt_compute has not succeeded on this context");
+        NL_REQUIRE(n == c.plugin_ilt.n, NLGPU_ERR_ARG, "vector size differs from the factorised matrix");
+        dbuf<double> dx, dy;
+        dx.upload(x, size_t(n), c.stream);
+        dy.resize(size_t(n));
+        c.sweep_error.zero(c.stream);
+        ilt_apply(c, c.plugin_ilt, dx.p, dy.p);
+        dy.download(y, size_t(n), c.stream);
+        int err = 0;
+        c.sweep_error.download(&err, 1, c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        NL_REQUIRE(err == 0, NLGPU_ERR_TIMEOUT, "a triangular sweep gave up waiting for its data");
+    });
+}
+
 int nlgpu_nonstationary_2d_compute(nlgpu_ctx* ctx, double time_step, const double* initial) {
     if (!ctx || !(time_step > 0.0)) return NLGPU_ERR_ARG;
     return guarded([&] {

@@ -243,6 +243,8 @@ struct Ctx {
     dbuf<i64> full_from_upper;   // full entry -> upper entry (lower part via transpose)
     bool inner_ready = false, local_ready = false;
     IncompleteCholesky ilt;
+    IncompleteCholesky plugin_ilt;   // nlgpu_illt_compute / nlgpu_illt_solve
+    bool plugin_ilt_ready = false;
     CgWork cg;
     // nonstationary
     Csr capacity_m, capacity_full;

@@ -12,9 +12,9 @@
 //   * all CG scalars stay on the device: reductions write one partial per
 //     block, and every block of the consuming kernel re-adds the partials in a
 //     fixed order (deterministic, no extra launch);
-//   * iterations are enqueued as a CUDA graph of GRAPH_ITERS iterations; each
+//   * iterations are enqueued in chunks of GRAPH_ITERS iterations; each
 //     kernel returns at once after convergence, the host reads the flag once
-//     per graph;
+//     per chunk;
 //   * ILLT: Lin-More scaling S = diag(|a_j|_2)^(-1/2) and diagonal shift retry
 //     (alpha_S = 1e-3, doubled, at most 10 attempts) around IC(0) on the
 //     pattern of the upper local matrix, factored level by level in one CTA;

@@ -284,6 +284,46 @@ class NonstationaryHeatEquationSolver2D:
         return t
 
 
+class EigenILLTPreconditioner:
+    """ILLT behind slae::preconditioner_base (preconditioner_base.hpp:8-15): the GPU
+    counterpart of eigen_preconditioner with Eigen::IncompleteCholesky.
+
+    ``compute`` factorises an upper-stored symmetric CSR (diagonal first);
+    ``computation_info`` is Eigen's code (0 Success, 1 NumericalIssue);
+    ``solve`` returns M^-1 x."""
+
+    SUCCESS, NUMERICAL_ISSUE = 0, 1
+
+    def __init__(self, context: Context | None = None):
+        self.context = context if context is not None else Context()
+        self._info = self.NUMERICAL_ISSUE
+        self._n = 0
+
+    def analyze_pattern(self, csr) -> "EigenILLTPreconditioner":
+        return self          # the pattern is analysed by compute
+
+    def factorize(self, csr) -> "EigenILLTPreconditioner":
+        return self.compute(csr)
+
+    def compute(self, csr) -> "EigenILLTPreconditioner":
+        rp, col, val = L.i64(csr[0]), L.i64(csr[1]), L.f64(csr[2])
+        n = rp.shape[0] - 1
+        info = ctypes.c_int()
+        L.check(self.context._lib.nlgpu_illt_compute(self.context.handle, n, L.ptr(rp), L.ptr(col), L.ptr(val),
+                                                     ctypes.byref(info)))
+        self._info, self._n = int(info.value), n
+        return self
+
+    def computation_info(self) -> int:
+        return self._info
+
+    def solve(self, x) -> np.ndarray:
+        x = L.f64(x)
+        y = np.empty_like(x)
+        L.check(self.context._lib.nlgpu_illt_solve(self.context.handle, x.shape[0], L.ptr(x), L.ptr(y)))
+        return y
+
+
 def conjugate_gradient(problem: Problem2D, a_csr, b, x0=None, preconditioner_csr=None, tolerance=1e-10,
                        max_iterations=10000):
     """slae::conjugate_gradient on an upper-stored symmetric CSR (diagonal first in each row)."""
