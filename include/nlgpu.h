@@ -212,6 +212,30 @@ int nlgpu_illt_compute(nlgpu_ctx* ctx, int64_t n, const int64_t* rowptr, const i
                        int* computation_info);
 int nlgpu_illt_solve(nlgpu_ctx* ctx, int64_t n, const double* x, double* y);
 
+/* ---- conjugate gradient that allocates nothing (no counterpart in the reference)
+ * For callers that cannot allocate device memory when they solve (an external
+ * memory budget or pool, a loop that must not touch the allocator, buffers
+ * owned by another framework): identity-preconditioned CG on a symmetric
+ * matrix already in device memory, full-row CSR (row pointers int64 [n + 1],
+ * columns int32, values double), right-hand side d_b [n] and solution d_x [n]
+ * (initial guess on entry) also in device memory.  Its work vectors live in
+ * a fixed scratch array inside the library, sized for at most
+ * NLGPU_NOALLOC_MAX_ROWS rows (about 1.6 MB, held on every GPU that loads the
+ * library until the process exits); no cudaMalloc or cudaFree is called, and
+ * n above NLGPU_NOALLOC_MAX_ROWS is rejected with NLGPU_ERR_ARG.  The first
+ * call on a device looks the array's device address up (make it before any
+ * stream capture).  The call zeroes its own counters in the array; d_x must
+ * hold the starting guess (zeros for a zero start).  All calls share the
+ * array: calls that overlap on the GPU race.  Stops when |r| <= tolerance |b|
+ * (|r| of the CG recurrence) or after max_iterations; reports the iterations
+ * and |b - A x| / |b| recomputed from x.
+ * `stream` is a cudaStream_t or NULL; the call returns after the stream has
+ * finished its work. */
+#define NLGPU_NOALLOC_MAX_ROWS 65536
+int nlgpu_cg_solve_noalloc(void* stream, int64_t n, const int64_t* d_rowptr, const int32_t* d_col,
+                           const double* d_val, const double* d_b, double* d_x, double tolerance,
+                           int64_t max_iterations, int64_t* iterations, double* residual);
+
 /* ---- nonstationary_heat_equation_solver_2d (nonstationary_heat_equation_solver_2d.hpp:16-106)
  * compute: assembles dt*K + C (unit Dirichlet diagonal) for the current mesh,
  * model and boundary groups; initial temperature [n_nodes] or NULL (zero).

@@ -91,6 +91,8 @@ SIGNATURES = {
     "nlgpu_nonstationary_2d_compute": (c_int, [c_p, c_d, c_p]),
     "nlgpu_nonstationary_2d_step": (c_int, [c_p, c_d, c_p, c_d, c_i64, c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),
+    "nlgpu_cg_solve_noalloc": (c_int, [c_p, c_i64, c_p, c_p, c_p, c_p, c_p, c_d, c_i64, ctypes.POINTER(c_i64),
+                                       ctypes.POINTER(c_d)]),
     "nlgpu_set_option": (c_int, [c_p, c_int, c_int]),
     "nlgpu_event_record": (c_int, [c_p, c_int]),
     "nlgpu_event_elapsed": (c_int, [c_p, c_int, c_int, ctypes.POINTER(c_d)]),

@@ -648,6 +648,16 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
     });
 }
 
+int nlgpu_cg_solve_noalloc(void* stream, int64_t n, const int64_t* d_rowptr, const int32_t* d_col, const double* d_val,
+                           const double* d_b, double* d_x, double tolerance, int64_t max_iterations, int64_t* iterations,
+                           double* residual) {
+    if (!iterations || !residual) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        cg_solve_noalloc(static_cast<cudaStream_t>(stream), n, d_rowptr, d_col, d_val, d_b, d_x, tolerance,
+                         max_iterations, iterations, residual);
+    });
+}
+
 int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value) {
     if (!ctx) return NLGPU_ERR_ARG;
     if (option == NLGPU_OPTION_GLOBAL_SWEEPS) { ctx->force_global_sweeps = value != 0; return NLGPU_OK; }

@@ -304,6 +304,9 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
 void sweep_plan_fill(Ctx& ctx, SweepPlan& plan, const double* u);
 void sweep_apply(Ctx& ctx, IncompleteCholesky& ic, const double* r, double* z, const double* partials,
                  const double* flags, double tol2);
+// noalloc.cu
+void cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, const double* val, const double* b,
+                      double* x, double tolerance, i64 max_iterations, i64* iterations, double* residual);
 // onedim.cu
 void stationary_1d(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight, int influence,
                    double conductivity, double t_left, double q_right, bool sin_source, double* temperature);
