@@ -4,15 +4,18 @@
 Workload (default ``config2``): unit square, 200x200 bilinear elements, 2x2
 Gauss, isotropic conductivity 1, p1 = 0.5, polynomial-bell (fast_polynomial)
 influence r = 0.05 (search radius widened to r + h*sqrt(2)), T = 0 on the
-left edge, unit flux on the right edge, no source; ILLT-preconditioned CG to
-relative residual |b - Ax| / |b| <= 1e-10 in FP64.  Synthetic structured
+left edge, unit flux on the right edge, no source; solved to relative
+residual |b - Ax| / |b| <= 1e-10 (FP64 residual).  Synthetic structured
 mesh, deterministic.
 
 One step = one stationary solve from the resident mesh: neighbour search,
-sparsity patterns, nonlocal + local assembly, boundary conditions, ILLT
-factorisation and CG.  value = device time per solve (CUDA events on the
-library's stream), L2 flushed between steps.  e2e = the same solve through
-the C ABI from host buffers (mesh upload and temperature download included).
+sparsity patterns, nonlocal + local assembly (FP64), boundary conditions,
+ILLT factorisation and the solve.  value = device time per solve of the
+mixed-precision form (FP32 inner flexible CG with FP32 ILLT sweeps, FP64
+iterative refinement) by CUDA events on the library's stream, L2 flushed
+between steps; the plain FP64 ILLT-CG solve is timed the same way and
+reported beside it.  e2e = the mixed solve through the C ABI from host
+buffers (mesh upload and temperature download included).
 
 --impl reference times the reference algorithm on the host cores instead
 (the CPU restatement in oracle/, all threads), same workload and metric.
@@ -33,7 +36,9 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "time to 1e-10 relative residual, nonlocal stationary 2D solve (plain FP64 ILLT-CG, full pipeline)"
+METRIC = ("time to 1e-10 relative residual, nonlocal stationary 2D solve (full pipeline): mixed-precision FCG "
+          "(FP32 inner, FP64 refinement) with ILLT; plain FP64 ILLT-CG beside it")
+PRIMARY = "mixed"
 
 WORKLOADS = {
     "config2": dict(name="200x200 bilinear, fast_polynomial r=0.05, p1=0.5, left T=0 / right flux 1, FP64 ILLT-CG 1e-10",
@@ -217,49 +222,64 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     h = pb.handle
     tol = w["tolerance"]
 
-    def step():
+    def step(precision):
         pb.find_neighbours()
-        return pb.stationary(tolerance=tol, max_iterations=100000)
+        return pb.stationary(tolerance=tol, max_iterations=100000, precision=precision)
+
+    def timed(precision):
+        """K device-timed solves (CUDA events on the library's stream), L2 flushed before each."""
+        ms_steps, reports = [], []
+        for k in range(args.steps):
+            L.check(lib.nlgpu_flush_l2(h, L2_FLUSH_BYTES))
+            L.check(lib.nlgpu_event_record(h, 0))
+            t_, rep_ = step(precision)
+            L.check(lib.nlgpu_event_record(h, 1))
+            ms = ctypes.c_double()
+            L.check(lib.nlgpu_event_elapsed(h, 0, 1, ctypes.byref(ms)))
+            ms_steps.append(ms.value)
+            reports.append(rep_)
+        return ms_steps, reports, t_
 
     for _ in range(args.warmup):
-        temp, rep = step()
-    # -------- timed region: device time per solve, L2 flushed between solves
+        step(PRIMARY)
+        step("fp64")
+    # -------- timed region: the primary method, then the plain FP64 method
     sampler = ClockSampler(local)
     launches0 = L.kernel_launches()
     barrier(dist)
     L.check(lib.nlgpu_synchronize(h))
     sampler.start()
-    ms_steps = []
-    reports = []
-    for k in range(args.steps):
-        L.check(lib.nlgpu_flush_l2(h, L2_FLUSH_BYTES))
-        L.check(lib.nlgpu_event_record(h, 0))
-        temp, rep = step()
-        L.check(lib.nlgpu_event_record(h, 1))
-        ms = ctypes.c_double()
-        L.check(lib.nlgpu_event_elapsed(h, 0, 1, ctypes.byref(ms)))
-        ms_steps.append(ms.value)
-        reports.append(rep)
+    ms_steps, reports, temp = timed(PRIMARY)
+    L.check(lib.nlgpu_synchronize(h))
+    launches = L.kernel_launches() - launches0
+    ms_plain, reports_plain, temp_plain = timed("fp64")
     L.check(lib.nlgpu_synchronize(h))
     clocks = sampler.stop()
-    launches = L.kernel_launches() - launches0
     barrier(dist)
     mean_ms = max_over_ranks(dist, sum(ms_steps) / len(ms_steps))
+    plain_ms = max_over_ranks(dist, sum(ms_plain) / len(ms_plain))
     seconds = mean_ms / 1e3
     rep = reports[-1]
+    rep_plain = reports_plain[-1]
     pairs = rep.element_pairs
     iters = rep.iterations
 
     # -------- stage timings for the roofline (device events, this problem)
     stage_ms = {}
-    for stage, name, reps in [(0, "spmv", 50), (2, "illt_apply", 20), (1, "pair_assembly", 3)]:
+    for stage, name, reps in [(0, "spmv", 50), (4, "spmv32", 50), (2, "illt_apply", 10), (5, "illt_apply32", 10),
+                              (1, "pair_assembly", 3)]:
         v = ctypes.c_double()
         L.check(lib.nlgpu_time_stage(h, stage, reps, ctypes.byref(v)))
         stage_ms[name] = v.value
     n = pb.n_nodes
     nnz_solver = rep.nnz_solver
     spmv_bytes = nnz_solver * (8 + 4) + (n + 1) * 8 + 2 * n * 8
-    per_solve_ms = {"spmv": stage_ms["spmv"] * (iters + 2), "illt_apply": stage_ms["illt_apply"] * (iters + 1),
+    spmv32_bytes = nnz_solver * (4 + 4) + (n + 1) * 8 + 2 * n * 4
+    outer = rep.outer_iterations
+    # per solve of the primary (mixed) method: inner FP32 SpMV and sweeps per inner
+    # iteration (+1 start per outer step), FP64 SpMV per outer residual
+    per_solve_ms = {"spmv": stage_ms["spmv"] * (outer + 1), "spmv32": stage_ms["spmv32"] * iters,
+                    "illt_apply32": stage_ms["illt_apply32"] * (iters + outer),
                     "pair_assembly": stage_ms["pair_assembly"]}
     dominant = max(per_solve_ms, key=per_solve_ms.get)
     pk, pk_kind = peaks()
@@ -271,22 +291,25 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         roof = {"kernel": "k_assemble_pairs", "bound": "fp64", "achieved": achieved, "peak": fp64_peak,
                 "peak_kind": "nominal FP64 (no measured FP64 peak on this pool)", "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak, "traffic": traffic.get(("k_assemble_pairs", args.workload))}
-    elif dominant == "spmv":
-        achieved = spmv_bytes / (stage_ms["spmv"] * 1e-3) / 1e9
-        roof = {"kernel": "k_spmv", "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+    elif dominant in ("spmv", "spmv32"):
+        nbytes = spmv_bytes if dominant == "spmv" else spmv32_bytes
+        achieved = nbytes / (stage_ms[dominant] * 1e-3) / 1e9
+        kname = "k_spmv" if dominant == "spmv" else "k_spmv32"
+        roof = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
                 "peak_kind": pk_kind, "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
-                "traffic": traffic.get(("k_spmv", args.workload))}
+                "traffic": traffic.get((kname, args.workload))}
     else:
-        # both sweeps read each off-diagonal factor entry (value 8 B + column 4 B)
-        # once, per row its number and inverse diagonal (4 + 8 B) once, r and S
-        # (16 B) once, and write y, w and z (24 B)
-        ilt_bytes = factor_offdiag_entries(lib, h, n) * 12 + n * (4 + 8) * 2 + n * 8 * 5
-        achieved = ilt_bytes / (stage_ms["illt_apply"] * 1e-3) / 1e9
-        roof = {"kernel": "k_trisolve", "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+        # both FP32 sweeps read each off-diagonal factor entry (value 4 B + ring slot
+        # 2 B) once, per row its right-hand side and inverse diagonal (4 + 4 B) and
+        # write the solution (4 B); gather/scatter move r, S and z (4 + 8 + 4 B)
+        ilt_bytes = factor_offdiag_entries(lib, h, n) * 6 + n * 12 * 2 + n * 16
+        achieved = ilt_bytes / (stage_ms["illt_apply32"] * 1e-3) / 1e9
+        roof = {"kernel": "k_sweep_tma<float>", "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
                 "peak_kind": pk_kind, "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
-                "traffic": traffic.get(("k_trisolve", args.workload)),
-                "note": "level-scheduled sweeps: latency bound (one dependency level per step), not bandwidth bound"}
-    roof["algorithmic_per_launch"] = {"spmv_bytes": spmv_bytes,
+                "traffic": traffic.get(("k_sweep_tma", args.workload)),
+                "note": "level-scheduled sweeps in one CTA: latency bound (one dependency level per step), "
+                        "not bandwidth bound"}
+    roof["algorithmic_per_launch"] = {"spmv_bytes": spmv_bytes, "spmv32_bytes": spmv32_bytes,
                                       "pair_assembly_flops": pairs * PAIR_FLOPS[w["element"]]}
 
     # -------- end to end through the C ABI from host buffers
@@ -299,7 +322,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         t0 = time.perf_counter()
         pe = make_problem(w, T, mesh)
         pe.find_neighbours()
-        te, _ = pe.stationary(tolerance=tol, max_iterations=100000)
+        te, _ = pe.stationary(tolerance=tol, max_iterations=100000, precision=PRIMARY)
         e2e_s.append(time.perf_counter() - t0)
         pe.close()
     e2e = max_over_ranks(dist, sum(e2e_s) / len(e2e_s))
@@ -321,7 +344,8 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         return 0
     line = {
         "metric": METRIC, "value": seconds, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": mean_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "ms_per_step": mean_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 (FP32 inner solve; FP64 assembly, residual, refinement, dots)",
         "data": "synthetic",
         "config": {"workload": w["name"], "mesh": f"{w['nx']}x{w['ny']} {w['element']}",
                    "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",
@@ -330,10 +354,14 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
                        "pair_quadrature_contributions_per_s": pairs * PAIR_QUAD[w["element"]] / seconds,
                        "cg_iterations_per_s": iters / seconds},
         "solve": {"element_pairs": pairs, "nnz_inner_upper": rep.nnz_inner, "nnz_solver_full_padded": nnz_solver,
-                  "cg_iterations": iters, "residual": rep.residual, "reference_residual": rep.reference_residual,
+                  "cg_iterations": iters, "outer_iterations": rep.outer_iterations, "residual": rep.residual,
+                  "reference_residual": rep.reference_residual,
                   "phases_s": {k: getattr(rep, "seconds_" + k) for k in
                                ["neighbours", "pattern", "assembly", "boundary", "preconditioner", "solve"]},
                   "stage_ms": stage_ms, "per_solve_ms": per_solve_ms},
+        "plain_fp64": {"ms_per_step": plain_ms, "cg_iterations": rep_plain.iterations, "residual": rep_plain.residual,
+                       "temperature_rel_l2_vs_primary": float(np.linalg.norm(temp_plain - temp) / np.linalg.norm(temp_plain))},
+        "speedup_vs_plain_fp64": plain_ms / mean_ms,
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),

@@ -88,6 +88,7 @@ typedef struct nlgpu_solve_options {
     int64_t max_iterations;
     int preconditioner;       /* NLGPU_PRECONDITIONER_* */
     int precision;            /* NLGPU_PRECISION_* */
+    double inner_tolerance;   /* MIXED: relative reduction of each FP32 inner solve (<= 0: 1e-4) */
 } nlgpu_solve_options;
 
 typedef struct nlgpu_solve_report {
@@ -101,6 +102,7 @@ typedef struct nlgpu_solve_report {
     int64_t element_pairs;    /* sum over elements of the neighbour count */
     double seconds_neighbours, seconds_pattern, seconds_assembly, seconds_boundary,
            seconds_preconditioner, seconds_solve, seconds_total;
+    int64_t outer_iterations; /* MIXED: FP64 refinement steps (iterations counts the inner ones) */
 } nlgpu_solve_report;
 
 /* ---- library ------------------------------------------------------------ */
@@ -263,7 +265,8 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
  * between two of them; an L2 flush (writes `bytes` of scratch memory); and the
  * average device time of one kernel stage over `reps` launches on the current
  * problem: 0 SpMV of the solver matrix, 1 pair assembly (FULL part),
- * 2 ILLT application (both triangular sweeps), 3 neighbour search. */
+ * 2 ILLT application (both triangular sweeps), 3 neighbour search, 4 FP32
+ * SpMV of the solver matrix, 5 FP32 ILLT application (mixed precision). */
 /* Options of a context: NLGPU_OPTION_GLOBAL_SWEEPS = 1 makes the ILLT
  * triangular sweeps read and write their values in global memory instead of
  * the TMA-fed shared-memory ring (same arithmetic); NLGPU_OPTION_ORDERED_PAIRS

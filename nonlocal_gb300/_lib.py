@@ -43,7 +43,8 @@ class Model2D(ctypes.Structure):
 
 
 class SolveOptions(ctypes.Structure):
-    _fields_ = [("tolerance", c_d), ("max_iterations", c_i64), ("preconditioner", c_int), ("precision", c_int)]
+    _fields_ = [("tolerance", c_d), ("max_iterations", c_i64), ("preconditioner", c_int), ("precision", c_int),
+                ("inner_tolerance", c_d)]
 
 
 class SolveReport(ctypes.Structure):
@@ -51,7 +52,7 @@ class SolveReport(ctypes.Structure):
                 ("preconditioner_shifts", c_int), ("nnz_inner", c_i64), ("nnz_solver", c_i64),
                 ("element_pairs", c_i64), ("seconds_neighbours", c_d), ("seconds_pattern", c_d),
                 ("seconds_assembly", c_d), ("seconds_boundary", c_d), ("seconds_preconditioner", c_d),
-                ("seconds_solve", c_d), ("seconds_total", c_d)]
+                ("seconds_solve", c_d), ("seconds_total", c_d), ("outer_iterations", c_i64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -102,6 +102,7 @@ void fill_report(Ctx& c, nlgpu_solve_report* rep, const CgResult& r) {
     rep->nnz_inner = c.inner.nnz;
     rep->nnz_solver = c.full.nnz;
     rep->element_pairs = c.pairs;
+    rep->outer_iterations = r.outer_iterations;
 }
 
 CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep) {
@@ -120,7 +121,16 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     if (rep) rep->seconds_preconditioner = seconds(t0);
     t0 = std::chrono::steady_clock::now();
     c.temperature.resize(size_t(c.n_nodes));
-    const CgResult r = cg_solve(c, c.full, M, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations, false);
+    NL_REQUIRE(o.precision == NLGPU_PRECISION_FP64 || o.precision == NLGPU_PRECISION_MIXED, NLGPU_ERR_ARG,
+               "unknown precision");
+    CgResult r;
+    if (o.precision == NLGPU_PRECISION_MIXED) {
+        matrix_to_f32(c, c.full);
+        r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations,
+                        o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-4, false);
+    } else {
+        r = cg_solve(c, c.full, M, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations, false);
+    }
     if (rep) rep->seconds_solve = seconds(t0);
     if (M && c.sweep_error.n) {
         int err = 0;
@@ -703,11 +713,16 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
         NL_CUDA(cudaEventCreate(&e0));
         NL_CUDA(cudaEventCreate(&e1));
         dbuf<double> x, y;
-        if (stage == 0 || stage == 2) {
+        dbuf<float> x32, y32;
+        NL_REQUIRE(stage >= 0 && stage <= 5, NLGPU_ERR_ARG, "unknown stage");
+        if (stage == 0 || stage == 2 || stage == 4 || stage == 5) {
             NL_REQUIRE(c.full.nnz > 0, NLGPU_ERR_STATE, "assemble the system first");
             x.resize(size_t(c.n_nodes)); y.resize(size_t(c.n_nodes));
+            x32.resize(size_t(c.n_nodes)); y32.resize(size_t(c.n_nodes));
             NL_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), c.stream));
-            if (stage == 2) NL_REQUIRE(c.ilt.ok, NLGPU_ERR_STATE, "no ILLT factor");
+            NL_CUDA(cudaMemsetAsync(x32.p, 0, x32.bytes(), c.stream));
+            if (stage == 2 || stage == 5) NL_REQUIRE(c.ilt.ok, NLGPU_ERR_STATE, "no ILLT factor");
+            if (stage == 4 && c.full.val32.n != size_t(c.full.nnz)) matrix_to_f32(c, c.full);
         }
         if (stage == 1) NL_REQUIRE(c.inner.nnz > 0 && c.model.nonlocal(), NLGPU_ERR_STATE, "no nonlocal pattern");
         if (stage == 3) NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "no mesh/model");
@@ -717,7 +732,8 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
             else if (stage == 1) assemble_full(c);
             else if (stage == 2) ilt_apply(c, c.ilt, x.p, y.p);
             else if (stage == 3) find_neighbours(c, c.strategy);
-            else throw nlgpu::error{NLGPU_ERR_ARG, "unknown stage"};
+            else if (stage == 4) spmv32(c, c.full, x32.p, y32.p);
+            else ilt_apply32(c, c.ilt, x32.p, y32.p);
         }
         NL_CUDA(cudaEventRecord(e1, c.stream));
         NL_CUDA(cudaEventSynchronize(e1));

@@ -150,20 +150,27 @@ struct TriSlab {
     dbuf<float> val32, inv_diag32;
 };
 
+// Level blocks of a sweep plan for one value type (FP64 or FP32).
+struct SweepLayout {
+    int stage_bytes = 0;
+    size_t smem_bytes = 0;
+    dbuf<unsigned char> blocks;  // per level: values, inverse diagonal, ring slots
+    dbuf<i64> val_dst, inv_dst;  // block byte offset of each factor value source
+};
+
 // Triangular sweep fed by TMA bulk copies with a shared-memory ring (sweep.cu).
 struct SweepPlan {
     bool ok = false;
     i64 n_levels = 0, P = 0;     // levels, padded positions
-    int stage_bytes = 0;
-    size_t smem_bytes = 0;
     dbuf<int32_t> cnt, cntp, width;
     dbuf<ushort4> meta;          // per level: rows, padded rows, width
     dbuf<i64> ppos, block_off;
-    dbuf<unsigned char> blocks;  // per level: values, inverse diagonal, ring slots
     dbuf<int32_t> row_of;        // padded position -> row (-1 padding)
     dbuf<int32_t> ppos_of_row;
-    dbuf<i64> val_dst, val_src, inv_dst, inv_src;   // factor value -> block byte offset
+    dbuf<i64> val_src, inv_src;  // factor value index of each block entry (-1 padding)
+    SweepLayout f64, f32;
     dbuf<double> in, out;        // right-hand side / solution in padded level order
+    dbuf<float> in32, out32;
 };
 
 // CG reduction layout shared by the solver kernels
@@ -200,6 +207,39 @@ struct CgWork {
     dbuf<double> partial;        // block partial sums
     dbuf<double> scalars;        // see solver.cu
     dbuf<int> flags;
+};
+
+// Learned correction on top of ILLT (mpnn.cu): a 4-layer message-passing
+// network of width 64 over the local stiffness graph.  Parameters are packed
+// FP32 [W1 4x64 | W2 128x64 | W3 128x64 | w4 128]; BF16 copies feed the
+// tensor-core GEMMs (stored as uint16_t bit patterns).
+constexpr int MPNN_HIDDEN = 64;
+constexpr long long MPNN_PARAMS = 4 * 64 + 2 * 128 * 64 + 128;
+struct Mpnn {
+    bool ready = false;
+    i64 n = 0, ldt = 0;          // nodes; leading dimension of transposed copies (n rounded up to 8)
+    dbuf<i64> arp;               // A_hat: symmetric, zero diagonal, FP32 weights
+    dbuf<int32_t> acol;
+    dbuf<float> aw;
+    dbuf<float> params, grads, adam_m, adam_v;
+    long long adam_t = 0;
+    dbuf<uint16_t> w2t, w3t, w2b, w3b;   // BF16: [out][in] and [in][out]
+    dbuf<float> u0;              // [n][4]
+    dbuf<uint16_t> u1, u2, u3;   // [n][128] BF16: [H | A_hat H]
+    dbuf<uint16_t> u1t, u2t;     // [128][ldt] transposed (training)
+    dbuf<uint16_t> dp, dpt;      // [n][64] and [64][ldt] BF16 (training)
+    dbuf<float> du, dp32, d, ad; // training work
+    dbuf<double> part, part2, ee64;
+    dbuf<float> sc;              // scalars (1/rms r, 1/rms z, rms z, ...)
+    dbuf<int> error;
+};
+
+// Device state of the mixed-precision solve (mixed.cu).
+struct MixedWork {
+    i64 n = 0;
+    dbuf<double> r64, q64;       // outer residual and A x
+    dbuf<float> r, z, p, q, d;   // inner vectors
+    dbuf<double> partial, outer, flags;
 };
 
 struct Ctx {
@@ -246,6 +286,8 @@ struct Ctx {
     IncompleteCholesky plugin_ilt;   // nlgpu_illt_compute / nlgpu_illt_solve
     bool plugin_ilt_ready = false;
     CgWork cg;
+    MixedWork mx;
+    Mpnn mp;
     // nonstationary
     Csr capacity_m, capacity_full;
     dbuf<i64> capacity_map;
@@ -294,7 +336,11 @@ void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values);
 void spmv_full(Ctx& ctx, const Csr& A, const double* x, double* y);
 void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic);
 void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* z);
-struct CgResult { i64 iterations = 0; double residual = 0, reference_residual = 0; bool converged = false; };
+struct CgResult {
+    i64 iterations = 0, outer_iterations = 0;
+    double residual = 0, reference_residual = 0;
+    bool converged = false;
+};
 CgResult cg_solve(Ctx& ctx, const Csr& A_full, const IncompleteCholesky* M, const double* b, double* x,
                   double tolerance, i64 max_iterations, bool x_is_initial_guess);
 // sweep.cu
@@ -304,6 +350,24 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
 void sweep_plan_fill(Ctx& ctx, SweepPlan& plan, const double* u);
 void sweep_apply(Ctx& ctx, IncompleteCholesky& ic, const double* r, double* z, const double* partials,
                  const double* flags, double tol2);
+void sweep_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, const double* partials,
+                   const double* flags, double tol2);
+// mixed.cu
+void matrix_to_f32(Ctx& ctx, Csr& A);
+void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y);
+void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z);
+CgResult mixed_solve(Ctx& ctx, const Csr& A_full, IncompleteCholesky* M, const double* b, double* x, double tolerance,
+                     i64 max_iterations, double inner_tolerance, bool x_is_initial_guess);
+// mpnn.cu
+void mpnn_prepare(Ctx& ctx, const Csr& local_upper);
+void mpnn_init_weights(Ctx& ctx, unsigned seed);
+void mpnn_set_weights(Ctx& ctx, const float* host);
+void mpnn_get_weights(Ctx& ctx, float* host);
+void mpnn_apply(Ctx& ctx, const float* r, const float* z, float* out, bool training);
+void mpnn_backward(Ctx& ctx, const Csr& A, const float* r, const float* z, const float* e, float* p_out,
+                   double* loss_num, double* ee_out);
+void mpnn_adam_step(Ctx& ctx, float lr, int batch);
+void mpnn_check(Ctx& ctx);
 // noalloc.cu
 void cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, const double* val, const double* b,
                       double* x, double tolerance, i64 max_iterations, i64* iterations, double* residual);

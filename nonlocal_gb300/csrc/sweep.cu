@@ -158,15 +158,13 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_tma(SweepArgs<T> a) {
 }
 
 // level order <-> node order
-template<class T>
+template<class T, class R>
 __global__ void k_gather_scaled(i64 P, const int32_t* __restrict__ row_of, const double* __restrict__ scale,
-                                const double* __restrict__ r, T* __restrict__ out, const double* __restrict__ partials,
-                                const double* __restrict__ flags, double tol2) {
+                                const R* __restrict__ r, T* __restrict__ out) {
     for (i64 p = blockIdx.x * i64(blockDim.x) + threadIdx.x; p < P; p += i64(gridDim.x) * blockDim.x) {
         const int32_t row = row_of[p];
-        out[p] = row >= 0 ? T(scale[row] * r[row]) : T(0);
+        out[p] = row >= 0 ? T(scale[row] * double(r[row])) : T(0);
     }
-    (void)partials; (void)flags; (void)tol2;
 }
 
 template<class T>
@@ -178,21 +176,24 @@ __global__ void k_transfer(i64 P, const int32_t* __restrict__ row_of_b, const in
     }
 }
 
-template<class T>
+template<class T, class Z>
 __global__ void k_scatter_scaled(i64 P, const int32_t* __restrict__ row_of, const double* __restrict__ scale,
-                                 const T* __restrict__ in, double* __restrict__ z) {
+                                 const T* __restrict__ in, Z* __restrict__ z) {
     for (i64 p = blockIdx.x * i64(blockDim.x) + threadIdx.x; p < P; p += i64(gridDim.x) * blockDim.x) {
         const int32_t row = row_of[p];
-        if (row >= 0) z[row] = scale[row] * double(in[p]);
+        if (row >= 0) z[row] = Z(scale[row] * double(in[p]));
     }
 }
 
-__global__ void k_fill_blocks_f64(i64 count, const i64* __restrict__ dst_off, const i64* __restrict__ src,
-                                  const double* __restrict__ u, bool invert, unsigned char* __restrict__ blocks) {
+// factor values (FP64) into the level blocks, as T; the inverse diagonal is
+// formed in FP64 before the conversion
+template<class T>
+__global__ void k_fill_blocks(i64 count, const i64* __restrict__ dst_off, const i64* __restrict__ src,
+                              const double* __restrict__ u, bool invert, unsigned char* __restrict__ blocks) {
     for (i64 k = blockIdx.x * i64(blockDim.x) + threadIdx.x; k < count; k += i64(gridDim.x) * blockDim.x) {
         double v = src[k] >= 0 ? u[src[k]] : 0.0;
         if (invert) v = src[k] >= 0 ? 1.0 / v : 0.0;
-        *reinterpret_cast<double*>(blocks + dst_off[k]) = v;
+        *reinterpret_cast<T*>(blocks + dst_off[k]) = T(v);
     }
 }
 
@@ -208,8 +209,6 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
     std::vector<int32_t> cnt(static_cast<size_t>(L)), cntp(static_cast<size_t>(L)), width(static_cast<size_t>(L));
     std::vector<i64> ppos(static_cast<size_t>(L + 1), 0), block_off(static_cast<size_t>(L));
     std::vector<int32_t> ppos_of_row(static_cast<size_t>(n));
-    i64 bytes = 0;
-    int max_stage = 0;
     for (i64 l = 0; l < L; ++l) {
         const int c = int(lev_ptr[size_t(l) + 1] - lev_ptr[size_t(l)]);
         int w = 0;
@@ -222,56 +221,71 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
         width[size_t(l)] = w;
         ppos[size_t(l) + 1] = ppos[size_t(l)] + cntp[size_t(l)];
         for (int t = 0; t < c; ++t) ppos_of_row[size_t(rows[size_t(lev_ptr[size_t(l)] + t)])] = int32_t(ppos[size_t(l)] + t);
-        const i64 blk = (i64(w) * cntp[size_t(l)] * (8 + 2) + i64(cntp[size_t(l)]) * 8 + 15) / 16 * 16;
-        block_off[size_t(l)] = bytes;
-        bytes += blk;
-        max_stage = std::max<int>(max_stage, int(blk + i64(cntp[size_t(l)]) * 8));
     }
     const i64 P = ppos[size_t(L)];
-    // dependency distances must fit the ring, stages must fit shared memory
-    std::vector<int16_t> dep_all;
-    std::vector<i64> val_dst, val_src, inv_dst, inv_src;
-    std::vector<unsigned char> dep_bytes(static_cast<size_t>(bytes), 0);
+    // Level blocks for one value size es (8: FP64 sweeps, 4: FP32 sweeps); the
+    // factor-value sources (val_src, inv_src) are the same for both.
+    std::vector<i64> val_src, inv_src;
     i64 max_dist = 0;
-    for (i64 l = 0; l < L; ++l) {
-        const int c = cnt[size_t(l)], cp = cntp[size_t(l)], w = width[size_t(l)];
-        const i64 vbase = block_off[size_t(l)];
-        const i64 ibase = vbase + i64(w) * cp * 8;
-        const i64 dbase = ibase + i64(cp) * 8;
-        for (int t = 0; t < cp; ++t) {
-            const bool real = t < c;
-            const int32_t r = real ? rows[size_t(lev_ptr[size_t(l)] + t)] : -1;
-            inv_dst.push_back(ibase + i64(t) * 8);
-            inv_src.push_back(real ? val_index[size_t(diag_pos[size_t(r)])] : -1);
-            int k = 0;
-            if (real)
-                for (i64 s = rp[size_t(r)]; s < rp[size_t(r) + 1]; ++s) {
-                    if (s == diag_pos[size_t(r)]) continue;
-                    const i64 dp = ppos_of_row[size_t(col[size_t(s)])];
-                    max_dist = std::max(max_dist, ppos[size_t(l) + 1] - dp);
-                    const int16_t slot = int16_t(dp & (SW_RING - 1));
+    auto layout = [&](int es, SweepLayout& out, std::vector<unsigned char>& dep_bytes, std::vector<i64>& val_dst,
+                      std::vector<i64>& inv_dst, std::vector<i64>& block_off_out, bool record_src) {
+        i64 bytes = 0;
+        int max_stage = 0;
+        for (i64 l = 0; l < L; ++l) {
+            const i64 cp = cntp[size_t(l)], w = width[size_t(l)];
+            const i64 blk = (w * cp * (es + 2) + cp * es + 15) / 16 * 16;
+            block_off_out[size_t(l)] = bytes;
+            bytes += blk;
+            max_stage = std::max<int>(max_stage, int(blk + cp * es));
+        }
+        dep_bytes.assign(static_cast<size_t>(bytes), 0);
+        for (i64 l = 0; l < L; ++l) {
+            const int c = cnt[size_t(l)], cp = cntp[size_t(l)], w = width[size_t(l)];
+            const i64 vbase = block_off_out[size_t(l)];
+            const i64 ibase = vbase + i64(w) * cp * es;
+            const i64 dbase = ibase + i64(cp) * es;
+            for (int t = 0; t < cp; ++t) {
+                const bool real = t < c;
+                const int32_t r = real ? rows[size_t(lev_ptr[size_t(l)] + t)] : -1;
+                inv_dst.push_back(ibase + i64(t) * es);
+                if (record_src) inv_src.push_back(real ? val_index[size_t(diag_pos[size_t(r)])] : -1);
+                int k = 0;
+                if (real)
+                    for (i64 s = rp[size_t(r)]; s < rp[size_t(r) + 1]; ++s) {
+                        if (s == diag_pos[size_t(r)]) continue;
+                        const i64 dp = ppos_of_row[size_t(col[size_t(s)])];
+                        max_dist = std::max(max_dist, ppos[size_t(l) + 1] - dp);
+                        const int16_t slot = int16_t(dp & (SW_RING - 1));
+                        std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 2)], &slot, 2);
+                        val_dst.push_back(vbase + (i64(k) * cp + t) * es);
+                        if (record_src) val_src.push_back(val_index[size_t(s)]);
+                        ++k;
+                    }
+                for (; k < w; ++k) {
+                    const int16_t slot = int16_t(SW_ZERO);
                     std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 2)], &slot, 2);
-                    val_dst.push_back(vbase + (i64(k) * cp + t) * 8);
-                    val_src.push_back(val_index[size_t(s)]);
-                    ++k;
+                    val_dst.push_back(vbase + (i64(k) * cp + t) * es);
+                    if (record_src) val_src.push_back(-1);
                 }
-            for (; k < w; ++k) {
-                const int16_t slot = int16_t(SW_ZERO);
-                std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 2)], &slot, 2);
-                val_dst.push_back(vbase + (i64(k) * cp + t) * 8);
-                val_src.push_back(-1);
             }
         }
-    }
-    const size_t smem = ((sizeof(double) * (SW_RING + 1) + 127) / 128) * 128 + size_t(max_stage) * SW_STAGES +
-                        SW_STAGES * sizeof(uint64_t) + size_t(L) * sizeof(ushort4);
+        out.stage_bytes = max_stage;
+        out.smem_bytes = ((size_t(es) * (SW_RING + 1) + 127) / 128) * 128 + size_t(max_stage) * SW_STAGES +
+                         SW_STAGES * sizeof(uint64_t) + size_t(L) * sizeof(ushort4);
+    };
+    std::vector<unsigned char> dep64, dep32;
+    std::vector<i64> val_dst64, inv_dst64, val_dst32, inv_dst32;
+    std::vector<i64> block_off32(static_cast<size_t>(L));
+    layout(8, plan.f64, dep64, val_dst64, inv_dst64, block_off, true);
+    layout(4, plan.f32, dep32, val_dst32, inv_dst32, block_off32, false);
     std::vector<ushort4> meta(static_cast<size_t>(L));
     bool small = true;
     for (i64 l = 0; l < L; ++l) {
         small = small && cntp[size_t(l)] < 65536 && width[size_t(l)] < 65536;
         meta[size_t(l)] = make_ushort4(uint16_t(cnt[size_t(l)]), uint16_t(cntp[size_t(l)]), uint16_t(width[size_t(l)]), 0);
     }
-    plan.ok = small && max_dist <= SW_RING && smem <= 220 * 1024 && n < (i64(1) << 31);
+    // dependency distances must fit the ring, stages must fit shared memory
+    plan.ok = small && max_dist <= SW_RING && plan.f64.smem_bytes <= 220 * 1024 && n < (i64(1) << 31);
     if (!plan.ok) return false;
     plan.meta.upload(meta.data(), meta.size(), ctx.stream);
     std::vector<int32_t> row_of(static_cast<size_t>(P), -1);
@@ -279,46 +293,59 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
         for (int t = 0; t < cnt[size_t(l)]; ++t) row_of[size_t(ppos[size_t(l)] + t)] = rows[size_t(lev_ptr[size_t(l)] + t)];
     plan.n_levels = L;
     plan.P = P;
-    plan.stage_bytes = max_stage;
-    plan.smem_bytes = smem;
     plan.cnt.upload(cnt.data(), cnt.size(), ctx.stream);
     plan.cntp.upload(cntp.data(), cntp.size(), ctx.stream);
     plan.width.upload(width.data(), width.size(), ctx.stream);
     plan.ppos.upload(ppos.data(), ppos.size(), ctx.stream);
     plan.block_off.upload(block_off.data(), block_off.size(), ctx.stream);
-    plan.blocks.upload(dep_bytes.data(), dep_bytes.size(), ctx.stream);   // dependency slots; values filled later
     plan.row_of.upload(row_of.data(), row_of.size(), ctx.stream);
     plan.ppos_of_row.upload(ppos_of_row.data(), ppos_of_row.size(), ctx.stream);
-    plan.val_dst.upload(val_dst.data(), val_dst.size(), ctx.stream);
     plan.val_src.upload(val_src.data(), val_src.size(), ctx.stream);
-    plan.inv_dst.upload(inv_dst.data(), inv_dst.size(), ctx.stream);
     plan.inv_src.upload(inv_src.data(), inv_src.size(), ctx.stream);
+    // dependency slots now, values by sweep_plan_fill
+    plan.f64.blocks.upload(dep64.data(), dep64.size(), ctx.stream);
+    plan.f64.val_dst.upload(val_dst64.data(), val_dst64.size(), ctx.stream);
+    plan.f64.inv_dst.upload(inv_dst64.data(), inv_dst64.size(), ctx.stream);
+    plan.f32.blocks.upload(dep32.data(), dep32.size(), ctx.stream);
+    plan.f32.val_dst.upload(val_dst32.data(), val_dst32.size(), ctx.stream);
+    plan.f32.inv_dst.upload(inv_dst32.data(), inv_dst32.size(), ctx.stream);
     plan.in.resize(size_t(P)); plan.out.resize(size_t(P));
+    plan.in32.resize(size_t(P)); plan.out32.resize(size_t(P));
     NL_CUDA(cudaStreamSynchronize(ctx.stream));
     return true;
 }
 
 void sweep_plan_fill(Ctx& ctx, SweepPlan& plan, const double* u) {
     const i64 nv = i64(plan.val_src.n), ni = i64(plan.inv_src.n);
-    if (nv) NL_LAUNCH(k_fill_blocks_f64, grid_for(nv, 256), 256, 0, ctx.stream, nv, plan.val_dst.p, plan.val_src.p, u, false,
-                      plan.blocks.p);
-    NL_LAUNCH(k_fill_blocks_f64, grid_for(ni, 256), 256, 0, ctx.stream, ni, plan.inv_dst.p, plan.inv_src.p, u, true,
-              plan.blocks.p);
+    if (nv) {
+        NL_LAUNCH(k_fill_blocks<double>, grid_for(nv, 256), 256, 0, ctx.stream, nv, plan.f64.val_dst.p, plan.val_src.p, u,
+                  false, plan.f64.blocks.p);
+        NL_LAUNCH(k_fill_blocks<float>, grid_for(nv, 256), 256, 0, ctx.stream, nv, plan.f32.val_dst.p, plan.val_src.p, u,
+                  false, plan.f32.blocks.p);
+    }
+    NL_LAUNCH(k_fill_blocks<double>, grid_for(ni, 256), 256, 0, ctx.stream, ni, plan.f64.inv_dst.p, plan.inv_src.p, u, true,
+              plan.f64.blocks.p);
+    NL_LAUNCH(k_fill_blocks<float>, grid_for(ni, 256), 256, 0, ctx.stream, ni, plan.f32.inv_dst.p, plan.inv_src.p, u, true,
+              plan.f32.blocks.p);
 }
 
+template<class T>
 static void run_sweep(Ctx& ctx, SweepPlan& plan, const double* partials, const double* flags, double tol2) {
-    SweepArgs<double> a{};
+    const SweepLayout& lay = sizeof(T) == 8 ? plan.f64 : plan.f32;
+    SweepArgs<T> a{};
     a.n_levels = plan.n_levels; a.meta = plan.meta.p;
-    a.blocks = plan.blocks.p; a.in = plan.in.p; a.out = plan.out.p;
-    a.stage_bytes = plan.stage_bytes; a.partials = partials; a.flags = flags; a.tol2 = tol2;
+    a.blocks = lay.blocks.p;
+    if constexpr (sizeof(T) == 8) { a.in = plan.in.p; a.out = plan.out.p; }
+    else { a.in = plan.in32.p; a.out = plan.out32.p; }
+    a.stage_bytes = lay.stage_bytes; a.partials = partials; a.flags = flags; a.tol2 = tol2;
     ctx.sweep_error.reserve(1);
     a.error = ctx.sweep_error.p;
     static bool attr_set = false;
     if (!attr_set) {
-        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
         attr_set = true;
     }
-    NL_LAUNCH(k_sweep_tma<double>, 1, SW_THREADS, plan.smem_bytes, ctx.stream, a);
+    NL_LAUNCH(k_sweep_tma<T>, 1, SW_THREADS, lay.smem_bytes, ctx.stream, a);
 }
 
 // z = S U^-1 U^-T S r with the TMA sweeps (forward plan on U^T, backward on U)
@@ -326,12 +353,29 @@ void sweep_apply(Ctx& ctx, IncompleteCholesky& ic, const double* r, double* z, c
                  const double* flags, double tol2) {
     SweepPlan& F = ic.fwd_plan;
     SweepPlan& B = ic.bwd_plan;
-    NL_LAUNCH(k_gather_scaled<double>, grid_for(F.P, 256), 256, 0, ctx.stream, F.P, F.row_of.p, ic.scale.p, r, F.in.p,
-              partials, flags, tol2);
-    run_sweep(ctx, F, partials, flags, tol2);
+    NL_LAUNCH((k_gather_scaled<double, double>), grid_for(F.P, 256), 256, 0, ctx.stream, F.P, F.row_of.p, ic.scale.p, r,
+              F.in.p);
+    run_sweep<double>(ctx, F, partials, flags, tol2);
     NL_LAUNCH(k_transfer<double>, grid_for(B.P, 256), 256, 0, ctx.stream, B.P, B.row_of.p, F.ppos_of_row.p, F.out.p, B.in.p);
-    run_sweep(ctx, B, partials, flags, tol2);
-    NL_LAUNCH(k_scatter_scaled<double>, grid_for(B.P, 256), 256, 0, ctx.stream, B.P, B.row_of.p, ic.scale.p, B.out.p, z);
+    run_sweep<double>(ctx, B, partials, flags, tol2);
+    NL_LAUNCH((k_scatter_scaled<double, double>), grid_for(B.P, 256), 256, 0, ctx.stream, B.P, B.row_of.p, ic.scale.p,
+              B.out.p, z);
+}
+
+// The same with FP32 factor values, right-hand side and solution (the inner
+// solve of the mixed-precision form); the scaling S stays FP64.
+void sweep_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, const double* partials,
+                   const double* flags, double tol2) {
+    SweepPlan& F = ic.fwd_plan;
+    SweepPlan& B = ic.bwd_plan;
+    NL_LAUNCH((k_gather_scaled<float, float>), grid_for(F.P, 256), 256, 0, ctx.stream, F.P, F.row_of.p, ic.scale.p, r,
+              F.in32.p);
+    run_sweep<float>(ctx, F, partials, flags, tol2);
+    NL_LAUNCH(k_transfer<float>, grid_for(B.P, 256), 256, 0, ctx.stream, B.P, B.row_of.p, F.ppos_of_row.p, F.out32.p,
+              B.in32.p);
+    run_sweep<float>(ctx, B, partials, flags, tol2);
+    NL_LAUNCH((k_scatter_scaled<float, float>), grid_for(B.P, 256), 256, 0, ctx.stream, B.P, B.row_of.p, ic.scale.p,
+              B.out32.p, z);
 }
 
 }  // namespace nlgpu

@@ -212,15 +212,18 @@ class Problem2D(Context):
 
     # ---- solves -----------------------------------------------------------------
     @staticmethod
-    def _options(tolerance, max_iterations, preconditioner, precision) -> L.SolveOptions:
+    def _options(tolerance, max_iterations, preconditioner, precision, inner_tolerance=0.0) -> L.SolveOptions:
         o = L.SolveOptions()
         o.tolerance, o.max_iterations = float(tolerance), int(max_iterations)
         o.preconditioner, o.precision = L.PRECONDITIONER[preconditioner], L.PRECISION[precision]
+        o.inner_tolerance = float(inner_tolerance)
         return o
 
     def stationary(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64",
-                   check_convergence=True):
-        o = self._options(tolerance, max_iterations, preconditioner, precision)
+                   check_convergence=True, inner_tolerance=0.0):
+        """stationary_heat_equation_solver_2d; precision "mixed" runs the FP32 inner
+        solve with FP64 refinement (inner_tolerance: reduction per inner solve)."""
+        o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance)
         t = np.empty(self.n_nodes)
         rep = L.SolveReport()
         rc = self._lib.nlgpu_stationary_2d(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep))
@@ -228,8 +231,9 @@ class Problem2D(Context):
             L.check(rc)
         return t, SolveReport(rep.as_dict())
 
-    def solve_assembled(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64"):
-        o = self._options(tolerance, max_iterations, preconditioner, precision)
+    def solve_assembled(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64",
+                        inner_tolerance=0.0):
+        o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance)
         t = np.empty(self.n_nodes)
         rep = L.SolveReport()
         L.check(self._lib.nlgpu_solve_assembled(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep)))
