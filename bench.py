@@ -11,11 +11,15 @@ mesh, deterministic.
 One step = one stationary solve from the resident mesh: neighbour search,
 sparsity patterns, nonlocal + local assembly (FP64), boundary conditions,
 ILLT factorisation and the solve.  value = device time per solve of the
-mixed-precision form (FP32 inner flexible CG with FP32 ILLT sweeps, FP64
-iterative refinement) by CUDA events on the library's stream, L2 flushed
-between steps; the plain FP64 ILLT-CG solve is timed the same way and
-reported beside it.  e2e = the mixed solve through the C ABI from host
-buffers (mesh upload and temperature download included).
+learned mixed-precision form (flexible CG in FP32 with FP32 ILLT sweeps plus
+the message-passing correction, FP64 reliable updates of the residual and
+solution) by CUDA events on the library's stream, L2 flushed between steps;
+the network is trained once beforehand on (r, e) pairs the plain solver
+harvests from the same system (its time is reported apart).  The same
+solve without the correction and the plain FP64 ILLT-CG solve are timed
+the same way and reported beside it.  e2e = the learned solve through the
+C ABI from host buffers (mesh, weights upload and temperature download
+included).
 
 --impl reference times the reference algorithm on the host cores instead
 (the CPU restatement in oracle/, all threads), same workload and metric.
@@ -36,9 +40,12 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = ("time to 1e-10 relative residual, nonlocal stationary 2D solve (full pipeline): mixed-precision FCG "
-          "(FP32 inner, FP64 refinement) with ILLT; plain FP64 ILLT-CG beside it")
-PRIMARY = "mixed"
+METRIC = ("time to 1e-10 relative residual, nonlocal stationary 2D solve (full pipeline): learned mixed-precision "
+          "FCG (ILLT + message-passing correction, FP32 inner, FP64 reliable updates); plain FP64 ILLT-CG beside it")
+PRIMARY = "learned"
+# method -> (precision, preconditioner)
+METHODS = {"learned": ("mixed", "illt_learned"), "mixed": ("mixed", "illt"), "plain": ("fp64", "illt")}
+LEARNED_TRAINING = dict(right_hand_sides=4, epochs=20, batch=4, learning_rate=2e-3, seed=0)
 
 WORKLOADS = {
     "config2": dict(name="200x200 bilinear, fast_polynomial r=0.05, p1=0.5, left T=0 / right flux 1, FP64 ILLT-CG 1e-10",
@@ -222,17 +229,18 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     h = pb.handle
     tol = w["tolerance"]
 
-    def step(precision):
+    def step(method):
+        precision, pre = METHODS[method]
         pb.find_neighbours()
-        return pb.stationary(tolerance=tol, max_iterations=100000, precision=precision)
+        return pb.stationary(tolerance=tol, max_iterations=100000, precision=precision, preconditioner=pre)
 
-    def timed(precision):
+    def timed(method):
         """K device-timed solves (CUDA events on the library's stream), L2 flushed before each."""
         ms_steps, reports = [], []
         for k in range(args.steps):
             L.check(lib.nlgpu_flush_l2(h, L2_FLUSH_BYTES))
             L.check(lib.nlgpu_event_record(h, 0))
-            t_, rep_ = step(precision)
+            t_, rep_ = step(method)
             L.check(lib.nlgpu_event_record(h, 1))
             ms = ctypes.c_double()
             L.check(lib.nlgpu_event_elapsed(h, 0, 1, ctypes.byref(ms)))
@@ -241,9 +249,15 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         return ms_steps, reports, t_
 
     for _ in range(args.warmup):
+        step("plain")
+        step("mixed")
+    # the learned correction is trained once per operator, on pairs the plain
+    # solver harvests from this system (not timed as part of a solve)
+    train = pb.train_learned_preconditioner(**LEARNED_TRAINING)
+    learned_weights = pb.learned_weights()
+    for _ in range(args.warmup):
         step(PRIMARY)
-        step("fp64")
-    # -------- timed region: the primary method, then the plain FP64 method
+    # -------- timed region: the primary method, then the other two
     sampler = ClockSampler(local)
     launches0 = L.kernel_launches()
     barrier(dist)
@@ -252,12 +266,15 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     ms_steps, reports, temp = timed(PRIMARY)
     L.check(lib.nlgpu_synchronize(h))
     launches = L.kernel_launches() - launches0
-    ms_plain, reports_plain, temp_plain = timed("fp64")
+    ms_mixed, reports_mixed, temp_mixed = timed("mixed")
+    ms_plain, reports_plain, temp_plain = timed("plain")
     L.check(lib.nlgpu_synchronize(h))
     clocks = sampler.stop()
     barrier(dist)
     mean_ms = max_over_ranks(dist, sum(ms_steps) / len(ms_steps))
+    mixed_ms = max_over_ranks(dist, sum(ms_mixed) / len(ms_mixed))
     plain_ms = max_over_ranks(dist, sum(ms_plain) / len(ms_plain))
+    rep_mixed = reports_mixed[-1]
     seconds = mean_ms / 1e3
     rep = reports[-1]
     rep_plain = reports_plain[-1]
@@ -316,13 +333,15 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     e2e_s = []
     import numpy as np
     h2d = mesh.nodes.nbytes + mesh.n_elements * mesh.nodes_per_element * 8 + sum(
-        mesh.boundaries[g].size * 8 for g, _, _ in w["bcs"])
+        mesh.boundaries[g].size * 8 for g, _, _ in w["bcs"]) + learned_weights.nbytes
     d2h = n * 8
     for k in range(max(1, min(args.steps, 5))):
         t0 = time.perf_counter()
         pe = make_problem(w, T, mesh)
         pe.find_neighbours()
-        te, _ = pe.stationary(tolerance=tol, max_iterations=100000, precision=PRIMARY)
+        pe.set_learned_weights(learned_weights)
+        te, _ = pe.stationary(tolerance=tol, max_iterations=100000, precision=METHODS[PRIMARY][0],
+                              preconditioner=METHODS[PRIMARY][1])
         e2e_s.append(time.perf_counter() - t0)
         pe.close()
     e2e = max_over_ranks(dist, sum(e2e_s) / len(e2e_s))
@@ -359,6 +378,9 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
                   "phases_s": {k: getattr(rep, "seconds_" + k) for k in
                                ["neighbours", "pattern", "assembly", "boundary", "preconditioner", "solve"]},
                   "stage_ms": stage_ms, "per_solve_ms": per_solve_ms},
+        "learned_training": dict(train, **{"config": LEARNED_TRAINING}),
+        "mixed_illt": {"ms_per_step": mixed_ms, "cg_iterations": rep_mixed.iterations,
+                       "reliable_updates": rep_mixed.outer_iterations, "residual": rep_mixed.residual},
         "plain_fp64": {"ms_per_step": plain_ms, "cg_iterations": rep_plain.iterations, "residual": rep_plain.residual,
                        "temperature_rel_l2_vs_primary": float(np.linalg.norm(temp_plain - temp) / np.linalg.norm(temp_plain))},
         "speedup_vs_plain_fp64": plain_ms / mean_ms,

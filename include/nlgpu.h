@@ -65,7 +65,9 @@ enum { NLGPU_BC_TEMPERATURE = 0, NLGPU_BC_FLUX = 1 };
 enum { NLGPU_MATRIX_INNER = 0, NLGPU_MATRIX_BOUND = 1, NLGPU_MATRIX_LOCAL = 2 };
 
 /* preconditioners of the conjugate gradient */
-enum { NLGPU_PRECONDITIONER_IDENTITY = 0, NLGPU_PRECONDITIONER_ILLT = 1 };
+/* ILLT_LEARNED: ILLT plus the learned correction (see nlgpu_mpnn_*); it always
+ * runs in the mixed-precision flexible CG */
+enum { NLGPU_PRECONDITIONER_IDENTITY = 0, NLGPU_PRECONDITIONER_ILLT = 1, NLGPU_PRECONDITIONER_ILLT_LEARNED = 2 };
 
 /* precision of the solve */
 enum { NLGPU_PRECISION_FP64 = 0, NLGPU_PRECISION_MIXED = 1 };
@@ -214,6 +216,43 @@ int nlgpu_illt_compute(nlgpu_ctx* ctx, int64_t n, const int64_t* rowptr, const i
                        int* computation_info);
 int nlgpu_illt_solve(nlgpu_ctx* ctx, int64_t n, const double* x, double* y);
 
+/* ---- learned correction on top of ILLT (no counterpart in the reference) ----
+ * A 4-layer message-passing network (width 64, tanh, no biases) over the
+ * graph of the local stiffness pattern, A_hat = D^-1/2 |offdiag K_local| D^-1/2:
+ *   X0 = [r / rms(r), z / rms(z)] with z = ILLT^-1 r,  U0 = [X0, A_hat X0],
+ *   H1 = tanh(U0 W1), H2 = tanh([H1, A_hat H1] W2), H3 = tanh([H2, A_hat H2] W3),
+ *   P(r) = z + rms(z) [H3, A_hat H3] w4.
+ * W2, W3 run as BF16 tensor-core GEMMs with FP32 accumulation.  Parameters
+ * are NLGPU_MPNN_PARAMS floats packed [W1 4x64 | W2 128x64 | W3 128x64 | w4 128]
+ * (row-major, input x output).  The correction is used by the solves with
+ * NLGPU_PRECONDITIONER_ILLT_LEARNED (inside the mixed-precision flexible CG,
+ * switched off for the rest of a solve when it stalls).
+ * train: on the context's assembled system (after nlgpu_conductivity_matrix_2d
+ * and boundary conditions): harvests (r, e) pairs from plain FP64 ILLT-CG runs
+ * on the system's right-hand side and random ones (x_k every 16 iterations,
+ * e = x* - x_k, r = A e), then minimises (P(r) - e)^T A (P(r) - e) / e^T A e
+ * with Adam.  loss_grad: one pair on the assembled system; writes z, P(r), the
+ * loss and its gradient (packed like the parameters); the weights do not change. */
+#define NLGPU_MPNN_PARAMS 16768
+typedef struct nlgpu_train_options {
+    int right_hand_sides;     /* solves harvested (the first uses the system's own right-hand side) */
+    int epochs;
+    int batch;                /* pairs per Adam step */
+    double learning_rate;
+    unsigned seed;
+} nlgpu_train_options;
+typedef struct nlgpu_train_report {
+    int64_t samples, steps;
+    double loss_illt;         /* mean loss of ILLT alone on the pairs */
+    double loss_first, loss_last;   /* mean loss after the first / last epoch */
+    double seconds_harvest, seconds_train;
+} nlgpu_train_report;
+int nlgpu_mpnn_set_weights(nlgpu_ctx* ctx, const float* params);
+int nlgpu_mpnn_get_weights(nlgpu_ctx* ctx, float* params);
+int nlgpu_mpnn_train(nlgpu_ctx* ctx, const nlgpu_train_options* options, nlgpu_train_report* report);
+int nlgpu_mpnn_loss_grad(nlgpu_ctx* ctx, const float* r, const float* e, float* z, float* p, double* loss,
+                         float* grad);
+
 /* ---- conjugate gradient that allocates nothing (no counterpart in the reference)
  * For callers that cannot allocate device memory when they solve (an external
  * memory budget or pool, a loop that must not touch the allocator, buffers
@@ -278,6 +317,11 @@ int nlgpu_event_record(nlgpu_ctx* ctx, int slot);
 int nlgpu_event_elapsed(nlgpu_ctx* ctx, int start_slot, int stop_slot, double* milliseconds);
 int nlgpu_flush_l2(nlgpu_ctx* ctx, int64_t bytes);
 int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* milliseconds);
+/* The learned correction's tensor-core GEMM on its own (for checking it):
+ * C[M x N] = A[M x K] . B[N x K]^T with A, B BF16 bit patterns (K contiguous,
+ * K a multiple of 8), N 64 or 128, FP32 accumulation and output; splits > 1
+ * splits K over CTAs that add with FP32 atomics. */
+int nlgpu_gemm_bf16(int64_t M, int N, int64_t K, int splits, const uint16_t* A, const uint16_t* B, float* C);
 
 #ifdef __cplusplus
 }

@@ -27,7 +27,7 @@ EXPAND = {"NO": 0, "MAX": 1, "MIN": 2, "MEAN": 3}
 PART_LOCAL, PART_FULL = 0, 2
 BC_TEMPERATURE, BC_FLUX = 0, 1
 MATRIX_INNER, MATRIX_BOUND, MATRIX_LOCAL = 0, 1, 2
-PRECONDITIONER = {"identity": 0, "illt": 1}
+PRECONDITIONER = {"identity": 0, "illt": 1, "illt_learned": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
 
 
@@ -57,6 +57,21 @@ class SolveReport(ctypes.Structure):
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
 
+
+class TrainOptions(ctypes.Structure):
+    _fields_ = [("right_hand_sides", c_int), ("epochs", c_int), ("batch", c_int), ("learning_rate", c_d),
+                ("seed", ctypes.c_uint)]
+
+
+class TrainReport(ctypes.Structure):
+    _fields_ = [("samples", c_i64), ("steps", c_i64), ("loss_illt", c_d), ("loss_first", c_d), ("loss_last", c_d),
+                ("seconds_harvest", c_d), ("seconds_train", c_d)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+MPNN_PARAMS = 16768
 
 # name -> (restype, argtypes); every function declared in include/nlgpu.h
 SIGNATURES = {
@@ -99,6 +114,11 @@ SIGNATURES = {
     "nlgpu_event_elapsed": (c_int, [c_p, c_int, c_int, ctypes.POINTER(c_d)]),
     "nlgpu_flush_l2": (c_int, [c_p, c_i64]),
     "nlgpu_time_stage": (c_int, [c_p, c_int, c_int, ctypes.POINTER(c_d)]),
+    "nlgpu_gemm_bf16": (c_int, [c_i64, c_int, c_i64, c_int, c_p, c_p, c_p]),
+    "nlgpu_mpnn_set_weights": (c_int, [c_p, c_p]),
+    "nlgpu_mpnn_get_weights": (c_int, [c_p, c_p]),
+    "nlgpu_mpnn_train": (c_int, [c_p, ctypes.POINTER(TrainOptions), ctypes.POINTER(TrainReport)]),
+    "nlgpu_mpnn_loss_grad": (c_int, [c_p, c_p, c_p, c_p, c_p, ctypes.POINTER(c_d), c_p]),
 }
 
 _lib = None

@@ -108,12 +108,19 @@ void fill_report(Ctx& c, nlgpu_solve_report* rep, const CgResult& r) {
 CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep) {
     NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "the system must be assembled first");
     NL_REQUIRE(c.symmetric, NLGPU_ERR_UNSUPPORTED, "non-symmetric systems (variable conductivity with a nonlocal model) need BiCGSTAB");
+    NL_REQUIRE(o.preconditioner >= NLGPU_PRECONDITIONER_IDENTITY && o.preconditioner <= NLGPU_PRECONDITIONER_ILLT_LEARNED,
+               NLGPU_ERR_ARG, "unknown preconditioner");
+    NL_REQUIRE(o.precision == NLGPU_PRECISION_FP64 || o.precision == NLGPU_PRECISION_MIXED, NLGPU_ERR_ARG,
+               "unknown precision");
+    const bool learned = o.preconditioner == NLGPU_PRECONDITIONER_ILLT_LEARNED;
+    NL_REQUIRE(!learned || c.mp.weights_set, NLGPU_ERR_STATE, "train the learned correction or set its weights first");
     const IncompleteCholesky* M = nullptr;
     auto t0 = std::chrono::steady_clock::now();
-    if (o.preconditioner == NLGPU_PRECONDITIONER_ILLT) {
+    if (o.preconditioner != NLGPU_PRECONDITIONER_IDENTITY) {
         if (!c.local_ready) build_local(c);
         ilt_build(c, c.local, c.ilt);
         if (c.ilt.ok) M = &c.ilt;   // identity fallback (stationary_heat_equation_solver_2d.hpp:97-101)
+        if (learned && M && !(c.mp.ready && c.mp.n == c.local.rows)) mpnn_prepare(c, c.local);
     } else {
         c.ilt.ok = false;
     }
@@ -121,13 +128,12 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     if (rep) rep->seconds_preconditioner = seconds(t0);
     t0 = std::chrono::steady_clock::now();
     c.temperature.resize(size_t(c.n_nodes));
-    NL_REQUIRE(o.precision == NLGPU_PRECISION_FP64 || o.precision == NLGPU_PRECISION_MIXED, NLGPU_ERR_ARG,
-               "unknown precision");
     CgResult r;
-    if (o.precision == NLGPU_PRECISION_MIXED) {
+    if (o.precision == NLGPU_PRECISION_MIXED || learned) {
         matrix_to_f32(c, c.full);
         r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations,
-                        o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-4, false);
+                        o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M);
+        if (learned && M) mpnn_check(c);
     } else {
         r = cg_solve(c, c.full, M, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations, false);
     }
@@ -595,6 +601,81 @@ int nlgpu_illt_solve(nlgpu_ctx* ctx, int64_t n, const double* x, double* y) {
         c.sweep_error.download(&err, 1, c.stream);
         NL_CUDA(cudaStreamSynchronize(c.stream));
         NL_REQUIRE(err == 0, NLGPU_ERR_TIMEOUT, "a triangular sweep gave up waiting for its data");
+    });
+}
+
+namespace {
+// assembled system + ILLT + FP32 matrix + prepared network, for training and gradient checks
+void ensure_learning_state(Ctx& c) {
+    NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "assemble the system first (nlgpu_conductivity_matrix_2d)");
+    NL_REQUIRE(c.symmetric, NLGPU_ERR_UNSUPPORTED, "the learned correction needs a symmetric system");
+    if (!c.local_ready) build_local(c);
+    if (!c.ilt.ok || c.ilt.n != c.local.rows) ilt_build(c, c.local, c.ilt);
+    NL_REQUIRE(c.ilt.ok, NLGPU_ERR_NUMERICAL, "ILLT failed on the local matrix");
+    if (c.full.val32.n != size_t(c.full.nnz)) matrix_to_f32(c, c.full);
+    if (!(c.mp.ready && c.mp.n == c.local.rows)) mpnn_prepare(c, c.local);
+}
+}  // namespace
+
+int nlgpu_mpnn_set_weights(nlgpu_ctx* ctx, const float* params) {
+    if (!ctx || !params) return NLGPU_ERR_ARG;
+    return guarded([&] { mpnn_set_weights(*ctx, params); NL_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+int nlgpu_mpnn_get_weights(nlgpu_ctx* ctx, float* params) {
+    if (!ctx || !params) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        NL_REQUIRE(ctx->mp.params.n == size_t(MPNN_PARAMS), NLGPU_ERR_STATE, "no weights yet");
+        mpnn_get_weights(*ctx, params);
+    });
+}
+
+int nlgpu_mpnn_train(nlgpu_ctx* ctx, const nlgpu_train_options* options, nlgpu_train_report* report) {
+    if (!ctx || !options) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        ensure_learning_state(c);
+        MpnnTrainOptions o;
+        o.right_hand_sides = options->right_hand_sides;
+        o.epochs = options->epochs;
+        o.batch = options->batch;
+        o.learning_rate = options->learning_rate;
+        o.seed = options->seed;
+        MpnnTrainResult r;
+        mpnn_train(c, c.full, c.ilt, c.rhs.p, o, r);
+        c.mp.weights_set = true;
+        if (report) {
+            report->samples = r.samples; report->steps = r.steps;
+            report->loss_illt = r.loss_illt; report->loss_first = r.loss_first; report->loss_last = r.loss_last;
+            report->seconds_harvest = r.seconds_harvest; report->seconds_train = r.seconds_train;
+        }
+    });
+}
+
+int nlgpu_mpnn_loss_grad(nlgpu_ctx* ctx, const float* r, const float* e, float* z, float* p, double* loss,
+                         float* grad) {
+    if (!ctx || !r || !e) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        ensure_learning_state(c);
+        const i64 n = c.full.rows;
+        dbuf<float> dr, de, dz, dp;
+        dbuf<double> num_ee;
+        dr.upload(r, size_t(n), c.stream);
+        de.upload(e, size_t(n), c.stream);
+        dz.resize(size_t(n)); dp.resize(size_t(n)); num_ee.resize(2);
+        c.mp.grads.zero(c.stream);
+        ilt_apply32(c, c.ilt, dr.p, dz.p);
+        mpnn_backward(c, c.full, dr.p, dz.p, de.p, dp.p, num_ee.p, num_ee.p + 1);
+        double h[2];
+        num_ee.download(h, 2, c.stream);
+        if (z) dz.download(z, size_t(n), c.stream);
+        if (p) dp.download(p, size_t(n), c.stream);
+        if (grad) c.mp.grads.download(grad, size_t(MPNN_PARAMS), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        c.mp.grads.zero(c.stream);
+        mpnn_check(c);
+        if (loss) *loss = h[0] / h[1];
     });
 }
 

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -124,6 +125,7 @@ struct Csr {
     dbuf<int32_t> col;
     dbuf<double> val;
     dbuf<float> val32;
+    dbuf<float> rowsum32;        // row sums of the FP64 values (difference-form FP32 SpMV)
 };
 
 struct BoundaryGroup {
@@ -162,6 +164,7 @@ struct SweepLayout {
 struct SweepPlan {
     bool ok = false;
     i64 n_levels = 0, P = 0;     // levels, padded positions
+    int max_width = 0;           // off-diagonal entries of the widest row
     dbuf<int32_t> cnt, cntp, width;
     dbuf<ushort4> meta;          // per level: rows, padded rows, width
     dbuf<i64> ppos, block_off;
@@ -216,7 +219,7 @@ struct CgWork {
 constexpr int MPNN_HIDDEN = 64;
 constexpr long long MPNN_PARAMS = 4 * 64 + 2 * 128 * 64 + 128;
 struct Mpnn {
-    bool ready = false;
+    bool ready = false, weights_set = false;
     i64 n = 0, ldt = 0;          // nodes; leading dimension of transposed copies (n rounded up to 8)
     dbuf<i64> arp;               // A_hat: symmetric, zero diagonal, FP32 weights
     dbuf<int32_t> acol;
@@ -340,9 +343,13 @@ struct CgResult {
     i64 iterations = 0, outer_iterations = 0;
     double residual = 0, reference_residual = 0;
     bool converged = false;
+    bool learned_fallback = false;   // the learned correction stalled and was switched off
 };
+// on_chunk (optional) is called with the iteration count and x after every
+// chunk of iterations the host checks (used to harvest training snapshots)
+using CgChunkHook = std::function<void(i64 iterations, const double* x)>;
 CgResult cg_solve(Ctx& ctx, const Csr& A_full, const IncompleteCholesky* M, const double* b, double* x,
-                  double tolerance, i64 max_iterations, bool x_is_initial_guess);
+                  double tolerance, i64 max_iterations, bool x_is_initial_guess, const CgChunkHook& on_chunk = {});
 // sweep.cu
 bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vector<int32_t>& rows,
                       const std::vector<i64>& rp, const std::vector<int32_t>& col, const std::vector<i64>& val_index,
@@ -357,7 +364,7 @@ void matrix_to_f32(Ctx& ctx, Csr& A);
 void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y);
 void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z);
 CgResult mixed_solve(Ctx& ctx, const Csr& A_full, IncompleteCholesky* M, const double* b, double* x, double tolerance,
-                     i64 max_iterations, double inner_tolerance, bool x_is_initial_guess);
+                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned);
 // mpnn.cu
 void mpnn_prepare(Ctx& ctx, const Csr& local_upper);
 void mpnn_init_weights(Ctx& ctx, unsigned seed);
@@ -368,6 +375,17 @@ void mpnn_backward(Ctx& ctx, const Csr& A, const float* r, const float* z, const
                    double* loss_num, double* ee_out);
 void mpnn_adam_step(Ctx& ctx, float lr, int batch);
 void mpnn_check(Ctx& ctx);
+struct MpnnTrainOptions {
+    int right_hand_sides = 4, epochs = 20, batch = 8;
+    double learning_rate = 1e-3;
+    unsigned seed = 0;
+};
+struct MpnnTrainResult {
+    i64 samples = 0, steps = 0;
+    double loss_illt = 0, loss_first = 0, loss_last = 0, seconds_harvest = 0, seconds_train = 0;
+};
+void mpnn_train(Ctx& ctx, const Csr& A, IncompleteCholesky& M, const double* b, const MpnnTrainOptions& o,
+                MpnnTrainResult& out);
 // noalloc.cu
 void cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, const double* val, const double* b,
                       double* x, double tolerance, i64 max_iterations, i64* iterations, double* residual);

@@ -1,26 +1,28 @@
-// Mixed-precision solve: FP64 iterative refinement around an FP32 inner solve.
+// Mixed-precision solve: flexible CG in FP32 with FP64 reliable updates.
 //
 // The plain path runs slae::conjugate_gradient (conjugate_gradient.hpp:48-79)
-// in FP64.  This form keeps FP64 only where accuracy is decided -- the outer
-// residual b - A x (FP64 matrix, FP64 SpMV), the solution update, every
-// global dot product and norm (FP64 partial sums), and the IC(0) pivots (the
-// factor is computed in FP64) -- and runs the inner solve in FP32:
+// in FP64.  This form keeps FP64 only where accuracy is decided -- the
+// residual b - A x (FP64 matrix, FP64 SpMV), the solution, every global dot
+// product and norm (FP64 partial sums), and the IC(0) pivots (the factor is
+// computed in FP64) -- and runs the iteration itself in FP32:
 //
-//   x = x0;  repeat
-//     r = b - A x                                   FP64
-//     stop when |r| <= tol |b|
-//     r32 = r / |r|                                  scaled into FP32
-//     d32 ~ A^-1 r32 by flexible CG in FP32 with the FP32 ILLT sweeps,
-//           until |r_inner| <= eta |r32|
-//     x += |r| d32                                   FP64
+//   r = b - A x (FP64); r32 = r / s0; d32 = 0; p_0 = z = P(r32)
+//   repeat k   (FP32 vectors, FP32 matrix copy, FP32 ILLT sweeps)
+//     q_k = A32 p_k;  alpha = p_k.r / p_k.q_k;  d += alpha p_k;  r32 -= alpha q_k
+//     z = P(r32);  p_k+1 = z - sum_i (z.q_i / p_i.q_i) p_i   (last MX_M directions)
+//     when |r32| has dropped by update_factor since the last update (or after
+//     MX_UPDATE_MAX iterations):
+//       x += s0 d (FP64), d = 0;  r = b - A x (FP64);  stop when |r| <= tol |b|;
+//       r32 = r / s0 replaces the recurrence residual; the directions are kept
 //
-// The inner iteration is flexible CG (beta = -(z.q)/(p.q) with q = A p),
-// which stays correct when the preconditioner is not exactly symmetric (FP32
-// rounding in the sweeps, or a learned correction added to the ILLT output).
-// The inner matrix is the FP32 copy of the solver's full-row matrix (values
-// rounded once), so each inner SpMV moves 8 bytes per entry instead of 12.
-// Scalars stay on the device (block partials re-summed by each consuming
-// block); the host reads the done flag once per GRAPH_ITERS iterations.
+// Flexible CG with a few stored directions (Notay's FCG(m)) stays correct when
+// the preconditioner is not exactly symmetric or not linear (FP32 rounding in
+// the sweeps, the learned correction added to the ILLT output).  The reliable
+// updates keep the directions, so no Krylov restart is paid per update.  The
+// FP32 SpMV runs in difference form against the FP64 row sums (see k_spmv32)
+// and moves 8 bytes per entry instead of 12.  Scalars stay on the device
+// (block partials re-summed by each consuming block); the host reads the done
+// flag once per MX_ITERS iterations.
 #include "common.cuh"
 
 #include <cmath>
@@ -31,9 +33,11 @@ namespace {
 
 constexpr int MX_THREADS = 256;
 constexpr int MX_ITERS = 16;
-// partial slots (P_PQ, P_RR, P_RZ_A, P_RZ_B as in the FP64 solver, so the
-// sweeps' early exit reads the inner residual) and one more for z.q
-enum { M_ZQ = P_COUNT, M_SLOTS = P_COUNT + 1 };
+constexpr int MX_M = 4;   // directions kept for the A-orthogonalisation (flexible CG truncation)
+constexpr i64 MX_UPDATE_MAX = 64;   // iterations between reliable updates at most
+// partial slots: P_RR, P_RZ_A, P_RZ_B as in the FP64 solver (the sweeps' early
+// exit reads the residual there), then p_i.q_i and z.q_i of the stored directions
+enum { M_PQ = P_COUNT, M_ZQ = P_COUNT + MX_M, M_SLOTS = P_COUNT + 2 * MX_M };
 
 __device__ __forceinline__ double mx_block_sum(double v, double* sh) {
     v = warp_sum(v);
@@ -61,9 +65,15 @@ __device__ __forceinline__ bool mx_converged(const double* part, const double* f
     return mx_partials(part + P_RR * RED_BLOCKS, sh) <= tol2 * flags[S_BB];
 }
 
-// q = A32 p (FP32 values, FP32 accumulation), warp per padded full row; partial of p.q in FP64
+// q = A32 p (FP32 values, FP32 accumulation), warp per padded full row, in
+// difference form  y_i = sum_j a_ij (x_j - x_i) + s_i x_i  with s_i the row sum
+// of the FP64 matrix: the rows of the conductivity matrix sum to (nearly) zero,
+// so for smooth x the plain FP32 sum would cancel to a result far below the
+// rounding error of its terms, while here each FP32 entry multiplies a small
+// difference.  Partial of p.q in FP64.
 __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restrict__ rp, const int4* __restrict__ col4,
-                                                       const float4* __restrict__ val4, const float* __restrict__ x,
+                                                       const float4* __restrict__ val4,
+                                                       const float* __restrict__ rowsum, const float* __restrict__ x,
                                                        float* __restrict__ y, double* __restrict__ dot_partial,
                                                        const double* __restrict__ flags) {
     __shared__ double sh[40];
@@ -73,14 +83,19 @@ __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restr
     double dot = 0.0;
     for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
         const i64 b4 = rp[r] >> 2, e4 = rp[r + 1] >> 2;
+        const float xr = x[r];
         float s = 0.0f;
         for (i64 k = b4 + lane; k < e4; k += 32) {
             const int4 c = __ldg(col4 + k);
             const float4 v = __ldg(val4 + k);
-            s += v.x * x[c.x] + v.y * x[c.y] + v.z * x[c.z] + v.w * x[c.w];
+            s += v.x * (x[c.x] - xr) + v.y * (x[c.y] - xr) + v.z * (x[c.z] - xr) + v.w * (x[c.w] - xr);
         }
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) { y[r] = s; dot += double(s) * double(x[r]); }
+        if (lane == 0) {
+            s += rowsum[r] * xr;
+            y[r] = s;
+            dot += double(s) * double(xr);
+        }
     }
     if (dot_partial) {
         const double t = mx_block_sum(dot, sh);
@@ -110,6 +125,14 @@ __global__ void __launch_bounds__(MX_THREADS) k_residual_f64(i64 n, const double
     }
     const double t = mx_block_sum(s, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+__global__ void k_rowsum(i64 n, const i64* __restrict__ rp, const double* __restrict__ val, float* __restrict__ out) {
+    for (i64 r = blockIdx.x * i64(blockDim.x) + threadIdx.x; r < n; r += i64(gridDim.x) * blockDim.x) {
+        double s = 0.0;
+        for (i64 k = rp[r]; k < rp[r + 1]; ++k) s += val[k];
+        out[r] = float(s);
+    }
 }
 
 __global__ void k_to_f32(i64 n, const double* __restrict__ a, float* __restrict__ b) {
@@ -143,11 +166,13 @@ __global__ void k_scale_to_f32(i64 n, const double* __restrict__ r, const double
     }
 }
 
-// x += |r| d32 in FP64
-__global__ void k_refine(i64 n, double* __restrict__ x, const float* __restrict__ d32, const double* __restrict__ rr) {
+// x += s d32 in FP64 (s^2 read from the device), d32 = 0
+__global__ void k_refine(i64 n, double* __restrict__ x, float* __restrict__ d32, const double* __restrict__ rr) {
     const double s = sqrt(*rr);
-    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
+    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         x[i] += s * double(d32[i]);
+        d32[i] = 0.0f;
+    }
 }
 
 __global__ void k_copy32(i64 n, const float* __restrict__ a, float* __restrict__ b, const double* __restrict__ part,
@@ -157,14 +182,14 @@ __global__ void k_copy32(i64 n, const float* __restrict__ a, float* __restrict__
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) b[i] = a[i];
 }
 
-// alpha = rz / pq; d += alpha p; r -= alpha q; partial of r.r; counts the iteration
+// alpha = p_j.r / p_j.q_j; d += alpha p_j; r -= alpha q_j; partial of r.r; counts the iteration
 __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __restrict__ d, float* __restrict__ r,
                                                             const float* __restrict__ p, const float* __restrict__ q,
-                                                            double* __restrict__ part, int parity,
+                                                            double* __restrict__ part, int parity, int slot,
                                                             double* __restrict__ flags) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
-    const double pq = mx_partials(part + P_PQ * RED_BLOCKS, sh);
+    const double pq = mx_partials(part + (M_PQ + slot) * RED_BLOCKS, sh);
     const double rz = mx_partials(part + (parity ? P_RZ_A : P_RZ_B) * RED_BLOCKS, sh);
     const float alpha = float(rz / pq);
     double s = 0.0;
@@ -179,30 +204,34 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __rest
     if (blockIdx.x == 0 && threadIdx.x == 0) flags[S_ITERS] += 1.0;
 }
 
-// partials of z.r (the next iteration's rz) and z.q
-__global__ void __launch_bounds__(MX_THREADS) k_dot2_32(i64 n, const float* __restrict__ z, const float* __restrict__ r,
-                                                        const float* __restrict__ q, double* __restrict__ part, int parity,
-                                                        const double* __restrict__ flags, double tol2) {
+// partials of z.q_i for the `count` stored directions
+__global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __restrict__ z, const float* __restrict__ qring,
+                                                       int count, double* __restrict__ part,
+                                                       const double* __restrict__ flags, double tol2) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0 || mx_converged(part, flags, tol2, sh)) return;
-    double zr = 0.0, zq = 0.0;
+    double zq[MX_M] = {};
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         const double zi = z[i];
-        zr += zi * double(r[i]);
-        zq += zi * double(q[i]);
+#pragma unroll
+        for (int s = 0; s < MX_M; ++s)
+            if (s < count) zq[s] += zi * double(qring[i64(s) * n + i]);
     }
-    const double t1 = mx_block_sum(zr, sh);
-    const double t2 = mx_block_sum(zq, sh);
-    if (threadIdx.x == 0) {
-        part[(parity ? P_RZ_B : P_RZ_A) * RED_BLOCKS + blockIdx.x] = t1;
-        part[M_ZQ * RED_BLOCKS + blockIdx.x] = t2;
+#pragma unroll
+    for (int s = 0; s < MX_M; ++s) {
+        if (s >= count) break;
+        const double ts = mx_block_sum(zq[s], sh);
+        if (threadIdx.x == 0) part[(M_ZQ + s) * RED_BLOCKS + blockIdx.x] = ts;
     }
 }
 
-// beta = -(z.q) / (p.q); p = z + beta p; raises the done flag
-__global__ void __launch_bounds__(MX_THREADS) k_update_p32(i64 n, float* __restrict__ p, const float* __restrict__ z,
-                                                           const double* __restrict__ part, double* __restrict__ flags,
-                                                           double tol2, double max_iterations) {
+// p_next = z - sum_i (z.q_i / p_i.q_i) p_i over the stored directions (A-orthogonal
+// to the last MX_M directions) and the partial of p_next.r (the next alpha's
+// numerator, slot by parity); raises the done flag on convergence
+__global__ void __launch_bounds__(MX_THREADS) k_update_pm32(i64 n, float* __restrict__ pring, const float* __restrict__ z,
+                                                            const float* __restrict__ r, int count, int next, int parity,
+                                                            double* __restrict__ part, double* __restrict__ flags,
+                                                            double tol2, double max_iterations) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
     if (mx_converged(part, flags, tol2, sh) || flags[S_ITERS] >= max_iterations) {
@@ -210,11 +239,25 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_p32(i64 n, float* __restr
         if (blockIdx.x == 0 && threadIdx.x == 0) flags[S_DONE] = 1.0;
         return;
     }
-    const double zq = mx_partials(part + M_ZQ * RED_BLOCKS, sh);
-    const double pq = mx_partials(part + P_PQ * RED_BLOCKS, sh);
-    const float beta = float(-zq / pq);
-    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
-        p[i] = z[i] + beta * p[i];
+    float beta[MX_M];
+#pragma unroll
+    for (int s = 0; s < MX_M; ++s) {
+        beta[s] = 0.0f;
+        if (s < count)
+            beta[s] = float(-mx_partials(part + (M_ZQ + s) * RED_BLOCKS, sh) / mx_partials(part + (M_PQ + s) * RED_BLOCKS, sh));
+    }
+    float* pn = pring + i64(next) * n;
+    double pr = 0.0;
+    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+        float v = z[i];
+#pragma unroll
+        for (int s = 0; s < MX_M; ++s)
+            if (s < count) v += beta[s] * pring[i64(s) * n + i];
+        pn[i] = v;   // may overwrite the oldest direction: element i was read above
+        pr += double(v) * double(r[i]);
+    }
+    const double t = mx_block_sum(pr, sh);
+    if (threadIdx.x == 0) part[(parity ? P_RZ_B : P_RZ_A) * RED_BLOCKS + blockIdx.x] = t;
 }
 
 __global__ void k_widen(i64 n, const float* __restrict__ a, double* __restrict__ b) {
@@ -242,7 +285,7 @@ void precondition32(Ctx& ctx, IncompleteCholesky* M, const float* r, float* z, c
 
 void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y) {
     NL_LAUNCH(k_spmv32, RED_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p, reinterpret_cast<const int4*>(A.col.p),
-              reinterpret_cast<const float4*>(A.val32.p), x, y, static_cast<double*>(nullptr),
+              reinterpret_cast<const float4*>(A.val32.p), A.rowsum32.p, x, y, static_cast<double*>(nullptr),
               static_cast<const double*>(nullptr));
 }
 
@@ -254,71 +297,131 @@ void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z) {
 
 void matrix_to_f32(Ctx& ctx, Csr& A) {
     A.val32.resize(size_t(A.nnz));
+    A.rowsum32.resize(size_t(A.rows));
     NL_LAUNCH(k_to_f32, grid_for(A.nnz, 256), 256, 0, ctx.stream, A.nnz, A.val.p, A.val32.p);
+    NL_LAUNCH(k_rowsum, grid_for(A.rows, 256), 256, 0, ctx.stream, A.rows, A.rowptr.p, A.val.p, A.rowsum32.p);
 }
 
+// One flexible CG in FP32 with reliable updates: the FP32 recurrence runs
+// until its residual has dropped by `update_factor` since the last update;
+// then the FP32 correction d is added to x in FP64, the residual is replaced
+// by the true FP64 residual b - A x, and the iteration continues with the
+// same search direction (no Krylov restart).  Every vector keeps the scale
+// s0 = |r0| of the first residual (FP32 precision is scale-free).
 CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double* b, double* x, double tolerance,
-                     i64 max_iterations, double inner_tolerance, bool x_is_initial_guess) {
+                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned) {
     NL_REQUIRE(A.val32.n == size_t(A.nnz), NLGPU_ERR_STATE, "the FP32 copy of the matrix is missing");
+    NL_REQUIRE(!learned || (M && ctx.mp.ready && ctx.mp.n == A.rows), NLGPU_ERR_STATE,
+               "the learned correction needs ILLT and a prepared network");
     const i64 n = A.rows;
     MixedWork& w = ctx.mx;
     w.n = n;
     w.r64.reserve(size_t(n)); w.q64.reserve(size_t(n));
-    w.r.reserve(size_t(n)); w.z.reserve(size_t(n)); w.p.reserve(size_t(n)); w.q.reserve(size_t(n)); w.d.reserve(size_t(n));
+    w.r.reserve(size_t(n)); w.z.reserve(size_t(n)); w.d.reserve(size_t(n));
+    w.p.reserve(size_t(MX_M) * size_t(n)); w.q.reserve(size_t(MX_M) * size_t(n));   // direction rings
     w.partial.reserve(size_t(M_SLOTS) * RED_BLOCKS);
     w.outer.reserve(size_t(2) * RED_BLOCKS + 8);
     w.flags.reserve(8);
     double* part = w.partial.p;
     double* flags = w.flags.p;
     double* outer_part = w.outer.p;
-    double* outer_sc = w.outer.p + 2 * RED_BLOCKS;   // [0] |b|^2, [1] |r|^2
+    double* outer_sc = w.outer.p + 2 * RED_BLOCKS;   // [0] |b|^2, [1] |r|^2, [2] s0^2
     const unsigned G = RED_BLOCKS;
     if (!x_is_initial_guess) NL_CUDA(cudaMemsetAsync(x, 0, size_t(n) * sizeof(double), ctx.stream));
-    const double eta2 = inner_tolerance * inner_tolerance;
+    const double eta2 = update_factor * update_factor;
     CgResult res;
-    // |b|^2
+    auto precondition = [&](const double* pt, const double* fl, double t2) {
+        precondition32(ctx, M, w.r.p, w.z.p, pt, fl, t2);
+        if (learned) mpnn_apply(ctx, w.r.p, w.z.p, w.z.p, false);
+    };
+    // |b|^2 and the first residual
     NL_LAUNCH(k_dot_f64, G, MX_THREADS, 0, ctx.stream, n, b, b, outer_part);
     NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, outer_part, outer_sc);
-    i64 inner_total = 0;
-    for (int outer = 0; outer < 64; ++outer) {
-        // r = b - A x in FP64
+    auto true_residual = [&](double* hs) {
         spmv_full(ctx, A, x, w.q64.p);
         NL_LAUNCH(k_residual_f64, G, MX_THREADS, 0, ctx.stream, n, b, w.q64.p, w.r64.p, outer_part + RED_BLOCKS);
         NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, outer_part + RED_BLOCKS, outer_sc + 1);
-        double hs[2];
-        NL_CUDA(cudaMemcpyAsync(hs, outer_sc, sizeof hs, cudaMemcpyDeviceToHost, ctx.stream));
+        NL_CUDA(cudaMemcpyAsync(hs, outer_sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
         NL_CUDA(cudaStreamSynchronize(ctx.stream));
+    };
+    double hs[2];
+    true_residual(hs);
+    if (hs[0] == 0.0 || hs[1] <= tolerance * tolerance * hs[0] || !std::isfinite(hs[1])) {
         res.residual = hs[0] > 0.0 ? std::sqrt(hs[1] / hs[0]) : 0.0;
-        res.outer_iterations = outer;
-        if (hs[0] == 0.0 || hs[1] <= tolerance * tolerance * hs[0]) { res.converged = true; break; }
-        if (inner_total >= max_iterations || !std::isfinite(hs[1])) break;
-        // inner flexible CG in FP32 on A d = r / |r|
-        NL_LAUNCH(k_scale_to_f32, G, MX_THREADS, 0, ctx.stream, n, w.r64.p, outer_sc + 1, w.r.p, w.d.p);
-        NL_CUDA(cudaMemsetAsync(flags, 0, 8 * sizeof(double), ctx.stream));
-        NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.r.p, w.r.p, part + P_RR * RED_BLOCKS);
-        NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, part + P_RR * RED_BLOCKS, flags + S_BB);
-        precondition32(ctx, M, w.r.p, w.z.p, nullptr, nullptr, 0.0);
-        NL_CUDA(cudaMemcpyAsync(w.p.p, w.z.p, size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, ctx.stream));
-        NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.r.p, w.z.p, part + P_RZ_B * RED_BLOCKS);
-        const double cap = double(max_iterations - inner_total);
+        res.converged = std::isfinite(hs[1]);
+        return res;
+    }
+    NL_CUDA(cudaMemcpyAsync(outer_sc + 2, outer_sc + 1, sizeof(double), cudaMemcpyDeviceToDevice, ctx.stream));
+    // r32 = r / s0, d = 0, p_0 = z = P(r) in ring slot 0, rz -> the slot iteration 0 reads
+    NL_LAUNCH(k_scale_to_f32, G, MX_THREADS, 0, ctx.stream, n, w.r64.p, outer_sc + 2, w.r.p, w.d.p);
+    NL_CUDA(cudaMemsetAsync(flags, 0, 8 * sizeof(double), ctx.stream));
+    NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.r.p, w.r.p, part + P_RR * RED_BLOCKS);
+    NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, part + P_RR * RED_BLOCKS, flags + S_BB);
+    precondition(nullptr, nullptr, 0.0);
+    NL_CUDA(cudaMemcpyAsync(w.p.p, w.z.p, size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, ctx.stream));
+    NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.r.p, w.z.p, part + P_RZ_B * RED_BLOCKS);
+    const double cap = double(std::min<i64>(max_iterations, i64(1) << 40));
+    double last_rr = hs[1];
+    i64 k = 0;   // iteration about to run: direction slot k mod MX_M, rz slot by parity of k
+    i64 iters_at_update = 0;
+    for (;;) {
+        bool forced = false;
         for (;;) {
-            for (int it = 0; it < MX_ITERS; ++it) {   // even: every chunk starts at parity 0
-                const int parity = it & 1;
+            for (int it = 0; it < MX_ITERS; ++it, ++k) {
+                const int parity = int(k & 1), slot = int(k % MX_M), next = int((k + 1) % MX_M);
+                const int count = int(std::min<i64>(k + 1, MX_M));
+                float* pj = w.p.p + i64(slot) * n;
+                float* qj = w.q.p + i64(slot) * n;
                 NL_LAUNCH(k_spmv32, G, MX_THREADS, 0, ctx.stream, n, A.rowptr.p, reinterpret_cast<const int4*>(A.col.p),
-                          reinterpret_cast<const float4*>(A.val32.p), w.p.p, w.q.p, part + P_PQ * RED_BLOCKS, flags);
-                NL_LAUNCH(k_update_dr32, G, MX_THREADS, 0, ctx.stream, n, w.d.p, w.r.p, w.p.p, w.q.p, part, parity, flags);
-                precondition32(ctx, M, w.r.p, w.z.p, part, flags, eta2);
-                NL_LAUNCH(k_dot2_32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.r.p, w.q.p, part, parity, flags, eta2);
-                NL_LAUNCH(k_update_p32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, part, flags, eta2, cap);
+                          reinterpret_cast<const float4*>(A.val32.p), A.rowsum32.p, pj, qj,
+                          part + (M_PQ + slot) * RED_BLOCKS, flags);
+                NL_LAUNCH(k_update_dr32, G, MX_THREADS, 0, ctx.stream, n, w.d.p, w.r.p, pj, qj, part, parity, slot, flags);
+                precondition(part, flags, eta2);
+                NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, count, part, flags, eta2);
+                NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, count, next, parity, part,
+                          flags, eta2, cap);
             }
             double hf[8];
             NL_CUDA(cudaMemcpyAsync(hf, flags, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
             NL_CUDA(cudaStreamSynchronize(ctx.stream));
-            if (hf[S_DONE] != 0.0) { inner_total += i64(hf[S_ITERS]); break; }
+            res.iterations = i64(hf[S_ITERS]);
+            if (hf[S_DONE] != 0.0) break;
+            // a recurrence that stalls still gets an update (and the progress check below)
+            if (res.iterations - iters_at_update >= MX_UPDATE_MAX) { forced = true; break; }
         }
-        NL_LAUNCH(k_refine, G, MX_THREADS, 0, ctx.stream, n, x, w.d.p, outer_sc + 1);
+        k = res.iterations;   // the iterations after the one that stopped were skipped
+        iters_at_update = res.iterations;
+        // reliable update: x += s0 d (FP64), r = b - A x (FP64)
+        NL_LAUNCH(k_refine, G, MX_THREADS, 0, ctx.stream, n, x, w.d.p, outer_sc + 2);
+        true_residual(hs);
+        ++res.outer_iterations;
+        res.residual = std::sqrt(hs[1] / hs[0]);
+        if (hs[1] <= tolerance * tolerance * hs[0]) { res.converged = true; break; }
+        if (res.iterations >= max_iterations || !std::isfinite(hs[1])) break;
+        // the learned correction must buy at least a factor 10 per update interval,
+        // or the rest of the solve runs with ILLT alone
+        if (learned && hs[1] > 1e-2 * last_rr) { learned = false; res.learned_fallback = true; }
+        last_rr = hs[1];
+        // r32 = r / s0 replaces the recurrence residual; the stored directions are kept
+        NL_LAUNCH(k_scale_to_f32, G, MX_THREADS, 0, ctx.stream, n, w.r64.p, outer_sc + 2, w.r.p, w.d.p);
+        NL_CUDA(cudaMemsetAsync(flags + S_DONE, 0, sizeof(double), ctx.stream));
+        NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.r.p, w.r.p, part + P_RR * RED_BLOCKS);
+        NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, part + P_RR * RED_BLOCKS, flags + S_BB);
+        const int next = int(k % MX_M);
+        if (forced) {
+            // the last chunk already formed p_k: only its alpha numerator p_k.r changes
+            NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.p.p + i64(next) * n, w.r.p,
+                      part + ((k & 1) ? P_RZ_A : P_RZ_B) * RED_BLOCKS);
+        } else {
+            // the stop skipped p_k: z = P(r), p_k = z - sum_i (z.q_i / p_i.q_i) p_i as at
+            // the end of iteration k - 1
+            precondition(nullptr, nullptr, 0.0);
+            const int count = int(std::min<i64>(k, MX_M)), parity = int((k + 1) & 1);
+            NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, count, part, flags, eta2);
+            NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, count, next, parity, part,
+                      flags, eta2, cap);
+        }
     }
-    res.iterations = inner_total;
     return res;
 }
 

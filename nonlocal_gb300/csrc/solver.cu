@@ -530,7 +530,7 @@ void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* 
 }
 
 CgResult cg_solve(Ctx& ctx, const Csr& A, const IncompleteCholesky* M, const double* b, double* x,
-                  double tolerance, i64 max_iterations, bool x_is_initial_guess) {
+                  double tolerance, i64 max_iterations, bool x_is_initial_guess, const CgChunkHook& on_chunk) {
     const i64 n = A.rows;
     CgWork& w = ctx.cg;
     w.n = n;
@@ -587,6 +587,7 @@ CgResult cg_solve(Ctx& ctx, const Csr& A, const IncompleteCholesky* M, const dou
             NL_CUDA(cudaStreamSynchronize(ctx.stream));
             done_iters = i64(host[S_ITERS]);
             done = host[S_DONE] != 0.0 || done_iters >= max_iterations;
+            if (on_chunk && !done) on_chunk(done_iters, x);
         }
         res.iterations = done_iters;
         // reference measure sqrt(r.z)/|b| from the last r.z partials

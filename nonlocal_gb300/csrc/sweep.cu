@@ -5,21 +5,22 @@
 // by level (rows of one level depend only on earlier levels).  Everything the
 // sweep reads is laid out per level, contiguously, in level order:
 //   * a "level block": off-diagonal values [w][cntp], inverse diagonal [cntp]
-//     and dependency slots [w][cntp] (int16), padded to 16 bytes;
+//     and dependency positions [w][cntp] (int32 padded level-order position,
+//     -1 for padding), padded to 16 bytes;
 //   * the right-hand side, pre-gathered into level order (padded positions).
 // One CTA walks the levels.  Thread 0 keeps STAGES levels in flight with
 // cp.async.bulk (one copy per block, one per right-hand-side chunk) completing
 // on an mbarrier per stage; the other threads wait on the stage's barrier
 // (bounded spin), solve their row and put the value into a ring of RING
-// doubles in shared memory at (padded position mod RING).  The dependency slot
-// of an entry is that ring index, valid because every dependency lies fewer
-// than RING positions back (checked when the plan is built; otherwise the
-// global-memory sweep of solver.cu is used).  Results also stream to global
-// memory in level order; small gather/scatter kernels convert between level
-// order and node order before and after the sweeps.
+// values in shared memory at (padded position mod RING) and into the
+// level-ordered output in global memory.  A dependency within the last RING
+// positions is read from the ring, an older one from the global output
+// (written levels earlier by this CTA).  Small gather/scatter kernels convert
+// between level order and node order before and after the sweeps.
 #include "common.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 namespace nlgpu {
@@ -29,7 +30,7 @@ namespace {
 constexpr int SW_THREADS = 256;
 constexpr int SW_STAGES = 6;
 constexpr int SW_RING = 4096;
-constexpr int SW_ZERO = SW_RING;          // ring slot holding 0 (padding)
+constexpr int SW_MAX_WIDTH = 16;          // widest level the unrolled row loop handles
 constexpr unsigned long long SW_WAIT_LIMIT_NS = 2000000000ull;   // a stage wait gives up after 2 s
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -78,12 +79,18 @@ struct SweepArgs {
     double tol2;
 };
 
-template<class T>
-__global__ void __launch_bounds__(SW_THREADS) k_sweep_tma(SweepArgs<T> a) {
+// SW_THREADS compute threads (one row each per pass) plus one producer warp
+// that only issues the copies: a stage is refilled once the compute threads
+// have released it (empty barrier), so the copy issue is off the critical
+// path of the level chain.  MAXW bounds the level width so the dependency
+// loads of a row are unrolled and issued together.
+template<class T, int MAXW>
+__global__ void __launch_bounds__(SW_THREADS + 32) k_sweep_tma(SweepArgs<T> a) {
     extern __shared__ __align__(128) unsigned char smem[];
     T* ring = reinterpret_cast<T*>(smem);
     unsigned char* stage_base = smem + ((sizeof(T) * (SW_RING + 1) + 127) / 128) * 128;
     uint64_t* bars = reinterpret_cast<uint64_t*>(stage_base + size_t(a.stage_bytes) * SW_STAGES);
+    uint64_t* empty = bars + SW_STAGES;
     __shared__ double sh[40];
     __shared__ int skip;
     if (a.flags) {
@@ -102,58 +109,90 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_tma(SweepArgs<T> a) {
         if (skip) return;
     }
     // per-level (rows, padded rows, width) for every level, read once
-    ushort4* meta = reinterpret_cast<ushort4*>(bars + SW_STAGES);
+    ushort4* meta = reinterpret_cast<ushort4*>(empty + SW_STAGES);
+    __shared__ int abort_flag;
     for (i64 l = threadIdx.x; l < a.n_levels; l += blockDim.x) meta[l] = a.meta[l];
     for (int k = threadIdx.x; k <= SW_RING; k += blockDim.x) ring[k] = T(0);
     if (threadIdx.x == 0) {
-        for (int s = 0; s < SW_STAGES; ++s) mbar_init(&bars[s], 1);
+        abort_flag = 0;
+        for (int s = 0; s < SW_STAGES; ++s) { mbar_init(&bars[s], 1); mbar_init(&empty[s], 1); }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
-    // the issuing thread walks the level blocks and right-hand-side chunks in order
-    i64 issue_block = 0, issue_pos = 0;
-    auto issue = [&](i64 l) {
-        const int s = int(l % SW_STAGES);
-        unsigned char* dst = stage_base + size_t(s) * a.stage_bytes;
-        const int cp = meta[l].y, w = meta[l].z;
-        const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 2) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
-        const uint32_t rhs_bytes = uint32_t(size_t(cp) * sizeof(T));
-        mbar_expect_tx(&bars[s], block_bytes + rhs_bytes);
-        bulk_g2s(dst, a.blocks + issue_block, block_bytes, &bars[s]);
-        bulk_g2s(dst + block_bytes, a.in + issue_pos, rhs_bytes, &bars[s]);
-        issue_block += block_bytes;
-        issue_pos += cp;
-    };
-    if (threadIdx.x == 0)
-        for (i64 l = 0; l < a.n_levels && l < SW_STAGES; ++l) issue(l);
-    i64 p0 = 0;
-    for (i64 l = 0; l < a.n_levels; ++l) {
-        const int s = int(l % SW_STAGES);
+    const int L = int(a.n_levels);
+    if (threadIdx.x >= SW_THREADS) {
+        // producer warp: lane 0 walks the level blocks and right-hand-side chunks in order
+        if (threadIdx.x != SW_THREADS) return;
+        i64 issue_block = 0, issue_pos = 0;
+        for (int l = 0; l < L; ++l) {
+            const int s = l % SW_STAGES;
+            if (l >= SW_STAGES) {   // wait until the compute threads released level l - STAGES
+                const uint32_t par = uint32_t((l / SW_STAGES - 1) & 1);
+                if (!mbar_try_wait(&empty[s], par)) {
+                    const unsigned long long t0 = globaltimer_ns();
+                    while (!mbar_try_wait(&empty[s], par))
+                        if (globaltimer_ns() - t0 > SW_WAIT_LIMIT_NS) { atomicExch(a.error, 1); return; }
+                }
+            }
+            unsigned char* dst = stage_base + size_t(s) * a.stage_bytes;
+            const int cp = meta[l].y, w = meta[l].z;
+            const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 4) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
+            const uint32_t rhs_bytes = uint32_t(size_t(cp) * sizeof(T));
+            mbar_expect_tx(&bars[s], block_bytes + rhs_bytes);
+            bulk_g2s(dst, a.blocks + issue_block, block_bytes, &bars[s]);
+            bulk_g2s(dst + block_bytes, a.in + issue_pos, rhs_bytes, &bars[s]);
+            issue_block += block_bytes;
+            issue_pos += cp;
+        }
+        return;
+    }
+    int p0 = 0;
+    for (int l = 0; l < L; ++l) {
+        const int s = l % SW_STAGES;
         const uint32_t parity = uint32_t((l / SW_STAGES) & 1);
         if (!mbar_try_wait(&bars[s], parity)) {
             const unsigned long long t0 = globaltimer_ns();
             while (!mbar_try_wait(&bars[s], parity)) {
-                if (globaltimer_ns() - t0 > SW_WAIT_LIMIT_NS) { atomicExch(a.error, 1); return; }
+                // a wait that gives up still reaches the level barrier below, where
+                // every compute thread sees the flag and returns
+                if (globaltimer_ns() - t0 > SW_WAIT_LIMIT_NS) { abort_flag = 1; atomicExch(a.error, 1); break; }
             }
         }
-        const int c = meta[l].x, cp = meta[l].y, w = meta[l].z;
+        const ushort4 mt = meta[l];
+        const int c = mt.x, cp = mt.y, w = mt.z;
         const unsigned char* blk = stage_base + size_t(s) * a.stage_bytes;
         const T* vals = reinterpret_cast<const T*>(blk);
         const T* inv = vals + size_t(w) * cp;
-        const int16_t* dep = reinterpret_cast<const int16_t*>(inv + cp);
-        const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 2) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
+        const int32_t* dep = reinterpret_cast<const int32_t*>(inv + cp);
+        const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 4) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
         const T* rhs = reinterpret_cast<const T*>(blk + block_bytes);
-        for (int t = threadIdx.x; t < c; t += blockDim.x) {
+        for (int t = threadIdx.x; t < c; t += SW_THREADS) {
+            // all dependency positions first, then the values (ring for the last RING
+            // positions, global memory for older ones), then the products
+            int32_t d[MAXW];
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k) d[k] = k < w ? dep[k * cp + t] : -1;
+            T y[MAXW];
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k)
+                y[k] = d[k] < 0 ? T(0) : (d[k] >= p0 - SW_RING ? ring[d[k] & (SW_RING - 1)] : __ldcg(a.out + d[k]));
             T acc = rhs[t];
-            for (int k = 0; k < w; ++k) acc -= vals[k * cp + t] * ring[dep[k * cp + t]];
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k)
+                if (k < w) acc -= vals[k * cp + t] * y[k];
             const T v = acc * inv[t];
             ring[(p0 + t) & (SW_RING - 1)] = v;
             a.out[p0 + t] = v;
         }
         p0 += cp;
-        __syncthreads();   // stage s is consumed and the level's ring values are visible
-        if (threadIdx.x == 0 && l + SW_STAGES < a.n_levels) issue(l + SW_STAGES);
+        // the level's ring values are visible and stage s is consumed: release it
+        asm volatile("bar.sync 1, %0;" ::"n"(SW_THREADS) : "memory");
+        if (abort_flag) return;
+        if (threadIdx.x == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&empty[s])) : "memory");
+        }
     }
 }
 
@@ -233,7 +272,7 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
         int max_stage = 0;
         for (i64 l = 0; l < L; ++l) {
             const i64 cp = cntp[size_t(l)], w = width[size_t(l)];
-            const i64 blk = (w * cp * (es + 2) + cp * es + 15) / 16 * 16;
+            const i64 blk = (w * cp * (es + 4) + cp * es + 15) / 16 * 16;
             block_off_out[size_t(l)] = bytes;
             bytes += blk;
             max_stage = std::max<int>(max_stage, int(blk + cp * es));
@@ -255,15 +294,15 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
                         if (s == diag_pos[size_t(r)]) continue;
                         const i64 dp = ppos_of_row[size_t(col[size_t(s)])];
                         max_dist = std::max(max_dist, ppos[size_t(l) + 1] - dp);
-                        const int16_t slot = int16_t(dp & (SW_RING - 1));
-                        std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 2)], &slot, 2);
+                        const int32_t slot = int32_t(dp);
+                        std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 4)], &slot, 4);
                         val_dst.push_back(vbase + (i64(k) * cp + t) * es);
                         if (record_src) val_src.push_back(val_index[size_t(s)]);
                         ++k;
                     }
                 for (; k < w; ++k) {
-                    const int16_t slot = int16_t(SW_ZERO);
-                    std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 2)], &slot, 2);
+                    const int32_t slot = -1;
+                    std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 4)], &slot, 4);
                     val_dst.push_back(vbase + (i64(k) * cp + t) * es);
                     if (record_src) val_src.push_back(-1);
                 }
@@ -271,7 +310,7 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
         }
         out.stage_bytes = max_stage;
         out.smem_bytes = ((size_t(es) * (SW_RING + 1) + 127) / 128) * 128 + size_t(max_stage) * SW_STAGES +
-                         SW_STAGES * sizeof(uint64_t) + size_t(L) * sizeof(ushort4);
+                         2 * SW_STAGES * sizeof(uint64_t) + size_t(L) * sizeof(ushort4);
     };
     std::vector<unsigned char> dep64, dep32;
     std::vector<i64> val_dst64, inv_dst64, val_dst32, inv_dst32;
@@ -280,12 +319,18 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
     layout(4, plan.f32, dep32, val_dst32, inv_dst32, block_off32, false);
     std::vector<ushort4> meta(static_cast<size_t>(L));
     bool small = true;
+    plan.max_width = 0;
     for (i64 l = 0; l < L; ++l) {
-        small = small && cntp[size_t(l)] < 65536 && width[size_t(l)] < 65536;
+        small = small && cntp[size_t(l)] < 65536 && width[size_t(l)] <= SW_MAX_WIDTH;
+        plan.max_width = std::max(plan.max_width, int(width[size_t(l)]));
         meta[size_t(l)] = make_ushort4(uint16_t(cnt[size_t(l)]), uint16_t(cntp[size_t(l)]), uint16_t(width[size_t(l)]), 0);
     }
-    // dependency distances must fit the ring, stages must fit shared memory
-    plan.ok = small && max_dist <= SW_RING && plan.f64.smem_bytes <= 220 * 1024 && n < (i64(1) << 31);
+    // level widths within the unrolled bound, stages within shared memory
+    plan.ok = small && plan.f64.smem_bytes <= 220 * 1024 && P < (i64(1) << 31);
+    if (std::getenv("NLGPU_DEBUG_SWEEPS"))
+        std::fprintf(stderr, "sweep plan: levels %lld positions %lld max distance %lld smem %zu/%zu small %d -> %s\n",
+                     static_cast<long long>(L), static_cast<long long>(P), static_cast<long long>(max_dist),
+                     plan.f64.smem_bytes, plan.f32.smem_bytes, int(small), plan.ok ? "ring" : "global");
     if (!plan.ok) return false;
     plan.meta.upload(meta.data(), meta.size(), ctx.stream);
     std::vector<int32_t> row_of(static_cast<size_t>(P), -1);
@@ -342,10 +387,17 @@ static void run_sweep(Ctx& ctx, SweepPlan& plan, const double* partials, const d
     a.error = ctx.sweep_error.p;
     static bool attr_set = false;
     if (!attr_set) {
-        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
         attr_set = true;
     }
-    NL_LAUNCH(k_sweep_tma<T>, 1, SW_THREADS, lay.smem_bytes, ctx.stream, a);
+    const int threads = SW_THREADS + 32;
+    if (plan.max_width <= 4) NL_LAUNCH((k_sweep_tma<T, 4>), 1, threads, lay.smem_bytes, ctx.stream, a);
+    else if (plan.max_width <= 8) NL_LAUNCH((k_sweep_tma<T, 8>), 1, threads, lay.smem_bytes, ctx.stream, a);
+    else if (plan.max_width <= 12) NL_LAUNCH((k_sweep_tma<T, 12>), 1, threads, lay.smem_bytes, ctx.stream, a);
+    else NL_LAUNCH((k_sweep_tma<T, 16>), 1, threads, lay.smem_bytes, ctx.stream, a);
 }
 
 // z = S U^-1 U^-T S r with the TMA sweeps (forward plan on U^T, backward on U)

@@ -239,6 +239,51 @@ class Problem2D(Context):
         L.check(self._lib.nlgpu_solve_assembled(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep)))
         return t, SolveReport(rep.as_dict())
 
+    # ---- learned correction on top of ILLT ------------------------------------------
+    def train_learned_preconditioner(self, right_hand_sides=4, epochs=20, batch=8, learning_rate=1e-3,
+                                     seed=0) -> dict:
+        """Harvests (r, e) pairs from plain ILLT-CG on this (assembled) system and
+        trains the message-passing correction on the GPU; returns the report."""
+        o = L.TrainOptions(int(right_hand_sides), int(epochs), int(batch), float(learning_rate), int(seed))
+        rep = L.TrainReport()
+        L.check(self._lib.nlgpu_mpnn_train(self._h, ctypes.byref(o), ctypes.byref(rep)))
+        return rep.as_dict()
+
+    def learned_weights(self) -> np.ndarray:
+        w = np.empty(L.MPNN_PARAMS, dtype=np.float32)
+        L.check(self._lib.nlgpu_mpnn_get_weights(self._h, w.ctypes.data))
+        return w
+
+    def set_learned_weights(self, w) -> None:
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == L.MPNN_PARAMS
+        L.check(self._lib.nlgpu_mpnn_set_weights(self._h, w.ctypes.data))
+
+    def learned_loss_grad(self, r, e):
+        """One (r, e) pair on the assembled system: z = ILLT^-1 r, P(r), loss, gradient."""
+        r = np.ascontiguousarray(r, dtype=np.float32)
+        e = np.ascontiguousarray(e, dtype=np.float32)
+        z = np.empty_like(r)
+        p = np.empty_like(r)
+        g = np.empty(L.MPNN_PARAMS, dtype=np.float32)
+        loss = ctypes.c_double()
+        L.check(self._lib.nlgpu_mpnn_loss_grad(self._h, r.ctypes.data, e.ctypes.data, z.ctypes.data, p.ctypes.data,
+                                               ctypes.byref(loss), g.ctypes.data))
+        return z, p, loss.value, g
+
+
+def unpack_learned_weights(w) -> dict:
+    """Packed parameters -> {w1 4x64, w2 128x64, w3 128x64, w4 128x1} (input x output)."""
+    w = np.asarray(w, dtype=np.float64)
+    o1, o2, o3 = 4 * 64, 4 * 64 + 128 * 64, 4 * 64 + 2 * 128 * 64
+    return {"w1": w[:o1].reshape(4, 64), "w2": w[o1:o2].reshape(128, 64), "w3": w[o2:o3].reshape(128, 64),
+            "w4": w[o3:].reshape(128, 1)}
+
+
+def pack_learned_weights(d) -> np.ndarray:
+    return np.concatenate([np.asarray(d[k], dtype=np.float64).ravel() for k in ("w1", "w2", "w3", "w4")]).astype(
+        np.float32)
+
 
 def find_neighbours(problem: Problem2D, strategy: str = "MAX"):
     """mesh::find_neighbours: widened radii, offsets, lists (reference order)."""

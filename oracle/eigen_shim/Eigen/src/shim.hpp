@@ -560,13 +560,89 @@ struct ConjugateGradient {
     template<class V> V solve(const V& b) const { return b; }
     template<class V> V solveWithGuess(const V& b, const V&) const { return b; }
 };
+// Eigen::BiCGSTAB<SparseMatrix> as documented: default DiagonalPreconditioner
+// (inverse of the diagonal, 1 where it is zero), tolerance = machine epsilon
+// on |r| / |b|, at most 2 n iterations.  The iteration is the right-
+// preconditioned BiCGSTAB of van der Vorst (1992); when the shadow residual
+// becomes orthogonal to the residual it restarts from the true residual.
 template<class Sparse>
 struct BiCGSTAB {
-    template<class... A> explicit BiCGSTAB(const A&...) {
-        throw std::logic_error{"Eigen::BiCGSTAB is not part of the oracle build"};
+    using T = typename Sparse::Scalar;
+    using V = Matrix<T, Dynamic, 1>;
+    const Sparse* _a = nullptr;
+    V _inv;
+    T _tol = std::numeric_limits<T>::epsilon();
+    long _max = -1;
+    mutable long _iters = 0;
+    mutable T _error = T{0};
+    explicit BiCGSTAB(const Sparse& a) : _a{&a}, _inv(a.rows()) {
+        const auto* op = a.outerIndexPtr();
+        const auto* ip = a.innerIndexPtr();
+        const T* vp = a.valuePtr();
+        for (long r = 0; r < a.rows(); ++r) {
+            T d = T{0};
+            for (auto k = op[r]; k < op[r + 1]; ++k)
+                if (long(ip[k]) == r) d = vp[k];
+            _inv[r] = d != T{0} ? T{1} / d : T{1};
+        }
     }
-    template<class V> V solve(const V& b) const { return b; }
-    template<class V> V solveWithGuess(const V& b, const V&) const { return b; }
+    void setTolerance(T t) { _tol = t; }
+    void setMaxIterations(long m) { _max = m; }
+    long iterations() const { return _iters; }
+    T error() const { return _error; }
+    ComputationInfo info() const { return Success; }
+    V precond(const V& v) const {
+        V z(v.size());
+        for (long i = 0; i < v.size(); ++i) z[i] = _inv[i] * v[i];
+        return z;
+    }
+    V solve(const V& b) const { return solveWithGuess(b, V::Zero(b.size())); }
+    V solveWithGuess(const V& b, const V& x0) const {
+        const Sparse& A = *_a;
+        const long n = b.size();
+        const long maxit = _max < 0 ? 2 * n : _max;
+        V x = x0;
+        V r = b - A * x;
+        V r0 = r;
+        const T bb = b.squaredNorm();
+        const T tol2 = _tol * _tol * bb;
+        T rho = 1, alpha = 1, w = 1;
+        V v = V::Zero(n), p = V::Zero(n);
+        long i = 0;
+        T r0n2 = r0.squaredNorm();
+        while (r.squaredNorm() > tol2 && i < maxit) {
+            const T rho_old = rho;
+            rho = r0.dot(r);
+            if (std::abs(rho) < std::numeric_limits<T>::epsilon() * std::numeric_limits<T>::epsilon() * r0n2) {
+                r = b - A * x;     // restart
+                r0 = r;
+                rho = r0n2 = r.squaredNorm();
+                v = V::Zero(n);
+                p = V::Zero(n);
+                alpha = w = T{1};
+                if (r0n2 == T{0}) break;
+            }
+            const T beta = (rho / rho_old) * (alpha / w);
+            for (long k = 0; k < n; ++k) p[k] = r[k] + beta * (p[k] - w * v[k]);
+            const V y = precond(p);
+            v = A * y;
+            alpha = rho / r0.dot(v);
+            V s = r;
+            for (long k = 0; k < n; ++k) s[k] -= alpha * v[k];
+            const V z = precond(s);
+            const V t = A * z;
+            const T tt = t.squaredNorm();
+            w = tt > T{0} ? t.dot(s) / tt : T{0};
+            for (long k = 0; k < n; ++k) {
+                x[k] += alpha * y[k] + w * z[k];
+                r[k] = s[k] - w * t[k];
+            }
+            ++i;
+        }
+        _iters = i;
+        _error = bb > T{0} ? std::sqrt(r.squaredNorm() / bb) : T{0};
+        return x;
+    }
 };
 template<class Sparse, class Ordering>
 struct SparseLU {

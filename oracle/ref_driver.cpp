@@ -84,12 +84,20 @@ std::function<T(const std::array<T, 2>&, const std::array<T, 2>&)> make_influenc
     throw std::domain_error{"unknown influence " + kind};
 }
 
+// lambda(x, y) = 1 + 0.5 sin(2 pi x) cos(pi y): with a nonlocal model this makes
+// the reference's system non-symmetric (problem_settings::is_symmetric)
+T conductivity_wave(const std::array<T, 2>& x) {
+    return 1.0 + 0.5 * std::sin(2.0 * std::numbers::pi * x[0]) * std::cos(std::numbers::pi * x[1]);
+}
+
 nonlocal::solver_2d::thermal::raw_conductivity_t<T> make_conductivity() {
     const std::string c = get("conductivity", "1");
     std::stringstream s{c};
     std::vector<T> v; std::string tok;
     while (std::getline(s, tok, ',')) v.push_back(std::stod(tok));
     using namespace nonlocal;
+    if (get("conductivity_field") == "wave")   // a spatially varying isotropic conductivity
+        return solver_2d::thermal::raw_conductivity_t<T>{coefficient_t<T, 2>{spatial_dependency<T, 2>{conductivity_wave}}};
     if (v.size() == 1) return solver_2d::thermal::raw_conductivity_t<T>{coefficient_t<T, 2>{v[0]}};
     if (v.size() == 2) return solver_2d::thermal::raw_orthotropic_conductivity_t<T>{coefficient_t<T, 2>{v[0]}, coefficient_t<T, 2>{v[1]}};
     return solver_2d::thermal::raw_anisotropic_conductivity_t<T>{coefficient_t<T, 2>{v[0]}, coefficient_t<T, 2>{v[1]}, coefficient_t<T, 2>{v[2]}};
@@ -268,6 +276,24 @@ int stationary2d() {
     dump_csr("K_bound", conductivity.matrix().bound());
     dumpv("rhs", std::vector<double>(f.begin(), f.end()));
     residual -= residual_rad + f;
+    if (!settings.is_symmetric()) {
+        // stationary_heat_equation_solver_2d.hpp:105-108: full storage, Eigen::BiCGSTAB
+        std::vector<double> lq;
+        const size_t nq_total = mesh->quad_shift(mesh->container().elements_2d_count());
+        for (size_t q = 0; q < nq_total; ++q) lq.push_back(conductivity_wave(mesh->quad_coord(q)));
+        dumpv("conductivity_q", lq);
+        t0 = std::chrono::steady_clock::now();
+        const Eigen::BiCGSTAB<Eigen::SparseMatrix<T, Eigen::RowMajor, J>> solver{conductivity.matrix().inner()};
+        const Eigen::Matrix<T, Eigen::Dynamic, 1> delta = solver.solve(residual);
+        dumps("t_cg", seconds_since(t0));
+        const Eigen::Matrix<T, Eigen::Dynamic, 1> temperature = temperature_prev - delta;
+        dumpv("temperature", std::vector<double>(temperature.begin(), temperature.end()));
+        dumps("cg_iterations", double(solver.iterations()));
+        dumps("cg_residual", double(solver.error()));
+        const auto Ax = conductivity.matrix().inner() * temperature;
+        dumps("true_residual", (f - Ax).norm() / f.norm());
+        return 0;
+    }
 
     t0 = std::chrono::steady_clock::now();
     conductivity_matrix_2d<T, I, J> conductivity_local{mesh};

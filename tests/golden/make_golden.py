@@ -64,6 +64,12 @@ CASES = {
     "ref_solid_ring": ({"su2": "solid_ring.su2"},
                        {"mode": "stationary2d", "local_weight": 1, "conductivity": "1",
                         "bc.Inner": "temperature:0", "bc.Outer": "temperature:1", "tolerance": 1e-14}),
+    # spatially varying conductivity with a nonlocal model: the reference's system is
+    # non-symmetric (full storage) and solved by Eigen::BiCGSTAB
+    "b10_field_nonsym": ({"nx": 10, "ny": 10, "element": BILINEAR},
+                         {"mode": "stationary2d", "influence": "fast_polynomial", "radius": 0.25,
+                          "local_weight": 0.5, "conductivity": "1", "conductivity_field": "wave",
+                          "bc.left": "temperature:0", "bc.right": "flux:1", "bc.down": "temperature:0.5"}),
     # nonstationary 2D: left T = sin(10 t), identity-preconditioned CG per step
     "b8_nonstationary": ({"nx": 8, "ny": 8, "element": BILINEAR},
                          {"mode": "nonstationary2d", "influence": "fast_polynomial", "radius": 0.3,

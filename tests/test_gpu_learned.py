@@ -1,0 +1,110 @@
+"""The learned correction on top of ILLT: its tensor-core GEMM, its forward
+values and gradients against the CPU FP64 restatement (oracle/mpnn.py), and
+what training gains over ILLT alone."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+
+def to_bf16_bits(x):
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return u.astype(np.uint16)
+
+
+def from_bf16_bits(b):
+    return (b.astype(np.uint32) << 16).view(np.float32)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from nonlocal_gb300 import _lib, build
+    build.build()
+    _lib.load()
+    if _lib.device_count() == 0:
+        pytest.fail("no CUDA device visible to the nlgpu library")
+    return _lib
+
+
+@pytest.mark.parametrize("M,N,K,splits", [(300, 64, 128, 1), (257, 128, 64, 1), (128, 64, 1000, 7), (1, 64, 8, 1)])
+def test_tensor_core_gemm(lib, M, N, K, splits):
+    rng = np.random.default_rng(M + N + K)
+    a = to_bf16_bits(rng.standard_normal((M, K)))
+    b = to_bf16_bits(rng.standard_normal((N, K)))
+    c = np.empty((M, N), dtype=np.float32)
+    lib.check(lib.load().nlgpu_gemm_bf16(M, N, K, splits, a.ctypes.data, b.ctypes.data, c.ctypes.data))
+    ref = from_bf16_bits(a).astype(np.float64) @ from_bf16_bits(b).astype(np.float64).T
+    # FP32 accumulation of exact BF16 products
+    np.testing.assert_allclose(c, ref, rtol=1e-4, atol=1e-4 * np.sqrt(K))
+
+
+def assembled(fx):
+    from test_gpu_parity import gpu_problem
+    pb = gpu_problem(fx)
+    if fx["config"].get("local_weight", 1) < 0.999:
+        pb.find_neighbours()
+    pb.conductivity_matrix("FULL")
+    return pb
+
+
+@pytest.mark.parametrize("name", ["b12_fastpoly", "s6_exp_ortho_jitter"])
+def test_forward_and_gradient_match_oracle(lib, name):
+    from nonlocal_gb300 import thermal as T
+    from oracle import mpnn
+    fx = gc.load(name)
+    pb = assembled(fx)
+    n = fx["K_inner_rowptr"].shape[0] - 1
+    W = mpnn.init_weights(seed=7, scale=1.0)
+    W["w4"] *= 10.0
+    pb.set_learned_weights(T.pack_learned_weights(W))
+    Wb = {k: from_bf16_bits(to_bf16_bits(v)).astype(np.float64) if k in ("w2", "w3") else v for k, v in W.items()}
+    a = gc.csr_to_dense(fx["K_inner_rowptr"], fx["K_inner_col"], fx["K_inner_val"], n, n)
+    a = a + np.triu(a, 1).T
+    rng = np.random.default_rng(11)
+    e = rng.standard_normal(n)
+    r = a @ e
+    s = np.linalg.norm(r)
+    z, p, loss, g = pb.learned_loss_grad(r / s, e / s)
+    adj = mpnn.normalized_adjacency(fx["K_local_rowptr"], fx["K_local_col"], fx["K_local_val"], n)
+    rr, ee, zz = (r / s).astype(np.float32).astype(np.float64), (e / s).astype(np.float32).astype(np.float64), \
+        z.astype(np.float64)
+    p_ref, _ = mpnn.forward(adj, rr, zz, Wb)
+    loss_ref, g_ref = mpnn.loss_and_grad(adj, lambda v: a @ v, rr, zz, ee, Wb)
+    # BF16 activations and GEMM operands: a few parts in 1e3 on the output and loss,
+    # a few percent on the gradients
+    assert np.linalg.norm(p - p_ref) / np.linalg.norm(p_ref - zz) < 3e-2
+    assert abs(loss - loss_ref) / loss_ref < 2e-2
+    gd = T.unpack_learned_weights(g)
+    for k in ("w1", "w2", "w3", "w4"):
+        err = np.linalg.norm(gd[k] - g_ref[k]) / np.linalg.norm(g_ref[k])
+        assert err < 6e-2, (k, err)
+
+
+def test_training_beats_illt_and_solve_converges(lib):
+    """Training lowers the energy-norm error of the preconditioner below ILLT alone on the
+    harvested pairs; the learned FCG reaches the FP64 solution of the oracle's problem."""
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    from test_gpu_parity import oracle_and_gpu, rel, SOLUTION_RTOL
+    mesh = structured_quad_mesh(40, 40, "bilinear")
+    model = dict(influence="fast_polynomial", radius=(0.25, 0.25), local_weight=0.5, conductivity=(1.0,))
+    bcs = [("left", "temperature", 0.0), ("right", "flux", 1.0)]
+    prob, pb = oracle_and_gpu(mesh, model, bcs, lib)
+    prob.find_neighbours()
+    prob.assemble()
+    prob.assemble_local()
+    prob.solve(variant=1, tol=1e-13)
+    pb.find_neighbours()
+    pb.conductivity_matrix("FULL")
+    rep = pb.train_learned_preconditioner(right_hand_sides=6, epochs=30, batch=4, learning_rate=2e-3, seed=1)
+    assert rep["samples"] >= 4
+    assert rep["loss_last"] < rep["loss_illt"], rep
+    t, srep = pb.solve_assembled(tolerance=1e-13, preconditioner="illt_learned", precision="mixed")
+    assert srep.residual <= 1e-13
+    assert rel(t, prob.get("solution")) < SOLUTION_RTOL
+    _, plain = pb.solve_assembled(tolerance=1e-13, preconditioner="illt", precision="mixed")
+    print("learned", srep.iterations, "ILLT", plain.iterations, rep)
