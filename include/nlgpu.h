@@ -105,6 +105,7 @@ typedef struct nlgpu_solve_report {
     double seconds_neighbours, seconds_pattern, seconds_assembly, seconds_boundary,
            seconds_preconditioner, seconds_solve, seconds_total;
     int64_t outer_iterations; /* MIXED: FP64 refinement steps (iterations counts the inner ones) */
+    int learned_fallback;     /* ILLT_LEARNED: 1 when the correction was gated off or stalled */
 } nlgpu_solve_report;
 
 /* ---- library ------------------------------------------------------------ */
@@ -246,6 +247,11 @@ typedef struct nlgpu_train_report {
     double loss_illt;         /* mean loss of ILLT alone on the pairs */
     double loss_first, loss_last;   /* mean loss after the first / last epoch */
     double seconds_harvest, seconds_train;
+    /* validation gate: the system's own right-hand side solved to 1e-10 with and
+     * without the correction; it stays enabled only when it was faster */
+    int64_t validation_iterations_learned, validation_iterations_illt;
+    double validation_seconds_learned, validation_seconds_illt;
+    int learned_enabled;
 } nlgpu_train_report;
 int nlgpu_mpnn_set_weights(nlgpu_ctx* ctx, const float* params);
 int nlgpu_mpnn_get_weights(nlgpu_ctx* ctx, float* params);

@@ -52,7 +52,8 @@ class SolveReport(ctypes.Structure):
                 ("preconditioner_shifts", c_int), ("nnz_inner", c_i64), ("nnz_solver", c_i64),
                 ("element_pairs", c_i64), ("seconds_neighbours", c_d), ("seconds_pattern", c_d),
                 ("seconds_assembly", c_d), ("seconds_boundary", c_d), ("seconds_preconditioner", c_d),
-                ("seconds_solve", c_d), ("seconds_total", c_d), ("outer_iterations", c_i64)]
+                ("seconds_solve", c_d), ("seconds_total", c_d), ("outer_iterations", c_i64),
+                ("learned_fallback", c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -65,7 +66,9 @@ class TrainOptions(ctypes.Structure):
 
 class TrainReport(ctypes.Structure):
     _fields_ = [("samples", c_i64), ("steps", c_i64), ("loss_illt", c_d), ("loss_first", c_d), ("loss_last", c_d),
-                ("seconds_harvest", c_d), ("seconds_train", c_d)]
+                ("seconds_harvest", c_d), ("seconds_train", c_d), ("validation_iterations_learned", c_i64),
+                ("validation_iterations_illt", c_i64), ("validation_seconds_learned", c_d),
+                ("validation_seconds_illt", c_d), ("learned_enabled", c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -103,11 +103,21 @@ void fill_report(Ctx& c, nlgpu_solve_report* rep, const CgResult& r) {
     rep->nnz_solver = c.full.nnz;
     rep->element_pairs = c.pairs;
     rep->outer_iterations = r.outer_iterations;
+    rep->learned_fallback = r.learned_fallback ? 1 : 0;
 }
 
 CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep) {
     NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "the system must be assembled first");
-    NL_REQUIRE(c.symmetric, NLGPU_ERR_UNSUPPORTED, "non-symmetric systems (variable conductivity with a nonlocal model) need BiCGSTAB");
+    if (!c.symmetric) {
+        // variable conductivity with a nonlocal model: full storage, BiCGSTAB with
+        // the diagonal preconditioner (stationary_heat_equation_solver_2d.hpp:105-108)
+        const auto t0 = std::chrono::steady_clock::now();
+        c.temperature.resize(size_t(c.n_nodes));
+        CgResult r = bicgstab_solve(c, c.full, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations);
+        if (rep) rep->seconds_solve = seconds(t0);
+        fill_report(c, rep, r);
+        return r;
+    }
     NL_REQUIRE(o.preconditioner >= NLGPU_PRECONDITIONER_IDENTITY && o.preconditioner <= NLGPU_PRECONDITIONER_ILLT_LEARNED,
                NLGPU_ERR_ARG, "unknown preconditioner");
     NL_REQUIRE(o.precision == NLGPU_PRECISION_FP64 || o.precision == NLGPU_PRECISION_MIXED, NLGPU_ERR_ARG,
@@ -132,8 +142,9 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     if (o.precision == NLGPU_PRECISION_MIXED || learned) {
         matrix_to_f32(c, c.full);
         r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations,
-                        o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M);
-        if (learned && M) mpnn_check(c);
+                        o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M && c.mp.use);
+        if (learned && M && c.mp.use) mpnn_check(c);
+        if (learned && !(M && c.mp.use)) r.learned_fallback = true;   // gated off: ILLT alone
     } else {
         r = cg_solve(c, c.full, M, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations, false);
     }
@@ -648,6 +659,11 @@ int nlgpu_mpnn_train(nlgpu_ctx* ctx, const nlgpu_train_options* options, nlgpu_t
             report->samples = r.samples; report->steps = r.steps;
             report->loss_illt = r.loss_illt; report->loss_first = r.loss_first; report->loss_last = r.loss_last;
             report->seconds_harvest = r.seconds_harvest; report->seconds_train = r.seconds_train;
+            report->validation_iterations_learned = r.validation_iterations_learned;
+            report->validation_iterations_illt = r.validation_iterations_illt;
+            report->validation_seconds_learned = r.validation_seconds_learned;
+            report->validation_seconds_illt = r.validation_seconds_illt;
+            report->learned_enabled = r.learned_enabled ? 1 : 0;
         }
     });
 }

@@ -220,6 +220,7 @@ constexpr int MPNN_HIDDEN = 64;
 constexpr long long MPNN_PARAMS = 4 * 64 + 2 * 128 * 64 + 128;
 struct Mpnn {
     bool ready = false, weights_set = false;
+    bool use = true;             // validation gate: the correction beat ILLT alone on its own system
     i64 n = 0, ldt = 0;          // nodes; leading dimension of transposed copies (n rounded up to 8)
     dbuf<i64> arp;               // A_hat: symmetric, zero diagonal, FP32 weights
     dbuf<int32_t> acol;
@@ -235,6 +236,11 @@ struct Mpnn {
     dbuf<double> part, part2, ee64;
     dbuf<float> sc;              // scalars (1/rms r, 1/rms z, rms z, ...)
     dbuf<int> error;
+};
+
+// Device state of BiCGSTAB (bicgstab.cu).
+struct BicgWork {
+    dbuf<double> r, r0, p, v, s, t, y, z, dinv, part, sc;
 };
 
 // Device state of the mixed-precision solve (mixed.cu).
@@ -290,6 +296,7 @@ struct Ctx {
     bool plugin_ilt_ready = false;
     CgWork cg;
     MixedWork mx;
+    BicgWork bi;
     Mpnn mp;
     // nonstationary
     Csr capacity_m, capacity_full;
@@ -365,6 +372,8 @@ void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y);
 void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z);
 CgResult mixed_solve(Ctx& ctx, const Csr& A_full, IncompleteCholesky* M, const double* b, double* x, double tolerance,
                      i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned);
+// bicgstab.cu: Jacobi-preconditioned BiCGSTAB on a full-row (non-symmetric) matrix, zero start
+CgResult bicgstab_solve(Ctx& ctx, const Csr& A_full, const double* b, double* x, double tolerance, i64 max_iterations);
 // mpnn.cu
 void mpnn_prepare(Ctx& ctx, const Csr& local_upper);
 void mpnn_init_weights(Ctx& ctx, unsigned seed);
@@ -383,6 +392,9 @@ struct MpnnTrainOptions {
 struct MpnnTrainResult {
     i64 samples = 0, steps = 0;
     double loss_illt = 0, loss_first = 0, loss_last = 0, seconds_harvest = 0, seconds_train = 0;
+    i64 validation_iterations_learned = 0, validation_iterations_illt = 0;
+    double validation_seconds_learned = 0, validation_seconds_illt = 0;
+    bool learned_enabled = false;
 };
 void mpnn_train(Ctx& ctx, const Csr& A, IncompleteCholesky& M, const double* b, const MpnnTrainOptions& o,
                 MpnnTrainResult& out);

@@ -575,6 +575,29 @@ void mpnn_train(Ctx& ctx, const Csr& A, IncompleteCholesky& M, const double* b_g
     }
     mpnn_check(ctx);
     out.seconds_train = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+    m.weights_set = true;
+    // validation gate: the system's own right-hand side solved with and without
+    // the correction; it stays enabled only when it is faster
+    if (b_given) {
+        dbuf<double> xv;
+        xv.resize(size_t(n));
+        auto timed = [&](bool learned, double& secs) {
+            const auto s0 = std::chrono::steady_clock::now();
+            const CgResult r = mixed_solve(ctx, A, &M, b_given, xv.p, 1e-10, 20 * n + 1000, 1e-2, false, learned);
+            NL_CUDA(cudaStreamSynchronize(ctx.stream));
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - s0).count();
+            return r;
+        };
+        m.use = true;
+        const CgResult with = timed(true, out.validation_seconds_learned);
+        const CgResult without = timed(false, out.validation_seconds_illt);
+        out.validation_iterations_learned = with.iterations;
+        out.validation_iterations_illt = without.iterations;
+        m.use = with.converged && !with.learned_fallback && out.validation_seconds_learned < out.validation_seconds_illt;
+    } else {
+        m.use = true;
+    }
+    out.learned_enabled = m.use;
 }
 
 void mpnn_check(Ctx& ctx) {

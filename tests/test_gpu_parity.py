@@ -115,6 +115,28 @@ def test_stationary_solution(golden):
     assert rel(t, fx["temperature"]) < SOLUTION_RTOL
 
 
+def test_nonsymmetric_variable_conductivity(lib):
+    """A spatially varying conductivity with a nonlocal model makes the reference's
+    system non-symmetric (full storage) and solved by BiCGSTAB: same neighbours,
+    patterns, values, right-hand side and solution."""
+    fx = gc.load("b10_field_nonsym")
+    pb = gpu_problem(fx)
+    pb.set_conductivity_field(fx["conductivity_q"])
+    pb.find_neighbours(fx["config"].get("strategy", "MAX"))
+    off, lst = pb.neighbours()
+    assert np.array_equal(off, fx["neigh_offsets"]) and np.array_equal(lst, fx["neigh_list"])
+    pb.conductivity_matrix("FULL")
+    assert_csr_equal(pb.matrix("inner"), fx, "K_inner")
+    assert_csr_equal(pb.matrix("bound"), fx, "K_bound")
+    rp = fx["K_inner_rowptr"]
+    assert rp[-1] > 2 * (rp.shape[0] - 1) and np.any(np.diff(rp) > 20)   # full rows, not the upper half
+    f, _ = pb.rhs()
+    np.testing.assert_allclose(f, fx["rhs"], rtol=MATRIX_RTOL, atol=MATRIX_RTOL * np.abs(fx["rhs"]).max())
+    t, rep = pb.solve_assembled(tolerance=1e-13, max_iterations=20000)
+    assert rep.residual <= 1e-13
+    assert rel(t, fx["temperature"]) < SOLUTION_RTOL
+
+
 def test_mixed_precision_solution(golden):
     """FP32 inner flexible CG + FP64 refinement reaches the reference's FP64 solution:
     the FP64 residual decides convergence, so the bar is the plain one."""

@@ -76,6 +76,28 @@ def test_solution(solved):
     assert rel(prob.get("solution"), fx["temperature"]) < 1e-10
 
 
+def test_nonsymmetric_field_matrices():
+    """Variable conductivity with a nonlocal model: the oracle reproduces the reference's
+    full (non-symmetric) storage bit for bit in pattern and to 1e-12 in values."""
+    fx = gc.load("b10_field_nonsym")
+    prob = gc.oracle_problem(fx)
+    prob.set_conductivity_field(fx["conductivity_q"])
+    prob.find_neighbours()
+    prob.assemble()
+    assert np.array_equal(prob.get("neigh_list"), fx["neigh_list"])
+    for mat in ("K_inner", "K_bound"):
+        rp, ci, va = prob.csr(mat)
+        assert np.array_equal(rp, fx[mat + "_rowptr"]) and np.array_equal(ci, fx[mat + "_col"]), mat
+        ref = fx[mat + "_val"]
+        np.testing.assert_allclose(va, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    np.testing.assert_allclose(prob.get("rhs"), fx["rhs"], rtol=1e-12, atol=1e-12 * np.abs(fx["rhs"]).max())
+    # the fixture's solution solves the full system
+    n = fx["K_inner_rowptr"].shape[0] - 1
+    a = gc.csr_to_dense(fx["K_inner_rowptr"], fx["K_inner_col"], fx["K_inner_val"], n, n)
+    assert not np.allclose(a, a.T)
+    assert np.linalg.norm(a @ fx["temperature"] - fx["rhs"]) <= 1e-12 * np.linalg.norm(fx["rhs"])
+
+
 def test_known_answers():
     """The reference's own analytic checks, on the oracle's solution."""
     fx = gc.load("ref_square16_manufactured")
