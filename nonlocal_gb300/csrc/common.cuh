@@ -154,6 +154,8 @@ struct TriSlab {
 
 // Level blocks of a sweep plan for one value type (FP64 or FP32).
 struct SweepLayout {
+    int farmax = 0;              // most dependencies of one level that lie beyond the ring
+    dbuf<int32_t> far_off, far_pos;   // per level: level-order positions the producer prefetches
     int stage_bytes = 0;
     size_t smem_bytes = 0;
     dbuf<unsigned char> blocks;  // per level: values, inverse diagonal, ring slots
@@ -165,6 +167,7 @@ struct SweepPlan {
     bool ok = false;
     i64 n_levels = 0, P = 0;     // levels, padded positions
     int max_width = 0;           // off-diagonal entries of the widest row
+    int threads = 0;             // compute threads (widest level rounded up to a warp)
     dbuf<int32_t> cnt, cntp, width;
     dbuf<ushort4> meta;          // per level: rows, padded rows, width
     dbuf<i64> ppos, block_off;

@@ -38,6 +38,8 @@ constexpr i64 MX_UPDATE_MAX = 64;   // iterations between reliable updates at mo
 // partial slots: P_RR, P_RZ_A, P_RZ_B as in the FP64 solver (the sweeps' early
 // exit reads the residual there), then p_i.q_i and z.q_i of the stored directions
 enum { M_PQ = P_COUNT, M_ZQ = P_COUNT + MX_M, M_SLOTS = P_COUNT + 2 * MX_M };
+// scalar slots after the solver's (S_BB .. S_RR_FINAL): alpha and the betas
+enum { S_ALPHA = 8, S_BETA = 9, S_MIXED_COUNT = 9 + MX_M };
 
 __device__ __forceinline__ double mx_block_sum(double v, double* sh) {
     v = warp_sum(v);
@@ -182,16 +184,43 @@ __global__ void k_copy32(i64 n, const float* __restrict__ a, float* __restrict__
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) b[i] = a[i];
 }
 
-// alpha = p_j.r / p_j.q_j; d += alpha p_j; r -= alpha q_j; partial of r.r; counts the iteration
-__global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __restrict__ d, float* __restrict__ r,
-                                                            const float* __restrict__ p, const float* __restrict__ q,
-                                                            double* __restrict__ part, int parity, int slot,
-                                                            double* __restrict__ flags) {
+// one block: alpha = p_j.r / p_j.q_j into the scalars
+__global__ void __launch_bounds__(MX_THREADS) k_alpha32(const double* __restrict__ part, int parity, int slot,
+                                                        double* __restrict__ flags) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
     const double pq = mx_partials(part + (M_PQ + slot) * RED_BLOCKS, sh);
-    const double rz = mx_partials(part + (parity ? P_RZ_A : P_RZ_B) * RED_BLOCKS, sh);
-    const float alpha = float(rz / pq);
+    const double pr = mx_partials(part + (parity ? P_RZ_A : P_RZ_B) * RED_BLOCKS, sh);
+    if (threadIdx.x == 0) flags[S_ALPHA] = pr / pq;
+}
+
+// one block: the done flag when |r| <= tol |r_update| or the iteration cap is reached
+__global__ void __launch_bounds__(MX_THREADS) k_check32(const double* __restrict__ part, double* __restrict__ flags,
+                                                        double tol2, double max_iterations) {
+    __shared__ double sh[40];
+    if (flags[S_DONE] != 0.0) return;
+    if (mx_converged(part, flags, tol2, sh) || flags[S_ITERS] >= max_iterations)
+        if (threadIdx.x == 0) flags[S_DONE] = 1.0;
+}
+
+// one block: beta_i = -(z.q_i) / (p_i.q_i) into the scalars
+__global__ void __launch_bounds__(MX_THREADS) k_betas32(const double* __restrict__ part, int count,
+                                                        double* __restrict__ flags) {
+    __shared__ double sh[40];
+    if (flags[S_DONE] != 0.0) return;
+    for (int s = 0; s < count; ++s) {
+        const double b = -mx_partials(part + (M_ZQ + s) * RED_BLOCKS, sh) / mx_partials(part + (M_PQ + s) * RED_BLOCKS, sh);
+        if (threadIdx.x == 0) flags[S_BETA + s] = b;
+    }
+}
+
+// d += alpha p_j; r -= alpha q_j; partial of r.r; counts the iteration
+__global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __restrict__ d, float* __restrict__ r,
+                                                            const float* __restrict__ p, const float* __restrict__ q,
+                                                            double* __restrict__ part, double* __restrict__ flags) {
+    __shared__ double sh[40];
+    if (flags[S_DONE] != 0.0) return;
+    const float alpha = float(flags[S_ALPHA]);
     double s = 0.0;
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         d[i] += alpha * p[i];
@@ -207,9 +236,9 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __rest
 // partials of z.q_i for the `count` stored directions
 __global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __restrict__ z, const float* __restrict__ qring,
                                                        int count, double* __restrict__ part,
-                                                       const double* __restrict__ flags, double tol2) {
+                                                       const double* __restrict__ flags) {
     __shared__ double sh[40];
-    if (flags[S_DONE] != 0.0 || mx_converged(part, flags, tol2, sh)) return;
+    if (flags[S_DONE] != 0.0) return;
     double zq[MX_M] = {};
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         const double zi = z[i];
@@ -225,27 +254,17 @@ __global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __res
     }
 }
 
-// p_next = z - sum_i (z.q_i / p_i.q_i) p_i over the stored directions (A-orthogonal
-// to the last MX_M directions) and the partial of p_next.r (the next alpha's
-// numerator, slot by parity); raises the done flag on convergence
+// p_next = z + sum_i beta_i p_i over the stored directions (A-orthogonal to the
+// last MX_M directions) and the partial of p_next.r (the next alpha's numerator,
+// slot by parity)
 __global__ void __launch_bounds__(MX_THREADS) k_update_pm32(i64 n, float* __restrict__ pring, const float* __restrict__ z,
                                                             const float* __restrict__ r, int count, int next, int parity,
-                                                            double* __restrict__ part, double* __restrict__ flags,
-                                                            double tol2, double max_iterations) {
+                                                            double* __restrict__ part, const double* __restrict__ flags) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
-    if (mx_converged(part, flags, tol2, sh) || flags[S_ITERS] >= max_iterations) {
-        __syncthreads();
-        if (blockIdx.x == 0 && threadIdx.x == 0) flags[S_DONE] = 1.0;
-        return;
-    }
     float beta[MX_M];
 #pragma unroll
-    for (int s = 0; s < MX_M; ++s) {
-        beta[s] = 0.0f;
-        if (s < count)
-            beta[s] = float(-mx_partials(part + (M_ZQ + s) * RED_BLOCKS, sh) / mx_partials(part + (M_PQ + s) * RED_BLOCKS, sh));
-    }
+    for (int s = 0; s < MX_M; ++s) beta[s] = s < count ? float(flags[S_BETA + s]) : 0.0f;
     float* pn = pring + i64(next) * n;
     double pr = 0.0;
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
@@ -321,7 +340,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     w.p.reserve(size_t(MX_M) * size_t(n)); w.q.reserve(size_t(MX_M) * size_t(n));   // direction rings
     w.partial.reserve(size_t(M_SLOTS) * RED_BLOCKS);
     w.outer.reserve(size_t(2) * RED_BLOCKS + 8);
-    w.flags.reserve(8);
+    w.flags.reserve(S_MIXED_COUNT);
     double* part = w.partial.p;
     double* flags = w.flags.p;
     double* outer_part = w.outer.p;
@@ -375,11 +394,14 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
                 NL_LAUNCH(k_spmv32, G, MX_THREADS, 0, ctx.stream, n, A.rowptr.p, reinterpret_cast<const int4*>(A.col.p),
                           reinterpret_cast<const float4*>(A.val32.p), A.rowsum32.p, pj, qj,
                           part + (M_PQ + slot) * RED_BLOCKS, flags);
-                NL_LAUNCH(k_update_dr32, G, MX_THREADS, 0, ctx.stream, n, w.d.p, w.r.p, pj, qj, part, parity, slot, flags);
+                NL_LAUNCH(k_alpha32, 1, MX_THREADS, 0, ctx.stream, part, parity, slot, flags);
+                NL_LAUNCH(k_update_dr32, G, MX_THREADS, 0, ctx.stream, n, w.d.p, w.r.p, pj, qj, part, flags);
+                NL_LAUNCH(k_check32, 1, MX_THREADS, 0, ctx.stream, part, flags, eta2, cap);
                 precondition(part, flags, eta2);
-                NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, count, part, flags, eta2);
+                NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, count, part, flags);
+                NL_LAUNCH(k_betas32, 1, MX_THREADS, 0, ctx.stream, part, count, flags);
                 NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, count, next, parity, part,
-                          flags, eta2, cap);
+                          flags);
             }
             double hf[8];
             NL_CUDA(cudaMemcpyAsync(hf, flags, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
@@ -417,9 +439,10 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
             // the end of iteration k - 1
             precondition(nullptr, nullptr, 0.0);
             const int count = int(std::min<i64>(k, MX_M)), parity = int((k + 1) & 1);
-            NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, count, part, flags, eta2);
+            NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, count, part, flags);
+            NL_LAUNCH(k_betas32, 1, MX_THREADS, 0, ctx.stream, part, count, flags);
             NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, count, next, parity, part,
-                      flags, eta2, cap);
+                      flags);
         }
     }
     return res;

@@ -12,11 +12,15 @@
 // cp.async.bulk (one copy per block, one per right-hand-side chunk) completing
 // on an mbarrier per stage; the other threads wait on the stage's barrier
 // (bounded spin), solve their row and put the value into a ring of RING
-// values in shared memory at (padded position mod RING) and into the
-// level-ordered output in global memory.  A dependency within the last RING
-// positions is read from the ring, an older one from the global output
-// (written levels earlier by this CTA).  Small gather/scatter kernels convert
-// between level order and node order before and after the sweeps.
+// values in shared memory at (padded position mod RING; RING = 16384 FP32 or
+// 4096 FP64 entries) and into the level-ordered output in global memory.
+// The block stores, per entry, the shared-memory slot its value is read from:
+// the ring slot for a dependency within RING positions of the end of its
+// level, the zero slot RING for padding, or a per-stage "far" slot after the
+// ring for the few older dependencies, whose values the producer warp copies
+// from the global output (finished levels earlier) when it issues the stage.
+// So the compute threads only ever read shared memory.  Small gather/scatter
+// kernels convert between level order and node order around the sweeps.
 #include "common.cuh"
 
 #include <algorithm>
@@ -29,7 +33,9 @@ namespace {
 
 constexpr int SW_THREADS = 256;
 constexpr int SW_STAGES = 6;
-constexpr int SW_RING = 4096;
+// shared-memory ring of solved values: 16384 FP32 or 4096 FP64 entries (64 / 32 KB)
+constexpr int ring_for_bytes(int es) { return es == 4 ? 16384 : 4096; }
+template<class T> constexpr int ring_size() { return ring_for_bytes(int(sizeof(T))); }
 constexpr int SW_MAX_WIDTH = 16;          // widest level the unrolled row loop handles
 constexpr unsigned long long SW_WAIT_LIMIT_NS = 2000000000ull;   // a stage wait gives up after 2 s
 
@@ -73,13 +79,17 @@ struct SweepArgs {
     const T* in;              // right-hand side in padded level order
     T* out;                   // solution in padded level order
     int stage_bytes;          // bytes of one stage (block + rhs chunk)
+    int nct;                  // compute threads (a multiple of 32, <= SW_THREADS)
+    int farmax;               // far slots per stage after the ring
+    const int32_t* far_off;   // [L + 1]
+    const int32_t* far_pos;   // positions of the far dependencies, level by level
     int* error;
     const double* partials;   // optional CG state: skip after convergence
     const double* flags;
     double tol2;
 };
 
-// SW_THREADS compute threads (one row each per pass) plus one producer warp
+// nct compute threads (one row each per pass) plus one producer warp
 // that only issues the copies: a stage is refilled once the compute threads
 // have released it (empty barrier), so the copy issue is off the critical
 // path of the level chain.  MAXW bounds the level width so the dependency
@@ -88,7 +98,8 @@ template<class T, int MAXW>
 __global__ void __launch_bounds__(SW_THREADS + 32) k_sweep_tma(SweepArgs<T> a) {
     extern __shared__ __align__(128) unsigned char smem[];
     T* ring = reinterpret_cast<T*>(smem);
-    unsigned char* stage_base = smem + ((sizeof(T) * (SW_RING + 1) + 127) / 128) * 128;
+    constexpr int RING = ring_size<T>();
+    unsigned char* stage_base = smem + ((sizeof(T) * (RING + 1 + SW_STAGES * a.farmax) + 127) / 128) * 128;
     uint64_t* bars = reinterpret_cast<uint64_t*>(stage_base + size_t(a.stage_bytes) * SW_STAGES);
     uint64_t* empty = bars + SW_STAGES;
     __shared__ double sh[40];
@@ -112,7 +123,7 @@ __global__ void __launch_bounds__(SW_THREADS + 32) k_sweep_tma(SweepArgs<T> a) {
     ushort4* meta = reinterpret_cast<ushort4*>(empty + SW_STAGES);
     __shared__ int abort_flag;
     for (i64 l = threadIdx.x; l < a.n_levels; l += blockDim.x) meta[l] = a.meta[l];
-    for (int k = threadIdx.x; k <= SW_RING; k += blockDim.x) ring[k] = T(0);
+    for (int k = threadIdx.x; k <= RING; k += blockDim.x) ring[k] = T(0);
     if (threadIdx.x == 0) {
         abort_flag = 0;
         for (int s = 0; s < SW_STAGES; ++s) { mbar_init(&bars[s], 1); mbar_init(&empty[s], 1); }
@@ -121,9 +132,9 @@ __global__ void __launch_bounds__(SW_THREADS + 32) k_sweep_tma(SweepArgs<T> a) {
     }
     __syncthreads();
     const int L = int(a.n_levels);
-    if (threadIdx.x >= SW_THREADS) {
+    if (int(threadIdx.x) >= a.nct) {
         // producer warp: lane 0 walks the level blocks and right-hand-side chunks in order
-        if (threadIdx.x != SW_THREADS) return;
+        if (int(threadIdx.x) != a.nct) return;
         i64 issue_block = 0, issue_pos = 0;
         for (int l = 0; l < L; ++l) {
             const int s = l % SW_STAGES;
@@ -135,6 +146,11 @@ __global__ void __launch_bounds__(SW_THREADS + 32) k_sweep_tma(SweepArgs<T> a) {
                         if (globaltimer_ns() - t0 > SW_WAIT_LIMIT_NS) { atomicExch(a.error, 1); return; }
                 }
             }
+            // dependencies older than the ring: prefetch their (long finished) values
+            // from the global output into this stage's far slots; the arrive below
+            // publishes them with the stage
+            for (int j = a.far_off[l], f = 0; j < a.far_off[l + 1]; ++j, ++f)
+                ring[RING + 1 + s * a.farmax + f] = __ldcg(a.out + a.far_pos[j]);
             unsigned char* dst = stage_base + size_t(s) * a.stage_bytes;
             const int cp = meta[l].y, w = meta[l].z;
             const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 4) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
@@ -167,27 +183,26 @@ __global__ void __launch_bounds__(SW_THREADS + 32) k_sweep_tma(SweepArgs<T> a) {
         const int32_t* dep = reinterpret_cast<const int32_t*>(inv + cp);
         const uint32_t block_bytes = uint32_t((size_t(w) * cp * (sizeof(T) + 4) + size_t(cp) * sizeof(T) + 15) / 16 * 16);
         const T* rhs = reinterpret_cast<const T*>(blk + block_bytes);
-        for (int t = threadIdx.x; t < c; t += SW_THREADS) {
-            // all dependency positions first, then the values (ring for the last RING
-            // positions, global memory for older ones), then the products
+        for (int t = threadIdx.x; t < c; t += a.nct) {
+            // all dependency slots first (ring, prefetched far slot, or the zero slot
+            // RING for padding), then the values, then the products
             int32_t d[MAXW];
 #pragma unroll
-            for (int k = 0; k < MAXW; ++k) d[k] = k < w ? dep[k * cp + t] : -1;
+            for (int k = 0; k < MAXW; ++k) d[k] = k < w ? dep[k * cp + t] : RING;
             T y[MAXW];
 #pragma unroll
-            for (int k = 0; k < MAXW; ++k)
-                y[k] = d[k] < 0 ? T(0) : (d[k] >= p0 - SW_RING ? ring[d[k] & (SW_RING - 1)] : __ldcg(a.out + d[k]));
+            for (int k = 0; k < MAXW; ++k) y[k] = ring[d[k]];
             T acc = rhs[t];
 #pragma unroll
             for (int k = 0; k < MAXW; ++k)
                 if (k < w) acc -= vals[k * cp + t] * y[k];
             const T v = acc * inv[t];
-            ring[(p0 + t) & (SW_RING - 1)] = v;
+            ring[(p0 + t) & (RING - 1)] = v;
             a.out[p0 + t] = v;
         }
         p0 += cp;
         // the level's ring values are visible and stage s is consumed: release it
-        asm volatile("bar.sync 1, %0;" ::"n"(SW_THREADS) : "memory");
+        asm volatile("bar.sync 1, %0;" ::"r"(a.nct) : "memory");
         if (abort_flag) return;
         if (threadIdx.x == 0) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -265,11 +280,49 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
     // Level blocks for one value size es (8: FP64 sweeps, 4: FP32 sweeps); the
     // factor-value sources (val_src, inv_src) are the same for both.
     std::vector<i64> val_src, inv_src;
+    // farthest dependency, counted from the end of its level (reported), and the
+    // widest level (compute threads)
     i64 max_dist = 0;
+    int max_rows = 0;
+    for (i64 l = 0; l < L; ++l) {
+        max_rows = std::max(max_rows, cnt[size_t(l)]);
+        for (i64 t = lev_ptr[size_t(l)]; t < lev_ptr[size_t(l) + 1]; ++t) {
+            const int32_t r = rows[size_t(t)];
+            for (i64 s = rp[size_t(r)]; s < rp[size_t(r) + 1]; ++s)
+                if (s != diag_pos[size_t(r)])
+                    max_dist = std::max(max_dist, ppos[size_t(l) + 1] - ppos_of_row[size_t(col[size_t(s)])]);
+        }
+    }
+    plan.threads = std::min(SW_THREADS, std::max(32, (max_rows + 31) / 32 * 32));
     auto layout = [&](int es, SweepLayout& out, std::vector<unsigned char>& dep_bytes, std::vector<i64>& val_dst,
                       std::vector<i64>& inv_dst, std::vector<i64>& block_off_out, bool record_src) {
         i64 bytes = 0;
         int max_stage = 0;
+        const int ring = ring_for_bytes(es);
+        // dependencies beyond the ring (counted from the end of their level): per
+        // level the distinct positions the producer prefetches into far slots
+        std::vector<int32_t> far_off(static_cast<size_t>(L + 1), 0), far_pos;
+        std::vector<std::vector<i64>> far_of(static_cast<size_t>(L));
+        out.farmax = 0;
+        for (i64 l = 0; l < L; ++l) {
+            auto& f = far_of[size_t(l)];
+            for (i64 t = lev_ptr[size_t(l)]; t < lev_ptr[size_t(l) + 1]; ++t) {
+                const int32_t r = rows[size_t(t)];
+                for (i64 s = rp[size_t(r)]; s < rp[size_t(r) + 1]; ++s) {
+                    if (s == diag_pos[size_t(r)]) continue;
+                    const i64 dp = ppos_of_row[size_t(col[size_t(s)])];
+                    if (ppos[size_t(l) + 1] - dp > ring) f.push_back(dp);
+                }
+            }
+            std::sort(f.begin(), f.end());
+            f.erase(std::unique(f.begin(), f.end()), f.end());
+            out.farmax = std::max(out.farmax, int(f.size()));
+            far_off[size_t(l) + 1] = far_off[size_t(l)] + int32_t(f.size());
+            for (const i64 dp : f) far_pos.push_back(int32_t(dp));
+        }
+        if (far_pos.empty()) far_pos.push_back(0);   // never read; keeps the buffer non-empty
+        out.far_off.upload(far_off.data(), far_off.size(), ctx.stream);
+        out.far_pos.upload(far_pos.data(), far_pos.size(), ctx.stream);
         for (i64 l = 0; l < L; ++l) {
             const i64 cp = cntp[size_t(l)], w = width[size_t(l)];
             const i64 blk = (w * cp * (es + 4) + cp * es + 15) / 16 * 16;
@@ -293,15 +346,19 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
                     for (i64 s = rp[size_t(r)]; s < rp[size_t(r) + 1]; ++s) {
                         if (s == diag_pos[size_t(r)]) continue;
                         const i64 dp = ppos_of_row[size_t(col[size_t(s)])];
-                        max_dist = std::max(max_dist, ppos[size_t(l) + 1] - dp);
-                        const int32_t slot = int32_t(dp);
+                        int32_t slot = int32_t(dp & (ring - 1));
+                        if (ppos[size_t(l) + 1] - dp > ring) {
+                            const auto& f = far_of[size_t(l)];
+                            const i64 idx = std::lower_bound(f.begin(), f.end(), dp) - f.begin();
+                            slot = int32_t(ring + 1 + (l % SW_STAGES) * out.farmax + idx);
+                        }
                         std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 4)], &slot, 4);
                         val_dst.push_back(vbase + (i64(k) * cp + t) * es);
                         if (record_src) val_src.push_back(val_index[size_t(s)]);
                         ++k;
                     }
                 for (; k < w; ++k) {
-                    const int32_t slot = -1;
+                    const int32_t slot = ring;   // ring slot RING holds 0
                     std::memcpy(&dep_bytes[size_t(dbase + (i64(k) * cp + t) * 4)], &slot, 4);
                     val_dst.push_back(vbase + (i64(k) * cp + t) * es);
                     if (record_src) val_src.push_back(-1);
@@ -309,7 +366,8 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
             }
         }
         out.stage_bytes = max_stage;
-        out.smem_bytes = ((size_t(es) * (SW_RING + 1) + 127) / 128) * 128 + size_t(max_stage) * SW_STAGES +
+        out.smem_bytes = ((size_t(es) * (ring + 1 + SW_STAGES * out.farmax) + 127) / 128) * 128 +
+                         size_t(max_stage) * SW_STAGES +
                          2 * SW_STAGES * sizeof(uint64_t) + size_t(L) * sizeof(ushort4);
     };
     std::vector<unsigned char> dep64, dep32;
@@ -326,11 +384,32 @@ bool sweep_plan_build(Ctx& ctx, const std::vector<i64>& lev_ptr, const std::vect
         meta[size_t(l)] = make_ushort4(uint16_t(cnt[size_t(l)]), uint16_t(cntp[size_t(l)]), uint16_t(width[size_t(l)]), 0);
     }
     // level widths within the unrolled bound, stages within shared memory
-    plan.ok = small && plan.f64.smem_bytes <= 220 * 1024 && P < (i64(1) << 31);
+    plan.ok = small && plan.f64.smem_bytes <= 220 * 1024 && plan.f32.smem_bytes <= 220 * 1024 && P < (i64(1) << 31);
     if (std::getenv("NLGPU_DEBUG_SWEEPS"))
-        std::fprintf(stderr, "sweep plan: levels %lld positions %lld max distance %lld smem %zu/%zu small %d -> %s\n",
-                     static_cast<long long>(L), static_cast<long long>(P), static_cast<long long>(max_dist),
-                     plan.f64.smem_bytes, plan.f32.smem_bytes, int(small), plan.ok ? "ring" : "global");
+        for (int ring : {4096, 16384}) {   // dependencies beyond the ring: total, unique per level (max)
+            i64 total = 0, max_unique = 0;
+            for (i64 l = 0; l < L; ++l) {
+                std::vector<i64> far;
+                for (i64 t = lev_ptr[size_t(l)]; t < lev_ptr[size_t(l) + 1]; ++t) {
+                    const int32_t r = rows[size_t(t)];
+                    for (i64 s = rp[size_t(r)]; s < rp[size_t(r) + 1]; ++s) {
+                        if (s == diag_pos[size_t(r)]) continue;
+                        const i64 dp = ppos_of_row[size_t(col[size_t(s)])];
+                        if (ppos[size_t(l) + 1] - dp > ring) far.push_back(dp);
+                    }
+                }
+                total += i64(far.size());
+                std::sort(far.begin(), far.end());
+                max_unique = std::max<i64>(max_unique, i64(std::unique(far.begin(), far.end()) - far.begin()));
+            }
+            std::fprintf(stderr, "  ring %d: far dependencies %lld, max unique per level %lld\n", ring,
+                         static_cast<long long>(total), static_cast<long long>(max_unique));
+        }
+    if (std::getenv("NLGPU_DEBUG_SWEEPS"))
+        std::fprintf(stderr, "sweep plan: levels %lld positions %lld max distance %lld smem %zu/%zu far slots %d/%d "
+                     "threads %d -> %s\n", static_cast<long long>(L), static_cast<long long>(P),
+                     static_cast<long long>(max_dist), plan.f64.smem_bytes, plan.f32.smem_bytes, plan.f64.farmax,
+                     plan.f32.farmax, plan.threads, plan.ok ? "ring" : "global");
     if (!plan.ok) return false;
     plan.meta.upload(meta.data(), meta.size(), ctx.stream);
     std::vector<int32_t> row_of(static_cast<size_t>(P), -1);
@@ -374,6 +453,24 @@ void sweep_plan_fill(Ctx& ctx, SweepPlan& plan, const double* u) {
               plan.f32.blocks.p);
 }
 
+template<class T, int MAXW>
+static void launch_sweep_w(Ctx& ctx, int threads, size_t smem, const SweepArgs<T>& a) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, MAXW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        attr_set = true;
+    }
+    NL_LAUNCH((k_sweep_tma<T, MAXW>), 1, threads, smem, ctx.stream, a);
+}
+
+template<class T>
+static void launch_sweep(Ctx& ctx, int max_width, int threads, size_t smem, const SweepArgs<T>& a) {
+    if (max_width <= 4) launch_sweep_w<T, 4>(ctx, threads, smem, a);
+    else if (max_width <= 8) launch_sweep_w<T, 8>(ctx, threads, smem, a);
+    else if (max_width <= 12) launch_sweep_w<T, 12>(ctx, threads, smem, a);
+    else launch_sweep_w<T, 16>(ctx, threads, smem, a);
+}
+
 template<class T>
 static void run_sweep(Ctx& ctx, SweepPlan& plan, const double* partials, const double* flags, double tol2) {
     const SweepLayout& lay = sizeof(T) == 8 ? plan.f64 : plan.f32;
@@ -385,19 +482,11 @@ static void run_sweep(Ctx& ctx, SweepPlan& plan, const double* partials, const d
     a.stage_bytes = lay.stage_bytes; a.partials = partials; a.flags = flags; a.tol2 = tol2;
     ctx.sweep_error.reserve(1);
     a.error = ctx.sweep_error.p;
-    static bool attr_set = false;
-    if (!attr_set) {
-        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        NL_CUDA(cudaFuncSetAttribute(k_sweep_tma<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        attr_set = true;
-    }
-    const int threads = SW_THREADS + 32;
-    if (plan.max_width <= 4) NL_LAUNCH((k_sweep_tma<T, 4>), 1, threads, lay.smem_bytes, ctx.stream, a);
-    else if (plan.max_width <= 8) NL_LAUNCH((k_sweep_tma<T, 8>), 1, threads, lay.smem_bytes, ctx.stream, a);
-    else if (plan.max_width <= 12) NL_LAUNCH((k_sweep_tma<T, 12>), 1, threads, lay.smem_bytes, ctx.stream, a);
-    else NL_LAUNCH((k_sweep_tma<T, 16>), 1, threads, lay.smem_bytes, ctx.stream, a);
+    a.nct = plan.threads;
+    a.farmax = lay.farmax;
+    a.far_off = lay.far_off.p;
+    a.far_pos = lay.far_pos.p;
+    launch_sweep<T>(ctx, plan.max_width, plan.threads + 32, lay.smem_bytes, a);
 }
 
 // z = S U^-1 U^-T S r with the TMA sweeps (forward plan on U^T, backward on U)
