@@ -339,7 +339,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         t0 = time.perf_counter()
         pe = make_problem(w, T, mesh)
         pe.find_neighbours()
-        pe.set_learned_weights(learned_weights)
+        pe.set_learned_weights(learned_weights, enabled=bool(train["learned_enabled"]))
         te, _ = pe.stationary(tolerance=tol, max_iterations=100000, precision=METHODS[PRIMARY][0],
                               preconditioner=METHODS[PRIMARY][1])
         e2e_s.append(time.perf_counter() - t0)
@@ -404,19 +404,110 @@ def factor_offdiag_entries(lib, h, n: int) -> int:
     return int(2 * (rp[-1] - n))
 
 
+def batch_instances(count: int, seed: int = 0):
+    """Batched nonstationary workload: meshes with edge counts ~U{64..256}, r ~ U[0.03, 0.1],
+    p1 = 0.5, conductivity 1, dt = 1e-3, T = sin(10 t) on the left edge (seeded)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(64, 257)), float(rng.uniform(0.03, 0.1))) for _ in range(count)]
+
+
+def run_batch(args, world, rank, local, dist):
+    """--workload config5: many nonstationary instances stepped together."""
+    import numpy as np
+    from nonlocal_gb300 import _lib as L
+    from nonlocal_gb300 import build as nbuild
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    nbuild.build()
+    lib = L.load()
+    L.check(lib.nlgpu_set_device(local))
+    dt, tol = 1e-3, 1e-10
+    specs = batch_instances(args.instances, seed=rank)
+    t0 = time.perf_counter()
+    solvers = []
+    for edges, r in specs:
+        mesh = structured_quad_mesh(edges, edges, "bilinear")
+        pb = T.Problem2D.from_mesh(mesh)
+        pb.set_model(T.Model2D(influence="fast_polynomial", radius=(r, r), local_weight=0.5))
+        pb.add_boundary(T.Boundary(edges=mesh.boundaries["left"], kind="temperature", value=0.0))
+        pb.find_neighbours()
+        s = T.NonstationaryHeatEquationSolver2D(pb, dt)
+        s.compute()
+        solvers.append(s)
+    batch = T.BatchNonstationary(solvers)
+    setup_s = time.perf_counter() - t0
+    step = 0
+    for _ in range(args.warmup):
+        step += 1
+        batch.step(np.full(len(specs), np.sin(10.0 * step * dt)), tolerance=tol, max_iterations=10000)
+    sampler = ClockSampler(local)
+    barrier(dist)
+    launches0 = L.kernel_launches()
+    sampler.start()
+    lat, its = [], []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        step += 1
+        t1 = time.perf_counter()
+        it = batch.step(np.full(len(specs), np.sin(10.0 * step * dt)), tolerance=tol, max_iterations=10000)
+        lat.append(time.perf_counter() - t1)
+        its.append(it)
+    total = time.perf_counter() - t_all
+    clocks = sampler.stop()
+    launches = L.kernel_launches() - launches0
+    barrier(dist)
+    total = max_over_ranks(dist, total)
+    its = np.array(its)
+    nodes = sum((e + 1) ** 2 for e, _ in specs)
+    if rank != 0:
+        return 0
+    value = len(specs) * args.steps * world / total
+    line = {
+        "metric": "batched nonstationary 2D nonlocal steps: instance-steps per second (implicit Euler, identity CG to 1e-10)",
+        "value": value, "unit": "instance-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{len(specs)} instances, edges ~U{{64..256}}, r ~ U[0.03, 0.1], p1 = 0.5, dt = 1e-3, "
+                               "left T = sin(10 t), bilinear", "instances": len(specs), "nodes": int(nodes),
+                   "parallelism": f"replicas x{world}"},
+        "step_latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "cg_iterations": {"max_per_step": int(its.max()), "mean": float(its.mean())},
+        "setup_s": setup_s, "clocks": clocks, "gpu_launches": int(launches),
+        "e2e": {"value": value, "unit": "instance-steps/s", "h2d_bytes_per_step": 8 * len(specs),
+                "d2h_bytes_per_step": 8 * len(specs)},
+        "roofline": None, "cpu_baseline": None,
+    }
+    print(json.dumps(line))
+    batch.close()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["nlgpu", "reference"], default="nlgpu")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["config5"], default="config2")
+    ap.add_argument("--instances", type=int, default=256, help="config5: number of instances")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
+    world, rank, local, dist = dist_setup()
+    if args.workload == "config5":
+        try:
+            if args.impl == "reference":
+                if rank == 0:
+                    print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no CPU arm here; "
+                                      "the reference steps one instance at a time"}))
+                return 0
+            return run_batch(args, world, rank, local, dist)
+        finally:
+            if dist is not None:
+                dist.destroy_process_group()
     from nonlocal_gb300.meshgen import structured_quad_mesh
     w = WORKLOADS[args.workload]
     mesh = structured_quad_mesh(w["nx"], w["ny"], w["element"], jitter=w["jitter"], seed=0)
-    world, rank, local, dist = dist_setup()
     try:
         if args.impl == "reference":
             return run_reference(args, w, mesh, world, rank, dist)

@@ -254,6 +254,9 @@ typedef struct nlgpu_train_report {
     int learned_enabled;
 } nlgpu_train_report;
 int nlgpu_mpnn_set_weights(nlgpu_ctx* ctx, const float* params);
+/* The validation gate's decision, to carry it with the weights to another
+ * context (1: the correction is used; 0: ILLT alone).  Setting weights enables it. */
+int nlgpu_mpnn_set_enabled(nlgpu_ctx* ctx, int enabled);
 int nlgpu_mpnn_get_weights(nlgpu_ctx* ctx, float* params);
 int nlgpu_mpnn_train(nlgpu_ctx* ctx, const nlgpu_train_options* options, nlgpu_train_report* report);
 int nlgpu_mpnn_loss_grad(nlgpu_ctx* ctx, const float* r, const float* e, float* z, float* p, double* loss,
@@ -293,6 +296,25 @@ int nlgpu_nonstationary_2d_compute(nlgpu_ctx* ctx, double time_step, const doubl
 int nlgpu_nonstationary_2d_step(nlgpu_ctx* ctx, double dirichlet_value, const double* dirichlet_values,
                                 double tolerance, int64_t max_iterations, double* temperature,
                                 int64_t* iterations);
+
+/* ---- batched nonstationary stepping (no counterpart in the reference: it
+ * batches calls of nonstationary_heat_equation_solver_2d::calc_step)
+ * create: instances already set up by nlgpu_nonstationary_2d_compute (each with
+ * its own mesh, model, time step and boundaries; their sizes may differ); the
+ * batch copies their matrices and current temperatures and leaves the
+ * contexts unchanged.  step: one implicit-Euler step of every instance, the
+ * Dirichlet nodes of instance k set to dirichlet_values[k]; CG with the
+ * identity preconditioner from the previous temperature, as calc_step, on the
+ * block-diagonal system of all instances (one launch per stage for all of
+ * them, CUDA-graph replayed iteration chunks, each instance stopping on its
+ * own |r| <= tolerance |b|); iterations[k] (or NULL) receives each count.
+ * temperature: copies instance `index`'s current temperature out. */
+typedef struct nlgpu_batch nlgpu_batch;
+int nlgpu_batch_create(nlgpu_batch** batch, int64_t count, nlgpu_ctx* const* instances);
+int nlgpu_batch_destroy(nlgpu_batch* batch);
+int nlgpu_batch_step(nlgpu_batch* batch, const double* dirichlet_values, double tolerance, int64_t max_iterations,
+                     int64_t* iterations);
+int nlgpu_batch_temperature(nlgpu_batch* batch, int64_t index, double* temperature);
 
 /* ---- stationary_heat_equation_solver_1d (stationary_heat_equation_solver_1d.hpp:43-122)
  * One segment [0, length] of `elements` Lagrange elements of `order` 1

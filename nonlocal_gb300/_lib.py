@@ -107,6 +107,10 @@ SIGNATURES = {
                                ctypes.POINTER(SolveReport)]),
     "nlgpu_illt_compute": (c_int, [c_p, c_i64, c_p, c_p, c_p, ctypes.POINTER(c_int)]),
     "nlgpu_illt_solve": (c_int, [c_p, c_i64, c_p, c_p]),
+    "nlgpu_batch_create": (c_int, [ctypes.POINTER(c_p), c_i64, c_p]),
+    "nlgpu_batch_destroy": (c_int, [c_p]),
+    "nlgpu_batch_step": (c_int, [c_p, c_p, c_d, c_i64, c_p]),
+    "nlgpu_batch_temperature": (c_int, [c_p, c_i64, c_p]),
     "nlgpu_nonstationary_2d_compute": (c_int, [c_p, c_d, c_p]),
     "nlgpu_nonstationary_2d_step": (c_int, [c_p, c_d, c_p, c_d, c_i64, c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),
@@ -119,6 +123,7 @@ SIGNATURES = {
     "nlgpu_time_stage": (c_int, [c_p, c_int, c_int, ctypes.POINTER(c_d)]),
     "nlgpu_gemm_bf16": (c_int, [c_i64, c_int, c_i64, c_int, c_p, c_p, c_p]),
     "nlgpu_mpnn_set_weights": (c_int, [c_p, c_p]),
+    "nlgpu_mpnn_set_enabled": (c_int, [c_p, c_int]),
     "nlgpu_mpnn_get_weights": (c_int, [c_p, c_p]),
     "nlgpu_mpnn_train": (c_int, [c_p, ctypes.POINTER(TrainOptions), ctypes.POINTER(TrainReport)]),
     "nlgpu_mpnn_loss_grad": (c_int, [c_p, c_p, c_p, c_p, c_p, ctypes.POINTER(c_d), c_p]),

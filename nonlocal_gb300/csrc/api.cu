@@ -633,6 +633,12 @@ int nlgpu_mpnn_set_weights(nlgpu_ctx* ctx, const float* params) {
     return guarded([&] { mpnn_set_weights(*ctx, params); NL_CUDA(cudaStreamSynchronize(ctx->stream)); });
 }
 
+int nlgpu_mpnn_set_enabled(nlgpu_ctx* ctx, int enabled) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    ctx->mp.use = enabled != 0;
+    return NLGPU_OK;
+}
+
 int nlgpu_mpnn_get_weights(nlgpu_ctx* ctx, float* params) {
     if (!ctx || !params) return NLGPU_ERR_ARG;
     return guarded([&] {
@@ -743,6 +749,50 @@ int nlgpu_nonstationary_2d_step(nlgpu_ctx* ctx, double dirichlet_value, const do
         if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
     });
     return rc != NLGPU_OK ? rc : conv_status;
+}
+
+struct nlgpu_batch {
+    nlgpu::Batch* impl = nullptr;
+    int64_t count = 0;
+};
+
+int nlgpu_batch_create(nlgpu_batch** batch, int64_t count, nlgpu_ctx* const* instances) {
+    if (!batch || count <= 0 || !instances) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        std::vector<Ctx*> v;
+        for (int64_t k = 0; k < count; ++k) {
+            NL_REQUIRE(instances[k], NLGPU_ERR_ARG, "null instance");
+            v.push_back(instances[k]);
+        }
+        auto* b = new nlgpu_batch{};
+        try {
+            b->impl = batch_create(v);
+        } catch (...) {
+            delete b;
+            throw;
+        }
+        b->count = count;
+        *batch = b;
+    });
+}
+
+int nlgpu_batch_destroy(nlgpu_batch* batch) {
+    if (!batch) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        batch_destroy(batch->impl);
+        delete batch;
+    });
+}
+
+int nlgpu_batch_step(nlgpu_batch* batch, const double* dirichlet_values, double tolerance, int64_t max_iterations,
+                     int64_t* iterations) {
+    if (!batch || !dirichlet_values || !(tolerance > 0.0) || max_iterations <= 0) return NLGPU_ERR_ARG;
+    return guarded([&] { batch_step(*batch->impl, dirichlet_values, tolerance, max_iterations, iterations); });
+}
+
+int nlgpu_batch_temperature(nlgpu_batch* batch, int64_t index, double* temperature) {
+    if (!batch || !temperature) return NLGPU_ERR_ARG;
+    return guarded([&] { batch_temperature(*batch->impl, index, temperature); });
 }
 
 int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double length, double radius, double local_weight,

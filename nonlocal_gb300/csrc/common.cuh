@@ -375,6 +375,13 @@ void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y);
 void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z);
 CgResult mixed_solve(Ctx& ctx, const Csr& A_full, IncompleteCholesky* M, const double* b, double* x, double tolerance,
                      i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned);
+// batch.cu: many nonstationary instances stepped together (block-diagonal system)
+struct Batch;
+Batch* batch_create(const std::vector<Ctx*>& instances);
+void batch_destroy(Batch* bt);
+i64 batch_step(Batch& bt, const double* dirichlet_values, double tolerance, i64 max_iterations, i64* iterations);
+void batch_temperature(Batch& bt, i64 index, double* out);
+cudaStream_t batch_stream(Batch& bt);
 // bicgstab.cu: Jacobi-preconditioned BiCGSTAB on a full-row (non-symmetric) matrix, zero start
 CgResult bicgstab_solve(Ctx& ctx, const Csr& A_full, const double* b, double* x, double tolerance, i64 max_iterations);
 // mpnn.cu

@@ -352,6 +352,7 @@ void mpnn_set_weights(Ctx& ctx, const float* host) {
     Mpnn& m = ctx.mp;
     m.params.upload(host, size_t(MPNN_PARAMS), ctx.stream);
     m.weights_set = true;
+    m.use = true;
     m.grads.resize(size_t(MPNN_PARAMS)); m.grads.zero(ctx.stream);
     m.adam_m.resize(size_t(MPNN_PARAMS)); m.adam_m.zero(ctx.stream);
     m.adam_v.resize(size_t(MPNN_PARAMS)); m.adam_v.zero(ctx.stream);

@@ -254,10 +254,12 @@ class Problem2D(Context):
         L.check(self._lib.nlgpu_mpnn_get_weights(self._h, w.ctypes.data))
         return w
 
-    def set_learned_weights(self, w) -> None:
+    def set_learned_weights(self, w, enabled: bool = True) -> None:
+        """Weights of the learned correction (and the validation gate's decision)."""
         w = np.ascontiguousarray(w, dtype=np.float32)
         assert w.size == L.MPNN_PARAMS
         L.check(self._lib.nlgpu_mpnn_set_weights(self._h, w.ctypes.data))
+        L.check(self._lib.nlgpu_mpnn_set_enabled(self._h, int(bool(enabled))))
 
     def learned_loss_grad(self, r, e):
         """One (r, e) pair on the assembled system: z = ILLT^-1 r, P(r), loss, gradient."""
@@ -302,6 +304,41 @@ def stationary_heat_equation_solver_2d(problem: Problem2D, model: Model2D, bound
     if source:
         problem.set_source(source)
     return problem.stationary(tolerance, max_iterations, preconditioner, precision)
+
+
+class BatchNonstationary:
+    """Many nonstationary instances (each a ``NonstationaryHeatEquationSolver2D``
+    after ``compute``) stepped together as one block-diagonal system."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        self._lib = L.load()
+        handles = (ctypes.c_void_p * len(self.solvers))(*[s.problem.handle.value for s in self.solvers])
+        self._h = ctypes.c_void_p()
+        L.check(self._lib.nlgpu_batch_create(ctypes.byref(self._h), len(self.solvers), handles))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.nlgpu_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, dirichlet_values, tolerance: float = 1e-15, max_iterations: int = 10000) -> np.ndarray:
+        """One implicit-Euler step of every instance; returns each instance's CG iterations."""
+        dv = L.f64(np.broadcast_to(np.asarray(dirichlet_values, dtype=np.float64), (len(self.solvers),)))
+        it = np.empty(len(self.solvers), dtype=np.int64)
+        L.check(self._lib.nlgpu_batch_step(self._h, L.ptr(dv), float(tolerance), int(max_iterations), L.ptr(it)))
+        return it
+
+    def temperature(self, index: int) -> np.ndarray:
+        t = np.empty(self.solvers[index].problem.n_nodes)
+        L.check(self._lib.nlgpu_batch_temperature(self._h, int(index), L.ptr(t)))
+        return t
 
 
 class NonstationaryHeatEquationSolver2D:
