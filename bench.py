@@ -43,8 +43,10 @@ sys.path.insert(0, ROOT)
 METRIC = ("time to 1e-10 relative residual, nonlocal stationary 2D solve (full pipeline): learned mixed-precision "
           "FCG (ILLT + message-passing correction, FP32 inner, FP64 reliable updates); plain FP64 ILLT-CG beside it")
 PRIMARY = "learned"
-# method -> (precision, preconditioner)
-METHODS = {"learned": ("mixed", "illt_learned"), "mixed": ("mixed", "illt"), "plain": ("fp64", "illt")}
+# method -> (precision, preconditioner, triangular sweeps of the FP32 ILLT: 0 the library's
+# default Jacobi sweeps, -1 exact level-scheduled substitution)
+METHODS = {"learned": ("mixed", "illt_learned", 0), "mixed": ("mixed", "illt", 0),
+           "mixed_exact": ("mixed", "illt", -1), "plain": ("fp64", "illt", 0)}
 LEARNED_TRAINING = dict(right_hand_sides=4, epochs=20, batch=4, learning_rate=2e-3, seed=0)
 
 WORKLOADS = {
@@ -230,9 +232,10 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     tol = w["tolerance"]
 
     def step(method):
-        precision, pre = METHODS[method]
+        precision, pre, sweeps = METHODS[method]
         pb.find_neighbours()
-        return pb.stationary(tolerance=tol, max_iterations=100000, precision=precision, preconditioner=pre)
+        return pb.stationary(tolerance=tol, max_iterations=100000, precision=precision, preconditioner=pre,
+                             triangular_sweeps=sweeps)
 
     def timed(method):
         """K device-timed solves (CUDA events on the library's stream), L2 flushed before each."""
@@ -251,6 +254,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     for _ in range(args.warmup):
         step("plain")
         step("mixed")
+        step("mixed_exact")
     # the learned correction is trained once per operator, on pairs the plain
     # solver harvests from this system (not timed as part of a solve)
     train = pb.train_learned_preconditioner(**LEARNED_TRAINING)
@@ -267,6 +271,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     L.check(lib.nlgpu_synchronize(h))
     launches = L.kernel_launches() - launches0
     ms_mixed, reports_mixed, temp_mixed = timed("mixed")
+    ms_exact, reports_exact, _ = timed("mixed_exact")
     ms_plain, reports_plain, temp_plain = timed("plain")
     L.check(lib.nlgpu_synchronize(h))
     clocks = sampler.stop()
@@ -274,7 +279,9 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     mean_ms = max_over_ranks(dist, sum(ms_steps) / len(ms_steps))
     mixed_ms = max_over_ranks(dist, sum(ms_mixed) / len(ms_mixed))
     plain_ms = max_over_ranks(dist, sum(ms_plain) / len(ms_plain))
+    exact_ms = max_over_ranks(dist, sum(ms_exact) / len(ms_exact))
     rep_mixed = reports_mixed[-1]
+    rep_exact = reports_exact[-1]
     seconds = mean_ms / 1e3
     rep = reports[-1]
     rep_plain = reports_plain[-1]
@@ -284,7 +291,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     # -------- stage timings for the roofline (device events, this problem)
     stage_ms = {}
     for stage, name, reps in [(0, "spmv", 50), (4, "spmv32", 50), (2, "illt_apply", 10), (5, "illt_apply32", 10),
-                              (1, "pair_assembly", 3)]:
+                              (6, "illt_jacobi32", 20), (1, "pair_assembly", 3)]:
         v = ctypes.c_double()
         L.check(lib.nlgpu_time_stage(h, stage, reps, ctypes.byref(v)))
         stage_ms[name] = v.value
@@ -296,7 +303,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     # per solve of the primary (mixed) method: inner FP32 SpMV and sweeps per inner
     # iteration (+1 start per outer step), FP64 SpMV per outer residual
     per_solve_ms = {"spmv": stage_ms["spmv"] * (outer + 1), "spmv32": stage_ms["spmv32"] * iters,
-                    "illt_apply32": stage_ms["illt_apply32"] * (iters + outer),
+                    "illt_jacobi32": stage_ms["illt_jacobi32"] * (iters + outer),
                     "pair_assembly": stage_ms["pair_assembly"]}
     dominant = max(per_solve_ms, key=per_solve_ms.get)
     pk, pk_kind = peaks()
@@ -315,6 +322,17 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         roof = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
                 "peak_kind": pk_kind, "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
                 "traffic": traffic.get((kname, args.workload))}
+    elif dominant == "illt_jacobi32":
+        # k Jacobi sweeps per triangle; each reads every off-diagonal entry of its
+        # triangle once (value 4 B + column 4 B) and per row the right-hand side, the
+        # gathered iterate and a scale (4 + 4 + 4 B) and writes the new iterate (4 B)
+        k = L.DEFAULT_TRIANGULAR_SWEEPS
+        jac_bytes = k * (factor_offdiag_entries(lib, h, n) * 8 + 2 * n * 16)
+        achieved = jac_bytes / (stage_ms["illt_jacobi32"] * 1e-3) / 1e9
+        roof = {"kernel": "k_jacobi32", "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                "peak_kind": pk_kind, "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                "traffic": traffic.get(("k_jacobi32", args.workload)),
+                "launches_per_application": 2 * k}
     else:
         # both FP32 sweeps read each off-diagonal factor entry (value 4 B + ring slot
         # 2 B) once, per row its right-hand side and inverse diagonal (4 + 4 B) and
@@ -380,7 +398,10 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
                   "stage_ms": stage_ms, "per_solve_ms": per_solve_ms},
         "learned_training": dict(train, **{"config": LEARNED_TRAINING}),
         "mixed_illt": {"ms_per_step": mixed_ms, "cg_iterations": rep_mixed.iterations,
-                       "reliable_updates": rep_mixed.outer_iterations, "residual": rep_mixed.residual},
+                       "reliable_updates": rep_mixed.outer_iterations, "residual": rep_mixed.residual,
+                       "triangular_sweeps": L.DEFAULT_TRIANGULAR_SWEEPS},
+        "mixed_illt_exact_sweeps": {"ms_per_step": exact_ms, "cg_iterations": rep_exact.iterations,
+                                    "reliable_updates": rep_exact.outer_iterations, "residual": rep_exact.residual},
         "plain_fp64": {"ms_per_step": plain_ms, "cg_iterations": rep_plain.iterations, "residual": rep_plain.residual,
                        "temperature_rel_l2_vs_primary": float(np.linalg.norm(temp_plain - temp) / np.linalg.norm(temp_plain))},
         "speedup_vs_plain_fp64": plain_ms / mean_ms,

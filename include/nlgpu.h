@@ -72,6 +72,14 @@ enum { NLGPU_PRECONDITIONER_IDENTITY = 0, NLGPU_PRECONDITIONER_ILLT = 1, NLGPU_P
 /* precision of the solve */
 enum { NLGPU_PRECISION_FP64 = 0, NLGPU_PRECISION_MIXED = 1 };
 
+/* MIXED: how the FP32 ILLT application solves its two triangular systems.
+ * k > 0: k Jacobi sweeps per triangle (the first k + 1 terms of the Neumann
+ * series of each triangular inverse; fully parallel passes); < 0: exact
+ * level-scheduled substitution, as the FP64 path.  0 in the options selects
+ * the default below. */
+#define NLGPU_DEFAULT_TRIANGULAR_SWEEPS 6
+#define NLGPU_EXACT_TRIANGULAR_SWEEPS (-1)
+
 /* Nonlocal model of one material: model_parameters<2, T> (equation_parameters.hpp:251-257)
  * plus its influence function and constant conductivity (parameter_2d). */
 typedef struct nlgpu_model_2d {
@@ -90,7 +98,8 @@ typedef struct nlgpu_solve_options {
     int64_t max_iterations;
     int preconditioner;       /* NLGPU_PRECONDITIONER_* */
     int precision;            /* NLGPU_PRECISION_* */
-    double inner_tolerance;   /* MIXED: relative reduction of each FP32 inner solve (<= 0: 1e-4) */
+    double inner_tolerance;   /* MIXED: relative reduction of each FP32 inner solve (<= 0: 1e-2) */
+    int triangular_sweeps;    /* MIXED: see NLGPU_DEFAULT_TRIANGULAR_SWEEPS (0: the default) */
 } nlgpu_solve_options;
 
 typedef struct nlgpu_solve_report {
@@ -216,6 +225,10 @@ int nlgpu_cg_solve(nlgpu_ctx* ctx, int64_t n, const int64_t* a_rowptr, const int
 int nlgpu_illt_compute(nlgpu_ctx* ctx, int64_t n, const int64_t* rowptr, const int64_t* col, const double* val,
                        int* computation_info);
 int nlgpu_illt_solve(nlgpu_ctx* ctx, int64_t n, const double* x, double* y);
+/* The same factor applied in FP32 as the mixed-precision solve applies it:
+ * sweeps > 0 Jacobi sweeps per triangle, < 0 exact level-scheduled sweeps
+ * (no counterpart in the reference). */
+int nlgpu_illt_solve_f32(nlgpu_ctx* ctx, int64_t n, int sweeps, const float* x, float* y);
 
 /* ---- learned correction on top of ILLT (no counterpart in the reference) ----
  * A 4-layer message-passing network (width 64, tanh, no biases) over the
@@ -333,7 +346,9 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
  * average device time of one kernel stage over `reps` launches on the current
  * problem: 0 SpMV of the solver matrix, 1 pair assembly (FULL part),
  * 2 ILLT application (both triangular sweeps), 3 neighbour search, 4 FP32
- * SpMV of the solver matrix, 5 FP32 ILLT application (mixed precision). */
+ * SpMV of the solver matrix, 5 FP32 ILLT application with exact level-scheduled
+ * sweeps, 6 FP32 ILLT application with the Jacobi sweeps of the last mixed
+ * solve (NLGPU_DEFAULT_TRIANGULAR_SWEEPS before any). */
 /* Options of a context: NLGPU_OPTION_GLOBAL_SWEEPS = 1 makes the ILLT
  * triangular sweeps read and write their values in global memory instead of
  * the TMA-fed shared-memory ring (same arithmetic); NLGPU_OPTION_ORDERED_PAIRS

@@ -44,7 +44,11 @@ class Model2D(ctypes.Structure):
 
 class SolveOptions(ctypes.Structure):
     _fields_ = [("tolerance", c_d), ("max_iterations", c_i64), ("preconditioner", c_int), ("precision", c_int),
-                ("inner_tolerance", c_d)]
+                ("inner_tolerance", c_d), ("triangular_sweeps", c_int)]
+
+
+DEFAULT_TRIANGULAR_SWEEPS = 6   # NLGPU_DEFAULT_TRIANGULAR_SWEEPS
+EXACT_TRIANGULAR_SWEEPS = -1    # NLGPU_EXACT_TRIANGULAR_SWEEPS
 
 
 class SolveReport(ctypes.Structure):
@@ -107,6 +111,7 @@ SIGNATURES = {
                                ctypes.POINTER(SolveReport)]),
     "nlgpu_illt_compute": (c_int, [c_p, c_i64, c_p, c_p, c_p, ctypes.POINTER(c_int)]),
     "nlgpu_illt_solve": (c_int, [c_p, c_i64, c_p, c_p]),
+    "nlgpu_illt_solve_f32": (c_int, [c_p, c_i64, c_int, c_p, c_p]),
     "nlgpu_batch_create": (c_int, [ctypes.POINTER(c_p), c_i64, c_p]),
     "nlgpu_batch_destroy": (c_int, [c_p]),
     "nlgpu_batch_step": (c_int, [c_p, c_p, c_d, c_i64, c_p]),

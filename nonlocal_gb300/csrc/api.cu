@@ -122,6 +122,7 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
                NLGPU_ERR_ARG, "unknown preconditioner");
     NL_REQUIRE(o.precision == NLGPU_PRECISION_FP64 || o.precision == NLGPU_PRECISION_MIXED, NLGPU_ERR_ARG,
                "unknown precision");
+    NL_REQUIRE(o.triangular_sweeps <= 4096, NLGPU_ERR_ARG, "at most 4096 Jacobi sweeps per triangle");
     const bool learned = o.preconditioner == NLGPU_PRECONDITIONER_ILLT_LEARNED;
     NL_REQUIRE(!learned || c.mp.weights_set, NLGPU_ERR_STATE, "train the learned correction or set its weights first");
     const IncompleteCholesky* M = nullptr;
@@ -141,8 +142,10 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     CgResult r;
     if (o.precision == NLGPU_PRECISION_MIXED || learned) {
         matrix_to_f32(c, c.full);
+        c.ilt_sweeps = o.triangular_sweeps == 0 ? NLGPU_DEFAULT_TRIANGULAR_SWEEPS : std::max(o.triangular_sweeps, 0);
         r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations,
-                        o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M && c.mp.use);
+                        o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M && c.mp.use,
+                        c.ilt_sweeps);
         if (learned && M && c.mp.use) mpnn_check(c);
         if (learned && !(M && c.mp.use)) r.learned_fallback = true;   // gated off: ILLT alone
     } else {
@@ -615,6 +618,25 @@ int nlgpu_illt_solve(nlgpu_ctx* ctx, int64_t n, const double* x, double* y) {
     });
 }
 
+int nlgpu_illt_solve_f32(nlgpu_ctx* ctx, int64_t n, int sweeps, const float* x, float* y) {
+    if (!ctx || !x || !y || sweeps == 0 || sweeps > 4096) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.plugin_ilt_ready, NLGPU_ERR_STATE, "nlgpu_illt_compute has not succeeded on this context");
+        NL_REQUIRE(n == c.plugin_ilt.n, NLGPU_ERR_ARG, "vector size differs from the factorised matrix");
+        dbuf<float> dx, dy;
+        dx.upload(x, size_t(n), c.stream);
+        dy.resize(size_t(n));
+        c.sweep_error.zero(c.stream);
+        ilt_apply32(c, c.plugin_ilt, dx.p, dy.p, std::max(sweeps, 0));
+        dy.download(y, size_t(n), c.stream);
+        int err = 0;
+        c.sweep_error.download(&err, 1, c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        NL_REQUIRE(err == 0, NLGPU_ERR_TIMEOUT, "a triangular sweep gave up waiting for its data");
+    });
+}
+
 namespace {
 // assembled system + ILLT + FP32 matrix + prepared network, for training and gradient checks
 void ensure_learning_state(Ctx& c) {
@@ -687,7 +709,7 @@ int nlgpu_mpnn_loss_grad(nlgpu_ctx* ctx, const float* r, const float* e, float* 
         de.upload(e, size_t(n), c.stream);
         dz.resize(size_t(n)); dp.resize(size_t(n)); num_ee.resize(2);
         c.mp.grads.zero(c.stream);
-        ilt_apply32(c, c.ilt, dr.p, dz.p);
+        ilt_apply32(c, c.ilt, dr.p, dz.p, c.ilt_sweeps);
         mpnn_backward(c, c.full, dr.p, dz.p, de.p, dp.p, num_ee.p, num_ee.p + 1);
         double h[2];
         num_ee.download(h, 2, c.stream);
@@ -861,14 +883,14 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
         NL_CUDA(cudaEventCreate(&e1));
         dbuf<double> x, y;
         dbuf<float> x32, y32;
-        NL_REQUIRE(stage >= 0 && stage <= 5, NLGPU_ERR_ARG, "unknown stage");
-        if (stage == 0 || stage == 2 || stage == 4 || stage == 5) {
+        NL_REQUIRE(stage >= 0 && stage <= 6, NLGPU_ERR_ARG, "unknown stage");
+        if (stage == 0 || stage == 2 || stage >= 4) {
             NL_REQUIRE(c.full.nnz > 0, NLGPU_ERR_STATE, "assemble the system first");
             x.resize(size_t(c.n_nodes)); y.resize(size_t(c.n_nodes));
             x32.resize(size_t(c.n_nodes)); y32.resize(size_t(c.n_nodes));
             NL_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), c.stream));
             NL_CUDA(cudaMemsetAsync(x32.p, 0, x32.bytes(), c.stream));
-            if (stage == 2 || stage == 5) NL_REQUIRE(c.ilt.ok, NLGPU_ERR_STATE, "no ILLT factor");
+            if (stage == 2 || stage >= 5) NL_REQUIRE(c.ilt.ok, NLGPU_ERR_STATE, "no ILLT factor");
             if (stage == 4 && c.full.val32.n != size_t(c.full.nnz)) matrix_to_f32(c, c.full);
         }
         if (stage == 1) NL_REQUIRE(c.inner.nnz > 0 && c.model.nonlocal(), NLGPU_ERR_STATE, "no nonlocal pattern");
@@ -880,7 +902,8 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
             else if (stage == 2) ilt_apply(c, c.ilt, x.p, y.p);
             else if (stage == 3) find_neighbours(c, c.strategy);
             else if (stage == 4) spmv32(c, c.full, x32.p, y32.p);
-            else ilt_apply32(c, c.ilt, x32.p, y32.p);
+            else if (stage == 5) ilt_apply32(c, c.ilt, x32.p, y32.p, 0);
+            else ilt_apply32(c, c.ilt, x32.p, y32.p, std::max(c.ilt_sweeps, 1));
         }
         NL_CUDA(cudaEventRecord(e1, c.stream));
         NL_CUDA(cudaEventSynchronize(e1));

@@ -152,6 +152,19 @@ struct TriSlab {
     dbuf<float> val32, inv_diag32;
 };
 
+// One triangle of the factor for Jacobi sweeps (jacobi.cu): the off-diagonal
+// entries of each row divided by the row's diagonal, FP32, in sliced ELL with
+// 32-row slices (entry k of row 32 s + l at slice[s] + 32 k + l), so that the
+// thread of a row and its 31 neighbours read consecutive words.  Padding
+// entries point at their own row with value 0.
+struct JacobiSlab {
+    i64 entries = 0;
+    dbuf<i64> slice;             // [slices + 1] entry offsets
+    dbuf<int32_t> col;
+    dbuf<i64> src;               // entry -> factor value (-1: padding)
+    dbuf<float> val;
+};
+
 // Level blocks of a sweep plan for one value type (FP64 or FP32).
 struct SweepLayout {
     int farmax = 0;              // most dependencies of one level that lie beyond the ring
@@ -201,6 +214,9 @@ struct IncompleteCholesky {
     TriSlab fwd, bwd;
     dbuf<double> y, w;           // sweep buffers, n + 1 entries
     dbuf<float> y32, w32;
+    JacobiSlab jlo, jup;         // U^T and U for Jacobi sweeps, rows scaled by 1 / u_ii
+    dbuf<float> jc, jdinv;       // s_i / u_ii and 1 / u_ii
+    dbuf<float> jt0, jt1, jy;    // Jacobi iterates and the scaled forward result
     bool ok = false;
     int attempts = 0;
     double shift = 0.0;
@@ -252,6 +268,12 @@ struct MixedWork {
     dbuf<double> r64, q64;       // outer residual and A x
     dbuf<float> r, z, p, q, d;   // inner vectors
     dbuf<double> partial, outer, flags;
+    cudaGraphExec_t chunk = nullptr;   // a chunk of inner iterations, re-captured per solve
+    int chunk_kernels = 0;
+    MixedWork() = default;
+    MixedWork(const MixedWork&) = delete;
+    MixedWork& operator=(const MixedWork&) = delete;
+    ~MixedWork() { if (chunk) cudaGraphExecDestroy(chunk); }
 };
 
 struct Ctx {
@@ -310,6 +332,7 @@ struct Ctx {
     bool nonstationary_ready = false;
     dbuf<int> sweep_error;
     bool force_global_sweeps = false;   // use the global-memory sweeps (for comparison)
+    int ilt_sweeps = NLGPU_DEFAULT_TRIANGULAR_SWEEPS;   // FP32 ILLT: Jacobi sweeps per triangle (0: exact)
     bool ordered_pairs = false;         // evaluate every ordered element pair (for comparison)
     // measurement
     cudaEvent_t events[64] = {};
@@ -369,12 +392,18 @@ void sweep_apply(Ctx& ctx, IncompleteCholesky& ic, const double* r, double* z, c
                  const double* flags, double tol2);
 void sweep_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, const double* partials,
                    const double* flags, double tol2);
+// jacobi.cu: the factor applied by Jacobi sweeps on its two triangles
+void jacobi_build(Ctx& ctx, IncompleteCholesky& ic, const std::vector<i64>& rp, const std::vector<int32_t>& col,
+                  const std::vector<i64>& lrp, const std::vector<int32_t>& lcol, const std::vector<i64>& l_to_u);
+void jacobi_fill(Ctx& ctx, IncompleteCholesky& ic);
+void jacobi_apply32(Ctx& ctx, IncompleteCholesky& ic, int sweeps, const float* r, float* z, const double* flags);
 // mixed.cu
 void matrix_to_f32(Ctx& ctx, Csr& A);
 void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y);
-void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z);
+// sweeps 0: level-scheduled triangular solves; > 0: that many Jacobi sweeps per triangle
+void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, int sweeps = 0);
 CgResult mixed_solve(Ctx& ctx, const Csr& A_full, IncompleteCholesky* M, const double* b, double* x, double tolerance,
-                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned);
+                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps);
 // batch.cu: many nonstationary instances stepped together (block-diagonal system)
 struct Batch;
 Batch* batch_create(const std::vector<Ctx*>& instances);

@@ -77,9 +77,13 @@ __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restr
                                                        const float4* __restrict__ val4,
                                                        const float* __restrict__ rowsum, const float* __restrict__ x,
                                                        float* __restrict__ y, double* __restrict__ dot_partial,
-                                                       const double* __restrict__ flags) {
+                                                       const double* __restrict__ flags, i64 ring) {
     __shared__ double sh[40];
     if (flags && flags[S_DONE] != 0.0) return;
+    if (ring) {   // direction slot of the current iteration in the rings of x, y and the partials
+        const i64 slot = i64(flags[S_ITERS]) % MX_M;
+        x += slot * ring; y += slot * ring; dot_partial += slot * RED_BLOCKS;
+    }
     const int lane = threadIdx.x & 31;
     const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
     double dot = 0.0;
@@ -185,41 +189,56 @@ __global__ void k_copy32(i64 n, const float* __restrict__ a, float* __restrict__
 }
 
 // one block: alpha = p_j.r / p_j.q_j into the scalars
-__global__ void __launch_bounds__(MX_THREADS) k_alpha32(const double* __restrict__ part, int parity, int slot,
-                                                        double* __restrict__ flags) {
+__global__ void __launch_bounds__(MX_THREADS) k_alpha32(const double* __restrict__ part, double* __restrict__ flags) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
+    const i64 k = i64(flags[S_ITERS]);
+    const int parity = int(k & 1), slot = int(k % MX_M);
     const double pq = mx_partials(part + (M_PQ + slot) * RED_BLOCKS, sh);
     const double pr = mx_partials(part + (parity ? P_RZ_A : P_RZ_B) * RED_BLOCKS, sh);
     if (threadIdx.x == 0) flags[S_ALPHA] = pr / pq;
 }
 
-// one block: the done flag when |r| <= tol |r_update| or the iteration cap is reached
+// one block: counts the iteration; the done flag when |r| <= tol |r_update| or
+// the iteration cap is reached.  The kernels after it in the iteration read
+// the new count (k + 1).
 __global__ void __launch_bounds__(MX_THREADS) k_check32(const double* __restrict__ part, double* __restrict__ flags,
                                                         double tol2, double max_iterations) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
-    if (mx_converged(part, flags, tol2, sh) || flags[S_ITERS] >= max_iterations)
-        if (threadIdx.x == 0) flags[S_DONE] = 1.0;
+    const bool converged = mx_converged(part, flags, tol2, sh);
+    if (threadIdx.x == 0) {
+        const double it = flags[S_ITERS] + 1.0;
+        flags[S_ITERS] = it;
+        if (converged || it >= max_iterations) flags[S_DONE] = 1.0;
+    }
+}
+
+// directions stored after k iterations
+__device__ __forceinline__ int mx_count(const double* flags) {
+    return int(min(i64(flags[S_ITERS]), i64(MX_M)));
 }
 
 // one block: beta_i = -(z.q_i) / (p_i.q_i) into the scalars
-__global__ void __launch_bounds__(MX_THREADS) k_betas32(const double* __restrict__ part, int count,
-                                                        double* __restrict__ flags) {
+__global__ void __launch_bounds__(MX_THREADS) k_betas32(const double* __restrict__ part, double* __restrict__ flags) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
+    const int count = mx_count(flags);
     for (int s = 0; s < count; ++s) {
         const double b = -mx_partials(part + (M_ZQ + s) * RED_BLOCKS, sh) / mx_partials(part + (M_PQ + s) * RED_BLOCKS, sh);
         if (threadIdx.x == 0) flags[S_BETA + s] = b;
     }
 }
 
-// d += alpha p_j; r -= alpha q_j; partial of r.r; counts the iteration
+// d += alpha p_j; r -= alpha q_j (j the current direction slot); partial of r.r
 __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __restrict__ d, float* __restrict__ r,
                                                             const float* __restrict__ p, const float* __restrict__ q,
-                                                            double* __restrict__ part, double* __restrict__ flags) {
+                                                            double* __restrict__ part, const double* __restrict__ flags) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
+    const i64 slot = i64(flags[S_ITERS]) % MX_M;
+    p += slot * n;
+    q += slot * n;
     const float alpha = float(flags[S_ALPHA]);
     double s = 0.0;
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
@@ -230,15 +249,14 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __rest
     }
     const double t = mx_block_sum(s, sh);
     if (threadIdx.x == 0) part[P_RR * RED_BLOCKS + blockIdx.x] = t;
-    if (blockIdx.x == 0 && threadIdx.x == 0) flags[S_ITERS] += 1.0;
 }
 
-// partials of z.q_i for the `count` stored directions
+// partials of z.q_i for the stored directions
 __global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __restrict__ z, const float* __restrict__ qring,
-                                                       int count, double* __restrict__ part,
-                                                       const double* __restrict__ flags) {
+                                                       double* __restrict__ part, const double* __restrict__ flags) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
+    const int count = mx_count(flags);
     double zq[MX_M] = {};
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         const double zi = z[i];
@@ -254,14 +272,16 @@ __global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __res
     }
 }
 
-// p_next = z + sum_i beta_i p_i over the stored directions (A-orthogonal to the
-// last MX_M directions) and the partial of p_next.r (the next alpha's numerator,
-// slot by parity)
+// p_k = z + sum_i beta_i p_i over the stored directions (A-orthogonal to the
+// last MX_M directions), k the iteration count, and the partial of p_k.r (the
+// next alpha's numerator, slot by the parity of k - 1)
 __global__ void __launch_bounds__(MX_THREADS) k_update_pm32(i64 n, float* __restrict__ pring, const float* __restrict__ z,
-                                                            const float* __restrict__ r, int count, int next, int parity,
-                                                            double* __restrict__ part, const double* __restrict__ flags) {
+                                                            const float* __restrict__ r, double* __restrict__ part,
+                                                            const double* __restrict__ flags) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
+    const i64 k = i64(flags[S_ITERS]);
+    const int count = mx_count(flags), next = int(k % MX_M), parity = int((k - 1) & 1);
     float beta[MX_M];
 #pragma unroll
     for (int s = 0; s < MX_M; ++s) beta[s] = s < count ? float(flags[S_BETA + s]) : 0.0f;
@@ -284,10 +304,12 @@ __global__ void k_widen(i64 n, const float* __restrict__ a, double* __restrict__
 }
 
 void precondition32(Ctx& ctx, IncompleteCholesky* M, const float* r, float* z, const double* part, const double* flags,
-                    double tol2) {
+                    double tol2, int sweeps) {
     const i64 n = ctx.mx.n;
     if (!M) {
         NL_LAUNCH(k_copy32, RED_BLOCKS, MX_THREADS, 0, ctx.stream, n, r, z, part, flags, tol2);
+    } else if (sweeps > 0) {
+        jacobi_apply32(ctx, *M, sweeps, r, z, flags);
     } else if (M->fwd_plan.ok && M->bwd_plan.ok && !ctx.force_global_sweeps) {
         sweep_apply32(ctx, *M, r, z, part, flags, tol2);
     } else {
@@ -305,13 +327,13 @@ void precondition32(Ctx& ctx, IncompleteCholesky* M, const float* r, float* z, c
 void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y) {
     NL_LAUNCH(k_spmv32, RED_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p, reinterpret_cast<const int4*>(A.col.p),
               reinterpret_cast<const float4*>(A.val32.p), A.rowsum32.p, x, y, static_cast<double*>(nullptr),
-              static_cast<const double*>(nullptr));
+              static_cast<const double*>(nullptr), i64(0));
 }
 
-void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z) {
+void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, int sweeps) {
     ctx.mx.n = ic.n;
     ctx.mx.r64.reserve(size_t(ic.n)); ctx.mx.q64.reserve(size_t(ic.n));
-    precondition32(ctx, &ic, r, z, nullptr, nullptr, 0.0);
+    precondition32(ctx, &ic, r, z, nullptr, nullptr, 0.0, sweeps);
 }
 
 void matrix_to_f32(Ctx& ctx, Csr& A) {
@@ -326,9 +348,14 @@ void matrix_to_f32(Ctx& ctx, Csr& A) {
 // then the FP32 correction d is added to x in FP64, the residual is replaced
 // by the true FP64 residual b - A x, and the iteration continues with the
 // same search direction (no Krylov restart).  Every vector keeps the scale
-// s0 = |r0| of the first residual (FP32 precision is scale-free).
+// s0 = |r0| of the first residual (FP32 precision is scale-free).  Every
+// index an iteration needs (direction slot, partial slot) is derived on the
+// device from the iteration count, so all iterations launch the same kernels
+// with the same arguments: after the first chunk, a chunk of MX_ITERS
+// iterations is captured once per solve and replayed as one CUDA graph (not
+// with the learned correction, whose network runs outside graphs).
 CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double* b, double* x, double tolerance,
-                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned) {
+                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps) {
     NL_REQUIRE(A.val32.n == size_t(A.nnz), NLGPU_ERR_STATE, "the FP32 copy of the matrix is missing");
     NL_REQUIRE(!learned || (M && ctx.mp.ready && ctx.mp.n == A.rows), NLGPU_ERR_STATE,
                "the learned correction needs ILLT and a prepared network");
@@ -350,7 +377,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     const double eta2 = update_factor * update_factor;
     CgResult res;
     auto precondition = [&](const double* pt, const double* fl, double t2) {
-        precondition32(ctx, M, w.r.p, w.z.p, pt, fl, t2);
+        precondition32(ctx, M, w.r.p, w.z.p, pt, fl, t2, sweeps);
         if (learned) mpnn_apply(ctx, w.r.p, w.z.p, w.z.p, false);
     };
     // |b|^2 and the first residual
@@ -381,28 +408,59 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.r.p, w.z.p, part + P_RZ_B * RED_BLOCKS);
     const double cap = double(std::min<i64>(max_iterations, i64(1) << 40));
     double last_rr = hs[1];
-    i64 k = 0;   // iteration about to run: direction slot k mod MX_M, rz slot by parity of k
+    i64 k = 0;
     i64 iters_at_update = 0;
+    // one iteration k (k read on the device): q_j = A p_j (j = k mod MX_M),
+    // alpha, d and r, the count and stop test, z = P(r), the betas, p_k+1
+    auto iteration = [&] {
+        NL_LAUNCH(k_spmv32, G, MX_THREADS, 0, ctx.stream, n, A.rowptr.p, reinterpret_cast<const int4*>(A.col.p),
+                  reinterpret_cast<const float4*>(A.val32.p), A.rowsum32.p, w.p.p, w.q.p, part + M_PQ * RED_BLOCKS,
+                  flags, n);
+        NL_LAUNCH(k_alpha32, 1, MX_THREADS, 0, ctx.stream, part, flags);
+        NL_LAUNCH(k_update_dr32, G, MX_THREADS, 0, ctx.stream, n, w.d.p, w.r.p, w.p.p, w.q.p, part, flags);
+        NL_LAUNCH(k_check32, 1, MX_THREADS, 0, ctx.stream, part, flags, eta2, cap);
+        precondition(part, flags, eta2);
+        NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, part, flags);
+        NL_LAUNCH(k_betas32, 1, MX_THREADS, 0, ctx.stream, part, flags);
+        NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags);
+    };
+    bool eager_done = false, captured = false;
+    auto run_chunk = [&] {
+        if (learned || !eager_done) {   // the first chunk also makes every lazy allocation
+            for (int it = 0; it < MX_ITERS; ++it) iteration();
+            eager_done = true;
+            return;
+        }
+        if (!captured) {
+            cudaGraph_t g = nullptr;
+            const i64 before = g_launches.load();
+            NL_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+            for (int it = 0; it < MX_ITERS; ++it) iteration();
+            NL_CUDA(cudaStreamEndCapture(ctx.stream, &g));
+            w.chunk_kernels = int(g_launches.load() - before);
+            g_launches.fetch_sub(w.chunk_kernels);   // counted when the graph is launched
+            cudaError_t e = cudaErrorGraphExecUpdateFailure;
+            if (w.chunk) {
+                cudaGraphExecUpdateResultInfo info;
+                e = cudaGraphExecUpdate(w.chunk, g, &info);
+                if (e != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    cudaGraphExecDestroy(w.chunk);
+                    w.chunk = nullptr;
+                }
+            }
+            if (e != cudaSuccess) e = cudaGraphInstantiate(&w.chunk, g, 0);
+            cudaGraphDestroy(g);
+            NL_CUDA(e);
+            captured = true;
+        }
+        NL_CUDA(cudaGraphLaunch(w.chunk, ctx.stream));
+        g_launches.fetch_add(w.chunk_kernels);
+    };
     for (;;) {
         bool forced = false;
         for (;;) {
-            for (int it = 0; it < MX_ITERS; ++it, ++k) {
-                const int parity = int(k & 1), slot = int(k % MX_M), next = int((k + 1) % MX_M);
-                const int count = int(std::min<i64>(k + 1, MX_M));
-                float* pj = w.p.p + i64(slot) * n;
-                float* qj = w.q.p + i64(slot) * n;
-                NL_LAUNCH(k_spmv32, G, MX_THREADS, 0, ctx.stream, n, A.rowptr.p, reinterpret_cast<const int4*>(A.col.p),
-                          reinterpret_cast<const float4*>(A.val32.p), A.rowsum32.p, pj, qj,
-                          part + (M_PQ + slot) * RED_BLOCKS, flags);
-                NL_LAUNCH(k_alpha32, 1, MX_THREADS, 0, ctx.stream, part, parity, slot, flags);
-                NL_LAUNCH(k_update_dr32, G, MX_THREADS, 0, ctx.stream, n, w.d.p, w.r.p, pj, qj, part, flags);
-                NL_LAUNCH(k_check32, 1, MX_THREADS, 0, ctx.stream, part, flags, eta2, cap);
-                precondition(part, flags, eta2);
-                NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, count, part, flags);
-                NL_LAUNCH(k_betas32, 1, MX_THREADS, 0, ctx.stream, part, count, flags);
-                NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, count, next, parity, part,
-                          flags);
-            }
+            run_chunk();
             double hf[8];
             NL_CUDA(cudaMemcpyAsync(hf, flags, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
             NL_CUDA(cudaStreamSynchronize(ctx.stream));
@@ -436,13 +494,11 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
                       part + ((k & 1) ? P_RZ_A : P_RZ_B) * RED_BLOCKS);
         } else {
             // the stop skipped p_k: z = P(r), p_k = z - sum_i (z.q_i / p_i.q_i) p_i as at
-            // the end of iteration k - 1
+            // the end of iteration k - 1 (the kernels read k from the count)
             precondition(nullptr, nullptr, 0.0);
-            const int count = int(std::min<i64>(k, MX_M)), parity = int((k + 1) & 1);
-            NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, count, part, flags);
-            NL_LAUNCH(k_betas32, 1, MX_THREADS, 0, ctx.stream, part, count, flags);
-            NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, count, next, parity, part,
-                      flags);
+            NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, part, flags);
+            NL_LAUNCH(k_betas32, 1, MX_THREADS, 0, ctx.stream, part, flags);
+            NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags);
         }
     }
     return res;

@@ -545,7 +545,7 @@ void mpnn_train(Ctx& ctx, const Csr& A, IncompleteCholesky& M, const double* b_g
     // the plain ILLT error on the same pairs: (z - e)^T A (z - e) / e^T A e
     m.d.reserve(size_t(n)); m.ad.reserve(size_t(n)); m.part2.reserve(RED_BLOCKS);
     for (i64 k = 0; k < S; ++k) {
-        ilt_apply32(ctx, M, R[size_t(k)].p, z.p);
+        ilt_apply32(ctx, M, R[size_t(k)].p, z.p, ctx.ilt_sweeps);
         spmv32(ctx, A, E[size_t(k)].p, m.ad.p);
         NL_LAUNCH(k_mp_dot, RED_BLOCKS, MP_THREADS, 0, ctx.stream, n, E[size_t(k)].p, m.ad.p, m.part2.p);
         NL_LAUNCH(k_mp_finish, 1, MP_THREADS, 0, ctx.stream, m.part2.p, m.sc.p, SC_EE, ee.p + k);
@@ -564,7 +564,7 @@ void mpnn_train(Ctx& ctx, const Csr& A, IncompleteCholesky& M, const double* b_g
             const i64 k1 = std::min<i64>(S, k0 + o.batch);
             for (i64 k = k0; k < k1; ++k) {
                 const i64 s = order[size_t(k)];
-                ilt_apply32(ctx, M, R[size_t(s)].p, z.p);
+                ilt_apply32(ctx, M, R[size_t(s)].p, z.p, ctx.ilt_sweeps);
                 mpnn_backward(ctx, A, R[size_t(s)].p, z.p, E[size_t(s)].p, p.p, num.p + s, ee.p + s);
             }
             mpnn_adam_step(ctx, float(o.learning_rate), int(k1 - k0));
@@ -584,7 +584,8 @@ void mpnn_train(Ctx& ctx, const Csr& A, IncompleteCholesky& M, const double* b_g
         xv.resize(size_t(n));
         auto timed = [&](bool learned, double& secs) {
             const auto s0 = std::chrono::steady_clock::now();
-            const CgResult r = mixed_solve(ctx, A, &M, b_given, xv.p, 1e-10, 20 * n + 1000, 1e-2, false, learned);
+            const CgResult r = mixed_solve(ctx, A, &M, b_given, xv.p, 1e-10, 20 * n + 1000, 1e-2, false, learned,
+                                           ctx.ilt_sweeps);
             NL_CUDA(cudaStreamSynchronize(ctx.stream));
             secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - s0).count();
             return r;

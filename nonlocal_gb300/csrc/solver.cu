@@ -476,6 +476,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     ic.col.upload(col.data(), col.size(), ctx.stream);
     ic.y.resize(size_t(n + 1)); ic.w.resize(size_t(n + 1));
     ic.y32.resize(size_t(n + 1)); ic.w32.resize(size_t(n + 1));
+    jacobi_build(ctx, ic, rp, col, lrp, lcol, l_to_u);
     // Lin-More scaling and the shifted factorisation
     ic.scale.resize(size_t(n)); ic.scale.zero(ctx.stream);
     ic.scale32.resize(size_t(n));
@@ -511,6 +512,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     }
     ic.shift = shift;
     if (!ic.ok) return;
+    jacobi_fill(ctx, ic);
     if (ic.fwd_plan.ok && ic.bwd_plan.ok) {
         sweep_plan_fill(ctx, ic.fwd_plan, ic.u.p);
         sweep_plan_fill(ctx, ic.bwd_plan, ic.u.p);

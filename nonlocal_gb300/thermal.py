@@ -212,18 +212,22 @@ class Problem2D(Context):
 
     # ---- solves -----------------------------------------------------------------
     @staticmethod
-    def _options(tolerance, max_iterations, preconditioner, precision, inner_tolerance=0.0) -> L.SolveOptions:
+    def _options(tolerance, max_iterations, preconditioner, precision, inner_tolerance=0.0,
+                 triangular_sweeps=0) -> L.SolveOptions:
         o = L.SolveOptions()
         o.tolerance, o.max_iterations = float(tolerance), int(max_iterations)
         o.preconditioner, o.precision = L.PRECONDITIONER[preconditioner], L.PRECISION[precision]
         o.inner_tolerance = float(inner_tolerance)
+        o.triangular_sweeps = int(triangular_sweeps)
         return o
 
     def stationary(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64",
-                   check_convergence=True, inner_tolerance=0.0):
+                   check_convergence=True, inner_tolerance=0.0, triangular_sweeps=0):
         """stationary_heat_equation_solver_2d; precision "mixed" runs the FP32 inner
-        solve with FP64 refinement (inner_tolerance: reduction per inner solve)."""
-        o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance)
+        solve with FP64 refinement (inner_tolerance: reduction per inner solve;
+        triangular_sweeps: Jacobi sweeps per triangle of the FP32 ILLT application,
+        0 the default, -1 exact level-scheduled substitution)."""
+        o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance, triangular_sweeps)
         t = np.empty(self.n_nodes)
         rep = L.SolveReport()
         rc = self._lib.nlgpu_stationary_2d(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep))
@@ -232,8 +236,8 @@ class Problem2D(Context):
         return t, SolveReport(rep.as_dict())
 
     def solve_assembled(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64",
-                        inner_tolerance=0.0):
-        o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance)
+                        inner_tolerance=0.0, triangular_sweeps=0):
+        o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance, triangular_sweeps)
         t = np.empty(self.n_nodes)
         rep = L.SolveReport()
         L.check(self._lib.nlgpu_solve_assembled(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep)))
@@ -407,6 +411,15 @@ class EigenILLTPreconditioner:
         x = L.f64(x)
         y = np.empty_like(x)
         L.check(self.context._lib.nlgpu_illt_solve(self.context.handle, x.shape[0], L.ptr(x), L.ptr(y)))
+        return y
+
+    def solve_f32(self, x, sweeps=L.DEFAULT_TRIANGULAR_SWEEPS) -> np.ndarray:
+        """M^-1 x in FP32 as the mixed-precision solve applies it: ``sweeps`` Jacobi
+        sweeps per triangle, or -1 for the exact level-scheduled sweeps."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty_like(x)
+        L.check(self.context._lib.nlgpu_illt_solve_f32(self.context.handle, x.shape[0], int(sweeps), L.ptr(x),
+                                                       L.ptr(y)))
         return y
 
 

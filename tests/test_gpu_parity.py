@@ -143,11 +143,13 @@ def test_mixed_precision_solution(golden):
     _, fx, pb = golden
     if fx["config"].get("local_weight", 1) < 0.999:
         pb.find_neighbours(fx["config"].get("strategy", "MAX"))
-    for pre in ("illt", "identity"):
-        t, rep = pb.stationary(tolerance=1e-13, max_iterations=50000, preconditioner=pre, precision="mixed")
+    # ILLT applied by Jacobi sweeps (the default) and by exact level-scheduled sweeps
+    for pre, sweeps in (("illt", 0), ("illt", -1), ("identity", 0)):
+        t, rep = pb.stationary(tolerance=1e-13, max_iterations=50000, preconditioner=pre, precision="mixed",
+                               triangular_sweeps=sweeps)
         assert rep.residual <= 1e-13
         assert rep.outer_iterations >= 1 and rep.iterations > 0
-        assert rel(t, fx["temperature"]) < SOLUTION_RTOL, pre
+        assert rel(t, fx["temperature"]) < SOLUTION_RTOL, (pre, sweeps)
 
 
 @pytest.mark.parametrize("name", ["b12_fastpoly", "s6_exp_ortho_jitter"])
@@ -335,10 +337,56 @@ def test_against_oracle_scaled(lib, case):
     assert rel(t, prob.get("solution")) < SOLUTION_RTOL
     # same preconditioner (fixed-pattern IC(0) on the scaled, shifted local matrix): iteration counts agree
     assert abs(rep.iterations - prob.scalar("iterations")) <= 2
-    # the mixed-precision form against the FP64 oracle solution
-    tm, repm = pb.solve_assembled(tolerance=1e-13, precision="mixed")
-    assert repm.residual <= 1e-13
-    assert rel(tm, prob.get("solution")) < SOLUTION_RTOL
+    # the mixed-precision form against the FP64 oracle solution (Jacobi and exact sweeps)
+    for sweeps in (0, -1):
+        tm, repm = pb.solve_assembled(tolerance=1e-13, precision="mixed", triangular_sweeps=sweeps)
+        assert repm.residual <= 1e-13
+        assert rel(tm, prob.get("solution")) < SOLUTION_RTOL, sweeps
+
+
+def test_illt_jacobi_sweeps(lib):
+    """The FP32 ILLT application of the mixed solve: k Jacobi sweeps per triangle
+    equal the first k + 1 terms of the Neumann series of each triangular inverse,
+    computed here in FP64 from the oracle's factor of the same matrix; exact
+    FP32 sweeps and enough Jacobi sweeps (more than the level count) reproduce
+    the exact FP64 application."""
+    import scipy.sparse as sp
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    mesh = structured_quad_mesh(20, 20, "serendipity", jitter=0.2, seed=0)
+    model = dict(influence="exponential", radius=(0.15, 0.15), local_weight=0.3, conductivity=(1.0, 0.1))
+    prob, _ = oracle_and_gpu(mesh, model, [("up", "temperature", 1.0), ("down", "temperature", 0.0)], lib)
+    prob.find_neighbours()
+    prob.assemble()
+    prob.assemble_local()
+    prob.solve(variant=1, tol=1e-6)   # the fixed-pattern IC(0) factor the CUDA path computes
+    rp, col, val = prob.csr("K_local")
+    n = rp.shape[0] - 1
+    pre = T.EigenILLTPreconditioner()
+    assert pre.compute((rp, col, val)).computation_info() == pre.SUCCESS
+    u = sp.csr_matrix((prob.get("L_val"), prob.get("L_col"), prob.get("L_rowptr")), shape=(n, n))
+    s, d = prob.get("L_scale"), u.diagonal()
+    upper = sp.diags(1.0 / d) @ sp.triu(u, 1).tocsr()          # D^-1 N^T
+    lower = sp.diags(1.0 / d) @ sp.triu(u, 1).T.tocsr()        # D^-1 N
+
+    def neumann(x, k):
+        c = s / d
+        y = c * x
+        for _ in range(k):
+            y = c * x - lower @ y
+        yt = y / d
+        z = yt.copy()
+        for _ in range(k):
+            z = yt - upper @ z
+        return s * z
+
+    x = np.random.default_rng(5).standard_normal(n)
+    for k in (1, 2, 6):
+        assert rel(pre.solve_f32(x, k).astype(np.float64), neumann(x, k)) < 2e-5, k
+    exact = pre.solve(x)
+    assert rel(pre.solve_f32(x, -1).astype(np.float64), exact) < 2e-5
+    assert rel(pre.solve_f32(x, n).astype(np.float64), exact) < 1e-4
+    assert rel(neumann(x, 6), exact) > 1e-3   # six sweeps are an approximation here
 
 
 def test_operator_annihilates_constants_full_size(lib):
