@@ -298,7 +298,9 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     n = pb.n_nodes
     nnz_solver = rep.nnz_solver
     spmv_bytes = nnz_solver * (8 + 4) + (n + 1) * 8 + 2 * n * 8
-    spmv32_bytes = nnz_solver * (4 + 4) + (n + 1) * 8 + 2 * n * 4
+    # FP32 values, int32 columns or 16-bit row offsets, row pointers, x, the row
+    # sums and y once each
+    spmv32_bytes = nnz_solver * (4 + rep.column_bytes) + (n + 1) * 8 + 3 * n * 4
     outer = rep.outer_iterations
     # per solve of the primary (mixed) method: inner FP32 SpMV and sweeps per inner
     # iteration (+1 start per outer step), FP64 SpMV per outer residual

@@ -115,6 +115,7 @@ typedef struct nlgpu_solve_report {
            seconds_preconditioner, seconds_solve, seconds_total;
     int64_t outer_iterations; /* MIXED: FP64 refinement steps (iterations counts the inner ones) */
     int learned_fallback;     /* ILLT_LEARNED: 1 when the correction was gated off or stalled */
+    int column_bytes;         /* MIXED: bytes per column index the FP32 SpMV reads (2: 16-bit row offsets) */
 } nlgpu_solve_report;
 
 /* ---- library ------------------------------------------------------------ */

@@ -57,7 +57,7 @@ class SolveReport(ctypes.Structure):
                 ("element_pairs", c_i64), ("seconds_neighbours", c_d), ("seconds_pattern", c_d),
                 ("seconds_assembly", c_d), ("seconds_boundary", c_d), ("seconds_preconditioner", c_d),
                 ("seconds_solve", c_d), ("seconds_total", c_d), ("outer_iterations", c_i64),
-                ("learned_fallback", c_int)]
+                ("learned_fallback", c_int), ("column_bytes", c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -104,6 +104,7 @@ void fill_report(Ctx& c, nlgpu_solve_report* rep, const CgResult& r) {
     rep->element_pairs = c.pairs;
     rep->outer_iterations = r.outer_iterations;
     rep->learned_fallback = r.learned_fallback ? 1 : 0;
+    rep->column_bytes = c.full.col16_ok ? 2 : 4;
 }
 
 CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep) {
@@ -127,9 +128,15 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     NL_REQUIRE(!learned || c.mp.weights_set, NLGPU_ERR_STATE, "train the learned correction or set its weights first");
     const IncompleteCholesky* M = nullptr;
     auto t0 = std::chrono::steady_clock::now();
+    PhaseTimer timer(c.stream, "solve_system");
+    const bool mixed = o.precision == NLGPU_PRECISION_MIXED || learned;
+    const int sweeps = o.triangular_sweeps == 0 ? NLGPU_DEFAULT_TRIANGULAR_SWEEPS : std::max(o.triangular_sweeps, 0);
     if (o.preconditioner != NLGPU_PRECONDITIONER_IDENTITY) {
         if (!c.local_ready) build_local(c);
-        ilt_build(c, c.local, c.ilt);
+        timer.mark("local matrix");
+        // the exact sweeps' shared-memory plans only when this solve uses them
+        ilt_build(c, c.local, c.ilt, !(mixed && sweeps > 0));
+        timer.mark("preconditioner");
         if (c.ilt.ok) M = &c.ilt;   // identity fallback (stationary_heat_equation_solver_2d.hpp:97-101)
         if (learned && M && !(c.mp.ready && c.mp.n == c.local.rows)) mpnn_prepare(c, c.local);
     } else {
@@ -140,9 +147,10 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     t0 = std::chrono::steady_clock::now();
     c.temperature.resize(size_t(c.n_nodes));
     CgResult r;
-    if (o.precision == NLGPU_PRECISION_MIXED || learned) {
+    if (mixed) {
         matrix_to_f32(c, c.full);
-        c.ilt_sweeps = o.triangular_sweeps == 0 ? NLGPU_DEFAULT_TRIANGULAR_SWEEPS : std::max(o.triangular_sweeps, 0);
+        timer.mark("FP32 matrix");
+        c.ilt_sweeps = sweeps;
         r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations,
                         o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M && c.mp.use,
                         c.ilt_sweeps);
@@ -891,7 +899,7 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
             NL_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), c.stream));
             NL_CUDA(cudaMemsetAsync(x32.p, 0, x32.bytes(), c.stream));
             if (stage == 2 || stage >= 5) NL_REQUIRE(c.ilt.ok, NLGPU_ERR_STATE, "no ILLT factor");
-            if (stage == 4 && c.full.val32.n != size_t(c.full.nnz)) matrix_to_f32(c, c.full);
+            if (stage == 4 && (c.full.val32.n != size_t(c.full.nnz) || !c.full.col16_ok)) matrix_to_f32(c, c.full);
         }
         if (stage == 1) NL_REQUIRE(c.inner.nnz > 0 && c.model.nonlocal(), NLGPU_ERR_STATE, "no nonlocal pattern");
         if (stage == 3) NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "no mesh/model");

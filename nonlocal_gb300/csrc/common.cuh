@@ -5,8 +5,10 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <functional>
 #include <stdexcept>
 #include <string>
@@ -48,6 +50,25 @@ extern std::atomic<int64_t> g_launches;
         ::nlgpu::g_launches.fetch_add(1, std::memory_order_relaxed);           \
         NL_CUDA(cudaGetLastError());                                           \
     } while (0)
+
+// Diagnostics: with NLGPU_DEBUG_TIMING set in the environment, mark() prints
+// the wall time since the previous mark (after synchronising the stream).
+struct PhaseTimer {
+    cudaStream_t stream;
+    const char* scope;
+    bool on;
+    std::chrono::steady_clock::time_point t;
+    PhaseTimer(cudaStream_t s, const char* name)
+        : stream{s}, scope{name}, on{std::getenv("NLGPU_DEBUG_TIMING") != nullptr}, t{std::chrono::steady_clock::now()} {}
+    void mark(const char* what) {
+        if (!on) return;
+        cudaStreamSynchronize(stream);
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[nlgpu timing] %s/%s %.3f ms\n", scope, what,
+                     std::chrono::duration<double, std::milli>(now - t).count());
+        t = now;
+    }
+};
 
 inline unsigned grid_for(i64 n, int block, i64 cap = 152 * 32) {
     i64 g = (n + block - 1) / block;
@@ -126,6 +147,8 @@ struct Csr {
     dbuf<double> val;
     dbuf<float> val32;
     dbuf<float> rowsum32;        // row sums of the FP64 values (difference-form FP32 SpMV)
+    dbuf<int16_t> col16;         // column - row, when every entry's offset fits 16 bits
+    bool col16_ok = false;
 };
 
 struct BoundaryGroup {
@@ -268,6 +291,7 @@ struct MixedWork {
     dbuf<double> r64, q64;       // outer residual and A x
     dbuf<float> r, z, p, q, d;   // inner vectors
     dbuf<double> partial, outer, flags;
+    dbuf<unsigned> ticket;             // blocks done in the current reducing kernel
     cudaGraphExec_t chunk = nullptr;   // a chunk of inner iterations, re-captured per solve
     int chunk_kernels = 0;
     MixedWork() = default;
@@ -370,7 +394,9 @@ void combine_nonstationary(Ctx& ctx, double dt);
 void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values);
 // solver.cu
 void spmv_full(Ctx& ctx, const Csr& A, const double* x, double* y);
-void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic);
+// tma_plans: also build the TMA-fed shared-memory sweep plans of the exact
+// triangular solves (without them exact solves use the global-memory sweeps)
+void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plans = true);
 void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* z);
 struct CgResult {
     i64 iterations = 0, outer_iterations = 0;

@@ -20,9 +20,11 @@
 // the sweeps, the learned correction added to the ILLT output).  The reliable
 // updates keep the directions, so no Krylov restart is paid per update.  The
 // FP32 SpMV runs in difference form against the FP64 row sums (see k_spmv32)
-// and moves 8 bytes per entry instead of 12.  Scalars stay on the device
-// (block partials re-summed by each consuming block); the host reads the done
-// flag once per MX_ITERS iterations.
+// and moves 8 bytes per entry instead of 12 (6 with 16-bit column offsets).
+// Scalars stay on the device: the block that finishes last in each reducing
+// kernel sums the block partials and forms alpha, the betas and the stop test
+// (no separate scalar kernels); the host reads the done flag once per
+// MX_ITERS iterations.
 #include "common.cuh"
 
 #include <cmath>
@@ -35,11 +37,12 @@ constexpr int MX_THREADS = 256;
 constexpr int MX_ITERS = 16;
 constexpr int MX_M = 4;   // directions kept for the A-orthogonalisation (flexible CG truncation)
 constexpr i64 MX_UPDATE_MAX = 64;   // iterations between reliable updates at most
-// partial slots: P_RR, P_RZ_A, P_RZ_B as in the FP64 solver (the sweeps' early
-// exit reads the residual there), then p_i.q_i and z.q_i of the stored directions
+// partial slots: P_RR as in the FP64 solver (the exact sweeps' early exit reads
+// the residual there), P_RZ_A / P_RZ_B for p.r, then p_i.q_i and z.q_i
 enum { M_PQ = P_COUNT, M_ZQ = P_COUNT + MX_M, M_SLOTS = P_COUNT + 2 * MX_M };
-// scalar slots after the solver's (S_BB .. S_RR_FINAL): alpha and the betas
-enum { S_ALPHA = 8, S_BETA = 9, S_MIXED_COUNT = 9 + MX_M };
+// scalar slots after the solver's (S_BB .. S_RR_FINAL): alpha, the betas, p_k.r
+// (the next alpha's numerator) and p_i.q_i of the stored directions
+enum { S_ALPHA = 8, S_BETA = 9, S_PR = 9 + MX_M, S_PQ = 10 + MX_M, S_MIXED_COUNT = 10 + 2 * MX_M };
 
 __device__ __forceinline__ double mx_block_sum(double v, double* sh) {
     v = warp_sum(v);
@@ -63,8 +66,55 @@ __device__ __forceinline__ double mx_partials(const double* part, double* sh) {
     return s;
 }
 
-__device__ __forceinline__ bool mx_converged(const double* part, const double* flags, double tol2, double* sh) {
-    return mx_partials(part + P_RR * RED_BLOCKS, sh) <= tol2 * flags[S_BB];
+// N block sums in one pass (sh: at least 33 N doubles); every thread gets them
+template<int N>
+__device__ __forceinline__ void mx_block_sums(double (&v)[N], double* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = int(blockDim.x >> 5);
+#pragma unroll
+    for (int s = 0; s < N; ++s) v[s] = warp_sum(v[s]);
+    if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < N; ++s) sh[s * 32 + warp] = v[s];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int s = 0; s < N; ++s) {
+            const double t = warp_sum(lane < nw ? sh[s * 32 + lane] : 0.0);
+            if (lane == 0) sh[32 * N + s] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < N; ++s) v[s] = sh[32 * N + s];
+    __syncthreads();
+}
+
+// Publishes this block's N sums as partials (slot s at part + s RED_BLOCKS) and
+// returns true in the block that finished last, with v replaced by the totals
+// over all blocks; that block also re-arms the ticket for the next kernel.
+// (Every later kernel of the stream starts after this one has ended.)
+template<int N>
+__device__ __forceinline__ bool mx_reduce_last(double (&v)[N], double* part, unsigned* ticket, double* sh) {
+    __shared__ unsigned last;
+    mx_block_sums<N>(v, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int s = 0; s < N; ++s) part[s * RED_BLOCKS + blockIdx.x] = v[s];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1 ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!last) return false;
+#pragma unroll
+    for (int s = 0; s < N; ++s) v[s] = 0.0;
+    for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+#pragma unroll
+        for (int s = 0; s < N; ++s) v[s] += __ldcg(part + s * RED_BLOCKS + k);
+    }
+    mx_block_sums<N>(v, sh);
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
 }
 
 // q = A32 p (FP32 values, FP32 accumulation), warp per padded full row, in
@@ -72,17 +122,22 @@ __device__ __forceinline__ bool mx_converged(const double* part, const double* f
 // of the FP64 matrix: the rows of the conductivity matrix sum to (nearly) zero,
 // so for smooth x the plain FP32 sum would cancel to a result far below the
 // rounding error of its terms, while here each FP32 entry multiplies a small
-// difference.  Partial of p.q in FP64.
-__global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restrict__ rp, const int4* __restrict__ col4,
+// difference.  p.q in FP64; in the solve the last block stores it and forms
+// alpha.  Columns are int32 (C4 = int4) or, when every |column - row| fits
+// 16 bits, int16 offsets from the row (C4 = short4): 6 instead of 8 bytes per
+// entry.
+template<class C4>
+__global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restrict__ rp, const C4* __restrict__ col4,
                                                        const float4* __restrict__ val4,
                                                        const float* __restrict__ rowsum, const float* __restrict__ x,
                                                        float* __restrict__ y, double* __restrict__ dot_partial,
-                                                       const double* __restrict__ flags, i64 ring) {
+                                                       double* __restrict__ flags, i64 ring, unsigned* ticket) {
     __shared__ double sh[40];
     if (flags && flags[S_DONE] != 0.0) return;
-    if (ring) {   // direction slot of the current iteration in the rings of x, y and the partials
-        const i64 slot = i64(flags[S_ITERS]) % MX_M;
-        x += slot * ring; y += slot * ring; dot_partial += slot * RED_BLOCKS;
+    i64 slot = 0;
+    if (ring) {   // direction slot of the current iteration in the rings of x and y
+        slot = i64(flags[S_ITERS]) % MX_M;
+        x += slot * ring; y += slot * ring;
     }
     const int lane = threadIdx.x & 31;
     const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
@@ -90,12 +145,19 @@ __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restr
     for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
         const i64 b4 = rp[r] >> 2, e4 = rp[r + 1] >> 2;
         const float xr = x[r];
+        const float* xo = sizeof(C4) == 16 ? x : x + r;   // int16 offsets count from the row
+        auto term = [&](const C4& c, const float4& v) {
+            return v.x * (xo[c.x] - xr) + v.y * (xo[c.y] - xr) + v.z * (xo[c.z] - xr) + v.w * (xo[c.w] - xr);
+        };
         float s = 0.0f;
-        for (i64 k = b4 + lane; k < e4; k += 32) {
-            const int4 c = __ldg(col4 + k);
-            const float4 v = __ldg(val4 + k);
-            s += v.x * (x[c.x] - xr) + v.y * (x[c.y] - xr) + v.z * (x[c.z] - xr) + v.w * (x[c.w] - xr);
+        // two column/value loads in flight per lane before their gathers
+        i64 k = b4 + lane;
+        for (; k + 32 < e4; k += 64) {
+            const C4 c0 = __ldg(col4 + k), c1 = __ldg(col4 + k + 32);
+            const float4 v0 = __ldg(val4 + k), v1 = __ldg(val4 + k + 32);
+            s += term(c0, v0) + term(c1, v1);
         }
+        if (k < e4) s += term(__ldg(col4 + k), __ldg(val4 + k));
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) {
             s += rowsum[r] * xr;
@@ -103,9 +165,12 @@ __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restr
             dot += double(s) * double(xr);
         }
     }
-    if (dot_partial) {
-        const double t = mx_block_sum(dot, sh);
-        if (threadIdx.x == 0) dot_partial[blockIdx.x] = t;
+    if (dot_partial) {   // p_j.q_j: the last block stores it and alpha = (p_j.r) / (p_j.q_j)
+        double v[1] = {dot};
+        if (mx_reduce_last<1>(v, dot_partial, ticket, sh) && threadIdx.x == 0) {
+            flags[S_PQ + slot] = v[0];
+            flags[S_ALPHA] = flags[S_PR] / v[0];
+        }
     }
 }
 
@@ -145,6 +210,30 @@ __global__ void k_to_f32(i64 n, const double* __restrict__ a, float* __restrict_
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) b[i] = float(a[i]);
 }
 
+// largest |column - row| of the matrix (warp per row)
+__global__ void k_max_offset(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col,
+                             unsigned long long* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
+    unsigned long long m = 0;
+    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps)
+        for (i64 k = rp[r] + lane; k < rp[r + 1]; k += 32) {
+            const i64 d = i64(col[k]) - r;
+            m = max(m, static_cast<unsigned long long>(d < 0 ? -d : d));
+        }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m) atomicMax(out, m);
+}
+
+// col16 = column - row (offsets checked to fit 16 bits)
+__global__ void k_col_offsets(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col,
+                              int16_t* __restrict__ col16) {
+    const int lane = threadIdx.x & 31;
+    const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
+    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps)
+        for (i64 k = rp[r] + lane; k < rp[r + 1]; k += 32) col16[k] = int16_t(i64(col[k]) - r);
+}
+
 // partial of a.b
 __global__ void __launch_bounds__(MX_THREADS) k_dot32(i64 n, const float* __restrict__ a, const float* __restrict__ b,
                                                       double* __restrict__ partial) {
@@ -181,37 +270,9 @@ __global__ void k_refine(i64 n, double* __restrict__ x, float* __restrict__ d32,
     }
 }
 
-__global__ void k_copy32(i64 n, const float* __restrict__ a, float* __restrict__ b, const double* __restrict__ part,
-                         const double* __restrict__ flags, double tol2) {
-    __shared__ double sh[40];
-    if (flags && (flags[S_DONE] != 0.0 || mx_converged(part, flags, tol2, sh))) return;
+__global__ void k_copy32(i64 n, const float* __restrict__ a, float* __restrict__ b, const double* __restrict__ flags) {
+    if (flags && flags[S_DONE] != 0.0) return;
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) b[i] = a[i];
-}
-
-// one block: alpha = p_j.r / p_j.q_j into the scalars
-__global__ void __launch_bounds__(MX_THREADS) k_alpha32(const double* __restrict__ part, double* __restrict__ flags) {
-    __shared__ double sh[40];
-    if (flags[S_DONE] != 0.0) return;
-    const i64 k = i64(flags[S_ITERS]);
-    const int parity = int(k & 1), slot = int(k % MX_M);
-    const double pq = mx_partials(part + (M_PQ + slot) * RED_BLOCKS, sh);
-    const double pr = mx_partials(part + (parity ? P_RZ_A : P_RZ_B) * RED_BLOCKS, sh);
-    if (threadIdx.x == 0) flags[S_ALPHA] = pr / pq;
-}
-
-// one block: counts the iteration; the done flag when |r| <= tol |r_update| or
-// the iteration cap is reached.  The kernels after it in the iteration read
-// the new count (k + 1).
-__global__ void __launch_bounds__(MX_THREADS) k_check32(const double* __restrict__ part, double* __restrict__ flags,
-                                                        double tol2, double max_iterations) {
-    __shared__ double sh[40];
-    if (flags[S_DONE] != 0.0) return;
-    const bool converged = mx_converged(part, flags, tol2, sh);
-    if (threadIdx.x == 0) {
-        const double it = flags[S_ITERS] + 1.0;
-        flags[S_ITERS] = it;
-        if (converged || it >= max_iterations) flags[S_DONE] = 1.0;
-    }
 }
 
 // directions stored after k iterations
@@ -219,21 +280,13 @@ __device__ __forceinline__ int mx_count(const double* flags) {
     return int(min(i64(flags[S_ITERS]), i64(MX_M)));
 }
 
-// one block: beta_i = -(z.q_i) / (p_i.q_i) into the scalars
-__global__ void __launch_bounds__(MX_THREADS) k_betas32(const double* __restrict__ part, double* __restrict__ flags) {
-    __shared__ double sh[40];
-    if (flags[S_DONE] != 0.0) return;
-    const int count = mx_count(flags);
-    for (int s = 0; s < count; ++s) {
-        const double b = -mx_partials(part + (M_ZQ + s) * RED_BLOCKS, sh) / mx_partials(part + (M_PQ + s) * RED_BLOCKS, sh);
-        if (threadIdx.x == 0) flags[S_BETA + s] = b;
-    }
-}
-
-// d += alpha p_j; r -= alpha q_j (j the current direction slot); partial of r.r
+// d += alpha p_j; r -= alpha q_j (j the current direction slot); r.r.  The last
+// block counts the iteration and sets the done flag when |r| <= tol |r_update|
+// or the iteration cap is reached; the kernels after it read the new count.
 __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __restrict__ d, float* __restrict__ r,
                                                             const float* __restrict__ p, const float* __restrict__ q,
-                                                            double* __restrict__ part, const double* __restrict__ flags) {
+                                                            double* __restrict__ part, double* __restrict__ flags,
+                                                            unsigned* ticket, double tol2, double max_iterations) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
     const i64 slot = i64(flags[S_ITERS]) % MX_M;
@@ -247,14 +300,19 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __rest
         r[i] = v;
         s += double(v) * double(v);
     }
-    const double t = mx_block_sum(s, sh);
-    if (threadIdx.x == 0) part[P_RR * RED_BLOCKS + blockIdx.x] = t;
+    double v[1] = {s};
+    if (mx_reduce_last<1>(v, part + P_RR * RED_BLOCKS, ticket, sh) && threadIdx.x == 0) {
+        const double it = flags[S_ITERS] + 1.0;
+        flags[S_ITERS] = it;
+        if (v[0] <= tol2 * flags[S_BB] || it >= max_iterations) flags[S_DONE] = 1.0;
+    }
 }
 
-// partials of z.q_i for the stored directions
+// z.q_i for the stored directions; the last block forms beta_i = -(z.q_i) / (p_i.q_i)
 __global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __restrict__ z, const float* __restrict__ qring,
-                                                       double* __restrict__ part, const double* __restrict__ flags) {
-    __shared__ double sh[40];
+                                                       double* __restrict__ part, double* __restrict__ flags,
+                                                       unsigned* ticket) {
+    __shared__ double sh[33 * MX_M];
     if (flags[S_DONE] != 0.0) return;
     const int count = mx_count(flags);
     double zq[MX_M] = {};
@@ -264,24 +322,20 @@ __global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __res
         for (int s = 0; s < MX_M; ++s)
             if (s < count) zq[s] += zi * double(qring[i64(s) * n + i]);
     }
-#pragma unroll
-    for (int s = 0; s < MX_M; ++s) {
-        if (s >= count) break;
-        const double ts = mx_block_sum(zq[s], sh);
-        if (threadIdx.x == 0) part[(M_ZQ + s) * RED_BLOCKS + blockIdx.x] = ts;
-    }
+    if (mx_reduce_last<MX_M>(zq, part + M_ZQ * RED_BLOCKS, ticket, sh) && threadIdx.x == 0)
+        for (int s = 0; s < count; ++s) flags[S_BETA + s] = -zq[s] / flags[S_PQ + s];
 }
 
 // p_k = z + sum_i beta_i p_i over the stored directions (A-orthogonal to the
-// last MX_M directions), k the iteration count, and the partial of p_k.r (the
-// next alpha's numerator, slot by the parity of k - 1)
+// last MX_M directions), k the iteration count, and p_k.r (the next alpha's
+// numerator, stored by the last block)
 __global__ void __launch_bounds__(MX_THREADS) k_update_pm32(i64 n, float* __restrict__ pring, const float* __restrict__ z,
                                                             const float* __restrict__ r, double* __restrict__ part,
-                                                            const double* __restrict__ flags) {
+                                                            double* __restrict__ flags, unsigned* ticket) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
     const i64 k = i64(flags[S_ITERS]);
-    const int count = mx_count(flags), next = int(k % MX_M), parity = int((k - 1) & 1);
+    const int count = mx_count(flags), next = int(k % MX_M);
     float beta[MX_M];
 #pragma unroll
     for (int s = 0; s < MX_M; ++s) beta[s] = s < count ? float(flags[S_BETA + s]) : 0.0f;
@@ -295,8 +349,8 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_pm32(i64 n, float* __rest
         pn[i] = v;   // may overwrite the oldest direction: element i was read above
         pr += double(v) * double(r[i]);
     }
-    const double t = mx_block_sum(pr, sh);
-    if (threadIdx.x == 0) part[(parity ? P_RZ_B : P_RZ_A) * RED_BLOCKS + blockIdx.x] = t;
+    double v[1] = {pr};
+    if (mx_reduce_last<1>(v, part + P_RZ_A * RED_BLOCKS, ticket, sh) && threadIdx.x == 0) flags[S_PR] = v[0];
 }
 
 __global__ void k_widen(i64 n, const float* __restrict__ a, double* __restrict__ b) {
@@ -307,7 +361,7 @@ void precondition32(Ctx& ctx, IncompleteCholesky* M, const float* r, float* z, c
                     double tol2, int sweeps) {
     const i64 n = ctx.mx.n;
     if (!M) {
-        NL_LAUNCH(k_copy32, RED_BLOCKS, MX_THREADS, 0, ctx.stream, n, r, z, part, flags, tol2);
+        NL_LAUNCH(k_copy32, RED_BLOCKS, MX_THREADS, 0, ctx.stream, n, r, z, flags);
     } else if (sweeps > 0) {
         jacobi_apply32(ctx, *M, sweeps, r, z, flags);
     } else if (M->fwd_plan.ok && M->bwd_plan.ok && !ctx.force_global_sweeps) {
@@ -322,12 +376,22 @@ void precondition32(Ctx& ctx, IncompleteCholesky* M, const float* r, float* z, c
     }
 }
 
+void launch_spmv32(Ctx& ctx, const Csr& A, const float* x, float* y, double* dot_partial, double* flags, i64 ring,
+                   unsigned* ticket) {
+    const auto* val4 = reinterpret_cast<const float4*>(A.val32.p);
+    if (A.col16_ok)
+        NL_LAUNCH(k_spmv32<short4>, RED_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p,
+                  reinterpret_cast<const short4*>(A.col16.p), val4, A.rowsum32.p, x, y, dot_partial, flags, ring,
+                  ticket);
+    else
+        NL_LAUNCH(k_spmv32<int4>, RED_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p,
+                  reinterpret_cast<const int4*>(A.col.p), val4, A.rowsum32.p, x, y, dot_partial, flags, ring, ticket);
+}
+
 }  // namespace
 
 void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y) {
-    NL_LAUNCH(k_spmv32, RED_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p, reinterpret_cast<const int4*>(A.col.p),
-              reinterpret_cast<const float4*>(A.val32.p), A.rowsum32.p, x, y, static_cast<double*>(nullptr),
-              static_cast<const double*>(nullptr), i64(0));
+    launch_spmv32(ctx, A, x, y, nullptr, nullptr, 0, nullptr);
 }
 
 void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, int sweeps) {
@@ -336,11 +400,27 @@ void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, int
     precondition32(ctx, &ic, r, z, nullptr, nullptr, 0.0, sweeps);
 }
 
+// FP32 values and FP64 row sums of the solver matrix, and 16-bit column
+// offsets when the pattern's bandwidth allows
 void matrix_to_f32(Ctx& ctx, Csr& A) {
     A.val32.resize(size_t(A.nnz));
     A.rowsum32.resize(size_t(A.rows));
     NL_LAUNCH(k_to_f32, grid_for(A.nnz, 256), 256, 0, ctx.stream, A.nnz, A.val.p, A.val32.p);
     NL_LAUNCH(k_rowsum, grid_for(A.rows, 256), 256, 0, ctx.stream, A.rows, A.rowptr.p, A.val.p, A.rowsum32.p);
+    dbuf<unsigned long long> widest;
+    widest.resize(1);
+    widest.zero(ctx.stream);
+    NL_LAUNCH(k_max_offset, RED_BLOCKS, 256, 0, ctx.stream, A.rows, A.rowptr.p, A.col.p, widest.p);
+    unsigned long long w = 0;
+    widest.download(&w, 1, ctx.stream);
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+    A.col16_ok = w <= 32767;
+    if (A.col16_ok) {
+        A.col16.resize(size_t(A.nnz));
+        NL_LAUNCH(k_col_offsets, RED_BLOCKS, 256, 0, ctx.stream, A.rows, A.rowptr.p, A.col.p, A.col16.p);
+    } else {
+        A.col16.release();
+    }
 }
 
 // One flexible CG in FP32 with reliable updates: the FP32 recurrence runs
@@ -360,6 +440,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     NL_REQUIRE(!learned || (M && ctx.mp.ready && ctx.mp.n == A.rows), NLGPU_ERR_STATE,
                "the learned correction needs ILLT and a prepared network");
     const i64 n = A.rows;
+    PhaseTimer timer(ctx.stream, "mixed_solve");
     MixedWork& w = ctx.mx;
     w.n = n;
     w.r64.reserve(size_t(n)); w.q64.reserve(size_t(n));
@@ -368,8 +449,11 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     w.partial.reserve(size_t(M_SLOTS) * RED_BLOCKS);
     w.outer.reserve(size_t(2) * RED_BLOCKS + 8);
     w.flags.reserve(S_MIXED_COUNT);
+    w.ticket.reserve(1);
+    w.ticket.zero(ctx.stream);
     double* part = w.partial.p;
     double* flags = w.flags.p;
+    unsigned* ticket = w.ticket.p;
     double* outer_part = w.outer.p;
     double* outer_sc = w.outer.p + 2 * RED_BLOCKS;   // [0] |b|^2, [1] |r|^2, [2] s0^2
     const unsigned G = RED_BLOCKS;
@@ -398,7 +482,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
         return res;
     }
     NL_CUDA(cudaMemcpyAsync(outer_sc + 2, outer_sc + 1, sizeof(double), cudaMemcpyDeviceToDevice, ctx.stream));
-    // r32 = r / s0, d = 0, p_0 = z = P(r) in ring slot 0, rz -> the slot iteration 0 reads
+    // r32 = r / s0, d = 0, p_0 = z = P(r) in ring slot 0, p_0.r for the first alpha
     NL_LAUNCH(k_scale_to_f32, G, MX_THREADS, 0, ctx.stream, n, w.r64.p, outer_sc + 2, w.r.p, w.d.p);
     NL_CUDA(cudaMemsetAsync(flags, 0, 8 * sizeof(double), ctx.stream));
     NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.r.p, w.r.p, part + P_RR * RED_BLOCKS);
@@ -406,23 +490,21 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     precondition(nullptr, nullptr, 0.0);
     NL_CUDA(cudaMemcpyAsync(w.p.p, w.z.p, size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, ctx.stream));
     NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.r.p, w.z.p, part + P_RZ_B * RED_BLOCKS);
+    NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, part + P_RZ_B * RED_BLOCKS, flags + S_PR);
     const double cap = double(std::min<i64>(max_iterations, i64(1) << 40));
     double last_rr = hs[1];
     i64 k = 0;
     i64 iters_at_update = 0;
-    // one iteration k (k read on the device): q_j = A p_j (j = k mod MX_M),
-    // alpha, d and r, the count and stop test, z = P(r), the betas, p_k+1
+    // one iteration k (k read on the device): q_j = A p_j (j = k mod MX_M) and
+    // alpha; d, r, the count and the stop test; z = P(r); the betas; p_k+1 and
+    // its alpha numerator.  Each reducing kernel's last block forms the scalars.
     auto iteration = [&] {
-        NL_LAUNCH(k_spmv32, G, MX_THREADS, 0, ctx.stream, n, A.rowptr.p, reinterpret_cast<const int4*>(A.col.p),
-                  reinterpret_cast<const float4*>(A.val32.p), A.rowsum32.p, w.p.p, w.q.p, part + M_PQ * RED_BLOCKS,
-                  flags, n);
-        NL_LAUNCH(k_alpha32, 1, MX_THREADS, 0, ctx.stream, part, flags);
-        NL_LAUNCH(k_update_dr32, G, MX_THREADS, 0, ctx.stream, n, w.d.p, w.r.p, w.p.p, w.q.p, part, flags);
-        NL_LAUNCH(k_check32, 1, MX_THREADS, 0, ctx.stream, part, flags, eta2, cap);
+        launch_spmv32(ctx, A, w.p.p, w.q.p, part + M_PQ * RED_BLOCKS, flags, n, ticket);
+        NL_LAUNCH(k_update_dr32, G, MX_THREADS, 0, ctx.stream, n, w.d.p, w.r.p, w.p.p, w.q.p, part, flags, ticket,
+                  eta2, cap);
         precondition(part, flags, eta2);
-        NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, part, flags);
-        NL_LAUNCH(k_betas32, 1, MX_THREADS, 0, ctx.stream, part, flags);
-        NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags);
+        NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, part, flags, ticket);
+        NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags, ticket);
     };
     bool eager_done = false, captured = false;
     auto run_chunk = [&] {
@@ -437,6 +519,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
             NL_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
             for (int it = 0; it < MX_ITERS; ++it) iteration();
             NL_CUDA(cudaStreamEndCapture(ctx.stream, &g));
+            timer.mark("first chunk, capture");
             w.chunk_kernels = int(g_launches.load() - before);
             g_launches.fetch_sub(w.chunk_kernels);   // counted when the graph is launched
             cudaError_t e = cudaErrorGraphExecUpdateFailure;
@@ -464,6 +547,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
             double hf[8];
             NL_CUDA(cudaMemcpyAsync(hf, flags, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
             NL_CUDA(cudaStreamSynchronize(ctx.stream));
+            timer.mark(captured ? "graph chunk" : "eager chunk");
             res.iterations = i64(hf[S_ITERS]);
             if (hf[S_DONE] != 0.0) break;
             // a recurrence that stalls still gets an update (and the progress check below)
@@ -474,6 +558,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
         // reliable update: x += s0 d (FP64), r = b - A x (FP64)
         NL_LAUNCH(k_refine, G, MX_THREADS, 0, ctx.stream, n, x, w.d.p, outer_sc + 2);
         true_residual(hs);
+        timer.mark("reliable update");
         ++res.outer_iterations;
         res.residual = std::sqrt(hs[1] / hs[0]);
         if (hs[1] <= tolerance * tolerance * hs[0]) { res.converged = true; break; }
@@ -491,16 +576,17 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
         if (forced) {
             // the last chunk already formed p_k: only its alpha numerator p_k.r changes
             NL_LAUNCH(k_dot32, G, MX_THREADS, 0, ctx.stream, n, w.p.p + i64(next) * n, w.r.p,
-                      part + ((k & 1) ? P_RZ_A : P_RZ_B) * RED_BLOCKS);
+                      part + P_RZ_B * RED_BLOCKS);
+            NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, part + P_RZ_B * RED_BLOCKS, flags + S_PR);
         } else {
             // the stop skipped p_k: z = P(r), p_k = z - sum_i (z.q_i / p_i.q_i) p_i as at
             // the end of iteration k - 1 (the kernels read k from the count)
             precondition(nullptr, nullptr, 0.0);
-            NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, part, flags);
-            NL_LAUNCH(k_betas32, 1, MX_THREADS, 0, ctx.stream, part, flags);
-            NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags);
+            NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, part, flags, ticket);
+            NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags, ticket);
         }
     }
+    timer.mark("remaining iterations");
     return res;
 }
 

@@ -222,6 +222,8 @@ void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* 
                     dbuf<i64>* full_from_upper) {
     const i64 n = ctx.n_nodes;
     NL_REQUIRE(local_only || ctx.neighbours_ready, NLGPU_ERR_STATE, "neighbour search must run before a nonlocal assembly");
+    for (Csr* m : {&inner, bound, full})   // 16-bit column offsets belong to the old pattern
+        if (m) m->col16_ok = false;
     dbuf<i64> ci, cb, cf;
     ci.resize(size_t(n + 1)); cb.resize(size_t(n + 1)); cf.resize(size_t(n + 1));
     ci.zero(ctx.stream); cb.zero(ctx.stream); cf.zero(ctx.stream);

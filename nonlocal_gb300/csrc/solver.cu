@@ -426,9 +426,10 @@ void spmv_full(Ctx& ctx, const Csr& A, const double* x, double* y) {
               static_cast<double*>(nullptr), static_cast<const double*>(nullptr));
 }
 
-void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
+void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plans) {
     const i64 n = upper.rows, nnz = upper.nnz;
     ic.n = n; ic.nnz = nnz;
+    PhaseTimer timer(ctx.stream, "ilt_build");
     std::vector<i64> rp(size_t(n + 1));
     std::vector<int32_t> col(static_cast<size_t>(nnz));
     upper.rowptr.download(rp.data(), rp.size(), ctx.stream);
@@ -437,6 +438,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     for (i64 r = 0; r < n; ++r)
         NL_REQUIRE(rp[size_t(r) + 1] > rp[size_t(r)] && col[size_t(rp[size_t(r)])] == int32_t(r), NLGPU_ERR_ARG,
                    "every row of the preconditioner matrix needs its diagonal first");
+    timer.mark("download");
     // U^T as lower CSR with the diagonal last, and the U position of each entry
     std::vector<i64> lrp(size_t(n + 1), 0);
     for (i64 k = 0; k < nnz; ++k) ++lrp[size_t(col[size_t(k)]) + 1];
@@ -459,13 +461,15 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     std::vector<int32_t> ic_rows, bwd_rows;
     build_slab(ctx, lrp, lcol, l_to_u, l_diag, true, ic.fwd, &ic_lev_ptr, &ic_rows);
     build_slab(ctx, rp, col, ident, u_diag, false, ic.bwd, &bwd_lev_ptr, &bwd_rows);
+    timer.mark("transpose, levels, slabs");
     // TMA-fed shared-memory sweeps when every dependency fits the ring
     ctx.sweep_error.resize(1);
     ctx.sweep_error.zero(ctx.stream);
     ic.fwd_plan = SweepPlan{};
     ic.bwd_plan = SweepPlan{};
-    if (sweep_plan_build(ctx, ic_lev_ptr, ic_rows, lrp, lcol, l_to_u, l_diag, ic.fwd_plan))
+    if (tma_plans && sweep_plan_build(ctx, ic_lev_ptr, ic_rows, lrp, lcol, l_to_u, l_diag, ic.fwd_plan))
         sweep_plan_build(ctx, bwd_lev_ptr, bwd_rows, rp, col, ident, u_diag, ic.bwd_plan);
+    timer.mark("sweep plans");
     ic.ic_levels = i64(ic_lev_ptr.size()) - 1;
     ic.ic_lev_ptr.upload(ic_lev_ptr.data(), ic_lev_ptr.size(), ctx.stream);
     ic.ic_rows.upload(ic_rows.data(), ic_rows.size(), ctx.stream);
@@ -477,6 +481,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     ic.y.resize(size_t(n + 1)); ic.w.resize(size_t(n + 1));
     ic.y32.resize(size_t(n + 1)); ic.w32.resize(size_t(n + 1));
     jacobi_build(ctx, ic, rp, col, lrp, lcol, l_to_u);
+    timer.mark("uploads, jacobi layout");
     // Lin-More scaling and the shifted factorisation
     ic.scale.resize(size_t(n)); ic.scale.zero(ctx.stream);
     ic.scale32.resize(size_t(n));
@@ -511,6 +516,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
         shift = std::max(initial_shift, 2.0 * shift);
     }
     ic.shift = shift;
+    timer.mark("scaling, factorisation");
     if (!ic.ok) return;
     jacobi_fill(ctx, ic);
     if (ic.fwd_plan.ok && ic.bwd_plan.ok) {
@@ -524,6 +530,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
         NL_LAUNCH(k_slab_diag, grid_for(n, 256), 256, 0, ctx.stream, n, s->diag_src.p, ic.u.p, s->inv_diag.p,
                   s->inv_diag32.p);
     }
+    timer.mark("value fills");
 }
 
 void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* z) {
