@@ -38,7 +38,10 @@ constexpr int MX_ITERS = 16;
 constexpr int MX_M = 4;   // directions kept for the A-orthogonalisation (flexible CG truncation)
 constexpr i64 MX_UPDATE_MAX = 64;   // iterations between reliable updates at most
 // partial slots: P_RR as in the FP64 solver (the exact sweeps' early exit reads
-// the residual there), P_RZ_A / P_RZ_B for p.r, then p_i.q_i and z.q_i
+// the residual there), P_RZ_A / P_RZ_B for p.r, then the SpMV's p.q partials
+// (MX_M slots of room: the SpMV runs SPMV_BLOCKS blocks) and z.q_i
+constexpr int SPMV_BLOCKS = 2 * RED_BLOCKS;
+static_assert(SPMV_BLOCKS <= MX_M * RED_BLOCKS, "the SpMV partials overflow their slots");
 enum { M_PQ = P_COUNT, M_ZQ = P_COUNT + MX_M, M_SLOTS = P_COUNT + 2 * MX_M };
 // scalar slots after the solver's (S_BB .. S_RR_FINAL): alpha, the betas, p_k.r
 // (the next alpha's numerator) and p_i.q_i of the stored directions
@@ -123,12 +126,16 @@ __device__ __forceinline__ bool mx_reduce_last(double (&v)[N], double* part, uns
 // so for smooth x the plain FP32 sum would cancel to a result far below the
 // rounding error of its terms, while here each FP32 entry multiplies a small
 // difference.  p.q in FP64; in the solve the last block stores it and forms
-// alpha.  Columns are int32 (C4 = int4) or, when every |column - row| fits
-// 16 bits, int16 offsets from the row (C4 = short4): 6 instead of 8 bytes per
-// entry.
-template<class C4>
-__global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restrict__ rp, const C4* __restrict__ col4,
-                                                       const float4* __restrict__ val4,
+// alpha.  Columns are int32 (C = int32_t) or, when every |column - row| fits
+// 16 bits, int16 offsets from the row (C = int16_t): 6 instead of 8 bytes per
+// entry.  Lane l takes entries l, l + 32, ... of its warp's row, so each
+// gather instruction of the warp reads 32 neighbouring columns (few cache
+// lines) rather than 32 columns four entries apart; four entries per lane are
+// loaded before their gathers.  Launched with SPMV_BLOCKS blocks of 256
+// threads: with at most 32 registers per thread, 8 blocks fill an SM.
+template<class C>
+__global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restrict__ rp, const C* __restrict__ col,
+                                                       const float* __restrict__ val,
                                                        const float* __restrict__ rowsum, const float* __restrict__ x,
                                                        float* __restrict__ y, double* __restrict__ dot_partial,
                                                        double* __restrict__ flags, i64 ring, unsigned* ticket) {
@@ -143,21 +150,18 @@ __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restr
     const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
     double dot = 0.0;
     for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
-        const i64 b4 = rp[r] >> 2, e4 = rp[r + 1] >> 2;
+        const i64 e = rp[r + 1];
         const float xr = x[r];
-        const float* xo = sizeof(C4) == 16 ? x : x + r;   // int16 offsets count from the row
-        auto term = [&](const C4& c, const float4& v) {
-            return v.x * (xo[c.x] - xr) + v.y * (xo[c.y] - xr) + v.z * (xo[c.z] - xr) + v.w * (xo[c.w] - xr);
-        };
+        const float* xo = sizeof(C) == 4 ? x : x + r;   // int16 offsets count from the row
         float s = 0.0f;
-        // two column/value loads in flight per lane before their gathers
-        i64 k = b4 + lane;
-        for (; k + 32 < e4; k += 64) {
-            const C4 c0 = __ldg(col4 + k), c1 = __ldg(col4 + k + 32);
-            const float4 v0 = __ldg(val4 + k), v1 = __ldg(val4 + k + 32);
-            s += term(c0, v0) + term(c1, v1);
+        i64 q = rp[r] + lane;
+        for (; q + 96 < e; q += 128) {
+            const C c0 = __ldg(col + q), c1 = __ldg(col + q + 32), c2 = __ldg(col + q + 64), c3 = __ldg(col + q + 96);
+            const float v0 = __ldg(val + q), v1 = __ldg(val + q + 32), v2 = __ldg(val + q + 64),
+                        v3 = __ldg(val + q + 96);
+            s += v0 * (xo[c0] - xr) + v1 * (xo[c1] - xr) + v2 * (xo[c2] - xr) + v3 * (xo[c3] - xr);
         }
-        if (k < e4) s += term(__ldg(col4 + k), __ldg(val4 + k));
+        for (; q < e; q += 32) s += __ldg(val + q) * (xo[__ldg(col + q)] - xr);
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) {
             s += rowsum[r] * xr;
@@ -378,14 +382,12 @@ void precondition32(Ctx& ctx, IncompleteCholesky* M, const float* r, float* z, c
 
 void launch_spmv32(Ctx& ctx, const Csr& A, const float* x, float* y, double* dot_partial, double* flags, i64 ring,
                    unsigned* ticket) {
-    const auto* val4 = reinterpret_cast<const float4*>(A.val32.p);
     if (A.col16_ok)
-        NL_LAUNCH(k_spmv32<short4>, RED_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p,
-                  reinterpret_cast<const short4*>(A.col16.p), val4, A.rowsum32.p, x, y, dot_partial, flags, ring,
-                  ticket);
+        NL_LAUNCH(k_spmv32<int16_t>, SPMV_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p, A.col16.p, A.val32.p,
+                  A.rowsum32.p, x, y, dot_partial, flags, ring, ticket);
     else
-        NL_LAUNCH(k_spmv32<int4>, RED_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p,
-                  reinterpret_cast<const int4*>(A.col.p), val4, A.rowsum32.p, x, y, dot_partial, flags, ring, ticket);
+        NL_LAUNCH(k_spmv32<int32_t>, SPMV_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p, A.col.p, A.val32.p,
+                  A.rowsum32.p, x, y, dot_partial, flags, ring, ticket);
 }
 
 }  // namespace
