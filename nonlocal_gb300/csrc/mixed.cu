@@ -458,7 +458,12 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     unsigned* ticket = w.ticket.p;
     double* outer_part = w.outer.p;
     double* outer_sc = w.outer.p + 2 * RED_BLOCKS;   // [0] |b|^2, [1] |r|^2, [2] s0^2
-    const unsigned G = RED_BLOCKS;
+    // vector kernels: one element per thread up to RED_BLOCKS blocks (a small
+    // system runs fewer blocks and fewer partials); partial entries of blocks
+    // that do not run stay zero, so every consumer may sum all RED_BLOCKS
+    const unsigned G = unsigned(std::min<i64>(RED_BLOCKS, std::max<i64>(1, (n + MX_THREADS - 1) / MX_THREADS)));
+    NL_CUDA(cudaMemsetAsync(part, 0, size_t(M_SLOTS) * RED_BLOCKS * sizeof(double), ctx.stream));
+    NL_CUDA(cudaMemsetAsync(outer_part, 0, size_t(2) * RED_BLOCKS * sizeof(double), ctx.stream));
     if (!x_is_initial_guess) NL_CUDA(cudaMemsetAsync(x, 0, size_t(n) * sizeof(double), ctx.stream));
     const double eta2 = update_factor * update_factor;
     CgResult res;
