@@ -9,8 +9,9 @@ residual |b - Ax| / |b| <= 1e-10 (FP64 residual).  Synthetic structured
 mesh, deterministic.
 
 One step = one stationary solve from the resident mesh: neighbour search,
-sparsity patterns, nonlocal + local assembly (FP64), boundary conditions,
-ILLT factorisation and the solve.  value = device time per solve of the
+sparsity patterns, nonlocal + local assembly (the mixed form's nonlocal pair
+blocks in float-float on the FP32 pipes, the plain form's in FP64), boundary
+conditions, ILLT factorisation and the solve.  value = device time per solve of the
 learned mixed-precision form (flexible CG in FP32 with FP32 ILLT sweeps plus
 the message-passing correction, FP64 reliable updates of the residual and
 solution) by CUDA events on the library's stream, L2 flushed between steps;
@@ -291,7 +292,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     # -------- stage timings for the roofline (device events, this problem)
     stage_ms = {}
     for stage, name, reps in [(0, "spmv", 50), (4, "spmv32", 50), (2, "illt_apply", 10), (5, "illt_apply32", 10),
-                              (6, "illt_jacobi32", 20), (1, "pair_assembly", 3)]:
+                              (6, "illt_jacobi32", 20), (1, "pair_assembly", 3), (7, "pair_assembly_ff", 3)]:
         v = ctypes.c_double()
         L.check(lib.nlgpu_time_stage(h, stage, reps, ctypes.byref(v)))
         stage_ms[name] = v.value
@@ -306,17 +307,23 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     # iteration (+1 start per outer step), FP64 SpMV per outer residual
     per_solve_ms = {"spmv": stage_ms["spmv"] * (outer + 1), "spmv32": stage_ms["spmv32"] * iters,
                     "illt_jacobi32": stage_ms["illt_jacobi32"] * (iters + outer),
-                    "pair_assembly": stage_ms["pair_assembly"]}
+                    "pair_assembly_ff": stage_ms["pair_assembly_ff"]}
     dominant = max(per_solve_ms, key=per_solve_ms.get)
     pk, pk_kind = peaks()
     traffic = profile_traffic()
-    if dominant == "pair_assembly":
+    if dominant == "pair_assembly_ff":
+        # the mixed form's pair blocks in float-float on the FP32 pipes: one
+        # algorithmic multiply-add is one float-float multiply-add, 18 FP32
+        # instructions (FMA-based exact product 4, renormalisation 3, TwoSum and
+        # renormalisation 11), so the float-float peak is the nominal FP32 rate
+        # (152 SMs x 128 lanes x 2 x 2.07 GHz = 80.5 TFLOP/s) / 18 x 2 / 2
         flops = pairs * PAIR_FLOPS[w["element"]]
-        achieved = flops / (stage_ms["pair_assembly"] * 1e-3) / 1e12
-        fp64_peak = 1.25   # nominal GB300 FP64 TFLOP/s (not in the measured peaks file)
-        roof = {"kernel": "k_assemble_pairs", "bound": "fp64", "achieved": achieved, "peak": fp64_peak,
-                "peak_kind": "nominal FP64 (no measured FP64 peak on this pool)", "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak, "traffic": traffic.get(("k_assemble_pairs", args.workload))}
+        achieved = flops / (stage_ms["pair_assembly_ff"] * 1e-3) / 1e12
+        ff_peak = 80.5 / 18
+        roof = {"kernel": "k_assemble_pairs_ff", "bound": "fp32", "achieved": achieved, "peak": ff_peak,
+                "peak_kind": "nominal FP32 rate / 18 instructions per float-float multiply-add", "unit": "TFLOP/s",
+                "frac": achieved / ff_peak, "traffic": traffic.get(("k_assemble_pairs_ff", args.workload)),
+                "fp64_kernel_ms": stage_ms["pair_assembly"]}
     elif dominant in ("spmv", "spmv32"):
         nbytes = spmv_bytes if dominant == "spmv" else spmv32_bytes
         achieved = nbytes / (stage_ms[dominant] * 1e-3) / 1e9
@@ -384,7 +391,8 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     line = {
         "metric": METRIC, "value": seconds, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": mean_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64 (FP32 inner solve; FP64 assembly, residual, refinement, dots)",
+        "dtype": "f32+f64 (FP32 inner solve; float-float (FP32 pipes) nonlocal pair blocks; FP64 residual, "
+                 "refinement, dots)",
         "data": "synthetic",
         "config": {"workload": w["name"], "mesh": f"{w['nx']}x{w['ny']} {w['element']}",
                    "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",

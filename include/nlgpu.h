@@ -349,13 +349,21 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
  * 2 ILLT application (both triangular sweeps), 3 neighbour search, 4 FP32
  * SpMV of the solver matrix, 5 FP32 ILLT application with exact level-scheduled
  * sweeps, 6 FP32 ILLT application with the Jacobi sweeps of the last mixed
- * solve (NLGPU_DEFAULT_TRIANGULAR_SWEEPS before any). */
+ * solve (NLGPU_DEFAULT_TRIANGULAR_SWEEPS before any), 7 pair assembly in
+ * float-float (stage 1 is the FP64 one). */
 /* Options of a context: NLGPU_OPTION_GLOBAL_SWEEPS = 1 makes the ILLT
  * triangular sweeps read and write their values in global memory instead of
  * the TMA-fed shared-memory ring (same arithmetic); NLGPU_OPTION_ORDERED_PAIRS
  * = 1 makes a symmetric assembly evaluate every ordered element pair instead
- * of each unordered pair once (both for comparison). */
-enum { NLGPU_OPTION_GLOBAL_SWEEPS = 0, NLGPU_OPTION_ORDERED_PAIRS = 1 };
+ * of each unordered pair once (both for comparison).
+ * NLGPU_OPTION_ASSEMBLY_PRECISION selects how the nonlocal pair blocks are
+ * computed: NLGPU_ASSEMBLY_AUTO (default) in float-float on the FP32 pipes for
+ * a mixed-precision stationary solve and in FP64 otherwise, NLGPU_ASSEMBLY_FF
+ * always in float-float, NLGPU_ASSEMBLY_FP64 always in FP64.  Float-float
+ * (about 48 significant bits) applies to the fast-polynomial, polynomial and
+ * exponential influence with constant conductivity; other models use FP64. */
+enum { NLGPU_OPTION_GLOBAL_SWEEPS = 0, NLGPU_OPTION_ORDERED_PAIRS = 1, NLGPU_OPTION_ASSEMBLY_PRECISION = 2 };
+enum { NLGPU_ASSEMBLY_AUTO = 0, NLGPU_ASSEMBLY_FF = 1, NLGPU_ASSEMBLY_FP64 = 2 };
 int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value);
 int nlgpu_event_record(nlgpu_ctx* ctx, int slot);
 int nlgpu_event_elapsed(nlgpu_ctx* ctx, int start_slot, int stop_slot, double* milliseconds);

@@ -29,6 +29,8 @@ BC_TEMPERATURE, BC_FLUX = 0, 1
 MATRIX_INNER, MATRIX_BOUND, MATRIX_LOCAL = 0, 1, 2
 PRECONDITIONER = {"identity": 0, "illt": 1, "illt_learned": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
+OPTION_GLOBAL_SWEEPS, OPTION_ORDERED_PAIRS, OPTION_ASSEMBLY_PRECISION = 0, 1, 2
+ASSEMBLY = {"auto": 0, "ff": 1, "fp64": 2}
 
 
 class NlgpuError(RuntimeError):

@@ -68,6 +68,7 @@ void build_inner(Ctx& c) {
     c.symmetric = !(c.model.nonlocal() && c.cond_field.n);   // problem_settings::is_symmetric (problem_settings.hpp:252-254)
     if (c.model.nonlocal()) ensure_neighbours(c);
     build_patterns(c, !c.model.nonlocal(), c.symmetric, c.inner, &c.bound, &c.full, &c.full_from_upper);
+    c.ff_assembly = c.assembly_precision == NLGPU_ASSEMBLY_FF;
     assemble_full(c);
     fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
     c.rhs.resize(size_t(c.n_nodes));
@@ -486,6 +487,11 @@ int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, doub
         NL_CUDA(cudaStreamSynchronize(c.stream));
         rep->seconds_pattern = seconds(t0);
         t0 = std::chrono::steady_clock::now();
+        // the mixed-precision form computes its nonlocal blocks on the FP32 pipes (float-float)
+        const bool mixed = options->precision == NLGPU_PRECISION_MIXED ||
+                           options->preconditioner == NLGPU_PRECONDITIONER_ILLT_LEARNED;
+        c.ff_assembly = c.assembly_precision == NLGPU_ASSEMBLY_FF ||
+                        (c.assembly_precision == NLGPU_ASSEMBLY_AUTO && mixed);
         assemble_full(c);
         fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
         assemble_local(c, c.local, c.model.p1, 0);
@@ -742,6 +748,7 @@ int nlgpu_nonstationary_2d_compute(nlgpu_ctx* ctx, double time_step, const doubl
         c.symmetric = true;
         if (c.model.nonlocal()) ensure_neighbours(c);
         build_patterns(c, !c.model.nonlocal(), true, c.inner, &c.bound, &c.full, &c.full_from_upper);
+        c.ff_assembly = c.assembly_precision == NLGPU_ASSEMBLY_FF;
         assemble_full(c);
         build_patterns(c, true, true, c.capacity_m, nullptr, &c.capacity_full, &c.capacity_map);
         assemble_local(c, c.capacity_m, c.capacity * c.density, 1);
@@ -849,6 +856,12 @@ int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value) {
     if (!ctx) return NLGPU_ERR_ARG;
     if (option == NLGPU_OPTION_GLOBAL_SWEEPS) { ctx->force_global_sweeps = value != 0; return NLGPU_OK; }
     if (option == NLGPU_OPTION_ORDERED_PAIRS) { ctx->ordered_pairs = value != 0; return NLGPU_OK; }
+    if (option == NLGPU_OPTION_ASSEMBLY_PRECISION) {
+        if (value < NLGPU_ASSEMBLY_AUTO || value > NLGPU_ASSEMBLY_FP64) return NLGPU_ERR_ARG;
+        ctx->assembly_precision = value;
+        ctx->inner_ready = false;   // the next use re-assembles
+        return NLGPU_OK;
+    }
     return NLGPU_ERR_ARG;
 }
 
@@ -891,8 +904,10 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
         NL_CUDA(cudaEventCreate(&e1));
         dbuf<double> x, y;
         dbuf<float> x32, y32;
-        NL_REQUIRE(stage >= 0 && stage <= 6, NLGPU_ERR_ARG, "unknown stage");
-        if (stage == 0 || stage == 2 || stage >= 4) {
+        NL_REQUIRE(stage >= 0 && stage <= 7, NLGPU_ERR_ARG, "unknown stage");
+        const bool ff_before = c.ff_assembly;
+        if (stage == 1 || stage == 7) c.ff_assembly = stage == 7;
+        if (stage == 0 || stage == 2 || (stage >= 4 && stage <= 6)) {
             NL_REQUIRE(c.full.nnz > 0, NLGPU_ERR_STATE, "assemble the system first");
             x.resize(size_t(c.n_nodes)); y.resize(size_t(c.n_nodes));
             x32.resize(size_t(c.n_nodes)); y32.resize(size_t(c.n_nodes));
@@ -901,12 +916,13 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
             if (stage == 2 || stage >= 5) NL_REQUIRE(c.ilt.ok, NLGPU_ERR_STATE, "no ILLT factor");
             if (stage == 4 && (c.full.val32.n != size_t(c.full.nnz) || !c.full.col16_ok)) matrix_to_f32(c, c.full);
         }
-        if (stage == 1) NL_REQUIRE(c.inner.nnz > 0 && c.model.nonlocal(), NLGPU_ERR_STATE, "no nonlocal pattern");
+        if (stage == 1 || stage == 7)
+            NL_REQUIRE(c.inner.nnz > 0 && c.model.nonlocal(), NLGPU_ERR_STATE, "no nonlocal pattern");
         if (stage == 3) NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "no mesh/model");
         NL_CUDA(cudaEventRecord(e0, c.stream));
         for (int k = 0; k < reps; ++k) {
             if (stage == 0) spmv_full(c, c.full, x.p, y.p);
-            else if (stage == 1) assemble_full(c);
+            else if (stage == 1 || stage == 7) assemble_full(c);
             else if (stage == 2) ilt_apply(c, c.ilt, x.p, y.p);
             else if (stage == 3) find_neighbours(c, c.strategy);
             else if (stage == 4) spmv32(c, c.full, x32.p, y32.p);
@@ -919,6 +935,7 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
         NL_CUDA(cudaEventElapsedTime(&f, e0, e1));
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        c.ff_assembly = ff_before;
         *ms = double(f) / reps;
     });
 }

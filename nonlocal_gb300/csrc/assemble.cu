@@ -25,6 +25,7 @@
 // When the CTA is done its accumulators are added to the global values.  Rows
 // too long for shared memory fall back to global atomics with a binary search.
 #include "common.cuh"
+#include "ff.cuh"
 
 namespace nlgpu {
 
@@ -254,6 +255,237 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, M
     }
 }
 
+// ---------------------------------------------------------------- float-float
+// The same pair blocks with the influence values and both contractions in
+// float-float arithmetic (ff.cuh) on the FP32 pipes -- the mixed-precision
+// form's FP32 nonlocal blocks, carried to about 48 bits so that the matrix
+// stays within the FP64 entries' tolerance and the FP64 refinement converges
+// to the FP64 solution.  Only the rows' accumulators, the rare self term and
+// the index work stay FP64 / integer.  Element data is staged once per
+// assembly as float-float (k_ff_stage), so the pair loop converts nothing.
+// 16 warps per CTA (the FP64 kernel's 8 leave the FP32 pipes idle).
+constexpr int AS_FF_THREADS = 512;
+constexpr int AS_FF_WARPS = AS_FF_THREADS / 32;
+
+struct FFArgs {
+    const float4* deriv;    // [e][i][q]: (gx.h, gx.l, gy.h, gy.l)
+    const float4* qcoord;   // [e][q]: (x.h, x.l, y.h, y.l)
+    const float2* cw;       // [e][q]: c_q = w_q norm (1 - p1) [lambda_q]
+};
+
+__global__ void k_ff_stage(i64 E, int nen, int nq, const double* __restrict__ deriv, const double* __restrict__ qcoord,
+                           const double* __restrict__ cond_field, Model m, Basis b, float4* __restrict__ dff,
+                           float4* __restrict__ qff, float2* __restrict__ cw) {
+    const double cnl = m.norm * (1.0 - m.p1);
+    const bool iso = m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC;
+    for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < E * nen * nq; t += i64(gridDim.x) * blockDim.x) {
+        const ff gx = ff_from(deriv[2 * t]), gy = ff_from(deriv[2 * t + 1]);
+        dff[t] = make_float4(gx.h, gx.l, gy.h, gy.l);
+        if (t < E * nq) {
+            const ff x = ff_from(qcoord[2 * t]), y = ff_from(qcoord[2 * t + 1]);
+            qff[t] = make_float4(x.h, x.l, y.h, y.l);
+            const double lam = cond_field ? cond_field[t] : m.cond[0];
+            const ff c = ff_from(b.w[t % nq] * cnl * (iso ? lam : 1.0));
+            cw[t] = make_float2(c.h, c.l);
+        }
+    }
+}
+
+template<int NEN, int NQ>
+struct PairFF {
+    ff qx[NQ], qy[NQ];
+    ff gx[NEN * NQ], gy[NEN * NQ];
+    ff phi[NQ * NQ];
+    ff hx[NQ * NEN], hy[NQ * NEN];
+    ff c[NQ];
+    int32_t nodes[NEN];
+};
+
+// shape<INF> in float-float (fast polynomial, polynomial and exponential with
+// p divisible by n; the host sends the other kinds to the FP64 kernel)
+template<int INF>
+__device__ __forceinline__ ff shape_ff(const Model& m, ff dx, ff dy, ff ir0, ff ir1, ff q) {
+    const ff z0 = ff_mul(dx, ir0), z1 = ff_mul(dy, ir1);
+    ff d;
+    if (m.n == 2) d = ff_add(ff_mul(z0, z0), ff_mul(z1, z1));
+    else if (m.n == 1) d = ff_add(ff_abs(z0), ff_abs(z1));
+    else d = ff_add(ff_ipow(ff_abs(z0), m.n), ff_ipow(ff_abs(z1), m.n));
+    if constexpr (INF == NLGPU_INFLUENCE_FAST_POLYNOMIAL) {
+        return ff_lt(d, 1.0f) ? ff_sub(ff_make(1.0f), d) : ff_make(0.0f);
+    } else {
+        const ff dp = ff_ipow(d, m.p / m.n);
+        if constexpr (INF == NLGPU_INFLUENCE_POLYNOMIAL)
+            return ff_lt(d, 1.0f) ? ff_ipow(ff_sub(ff_make(1.0f), dp), int(m.q)) : ff_make(0.0f);
+        else
+            return ff_exp_nonpositive(ff_neg(ff_mul(q, dp)));
+    }
+}
+
+template<int NEN, int NQ, int INF, bool SYM>
+__global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArgs a, FFArgs f, Model m, Basis b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ ff eqx[NQ], eqy[NQ], ewx[NEN * NQ], ewy[NEN * NQ];
+    __shared__ double egx[NEN * NQ], egy[NEN * NQ], ejac[NQ], elam[NQ];   // the self term stays FP64
+    __shared__ int32_t enodes[NEN];
+    __shared__ i64 row_start[NEN];
+    __shared__ int row_len[NEN], row_off[NEN + 1];
+    __shared__ int use_smem;
+
+    auto* pairs = reinterpret_cast<PairFF<NEN, NQ>*>(smem_raw);
+    double* acc = reinterpret_cast<double*>(smem_raw + sizeof(PairFF<NEN, NQ>) * AS_FF_WARPS);
+    int32_t* cols = reinterpret_cast<int32_t*>(acc + a.cap);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    PairFF<NEN, NQ>& ps = pairs[warp];
+    const bool iso = m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC;
+    const ff ir0 = ff_from(m.inv_r[0]), ir1 = ff_from(m.inv_r[1]), qf = ff_from(m.q);
+    const ff k0 = ff_from(m.cond[0]), k1 = ff_from(m.cond[1]), k2 = ff_from(m.cond[2]);
+
+    for (i64 eL = blockIdx.x; eL < a.E; eL += gridDim.x) {
+        // ---- element eL: quadrature data, weighted gradients and its node rows
+        for (int t = threadIdx.x; t < NEN * NQ; t += AS_FF_THREADS) {
+            egx[t] = a.deriv[2 * (eL * NEN * NQ + t)];
+            egy[t] = a.deriv[2 * (eL * NEN * NQ + t) + 1];
+            const float4 g = f.deriv[eL * NEN * NQ + t];
+            const ff w = ff_from(b.w[t % NQ]);
+            ewx[t] = ff_mul(w, ff{g.x, g.y});
+            ewy[t] = ff_mul(w, ff{g.z, g.w});
+        }
+        for (int t = threadIdx.x; t < NQ; t += AS_FF_THREADS) {
+            const float4 q = f.qcoord[eL * NQ + t];
+            eqx[t] = ff{q.x, q.y};
+            eqy[t] = ff{q.z, q.w};
+            ejac[t] = a.jac[eL * NQ + t];
+            elam[t] = a.cond_field ? a.cond_field[eL * NQ + t] : m.cond[0];
+        }
+        if (threadIdx.x < NEN) {
+            const int32_t r = a.elems[eL * NEN + threadIdx.x];
+            enodes[threadIdx.x] = r;
+            row_start[threadIdx.x] = a.in_rp[r];
+            row_len[threadIdx.x] = a.is_inner[r] ? int(a.in_rp[r + 1] - a.in_rp[r]) : 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int off = 0;
+            for (int i = 0; i < NEN; ++i) { row_off[i] = off; off += row_len[i]; }
+            row_off[NEN] = off;
+            use_smem = off <= a.cap;
+        }
+        __syncthreads();
+        const bool smem_rows = use_smem;
+        if (smem_rows) {
+            for (int i = 0; i < NEN; ++i)
+                for (int t = threadIdx.x; t < row_len[i]; t += AS_FF_THREADS) {
+                    cols[row_off[i] + t] = a.in_col[row_start[i] + t];
+                    acc[row_off[i] + t] = 0.0;
+                }
+        }
+        __syncthreads();
+        const int32_t key_l = SYM ? a.minnode[eL] : 0;
+
+        // ---- pairs (eL, eNL): one warp each
+        const i64 kb = a.noff[eL], ke = a.noff[eL + 1];
+        for (i64 k = kb + warp; k < ke; k += AS_FF_WARPS) {
+            const int32_t eNL = a.nlist[k];
+            if constexpr (SYM) {   // the pair belongs to the element with the smaller key
+                const int32_t key_n = a.minnode[eNL];
+                if (key_n < key_l || (key_n == key_l && eNL < int32_t(eL))) continue;
+            }
+            for (int t = lane; t < NEN * NQ; t += 32) {
+                const float4 g = f.deriv[i64(eNL) * NEN * NQ + t];
+                ps.gx[t] = ff{g.x, g.y};
+                ps.gy[t] = ff{g.z, g.w};
+            }
+            if (lane < NQ) {
+                const float4 q = f.qcoord[i64(eNL) * NQ + lane];
+                ps.qx[lane] = ff{q.x, q.y};
+                ps.qy[lane] = ff{q.z, q.w};
+                const float2 c = f.cw[i64(eNL) * NQ + lane];
+                ps.c[lane] = ff{c.x, c.y};
+            }
+            if (lane < NEN) ps.nodes[lane] = a.elems[i64(eNL) * NEN + lane];
+            __syncwarp();
+            for (int t = lane; t < NQ * NQ; t += 32) {
+                const int qL = t / NQ, qNL = t % NQ;
+                ps.phi[t] = ff_mul(ps.c[qNL], shape_ff<INF>(m, ff_sub(eqx[qL], ps.qx[qNL]), ff_sub(eqy[qL], ps.qy[qNL]),
+                                                             ir0, ir1, qf));
+            }
+            __syncwarp();
+            for (int t = lane; t < NQ * NEN; t += 32) {
+                const int qL = t / NEN, j = t % NEN;
+                ff h0 = ff_make(0.0f), h1 = ff_make(0.0f);
+#pragma unroll
+                for (int qNL = 0; qNL < NQ; ++qNL) {
+                    const ff fq = ps.phi[qL * NQ + qNL];
+                    const ff gx = ps.gx[j * NQ + qNL], gy = ps.gy[j * NQ + qNL];
+                    if (m.cond_kind != NLGPU_CONDUCTIVITY_ANISOTROPIC) {
+                        h0 = ff_fma(h0, fq, gx);
+                        h1 = ff_fma(h1, fq, gy);
+                    } else {
+                        h0 = ff_fma(h0, fq, ff_add(ff_mul(k0, gx), ff_mul(k2, gy)));
+                        h1 = ff_fma(h1, fq, ff_add(ff_mul(k2, gx), ff_mul(k1, gy)));
+                    }
+                }
+                if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) { h0 = ff_mul(h0, k0); h1 = ff_mul(h1, k1); }
+                ps.hx[t] = h0;
+                ps.hy[t] = h1;
+            }
+            __syncwarp();
+            const bool self = eNL == int32_t(eL);
+            for (int t = lane; t < NEN * NEN; t += 32) {
+                const int i = t / NEN, j = t % NEN;
+                const int32_t r = enodes[i], c = ps.nodes[j];
+                const bool r_in = a.is_inner[r], c_in = a.is_inner[c];
+                const bool fwd_inner = c_in && r_in && (!a.symmetric || r <= c);
+                const bool fwd_bound = !c_in && r != c;
+                const bool tr = SYM && !self;
+                const bool bwd_inner = tr && c_in && r_in && c <= r;
+                const bool bwd_bound = tr && !r_in && c != r;
+                if (!fwd_inner && !fwd_bound && !bwd_inner && !bwd_bound) continue;
+                ff vf = ff_make(0.0f);
+#pragma unroll
+                for (int qL = 0; qL < NQ; ++qL)
+                    vf = ff_fma(ff_fma(vf, ewx[i * NQ + qL], ps.hx[qL * NEN + j]), ewy[i * NQ + qL], ps.hy[qL * NEN + j]);
+                double v = ff_to(vf);
+                if (self) {
+                    double loc = 0.0;
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q) {
+                        const double ax = egx[i * NQ + q], ay = egy[i * NQ + q];
+                        const double bx = egx[j * NQ + q], by = egy[j * NQ + q];
+                        double val;
+                        if (iso) val = elam[q] * (ax * bx + ay * by);
+                        else if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) val = m.cond[0] * ax * bx + m.cond[1] * ay * by;
+                        else val = ax * (m.cond[0] * bx + m.cond[2] * by) + ay * (m.cond[2] * bx + m.cond[1] * by);
+                        loc += b.w[q] * val / ejac[q];
+                    }
+                    v += m.p1 * loc;
+                }
+                if (fwd_inner) {
+                    if (smem_rows) {
+                        const i64 pos = find_col(cols, row_off[i], row_off[i + 1], c);
+                        if (pos < row_off[i + 1] && cols[pos] == c) atomicAdd(acc + pos, v);
+                        else atomicExch(a.error, 1);
+                    } else {
+                        add_global(a.in_rp, a.in_col, a.in_val, r, c, v, a.error);
+                    }
+                }
+                if (fwd_bound) add_global(a.bd_rp, a.bd_col, a.bd_val, r, c, v, a.error);
+                if (bwd_inner) add_global(a.in_rp, a.in_col, a.in_val, c, r, v, a.error);
+                if (bwd_bound) add_global(a.bd_rp, a.bd_col, a.bd_val, c, r, v, a.error);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        if (smem_rows)
+            for (int i = 0; i < NEN; ++i)
+                for (int t = threadIdx.x; t < row_len[i]; t += AS_FF_THREADS) {
+                    const double v = acc[row_off[i] + t];
+                    if (v != 0.0) atomicAdd(a.in_val + row_start[i] + t, v);
+                }
+        __syncthreads();
+    }
+}
+
 // Local integrands, one thread per (e, i, j): conductivity
 // (integrate_local, conductivity_matrix_2d.hpp:106-130) or capacity
 // (integrate_basic_pair, heat_capacity_matrix_2d.hpp:137-144).
@@ -338,6 +570,43 @@ void dispatch_influence(Ctx& ctx, const AssembleArgs& a, bool sym) {
     }
 }
 
+template<int NEN, int NQ, int INF>
+void launch_pairs_ff(Ctx& ctx, AssembleArgs a, const FFArgs& f, bool sym) {
+    const size_t fixed = sizeof(PairFF<NEN, NQ>) * AS_FF_WARPS;
+    a.cap = int((200 * 1024 - fixed) / 12);
+    const size_t dyn = fixed + size_t(a.cap) * (sizeof(double) + sizeof(int32_t));
+    const unsigned grid = unsigned(std::min<i64>(a.E, 152 * 16));
+    if (sym) {
+        auto kernel = k_assemble_pairs_ff<NEN, NQ, INF, true>;
+        NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
+        NL_LAUNCH(kernel, grid, AS_FF_THREADS, dyn, ctx.stream, a, f, ctx.model, ctx.basis);
+    } else {
+        auto kernel = k_assemble_pairs_ff<NEN, NQ, INF, false>;
+        NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
+        NL_LAUNCH(kernel, grid, AS_FF_THREADS, dyn, ctx.stream, a, f, ctx.model, ctx.basis);
+    }
+}
+
+template<int NEN, int NQ>
+void dispatch_influence_ff(Ctx& ctx, const AssembleArgs& a, const FFArgs& f, bool sym) {
+    switch (ctx.model.influence) {
+    case NLGPU_INFLUENCE_FAST_POLYNOMIAL: launch_pairs_ff<NEN, NQ, NLGPU_INFLUENCE_FAST_POLYNOMIAL>(ctx, a, f, sym); break;
+    case NLGPU_INFLUENCE_POLYNOMIAL: launch_pairs_ff<NEN, NQ, NLGPU_INFLUENCE_POLYNOMIAL>(ctx, a, f, sym); break;
+    default: launch_pairs_ff<NEN, NQ, NLGPU_INFLUENCE_EXPONENTIAL>(ctx, a, f, sym); break;
+    }
+}
+
+// float-float covers the continuous influence kinds with an integral power
+// p / n and constant conductivity; the rest runs the FP64 kernel
+bool ff_supported(const Ctx& ctx) {
+    const Model& m = ctx.model;
+    if (ctx.cond_field.n || m.n < 1) return false;
+    if (m.influence == NLGPU_INFLUENCE_FAST_POLYNOMIAL) return true;
+    if (m.influence == NLGPU_INFLUENCE_POLYNOMIAL || m.influence == NLGPU_INFLUENCE_EXPONENTIAL)
+        return m.p >= 0 && m.p % m.n == 0;
+    return false;
+}
+
 }  // namespace
 
 // Assembles p1*K_local + (1-p1)*K_nonlocal (or p1*K_local for a local model)
@@ -363,7 +632,19 @@ void assemble_full(Ctx& ctx) {
     a.error = err.p;
     // unordered pairs need a symmetric influence and constant conductivity
     const bool sym = ctx.symmetric && !ctx.cond_field.n && !ctx.ordered_pairs;
-    if (ctx.basis.nen == 4) {
+    ctx.ff_assembled = ctx.ff_assembly && ff_supported(ctx);
+    if (ctx.ff_assembled) {
+        const int nen = ctx.basis.nen, nq = ctx.basis.nq;
+        ctx.deriv_ff.reserve(size_t(ctx.n_elems * nen * nq));
+        ctx.qcoord_ff.reserve(size_t(ctx.n_elems * nq));
+        ctx.cw_ff.reserve(size_t(ctx.n_elems * nq));
+        NL_LAUNCH(k_ff_stage, grid_for(ctx.n_elems * nen * nq, 256), 256, 0, ctx.stream, ctx.n_elems, nen, nq,
+                  ctx.deriv.p, ctx.qcoord.p, a.cond_field, ctx.model, ctx.basis, ctx.deriv_ff.p, ctx.qcoord_ff.p,
+                  ctx.cw_ff.p);
+        const FFArgs f{ctx.deriv_ff.p, ctx.qcoord_ff.p, ctx.cw_ff.p};
+        if (nen == 4) dispatch_influence_ff<4, 4>(ctx, a, f, sym);
+        else dispatch_influence_ff<8, 9>(ctx, a, f, sym);
+    } else if (ctx.basis.nen == 4) {
         a.cap = int((200 * 1024 - sizeof(PairSmem<4, 4>) * AS_WARPS) / 12);
         dispatch_influence<4, 4>(ctx, a, sym);
     } else {

@@ -358,6 +358,11 @@ struct Ctx {
     bool force_global_sweeps = false;   // use the global-memory sweeps (for comparison)
     int ilt_sweeps = NLGPU_DEFAULT_TRIANGULAR_SWEEPS;   // FP32 ILLT: Jacobi sweeps per triangle (0: exact)
     bool ordered_pairs = false;         // evaluate every ordered element pair (for comparison)
+    int assembly_precision = NLGPU_ASSEMBLY_AUTO;
+    bool ff_assembly = false;           // pair blocks in float-float on the FP32 pipes (mixed precision)
+    bool ff_assembled = false;          // the last assembly ran in float-float
+    dbuf<float4> deriv_ff, qcoord_ff;   // float-float copies: (gx, gy) / (x, y) as (hi, lo, hi, lo)
+    dbuf<float2> cw_ff;                 // w_q norm (1 - p1) [lambda_q] per element and point
     // measurement
     cudaEvent_t events[64] = {};
     dbuf<unsigned char> flush;

@@ -169,6 +169,11 @@ class Problem2D(Context):
         L.check(self._lib.nlgpu_get_basis(self._h, None, None, L.ptr(qN), L.ptr(qNxi), L.ptr(qNeta), L.ptr(w), L.ptr(c)))
         return {"basis_qN": qN, "basis_qNxi": qNxi, "basis_qNeta": qNeta, "basis_weights": w, "basis_centre": c}
 
+    def set_assembly_precision(self, kind: str = "auto") -> None:
+        """How the nonlocal pair blocks are computed: "auto" (float-float on the FP32
+        pipes for mixed-precision solves, FP64 otherwise), "ff" or "fp64" always."""
+        L.check(self._lib.nlgpu_set_option(self._h, L.OPTION_ASSEMBLY_PRECISION, L.ASSEMBLY[kind]))
+
     # ---- neighbours -----------------------------------------------------------
     def find_neighbours(self, strategy: str = "MAX") -> tuple[np.ndarray, int]:
         r = np.empty(2)

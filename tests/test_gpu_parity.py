@@ -105,6 +105,22 @@ def test_matrices_and_rhs(golden):
     assert_csr_equal(pb.matrix("local"), fx, "K_local")
 
 
+def test_float_float_assembly_matrices(golden):
+    """The mixed-precision form's pair blocks, computed in float-float on the FP32
+    pipes, meet the FP64 entries' bar against the reference's matrices (models
+    outside its scope run the FP64 kernel and pass trivially)."""
+    _, fx, pb = golden
+    if fx["config"].get("local_weight", 1) < 0.999:
+        pb.find_neighbours(fx["config"].get("strategy", "MAX"))
+    pb.set_assembly_precision("ff")
+    try:
+        pb.conductivity_matrix("FULL")
+        assert_csr_equal(pb.matrix("inner"), fx, "K_inner")
+        assert_csr_equal(pb.matrix("bound"), fx, "K_bound")
+    finally:
+        pb.set_assembly_precision("auto")
+
+
 def test_stationary_solution(golden):
     _, fx, pb = golden
     if fx["config"].get("local_weight", 1) < 0.999:
@@ -333,6 +349,11 @@ def test_against_oracle_scaled(lib, case):
     orp, ocol, oval = prob.csr("K_inner")
     assert np.array_equal(rp, orp) and np.array_equal(col, ocol)
     np.testing.assert_allclose(val, oval, rtol=MATRIX_RTOL, atol=MATRIX_RTOL * np.abs(oval).max())
+    # the float-float pair blocks of the mixed-precision form, same bar
+    pb.set_assembly_precision("ff")
+    pb.conductivity_matrix("FULL")
+    np.testing.assert_allclose(pb.matrix("inner")[2], oval, rtol=MATRIX_RTOL, atol=MATRIX_RTOL * np.abs(oval).max())
+    pb.set_assembly_precision("auto")
     t, rep = pb.stationary(tolerance=1e-13)
     assert rel(t, prob.get("solution")) < SOLUTION_RTOL
     # same preconditioner (fixed-pattern IC(0) on the scaled, shifted local matrix): iteration counts agree
