@@ -514,6 +514,36 @@ def run_batch(args, world, rank, local, dist):
     return 0
 
 
+ONCE_STAGES = ("assembly_fp64", "assembly_ff", "solve_mixed", "solve_fp64")
+
+
+def run_once(args) -> int:
+    """One stage of one workload, once, for ncu captures of a single kernel on a
+    case of the benchmark's shape: the pair assembly in FP64 or float-float, or a
+    whole stationary solve (mixed-precision or plain FP64)."""
+    from nonlocal_gb300 import build as nbuild
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    nbuild.build()
+    w = dict(WORKLOADS[args.workload])
+    s = max(1, args.scale)
+    w["nx"], w["ny"] = w["nx"] // s, w["ny"] // s
+    w["model"] = dict(w["model"], radius=tuple(r * s for r in w["model"]["radius"]))
+    mesh = structured_quad_mesh(w["nx"], w["ny"], w["element"], jitter=w["jitter"], seed=0)
+    pb = make_problem(w, T, mesh)
+    pb.find_neighbours()
+    if args.once.startswith("assembly"):
+        pb.set_assembly_precision("ff" if args.once == "assembly_ff" else "fp64")
+        pb.conductivity_matrix("FULL")
+        print(json.dumps({"once": args.once, "workload": args.workload, "scale": s, "element_pairs": pb.pairs}))
+    else:
+        _, rep = pb.stationary(tolerance=w["tolerance"], max_iterations=100000,
+                               precision="mixed" if args.once == "solve_mixed" else "fp64")
+        print(json.dumps({"once": args.once, "workload": args.workload, "scale": s, "iterations": rep.iterations,
+                          "residual": rep.residual}))
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -523,7 +553,13 @@ def main() -> int:
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["config5"], default="config2")
     ap.add_argument("--instances", type=int, default=256, help="config5: number of instances")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--once", choices=sorted(ONCE_STAGES),
+                    help="run one stage once on the workload and exit (profiling captures)")
+    ap.add_argument("--scale", type=int, default=1,
+                    help="with --once: elements per edge / scale and radius x scale (same r/h, fewer pairs)")
     args = ap.parse_args()
+    if args.once:
+        return run_once(args)
     world, rank, local, dist = dist_setup()
     if args.workload == "config5":
         try:

@@ -3,8 +3,10 @@
 // The plain path runs slae::conjugate_gradient (conjugate_gradient.hpp:48-79)
 // in FP64.  This form keeps FP64 only where accuracy is decided -- the
 // residual b - A x (FP64 matrix, FP64 SpMV), the solution, every global dot
-// product and norm (FP64 partial sums), and the IC(0) pivots (the factor is
-// computed in FP64) -- and runs the iteration itself in FP32:
+// product and norm (FP64 block and global sums; the inner iteration's
+// products and each thread's one or two elements in FP32, since a warp-wide
+// FP64 instruction costs GB300 16 issue cycles of its FP64 pipe), and the IC(0)
+// pivots (the factor is computed in FP64) -- and runs the iteration itself in FP32:
 //
 //   r = b - A x (FP64); r32 = r / s0; d32 = 0; p_0 = z = P(r32)
 //   repeat k   (FP32 vectors, FP32 matrix copy, FP32 ILLT sweeps)
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restr
     }
     const int lane = threadIdx.x & 31;
     const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
-    double dot = 0.0;
+    float dot = 0.0f;   // this warp's few rows in FP32; block and global sums in FP64
     for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
         const i64 e = rp[r + 1];
         const float xr = x[r];
@@ -166,11 +168,11 @@ __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restr
         if (lane == 0) {
             s += rowsum[r] * xr;
             y[r] = s;
-            dot += double(s) * double(xr);
+            dot = fmaf(s, xr, dot);
         }
     }
     if (dot_partial) {   // p_j.q_j: the last block stores it and alpha = (p_j.r) / (p_j.q_j)
-        double v[1] = {dot};
+        double v[1] = {double(dot)};
         if (mx_reduce_last<1>(v, dot_partial, ticket, sh) && threadIdx.x == 0) {
             flags[S_PQ + slot] = v[0];
             flags[S_ALPHA] = flags[S_PR] / v[0];
@@ -297,14 +299,14 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __rest
     p += slot * n;
     q += slot * n;
     const float alpha = float(flags[S_ALPHA]);
-    double s = 0.0;
+    float s = 0.0f;   // a thread's one or two elements in FP32; block and global sums in FP64
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         d[i] += alpha * p[i];
         const float v = r[i] - alpha * q[i];
         r[i] = v;
-        s += double(v) * double(v);
+        s = fmaf(v, v, s);
     }
-    double v[1] = {s};
+    double v[1] = {double(s)};
     if (mx_reduce_last<1>(v, part + P_RR * RED_BLOCKS, ticket, sh) && threadIdx.x == 0) {
         const double it = flags[S_ITERS] + 1.0;
         flags[S_ITERS] = it;
@@ -319,13 +321,16 @@ __global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __res
     __shared__ double sh[33 * MX_M];
     if (flags[S_DONE] != 0.0) return;
     const int count = mx_count(flags);
-    double zq[MX_M] = {};
+    float zq32[MX_M] = {};
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
-        const double zi = z[i];
+        const float zi = z[i];
 #pragma unroll
         for (int s = 0; s < MX_M; ++s)
-            if (s < count) zq[s] += zi * double(qring[i64(s) * n + i]);
+            if (s < count) zq32[s] = fmaf(zi, qring[i64(s) * n + i], zq32[s]);
     }
+    double zq[MX_M];
+#pragma unroll
+    for (int s = 0; s < MX_M; ++s) zq[s] = zq32[s];
     if (mx_reduce_last<MX_M>(zq, part + M_ZQ * RED_BLOCKS, ticket, sh) && threadIdx.x == 0)
         for (int s = 0; s < count; ++s) flags[S_BETA + s] = -zq[s] / flags[S_PQ + s];
 }
@@ -344,16 +349,16 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_pm32(i64 n, float* __rest
 #pragma unroll
     for (int s = 0; s < MX_M; ++s) beta[s] = s < count ? float(flags[S_BETA + s]) : 0.0f;
     float* pn = pring + i64(next) * n;
-    double pr = 0.0;
+    float pr = 0.0f;
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         float v = z[i];
 #pragma unroll
         for (int s = 0; s < MX_M; ++s)
             if (s < count) v += beta[s] * pring[i64(s) * n + i];
         pn[i] = v;   // may overwrite the oldest direction: element i was read above
-        pr += double(v) * double(r[i]);
+        pr = fmaf(v, r[i], pr);
     }
-    double v[1] = {pr};
+    double v[1] = {double(pr)};
     if (mx_reduce_last<1>(v, part + P_RZ_A * RED_BLOCKS, ticket, sh) && threadIdx.x == 0) flags[S_PR] = v[0];
 }
 
