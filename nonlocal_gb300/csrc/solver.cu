@@ -207,42 +207,122 @@ __global__ void k_scaled(i64 n, const i64* __restrict__ rp, const int32_t* __res
         }
 }
 
-// Up-looking IC(0), one CTA, rows of a level in parallel.  U has the pattern
-// of the upper matrix; row i subtracts u_ki * row k for every k < i with
-// u_ki != 0 (L row i, with its U position in l_to_u).
-__global__ void __launch_bounds__(TRI_THREADS) k_ic0(i64 n_levels, const i64* __restrict__ lev_ptr,
-                                                     const int32_t* __restrict__ lev_rows, const i64* __restrict__ rp,
-                                                     const int32_t* __restrict__ col, const double* __restrict__ a,
-                                                     double shift, const i64* __restrict__ lrp,
-                                                     const int32_t* __restrict__ lcol, const i64* __restrict__ l_to_u,
-                                                     double* __restrict__ u, int* __restrict__ failed) {
-    for (i64 l = 0; l < n_levels; ++l) {
-        for (i64 t = lev_ptr[l] + threadIdx.x; t < lev_ptr[l + 1]; t += blockDim.x) {
-            const int32_t i = lev_rows[t];
-            const i64 b = rp[i], e = rp[i + 1];
-            for (i64 s = b; s < e; ++s) u[s] = a[s];
-            u[b] += shift;
-            for (i64 s = lrp[i]; s < lrp[i + 1] - 1; ++s) {   // last entry of L row i is the diagonal
-                const int32_t k = lcol[s];
-                const i64 pk = l_to_u[s];                      // position of (k, i) in U
-                const double uki = u[pk];
-                i64 x = pk, y = b;                             // merge row k (from column i on) into row i
-                const i64 ke = rp[k + 1];
-                while (x < ke && y < e) {
-                    const int32_t cx = col[x], cy = col[y];
-                    if (cx < cy) ++x;
-                    else if (cx > cy) ++y;
-                    else { u[y] -= uki * u[x]; ++x; ++y; }
-                }
-            }
-            const double d = u[b];
-            if (!(d > 0.0)) { atomicExch(failed, 1); continue; }
-            const double rd = sqrt(d);
-            u[b] = rd;
-            for (i64 s = b + 1; s < e; ++s) u[s] /= rd;
+// Up-looking IC(0): U has the pattern of the upper matrix; row i subtracts
+// u_ki * row k for every k < i with u_ki != 0 (L row i, with its U position in
+// l_to_u), then divides by the root of its pivot.  One launch per level, one
+// warp per row of the level (rows of one level only read rows of earlier
+// levels).  Lane y owns entry y of row i (rows of up to 32 entries; longer
+// rows run the sequential merge on lane 0).  For up to IC_MAXS rows k of L row i at a time,
+// the warp's lanes spread over the entries of those rows' segments (columns
+// >= i), each finds its column among row i's (binary search in shared memory)
+// and stores u_ki u_kj in a table; lane y then subtracts the table's column y
+// in the order of k, as the sequential form does (product and subtraction
+// rounded separately).  The chain of dependent global loads per row is a few
+// instead of one per merge step.
+constexpr int IC_WARPS = 8;
+constexpr int IC_MAXS = 16;
+
+__device__ void ic0_row_sequential(int32_t i, const i64* __restrict__ rp, const int32_t* __restrict__ col,
+                                   const double* __restrict__ a, double shift, const i64* __restrict__ lrp,
+                                   const int32_t* __restrict__ lcol, const i64* __restrict__ l_to_u,
+                                   double* __restrict__ u, int* __restrict__ failed) {
+    const i64 b = rp[i], e = rp[i + 1];
+    for (i64 s = b; s < e; ++s) u[s] = a[s];
+    u[b] += shift;
+    for (i64 s = lrp[i]; s < lrp[i + 1] - 1; ++s) {
+        const int32_t k = lcol[s];
+        const i64 pk = l_to_u[s];
+        const double uki = u[pk];
+        i64 x = pk, y = b;
+        const i64 ke = rp[k + 1];
+        while (x < ke && y < e) {
+            const int32_t cx = col[x], cy = col[y];
+            if (cx < cy) ++x;
+            else if (cx > cy) ++y;
+            else { u[y] = __dsub_rn(u[y], __dmul_rn(uki, u[x])); ++x; ++y; }
         }
-        __syncthreads();
     }
+    const double d = u[b];
+    if (!(d > 0.0)) { atomicExch(failed, 1); return; }
+    const double rd = sqrt(d);
+    u[b] = rd;
+    for (i64 s = b + 1; s < e; ++s) u[s] /= rd;
+}
+
+__global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_level(i64 t0, i64 t1, const int32_t* __restrict__ lev_rows,
+                                                             const i64* __restrict__ rp, const int32_t* __restrict__ col,
+                                                             const double* __restrict__ a, double shift,
+                                                             const i64* __restrict__ lrp,
+                                                             const int32_t* __restrict__ lcol,
+                                                             const i64* __restrict__ l_to_u, double* __restrict__ u,
+                                                             int* __restrict__ failed) {
+    __shared__ double table[IC_WARPS][IC_MAXS][32];
+    __shared__ int32_t rowcol[IC_WARPS][32];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+    const i64 t = t0 + i64(blockIdx.x) * IC_WARPS + wb;
+    if (t >= t1) return;   // whole warps
+    const int32_t i = lev_rows[t];
+    const i64 b = rp[i], e = rp[i + 1];
+    const int m = int(e - b);
+    if (m > 32) {
+        if (lane == 0) ic0_row_sequential(i, rp, col, a, shift, lrp, lcol, l_to_u, u, failed);
+        return;
+    }
+    const bool own = lane < m;
+    rowcol[wb][lane] = own ? col[b + lane] : 0x7fffffff;
+    double acc = own ? a[b + lane] : 0.0;
+    if (lane == 0) acc += shift;
+    const i64 lb = lrp[i], le = lrp[i + 1] - 1;   // L row i without its diagonal (its last entry)
+    for (i64 s0 = lb; s0 < le; s0 += IC_MAXS) {
+        const int ns = le - s0 < IC_MAXS ? int(le - s0) : IC_MAXS;
+        i64 pk = 0;
+        double uki = 0.0;
+        int len = 0;
+        if (lane < ns) {
+            pk = l_to_u[s0 + lane];   // (k, i) in U: row k's segment from column i on
+            len = int(rp[lcol[s0 + lane] + 1] - pk);
+            uki = u[pk];
+        }
+        int incl = len;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(full, incl, 31);
+        for (int q = 0; q < ns; ++q) table[wb][q][lane] = 0.0;
+        __syncwarp();
+        for (int base = 0; base < total; base += 32) {
+            const int idx = base + lane;
+            int s = 0;
+            for (int q = 0; q < ns; ++q) s += __shfl_sync(full, incl, q) <= idx ? 1 : 0;
+            const int sc = min(s, ns - 1);
+            const int start = __shfl_sync(full, incl, max(sc - 1, 0)) * (sc > 0 ? 1 : 0);
+            const i64 pks = __shfl_sync(full, pk, sc);
+            const double ukis = __shfl_sync(full, uki, sc);
+            if (idx < total) {
+                const i64 x = pks + (idx - start);
+                const int32_t cx = col[x];
+                int lo = 0, hi = m;   // column cx among row i's
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (rowcol[wb][mid] < cx) lo = mid + 1; else hi = mid;
+                }
+                if (lo < m && rowcol[wb][lo] == cx) table[wb][s][lo] = __dmul_rn(ukis, u[x]);
+            }
+        }
+        __syncwarp();
+        for (int q = 0; q < ns; ++q) acc = __dsub_rn(acc, table[wb][q][lane]);
+        __syncwarp();
+    }
+    const double d = __shfl_sync(full, acc, 0);
+    if (!(d > 0.0)) {
+        if (lane == 0) atomicExch(failed, 1);
+        return;
+    }
+    const double rd = sqrt(d);
+    if (lane == 0) u[b] = rd;
+    else if (own) u[b + lane] = acc / rd;
 }
 
 __global__ void k_slab_values(i64 count, const i64* __restrict__ src, const double* __restrict__ u,
@@ -507,8 +587,12 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
     ic.ok = false;
     for (ic.attempts = 1; ic.attempts <= 10; ++ic.attempts) {
         failed.zero(ctx.stream);
-        NL_LAUNCH(k_ic0, 1, TRI_THREADS, 0, ctx.stream, ic.ic_levels, ic.ic_lev_ptr.p, ic.ic_rows.p, ic.rp.p, ic.col.p,
-                  ic.a_scaled.p, shift, ic.lrp.p, ic.lcol.p, ic.l_to_u.p, ic.u.p, failed.p);
+        for (i64 l = 0; l < ic.ic_levels; ++l) {
+            const i64 t0 = ic_lev_ptr[size_t(l)], t1 = ic_lev_ptr[size_t(l) + 1];
+            NL_LAUNCH(k_ic0_level, unsigned((t1 - t0 + IC_WARPS - 1) / IC_WARPS), IC_WARPS * 32, 0, ctx.stream, t0, t1,
+                      ic.ic_rows.p, ic.rp.p, ic.col.p, ic.a_scaled.p, shift, ic.lrp.p, ic.lcol.p, ic.l_to_u.p, ic.u.p,
+                      failed.p);
+        }
         int hf = 0;
         NL_CUDA(cudaMemcpyAsync(&hf, failed.p, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
         NL_CUDA(cudaStreamSynchronize(ctx.stream));
