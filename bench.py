@@ -514,17 +514,31 @@ def run_batch(args, world, rank, local, dist):
     return 0
 
 
-ONCE_STAGES = ("assembly_fp64", "assembly_ff", "solve_mixed", "solve_fp64")
+ONCE_STAGES = ("assembly_fp64", "assembly_ff", "solve_mixed", "solve_fp64", "gemm_bf16")
 
 
 def run_once(args) -> int:
     """One stage of one workload, once, for ncu captures of a single kernel on a
-    case of the benchmark's shape: the pair assembly in FP64 or float-float, or a
-    whole stationary solve (mixed-precision or plain FP64)."""
+    case of the benchmark's shape: the pair assembly in FP64 or float-float, a
+    whole stationary solve (mixed-precision or plain FP64), or the learned
+    correction's tensor-core GEMM at one message-passing layer's shape (rows =
+    the workload's nodes, 128 inputs, 64 outputs)."""
     from nonlocal_gb300 import build as nbuild
     from nonlocal_gb300 import thermal as T
     from nonlocal_gb300.meshgen import structured_quad_mesh
     nbuild.build()
+    if args.once == "gemm_bf16":
+        import numpy as np
+        from nonlocal_gb300 import _lib as L
+        w = WORKLOADS[args.workload]
+        m = (w["nx"] + 1) * (w["ny"] + 1)
+        rng = np.random.default_rng(0)
+        a = (rng.standard_normal((m, 128)).astype(np.float32).view(np.uint32) >> 16).astype(np.uint16)
+        b = (rng.standard_normal((64, 128)).astype(np.float32).view(np.uint32) >> 16).astype(np.uint16)
+        c = np.empty((m, 64), dtype=np.float32)
+        L.check(L.load().nlgpu_gemm_bf16(m, 64, 128, 1, a.ctypes.data, b.ctypes.data, c.ctypes.data))
+        print(json.dumps({"once": args.once, "workload": args.workload, "M": m, "N": 64, "K": 128}))
+        return 0
     w = dict(WORKLOADS[args.workload])
     s = max(1, args.scale)
     w["nx"], w["ny"] = w["nx"] // s, w["ny"] // s
