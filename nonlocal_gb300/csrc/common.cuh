@@ -310,6 +310,7 @@ struct Ctx {
     dbuf<double> nodes;          // [n][2]
     dbuf<int32_t> elems;         // [e][nen]
     dbuf<double> qcoord, jac, deriv, centres;
+    dbuf<float2> centres32;             // FP32 copies for the neighbour search's pre-test
     dbuf<i64> ne_off;            // node -> elements CSR
     dbuf<int32_t> ne_elem;
     dbuf<int8_t> ne_local;

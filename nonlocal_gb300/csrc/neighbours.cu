@@ -81,7 +81,17 @@ struct Grid {
     double maxr, R0, R1;
     i64 rows, cols;
     int n;   // powered-distance exponent
+    // FP32 pre-test (n = 2): a candidate whose FP32 distance is farther than
+    // tau from 1 is decided by it; the others by the FP64 test
+    int filter;
+    float inv_r0, inv_r1, tau;
 };
+
+// centres rounded to FP32 for the pre-test
+__global__ void k_centres32(i64 E, const double* __restrict__ centres, float2* __restrict__ c32) {
+    for (i64 e = blockIdx.x * i64(blockDim.x) + threadIdx.x; e < E; e += i64(gridDim.x) * blockDim.x)
+        c32[e] = make_float2(float(centres[2 * e]), float(centres[2 * e + 1]));
+}
 
 __device__ __forceinline__ void cell_of(const Grid& g, double cx, double cy, i64& row, i64& col) {
     const double fx = (cx - g.left) / g.maxr, fy = (cy - g.down) / g.maxr;
@@ -132,13 +142,20 @@ __device__ __forceinline__ double powered(double z0, double z1, int n) {
 }
 
 // Warp per element: count (list == nullptr) or write the neighbour list.
-__global__ void k_neighbours(i64 E, const double* __restrict__ centres, Grid g, const int32_t* __restrict__ cell,
-                             const i64* __restrict__ cell_off, const int32_t* __restrict__ cell_elems,
-                             i64* __restrict__ counts, const i64* __restrict__ offsets, int32_t* __restrict__ list) {
+// The reference's test -- sum of ((c_e - c_f) / R)^n <= 1 in FP64 -- is
+// applied to the candidates whose FP32 distance lies within tau of 1 (with
+// n = 2; tau bounds the FP32 error from above, so the lists are the FP64
+// test's); GB300's FP64 pipe made the two FP64 divisions per candidate the
+// kernel's bound.
+__global__ void k_neighbours(i64 E, const double* __restrict__ centres, const float2* __restrict__ c32, Grid g,
+                             const int32_t* __restrict__ cell, const i64* __restrict__ cell_off,
+                             const int32_t* __restrict__ cell_elems, i64* __restrict__ counts,
+                             const i64* __restrict__ offsets, int32_t* __restrict__ list) {
     const int lane = threadIdx.x & 31;
     const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
     for (i64 e = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; e < E; e += warps) {
         const double cx = centres[2 * e], cy = centres[2 * e + 1];
+        const float2 me = c32[e];
         const i64 id = cell[e];
         const i64 row = id / g.cols, col = id % g.cols;
         i64 found = 0;
@@ -153,9 +170,19 @@ __global__ void k_neighbours(i64 E, const double* __restrict__ centres, Grid g, 
                     int32_t f = -1;
                     if (k + lane < ce) {
                         f = cell_elems[k + lane];
-                        const double z0 = (cx - centres[2 * i64(f)]) / g.R0;
-                        const double z1 = (cy - centres[2 * i64(f) + 1]) / g.R1;
-                        hit = powered(z0, z1, g.n) <= 1.0;
+                        bool decided = false;
+                        if (g.filter) {
+                            const float2 cf = c32[f];
+                            const float z0 = (me.x - cf.x) * g.inv_r0, z1 = (me.y - cf.y) * g.inv_r1;
+                            const float d32 = z0 * z0 + z1 * z1;
+                            if (d32 < 1.0f - g.tau) { hit = true; decided = true; }
+                            else if (d32 > 1.0f + g.tau) { hit = false; decided = true; }
+                        }
+                        if (!decided) {
+                            const double z0 = (cx - centres[2 * i64(f)]) / g.R0;
+                            const double z1 = (cy - centres[2 * i64(f) + 1]) / g.R1;
+                            hit = powered(z0, z1, g.n) <= 1.0;
+                        }
                     }
                     const unsigned mask = __ballot_sync(0xffffffffu, hit);
                     if (list && hit) list[out + __popc(mask & ((1u << lane) - 1u))] = f;
@@ -209,6 +236,18 @@ void find_neighbours(Ctx& ctx, int strategy) {
     g.R0 = R0; g.R1 = R1; g.n = ctx.model.n;
     g.rows = i64(size_t((right - g.left) / g.maxr) + 1);
     g.cols = i64(size_t((up - g.down) / g.maxr) + 1);
+    // FP32 pre-test bound: centres rounded to FP32 (|c| <= M), the
+    // difference, the scaling by 1/R and the square sum each add relative
+    // errors of 2^-24; near the boundary (|z| <= 1) the FP32 distance is
+    // within (19 + 8 M / R) 2^-24 of the exact one, doubled here
+    const double M = std::max(std::max(std::fabs(g.left), std::fabs(right)), std::max(std::fabs(g.down), std::fabs(up)));
+    const double tau = (32.0 + 16.0 * M / std::min(R0, R1)) * std::ldexp(1.0, -24);
+    g.filter = ctx.model.n == 2 && tau < 0.25;
+    g.inv_r0 = float(1.0 / R0);
+    g.inv_r1 = float(1.0 / R1);
+    g.tau = float(tau);
+    ctx.centres32.reserve(size_t(E));
+    NL_LAUNCH(k_centres32, grid_for(E, 256), 256, 0, ctx.stream, E, ctx.centres.p, ctx.centres32.p);
     const i64 n_cells = g.rows * g.cols;
     // scratch: cell id per element, cell offsets, cursors, unsorted and sorted cell lists
     dbuf<int32_t> cell, unsorted, sorted;
@@ -226,13 +265,13 @@ void find_neighbours(Ctx& ctx, int strategy) {
     i64* counts = ctx.i64_scratch_b.p;
     NL_CUDA(cudaMemsetAsync(counts + E, 0, sizeof(i64), ctx.stream));
     const unsigned blocks = grid_for(E * 32, 256, 152 * 64);
-    NL_LAUNCH(k_neighbours, blocks, 256, 0, ctx.stream, E, ctx.centres.p, g, cell.p, cell_off.p, sorted.p, counts,
-              nullptr, nullptr);
+    NL_LAUNCH(k_neighbours, blocks, 256, 0, ctx.stream, E, ctx.centres.p, ctx.centres32.p, g, cell.p, cell_off.p,
+              sorted.p, counts, nullptr, nullptr);
     i64 total = 0;
     exclusive_scan(ctx, counts, ctx.noff.p, E + 1, &total);
     ctx.nlist.resize(size_t(total));
-    NL_LAUNCH(k_neighbours, blocks, 256, 0, ctx.stream, E, ctx.centres.p, g, cell.p, cell_off.p, sorted.p, nullptr,
-              ctx.noff.p, ctx.nlist.p);
+    NL_LAUNCH(k_neighbours, blocks, 256, 0, ctx.stream, E, ctx.centres.p, ctx.centres32.p, g, cell.p, cell_off.p,
+              sorted.p, nullptr, ctx.noff.p, ctx.nlist.p);
     NL_CUDA(cudaStreamSynchronize(ctx.stream));   // scratch buffers are freed on return
     ctx.pairs = total;
     ctx.neighbours_ready = true;
