@@ -315,6 +315,7 @@ struct Ctx {
     dbuf<int32_t> ne_elem;
     dbuf<int8_t> ne_local;
     dbuf<int32_t> elem_minnode;  // smallest node number per element
+    dbuf<int32_t> elem_maxnode;  // largest node number per element
     bool mesh_ready = false;
     // model
     Model model{};

@@ -96,11 +96,14 @@ __global__ void k_quadrature(i64 E, int nen, int nq, const double* __restrict__ 
 
 // smallest node number of each element: orders element pairs for the
 // symmetric assembly (assemble.cu)
-__global__ void k_elem_minnode(i64 E, int nen, const int32_t* __restrict__ elems, int32_t* __restrict__ out) {
+// smallest and largest node number of every element
+__global__ void k_elem_minnode(i64 E, int nen, const int32_t* __restrict__ elems, int32_t* __restrict__ out,
+                               int32_t* __restrict__ out_max) {
     for (i64 e = blockIdx.x * i64(blockDim.x) + threadIdx.x; e < E; e += i64(gridDim.x) * blockDim.x) {
-        int32_t m = elems[e * nen];
-        for (int i = 1; i < nen; ++i) m = min(m, elems[e * nen + i]);
+        int32_t m = elems[e * nen], x = m;
+        for (int i = 1; i < nen; ++i) { m = min(m, elems[e * nen + i]); x = max(x, elems[e * nen + i]); }
         out[e] = m;
+        out_max[e] = x;
     }
 }
 
@@ -203,7 +206,9 @@ void mesh_init(Ctx& ctx) {
     NL_LAUNCH(k_quadrature, grid_for(E * (nq + 1), 256), 256, 0, ctx.stream, E, nen, nq, ctx.nodes.p, ctx.elems.p,
               ctx.basis, ctx.qcoord.p, ctx.jac.p, ctx.deriv.p, ctx.centres.p);
     ctx.elem_minnode.resize(size_t(E));
-    NL_LAUNCH(k_elem_minnode, grid_for(E, 256), 256, 0, ctx.stream, E, nen, ctx.elems.p, ctx.elem_minnode.p);
+    ctx.elem_maxnode.resize(size_t(E));
+    NL_LAUNCH(k_elem_minnode, grid_for(E, 256), 256, 0, ctx.stream, E, nen, ctx.elems.p, ctx.elem_minnode.p,
+              ctx.elem_maxnode.p);
     // node -> elements
     ctx.ne_off.resize(size_t(n + 1));
     ctx.ne_off.zero(ctx.stream);

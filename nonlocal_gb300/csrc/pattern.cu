@@ -10,14 +10,14 @@
 // The candidate columns of row r are the nodes of every neighbour eNL of every
 // element eL containing r (nodes of eL itself for the local part).
 //
-// Here one CTA owns a row.  Candidates are OR-ed into shared-memory bitmaps
+// Here one CTA owns a row.  Candidates are OR-ed into a shared-memory bitmap
 // over a window of node numbers (windows repeat when the row spans more
 // nodes than a window holds, so any numbering works), then the set bits are
-// emitted in increasing order with popcounts and a block scan: the result is
-// the reference's sorted column list without any sort.  Three bitmaps are
-// filled at once: the inner part (upper or full), the bound part, and the
-// full-row inner pattern the solver's SpMV reads (rows padded to a multiple
-// of 4 entries for 16-byte vector loads).
+// classified and emitted in increasing order with per-thread counts and block
+// scans: the result is the reference's sorted column list without any sort.
+// Three lists come out at once: the inner part (upper or full), the bound
+// part, and the full-row inner pattern the solver's SpMV reads (rows padded
+// to a multiple of 4 entries).
 #include "common.cuh"
 
 namespace nlgpu {
@@ -25,7 +25,7 @@ namespace nlgpu {
 namespace {
 
 constexpr int PT_THREADS = 256;
-constexpr int PT_WORDS = 3840;                 // 122880 node numbers per window (3 bitmaps < 48 KB)
+constexpr int PT_WORDS = 11264;                // 360448 node numbers per window (44 KB)
 constexpr i64 PT_WINDOW = i64(PT_WORDS) * 32;
 constexpr int PT_MAX_ELEMS = 16;               // elements sharing one node
 
@@ -39,6 +39,8 @@ struct PatternArgs {
     const i64* noff;
     const int32_t* nlist;
     const uint8_t* is_inner;
+    const int32_t* emin;   // smallest / largest node number of every element
+    const int32_t* emax;
     // count pass outputs
     i64* cnt_inner;
     i64* cnt_bound;
@@ -77,11 +79,17 @@ __device__ __forceinline__ i64 block_scan_excl(i64 v, i64* sh, i64* total) {
     return off + incl - v;
 }
 
+// One CTA per row.  Every candidate column goes into one shared-memory
+// bitmap over a window of node numbers; the set bits are then classified
+// (inner / bound / full) and emitted in increasing order with per-thread
+// counts and block scans.  The window's node range comes from the candidate
+// elements' smallest and largest node numbers, and NEN is a template
+// parameter, so a candidate costs two loads and one shared-memory OR.
+template<int NEN>
 __global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
-    __shared__ uint32_t bm_inner[PT_WORDS], bm_bound[PT_WORDS], bm_full[PT_WORDS];
-    __shared__ i64 seg_end[PT_MAX_ELEMS];     // cumulative candidate counts per element of the row
+    __shared__ uint32_t bm[PT_WORDS];
     __shared__ int32_t seg_elem[PT_MAX_ELEMS];
-    __shared__ i64 seg_noff[PT_MAX_ELEMS];
+    __shared__ i64 seg_noff[PT_MAX_ELEMS], seg_len[PT_MAX_ELEMS];
     __shared__ i64 sh_scan[PT_THREADS / 32];
     __shared__ int red_min[PT_THREADS / 32], red_max[PT_THREADS / 32];
     const bool fill = a.col_inner != nullptr;
@@ -90,38 +98,26 @@ __global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
         const i64 eb = a.ne_off[r], ee = a.ne_off[r + 1];
         const int ne = int(ee - eb);
         if (ne > PT_MAX_ELEMS) { if (threadIdx.x == 0) atomicExch(a.error, 1); continue; }
-        if (threadIdx.x == 0) {
-            i64 acc = 0;
-            for (int s = 0; s < ne; ++s) {
-                const int32_t e = a.ne_elem[eb + s];
-                const i64 len = a.local_only ? 1 : a.noff[e + 1] - a.noff[e];
-                seg_elem[s] = e;
-                seg_noff[s] = a.local_only ? 0 : a.noff[e];
-                acc += len * a.nen;
-                seg_end[s] = acc;
-            }
+        if (threadIdx.x < ne) {
+            const int32_t e = a.ne_elem[eb + threadIdx.x];
+            seg_elem[threadIdx.x] = e;
+            seg_noff[threadIdx.x] = a.local_only ? 0 : a.noff[e];
+            seg_len[threadIdx.x] = a.local_only ? 1 : a.noff[e + 1] - a.noff[e];
         }
         __syncthreads();
-        const i64 total_cand = ne ? seg_end[ne - 1] : 0;
         const bool row_inner = a.is_inner[r];
-
-        // candidate flat index -> node number
-        auto candidate = [&](i64 t) -> int32_t {
-            int s = 0;
-            while (s < ne - 1 && t >= seg_end[s]) ++s;
-            const i64 local = t - (s ? seg_end[s - 1] : 0);
-            const i64 k = local / a.nen;
-            const int j = int(local % a.nen);
-            const int32_t eNL = a.local_only ? seg_elem[s] : a.nlist[seg_noff[s] + k];
-            return a.elems[i64(eNL) * a.nen + j];
+        auto cand_elem = [&](int s, i64 k) -> int32_t {
+            return a.local_only ? seg_elem[s] : a.nlist[seg_noff[s] + k];
         };
 
-        // node range of the candidates
+        // node range of the candidates from their elements' extreme nodes
         int lo = 0x7fffffff, hi = -1;
-        for (i64 t = threadIdx.x; t < total_cand; t += PT_THREADS) {
-            const int32_t c = candidate(t);
-            lo = min(lo, c); hi = max(hi, c);
-        }
+        for (int s = 0; s < ne; ++s)
+            for (i64 k = threadIdx.x; k < seg_len[s]; k += PT_THREADS) {
+                const int32_t e = cand_elem(s, k);
+                lo = min(lo, a.emin[e]);
+                hi = max(hi, a.emax[e]);
+            }
         for (int o = 16; o > 0; o >>= 1) {
             lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
             hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
@@ -138,41 +134,49 @@ __global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
             if (fill && threadIdx.x == 0) { a.col_inner[a.rp_inner[r]] = int32_t(r); a.col_full[a.rp_full[r]] = int32_t(r); }
         }
         for (i64 base = lo; hi >= 0 && base <= hi; base += PT_WINDOW) {
-            for (int w = threadIdx.x; w < PT_WORDS; w += PT_THREADS) { bm_inner[w] = 0u; bm_bound[w] = 0u; bm_full[w] = 0u; }
+            for (int w = threadIdx.x; w < PT_WORDS; w += PT_THREADS) bm[w] = 0u;
             __syncthreads();
-            for (i64 t = threadIdx.x; t < total_cand; t += PT_THREADS) {
-                const int32_t c = candidate(t);
-                const i64 off = i64(c) - base;
-                if (off < 0 || off >= PT_WINDOW) continue;
-                const uint32_t bit = 1u << (off & 31);
-                const int word = int(off >> 5);
-                if (a.is_inner[c]) {
-                    if (row_inner) {
-                        atomicOr(&bm_full[word], bit);
-                        if (!a.symmetric || r <= c) atomicOr(&bm_inner[word], bit);
-                    }
-                } else if (c != r) {
-                    atomicOr(&bm_bound[word], bit);
+            for (int s = 0; s < ne; ++s)
+                for (i64 t = threadIdx.x; t < seg_len[s] * NEN; t += PT_THREADS) {
+                    const int32_t e = cand_elem(s, t / NEN);
+                    const i64 off = i64(a.elems[i64(e) * NEN + int(t % NEN)]) - base;
+                    if (off < 0 || off >= PT_WINDOW) continue;
+                    atomicOr(&bm[off >> 5], 1u << (off & 31));
                 }
-            }
             __syncthreads();
             const i64 span = min(i64(hi) - base + 1, PT_WINDOW);
             const int words = int((span + 31) >> 5);
             const int per = (words + PT_THREADS - 1) / PT_THREADS;
             const int w0 = threadIdx.x * per, w1 = min(words, w0 + per);
+            // matrix_separator_base::part on every distinct candidate column
+            auto classify = [&](int32_t c, bool& in_inner, bool& in_bound, bool& in_full) {
+                const bool c_in = a.is_inner[c];
+                in_full = c_in && row_inner;
+                in_inner = in_full && (!a.symmetric || r <= c);
+                in_bound = !c_in && c != r;
+            };
             i64 ci = 0, cb = 0, cf = 0;
-            for (int w = w0; w < w1; ++w) { ci += __popc(bm_inner[w]); cb += __popc(bm_bound[w]); cf += __popc(bm_full[w]); }
+            for (int w = w0; w < w1; ++w)
+                for (uint32_t m = bm[w]; m; m &= m - 1) {
+                    bool ii, bb, ff;
+                    classify(int32_t(base + i64(w) * 32 + __ffs(m) - 1), ii, bb, ff);
+                    ci += ii; cb += bb; cf += ff;
+                }
             i64 ti, tb, tf;
             const i64 oi = block_scan_excl(ci, sh_scan, &ti);
             const i64 ob = block_scan_excl(cb, sh_scan, &tb);
             const i64 of = block_scan_excl(cf, sh_scan, &tf);
             if (fill) {
                 i64 pi = a.rp_inner[r] + n_inner + oi, pb = a.rp_bound[r] + n_bound + ob, pf = a.rp_full[r] + n_full + of;
-                for (int w = w0; w < w1; ++w) {
-                    for (uint32_t m = bm_inner[w]; m; m &= m - 1) a.col_inner[pi++] = int32_t(base + i64(w) * 32 + __ffs(m) - 1);
-                    for (uint32_t m = bm_bound[w]; m; m &= m - 1) a.col_bound[pb++] = int32_t(base + i64(w) * 32 + __ffs(m) - 1);
-                    for (uint32_t m = bm_full[w]; m; m &= m - 1) a.col_full[pf++] = int32_t(base + i64(w) * 32 + __ffs(m) - 1);
-                }
+                for (int w = w0; w < w1; ++w)
+                    for (uint32_t m = bm[w]; m; m &= m - 1) {
+                        const int32_t c = int32_t(base + i64(w) * 32 + __ffs(m) - 1);
+                        bool ii, bb, ff;
+                        classify(c, ii, bb, ff);
+                        if (ii) a.col_inner[pi++] = c;
+                        if (bb) a.col_bound[pb++] = c;
+                        if (ff) a.col_full[pf++] = c;
+                    }
             }
             n_inner += ti; n_bound += tb; n_full += tf;
             __syncthreads();
@@ -185,6 +189,12 @@ __global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
         }
         __syncthreads();
     }
+}
+
+void launch_pattern(Ctx& ctx, unsigned grid, const PatternArgs& a) {
+    if (a.nen == 4) NL_LAUNCH(k_pattern<4>, grid, PT_THREADS, 0, ctx.stream, a);
+    else if (a.nen == 8) NL_LAUNCH(k_pattern<8>, grid, PT_THREADS, 0, ctx.stream, a);
+    else NL_REQUIRE(false, NLGPU_ERR_UNSUPPORTED, "elements of 4 or 8 nodes");
 }
 
 // full-row entry -> index of the same value in the upper storage (or -1 for padding)
@@ -234,9 +244,10 @@ void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* 
     a.elems = ctx.elems.p; a.ne_off = ctx.ne_off.p; a.ne_elem = ctx.ne_elem.p;
     a.noff = local_only ? nullptr : ctx.noff.p; a.nlist = local_only ? nullptr : ctx.nlist.p;
     a.is_inner = ctx.is_inner.p;
+    a.emin = ctx.elem_minnode.p; a.emax = ctx.elem_maxnode.p;
     a.cnt_inner = ci.p; a.cnt_bound = cb.p; a.cnt_full = cf.p; a.error = err.p;
     const unsigned grid = unsigned(std::min<i64>(n, 152 * 8));
-    NL_LAUNCH(k_pattern, grid, PT_THREADS, 0, ctx.stream, a);
+    launch_pattern(ctx, grid, a);
     int herr = 0;
     NL_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof herr, cudaMemcpyDeviceToHost, ctx.stream));
     i64 nnz_i = 0, nnz_b = 0, nnz_f = 0;
@@ -255,7 +266,7 @@ void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* 
     a.rp_inner = inner.rowptr.p; a.rp_bound = B.rowptr.p; a.rp_full = F.rowptr.p;
     a.col_inner = inner.col.p; a.col_bound = B.col.p; a.col_full = F.col.p;
     // count pointers stay set but are not written in the fill pass
-    NL_LAUNCH(k_pattern, grid, PT_THREADS, 0, ctx.stream, a);
+    launch_pattern(ctx, grid, a);
     inner.val.resize(size_t(nnz_i)); inner.val.zero(ctx.stream);
     B.val.resize(size_t(nnz_b)); B.val.zero(ctx.stream);
     if (full && full_from_upper) {
