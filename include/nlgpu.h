@@ -194,6 +194,16 @@ int nlgpu_get_matrix(nlgpu_ctx* ctx, int which, int64_t* rowptr, int64_t* col, d
  * rhs_init (may be NULL) receives the vector before the first-kind step. */
 int nlgpu_get_rhs(nlgpu_ctx* ctx, double* rhs, double* rhs_init);
 
+/* ---- heat_equation_solution_2d::calc_flux (heat_equation_solution_2d.hpp:99-137)
+ * Nodal heat flux of a temperature field [n_nodes] on the context's mesh and
+ * model: -Lambda grad T at the quadrature points, for a nonlocal model mixed
+ * p1 local + (1 - p1) influence-weighted average over the neighbours'
+ * quadrature points, then averaged to the nodes from the Gauss point nearest
+ * to each node, weighted by element area (mesh_2d_utils.hpp:82-101).
+ * Runs the neighbour search first if the model is nonlocal and it has not
+ * run.  flux_x, flux_y: [n_nodes]. */
+int nlgpu_calc_flux(nlgpu_ctx* ctx, const double* temperature, double* flux_x, double* flux_y);
+
 /* ---- solve: stationary_heat_equation_solver_2d (stationary_heat_equation_solver_2d.hpp:46-120)
  * Runs neighbours (if not yet run), both assemblies, boundary conditions,
  * ILLT(p1 K_local) and preconditioned CG; writes the nodal temperature

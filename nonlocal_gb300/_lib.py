@@ -114,6 +114,7 @@ SIGNATURES = {
     "nlgpu_illt_compute": (c_int, [c_p, c_i64, c_p, c_p, c_p, ctypes.POINTER(c_int)]),
     "nlgpu_illt_solve": (c_int, [c_p, c_i64, c_p, c_p]),
     "nlgpu_illt_solve_f32": (c_int, [c_p, c_i64, c_int, c_p, c_p]),
+    "nlgpu_calc_flux": (c_int, [c_p, c_p, c_p, c_p]),
     "nlgpu_batch_create": (c_int, [ctypes.POINTER(c_p), c_i64, c_p]),
     "nlgpu_batch_destroy": (c_int, [c_p]),
     "nlgpu_batch_step": (c_int, [c_p, c_p, c_d, c_i64, c_p]),

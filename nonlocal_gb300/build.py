@@ -20,8 +20,9 @@ OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libnlgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = ["util.cu", "mesh.cu", "neighbours.cu", "boundary.cu", "pattern.cu", "assemble.cu", "solver.cu",
-         "onedim.cu", "sweep.cu", "jacobi.cu", "mixed.cu", "bicgstab.cu", "batch.cu", "tc_gemm.cu", "mpnn.cu", "noalloc.cu",
-         "api.cu"]
+         "onedim.cu", "sweep.cu", "jacobi.cu", "mixed.cu", "flux.cu", "bicgstab.cu", "batch.cu", "tc_gemm.cu",
+         "mpnn.cu", "noalloc.cu", "api.cu"]
+HEADERS = ["common.cuh", "ff.cuh", "influence.cuh"]
 NO_FMA = {"mesh.cu", "neighbours.cu"}
 
 
@@ -41,9 +42,8 @@ def _flags(unit: str) -> list[str]:
 
 
 def _deps() -> list[str]:
-    files = [os.path.join(SRC, u) for u in UNITS] + [os.path.join(SRC, "common.cuh"),
-                                                      os.path.join(HERE, "..", "include", "nlgpu.h")]
-    return files
+    return ([os.path.join(SRC, u) for u in UNITS + HEADERS] +
+            [os.path.join(HERE, "..", "include", "nlgpu.h")])
 
 
 def up_to_date() -> bool:

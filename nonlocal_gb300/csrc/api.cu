@@ -445,6 +445,24 @@ int nlgpu_get_rhs(nlgpu_ctx* ctx, double* rhs, double* rhs_init) {
     });
 }
 
+int nlgpu_calc_flux(nlgpu_ctx* ctx, const double* temperature, double* flux_x, double* flux_y) {
+    if (!ctx || !temperature || !flux_x || !flux_y) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "mesh and model must be set");
+        if (c.model.nonlocal()) ensure_neighbours(c);
+        const size_t n = size_t(c.n_nodes);
+        dbuf<double> t, fx, fy;
+        t.upload(temperature, n, c.stream);
+        fx.resize(n);
+        fy.resize(n);
+        calc_flux(c, t.p, fx.p, fy.p);
+        fx.download(flux_x, n, c.stream);
+        fy.download(flux_y, n, c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
 int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* temperature,
                           nlgpu_solve_report* report) {
     if (!ctx || !options || !temperature) return NLGPU_ERR_ARG;

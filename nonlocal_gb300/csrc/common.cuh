@@ -118,6 +118,7 @@ struct Basis {
     double qN[MAX_NEN * MAX_NQ], qNxi[MAX_NEN * MAX_NQ], qNeta[MAX_NEN * MAX_NQ];
     double w[MAX_NQ];
     double centre[MAX_NEN];
+    int nearest[MAX_NEN];        // Gauss point nearest to each local node (element_2d_integrate.hpp:87-105)
 };
 Basis make_basis(int element_type);
 
@@ -425,6 +426,8 @@ void sweep_apply(Ctx& ctx, IncompleteCholesky& ic, const double* r, double* z, c
                  const double* flags, double tol2);
 void sweep_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, const double* partials,
                    const double* flags, double tol2);
+// flux.cu: nodal heat flux of a temperature field (device vectors)
+void calc_flux(Ctx& ctx, const double* temperature, double* flux_x, double* flux_y);
 // jacobi.cu: the factor applied by Jacobi sweeps on its two triangles
 void jacobi_build(Ctx& ctx, IncompleteCholesky& ic, const std::vector<i64>& rp, const std::vector<int32_t>& col,
                   const std::vector<i64>& lrp, const std::vector<int32_t>& lcol, const std::vector<i64>& l_to_u);

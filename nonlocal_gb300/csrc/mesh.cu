@@ -5,6 +5,7 @@
 #include "common.cuh"
 
 #include <cmath>
+#include <limits>
 
 namespace nlgpu {
 
@@ -172,6 +173,21 @@ Basis make_basis(int element_type) {
                 shape(element_type, i, x[a], y[c], b.qN[k], b.qNxi[k], b.qNeta[k]);
             }
     for (int i = 0; i < b.nen; ++i) { double dx, dy; shape(element_type, i, 0.0, 0.0, b.centre[i], dx, dy); }
+    // local node coordinates on [-1,1]^2: corners counterclockwise from (-1,-1);
+    // the 8-node element interleaves the mid-sides
+    const double bx[4] = {-1, 1, 1, -1}, by[4] = {-1, -1, 1, 1};
+    const double sx[8] = {-1, 0, 1, 1, 1, 0, -1, -1}, sy[8] = {-1, -1, -1, 0, 1, 1, 1, 0};
+    for (int i = 0; i < b.nen; ++i) {
+        const double nx = b.nen == 4 ? bx[i] : sx[i], ny = b.nen == 4 ? by[i] : sy[i];
+        double best = std::numeric_limits<double>::max();
+        b.nearest[i] = 0;
+        for (int a = 0; a < n1; ++a)
+            for (int c = 0; c < n1; ++c)
+                if (const double d = std::sqrt((nx - x[a]) * (nx - x[a]) + (ny - y[c]) * (ny - y[c])); best > d) {
+                    best = d;
+                    b.nearest[i] = a * n1 + c;
+                }
+    }
     return b;
 }
 

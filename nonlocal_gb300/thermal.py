@@ -215,6 +215,16 @@ class Problem2D(Context):
         L.check(self._lib.nlgpu_get_rhs(self._h, L.ptr(f), L.ptr(f0)))
         return f, f0
 
+    def calc_flux(self, temperature) -> tuple[np.ndarray, np.ndarray]:
+        """heat_equation_solution_2d::calc_flux: the nodal heat flux (x, y) of a
+        temperature field on this problem's mesh and model."""
+        t = L.f64(temperature)
+        if t.shape != (self.n_nodes,):
+            raise ValueError(f"temperature needs {self.n_nodes} nodal values")
+        fx, fy = np.empty(self.n_nodes), np.empty(self.n_nodes)
+        L.check(self._lib.nlgpu_calc_flux(self._h, L.ptr(t), L.ptr(fx), L.ptr(fy)))
+        return fx, fy
+
     # ---- solves -----------------------------------------------------------------
     @staticmethod
     def _options(tolerance, max_iterations, preconditioner, precision, inner_tolerance=0.0,

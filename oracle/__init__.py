@@ -44,6 +44,7 @@ def lib() -> ctypes.CDLL:
         L.orc_solve.argtypes = [c_p, c_int, c_d, ctypes.c_long, c_int]
         L.orc_solve.restype = c_int
         L.orc_nonstationary.argtypes = [c_p, c_d, ctypes.c_long, c_d, c_d, ctypes.c_long]
+        L.orc_calc_flux.argtypes = [c_p, c_p, c_p, c_p]
         L.orc_size.argtypes = [c_p, ctypes.c_char_p]
         L.orc_size.restype = c_i64
         L.orc_get_f64.argtypes = [c_p, ctypes.c_char_p, c_p]
@@ -128,6 +129,13 @@ class Problem:
 
     def nonstationary(self, dt: float, steps: int, omega: float, tol: float = 1e-15, maxit: int = 10000):
         lib().orc_nonstationary(self.h, dt, steps, omega, tol, maxit)
+
+    def calc_flux(self, temperature: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """heat_equation_solution_2d::calc_flux of a nodal temperature field."""
+        t = np.ascontiguousarray(temperature, dtype=np.float64)
+        fx, fy = np.empty_like(t), np.empty_like(t)
+        lib().orc_calc_flux(self.h, _ptr(t), _ptr(fx), _ptr(fy))
+        return fx, fy
 
     def get(self, name: str) -> np.ndarray:
         n = lib().orc_size(self.h, name.encode())

@@ -799,6 +799,101 @@ int orc_solve(void* h, int variant, double tol, long maxit, int stop_true_residu
     return p.ilt_ok;
 }
 
+// heat_equation_solution_2d::calc_flux (heat_equation_solution_2d.hpp:99-137):
+// -Lambda grad T at the quadrature points (gradient_in_qnodes,
+// mesh_2d_utils.hpp:40-60; local_flux_in_qnodes, :72-96), the nonlocal mix
+// p1 local + (1 - p1) sum_eNL sum_qNL w |J| phi local, and the nodal values of
+// qnodes_to_nodes (mesh_2d_utils.hpp:82-101) with mesh_2d::area (mesh_2d.hpp:225-234)
+// and the nearest Gauss point of each local node (element_2d_integrate.hpp:87-105).
+void orc_calc_flux(void* h, const double* T, double* fx_out, double* fy_out) {
+    auto& p = *static_cast<Problem*>(h);
+    const int nen = p.el.nen, nq = p.el.nq;
+    const size_t E = size_t(p.n_elems);
+    std::vector<double> lx(E * size_t(nq)), ly(E * size_t(nq));
+    for (size_t e = 0; e < E; ++e)
+        for (int q = 0; q < nq; ++q) {
+            const size_t s = e * size_t(nq) + size_t(q);
+            double gx = 0, gy = 0;
+            for (int i = 0; i < nen; ++i) {
+                const double v = T[node_of(p, i64(e), i)];
+                const double* d = &p.deriv[2 * ((e * size_t(nen) + size_t(i)) * size_t(nq) + size_t(q))];
+                gx += v * d[0];
+                gy += v * d[1];
+            }
+            gx /= p.jac[s];
+            gy /= p.jac[s];
+            if (p.cond_kind == COND_ISO) {
+                const double c = p.cond_q.empty() ? p.cond[0] : p.cond_q[s];
+                lx[s] = gx * -c; ly[s] = gy * -c;
+            } else if (p.cond_kind == COND_ORTHO) {
+                lx[s] = gx * -p.cond[0]; ly[s] = gy * -p.cond[1];
+            } else {
+                lx[s] = -p.cond[0] * gx - p.cond[2] * gy;
+                ly[s] = -p.cond[2] * gx - p.cond[1] * gy;
+            }
+        }
+    std::vector<double> fx = lx, fy = ly;
+    if (nonlocal_model(p)) {
+        const double nw = 1.0 - p.p1;
+#pragma omp parallel for schedule(dynamic)
+        for (i64 eL = 0; eL < i64(E); ++eL)
+            for (int qL = 0; qL < nq; ++qL) {
+                const size_t sL = size_t(eL) * size_t(nq) + size_t(qL);
+                const vec2 xL{p.qcoord[2 * sL], p.qcoord[2 * sL + 1]};
+                double ngx = 0, ngy = 0;
+                for (i64 k = p.noff[size_t(eL)]; k < p.noff[size_t(eL) + 1]; ++k) {
+                    const size_t eNL = size_t(p.nlist[size_t(k)]);
+                    for (int qN = 0; qN < nq; ++qN) {
+                        const size_t s = eNL * size_t(nq) + size_t(qN);
+                        const double iw = p.el.w[size_t(qN)] * p.jac[s] *
+                                          influence(p, xL, vec2{p.qcoord[2 * s], p.qcoord[2 * s + 1]});
+                        ngx += iw * lx[s];
+                        ngy += iw * ly[s];
+                    }
+                }
+                ngx *= nw; ngy *= nw;
+                fx[sL] = lx[sL] * p.p1 + ngx;
+                fy[sL] = ly[sL] * p.p1 + ngy;
+            }
+    }
+    // nearest Gauss point of each local node on [-1,1]^2
+    const Gauss g = gauss(p.el.type == ORC_BILINEAR ? 2 : 3);
+    const int n1 = int(g.x.size());
+    const double bx[4] = {-1, 1, 1, -1}, by[4] = {-1, -1, 1, 1};
+    const double sx[8] = {-1, 0, 1, 1, 1, 0, -1, -1}, sy[8] = {-1, -1, -1, 0, 1, 1, 1, 0};
+    std::vector<int> nearest(size_t(nen), 0);
+    for (int i = 0; i < nen; ++i) {
+        const double nx = nen == 4 ? bx[i] : sx[i], ny = nen == 4 ? by[i] : sy[i];
+        double best = std::numeric_limits<double>::max();
+        for (int a = 0; a < n1; ++a)
+            for (int c = 0; c < n1; ++c)
+                if (const double d = std::sqrt((nx - g.x[size_t(a)]) * (nx - g.x[size_t(a)]) +
+                                               (ny - g.x[size_t(c)]) * (ny - g.x[size_t(c)])); best > d) {
+                    best = d;
+                    nearest[size_t(i)] = a * n1 + c;
+                }
+    }
+    std::vector<double> area(E, 0.0);
+    for (size_t e = 0; e < E; ++e)
+        for (int q = 0; q < nq; ++q) {
+            const double factor = p.el.w[size_t(q)] * p.jac[e * size_t(nq) + size_t(q)];
+            for (int i = 0; i < nen; ++i) area[e] += factor * p.el.qN[size_t(i * nq + q)];
+        }
+    for (i64 node = 0; node < p.n_nodes; ++node) {
+        double ax = 0, ay = 0, s = 0;
+        for (const i64 e : p.node_elements[size_t(node)]) {
+            int i = 0;
+            while (node_of(p, e, i) != node) ++i;
+            const size_t q = size_t(e) * size_t(nq) + size_t(nearest[size_t(i)]);
+            ax += area[size_t(e)] * fx[q];
+            ay += area[size_t(e)] * fy[q];
+            s += area[size_t(e)];
+        }
+        fx_out[node] = ax / s;
+        fy_out[node] = ay / s;
+    }
+}
+
 // nonstationary_heat_equation_solver_2d::compute + calc_step
 // (nonstationary_heat_equation_solver_2d.hpp:63-106): K <- dt*K + C with unit
 // Dirichlet diagonal, CG with the identity preconditioner and x0 = T_prev,

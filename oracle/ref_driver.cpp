@@ -205,6 +205,19 @@ void dump_neighbours(const nonlocal::mesh::mesh_2d<T, I>& mesh) {
     if (!inf.empty()) dump("search_radius", inf.begin()->second.radius.data(), 2, "2");
 }
 
+// heat_equation_solution_2d::calc_flux (heat_equation_solution_2d.hpp:99-137):
+// the nodal heat flux of a solution, local part -lambda grad T and the
+// influence-weighted nonlocal part, averaged from the nearest quadrature
+// points to the nodes
+template<class Conductivity, class Vector>
+void dump_flux(const std::shared_ptr<nonlocal::mesh::mesh_2d<T, I>>& mesh, const Conductivity& conductivity,
+               const Vector& temperature) {
+    nonlocal::solver_2d::thermal::heat_equation_solution_2d<T, I> solution{mesh, conductivity, temperature};
+    const auto& flux = solution.calc_flux();
+    dumpv("flux_x", flux[0]);
+    dumpv("flux_y", flux[1]);
+}
+
 int stationary2d() {
     using namespace nonlocal;
     using namespace nonlocal::solver_2d;
@@ -292,6 +305,7 @@ int stationary2d() {
         dumps("cg_residual", double(solver.error()));
         const auto Ax = conductivity.matrix().inner() * temperature;
         dumps("true_residual", (f - Ax).norm() / f.norm());
+        dump_flux(mesh, conductivity_parameters, temperature);
         return 0;
     }
 
@@ -319,6 +333,7 @@ int stationary2d() {
     dumps("cg_residual", double(solver.residual()));
     const auto Ax = conductivity.matrix().inner().template selfadjointView<Eigen::Upper>() * temperature;
     dumps("true_residual", (f - Ax).norm() / f.norm());
+    dump_flux(mesh, conductivity_parameters, temperature);
     return 0;
 }
 

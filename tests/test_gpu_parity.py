@@ -151,6 +151,24 @@ def test_nonsymmetric_variable_conductivity(lib):
     t, rep = pb.solve_assembled(tolerance=1e-13, max_iterations=20000)
     assert rep.residual <= 1e-13
     assert rel(t, fx["temperature"]) < SOLUTION_RTOL
+    assert_flux(pb.calc_flux(fx["temperature"]), fx)
+
+
+FLUX_RTOL = 1e-12
+
+
+def assert_flux(got, fx):
+    for g, key in zip(got, ("flux_x", "flux_y")):
+        ref = fx[key]
+        np.testing.assert_allclose(g, ref, rtol=FLUX_RTOL, atol=FLUX_RTOL * max(np.abs(ref).max(), 1e-300),
+                                   err_msg=key)
+
+
+def test_flux(golden):
+    """heat_equation_solution_2d::calc_flux of the reference's temperature: the
+    nodal flux within 1e-12 (max-norm scaled) of the reference's own."""
+    _, fx, pb = golden
+    assert_flux(pb.calc_flux(fx["temperature"]), fx)
 
 
 def test_mixed_precision_solution(golden):
@@ -363,6 +381,13 @@ def test_against_oracle_scaled(lib, case):
         tm, repm = pb.solve_assembled(tolerance=1e-13, precision="mixed", triangular_sweeps=sweeps)
         assert repm.residual <= 1e-13
         assert rel(tm, prob.get("solution")) < SOLUTION_RTOL, sweeps
+    # the nodal flux of the same temperature field (scaled by the flux vector's
+    # largest component: a component that nearly cancels keeps the other's scale)
+    gx, gy = pb.calc_flux(t)
+    ox, oy = prob.calc_flux(t)
+    scale = max(np.abs(ox).max(), np.abs(oy).max())
+    for g, o in ((gx, ox), (gy, oy)):
+        np.testing.assert_allclose(g, o, rtol=FLUX_RTOL, atol=FLUX_RTOL * scale)
 
 
 def test_illt_jacobi_sweeps(lib):

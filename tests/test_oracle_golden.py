@@ -76,6 +76,30 @@ def test_solution(solved):
     assert rel(prob.get("solution"), fx["temperature"]) < 1e-10
 
 
+FLUX_RTOL = 1e-12
+
+
+def assert_flux(got, fx):
+    for g, key in zip(got, ("flux_x", "flux_y")):
+        ref = fx[key]
+        np.testing.assert_allclose(g, ref, rtol=FLUX_RTOL, atol=FLUX_RTOL * max(np.abs(ref).max(), 1e-300), err_msg=key)
+
+
+def test_flux(solved):
+    """heat_equation_solution_2d::calc_flux of the reference's own temperature:
+    nodal flux within 1e-12 (max-norm scaled) of the reference's."""
+    _, fx, prob = solved
+    assert_flux(prob.calc_flux(fx["temperature"]), fx)
+
+
+def test_flux_variable_conductivity():
+    fx = gc.load("b10_field_nonsym")
+    prob = gc.oracle_problem(fx)
+    prob.set_conductivity_field(fx["conductivity_q"])
+    prob.find_neighbours()
+    assert_flux(prob.calc_flux(fx["temperature"]), fx)
+
+
 def test_nonsymmetric_field_matrices():
     """Variable conductivity with a nonlocal model: the oracle reproduces the reference's
     full (non-symmetric) storage bit for bit in pattern and to 1e-12 in values."""
