@@ -292,7 +292,8 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     # -------- stage timings for the roofline (device events, this problem)
     stage_ms = {}
     for stage, name, reps in [(0, "spmv", 50), (4, "spmv32", 50), (2, "illt_apply", 10), (5, "illt_apply32", 10),
-                              (6, "illt_jacobi32", 20), (1, "pair_assembly", 3), (7, "pair_assembly_ff", 3)]:
+                              (6, "illt_jacobi32", 20), (1, "pair_assembly", 3), (7, "pair_assembly_ff", 3),
+                              (8, "flux", 3)]:
         v = ctypes.c_double()
         L.check(lib.nlgpu_time_stage(h, stage, reps, ctypes.byref(v)))
         stage_ms[name] = v.value
@@ -415,6 +416,11 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         "plain_fp64": {"ms_per_step": plain_ms, "cg_iterations": rep_plain.iterations, "residual": rep_plain.residual,
                        "temperature_rel_l2_vs_primary": float(np.linalg.norm(temp_plain - temp) / np.linalg.norm(temp_plain))},
         "speedup_vs_plain_fp64": plain_ms / mean_ms,
+        # heat_equation_solution_2d::calc_flux of the solution (FP64): local flux, the
+        # nonlocal average over every ordered neighbour pair's nq x nq quadrature points
+        "post_processing": {"flux_ms": stage_ms["flux"],
+                            "flux_pair_quadrature_evaluations_per_s":
+                                pairs * PAIR_QUAD[w["element"]] / (stage_ms["flux"] * 1e-3)},
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),

@@ -360,7 +360,7 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
  * SpMV of the solver matrix, 5 FP32 ILLT application with exact level-scheduled
  * sweeps, 6 FP32 ILLT application with the Jacobi sweeps of the last mixed
  * solve (NLGPU_DEFAULT_TRIANGULAR_SWEEPS before any), 7 pair assembly in
- * float-float (stage 1 is the FP64 one). */
+ * float-float (stage 1 is the FP64 one), 8 nodal flux of the last solution. */
 /* Options of a context: NLGPU_OPTION_GLOBAL_SWEEPS = 1 makes the ILLT
  * triangular sweeps read and write their values in global memory instead of
  * the TMA-fed shared-memory ring (same arithmetic); NLGPU_OPTION_ORDERED_PAIRS

@@ -922,7 +922,13 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
         NL_CUDA(cudaEventCreate(&e1));
         dbuf<double> x, y;
         dbuf<float> x32, y32;
-        NL_REQUIRE(stage >= 0 && stage <= 7, NLGPU_ERR_ARG, "unknown stage");
+        NL_REQUIRE(stage >= 0 && stage <= 8, NLGPU_ERR_ARG, "unknown stage");
+        dbuf<double> flux_x, flux_y;
+        if (stage == 8) {
+            NL_REQUIRE(c.temperature.n == size_t(c.n_nodes), NLGPU_ERR_STATE, "solve first (the flux of its temperature)");
+            if (c.model.nonlocal()) ensure_neighbours(c);
+            flux_x.resize(size_t(c.n_nodes)); flux_y.resize(size_t(c.n_nodes));
+        }
         const bool ff_before = c.ff_assembly;
         if (stage == 1 || stage == 7) c.ff_assembly = stage == 7;
         if (stage == 0 || stage == 2 || (stage >= 4 && stage <= 6)) {
@@ -945,7 +951,8 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
             else if (stage == 3) find_neighbours(c, c.strategy);
             else if (stage == 4) spmv32(c, c.full, x32.p, y32.p);
             else if (stage == 5) ilt_apply32(c, c.ilt, x32.p, y32.p, 0);
-            else ilt_apply32(c, c.ilt, x32.p, y32.p, std::max(c.ilt_sweeps, 1));
+            else if (stage == 6) ilt_apply32(c, c.ilt, x32.p, y32.p, std::max(c.ilt_sweeps, 1));
+            else calc_flux(c, c.temperature.p, flux_x.p, flux_y.p);
         }
         NL_CUDA(cudaEventRecord(e1, c.stream));
         NL_CUDA(cudaEventSynchronize(e1));
