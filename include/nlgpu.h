@@ -150,6 +150,53 @@ int nlgpu_get_quadrature(nlgpu_ctx* ctx, double* qcoords, double* jacobians, dou
 int nlgpu_get_basis(nlgpu_ctx* ctx, int* nodes_per_element, int* qnodes, double* qN, double* qNxi,
                     double* qNeta, double* weights, double* centre);
 
+/* ---- mesh files: mesh_parser<T, I, mesh_format::SU2>::parse (su2_parser.hpp:165-195)
+ * Reads an SU2 file into the reference's mesh_container_2d numbering: the
+ * element lines pass through the same hashed containers as in the reference,
+ * so 2D elements, boundary (1D) elements and groups come out in the
+ * reference's order for the same file.  2D elements listed in no 2D marker
+ * form the group "DEFAULT".  Host code; needs no GPU. */
+typedef struct nlgpu_su2 nlgpu_su2;
+int nlgpu_su2_read(const char* path, nlgpu_su2** mesh);
+int nlgpu_su2_free(nlgpu_su2* mesh);
+/* Message of the last failed nlgpu_su2_read on the calling thread. */
+const char* nlgpu_su2_last_error(void);
+/* Any output may be NULL.  element_type: NLGPU_BILINEAR or
+ * NLGPU_QUADRATIC_SERENDIPITY when every 2D element has that type, else -1
+ * (nodes_per_element 0 when the 2D types differ). */
+int nlgpu_su2_info(const nlgpu_su2* mesh, int64_t* n_nodes, int64_t* n_elements_2d, int* nodes_per_element,
+                   int* element_type, int* n_groups);
+/* nodes [n_nodes][2] */
+int nlgpu_su2_nodes(const nlgpu_su2* mesh, double* nodes);
+/* 2D elements [n_elements_2d][nodes_per_element], local node order, the
+ * container's element numbering (ready for nlgpu_mesh_2d). */
+int nlgpu_su2_elements_2d(const nlgpu_su2* mesh, int64_t* elements);
+/* Group g (0 <= g < n_groups) in the container's group order: its name
+ * (NUL-terminated; name_capacity bytes available), dimension (1: boundary
+ * line elements, 2: area elements), first element and count in the
+ * container's numbering (1D elements are numbered after the 2D ones), nodes
+ * per element, and the elements' nodes [count][nodes_per_element] in local
+ * order (end, [middle,] end for line elements: ready for
+ * nlgpu_add_boundary_2d).  Any output may be NULL. */
+int nlgpu_su2_group(const nlgpu_su2* mesh, int g, char* name, int64_t name_capacity, int* dimension,
+                    int64_t* first, int64_t* count, int* nodes_per_element, int64_t* nodes);
+
+/* ---- node renumbering ------------------------------------------------------
+ * mesh::utils::cuthill_mckee (cuthill_mckee.hpp:166-171): the Cuthill-McKee
+ * order of the node graph (nodes coupled through an element when only_local
+ * or the model is local, else through an element and its neighbours, as the
+ * assembled matrix couples them), started from the first node of smallest
+ * degree.  permutation [n_nodes]: permutation[old] = new.  reverse != 0
+ * returns the inverse permutation, as the reference does.  The nonlocal graph
+ * needs the neighbour search (run here if it has not run).  A graph that is
+ * not connected is rejected (NLGPU_ERR_UNSUPPORTED). */
+int nlgpu_cuthill_mckee(nlgpu_ctx* ctx, int only_local, int reverse, int64_t* permutation);
+/* mesh_2d::renumbering (mesh_2d.hpp:258-262, mesh_container_2d.hpp:333-350):
+ * node i becomes node permutation[i]: coordinates, element connectivity,
+ * boundary groups and per-node Dirichlet values move with it; neighbour lists
+ * (per element) stay; matrices are assembled afresh on the next call. */
+int nlgpu_renumbering(nlgpu_ctx* ctx, const int64_t* permutation);
+
 /* ---- model ---------------------------------------------------------------- */
 int nlgpu_set_model_2d(nlgpu_ctx* ctx, const nlgpu_model_2d* model);
 /* Spatially varying isotropic conductivity, one value per quadrature point

@@ -95,6 +95,17 @@ SIGNATURES = {
     "nlgpu_mesh_2d": (c_int, [c_p, c_int, c_i64, c_p, c_i64, c_p]),
     "nlgpu_get_quadrature": (c_int, [c_p, c_p, c_p, c_p]),
     "nlgpu_get_basis": (c_int, [c_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), c_p, c_p, c_p, c_p, c_p]),
+    "nlgpu_su2_read": (c_int, [ctypes.c_char_p, ctypes.POINTER(c_p)]),
+    "nlgpu_su2_free": (c_int, [c_p]),
+    "nlgpu_su2_last_error": (ctypes.c_char_p, []),
+    "nlgpu_su2_info": (c_int, [c_p, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), ctypes.POINTER(c_int),
+                               ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "nlgpu_su2_nodes": (c_int, [c_p, c_p]),
+    "nlgpu_su2_elements_2d": (c_int, [c_p, c_p]),
+    "nlgpu_su2_group": (c_int, [c_p, c_int, c_p, c_i64, ctypes.POINTER(c_int), ctypes.POINTER(c_i64),
+                                ctypes.POINTER(c_i64), ctypes.POINTER(c_int), c_p]),
+    "nlgpu_cuthill_mckee": (c_int, [c_p, c_int, c_int, c_p]),
+    "nlgpu_renumbering": (c_int, [c_p, c_p]),
     "nlgpu_set_model_2d": (c_int, [c_p, ctypes.POINTER(Model2D)]),
     "nlgpu_set_conductivity_field": (c_int, [c_p, c_p]),
     "nlgpu_set_capacity": (c_int, [c_p, c_d, c_d]),

@@ -265,6 +265,44 @@ int nlgpu_mesh_2d(nlgpu_ctx* ctx, int element_type, int64_t n_nodes, const doubl
     });
 }
 
+int nlgpu_cuthill_mckee(nlgpu_ctx* ctx, int only_local, int reverse, int64_t* permutation) {
+    if (!ctx || !permutation) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        const bool local_graph = only_local || !(c.model_ready && c.model.nonlocal());
+        if (!local_graph) ensure_neighbours(c);
+        std::vector<i64> off;
+        std::vector<int32_t> adj;
+        node_graph(c, local_graph, off, adj);
+        const std::vector<i64> perm = cuthill_mckee_order(off, adj);
+        if (reverse)   // reverse_permutation (cuthill_mckee.hpp:157-164): the inverse
+            for (size_t i = 0; i < perm.size(); ++i) permutation[perm[i]] = int64_t(i);
+        else
+            std::copy(perm.begin(), perm.end(), permutation);
+    });
+}
+
+int nlgpu_renumbering(nlgpu_ctx* ctx, const int64_t* permutation) {
+    if (!ctx || !permutation) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        const size_t n = size_t(c.n_nodes);
+        std::vector<int32_t> perm(n);
+        std::vector<char> seen(n, 0);
+        for (size_t i = 0; i < n; ++i) {
+            NL_REQUIRE(permutation[i] >= 0 && permutation[i] < c.n_nodes, NLGPU_ERR_ARG,
+                       "Permutation entry out of range.");
+            NL_REQUIRE(!seen[size_t(permutation[i])], NLGPU_ERR_ARG, "Incorrect permutation, some of the nodes are the same.");
+            seen[size_t(permutation[i])] = 1;
+            perm[i] = int32_t(permutation[i]);
+        }
+        renumber_mesh(c, perm);
+        reset_from_boundary(c);   // element-based neighbour lists stay valid
+    });
+}
+
 int nlgpu_get_quadrature(nlgpu_ctx* ctx, double* qcoords, double* jacobians, double* derivatives) {
     if (!ctx) return NLGPU_ERR_ARG;
     return guarded([&] {

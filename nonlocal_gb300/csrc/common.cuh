@@ -428,6 +428,12 @@ void sweep_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, c
                    const double* flags, double tol2);
 // flux.cu: nodal heat flux of a temperature field (device vectors)
 void calc_flux(Ctx& ctx, const double* temperature, double* flux_x, double* flux_y);
+// renumber.cu: the node graph (adjacency in the reference's order, CSR on the
+// host), its Cuthill-McKee order (perm[old] = new), and the renumbering of
+// the context's mesh by a checked permutation
+void node_graph(Ctx& ctx, bool local_graph, std::vector<i64>& offsets, std::vector<int32_t>& adjacency);
+std::vector<i64> cuthill_mckee_order(const std::vector<i64>& offsets, const std::vector<int32_t>& adjacency);
+void renumber_mesh(Ctx& ctx, const std::vector<int32_t>& perm);
 // jacobi.cu: the factor applied by Jacobi sweeps on its two triangles
 void jacobi_build(Ctx& ctx, IncompleteCholesky& ic, const std::vector<i64>& rp, const std::vector<int32_t>& col,
                   const std::vector<i64>& lrp, const std::vector<int32_t>& lcol, const std::vector<i64>& l_to_u);

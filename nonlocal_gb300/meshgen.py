@@ -52,14 +52,29 @@ class QuadMesh:
         return int(self.elements.shape[0])
 
 
+def relabel_nodes(mesh: QuadMesh, new_of_old: np.ndarray) -> QuadMesh:
+    """The same mesh with node i renamed new_of_old[i] (element and edge order kept)."""
+    p = np.asarray(new_of_old, dtype=np.int64)
+    nodes = np.empty_like(mesh.nodes)
+    nodes[p] = mesh.nodes
+    return QuadMesh(mesh.element, nodes, p[mesh.elements], {k: p[v] for k, v in mesh.boundaries.items()})
+
+
 def structured_quad_mesh(nx: int, ny: int, element: str = BILINEAR, *, width: float = 1.0,
-                         height: float = 1.0, jitter: float = 0.0, seed: int = 0) -> QuadMesh:
+                         height: float = 1.0, jitter: float = 0.0, seed: int = 0,
+                         shuffle_seed: int | None = None) -> QuadMesh:
     """Uniform nx-by-ny quadrilateral mesh of [0,width]x[0,height].
 
     ``jitter`` moves every interior corner node by U(-jitter*h, +jitter*h) in
     each direction (numpy ``default_rng(seed)``); mid-side nodes of 8-node
-    elements are then put back at the midpoints of their edges.
+    elements are then put back at the midpoints of their edges.  With
+    ``shuffle_seed`` the nodes are numbered by a random permutation
+    (``default_rng(shuffle_seed)``) instead of row by row, as an unstructured
+    mesher might number them.
     """
+    if shuffle_seed is not None:
+        m = structured_quad_mesh(nx, ny, element, width=width, height=height, jitter=jitter, seed=seed)
+        return relabel_nodes(m, np.random.default_rng(shuffle_seed).permutation(m.n_nodes))
     if element not in (BILINEAR, SERENDIPITY):
         raise ValueError(f"unknown element type {element!r}")
     hx, hy = width / nx, height / ny
@@ -115,24 +130,38 @@ def structured_quad_mesh(nx: int, ny: int, element: str = BILINEAR, *, width: fl
     return QuadMesh(element, nodes, el.astype(np.int64), {k: v.astype(np.int64) for k, v in bnd.items()})
 
 
-def write_su2(mesh: QuadMesh, path: str) -> None:
-    """Write ``mesh`` as an SU2 text file the reference parser reads back."""
+def write_su2(mesh: QuadMesh, path: str, groups_2d: dict[str, list[int]] | None = None) -> None:
+    """Write ``mesh`` as an SU2 text file the reference parser reads back.
+
+    ``groups_2d`` adds markers of 2D elements (name -> element indices); the
+    reference puts the 2D elements no marker names into its default group.
+    """
     t2 = _SU2_TYPE_2D[mesh.element]
     t1 = _SU2_TYPE_1D[mesh.element]
     o2 = _FILE_ORDER_2D[mesh.element]
     o1 = _FILE_ORDER_1D[mesh.element]
+    groups_2d = groups_2d or {}
+
+    def element_line(e):
+        return f"{t2} " + " ".join(str(int(e[i])) for i in o2)
+
     lines = ["NDIME= 2", f"NELEM= {mesh.n_elements}"]
     for k, e in enumerate(mesh.elements):
-        lines.append(f"{t2} " + " ".join(str(int(e[i])) for i in o2) + f" {k}")
+        lines.append(element_line(e) + f" {k}")
     lines.append(f"NPOIN= {mesh.n_nodes}")
     for k, (x, y) in enumerate(mesh.nodes):
         lines.append(f"{float(x)!r} {float(y)!r} {k}")
-    lines.append(f"NMARK= {len(mesh.boundaries)}")
+    lines.append(f"NMARK= {len(mesh.boundaries) + len(groups_2d)}")
     for name, edges in mesh.boundaries.items():
         lines.append(f"MARKER_TAG= {name}")
         lines.append(f"MARKER_ELEMS= {len(edges)}")
         for e in edges:
             lines.append(f"{t1} " + " ".join(str(int(e[i])) for i in o1))
+    for name, members in groups_2d.items():
+        lines.append(f"MARKER_TAG= {name}")
+        lines.append(f"MARKER_ELEMS= {len(members)}")
+        for k in members:
+            lines.append(element_line(mesh.elements[k]))
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
 

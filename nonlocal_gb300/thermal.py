@@ -77,6 +77,72 @@ class SolveReport:
             raise AttributeError(name) from e
 
 
+@dataclass
+class Su2Mesh:
+    """An SU2 file as the reference's mesh_container_2d numbers it.
+
+    ``element`` is "bilinear" / "serendipity" when all 2D elements have that
+    type (else None); ``groups`` maps each marker (and "DEFAULT", the 2D
+    elements in no 2D marker) to (dimension, elements [count][nodes], first
+    index in the container), in the container's group order."""
+
+    element: str | None
+    nodes: np.ndarray
+    elements: np.ndarray
+    groups: dict[str, tuple[int, np.ndarray, int]]
+
+    def boundary(self, name: str) -> np.ndarray:
+        dim, edges, _ = self.groups[name]
+        if dim != 1:
+            raise ValueError(f"group {name!r} is not a boundary group")
+        return edges
+
+    def renumbered(self, p: np.ndarray) -> "Su2Mesh":
+        nodes = np.empty_like(self.nodes)
+        nodes[p] = self.nodes
+        return Su2Mesh(self.element, nodes, p[self.elements],
+                       {k: (d, p[e], f) for k, (d, e, f) in self.groups.items()})
+
+
+def read_su2(path: str) -> Su2Mesh:
+    """mesh_parser<T, I, mesh_format::SU2>::parse (su2_parser.hpp:165-195) through
+    nlgpu_su2_read: host code, no GPU needed."""
+    lib = L.load()
+    h = ctypes.c_void_p()
+    st = lib.nlgpu_su2_read(str(path).encode(), ctypes.byref(h))
+    if st != L.OK:
+        raise L.NlgpuError(st, lib.nlgpu_su2_last_error().decode())
+    try:
+        n, e2 = ctypes.c_int64(), ctypes.c_int64()
+        nen, et, ng = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        L.check(lib.nlgpu_su2_info(h, ctypes.byref(n), ctypes.byref(e2), ctypes.byref(nen), ctypes.byref(et),
+                                   ctypes.byref(ng)))
+        nodes = np.empty((n.value, 2))
+        L.check(lib.nlgpu_su2_nodes(h, L.ptr(nodes)))
+        elements = np.empty((e2.value, max(nen.value, 1)), dtype=np.int64)
+        if nen.value:
+            L.check(lib.nlgpu_su2_elements_2d(h, L.ptr(elements)))
+        groups = {}
+        name = ctypes.create_string_buffer(4096)
+        for g in range(ng.value):
+            dim, gnen = ctypes.c_int(), ctypes.c_int()
+            first, count = ctypes.c_int64(), ctypes.c_int64()
+            L.check(lib.nlgpu_su2_group(h, g, name, len(name), ctypes.byref(dim), ctypes.byref(first),
+                                        ctypes.byref(count), ctypes.byref(gnen), None))
+            members = np.empty((count.value, gnen.value), dtype=np.int64)
+            L.check(lib.nlgpu_su2_group(h, g, None, 0, None, None, None, None, L.ptr(members)))
+            groups[name.value.decode()] = (dim.value, members, first.value)
+    finally:
+        lib.nlgpu_su2_free(h)
+    element = {L.BILINEAR: BILINEAR, L.QUADRATIC_SERENDIPITY: SERENDIPITY}.get(et.value)
+    return Su2Mesh(element, nodes, elements, groups)
+
+
+def cuthill_mckee(problem: "Problem2D", only_local: bool = False, reverse: bool = False) -> np.ndarray:
+    """mesh::utils::cuthill_mckee(mesh, only_local, reverse) (cuthill_mckee.hpp:166-171)."""
+    return problem.cuthill_mckee(only_local, reverse)
+
+
 class Context:
     """An nlgpu_ctx: device state of one problem on one CUDA stream."""
 
@@ -122,6 +188,36 @@ class Problem2D(Context):
     @classmethod
     def from_mesh(cls, mesh: QuadMesh, **kw) -> "Problem2D":
         return cls(mesh.element, mesh.nodes, mesh.elements, **kw)
+
+    @classmethod
+    def from_su2(cls, path: str, **kw) -> "Problem2D":
+        """mesh_2d(path): the mesh of an SU2 file in the reference's element
+        numbering; the file's markers are kept in ``self.su2`` (see ``read_su2``)."""
+        m = read_su2(path)
+        if m.element is None:
+            raise L.NlgpuError(3, "the 2D elements are not all bilinear or all 8-node serendipity")
+        p = cls(m.element, m.nodes, m.elements, **kw)
+        p.su2 = m
+        return p
+
+    # ---- renumbering ------------------------------------------------------------
+    def cuthill_mckee(self, only_local: bool = False, reverse: bool = False) -> np.ndarray:
+        """mesh::utils::cuthill_mckee: permutation[old] = new (the inverse with reverse=True)."""
+        perm = np.empty(self.n_nodes, dtype=np.int64)
+        L.check(self._lib.nlgpu_cuthill_mckee(self._h, int(only_local), int(reverse), L.ptr(perm)))
+        return perm
+
+    def renumbering(self, permutation) -> None:
+        """mesh_2d::renumbering: node i becomes node permutation[i]."""
+        p = L.i64(permutation)
+        if p.shape != (self.n_nodes,):
+            raise ValueError(f"the permutation needs {self.n_nodes} entries")
+        L.check(self._lib.nlgpu_renumbering(self._h, L.ptr(p)))
+        nodes = np.empty_like(self.nodes)
+        nodes[p] = self.nodes
+        self.nodes, self.elements = nodes, p[self.elements]
+        if getattr(self, "su2", None) is not None:
+            self.su2 = self.su2.renumbered(p)
 
     # ---- model, boundaries ------------------------------------------------
     def set_model(self, model: Model2D) -> None:

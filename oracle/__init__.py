@@ -45,6 +45,8 @@ def lib() -> ctypes.CDLL:
         L.orc_solve.restype = c_int
         L.orc_nonstationary.argtypes = [c_p, c_d, ctypes.c_long, c_d, c_d, ctypes.c_long]
         L.orc_calc_flux.argtypes = [c_p, c_p, c_p, c_p]
+        L.orc_cuthill_mckee.argtypes = [c_p, c_int, c_int, c_p]
+        L.orc_cuthill_mckee.restype = c_int
         L.orc_size.argtypes = [c_p, ctypes.c_char_p]
         L.orc_size.restype = c_i64
         L.orc_get_f64.argtypes = [c_p, ctypes.c_char_p, c_p]
@@ -136,6 +138,13 @@ class Problem:
         fx, fy = np.empty_like(t), np.empty_like(t)
         lib().orc_calc_flux(self.h, _ptr(t), _ptr(fx), _ptr(fy))
         return fx, fy
+
+    def cuthill_mckee(self, only_local: bool = False, reverse: bool = False) -> np.ndarray:
+        """mesh::utils::cuthill_mckee: permutation[old] = new (inverse with reverse)."""
+        out = np.empty(self._nodes.shape[0], dtype=np.int64)
+        if lib().orc_cuthill_mckee(self.h, int(only_local), int(reverse), _ptr(out)) != 0:
+            raise RuntimeError("node graph is not connected")
+        return out
 
     def get(self, name: str) -> np.ndarray:
         n = lib().orc_size(self.h, name.encode())

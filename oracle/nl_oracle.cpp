@@ -24,9 +24,11 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <numbers>
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 namespace {
@@ -964,6 +966,75 @@ i64 orc_size(void* h, const char* name) {
     if (s == "L_col" || s == "L_val") return i64(p.L_rowidx.size());
     if (s == "L_scale") return i64(p.L_scale.size());
     return -1;
+}
+
+// mesh::utils::cuthill_mckee (cuthill_mckee.hpp:107-171).  The node graph of
+// init_graph: mesh_run over the nodes (mesh_2d_utils.hpp:13-37), local
+// theory (only_local or a local model: the nodes of each element of the node)
+// or nonlocal (the nodes of each neighbour of each element of the node), each
+// other node once in order of first meeting (neighbour_checker).  Then
+// calculate_permutation from the first node of smallest degree: layers in a
+// std::unordered_set, unvisited neighbours numbered in std::multimap order of
+// degree.  reverse returns the inverse permutation (reverse_permutation).
+// Returns -1 when the graph is not connected (the reference loops forever).
+int orc_cuthill_mckee(void* h, int only_local, int reverse, i64* out) {
+    auto& p = *static_cast<Problem*>(h);
+    const bool local = only_local || !nonlocal_model(p);
+    const i64 n = p.n_nodes;
+    const int nen = p.el.nen;
+    const size_t count = size_t(n);
+    std::vector<std::vector<i64>> graph(count);
+#pragma omp parallel
+    {
+        std::vector<bool> included(count, false);
+#pragma omp for schedule(dynamic)
+        for (i64 node = 0; node < n; ++node) {
+            auto& adj = graph[size_t(node)];
+            auto check = [&](const i64 neighbour) {
+                if (node != neighbour && !included[size_t(neighbour)]) {
+                    included[size_t(neighbour)] = true;
+                    adj.push_back(neighbour);
+                }
+            };
+            for (const i64 eL : p.node_elements[size_t(node)]) {
+                if (local) {
+                    for (int j = 0; j < nen; ++j) check(p.elems[size_t(eL * nen + j)]);
+                } else {
+                    for (i64 k = p.noff[size_t(eL)]; k < p.noff[size_t(eL) + 1]; ++k) {
+                        const i64 eNL = p.nlist[size_t(k)];
+                        for (int j = 0; j < nen; ++j) check(p.elems[size_t(eNL * nen + j)]);
+                    }
+                }
+            }
+            for (const i64 v : adj) included[size_t(v)] = false;
+        }
+    }
+    i64 init = 0, min_count = std::numeric_limits<i64>::max();
+    for (i64 node = 0; node < n; ++node)
+        if (const i64 c = i64(graph[size_t(node)].size()); c < min_count) { init = node; min_count = c; }
+    std::vector<i64> permutation(size_t(n), -1);
+    i64 curr_index = 0;
+    permutation[size_t(init)] = curr_index++;
+    std::unordered_set<i64> curr_layer{init}, next_layer;
+    while (curr_index < n) {
+        if (curr_layer.empty()) return -1;
+        next_layer.clear();
+        for (const i64 node : curr_layer) {
+            std::multimap<i64, i64> neighbours;
+            for (const i64 nb : graph[size_t(node)])
+                if (permutation[size_t(nb)] == -1) neighbours.emplace(i64(graph[size_t(nb)].size()), nb);
+            for (const auto& [count, nb] : neighbours) {
+                next_layer.emplace(nb);
+                permutation[size_t(nb)] = curr_index++;
+            }
+        }
+        std::swap(curr_layer, next_layer);
+    }
+    if (reverse)
+        for (i64 i = 0; i < n; ++i) out[size_t(permutation[size_t(i)])] = i;
+    else
+        std::copy(permutation.begin(), permutation.end(), out);
+    return 0;
 }
 
 int orc_get_f64(void* h, const char* name, double* out) {

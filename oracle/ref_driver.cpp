@@ -23,6 +23,9 @@
 #include <solvers/solver_1d/influence_functions_1d.hpp>
 #include <solvers/solver_1d/thermal/stationary_heat_equation_solver_1d.hpp>
 #include <metamath/finite_elements/finite_elements_1d/element/element_1d_integrate.hpp>
+#include <map>            // cuthill_mckee.hpp uses std::multimap without including <map>
+#include <unordered_set>
+#include <mesh/mesh_2d/cuthill_mckee.hpp>
 
 #include <chrono>
 #include <cstdio>
@@ -205,6 +208,31 @@ void dump_neighbours(const nonlocal::mesh::mesh_2d<T, I>& mesh) {
     if (!inf.empty()) dump("search_radius", inf.begin()->second.radius.data(), 2, "2");
 }
 
+// mesh::utils::cuthill_mckee (cuthill_mckee.hpp:166-171) for the local and,
+// when the mesh has neighbours, the nonlocal node graph, plain and with
+// reverse = true; then, with renumber=local|nonlocal[_reverse], the mesh is
+// renumbered by that permutation (mesh_2d::renumbering, mesh_2d.hpp:258-262)
+// and everything after this point runs on the renumbered mesh.
+void cuthill_mckee_and_renumber(nonlocal::mesh::mesh_2d<T, I>& mesh, const bool nonlocal_graph) {
+    std::map<std::string, std::vector<size_t>> perms;
+    for (const bool only_local : {true, false}) {
+        if (!only_local && !nonlocal_graph) continue;
+        for (const bool reverse : {false, true}) {
+            const std::string name = std::string{"cm_"} + (only_local ? "local" : "nonlocal") + (reverse ? "_reverse" : "");
+            perms[name] = nonlocal::mesh::utils::cuthill_mckee(mesh, only_local, reverse);
+            std::vector<int64_t> p(perms[name].begin(), perms[name].end());
+            dumpv(name, p);
+        }
+    }
+    const std::string rn = get("renumber");
+    if (rn.empty()) return;
+    const auto& c = mesh.container();
+    std::vector<double> nodes;
+    for (const size_t n : c.nodes()) { nodes.push_back(c.node_coord(n)[0]); nodes.push_back(c.node_coord(n)[1]); }
+    dump("nodes_before_renumbering", nodes.data(), nodes.size(), std::to_string(c.nodes_count()) + ",2");
+    mesh.renumbering(perms.at("cm_" + rn));
+}
+
 // heat_equation_solution_2d::calc_flux (heat_equation_solution_2d.hpp:99-137):
 // the nodal heat flux of a solution, local part -lambda grad T and the
 // influence-weighted nonlocal part, averaged from the nearest quadrature
@@ -239,6 +267,7 @@ int stationary2d() {
         mesh->neighbours(mesh::find_neighbours(*mesh, infl, s));
     }
     dumps("t_neighbours", seconds_since(t0));
+    cuthill_mckee_and_renumber(*mesh, theory_type(p1) == theory_t::NONLOCAL);
     dump_mesh(*mesh);
     dump_neighbours(*mesh);
 

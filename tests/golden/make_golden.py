@@ -70,6 +70,21 @@ CASES = {
                          {"mode": "stationary2d", "influence": "fast_polynomial", "radius": 0.25,
                           "local_weight": 0.5, "conductivity": "1", "conductivity_field": "wave",
                           "bc.left": "temperature:0", "bc.right": "flux:1", "bc.down": "temperature:0.5"}),
+    # nodes numbered at random; Cuthill-McKee of the nonlocal node graph, then the
+    # whole stationary solve on the renumbered mesh (mesh_2d::renumbering)
+    "b12_shuffled_cm": ({"nx": 12, "ny": 12, "element": BILINEAR, "shuffle_seed": 7},
+                        {"mode": "stationary2d", "influence": "fast_polynomial", "radius": 0.2, "local_weight": 0.5,
+                         "conductivity": "1", "bc.left": "temperature:0", "bc.right": "flux:1", "tolerance": 1e-14,
+                         "renumber": "nonlocal"}),
+    # serendipity, random numbering, renumbered by the inverse of the local-graph order
+    "s5_shuffled_cm": ({"nx": 5, "ny": 5, "element": SERENDIPITY, "jitter": 0.1, "seed": 2, "shuffle_seed": 11},
+                       {"mode": "stationary2d", "influence": "constant", "n": 2, "radius": 0.35, "local_weight": 0.6,
+                        "conductivity": "1", "bc.left": "temperature:0", "bc.right": "flux:1", "tolerance": 1e-14,
+                        "renumber": "local_reverse"}),
+    # a named marker of 2D elements beside the default group (SU2 reader's group handling), local model
+    "b6_groups_local": ({"nx": 6, "ny": 6, "element": BILINEAR, "groups_2d": {"inclusion": list(range(7, 21))}},
+                        {"mode": "stationary2d", "local_weight": 1, "conductivity": "1", "bc.left": "temperature:0",
+                         "bc.right": "flux:1", "tolerance": 1e-14}),
     # nonstationary 2D: left T = sin(10 t), identity-preconditioned CG per step
     "b8_nonstationary": ({"nx": 8, "ny": 8, "element": BILINEAR},
                          {"mode": "nonstationary2d", "influence": "fast_polynomial", "radius": 0.3,
@@ -107,13 +122,17 @@ def run_case(name: str, mesh_spec: dict, args: dict, tmp: str) -> None:
         args["mesh"] = os.path.join(REF_MESHES, mesh_spec["su2"])
     elif "nx" in mesh_spec:
         spec = dict(mesh_spec)
+        groups_2d = spec.pop("groups_2d", None)
         m = structured_quad_mesh(spec.pop("nx"), spec.pop("ny"), spec.pop("element"), **spec)
         args["mesh"] = os.path.join(tmp, name + ".su2")
-        write_su2(m, args["mesh"])
+        write_su2(m, args["mesh"], groups_2d)
     out = os.path.join(tmp, name)
     cmd = [DRIVER] + [f"{k}={v}" for k, v in args.items()] + [f"out={out}"]
     subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     data = load_dump(out)
+    if "none" not in mesh_spec:
+        with open(args["mesh"], "rb") as f:   # the exact file the reference parsed
+            data["su2_text"] = np.frombuffer(f.read(), dtype=np.uint8)
     for k in [k for k in data if k.startswith("t_")]:
         data.pop(k)   # wall times are not golden
     cfg = {k: v for k, v in args.items() if k != "mesh"}

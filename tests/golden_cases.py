@@ -12,8 +12,33 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 STATIONARY_2D = ["b12_fastpoly", "s6_exp_ortho_jitter", "b10_poly_no_aniso", "s5_const",
-                 "ref_square16_manufactured", "ref_solid_ring"]
+                 "ref_square16_manufactured", "ref_solid_ring",
+                 "b12_shuffled_cm", "s5_shuffled_cm", "b6_groups_local"]
 NONLOCAL_2D = ["b12_fastpoly", "s6_exp_ortho_jitter", "b10_poly_no_aniso", "s5_const"]
+# every fixture made from an SU2 file (its text is stored as su2_text)
+SU2_CASES = STATIONARY_2D + ["b10_field_nonsym", "b8_nonstationary"]
+# mesh::utils::cuthill_mckee variants stored in the fixtures: name -> (only_local, reverse)
+CUTHILL_MCKEE = {"cm_local": (True, False), "cm_local_reverse": (True, True),
+                 "cm_nonlocal": (False, False), "cm_nonlocal_reverse": (False, True)}
+
+
+def mesh_before_renumbering(fx: dict) -> tuple[np.ndarray, np.ndarray]:
+    """Nodes and elements as the reference read them from the SU2 file: a
+    fixture made with renumber=<variant> stores the renumbered mesh, whose
+    permutation (cm_<variant>, permutation[old] = new) is undone here."""
+    if "nodes_before_renumbering" not in fx:
+        return fx["nodes"], fx["elements"]
+    p = fx["cm_" + fx["config"]["renumber"]]
+    inverse = np.empty_like(p)
+    inverse[p] = np.arange(p.size)
+    return fx["nodes_before_renumbering"], inverse[fx["elements"]]
+
+
+def write_su2_text(fx: dict, path: str) -> str:
+    """Writes the exact SU2 file the reference parsed for this fixture."""
+    with open(path, "wb") as f:
+        f.write(fx["su2_text"].tobytes())
+    return path
 
 INFLUENCE = {"constant": 0, "polynomial": 1, "exponential": 2, "fast_polynomial": 3}
 
