@@ -373,6 +373,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         e2e_s.append(time.perf_counter() - t0)
         pe.close()
     e2e = max_over_ranks(dist, sum(e2e_s) / len(e2e_s))
+    renumbering = renumbering_report(w, mesh, T, L, lib, steps=2) if rank == 0 else None
 
     # -------- CPU baseline (rank 0, N=1): the CPU restatement on the host cores
     cpu = None
@@ -421,6 +422,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         "post_processing": {"flux_ms": stage_ms["flux"],
                             "flux_pair_quadrature_evaluations_per_s":
                                 pairs * PAIR_QUAD[w["element"]] / (stage_ms["flux"] * 1e-3)},
+        "renumbering": renumbering,
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -429,6 +431,51 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     }
     print(json.dumps(line))
     return 0
+
+
+def renumbering_report(w, mesh, T, L, lib, steps: int) -> dict:
+    """The same workload with its nodes numbered at random (as an unstructured
+    mesher may number them): mixed-precision solve time as numbered, the time
+    of mesh::utils::cuthill_mckee (nonlocal node graph) and mesh_2d::renumbering,
+    and the solve time after renumbering."""
+    import ctypes
+    import numpy as np
+    from nonlocal_gb300.meshgen import relabel_nodes
+    shuffled = relabel_nodes(mesh, np.random.default_rng(1).permutation(mesh.n_nodes))
+    pb = make_problem(w, T, shuffled)
+    h = pb.handle
+    precision, pre, sweeps = METHODS["mixed"]
+
+    def solve_ms():
+        out = []
+        for k in range(steps + 1):   # the first solve after a (re)numbering is a warm-up
+            pb.find_neighbours()
+            L.check(lib.nlgpu_flush_l2(h, L2_FLUSH_BYTES))
+            L.check(lib.nlgpu_event_record(h, 0))
+            _, rep = pb.stationary(tolerance=w["tolerance"], max_iterations=100000, precision=precision,
+                                   preconditioner=pre, triangular_sweeps=sweeps)
+            L.check(lib.nlgpu_event_record(h, 1))
+            ms = ctypes.c_double()
+            L.check(lib.nlgpu_event_elapsed(h, 0, 1, ctypes.byref(ms)))
+            if k:
+                out.append(ms.value)
+        return sum(out) / len(out), rep
+
+    before_ms, rep_before = solve_ms()
+    t0 = time.perf_counter()
+    perm = pb.cuthill_mckee(only_local=False, reverse=False)
+    cm_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pb.renumbering(perm)
+    pb.synchronize()
+    renumber_s = time.perf_counter() - t0
+    after_ms, rep_after = solve_ms()
+    pb.close()
+    return {"numbering": "random permutation of the workload's nodes (default_rng(1))",
+            "solve_ms_as_numbered": before_ms, "cg_iterations_as_numbered": rep_before.iterations,
+            "cuthill_mckee_s": cm_s, "renumbering_s": renumber_s,
+            "solve_ms_after_cuthill_mckee": after_ms, "cg_iterations_after": rep_after.iterations,
+            "method": "mixed"}
 
 
 def factor_offdiag_entries(lib, h, n: int) -> int:
