@@ -58,8 +58,10 @@ enum { NLGPU_EXPAND_NO = 0, NLGPU_EXPAND_MAX = 1, NLGPU_EXPAND_MIN = 2, NLGPU_EX
 /* assemble_part (libraries/solvers/solver_2d/base/matrix_assembler_2d.hpp:301-305) */
 enum { NLGPU_PART_LOCAL = 0, NLGPU_PART_FULL = 2 };
 
-/* boundary condition kinds (thermal_boundary_conditions_2d.hpp:271-301) */
-enum { NLGPU_BC_TEMPERATURE = 0, NLGPU_BC_FLUX = 1 };
+/* boundary condition kinds (thermal_boundary_conditions_2d.hpp:9-98): temperature_2d,
+ * flux_2d, convection_2d, radiation_2d, combined_flux_2d */
+enum { NLGPU_BC_TEMPERATURE = 0, NLGPU_BC_FLUX = 1, NLGPU_BC_CONVECTION = 2, NLGPU_BC_RADIATION = 3,
+       NLGPU_BC_COMBINED_FLUX = 4 };
 
 /* matrices that can be copied out */
 enum { NLGPU_MATRIX_INNER = 0, NLGPU_MATRIX_BOUND = 1, NLGPU_MATRIX_LOCAL = 2 };
@@ -116,6 +118,8 @@ typedef struct nlgpu_solve_report {
     int64_t outer_iterations; /* MIXED: FP64 refinement steps (iterations counts the inner ones) */
     int learned_fallback;     /* ILLT_LEARNED: 1 when the correction was gated off or stalled */
     int column_bytes;         /* MIXED: bytes per column index the FP32 SpMV reads (2: 16-bit row offsets) */
+    int64_t nonlinear_iterations; /* radiation: fixed-point steps (0 for a linear problem) */
+    int neumann;              /* 1 for a pure Neumann problem (integral condition) */
 } nlgpu_solve_report;
 
 /* ---- library ------------------------------------------------------------ */
@@ -222,6 +226,37 @@ int nlgpu_get_neighbours(nlgpu_ctx* ctx, int64_t* offsets, int64_t* list);
  * first non-zero value (boundary_condition_first_kind_2d.hpp:16-26). */
 int nlgpu_add_boundary_2d(nlgpu_ctx* ctx, int kind, int64_t n_edges, int nodes_per_edge,
                           const int64_t* edges, double value, const double* node_values);
+/* A second-kind group of any flux kind (thermal_boundary_conditions_2d.hpp:25-98):
+ *   NLGPU_BC_FLUX           flux q;
+ *   NLGPU_BC_CONVECTION     heat transfer alpha and ambient temperature T_a: the
+ *                           flux alpha T_a, and alpha int N_i N_j on the edges in
+ *                           the matrix (convection_condition_2d.hpp:11-31);
+ *   NLGPU_BC_RADIATION      emissivity eps: sigma eps T^4 leaves through the edges,
+ *                           solved by the reference's fixed-point loop
+ *                           (radiation_condition_2d.hpp:91-135,
+ *                           stationary_heat_equation_solver_2d.hpp:66-116);
+ *   NLGPU_BC_COMBINED_FLUX  all three (combined_flux_2d).
+ * A stationary problem whose groups are all NLGPU_BC_FLUX (or that has none) is
+ * a pure Neumann problem: the temperature is fixed by the integral condition
+ * int T = energy (conductivity_matrix_2d.hpp:83-104), after the check that the
+ * fluxes balance (|sum f| <= 1e-10, stationary_heat_equation_solver_2d.hpp:38-41).
+ * A convection or radiation edge that shares a node with a temperature group is
+ * rejected (NLGPU_ERR_UNSUPPORTED) when the solve starts: the reference then
+ * inserts couplings into the Dirichlet rows and columns that this library does
+ * not reproduce. */
+int nlgpu_add_flux_boundary_2d(nlgpu_ctx* ctx, int kind, int64_t n_edges, int nodes_per_edge, const int64_t* edges,
+                               double flux, double heat_transfer, double ambient_temperature, double emissivity);
+/* stationary_equation_parameters_2d (stationary_heat_equation_solver_2d.hpp:19-26):
+ * the radiation loop stops after max_iterations or when the relative change of
+ * the temperature or the norm of the residual falls to tolerance (defaults
+ * 1e-8, 100); energy is int T for a pure Neumann problem (default 0);
+ * initial_temperature [n_nodes] (may be NULL: zero) starts the radiation loop. */
+int nlgpu_set_stationary_parameters(nlgpu_ctx* ctx, double tolerance, int64_t max_iterations, double energy,
+                                    const double* initial_temperature);
+/* Rows of the stationary system: n_nodes, or n_nodes + 1 for a pure Neumann
+ * problem (the reference's Lagrange row; nlgpu_get_matrix and nlgpu_get_rhs then
+ * return n_nodes + 1 rows).  Valid after assembly. */
+int nlgpu_get_system_rows(nlgpu_ctx* ctx, int64_t* rows);
 /* Volume source: constant value, or one value per quadrature point [e][q] when
  * per_qnode is not NULL (right_part_2d.hpp:10-35). */
 int nlgpu_set_source(nlgpu_ctx* ctx, double value, const double* per_qnode);

@@ -25,7 +25,7 @@ INFLUENCE = {"constant": 0, "polynomial": 1, "exponential": 2, "fast_polynomial"
 CONDUCTIVITY_KIND = {1: 0, 2: 1, 3: 2}
 EXPAND = {"NO": 0, "MAX": 1, "MIN": 2, "MEAN": 3}
 PART_LOCAL, PART_FULL = 0, 2
-BC_TEMPERATURE, BC_FLUX = 0, 1
+BC_TEMPERATURE, BC_FLUX, BC_CONVECTION, BC_RADIATION, BC_COMBINED_FLUX = 0, 1, 2, 3, 4
 MATRIX_INNER, MATRIX_BOUND, MATRIX_LOCAL = 0, 1, 2
 PRECONDITIONER = {"identity": 0, "illt": 1, "illt_learned": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
@@ -59,7 +59,8 @@ class SolveReport(ctypes.Structure):
                 ("element_pairs", c_i64), ("seconds_neighbours", c_d), ("seconds_pattern", c_d),
                 ("seconds_assembly", c_d), ("seconds_boundary", c_d), ("seconds_preconditioner", c_d),
                 ("seconds_solve", c_d), ("seconds_total", c_d), ("outer_iterations", c_i64),
-                ("learned_fallback", c_int), ("column_bytes", c_int)]
+                ("learned_fallback", c_int), ("column_bytes", c_int), ("nonlinear_iterations", c_i64),
+                ("neumann", c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -112,6 +113,9 @@ SIGNATURES = {
     "nlgpu_find_neighbours": (c_int, [c_p, c_int, c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_get_neighbours": (c_int, [c_p, c_p, c_p]),
     "nlgpu_add_boundary_2d": (c_int, [c_p, c_int, c_i64, c_int, c_p, c_d, c_p]),
+    "nlgpu_add_flux_boundary_2d": (c_int, [c_p, c_int, c_i64, c_int, c_p, c_d, c_d, c_d, c_d]),
+    "nlgpu_set_stationary_parameters": (c_int, [c_p, c_d, c_i64, c_d, c_p]),
+    "nlgpu_get_system_rows": (c_int, [c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_set_source": (c_int, [c_p, c_d, c_p]),
     "nlgpu_set_dirichlet_values": (c_int, [c_p, c_p]),
     "nlgpu_clear_boundaries": (c_int, [c_p]),

@@ -20,7 +20,8 @@ OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libnlgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = ["util.cu", "mesh.cu", "neighbours.cu", "boundary.cu", "pattern.cu", "assemble.cu", "solver.cu",
-         "onedim.cu", "sweep.cu", "jacobi.cu", "mixed.cu", "flux.cu", "renumber.cu", "su2.cu", "bicgstab.cu",
+         "onedim.cu", "sweep.cu", "jacobi.cu", "mixed.cu", "flux.cu", "renumber.cu", "su2.cu", "nonlinear.cu",
+         "bicgstab.cu",
          "batch.cu", "tc_gemm.cu",
          "mpnn.cu", "noalloc.cu", "api.cu"]
 HEADERS = ["common.cuh", "ff.cuh", "influence.cuh"]

@@ -61,6 +61,36 @@ void ensure_boundary(Ctx& c) {
     if (!c.bc_ready) boundary_vectors(c);
 }
 
+// convection edges into the assembled matrix (convection_condition_2d.hpp:11-31),
+// and the index of every convection / radiation edge pair in it
+void boundary_matrix_terms(Ctx& c) {
+    if (!has_convection(c) && !has_radiation(c)) return;
+    NL_REQUIRE(c.symmetric || !has_radiation(c), NLGPU_ERR_UNSUPPORTED,
+               "radiation with a non-symmetric system (variable conductivity and a nonlocal model)");
+    boundary_matrix_index(c);
+    add_convection(c);
+}
+
+// pure Neumann problems: the Lagrange column int N_i, the balance check of the
+// fluxes (stationary_heat_equation_solver_2d.hpp:38-41) and the right-hand side
+// f - lambda b, lambda = sum f / sum b, the multiplier the bordered system has
+// (its first n rows sum to lambda sum b = sum f, as the rows of K sum to zero)
+void neumann_prepare(Ctx& c) {
+    c.neumann = pure_neumann(c);
+    if (!c.neumann) return;
+    NL_REQUIRE(c.symmetric, NLGPU_ERR_UNSUPPORTED, "a pure Neumann problem with a non-symmetric system");
+    neumann_integrals(c);
+    const size_t n = size_t(c.n_nodes);
+    std::vector<double> f(n), b(n);
+    c.rhs.download(f.data(), n, c.stream);
+    c.node_integral.download(b.data(), n, c.stream);
+    NL_CUDA(cudaStreamSynchronize(c.stream));
+    double sf = 0.0, sb = 0.0;
+    for (size_t i = 0; i < n; ++i) { sf += f[i]; sb += b[i]; }
+    NL_REQUIRE(std::abs(sf) <= 1e-10, NLGPU_ERR_ARG, "It's unsolvable Neumann problem.");
+    add_scaled(c, -sf / sb, c.node_integral.p, c.rhs.p);
+}
+
 // conductivity_matrix_2d::compute(FULL) into inner/bound, and the solver's full rows
 void build_inner(Ctx& c) {
     NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "mesh and model must be set before assembly");
@@ -70,10 +100,43 @@ void build_inner(Ctx& c) {
     build_patterns(c, !c.model.nonlocal(), c.symmetric, c.inner, &c.bound, &c.full, &c.full_from_upper);
     c.ff_assembly = c.assembly_precision == NLGPU_ASSEMBLY_FF;
     assemble_full(c);
+    boundary_matrix_terms(c);
     fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
     c.rhs.resize(size_t(c.n_nodes));
     apply_first_kind(c, c.bound, c.rhs_init.p, c.rhs.p, c.x_dirichlet.p);
+    neumann_prepare(c);
     c.inner_ready = true;
+}
+
+// CSR of n rows copied out as the reference stores a pure Neumann problem's
+// matrix: each row ends with the Lagrange column n (int N_i), and row n holds
+// its zero diagonal (conductivity_matrix_2d.hpp:39-72)
+void download_csr_bordered(Ctx& c, const Csr& m, const double* lagrange, int64_t* rowptr, int64_t* col, double* val) {
+    const size_t n = size_t(m.rows), nnz = size_t(m.nnz);
+    std::vector<int64_t> rp(n + 1);
+    std::vector<double> vl(val ? nnz : 0), b(n, 0.0);
+    m.rowptr.download(rp.data(), n + 1, c.stream);
+    std::vector<int32_t> c32(col ? nnz : 0);
+    if (col) m.col.download(c32.data(), nnz, c.stream);
+    if (val) m.val.download(vl.data(), nnz, c.stream);
+    if (lagrange && val) NL_CUDA(cudaMemcpyAsync(b.data(), lagrange, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    NL_CUDA(cudaStreamSynchronize(c.stream));
+    if (rowptr) {
+        for (size_t r = 0; r <= n; ++r) rowptr[r] = rp[r] + int64_t(r);
+        rowptr[n + 1] = rp[n] + int64_t(n) + 1;
+    }
+    for (size_t r = 0; r < n; ++r) {
+        const size_t out = size_t(rp[r]) + r;
+        const size_t len = size_t(rp[r + 1] - rp[r]);
+        for (size_t k = 0; k < len; ++k) {
+            if (col) col[out + k] = c32[size_t(rp[r]) + k];
+            if (val) val[out + k] = vl[size_t(rp[r]) + k];
+        }
+        if (col) col[out + len] = int64_t(n);
+        if (val) val[out + len] = b[r];
+    }
+    if (col) col[size_t(rp[n]) + n] = int64_t(n);
+    if (val) val[size_t(rp[n]) + n] = 0.0;
 }
 
 // p1 * K_local with the reference's LOCAL theories (stationary_heat_equation_solver_2d.hpp:91-93)
@@ -108,14 +171,19 @@ void fill_report(Ctx& c, nlgpu_solve_report* rep, const CgResult& r) {
     rep->column_bytes = c.full.col16_ok ? 2 : 4;
 }
 
-CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep) {
+// One linear solve of the assembled system with right-hand side rhs (default
+// ctx.rhs) into ctx.temperature.  keep_preconditioner reuses the ILLT factor
+// of the previous call (the radiation loop changes only boundary entries).
+CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep, const double* rhs = nullptr,
+                      bool keep_preconditioner = false) {
     NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "the system must be assembled first");
+    const double* b = rhs ? rhs : c.rhs.p;
     if (!c.symmetric) {
         // variable conductivity with a nonlocal model: full storage, BiCGSTAB with
         // the diagonal preconditioner (stationary_heat_equation_solver_2d.hpp:105-108)
         const auto t0 = std::chrono::steady_clock::now();
         c.temperature.resize(size_t(c.n_nodes));
-        CgResult r = bicgstab_solve(c, c.full, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations);
+        CgResult r = bicgstab_solve(c, c.full, b, c.temperature.p, o.tolerance, o.max_iterations);
         if (rep) rep->seconds_solve = seconds(t0);
         fill_report(c, rep, r);
         return r;
@@ -136,7 +204,7 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
         if (!c.local_ready) build_local(c);
         timer.mark("local matrix");
         // the exact sweeps' shared-memory plans only when this solve uses them
-        ilt_build(c, c.local, c.ilt, !(mixed && sweeps > 0));
+        if (!keep_preconditioner) ilt_build(c, c.local, c.ilt, !(mixed && sweeps > 0));
         timer.mark("preconditioner");
         if (c.ilt.ok) M = &c.ilt;   // identity fallback (stationary_heat_equation_solver_2d.hpp:97-101)
         if (learned && M && !(c.mp.ready && c.mp.n == c.local.rows)) mpnn_prepare(c, c.local);
@@ -152,13 +220,13 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
         matrix_to_f32(c, c.full);
         timer.mark("FP32 matrix");
         c.ilt_sweeps = sweeps;
-        r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations,
+        r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, b, c.temperature.p, o.tolerance, o.max_iterations,
                         o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M && c.mp.use,
                         c.ilt_sweeps);
         if (learned && M && c.mp.use) mpnn_check(c);
         if (learned && !(M && c.mp.use)) r.learned_fallback = true;   // gated off: ILLT alone
     } else {
-        r = cg_solve(c, c.full, M, c.rhs.p, c.temperature.p, o.tolerance, o.max_iterations, false);
+        r = cg_solve(c, c.full, M, b, c.temperature.p, o.tolerance, o.max_iterations, false);
     }
     if (rep) rep->seconds_solve = seconds(t0);
     if (M && c.sweep_error.n) {
@@ -168,6 +236,85 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
         NL_REQUIRE(err == 0, NLGPU_ERR_TIMEOUT, "a triangular sweep stage wait gave up");
     }
     fill_report(c, rep, r);
+    return r;
+}
+
+// stationary_heat_equation_solver_2d.hpp:66-116 with radiation edges: from the
+// initial temperature, each step solves K_T dT = K T_prev - r_rad - f, where K
+// holds conductivity and convection, K_T = K - 4 sigma eps int T_prev^3 N_i N_j
+// and r_rad = -sigma eps int T_prev^4 N_i, then T = T_prev - dT; it stops after
+// max_iterations or once |T - T_prev| / |T| or |residual| is at most the
+// tolerance.  The linear solves are this library's ILLT-CG (the reference uses
+// Jacobi-preconditioned CG to machine precision; both solve the same system).
+CgResult radiation_loop(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep) {
+    const i64 n = c.n_nodes;
+    c.nl_work.resize(size_t(4 * n));
+    double* kt = c.nl_work.p;            // K T_prev
+    double* rad = kt + n;                // r_rad
+    double* prev = rad + n;              // T_prev
+    double* residual = prev + n;
+    if (c.initial_temperature.n) {
+        NL_CUDA(cudaMemcpyAsync(prev, c.initial_temperature.p, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    } else {
+        NL_CUDA(cudaMemsetAsync(prev, 0, size_t(n) * sizeof(double), c.stream));
+    }
+    c.upper_base.resize(size_t(c.inner.nnz));
+    NL_CUDA(cudaMemcpyAsync(c.upper_base.p, c.inner.val.p, size_t(c.inner.nnz) * sizeof(double),
+                            cudaMemcpyDeviceToDevice, c.stream));
+    c.temperature.resize(size_t(n));
+    NL_CUDA(cudaMemcpyAsync(c.temperature.p, prev, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    CgResult total;
+    total.converged = true;
+    double difference = 1.0, norm = 1.0;
+    i64 it = 0;
+    while (it < c.nl_max_iterations && c.nl_tolerance < difference && c.nl_tolerance < norm) {
+        NL_CUDA(cudaMemcpyAsync(c.inner.val.p, c.upper_base.p, size_t(c.inner.nnz) * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c.stream));
+        fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
+        spmv_full(c, c.full, prev, kt);
+        NL_CUDA(cudaMemsetAsync(rad, 0, size_t(n) * sizeof(double), c.stream));
+        add_radiation(c, prev, rad, -4.0, -1.0);
+        fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
+        subtract3(c, kt, rad, c.rhs.p, residual);
+        const CgResult r = solve_system(c, o, rep, residual, it > 0);
+        total.iterations += r.iterations;
+        total.outer_iterations += r.outer_iterations;
+        total.residual = r.residual;
+        total.reference_residual = r.reference_residual;
+        total.converged = total.converged && r.converged;
+        const std::array<double, 3> s = step_norms(c, residual, prev, c.temperature.p);
+        ++it;
+        norm = std::sqrt(s[0]);
+        const double tn = std::sqrt(s[2]);
+        difference = std::sqrt(s[1]) / (tn != 0.0 ? tn : 1.0);
+        NL_CUDA(cudaMemcpyAsync(prev, c.temperature.p, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    }
+    // leave the assembled matrix (conductivity and convection) in place
+    NL_CUDA(cudaMemcpyAsync(c.inner.val.p, c.upper_base.p, size_t(c.inner.nnz) * sizeof(double),
+                            cudaMemcpyDeviceToDevice, c.stream));
+    fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
+    NL_CUDA(cudaStreamSynchronize(c.stream));
+    fill_report(c, rep, total);
+    if (rep) rep->nonlinear_iterations = it;
+    return total;
+}
+
+// The stationary solve of the assembled system: one linear solve, or the
+// radiation loop; a pure Neumann problem's temperature is then shifted to
+// int T = energy (the bordered system's last row)
+CgResult stationary_solve(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* rep) {
+    const CgResult r = has_radiation(c) ? radiation_loop(c, o, rep) : solve_system(c, o, rep);
+    if (c.neumann) {
+        const size_t n = size_t(c.n_nodes);
+        std::vector<double> t(n), b(n);
+        c.temperature.download(t.data(), n, c.stream);
+        c.node_integral.download(b.data(), n, c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        double bt = 0.0, sb = 0.0;
+        for (size_t i = 0; i < n; ++i) { bt += b[i] * t[i]; sb += b[i]; }
+        add_constant(c, (c.energy - bt) / sb, c.temperature.p);
+    }
+    if (rep) rep->neumann = c.neumann ? 1 : 0;
     return r;
 }
 
@@ -381,26 +528,79 @@ int nlgpu_get_neighbours(nlgpu_ctx* ctx, int64_t* offsets, int64_t* list) {
     });
 }
 
+namespace {
+
+// one boundary group; value is the temperature or the second-kind flux
+// (operator() of the condition classes, thermal_boundary_conditions_2d.hpp:20-97)
+void add_group(Ctx& c, int kind, int64_t n_edges, int nodes_per_edge, const int64_t* edges, double value,
+               const double* node_values, double heat_transfer, double emissivity) {
+    NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+    NL_REQUIRE(nodes_per_edge == 2 || nodes_per_edge == 3, NLGPU_ERR_UNSUPPORTED, "boundary edges have 2 or 3 nodes");
+    BoundaryGroup g;
+    g.kind = kind; g.nen = nodes_per_edge; g.n_edges = n_edges; g.value = value;
+    g.heat_transfer = heat_transfer; g.emissivity = emissivity;
+    std::vector<int32_t> e(size_t(n_edges * nodes_per_edge));
+    for (size_t k = 0; k < e.size(); ++k) {
+        NL_REQUIRE(edges[k] >= 0 && edges[k] < c.n_nodes, NLGPU_ERR_ARG, "boundary node out of range");
+        e[k] = int32_t(edges[k]);
+    }
+    g.edges.upload(e.data(), e.size(), c.stream);
+    if (node_values) g.node_values.upload(node_values, e.size(), c.stream);
+    NL_CUDA(cudaStreamSynchronize(c.stream));
+    c.groups.push_back(std::move(g));
+    reset_from_boundary(c);
+}
+
+}  // namespace
+
 int nlgpu_add_boundary_2d(nlgpu_ctx* ctx, int kind, int64_t n_edges, int nodes_per_edge, const int64_t* edges,
                           double value, const double* node_values) {
     if (!ctx || !edges || n_edges < 0) return NLGPU_ERR_ARG;
     return guarded([&] {
+        NL_REQUIRE(kind == NLGPU_BC_TEMPERATURE || kind == NLGPU_BC_FLUX, NLGPU_ERR_ARG,
+                   "unknown boundary kind (convection and radiation: nlgpu_add_flux_boundary_2d)");
+        add_group(*ctx, kind, n_edges, nodes_per_edge, edges, value, node_values, 0.0, 0.0);
+    });
+}
+
+int nlgpu_add_flux_boundary_2d(nlgpu_ctx* ctx, int kind, int64_t n_edges, int nodes_per_edge, const int64_t* edges,
+                               double flux, double heat_transfer, double ambient_temperature, double emissivity) {
+    if (!ctx || !edges || n_edges < 0) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        double value = 0.0;
+        switch (kind) {
+        case NLGPU_BC_FLUX: value = flux; heat_transfer = emissivity = 0.0; break;
+        case NLGPU_BC_CONVECTION: value = heat_transfer * ambient_temperature; emissivity = 0.0; break;
+        case NLGPU_BC_RADIATION: value = 0.0; heat_transfer = 0.0; break;
+        case NLGPU_BC_COMBINED_FLUX: value = flux + heat_transfer * ambient_temperature; break;
+        default: throw nlgpu::error{NLGPU_ERR_ARG, "unknown flux boundary kind"};
+        }
+        NL_REQUIRE(std::isfinite(value) && std::isfinite(heat_transfer) && std::isfinite(emissivity), NLGPU_ERR_ARG,
+                   "boundary coefficients must be finite");
+        add_group(*ctx, kind, n_edges, nodes_per_edge, edges, value, nullptr, heat_transfer, emissivity);
+    });
+}
+
+int nlgpu_set_stationary_parameters(nlgpu_ctx* ctx, double tolerance, int64_t max_iterations, double energy,
+                                    const double* initial_temperature) {
+    if (!ctx || max_iterations < 0 || !std::isfinite(energy)) return NLGPU_ERR_ARG;
+    return guarded([&] {
         Ctx& c = *ctx;
         NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
-        NL_REQUIRE(kind == NLGPU_BC_TEMPERATURE || kind == NLGPU_BC_FLUX, NLGPU_ERR_ARG, "unknown boundary kind");
-        NL_REQUIRE(nodes_per_edge == 2 || nodes_per_edge == 3, NLGPU_ERR_UNSUPPORTED, "boundary edges have 2 or 3 nodes");
-        BoundaryGroup g;
-        g.kind = kind; g.nen = nodes_per_edge; g.n_edges = n_edges; g.value = value;
-        std::vector<int32_t> e(size_t(n_edges * nodes_per_edge));
-        for (size_t k = 0; k < e.size(); ++k) {
-            NL_REQUIRE(edges[k] >= 0 && edges[k] < c.n_nodes, NLGPU_ERR_ARG, "boundary node out of range");
-            e[k] = int32_t(edges[k]);
-        }
-        g.edges.upload(e.data(), e.size(), c.stream);
-        if (node_values) g.node_values.upload(node_values, e.size(), c.stream);
+        c.nl_tolerance = tolerance;
+        c.nl_max_iterations = max_iterations;
+        c.energy = energy;
+        if (initial_temperature) c.initial_temperature.upload(initial_temperature, size_t(c.n_nodes), c.stream);
+        else c.initial_temperature.release();
         NL_CUDA(cudaStreamSynchronize(c.stream));
-        c.groups.push_back(std::move(g));
-        reset_from_boundary(c);
+    });
+}
+
+int nlgpu_get_system_rows(nlgpu_ctx* ctx, int64_t* rows) {
+    if (!ctx || !rows) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        NL_REQUIRE(ctx->inner_ready, NLGPU_ERR_STATE, "FULL part not assembled");
+        *rows = ctx->n_nodes + (ctx->neumann ? 1 : 0);
     });
 }
 
@@ -445,11 +645,12 @@ int nlgpu_conductivity_matrix_2d(nlgpu_ctx* ctx, int part, int64_t* nnz_inner, i
         NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "mesh and model must be set before assembly");
         if (part == NLGPU_PART_FULL) {
             build_inner(c);
-            if (nnz_inner) *nnz_inner = c.inner.nnz;
-            if (nnz_bound) *nnz_bound = c.bound.nnz;
+            // a pure Neumann problem is copied out with the Lagrange column and row
+            if (nnz_inner) *nnz_inner = c.inner.nnz + (c.neumann ? c.n_nodes + 1 : 0);
+            if (nnz_bound) *nnz_bound = c.neumann ? 0 : c.bound.nnz;
         } else {
             build_local(c);
-            if (nnz_inner) *nnz_inner = c.local.nnz;
+            if (nnz_inner) *nnz_inner = c.local.nnz + (c.neumann && c.node_integral.n ? c.n_nodes + 1 : 0);
             if (nnz_bound) *nnz_bound = 0;
         }
         NL_CUDA(cudaStreamSynchronize(c.stream));
@@ -462,10 +663,17 @@ int nlgpu_get_matrix(nlgpu_ctx* ctx, int which, int64_t* rowptr, int64_t* col, d
         Ctx& c = *ctx;
         if (which == NLGPU_MATRIX_INNER || which == NLGPU_MATRIX_BOUND) {
             NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "FULL part not assembled");
-            download_csr(c, which == NLGPU_MATRIX_INNER ? c.inner : c.bound, rowptr, col, val);
+            if (c.neumann && which == NLGPU_MATRIX_INNER) {
+                download_csr_bordered(c, c.inner, c.node_integral.p, rowptr, col, val);
+            } else if (c.neumann) {   // no temperature nodes: an empty bound part of n + 1 rows
+                if (rowptr) std::fill(rowptr, rowptr + c.n_nodes + 2, int64_t{0});
+            } else {
+                download_csr(c, which == NLGPU_MATRIX_INNER ? c.inner : c.bound, rowptr, col, val);
+            }
         } else if (which == NLGPU_MATRIX_LOCAL) {
             NL_REQUIRE(c.local_ready, NLGPU_ERR_STATE, "LOCAL part not assembled");
-            download_csr(c, c.local, rowptr, col, val);
+            if (c.neumann && c.node_integral.n) download_csr_bordered(c, c.local, c.node_integral.p, rowptr, col, val);
+            else download_csr(c, c.local, rowptr, col, val);
         } else {
             throw nlgpu::error{NLGPU_ERR_ARG, "unknown matrix"};
         }
@@ -477,8 +685,14 @@ int nlgpu_get_rhs(nlgpu_ctx* ctx, double* rhs, double* rhs_init) {
     return guarded([&] {
         Ctx& c = *ctx;
         NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "FULL part not assembled");
-        if (rhs) c.rhs.download(rhs, size_t(c.n_nodes), c.stream);
         if (rhs_init) c.rhs_init.download(rhs_init, size_t(c.n_nodes), c.stream);
+        if (rhs && c.neumann) {   // the reference's f: the fluxes (not shifted by lambda b) and the energy row
+            c.rhs_init.download(rhs, size_t(c.n_nodes), c.stream);
+            rhs[c.n_nodes] = c.energy;
+        } else if (rhs) {
+            c.rhs.download(rhs, size_t(c.n_nodes), c.stream);
+        }
+        if (rhs_init && c.neumann) rhs_init[c.n_nodes] = c.energy;
         NL_CUDA(cudaStreamSynchronize(c.stream));
     });
 }
@@ -508,7 +722,7 @@ int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, do
     const int rc = guarded([&] {
         Ctx& c = *ctx;
         const auto t0 = std::chrono::steady_clock::now();
-        const CgResult r = solve_system(c, *options, report);
+        const CgResult r = stationary_solve(c, *options, report);
         c.temperature.download(temperature, size_t(c.n_nodes), c.stream);
         NL_CUDA(cudaStreamSynchronize(c.stream));
         if (report) report->seconds_total = seconds(t0);
@@ -549,6 +763,7 @@ int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, doub
         c.ff_assembly = c.assembly_precision == NLGPU_ASSEMBLY_FF ||
                         (c.assembly_precision == NLGPU_ASSEMBLY_AUTO && mixed);
         assemble_full(c);
+        boundary_matrix_terms(c);
         fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
         assemble_local(c, c.local, c.model.p1, 0);
         c.local_ready = true;
@@ -557,10 +772,11 @@ int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, doub
         t0 = std::chrono::steady_clock::now();
         c.rhs.resize(size_t(c.n_nodes));
         apply_first_kind(c, c.bound, c.rhs_init.p, c.rhs.p, c.x_dirichlet.p);
+        neumann_prepare(c);
         NL_CUDA(cudaStreamSynchronize(c.stream));
         rep->seconds_boundary += seconds(t0);
         c.inner_ready = true;
-        const CgResult r = solve_system(c, *options, rep);
+        const CgResult r = stationary_solve(c, *options, rep);
         c.temperature.download(temperature, size_t(c.n_nodes), c.stream);
         NL_CUDA(cudaStreamSynchronize(c.stream));
         rep->seconds_total = seconds(t_all);
@@ -806,6 +1022,8 @@ int nlgpu_nonstationary_2d_compute(nlgpu_ctx* ctx, double time_step, const doubl
         build_patterns(c, !c.model.nonlocal(), true, c.inner, &c.bound, &c.full, &c.full_from_upper);
         c.ff_assembly = c.assembly_precision == NLGPU_ASSEMBLY_FF;
         assemble_full(c);
+        boundary_matrix_terms(c);   // convection before the time-step scaling (nonstationary_heat_equation_solver_2d.hpp:74)
+        c.neumann = false;
         build_patterns(c, true, true, c.capacity_m, nullptr, &c.capacity_full, &c.capacity_map);
         assemble_local(c, c.capacity_m, c.capacity * c.density, 1);
         fill_full_from_upper(c, c.capacity_m, c.capacity_full, c.capacity_map);
@@ -834,7 +1052,19 @@ int nlgpu_nonstationary_2d_step(nlgpu_ctx* ctx, double dirichlet_value, const do
         // calc_step (nonstationary_heat_equation_solver_2d.hpp:90-106):
         // f = dt * (flux + source) + C T_prev; f -= dt K_bound x_D; f[D] = x_D; CG from T_prev
         if (dirichlet_values) c.step_xd.upload(dirichlet_values, size_t(c.n_nodes), c.stream);
-        nonstationary_rhs(c, dirichlet_value, dirichlet_values != nullptr);
+        const double* radiation = nullptr;
+        if (has_radiation(c)) {
+            // radiation_condition_2d (radiation_condition_2d.hpp:43-88) on the previous
+            // temperature: dt 4 sigma eps int T^3 N_i N_j is added to the system matrix
+            // and stays there for the following steps, as in the reference; the
+            // vector 3 sigma eps int T^4 N_i joins the fluxes
+            c.nl_work.resize(size_t(c.n_nodes));
+            c.nl_work.zero(c.stream);
+            add_radiation(c, c.temperature.p, c.nl_work.p, 4.0 * c.time_step, 3.0);
+            fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
+            radiation = c.nl_work.p;
+        }
+        nonstationary_rhs(c, dirichlet_value, dirichlet_values != nullptr, radiation);
         const CgResult r = cg_solve(c, c.full, nullptr, c.rhs.p, c.temperature.p, tolerance, max_iterations, true);
         if (temperature) c.temperature.download(temperature, size_t(c.n_nodes), c.stream);
         NL_CUDA(cudaStreamSynchronize(c.stream));
@@ -855,6 +1085,8 @@ int nlgpu_batch_create(nlgpu_batch** batch, int64_t count, nlgpu_ctx* const* ins
         std::vector<Ctx*> v;
         for (int64_t k = 0; k < count; ++k) {
             NL_REQUIRE(instances[k], NLGPU_ERR_ARG, "null instance");
+            NL_REQUIRE(!has_radiation(*instances[k]), NLGPU_ERR_UNSUPPORTED,
+                       "radiation edges change the matrix every step: step such problems one by one");
             v.push_back(instances[k]);
         }
         auto* b = new nlgpu_batch{};

@@ -695,12 +695,14 @@ void combine_nonstationary(Ctx& ctx, double dt) {
 }
 
 // rhs = dt * rhs_init + C T_prev, then the first-kind step with the step's Dirichlet values
-void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values) {
+void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values, const double* radiation) {
     const i64 n = ctx.n_nodes;
     NL_LAUNCH(k_step_dirichlet, grid_for(n, 256), 256, 0, ctx.stream, n, ctx.is_inner.p, dirichlet_value,
               per_node_values, ctx.step_xd.p);
     spmv_full(ctx, ctx.capacity_full, ctx.temperature.p, ctx.step_tmp.p);
     NL_LAUNCH(k_axpy_into, grid_for(n, 256), 256, 0, ctx.stream, n, ctx.time_step, ctx.rhs_init.p, ctx.step_tmp.p);
+    if (radiation)
+        NL_LAUNCH(k_axpy_into, grid_for(n, 256), 256, 0, ctx.stream, n, ctx.time_step, radiation, ctx.step_tmp.p);
     apply_first_kind(ctx, ctx.bound, ctx.step_tmp.p, ctx.rhs.p, ctx.step_xd.p);
 }
 

@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <array>
 #include <functional>
 #include <stdexcept>
 #include <string>
@@ -155,9 +156,15 @@ struct Csr {
 struct BoundaryGroup {
     int kind = NLGPU_BC_TEMPERATURE, nen = 2;
     i64 n_edges = 0;
-    double value = 0.0;
+    double value = 0.0;                 // temperature, or the flux of the second-kind integral
+    double heat_transfer = 0.0;         // convection: alpha int N_i N_j in the matrix
+    double emissivity = 0.0;            // radiation: sigma eps T^4 (nonlinear)
     dbuf<int32_t> edges;
     dbuf<double> node_values;   // optional, per listed node
+    dbuf<i64> upper_index;      // [edge][i][j]: entry (row, col >= row) in the upper inner matrix, or -1
+    bool convection() const { return kind == NLGPU_BC_CONVECTION || kind == NLGPU_BC_COMBINED_FLUX; }
+    bool radiation() const { return kind == NLGPU_BC_RADIATION || kind == NLGPU_BC_COMBINED_FLUX; }
+    bool flux_kind() const { return kind != NLGPU_BC_TEMPERATURE; }
 };
 
 // One triangular sweep, level scheduled: rows grouped by level, each level's
@@ -338,6 +345,15 @@ struct Ctx {
     dbuf<uint8_t> is_inner;
     dbuf<double> x_dirichlet, rhs_init, rhs;
     bool bc_ready = false;
+    // stationary_equation_parameters_2d: the radiation loop's stop test, the
+    // Lagrange row's energy (pure Neumann problems) and the initial temperature
+    double nl_tolerance = 1e-8, energy = 0.0;
+    i64 nl_max_iterations = 100;
+    dbuf<double> initial_temperature;
+    bool neumann = false;        // stationary and every group a plain flux: integral condition
+    dbuf<double> node_integral;  // Neumann: int N_i over the node's elements (the Lagrange column)
+    dbuf<double> upper_base;     // radiation: the upper values before the temperature-dependent part
+    dbuf<double> nl_work;        // radiation: K T_prev, the radiation vector, T_prev, partial norms
     // matrices (reference storage) and the solver's full-row copy
     bool symmetric = true;
     Csr inner, bound, local, full;
@@ -399,7 +415,8 @@ void assemble_local(Ctx& ctx, Csr& m, double weight, int integrand);   // integr
 void fill_full_from_upper(Ctx& ctx, const Csr& upper, Csr& full, const dbuf<i64>& map);
 void set_dirichlet_diagonal(Ctx& ctx, Csr& m, double value);
 void combine_nonstationary(Ctx& ctx, double dt);
-void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values);
+// f = dt (flux + source [+ radiation]) + C T_prev, then the first kind
+void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values, const double* radiation = nullptr);
 // solver.cu
 void spmv_full(Ctx& ctx, const Csr& A, const double* x, double* y);
 // tma_plans: also build the TMA-fed shared-memory sweep plans of the exact
@@ -434,6 +451,21 @@ void calc_flux(Ctx& ctx, const double* temperature, double* flux_x, double* flux
 void node_graph(Ctx& ctx, bool local_graph, std::vector<i64>& offsets, std::vector<int32_t>& adjacency);
 std::vector<i64> cuthill_mckee_order(const std::vector<i64>& offsets, const std::vector<int32_t>& adjacency);
 void renumber_mesh(Ctx& ctx, const std::vector<int32_t>& perm);
+// nonlinear.cu: convection and radiation edges, pure Neumann problems
+bool has_convection(const Ctx& ctx);
+bool has_radiation(const Ctx& ctx);
+bool pure_neumann(const Ctx& ctx);
+// entries of the edge node pairs in ctx.inner; throws when an edge touches a temperature node
+void boundary_matrix_index(Ctx& ctx);
+void add_convection(Ctx& ctx);                                  // into ctx.inner.val
+// ctx.inner.val += matrix_factor sigma eps int T^3 N_i N_j, rad += vector_factor sigma eps int T^4 N_i
+void add_radiation(Ctx& ctx, const double* T, double* rad, double matrix_factor, double vector_factor);
+void neumann_integrals(Ctx& ctx);                               // ctx.node_integral
+void subtract3(Ctx& ctx, const double* a, const double* b, const double* d, double* y);
+// x <- prev - x; returns |residual|^2, |x - prev|^2, |x|^2 (deterministic order)
+std::array<double, 3> step_norms(Ctx& ctx, const double* residual, const double* prev, double* x);
+void add_scaled(Ctx& ctx, double a, const double* x, double* y);
+void add_constant(Ctx& ctx, double a, double* y);
 // jacobi.cu: the factor applied by Jacobi sweeps on its two triangles
 void jacobi_build(Ctx& ctx, IncompleteCholesky& ic, const std::vector<i64>& rp, const std::vector<int32_t>& col,
                   const std::vector<i64>& lrp, const std::vector<int32_t>& lcol, const std::vector<i64>& l_to_u);

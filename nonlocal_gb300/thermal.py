@@ -58,12 +58,23 @@ class Model2D:
 
 @dataclass
 class Boundary:
-    """A boundary group: ``kind`` 'temperature' or 'flux', constant value or per-node values."""
+    """A boundary group (thermal_boundary_conditions_2d.hpp:9-98).
+
+    ``kind``: 'temperature' (``value``, or per-node ``node_values``), 'flux'
+    (``value``), 'convection' (``heat_transfer``, ``ambient_temperature``),
+    'radiation' (``emissivity``) or 'combined' (flux ``value`` and all three)."""
 
     edges: np.ndarray
     kind: str = "temperature"
     value: float = 0.0
     node_values: np.ndarray | None = None
+    heat_transfer: float = 0.0
+    ambient_temperature: float = 0.0
+    emissivity: float = 0.0
+
+
+BOUNDARY_KIND = {"temperature": L.BC_TEMPERATURE, "flux": L.BC_FLUX, "convection": L.BC_CONVECTION,
+                 "radiation": L.BC_RADIATION, "combined": L.BC_COMBINED_FLUX}
 
 
 @dataclass
@@ -234,10 +245,29 @@ class Problem2D(Context):
 
     def add_boundary(self, b: Boundary) -> None:
         edges = L.i64(b.edges)
-        nv = None if b.node_values is None else L.f64(b.node_values)
-        kind = L.BC_TEMPERATURE if b.kind == "temperature" else L.BC_FLUX
-        L.check(self._lib.nlgpu_add_boundary_2d(self._h, kind, edges.shape[0], edges.shape[1], L.ptr(edges),
-                                                float(b.value), L.ptr(nv)))
+        kind = BOUNDARY_KIND[b.kind]
+        if kind == L.BC_TEMPERATURE:
+            nv = None if b.node_values is None else L.f64(b.node_values)
+            L.check(self._lib.nlgpu_add_boundary_2d(self._h, kind, edges.shape[0], edges.shape[1], L.ptr(edges),
+                                                    float(b.value), L.ptr(nv)))
+        else:
+            L.check(self._lib.nlgpu_add_flux_boundary_2d(self._h, kind, edges.shape[0], edges.shape[1], L.ptr(edges),
+                                                         float(b.value), float(b.heat_transfer),
+                                                         float(b.ambient_temperature), float(b.emissivity)))
+
+    def set_stationary_parameters(self, tolerance: float = 1e-8, max_iterations: int = 100, energy: float = 0.0,
+                                  initial_temperature=None) -> None:
+        """stationary_equation_parameters_2d: the radiation loop's stop test, int T of a
+        pure Neumann problem, and the loop's initial temperature."""
+        self._t0 = None if initial_temperature is None else L.f64(initial_temperature)
+        L.check(self._lib.nlgpu_set_stationary_parameters(self._h, float(tolerance), int(max_iterations),
+                                                          float(energy), L.ptr(self._t0)))
+
+    def system_rows(self) -> int:
+        """n_nodes, or n_nodes + 1 for a pure Neumann problem (the Lagrange row)."""
+        rows = ctypes.c_int64()
+        L.check(self._lib.nlgpu_get_system_rows(self._h, ctypes.byref(rows)))
+        return int(rows.value)
 
     def clear_boundaries(self) -> None:
         L.check(self._lib.nlgpu_clear_boundaries(self._h))
@@ -299,7 +329,11 @@ class Problem2D(Context):
 
     def matrix(self, which: str = "inner") -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         code = {"inner": L.MATRIX_INNER, "bound": L.MATRIX_BOUND, "local": L.MATRIX_LOCAL}[which]
-        rp = np.empty(self.n_nodes + 1, dtype=np.int64)
+        try:   # a pure Neumann problem's matrices carry the Lagrange row and column
+            rows = self.system_rows()
+        except L.NlgpuError:
+            rows = self.n_nodes   # only the LOCAL part assembled
+        rp = np.empty(rows + 1, dtype=np.int64)
         L.check(self._lib.nlgpu_get_matrix(self._h, code, L.ptr(rp), None, None))
         col = np.empty(int(rp[-1]), dtype=np.int64)
         val = np.empty(int(rp[-1]))
@@ -307,7 +341,8 @@ class Problem2D(Context):
         return rp, col, val
 
     def rhs(self) -> tuple[np.ndarray, np.ndarray]:
-        f, f0 = np.empty(self.n_nodes), np.empty(self.n_nodes)
+        rows = self.system_rows()
+        f, f0 = np.empty(rows), np.empty(rows)
         L.check(self._lib.nlgpu_get_rhs(self._h, L.ptr(f), L.ptr(f0)))
         return f, f0
 

@@ -35,6 +35,8 @@ def lib() -> ctypes.CDLL:
         L.orc_set_conductivity_field.argtypes = [c_p, c_p]
         L.orc_set_capacity.argtypes = [c_p, c_d, c_d]
         L.orc_add_boundary.argtypes = [c_p, c_int, c_i64, c_int, c_p, c_d]
+        L.orc_add_flux_boundary.argtypes = [c_p, c_int, c_i64, c_int, c_p, c_d, c_d, c_d, c_d]
+        L.orc_set_stationary.argtypes = [c_p, c_d, ctypes.c_long, c_d, c_p]
         L.orc_set_source.argtypes = [c_p, c_d]
         L.orc_set_source_field.argtypes = [c_p, c_p]
         L.orc_set_dirichlet_values.argtypes = [c_p, c_p]
@@ -61,8 +63,8 @@ def lib() -> ctypes.CDLL:
     return _lib
 
 
-def _ptr(a: np.ndarray) -> int:
-    return a.ctypes.data
+def _ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
 
 
 class Problem:
@@ -102,7 +104,23 @@ class Problem:
 
     def add_boundary(self, kind: int, edges: np.ndarray, value: float):
         e = np.ascontiguousarray(edges, dtype=np.int64)
+        self._keep.append(e)
         lib().orc_add_boundary(self.h, kind, e.shape[0], e.shape[1], _ptr(e), value)
+
+    def add_flux_boundary(self, kind: int, edges: np.ndarray, flux: float = 0.0, heat_transfer: float = 0.0,
+                          ambient_temperature: float = 0.0, emissivity: float = 0.0):
+        """flux (1), convection (2), radiation (3) or combined (4) group."""
+        e = np.ascontiguousarray(edges, dtype=np.int64)
+        lib().orc_add_flux_boundary(self.h, kind, e.shape[0], e.shape[1], _ptr(e), flux, heat_transfer,
+                                    ambient_temperature, emissivity)
+
+    def set_stationary(self, tolerance: float = 1e-8, max_iterations: int = 100, energy: float = 0.0,
+                       initial: np.ndarray | None = None):
+        """stationary_equation_parameters_2d: the radiation loop and the Neumann energy."""
+        t = None if initial is None else np.ascontiguousarray(initial, dtype=np.float64)
+        if t is not None:
+            self._keep.append(t)
+        lib().orc_set_stationary(self.h, tolerance, max_iterations, energy, _ptr(t))
 
     def set_source(self, value: float):
         lib().orc_set_source(self.h, value)

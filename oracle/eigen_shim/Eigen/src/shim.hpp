@@ -19,8 +19,12 @@
 //   * SimplicialCholesky<..., Upper, NaturalOrdering>: a band LDL^T
 //     factorisation (used by the 1D stationary solver,
 //     libraries/solvers/solver_1d/thermal/stationary_heat_equation_solver_1d.hpp:99-105).
-// Branches the configurations never reach (Eigen::ConjugateGradient,
-// Eigen::BiCGSTAB, Eigen::SparseLU) throw std::logic_error.
+//   * ConjugateGradient<..., Upper> and BiCGSTAB with the diagonal
+//     preconditioner: the textbook iterations (Hestenes & Stiefel 1952; van der
+//     Vorst 1992) with Eigen's documented defaults (used by the nonlinear
+//     boundary and non-symmetric branches of the stationary solver).
+// The branch the configurations never reach (Eigen::SparseLU) throws
+// std::logic_error.
 
 #include <algorithm>
 #include <cassert>
@@ -551,14 +555,71 @@ public:
     }
 };
 
-// Branches of the reference that the parity configurations never reach.
+// Eigen::ConjugateGradient<SparseMatrix, Upper> as documented: the matrix is
+// the self-adjoint view of its upper triangle, default DiagonalPreconditioner
+// (inverse of the diagonal, 1 where it is zero), tolerance = machine epsilon on
+// |r| / |b|, at most 2 n iterations, x0 = 0.  The iteration is the textbook
+// preconditioned conjugate gradient (Hestenes & Stiefel 1952).
 template<class Sparse, int UpLo = Lower>
 struct ConjugateGradient {
-    template<class... A> explicit ConjugateGradient(const A&...) {
-        throw std::logic_error{"Eigen::ConjugateGradient is not part of the oracle build"};
+    using T = typename Sparse::Scalar;
+    using V = Matrix<T, Dynamic, 1>;
+    const Sparse* _a = nullptr;
+    V _inv;
+    T _tol = std::numeric_limits<T>::epsilon();
+    long _max = -1;
+    mutable long _iters = 0;
+    mutable T _error = T{0};
+    explicit ConjugateGradient(const Sparse& a) : _a{&a}, _inv(a.rows()) {
+        static_assert(UpLo == Upper, "only the upper-storage form is used by the reference path");
+        const auto* op = a.outerIndexPtr();
+        const auto* ip = a.innerIndexPtr();
+        const T* vp = a.valuePtr();
+        for (long r = 0; r < a.rows(); ++r) {
+            T d = T{0};
+            for (auto k = op[r]; k < op[r + 1]; ++k)
+                if (long(ip[k]) == r) d = vp[k];
+            _inv[r] = d != T{0} ? T{1} / d : T{1};
+        }
     }
-    template<class V> V solve(const V& b) const { return b; }
-    template<class V> V solveWithGuess(const V& b, const V&) const { return b; }
+    void setTolerance(T t) { _tol = t; }
+    void setMaxIterations(long m) { _max = m; }
+    long iterations() const { return _iters; }
+    T error() const { return _error; }
+    ComputationInfo info() const { return Success; }
+    V solve(const V& b) const { return solveWithGuess(b, V::Zero(b.size())); }
+    V solveWithGuess(const V& b, const V& x0) const {
+        const Sparse& A = *_a;
+        const long n = b.size();
+        const long maxit = _max < 0 ? 2 * n : _max;
+        V x = x0;
+        V r = b - A.template selfadjointView<Upper>() * x;
+        const T bb = b.squaredNorm();
+        _iters = 0;
+        if (bb == T{0}) { _error = T{0}; return x; }
+        const T threshold = std::max(_tol * _tol * bb, std::numeric_limits<T>::min());
+        V z(n), p(n);
+        for (long k = 0; k < n; ++k) p[k] = _inv[k] * r[k];
+        T rz = r.dot(p);
+        T rr = r.squaredNorm();
+        long i = 0;
+        while (rr > threshold && i < maxit) {
+            const V q = A.template selfadjointView<Upper>() * p;
+            const T alpha = rz / p.dot(q);
+            for (long k = 0; k < n; ++k) { x[k] += alpha * p[k]; r[k] -= alpha * q[k]; }
+            rr = r.squaredNorm();
+            ++i;
+            if (rr < threshold) break;
+            for (long k = 0; k < n; ++k) z[k] = _inv[k] * r[k];
+            const T rz_new = r.dot(z);
+            const T beta = rz_new / rz;
+            rz = rz_new;
+            for (long k = 0; k < n; ++k) p[k] = z[k] + beta * p[k];
+        }
+        _iters = i;
+        _error = std::sqrt(rr / bb);
+        return x;
+    }
 };
 // Eigen::BiCGSTAB<SparseMatrix> as documented: default DiagonalPreconditioner
 // (inverse of the diagonal, 1 where it is zero), tolerance = machine epsilon

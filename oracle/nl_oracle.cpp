@@ -39,7 +39,10 @@ using vec2 = std::array<double, 2>;
 enum { ORC_BILINEAR = 2, ORC_SERENDIPITY = 3 };   // element_2d_t numbering (elements_set.hpp:231-237)
 enum { INF_CONSTANT = 0, INF_POLYNOMIAL = 1, INF_EXPONENTIAL = 2, INF_FAST_POLYNOMIAL = 3 };
 enum { COND_ISO = 0, COND_ORTHO = 1, COND_ANISO = 2 };
-enum { BC_TEMPERATURE = 0, BC_FLUX = 1 };
+// temperature_2d, flux_2d, convection_2d, radiation_2d, combined_flux_2d
+// (thermal_boundary_conditions_2d.hpp:9-98)
+enum { BC_TEMPERATURE = 0, BC_FLUX = 1, BC_CONVECTION = 2, BC_RADIATION = 3, BC_COMBINED = 4 };
+constexpr double STEFAN_BOLTZMANN = 5.67036713e-8;   // metamath/utils/constants.hpp:12
 
 // ------------------------------------------------------------------ elements
 // Gauss nodes/weights: gaussian_quadrature.hpp:22-40.
@@ -166,7 +169,13 @@ struct Csr {
     }
 };
 
-struct Boundary { int kind; int nen; std::vector<i64> edges; double value; std::vector<double> node_values; };
+// value: the temperature, or the second-kind flux (operator() of the condition)
+struct Boundary {
+    int kind; int nen; std::vector<i64> edges; double value; std::vector<double> node_values;
+    double heat_transfer = 0.0, emissivity = 0.0;
+    bool convection() const { return kind == BC_CONVECTION || kind == BC_COMBINED; }
+    bool radiation() const { return kind == BC_RADIATION || kind == BC_COMBINED; }
+};
 
 struct Problem {
     Element2d el;
@@ -200,6 +209,10 @@ struct Problem {
     long iterations = 0; double residual = 0, true_residual = 0, ilt_shift = 0; int ilt_ok = 0, ilt_attempts = 0;
     std::vector<i64> L_colptr, L_rowidx; std::vector<double> L_val, L_scale;
     std::vector<double> history;
+    // stationary_equation_parameters_2d (stationary_heat_equation_solver_2d.hpp:19-26)
+    double nl_tolerance = 1e-8, energy = 0.0;
+    long nl_max_iterations = 100, nonlinear_iterations = 0;
+    std::vector<double> initial;
     std::map<std::string, double> timings;
 };
 
@@ -487,7 +500,7 @@ void boundary_vectors(Problem& p) {
             for (const i64 v : b.edges) p.is_inner[size_t(v)] = 0;
     p.rhs_init.assign(size_t(n), 0.0);
     for (const Boundary& b : p.bnds) {
-        if (b.kind != BC_FLUX) continue;
+        if (b.kind == BC_TEMPERATURE) continue;
         const Element1d el = make_element1d(b.nen);
         const i64 ne = i64(b.edges.size()) / b.nen;
         for (i64 e = 0; e < ne; ++e)
@@ -535,6 +548,123 @@ void apply_first_kind(const Problem& p, const Csr& bound, std::vector<double>& f
         f[size_t(r)] -= s;
     }
     for (i64 r = 0; r < p.n_nodes; ++r) if (!p.is_inner[size_t(r)]) f[size_t(r)] = p.x_dirichlet[size_t(r)];
+}
+
+// |J| of boundary edge e of group b at its quadrature point q (element_1d_data::jacobi_matrix)
+double edge_jacobian(const Problem& p, const Boundary& b, const Element1d& el, i64 e, int q) {
+    double J0 = 0, J1 = 0;
+    for (int k = 0; k < b.nen; ++k) {
+        const double* x = &p.nodes[size_t(b.edges[size_t(e * b.nen + k)] * 2)];
+        J0 += x[0] * el.qNxi[size_t(k * el.nq + q)]; J1 += x[1] * el.qNxi[size_t(k * el.nq + q)];
+    }
+    return std::sqrt(J0 * J0 + J1 * J1);
+}
+
+// the stored entry (row, col) of A (sorted rows), or -1
+i64 find_entry(const Csr& A, i64 row, i64 col) {
+    for (i64 k = A.rowptr[size_t(row)]; k < A.rowptr[size_t(row) + 1]; ++k)
+        if (A.col[size_t(k)] == col) return k;
+    return -1;
+}
+
+// run_by_boundaries over the edges of every group of one kind (solvers_utils.hpp:11-29):
+// f(group, edge, i, row) for each local node i of each edge
+template<class Pred, class F>
+void for_boundary_rows(const Problem& p, Pred pred, F&& f) {
+    for (const Boundary& b : p.bnds) {
+        if (!pred(b)) continue;
+        const i64 ne = i64(b.edges.size()) / b.nen;
+        for (i64 e = 0; e < ne; ++e)
+            for (int i = 0; i < b.nen; ++i) f(b, e, i, b.edges[size_t(e * b.nen + i)]);
+    }
+}
+
+// convection_condition_2d (convection_condition_2d.hpp:11-31): alpha int N_i N_j |J|
+// into the entries (row, col >= row); rows of temperature nodes are skipped (the
+// reference resets them afterwards)
+void convection_condition(const Problem& p, Csr& K) {
+    for_boundary_rows(p, [](const Boundary& b) { return b.convection(); },
+        [&](const Boundary& b, i64 e, int i, i64 row) {
+            if (!p.is_inner[size_t(row)]) return;
+            const Element1d el = make_element1d(b.nen);
+            for (int j = 0; j < b.nen; ++j) {
+                const i64 col = b.edges[size_t(e * b.nen + j)];
+                if (col < row || !p.is_inner[size_t(col)]) continue;
+                double integral = 0.0;
+                for (int q = 0; q < el.nq; ++q)
+                    integral += el.w[size_t(q)] * el.qN[size_t(i * el.nq + q)] * el.qN[size_t(j * el.nq + q)] *
+                                edge_jacobian(p, b, el, e, q);
+                const i64 k = find_entry(K, row, col);
+                if (k >= 0) K.val[size_t(k)] += b.heat_transfer * integral;
+            }
+        });
+}
+
+// radiation_condition_2d, stationary overload (radiation_condition_2d.hpp:91-135):
+// K(row, col >= row) -= 4 sigma eps int T^3 N_i N_j |J|, r[row] -= sigma eps int T^4 N_i |J|
+// with T the previous temperature at the edge's quadrature points
+void radiation_condition(const Problem& p, Csr& K, std::vector<double>& r, const std::vector<double>& T) {
+    for_boundary_rows(p, [](const Boundary& b) { return b.radiation(); },
+        [&](const Boundary& b, i64 e, int i, i64 row) {
+            if (!p.is_inner[size_t(row)]) return;
+            const Element1d el = make_element1d(b.nen);
+            auto tq = [&](int q) {
+                double s = 0.0;
+                for (int k = 0; k < b.nen; ++k) s += el.qN[size_t(k * el.nq + q)] * T[size_t(b.edges[size_t(e * b.nen + k)])];
+                return s;
+            };
+            for (int j = 0; j < b.nen; ++j) {
+                const i64 col = b.edges[size_t(e * b.nen + j)];
+                if (col < row || !p.is_inner[size_t(col)]) continue;
+                double integral = 0.0;
+                for (int q = 0; q < el.nq; ++q)
+                    integral += el.w[size_t(q)] * std::pow(tq(q), 3) * el.qN[size_t(i * el.nq + q)] *
+                                el.qN[size_t(j * el.nq + q)] * edge_jacobian(p, b, el, e, q);
+                const i64 k = find_entry(K, row, col);
+                if (k >= 0) K.val[size_t(k)] -= 4.0 * STEFAN_BOLTZMANN * b.emissivity * integral;
+            }
+            double integral = 0.0;
+            for (int q = 0; q < el.nq; ++q)
+                integral += el.w[size_t(q)] * el.qN[size_t(i * el.nq + q)] * std::pow(tq(q), 4) * edge_jacobian(p, b, el, e, q);
+            r[size_t(row)] -= STEFAN_BOLTZMANN * b.emissivity * integral;
+        });
+}
+
+bool pure_neumann(const Problem& p) {   // init_problem_settings.hpp:18-21,43
+    for (const Boundary& b : p.bnds) if (b.kind != BC_FLUX) return false;
+    return true;
+}
+bool nonlinear_boundary(const Problem& p) {
+    for (const Boundary& b : p.bnds) if (b.radiation()) return true;
+    return false;
+}
+
+// The bordered matrix of a pure Neumann problem (conductivity_matrix_2d.hpp:39-104):
+// each row ends with the column n holding int N_i over the node's elements
+// (integral_condition), and row n holds its zero diagonal.
+Csr bordered(const Problem& p, const Csr& A) {
+    const i64 n = A.rows;
+    Csr B;
+    B.rows = B.cols = n + 1;
+    B.rowptr.assign(size_t(n) + 2, 0);
+    for (i64 r = 0; r < n; ++r) {
+        for (i64 k = A.rowptr[size_t(r)]; k < A.rowptr[size_t(r) + 1]; ++k) {
+            B.col.push_back(A.col[size_t(k)]); B.val.push_back(A.val[size_t(k)]);
+        }
+        double integral = 0.0;
+        for (const i64 e : p.node_elements[size_t(r)]) {
+            int i = 0;
+            while (node_of(p, e, i) != r) ++i;
+            double s = 0.0;
+            for (int q = 0; q < p.el.nq; ++q) s += p.el.w[size_t(q)] * p.el.qN[size_t(i * p.el.nq + q)] * p.jac[size_t(e * p.el.nq + q)];
+            integral += s;
+        }
+        B.col.push_back(n); B.val.push_back(integral);
+        B.rowptr[size_t(r) + 1] = i64(B.col.size());
+    }
+    B.col.push_back(n); B.val.push_back(0.0);
+    B.rowptr[size_t(n) + 1] = i64(B.col.size());
+    return B;
 }
 
 // Symmetric product from upper storage, first stored entry of a row being the
@@ -717,6 +847,26 @@ void orc_add_boundary(void* h, int kind, i64 n_edges, int nen, const i64* edges,
     p.bnds.push_back({kind, nen, std::vector<i64>(edges, edges + n_edges * nen), value, {}});
 }
 
+// flux-type groups: the second-kind flux is operator() of the condition
+// (flux q, convection alpha T_a, radiation 0, combined q + alpha T_a)
+void orc_add_flux_boundary(void* h, int kind, i64 n_edges, int nen, const i64* edges, double flux,
+                           double heat_transfer, double ambient, double emissivity) {
+    auto& p = *static_cast<Problem*>(h);
+    Boundary b{kind, nen, std::vector<i64>(edges, edges + n_edges * nen), 0.0, {}};
+    b.value = kind == BC_FLUX ? flux : kind == BC_CONVECTION ? heat_transfer * ambient :
+              kind == BC_COMBINED ? flux + heat_transfer * ambient : 0.0;
+    b.heat_transfer = (kind == BC_CONVECTION || kind == BC_COMBINED) ? heat_transfer : 0.0;
+    b.emissivity = (kind == BC_RADIATION || kind == BC_COMBINED) ? emissivity : 0.0;
+    p.bnds.push_back(std::move(b));
+}
+
+void orc_set_stationary(void* h, double tolerance, long max_iterations, double energy, const double* initial) {
+    auto& p = *static_cast<Problem*>(h);
+    p.nl_tolerance = tolerance; p.nl_max_iterations = max_iterations; p.energy = energy;
+    if (initial) p.initial.assign(initial, initial + p.n_nodes);
+    else p.initial.clear();
+}
+
 void orc_set_source(void* h, double value) { static_cast<Problem*>(h)->source = value; }
 
 void orc_set_source_field(void* h, const double* values) {   // [e][q]
@@ -745,6 +895,7 @@ void orc_assemble_stationary(void* h) {
     boundary_vectors(p);
     const double t0 = now();
     assemble(p, false, p.symmetric, p.K_inner, p.K_bound, integrate_local, p.p1, 1.0 - p.p1);
+    convection_condition(p, p.K_inner);   // stationary_heat_equation_solver_2d.hpp:76
     p.timings["assembly"] = now() - t0;
     p.rhs = p.rhs_init;
     apply_first_kind(p, p.K_bound, p.rhs);
@@ -761,8 +912,79 @@ void orc_assemble_local(void* h) {
 
 // ILLT-preconditioned CG (stationary_heat_equation_solver_2d.hpp:94-102).
 // variant 0: Eigen-style Lin-More ICF (reference); 1: fixed-pattern IC(0); 2: identity.
+// Pure Neumann problems (stationary_heat_equation_solver_2d.hpp:29-44, 52-103 with
+// is_neumann): the flux balance check, then CG with the ILLT of the bordered
+// local matrix on the bordered system [K b; b^T 0] [T; lambda] = [f; energy].
+// Returns -2 for an unbalanced problem.
+static int solve_neumann(Problem& p, double tol, long maxit, bool stop_true_residual) {
+    double s = 0.0;
+    for (const double v : p.rhs) s += v;
+    if (std::abs(s) > 1e-10) return -2;
+    const Csr K = bordered(p, p.K_inner), Kl = bordered(p, p.K_local);
+    std::vector<double> f = p.rhs, x;
+    f.push_back(p.energy);
+    const auto E = to_eigen(Kl);
+    Eigen::IncompleteCholesky<double, Eigen::Upper, Eigen::NaturalOrdering<i64>> ilt(E);
+    p.ilt_ok = ilt.info() == Eigen::Success;
+    if (p.ilt_ok)
+        cg(p, K, f, x, [&](const std::vector<double>& r, std::vector<double>& z) {
+            Eigen::Matrix<double, Eigen::Dynamic, 1> rr(long(r.size()));
+            std::copy(r.begin(), r.end(), rr.data());
+            const auto zz = ilt.solve(rr);
+            z.assign(zz.begin(), zz.end());
+        }, tol, maxit, stop_true_residual);
+    else
+        cg(p, K, f, x, [](const std::vector<double>& r, std::vector<double>& z) { z = r; }, tol, maxit, stop_true_residual);
+    p.solution.assign(x.begin(), x.begin() + p.n_nodes);
+    return p.ilt_ok;
+}
+
+// The radiation loop (stationary_heat_equation_solver_2d.hpp:66-116): from the
+// initial temperature, K_T dT = K T_prev - r_rad - f with K_T = K - 4 sigma eps
+// int T^3 N_i N_j, solved by CG with the diagonal preconditioner to machine
+// precision (Eigen::ConjugateGradient's defaults), T = T_prev - dT, until
+// max_iterations or until |T - T_prev| / |T| or |residual| is at most the tolerance.
+static int solve_radiation(Problem& p) {
+    const size_t n = size_t(p.n_nodes);
+    std::vector<double> curr = p.initial.empty() ? std::vector<double>(n, 0.0) : p.initial, prev = curr;
+    double difference = 1.0, norm = 1.0;
+    long it = 0;
+    while (it < p.nl_max_iterations && p.nl_tolerance < difference && p.nl_tolerance < norm) {
+        std::swap(curr, prev);
+        Csr K = p.K_inner;
+        std::vector<double> residual, rad(n, 0.0), dx;
+        sym_spmv(K, prev, residual);
+        radiation_condition(p, K, rad, prev);
+        for (size_t i = 0; i < n; ++i) residual[i] -= rad[i] + p.rhs[i];
+        std::vector<double> inv(n);
+        for (size_t r = 0; r < n; ++r) {
+            const double d = K.val[size_t(K.rowptr[r])];
+            inv[r] = d != 0.0 ? 1.0 / d : 1.0;
+        }
+        cg(p, K, residual, dx, [&](const std::vector<double>& r, std::vector<double>& z) {
+            z.resize(r.size());
+            for (size_t i = 0; i < r.size(); ++i) z[i] = inv[i] * r[i];
+        }, std::numeric_limits<double>::epsilon(), long(2 * n), true);
+        double rr = 0.0, dd = 0.0, tt = 0.0;
+        for (size_t i = 0; i < n; ++i) {
+            curr[i] = prev[i] - dx[i];
+            rr += residual[i] * residual[i];
+            dd += (curr[i] - prev[i]) * (curr[i] - prev[i]);
+            tt += curr[i] * curr[i];
+        }
+        ++it;
+        norm = std::sqrt(rr);
+        difference = std::sqrt(dd) / (tt != 0.0 ? std::sqrt(tt) : 1.0);
+    }
+    p.nonlinear_iterations = it;
+    p.solution = curr;
+    return 1;
+}
+
 int orc_solve(void* h, int variant, double tol, long maxit, int stop_true_residual) {
     auto& p = *static_cast<Problem*>(h);
+    if (nonlinear_boundary(p)) return solve_radiation(p);
+    if (pure_neumann(p)) return solve_neumann(p, tol, maxit, stop_true_residual);
     double t0 = now();
     std::vector<double> x;
     if (variant == 0) {
@@ -1082,6 +1304,7 @@ double orc_scalar(void* h, const char* name) {
     if (s == "ilt_attempts") return p.ilt_attempts;
     if (s == "ilt_shift") return p.ilt_shift;
     if (s == "threads") return omp_get_max_threads();
+    if (s == "nonlinear_iterations") return double(p.nonlinear_iterations);
     const auto it = p.timings.find(s);
     return it == p.timings.end() ? -1.0 : it->second;
 }

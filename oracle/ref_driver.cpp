@@ -125,7 +125,9 @@ struct manufactured {
     }
 };
 
-// bc.<group>=temperature:<v> | flux:<v> | temperature:manufactured
+// bc.<group>=temperature:<v> | flux:<v> | temperature:manufactured |
+//            convection:<heat transfer>,<ambient T> | radiation:<emissivity> |
+//            combined:<flux>,<heat transfer>,<ambient T>,<emissivity>
 nonlocal::solver_2d::thermal::thermal_boundaries_conditions_2d<T> make_bcs_2d() {
     using namespace nonlocal::solver_2d::thermal;
     thermal_boundaries_conditions_2d<T> bcs;
@@ -138,9 +140,14 @@ nonlocal::solver_2d::thermal::thermal_boundaries_conditions_2d<T> make_bcs_2d() 
             bcs[group] = std::make_unique<temperature_2d<T>>([](const std::array<T, 2>& x) { return manufactured::solution(x); });
             continue;
         }
-        const T value = std::stod(v.substr(colon + 1));
-        if (kind == "temperature") bcs[group] = std::make_unique<temperature_2d<T>>(value);
-        else if (kind == "flux") bcs[group] = std::make_unique<flux_2d<T>>(value);
+        std::vector<T> a;
+        std::stringstream s{v.substr(colon + 1)};
+        for (std::string tok; std::getline(s, tok, ',');) a.push_back(std::stod(tok));
+        if (kind == "temperature") bcs[group] = std::make_unique<temperature_2d<T>>(a.at(0));
+        else if (kind == "flux") bcs[group] = std::make_unique<flux_2d<T>>(a.at(0));
+        else if (kind == "convection") bcs[group] = std::make_unique<convection_2d<T>>(a.at(0), a.at(1));
+        else if (kind == "radiation") bcs[group] = std::make_unique<radiation_2d<T>>(a.at(0));
+        else if (kind == "combined") bcs[group] = std::make_unique<combined_flux_2d<T>>(a.at(0), a.at(1), a.at(2), a.at(3));
         else throw std::domain_error{"unknown bc " + kind};
     }
     return bcs;
@@ -279,6 +286,7 @@ int stationary2d() {
     }
     const auto bcs = make_bcs_2d();
     stationary_equation_parameters_2d<T> aux;
+    aux.energy = getd("energy", 0.0);   // the Lagrange row's right-hand side (pure Neumann problems)
     if (get("source") == "manufactured") {
         aux.right_part = [](const std::array<T, 2>& x) { return manufactured::source(x); };
         std::vector<double> sq, exact;
@@ -308,16 +316,34 @@ int stationary2d() {
     t0 = std::chrono::steady_clock::now();
     conductivity_matrix_2d<T, I, J> conductivity{mesh};
     conductivity.compute(conductivity_parameters, settings.is_inner_nodes, settings.is_symmetric(), settings.is_neumann);
+    convection_condition_2d(conductivity.matrix().inner(), *mesh, bcs);   // a no-op without convection groups
     dumps("t_assembly", seconds_since(t0));
-    Eigen::Matrix<T, Eigen::Dynamic, 1> temperature_prev = Eigen::Matrix<T, Eigen::Dynamic, 1>::Zero(mesh->container().nodes_count());
+    const size_t rows = mesh->container().nodes_count() + settings.is_neumann;
+    Eigen::Matrix<T, Eigen::Dynamic, 1> temperature_prev = Eigen::Matrix<T, Eigen::Dynamic, 1>::Zero(rows);
     Eigen::Matrix<T, Eigen::Dynamic, 1> residual = conductivity.matrix().inner().template selfadjointView<Eigen::Upper>() * temperature_prev;
-    Eigen::Matrix<T, Eigen::Dynamic, 1> residual_rad = Eigen::Matrix<T, Eigen::Dynamic, 1>::Zero(mesh->container().nodes_count());
-    first_kind_matrix_fill_2d(conductivity.matrix().inner(), residual_rad, *mesh, bcs);
-    boundary_condition_first_kind_2d(f, *mesh, bcs, conductivity.matrix().bound());
+    Eigen::Matrix<T, Eigen::Dynamic, 1> residual_rad = Eigen::Matrix<T, Eigen::Dynamic, 1>::Zero(rows);
+    if (!settings.is_neumann) {
+        first_kind_matrix_fill_2d(conductivity.matrix().inner(), residual_rad, *mesh, bcs);
+        boundary_condition_first_kind_2d(f, *mesh, bcs, conductivity.matrix().bound());
+    }
     dump_csr("K_inner", conductivity.matrix().inner());
     dump_csr("K_bound", conductivity.matrix().bound());
     dumpv("rhs", std::vector<double>(f.begin(), f.end()));
     residual -= residual_rad + f;
+    if (settings.is_nonlinear_boundary) {
+        // radiation: the reference's own fixed-point loop
+        // (stationary_heat_equation_solver_2d.hpp:66-116, Eigen::ConjugateGradient per step)
+        stationary_equation_parameters_2d<T> nl = aux;
+        nl.tolerance = getd("nonlinear_tolerance", nl.tolerance);
+        nl.max_iterations = size_t(getd("nonlinear_max_iterations", double(nl.max_iterations)));
+        t0 = std::chrono::steady_clock::now();
+        auto solution = stationary_heat_equation_solver_2d<J>(mesh, parameters, bcs, nl);
+        dumps("t_cg", seconds_since(t0));
+        dumpv("temperature", solution.temperature());
+        dumpv("flux_x", solution.flux()[0]);
+        dumpv("flux_y", solution.flux()[1]);
+        return 0;
+    }
     if (!settings.is_symmetric()) {
         // stationary_heat_equation_solver_2d.hpp:105-108: full storage, Eigen::BiCGSTAB
         std::vector<double> lq;

@@ -85,6 +85,29 @@ CASES = {
     "b6_groups_local": ({"nx": 6, "ny": 6, "element": BILINEAR, "groups_2d": {"inclusion": list(range(7, 21))}},
                         {"mode": "stationary2d", "local_weight": 1, "conductivity": "1", "bc.left": "temperature:0",
                          "bc.right": "flux:1", "tolerance": 1e-14}),
+    # convection on the right side (convection_condition_2d + the flux alpha T_a), linear
+    "b10_convection": ({"nx": 10, "ny": 10, "element": BILINEAR},
+                       {"mode": "stationary2d", "influence": "fast_polynomial", "radius": 0.25, "local_weight": 0.5,
+                        "conductivity": "1", "bc.left": "temperature:0", "bc.right": "convection:2,1",
+                        "tolerance": 1e-14}),
+    # radiation on the right side: the reference's own fixed-point loop (17 steps to 1e-8)
+    "b10_radiation": ({"nx": 10, "ny": 10, "element": BILINEAR},
+                      {"mode": "stationary2d", "influence": "fast_polynomial", "radius": 0.25, "local_weight": 0.5,
+                       "conductivity": "20", "bc.left": "temperature:300", "bc.right": "radiation:0.5",
+                       "tolerance": 1e-14}),
+    # flux, convection and radiation on one side (combined_flux_2d), serendipity, constant kernel
+    "s5_combined": ({"nx": 5, "ny": 5, "element": SERENDIPITY, "jitter": 0.1, "seed": 4},
+                    {"mode": "stationary2d", "influence": "constant", "n": 2, "radius": 0.35, "local_weight": 0.6,
+                     "conductivity": "20", "bc.left": "temperature:300", "bc.right": "combined:-100,2,280,0.3",
+                     "tolerance": 1e-14}),
+    # pure Neumann problems: the Lagrange row int T = energy (conductivity_matrix_2d.hpp:83-104)
+    "b8_neumann": ({"nx": 8, "ny": 8, "element": BILINEAR},
+                   {"mode": "stationary2d", "influence": "fast_polynomial", "radius": 0.3, "local_weight": 0.5,
+                    "conductivity": "1", "bc.left": "flux:-1", "bc.right": "flux:1", "energy": 0.5,
+                    "tolerance": 1e-14}),
+    "s5_neumann_local": ({"nx": 5, "ny": 5, "element": SERENDIPITY, "jitter": 0.1, "seed": 4},
+                         {"mode": "stationary2d", "local_weight": 1, "conductivity": "2,1", "bc.up": "flux:2",
+                          "bc.down": "flux:-2", "tolerance": 1e-14}),
     # nonstationary 2D: left T = sin(10 t), identity-preconditioned CG per step
     "b8_nonstationary": ({"nx": 8, "ny": 8, "element": BILINEAR},
                          {"mode": "nonstationary2d", "influence": "fast_polynomial", "radius": 0.3,

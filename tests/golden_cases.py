@@ -13,7 +13,8 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 STATIONARY_2D = ["b12_fastpoly", "s6_exp_ortho_jitter", "b10_poly_no_aniso", "s5_const",
                  "ref_square16_manufactured", "ref_solid_ring",
-                 "b12_shuffled_cm", "s5_shuffled_cm", "b6_groups_local"]
+                 "b12_shuffled_cm", "s5_shuffled_cm", "b6_groups_local",
+                 "b10_convection", "b10_radiation", "s5_combined", "b8_neumann", "s5_neumann_local"]
 NONLOCAL_2D = ["b12_fastpoly", "s6_exp_ortho_jitter", "b10_poly_no_aniso", "s5_const"]
 # every fixture made from an SU2 file (its text is stored as su2_text)
 SU2_CASES = STATIONARY_2D + ["b10_field_nonsym", "b8_nonstationary"]
@@ -34,6 +35,32 @@ def mesh_before_renumbering(fx: dict) -> tuple[np.ndarray, np.ndarray]:
     return fx["nodes_before_renumbering"], inverse[fx["elements"]]
 
 
+def lagrange_column(fx: dict) -> np.ndarray:
+    """int N_i over the elements of each node (conductivity_matrix_2d.hpp:75-104), from
+    the fixture's basis tables and Jacobians."""
+    nen = fx["elements"].shape[1]
+    qN = fx["basis_qN"].reshape(nen, -1)
+    per = (fx["basis_weights"][None, None, :] * qN[None, :, :] * fx["jacobians"][:, None, :]).sum(axis=2)
+    b = np.zeros(fx["nodes"].shape[0])
+    np.add.at(b, fx["elements"], per)
+    return b
+
+
+def bordered(rp, col, val, b):
+    """A pure Neumann problem's matrix as the reference stores it: every row ends with
+    the Lagrange column n (b_i), row n holds a zero diagonal."""
+    n = rp.shape[0] - 1
+    rows_c = [np.append(col[rp[r]:rp[r + 1]], n) for r in range(n)] + [np.array([n])]
+    rows_v = [np.append(val[rp[r]:rp[r + 1]], b[r]) for r in range(n)] + [np.array([0.0])]
+    new_rp = np.concatenate([[0], np.cumsum([len(c) for c in rows_c])]).astype(np.int64)
+    return new_rp, np.concatenate(rows_c).astype(np.int64), np.concatenate(rows_v)
+
+
+def neumann(fx: dict) -> bool:
+    """The fixture is a pure Neumann problem (its matrices carry the Lagrange row)."""
+    return fx["K_inner_rowptr"].shape[0] == fx["nodes"].shape[0] + 2
+
+
 def write_su2_text(fx: dict, path: str) -> str:
     """Writes the exact SU2 file the reference parsed for this fixture."""
     with open(path, "wb") as f:
@@ -47,6 +74,10 @@ def load(name: str) -> dict:
     with np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False) as z:
         data = {k: z[k] for k in z.files}
     data["config"] = json.loads(str(data["config"]))
+    if "temperature" in data and "nodes" in data and data["temperature"].shape[0] == data["nodes"].shape[0] + 1:
+        # a pure Neumann problem's solution ends with the Lagrange multiplier
+        data["lagrange_multiplier"] = data["temperature"][-1:]
+        data["temperature"] = data["temperature"][:-1]
     return data
 
 
@@ -70,17 +101,42 @@ def model(cfg: dict) -> dict:
                 cond_kind=kind, cond=cond)
 
 
-def boundaries(fx: dict) -> list[tuple[int, np.ndarray, float]]:
-    """(kind, edges, value) for each boundary group with a condition; kind 0 temperature, 1 flux."""
+BOUNDARY_KINDS = {"temperature": 0, "flux": 1, "convection": 2, "radiation": 3, "combined": 4}
+
+
+def boundary_specs(fx: dict) -> list[dict]:
+    """Each boundary group with a condition, as the fixture's configuration gives it
+    (temperature:v | flux:q | convection:alpha,T_a | radiation:eps | combined:q,alpha,T_a,eps)."""
     out = []
     for key, spec in fx["config"].items():
         if not key.startswith("bc."):
             continue
         group = key[3:]
-        kind, value = spec.split(":")
-        val = 0.0 if value == "manufactured" else float(value)
-        out.append((0 if kind == "temperature" else 1, fx["bnd_" + group], val))
+        kind, args = spec.split(":")
+        a = [0.0] if args == "manufactured" else [float(v) for v in args.split(",")]
+        d = {"kind": kind, "edges": fx["bnd_" + group], "value": 0.0, "heat_transfer": 0.0,
+             "ambient_temperature": 0.0, "emissivity": 0.0}
+        if kind in ("temperature", "flux"):
+            d["value"] = a[0]
+        elif kind == "convection":
+            d["heat_transfer"], d["ambient_temperature"] = a
+        elif kind == "radiation":
+            d["emissivity"] = a[0]
+        else:
+            d["value"], d["heat_transfer"], d["ambient_temperature"], d["emissivity"] = a
+        out.append(d)
     return out
+
+
+def boundaries(fx: dict) -> list[tuple[int, np.ndarray, float]]:
+    """(kind, edges, value) for each temperature (0) or flux (1) group."""
+    return [(BOUNDARY_KINDS[d["kind"]], d["edges"], d["value"]) for d in boundary_specs(fx)]
+
+
+def stationary_parameters(cfg: dict) -> dict:
+    """stationary_equation_parameters_2d of a fixture (defaults 1e-8, 100, 0)."""
+    return {"tolerance": float(cfg.get("nonlinear_tolerance", 1e-8)),
+            "max_iterations": int(cfg.get("nonlinear_max_iterations", 100)), "energy": float(cfg.get("energy", 0.0))}
 
 
 def oracle_problem(fx: dict):
@@ -89,8 +145,14 @@ def oracle_problem(fx: dict):
     cfg = fx["config"]
     prob = oracle.Problem(element_type(fx), fx["nodes"], fx["elements"])
     prob.set_model(**model(cfg))
-    for kind, edges, value in boundaries(fx):
-        prob.add_boundary(kind, edges, value)
+    for d in boundary_specs(fx):
+        if d["kind"] == "temperature":
+            prob.add_boundary(0, d["edges"], d["value"])
+        else:
+            prob.add_flux_boundary(BOUNDARY_KINDS[d["kind"]], d["edges"], d["value"], d["heat_transfer"],
+                                   d["ambient_temperature"], d["emissivity"])
+    p = stationary_parameters(cfg)
+    prob.set_stationary(p["tolerance"], p["max_iterations"], p["energy"])
     if cfg.get("source") == "manufactured":
         prob.set_source_field(fx["source_q"].reshape(-1))
     elif "source" in cfg:

@@ -42,8 +42,9 @@ def gpu_problem(fx):
     pb.set_model(T.Model2D(influence={v: k for k, v in gc.INFLUENCE.items()}[m["influence"]], radius=m["radius"],
                            local_weight=m["local_weight"], n=m["n"], p=m["p"], q=m["q"],
                            conductivity=cond[:kind + 1]))
-    for kind_, edges, value in gc.boundaries(fx):
-        pb.add_boundary(T.Boundary(edges=edges, kind="temperature" if kind_ == 0 else "flux", value=value))
+    for d in gc.boundary_specs(fx):
+        pb.add_boundary(T.Boundary(**d))
+    pb.set_stationary_parameters(**gc.stationary_parameters(cfg))
     if cfg.get("source") == "manufactured":
         pb.set_source(0.0, fx["source_q"])
     elif "source" in cfg:
@@ -101,8 +102,9 @@ def test_matrices_and_rhs(golden):
     f, f0 = pb.rhs()
     for got, key in [(f0, "rhs_init"), (f, "rhs")]:
         np.testing.assert_allclose(got, fx[key], rtol=MATRIX_RTOL, atol=MATRIX_RTOL * max(np.abs(fx[key]).max(), 1.0))
-    pb.conductivity_matrix("LOCAL")
-    assert_csr_equal(pb.matrix("local"), fx, "K_local")
+    if "K_local_rowptr" in fx:   # the radiation branch assembles no separate local matrix
+        pb.conductivity_matrix("LOCAL")
+        assert_csr_equal(pb.matrix("local"), fx, "K_local")
 
 
 def test_float_float_assembly_matrices(golden):
@@ -453,7 +455,84 @@ def test_operator_annihilates_constants_full_size(lib):
     pb.conductivity_matrix("FULL")
     rp, col, val = pb.matrix("inner")
     n = pb.n_nodes
-    rows = np.repeat(np.arange(n), np.diff(rp))
+    # no boundary conditions: a pure Neumann problem, copied out with the Lagrange
+    # row and column (int N_i, which sum to the area); drop them
+    assert rp.shape[0] == n + 2 and rp[-1] - rp[-2] == 1
+    lagrange = col == n
+    assert abs(val[lagrange].sum() - 1.0) < 1e-12
+    rows = np.repeat(np.arange(n + 1), np.diff(rp))
+    keep = ~lagrange
+    rows, col, val = rows[keep], col[keep], val[keep]
     off_diag = col != rows
     sums = np.bincount(rows, weights=val, minlength=n) + np.bincount(col[off_diag], weights=val[off_diag], minlength=n)
     assert np.abs(sums).max() < 1e-12 * np.abs(val).max() * 50
+
+
+@pytest.mark.parametrize("case", ["radiation", "convection", "neumann"])
+def test_boundary_kinds_against_oracle_scaled(lib, case):
+    """Convection, the radiation loop and pure Neumann problems on a 30 x 30 mesh,
+    against the oracle (which solves the Neumann problem as the reference does, on
+    the bordered system, and the radiation steps with Jacobi-preconditioned CG)."""
+    import oracle
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    m = structured_quad_mesh(30, 30, "bilinear", jitter=0.1, seed=9)
+    radius, p1 = 0.1, 0.5
+    specs = {"radiation": [("left", dict(kind="temperature", value=300.0)),
+                           ("right", dict(kind="combined", value=-50.0, heat_transfer=1.5, ambient_temperature=280.0,
+                                          emissivity=0.4))],
+             "convection": [("left", dict(kind="temperature", value=0.0)),
+                            ("right", dict(kind="convection", heat_transfer=3.0, ambient_temperature=1.0))],
+             "neumann": [("left", dict(kind="flux", value=-2.0)), ("right", dict(kind="flux", value=2.0))]}[case]
+    energy = 0.25 if case == "neumann" else 0.0
+    pb = T.Problem2D.from_mesh(m)
+    pb.set_model(T.Model2D(influence="fast_polynomial", radius=(radius, radius), local_weight=p1, conductivity=(20.0,)))
+    prob = oracle.Problem(2, m.nodes, m.elements)
+    prob.set_model(influence=3, radius=(radius, radius), local_weight=p1, cond_kind=0, cond=(20.0, 0.0, 0.0))
+    for group, d in specs:
+        pb.add_boundary(T.Boundary(edges=m.boundaries[group], **d))
+        if d["kind"] == "temperature":
+            prob.add_boundary(0, m.boundaries[group], d["value"])
+        else:
+            prob.add_flux_boundary(gc.BOUNDARY_KINDS[d["kind"]], m.boundaries[group], d.get("value", 0.0),
+                                   d.get("heat_transfer", 0.0), d.get("ambient_temperature", 0.0),
+                                   d.get("emissivity", 0.0))
+    pb.set_stationary_parameters(energy=energy)
+    prob.set_stationary(energy=energy)
+    pb.find_neighbours()
+    prob.find_neighbours()
+    prob.assemble(); prob.assemble_local(); prob.solve(tol=1e-14, maxit=50000)
+    # each linear solve to 1e-12: the later radiation steps' right-hand sides are
+    # small, and their relative residual floors near 1e-16 cond(K)
+    t, rep = pb.stationary(tolerance=1e-12, max_iterations=50000)
+    assert rel(t, prob.get("solution")) < SOLUTION_RTOL
+    assert rep.neumann == (1 if case == "neumann" else 0)
+    if case == "radiation":
+        assert rep.nonlinear_iterations == int(prob.scalar("nonlinear_iterations")) >= 3
+        tm, rep_m = pb.stationary(tolerance=1e-12, max_iterations=50000, precision="mixed")
+        assert rel(tm, prob.get("solution")) < SOLUTION_RTOL and rep_m.nonlinear_iterations == rep.nonlinear_iterations
+    if case == "neumann":
+        assert abs(gc.lagrange_column({"elements": m.elements, "nodes": m.nodes, "jacobians": pb.quadrature()[1],
+                                       "basis_qN": pb.basis()["basis_qN"],
+                                       "basis_weights": pb.basis()["basis_weights"]}) @ t - energy) < 1e-12
+
+
+def test_boundary_kind_errors(lib):
+    """A convection edge that shares a node with a temperature group is rejected
+    (the reference couples them through inserted Dirichlet entries); an unbalanced
+    pure Neumann problem is rejected as the reference rejects it."""
+    from nonlocal_gb300 import _lib
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    m = structured_quad_mesh(6, 6, "bilinear")
+    pb = T.Problem2D.from_mesh(m)
+    pb.set_model(T.Model2D(local_weight=1.0))
+    pb.add_boundary(T.Boundary(edges=m.boundaries["left"], kind="temperature", value=0.0))
+    pb.add_boundary(T.Boundary(edges=m.boundaries["down"], kind="convection", heat_transfer=1.0, ambient_temperature=1.0))
+    with pytest.raises(_lib.NlgpuError, match="temperature boundary"):
+        pb.stationary()
+    pb.clear_boundaries()
+    pb.add_boundary(T.Boundary(edges=m.boundaries["left"], kind="flux", value=1.0))
+    pb.add_boundary(T.Boundary(edges=m.boundaries["right"], kind="flux", value=1.0))
+    with pytest.raises(_lib.NlgpuError, match="unsolvable Neumann"):
+        pb.stationary()
