@@ -420,12 +420,13 @@ int nonstationary2d() {
     const T omega = getd("omega", 10.0);           // Dirichlet value amp*sin(omega*t) on `dirichlet_group`
     const std::string dgroup = get("dirichlet_group", "left");
     nonstationary_heat_equation_solver_2d<T, I, J> solver{mesh, dt};
-    const auto bcs_at = [&](const T t) {
-        thermal_boundaries_conditions_2d<T> bcs;
+    const auto bcs_at = [&](const T t) {   // the bc.<group> entries, plus the time-dependent temperature
+        thermal_boundaries_conditions_2d<T> bcs = make_bcs_2d();
         bcs[dgroup] = std::make_unique<temperature_2d<T>>(std::sin(omega * t));
         return bcs;
     };
-    solver.compute(parameters, bcs_at(0), [](const std::array<T, 2>&) { return T{0}; });
+    const T initial = getd("initial", 0.0);
+    solver.compute(parameters, bcs_at(0), [initial](const std::array<T, 2>&) { return initial; });
     std::vector<double> history;
     for (size_t s = 1; s <= steps; ++s) {
         solver.calc_step(bcs_at(T(s) * dt), [](const std::array<T, 2>&) { return T{0}; });

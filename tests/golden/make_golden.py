@@ -113,6 +113,13 @@ CASES = {
                          {"mode": "nonstationary2d", "influence": "fast_polynomial", "radius": 0.3,
                           "local_weight": 0.5, "conductivity": "1", "dt": 1e-3, "steps": 5, "omega": 10,
                           "dirichlet_group": "left"}),
+    # nonstationary with flux, convection and radiation on the right side (radiation terms
+    # of every step stay in the system matrix, as in the reference), initial T = 300
+    "b8_nonstationary_radiation": ({"nx": 8, "ny": 8, "element": BILINEAR},
+                                   {"mode": "nonstationary2d", "influence": "fast_polynomial", "radius": 0.3,
+                                    "local_weight": 0.5, "conductivity": "1", "dt": 1e-3, "steps": 5, "omega": 10,
+                                    "dirichlet_group": "left", "initial": 300,
+                                    "bc.right": "combined:-1,2,0.5,0.5"}),
     # 1D stationary, the full 1000-element quadratic configuration and a small linear one
     "d1_quadratic_1000": ({"none": True},
                           {"mode": "stationary1d", "elements": 1000, "order": 2, "radius": 0.1, "local_weight": 0.5,

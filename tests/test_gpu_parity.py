@@ -284,6 +284,28 @@ def test_nonstationary_history(lib):
         assert rel(t, fx["temperature_history"][s - 1]) < SOLUTION_RTOL, s
 
 
+def test_nonstationary_history_with_radiation(lib):
+    """Flux, convection and radiation on one side of a nonstationary problem: the
+    convection matrix scaled by dt at compute, and each step's radiation terms
+    (dt 4 sigma eps int T^3 N_i N_j kept in the matrix, 3 sigma eps int T^4 N_i in
+    the right-hand side), against the reference's 5-step history."""
+    from nonlocal_gb300 import thermal as T
+    fx = gc.load("b8_nonstationary_radiation")
+    cfg = fx["config"]
+    pb = T.Problem2D(gc.element_type(fx), fx["nodes"], fx["elements"])
+    m = gc.model(cfg)
+    pb.set_model(T.Model2D(influence="fast_polynomial", radius=m["radius"], local_weight=m["local_weight"]))
+    pb.add_boundary(T.Boundary(edges=fx["bnd_" + cfg["dirichlet_group"]], kind="temperature", value=0.0))
+    for d in gc.boundary_specs(fx):
+        pb.add_boundary(T.Boundary(**d))
+    dt, steps, omega = float(cfg["dt"]), int(cfg["steps"]), float(cfg["omega"])
+    solver = T.NonstationaryHeatEquationSolver2D(pb, dt)
+    solver.compute(np.full(pb.n_nodes, float(cfg["initial"])))
+    for s in range(1, steps + 1):
+        t = solver.calc_step(np.sin(omega * s * dt), tolerance=1e-15, max_iterations=10000)
+        assert rel(t, fx["temperature_history"][s - 1]) < SOLUTION_RTOL, s
+
+
 def test_batched_nonstationary_matches_single_instances(lib):
     """Instances of different sizes, radii and time steps stepped as one batch give
     the temperatures (and iteration counts) of stepping each on its own."""
