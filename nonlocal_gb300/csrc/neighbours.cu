@@ -41,27 +41,57 @@ struct WidenOut {
     unsigned long long bbox[4];   // ordered bits: min x, min y, max x, max y
 };
 
-// Squared centre distance over elements sharing a node (diameter_between_elements_centers).
-__global__ void k_widen(i64 E, int nen, const int32_t* __restrict__ elems, const double* __restrict__ centres,
-                        const double* __restrict__ nodes, const i64* __restrict__ ne_off,
-                        const int32_t* __restrict__ ne_elem, int strategy, WidenOut* out) {
+constexpr int WIDEN_THREADS = 256;
+
+// min / max of 64-bit keys over the block, then one atomic per block
+__device__ void block_min_max(unsigned long long (&v)[6], unsigned long long* out_min[3],
+                              unsigned long long* out_max[3]) {
+    __shared__ unsigned long long sh[6][WIDEN_THREADS / 32];
+    for (int k = 0; k < 6; ++k)
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_xor_sync(0xffffffffu, v[k], o);
+            v[k] = k < 3 ? (w < v[k] ? w : v[k]) : (w > v[k] ? w : v[k]);
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 6; ++k) sh[k][threadIdx.x >> 5] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        unsigned long long r = sh[k][0];
+        for (int w = 1; w < WIDEN_THREADS / 32; ++w) r = k < 3 ? (sh[k][w] < r ? sh[k][w] : r) : (sh[k][w] > r ? sh[k][w] : r);
+        if (k < 3) { if (out_min[k]) atomicMin(out_min[k], r); }
+        else if (out_max[k - 3]) atomicMax(out_max[k - 3], r);
+    }
+}
+
+// Squared centre distance over elements sharing a node (diameter_between_elements_centers),
+// and the bounding rectangle of the nodes; extremes reduced per block.
+__global__ void __launch_bounds__(WIDEN_THREADS) k_widen(i64 E, int nen, const int32_t* __restrict__ elems,
+                                                         const double* __restrict__ centres,
+                                                         const double* __restrict__ nodes,
+                                                         const i64* __restrict__ ne_off,
+                                                         const int32_t* __restrict__ ne_elem, int strategy,
+                                                         WidenOut* out) {
+    // min x, min y, min d, max x, max y, max d
+    unsigned long long v[6] = {~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull};
     for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < E * nen; t += i64(gridDim.x) * blockDim.x) {
         const i64 e = t / nen;
         const int i = int(t % nen);
         const int32_t node = elems[t];
-        const double x = nodes[2 * i64(node)], y = nodes[2 * i64(node) + 1];
-        atomicMin(&out->bbox[0], ordered_bits(x));
-        atomicMin(&out->bbox[1], ordered_bits(y));
-        atomicMax(&out->bbox[2], ordered_bits(x));
-        atomicMax(&out->bbox[3], ordered_bits(y));
+        const unsigned long long bx = ordered_bits(nodes[2 * i64(node)]), by = ordered_bits(nodes[2 * i64(node) + 1]);
+        v[0] = bx < v[0] ? bx : v[0];
+        v[1] = by < v[1] ? by : v[1];
+        v[3] = bx > v[3] ? bx : v[3];
+        v[4] = by > v[4] ? by : v[4];
         if (strategy == NLGPU_EXPAND_NO) continue;
         const double cx = centres[2 * e], cy = centres[2 * e + 1];
         for (i64 k = ne_off[node]; k < ne_off[node + 1]; ++k) {
             const int32_t a = ne_elem[k];
             const double zx = cx - centres[2 * i64(a)], zy = cy - centres[2 * i64(a) + 1];
             const double d = zx * zx + zy * zy;
-            if (strategy == NLGPU_EXPAND_MAX) atomicMax(&out->dmax, (unsigned long long)__double_as_longlong(d));
-            else if (strategy == NLGPU_EXPAND_MIN) atomicMin(&out->dmin, (unsigned long long)__double_as_longlong(d));
+            const unsigned long long db = (unsigned long long)__double_as_longlong(d);   // d >= 0: bits order as values
+            if (strategy == NLGPU_EXPAND_MAX) v[5] = db > v[5] ? db : v[5];
+            else if (strategy == NLGPU_EXPAND_MIN) v[2] = db < v[2] ? db : v[2];
             else if (a >= e) {
                 // count the unordered pair once: at the first local node of e shared with a
                 bool first = true;
@@ -74,6 +104,9 @@ __global__ void k_widen(i64 E, int nen, const int32_t* __restrict__ elems, const
             }
         }
     }
+    unsigned long long* mins[3] = {&out->bbox[0], &out->bbox[1], strategy == NLGPU_EXPAND_MIN ? &out->dmin : nullptr};
+    unsigned long long* maxs[3] = {&out->bbox[2], &out->bbox[3], strategy == NLGPU_EXPAND_MAX ? &out->dmax : nullptr};
+    block_min_max(v, mins, maxs);
 }
 
 struct Grid {
