@@ -25,8 +25,9 @@ namespace nlgpu {
 namespace {
 
 constexpr int PT_THREADS = 256;
-constexpr int PT_WORDS = 11264;                // 360448 node numbers per window (44 KB)
+constexpr int PT_WORDS = 10048;                // 321536 node numbers per window (39.3 KB)
 constexpr i64 PT_WINDOW = i64(PT_WORDS) * 32;
+constexpr int PT_ELEM_WORDS = 2048;            // 65536 element numbers for the element bitmap (8 KB)
 constexpr int PT_MAX_ELEMS = 16;               // elements sharing one node
 
 struct PatternArgs {
@@ -85,13 +86,19 @@ __device__ __forceinline__ i64 block_scan_excl(i64 v, i64* sh, i64* total) {
 // counts and block scans.  The window's node range comes from the candidate
 // elements' smallest and largest node numbers, and NEN is a template
 // parameter, so a candidate costs two loads and one shared-memory OR.
+// The elements of a node share most of their neighbours: each candidate
+// element is expanded into its nodes once per row, the first time it is met
+// (an element bitmap over a window of element numbers from the smallest
+// candidate; candidates beyond the window are expanded every time).
 template<int NEN>
 __global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
     __shared__ uint32_t bm[PT_WORDS];
+    __shared__ uint32_t ebm[PT_ELEM_WORDS];
     __shared__ int32_t seg_elem[PT_MAX_ELEMS];
     __shared__ i64 seg_noff[PT_MAX_ELEMS], seg_len[PT_MAX_ELEMS];
     __shared__ i64 sh_scan[PT_THREADS / 32];
-    __shared__ int red_min[PT_THREADS / 32], red_max[PT_THREADS / 32];
+    __shared__ int red_min[PT_THREADS / 32], red_max[PT_THREADS / 32], red_emin[PT_THREADS / 32],
+        red_emax[PT_THREADS / 32];
     const bool fill = a.col_inner != nullptr;
 
     for (i64 r = blockIdx.x; r < a.n; r += gridDim.x) {
@@ -110,22 +117,32 @@ __global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
             return a.local_only ? seg_elem[s] : a.nlist[seg_noff[s] + k];
         };
 
-        // node range of the candidates from their elements' extreme nodes
-        int lo = 0x7fffffff, hi = -1;
+        // node range of the candidates from their elements' extreme nodes, and
+        // the smallest candidate element
+        int lo = 0x7fffffff, hi = -1, elo = 0x7fffffff, ehi = -1;
         for (int s = 0; s < ne; ++s)
             for (i64 k = threadIdx.x; k < seg_len[s]; k += PT_THREADS) {
                 const int32_t e = cand_elem(s, k);
                 lo = min(lo, a.emin[e]);
                 hi = max(hi, a.emax[e]);
+                elo = min(elo, e);
+                ehi = max(ehi, e);
             }
         for (int o = 16; o > 0; o >>= 1) {
             lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
             hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            elo = min(elo, __shfl_xor_sync(0xffffffffu, elo, o));
+            ehi = max(ehi, __shfl_xor_sync(0xffffffffu, ehi, o));
         }
-        if ((threadIdx.x & 31) == 0) { red_min[threadIdx.x >> 5] = lo; red_max[threadIdx.x >> 5] = hi; }
+        if ((threadIdx.x & 31) == 0) {
+            red_min[threadIdx.x >> 5] = lo; red_max[threadIdx.x >> 5] = hi;
+            red_emin[threadIdx.x >> 5] = elo; red_emax[threadIdx.x >> 5] = ehi;
+        }
         __syncthreads();
-        lo = red_min[0]; hi = red_max[0];
-        for (int w = 1; w < PT_THREADS / 32; ++w) { lo = min(lo, red_min[w]); hi = max(hi, red_max[w]); }
+        lo = red_min[0]; hi = red_max[0]; elo = red_emin[0]; ehi = red_emax[0];
+        for (int w = 1; w < PT_THREADS / 32; ++w) {
+            lo = min(lo, red_min[w]); hi = max(hi, red_max[w]); elo = min(elo, red_emin[w]); ehi = max(ehi, red_emax[w]);
+        }
         __syncthreads();
 
         i64 n_inner = 0, n_bound = 0, n_full = 0;
@@ -134,14 +151,30 @@ __global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
             if (fill && threadIdx.x == 0) { a.col_inner[a.rp_inner[r]] = int32_t(r); a.col_full[a.rp_full[r]] = int32_t(r); }
         }
         for (i64 base = lo; hi >= 0 && base <= hi; base += PT_WINDOW) {
-            for (int w = threadIdx.x; w < PT_WORDS; w += PT_THREADS) bm[w] = 0u;
+            // clear only the words the candidates can reach
+            const int node_words = int(min(i64(hi) - base, PT_WINDOW - 1) >> 5) + 1;
+            for (int w = threadIdx.x; w < node_words; w += PT_THREADS) bm[w] = 0u;
+            if (ne > 1) {
+                const int elem_words = int(min(i64(ehi) - elo, i64(PT_ELEM_WORDS) * 32 - 1) >> 5) + 1;
+                for (int w = threadIdx.x; w < elem_words; w += PT_THREADS) ebm[w] = 0u;
+            }
             __syncthreads();
             for (int s = 0; s < ne; ++s)
-                for (i64 t = threadIdx.x; t < seg_len[s] * NEN; t += PT_THREADS) {
-                    const int32_t e = cand_elem(s, t / NEN);
-                    const i64 off = i64(a.elems[i64(e) * NEN + int(t % NEN)]) - base;
-                    if (off < 0 || off >= PT_WINDOW) continue;
-                    atomicOr(&bm[off >> 5], 1u << (off & 31));
+                for (i64 k = threadIdx.x; k < seg_len[s]; k += PT_THREADS) {
+                    const int32_t e = cand_elem(s, k);
+                    if (ne > 1) {   // an element met before in this row adds nothing new
+                        const i64 eo = i64(e) - elo;
+                        if (eo < i64(PT_ELEM_WORDS) * 32) {
+                            const uint32_t bit = 1u << (eo & 31);
+                            if (atomicOr(&ebm[eo >> 5], bit) & bit) continue;
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < NEN; ++j) {
+                        const i64 off = i64(a.elems[i64(e) * NEN + j]) - base;
+                        if (off < 0 || off >= PT_WINDOW) continue;
+                        atomicOr(&bm[off >> 5], 1u << (off & 31));
+                    }
                 }
             __syncthreads();
             const i64 span = min(i64(hi) - base + 1, PT_WINDOW);
