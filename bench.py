@@ -107,6 +107,12 @@ class ClockSampler:
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        # let nvidia-smi finish starting up (its NVML initialisation competes with
+        # the CUDA calls of the first timed steps) before the timed region begins
+        deadline = time.perf_counter() + 5.0
+        while time.perf_counter() < deadline and os.path.getsize(self.file.name) == 0 and self.proc.poll() is None:
+            time.sleep(0.02)
 
     def stop(self) -> dict:
         if self.proc is None:
