@@ -8,7 +8,7 @@
 // product.
 //
 // Usage: ref_driver key=value ...   (see parse() below)
-//   mode=stationary2d | nonstationary2d | stationary1d
+//   mode=stationary2d | nonstationary2d | stationary1d | mechanical2d
 //
 // The stationary 2D branch restates the ten driver lines of
 // libraries/solvers/solver_2d/thermal/stationary_heat_equation_solver_2d.hpp:72-103
@@ -20,6 +20,7 @@
 #include <solvers/solver_2d/influence_functions_2d.hpp>
 #include <solvers/solver_2d/thermal/stationary_heat_equation_solver_2d.hpp>
 #include <solvers/solver_2d/thermal/nonstationary_heat_equation_solver_2d.hpp>
+#include <solvers/solver_2d/mechanical/equilibrium_equation_2d.hpp>
 #include <solvers/solver_1d/influence_functions_1d.hpp>
 #include <solvers/solver_1d/thermal/stationary_heat_equation_solver_1d.hpp>
 #include <metamath/finite_elements/finite_elements_1d/element/element_1d_integrate.hpp>
@@ -392,6 +393,79 @@ int stationary2d() {
     return 0;
 }
 
+// Nonlocal plane elasticity, DoF = 2 (equilibrium_equation_2d.hpp:19-60): the
+// stiffness matrices, the right-hand side and the displacement of the
+// reference's own code, restated around its solve so the CG tolerance can be
+// set.  mbc.<group>=<x>,<y> with d:<value> (displacement_2d) or p:<value>
+// (pressure_2d) per component, e.g. mbc.left=d:0,d:0 mbc.right=p:1,p:0.
+int mechanical2d() {
+    using namespace nonlocal;
+    using namespace nonlocal::solver_2d;
+    using namespace nonlocal::solver_2d::mechanical;
+    auto mesh = std::make_shared<mesh::mesh_2d<T, I>>(std::filesystem::path{get("mesh")});
+    const std::array<T, 2> r = {getd("radius", 0.1), getd("radius2", getd("radius", 0.1))};
+    const T p1 = getd("local_weight", 1.0);
+    if (theory_type(p1) == theory_t::NONLOCAL) {
+        mesh::influences<T> infl;
+        for (const std::string& g : mesh->container().groups_2d())
+            infl[g] = {mesh::powered_distance<T>{size_t(getd("n", 2))}, r};
+        mesh->neighbours(mesh::find_neighbours(*mesh, infl, mesh::diameter_expanding_strategy::MAX));
+    }
+    dump_mesh(*mesh);
+    dump_neighbours(*mesh);
+    raw_mechanical_parameters<T> parameters;
+    for (const std::string& g : mesh->container().groups_2d()) {
+        parameters[g].model.local_weight = p1;
+        parameters[g].model.influence = make_influence(r);
+        isotropic_elastic_parameters<T> elastic;
+        elastic.young_modulus = getd("young_modulus", 210.0);
+        elastic.poissons_ratio = getd("poissons_ratio", 0.3);
+        parameters[g].physical.elastic = elastic;
+    }
+    mechanical_boundaries_conditions_2d<T> bcs;
+    for (const auto& [k, v] : cfg) {
+        if (k.rfind("mbc.", 0) != 0) continue;
+        auto& cond = bcs[k.substr(4)];
+        std::stringstream s{v};
+        std::string part;
+        for (size_t d = 0; d < 2 && std::getline(s, part, ','); ++d) {
+            const T value = std::stod(part.substr(2));
+            if (part[0] == 'd') cond[d] = std::make_unique<displacement_2d<T>>(value);
+            else cond[d] = std::make_unique<pressure_2d<T>>(value);
+        }
+    }
+    // equilibrium_equation_2d.hpp:26-45
+    const auto settings = init_problem_settings(mesh->container(), parameters, bcs);
+    std::vector<uint8_t> inner(settings.is_inner_nodes.begin(), settings.is_inner_nodes.end());
+    dumpv("is_inner", inner);
+    const auto evaluated = evaluate_mechanical_parameters(*mesh, parameters);
+    stiffness_matrix<T, I, J> stiffness{mesh};
+    stiffness.compute(evaluated, settings);
+    Eigen::Matrix<T, Eigen::Dynamic, 1> f = Eigen::Matrix<T, Eigen::Dynamic, 1>::Zero(stiffness.matrix().inner().cols());
+    boundary_condition_second_kind_2d(f, *mesh, bcs);
+    dumpv("rhs_init", std::vector<double>(f.begin(), f.end()));
+    boundary_condition_first_kind_2d(f, *mesh, bcs, stiffness.matrix().bound());
+    dump_csr("K_inner", stiffness.matrix().inner());
+    dump_csr("K_bound", stiffness.matrix().bound());
+    dumpv("rhs", std::vector<double>(f.begin(), f.end()));
+    stiffness_matrix<T, I, J> local{mesh};
+    local.nodes_for_processing(std::ranges::iota_view<size_t, size_t>{0u, mesh->container().nodes_count()});
+    local.compute(evaluated, settings, assemble_part::LOCAL);
+    dump_csr("K_local", local.matrix().inner());
+    slae::conjugate_gradient<T, J> solver{stiffness.matrix().inner()};
+    solver.set_tolerance(getd("tolerance", 1e-13));
+    solver.template init_preconditioner<slae::eigen_ILLT_preconditioner>(local.matrix().inner());
+    const bool illt_ok = solver.preconditioner().computation_info() == Eigen::Success;
+    if (!illt_ok) solver.template init_preconditioner<slae::eigen_identity_preconditioner>();
+    dumps("illt_ok", illt_ok ? 1.0 : 0.0);
+    const Eigen::Matrix<T, Eigen::Dynamic, 1> u = solver.solve(f);
+    dumpv("displacement", std::vector<double>(u.begin(), u.end()));
+    dumps("cg_iterations", double(solver.iterations()));
+    const auto Ku = stiffness.matrix().inner().template selfadjointView<Eigen::Upper>() * u;
+    dumps("true_residual", (f - Ku).norm() / f.norm());
+    return 0;
+}
+
 int nonstationary2d() {
     using namespace nonlocal;
     using namespace nonlocal::solver_2d;
@@ -490,6 +564,7 @@ int main(int argc, char** argv) {
         const std::string mode = get("mode", "stationary2d");
         if (mode == "stationary2d") return stationary2d();
         if (mode == "nonstationary2d") return nonstationary2d();
+        if (mode == "mechanical2d") return mechanical2d();
         if (mode == "stationary1d") return stationary1d();
         std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     } catch (const std::exception& e) {

@@ -120,6 +120,14 @@ CASES = {
                                     "local_weight": 0.5, "conductivity": "1", "dt": 1e-3, "steps": 5, "omega": 10,
                                     "dirichlet_group": "left", "initial": 300,
                                     "bc.right": "combined:-1,2,0.5,0.5"}),
+    # nonlocal plane elasticity (DoF = 2): left side clamped, pressure on the right side
+    "m8_mechanical": ({"nx": 8, "ny": 8, "element": BILINEAR},
+                      {"mode": "mechanical2d", "influence": "fast_polynomial", "radius": 0.3, "local_weight": 0.5,
+                       "young_modulus": 210, "poissons_ratio": 0.3, "mbc.left": "d:0,d:0", "mbc.right": "p:1,p:0",
+                       "tolerance": 1e-14}),
+    "s4_mechanical_local": ({"nx": 4, "ny": 4, "element": SERENDIPITY, "jitter": 0.1, "seed": 5},
+                            {"mode": "mechanical2d", "local_weight": 1, "young_modulus": 100, "poissons_ratio": 0.25,
+                             "mbc.down": "d:0,d:0", "mbc.up": "p:0,p:-2", "tolerance": 1e-14}),
     # 1D stationary, the full 1000-element quadratic configuration and a small linear one
     "d1_quadratic_1000": ({"none": True},
                           {"mode": "stationary1d", "elements": 1000, "order": 2, "radius": 0.1, "local_weight": 0.5,

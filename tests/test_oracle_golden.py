@@ -217,3 +217,24 @@ def test_stationary_1d(name):
                              conductivity=float(cfg["conductivity"]), t_left=float(cfg["left_temperature"]),
                              q_right=float(cfg["right_flux"]), sin_source=cfg["source"] == "sin")
     assert rel(t, fx["temperature"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["m8_mechanical", "s4_mechanical_local"])
+def test_mechanical_fixtures(name):
+    """The reference's plane-elasticity runs (DoF = 2): stiffness rows per node and
+    degree of freedom in upper storage, clamped degrees of freedom as unit rows,
+    and a displacement that solves the stored system."""
+    fx = gc.load(name)
+    n = fx["nodes"].shape[0]
+    rp, ci, va = fx["K_inner_rowptr"], fx["K_inner_col"], fx["K_inner_val"]
+    assert rp.shape[0] == 2 * n + 1
+    rows = np.repeat(np.arange(2 * n), np.diff(rp))
+    assert np.all(ci >= rows)
+    clamped = np.flatnonzero(fx["is_inner"] == 0)
+    for r in clamped:
+        assert rp[r + 1] - rp[r] == 1 and ci[rp[r]] == r and va[rp[r]] == 1.0
+    a = gc.csr_to_dense(rp, ci, va, 2 * n, 2 * n)
+    a = a + np.triu(a, 1).T
+    u, f = fx["displacement"], fx["rhs"]
+    assert np.linalg.norm(a @ u - f) <= 1e-12 * np.linalg.norm(f)
+    assert np.allclose(u[clamped], 0.0)
