@@ -120,6 +120,9 @@ typedef struct nlgpu_solve_report {
     int column_bytes;         /* MIXED: bytes per column index the FP32 SpMV reads (2: 16-bit row offsets) */
     int64_t nonlinear_iterations; /* radiation: fixed-point steps (0 for a linear problem) */
     int neumann;              /* 1 for a pure Neumann problem (integral condition) */
+    int64_t nnz_fp32;         /* MIXED: entries the FP32 SpMV reads (the strictly upper part with
+                                 NLGPU_OPTION_FP32_SYMMETRIC, else nnz_solver) */
+    int fp32_symmetric;       /* MIXED: 1 when the FP32 SpMV reads the strictly upper part */
 } nlgpu_solve_report;
 
 /* ---- library ------------------------------------------------------------ */
@@ -384,7 +387,10 @@ int nlgpu_mpnn_loss_grad(nlgpu_ctx* ctx, const float* r, const float* e, float* 
  * hold the starting guess (zeros for a zero start).  All calls share the
  * array: calls that overlap on the GPU race.  Stops when |r| <= tolerance |b|
  * (|r| of the CG recurrence) or after max_iterations; reports the iterations
- * and |b - A x| / |b| recomputed from x.
+ * and |b - A x| / |b| recomputed from x (also when the starting guess already
+ * meets the tolerance: 0 iterations).  b = 0 sets x = 0.  Returns
+ * NLGPU_ERR_NO_CONVERGENCE, with x, iterations and residual filled, when the
+ * iteration cap is reached and |b - A x| > tolerance |b|.
  * `stream` is a cudaStream_t or NULL; the call returns after the stream has
  * finished its work. */
 #define NLGPU_NOALLOC_MAX_ROWS 65536
@@ -453,8 +459,13 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
  * a mixed-precision stationary solve and in FP64 otherwise, NLGPU_ASSEMBLY_FF
  * always in float-float, NLGPU_ASSEMBLY_FP64 always in FP64.  Float-float
  * (about 48 significant bits) applies to the fast-polynomial, polynomial and
- * exponential influence with constant conductivity; other models use FP64. */
-enum { NLGPU_OPTION_GLOBAL_SWEEPS = 0, NLGPU_OPTION_ORDERED_PAIRS = 1, NLGPU_OPTION_ASSEMBLY_PRECISION = 2 };
+ * exponential influence with constant conductivity; other models use FP64.
+ * NLGPU_OPTION_FP32_SYMMETRIC = 1 makes the mixed solve's FP32 SpMV read only
+ * the strictly upper part of a symmetric solver matrix (half the entries,
+ * transposed contributions added with shared-memory atomics) instead of its
+ * full rows (the default; for comparison). */
+enum { NLGPU_OPTION_GLOBAL_SWEEPS = 0, NLGPU_OPTION_ORDERED_PAIRS = 1, NLGPU_OPTION_ASSEMBLY_PRECISION = 2,
+       NLGPU_OPTION_FP32_SYMMETRIC = 3 };
 enum { NLGPU_ASSEMBLY_AUTO = 0, NLGPU_ASSEMBLY_FF = 1, NLGPU_ASSEMBLY_FP64 = 2 };
 int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value);
 int nlgpu_event_record(nlgpu_ctx* ctx, int slot);

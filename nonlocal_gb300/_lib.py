@@ -29,7 +29,7 @@ BC_TEMPERATURE, BC_FLUX, BC_CONVECTION, BC_RADIATION, BC_COMBINED_FLUX = 0, 1, 2
 MATRIX_INNER, MATRIX_BOUND, MATRIX_LOCAL = 0, 1, 2
 PRECONDITIONER = {"identity": 0, "illt": 1, "illt_learned": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
-OPTION_GLOBAL_SWEEPS, OPTION_ORDERED_PAIRS, OPTION_ASSEMBLY_PRECISION = 0, 1, 2
+OPTION_GLOBAL_SWEEPS, OPTION_ORDERED_PAIRS, OPTION_ASSEMBLY_PRECISION, OPTION_FP32_SYMMETRIC = 0, 1, 2, 3
 ASSEMBLY = {"auto": 0, "ff": 1, "fp64": 2}
 
 
@@ -60,7 +60,7 @@ class SolveReport(ctypes.Structure):
                 ("seconds_assembly", c_d), ("seconds_boundary", c_d), ("seconds_preconditioner", c_d),
                 ("seconds_solve", c_d), ("seconds_total", c_d), ("outer_iterations", c_i64),
                 ("learned_fallback", c_int), ("column_bytes", c_int), ("nonlinear_iterations", c_i64),
-                ("neumann", c_int)]
+                ("neumann", c_int), ("nnz_fp32", c_i64), ("fp32_symmetric", c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -168,7 +168,9 @@ void fill_report(Ctx& c, nlgpu_solve_report* rep, const CgResult& r) {
     rep->element_pairs = c.pairs;
     rep->outer_iterations = r.outer_iterations;
     rep->learned_fallback = r.learned_fallback ? 1 : 0;
-    rep->column_bytes = c.full.col16_ok ? 2 : 4;
+    rep->column_bytes = c.full.up_ok || c.full.col16_ok ? 2 : 4;
+    rep->nnz_fp32 = c.full.up_ok ? c.full.up_nnz : c.full.nnz;
+    rep->fp32_symmetric = c.full.up_ok ? 1 : 0;
 }
 
 // One linear solve of the assembled system with right-hand side rhs (default
@@ -217,7 +219,7 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     c.temperature.resize(size_t(c.n_nodes));
     CgResult r;
     if (mixed) {
-        matrix_to_f32(c, c.full);
+        matrix_to_f32(c, c.full, c.symmetric && c.fp32_symmetric ? &c.inner : nullptr);
         timer.mark("FP32 matrix");
         c.ilt_sweeps = sweeps;
         r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, b, c.temperature.p, o.tolerance, o.max_iterations,
@@ -931,7 +933,8 @@ void ensure_learning_state(Ctx& c) {
     if (!c.local_ready) build_local(c);
     if (!c.ilt.ok || c.ilt.n != c.local.rows) ilt_build(c, c.local, c.ilt);
     NL_REQUIRE(c.ilt.ok, NLGPU_ERR_NUMERICAL, "ILLT failed on the local matrix");
-    if (c.full.val32.n != size_t(c.full.nnz)) matrix_to_f32(c, c.full);
+    if (!c.full.up_ok && c.full.val32.n != size_t(c.full.nnz))
+        matrix_to_f32(c, c.full, c.fp32_symmetric ? &c.inner : nullptr);
     if (!(c.mp.ready && c.mp.n == c.local.rows)) mpnn_prepare(c, c.local);
 }
 }  // namespace
@@ -1134,16 +1137,25 @@ int nlgpu_cg_solve_noalloc(void* stream, int64_t n, const int64_t* d_rowptr, con
                            const double* d_b, double* d_x, double tolerance, int64_t max_iterations, int64_t* iterations,
                            double* residual) {
     if (!iterations || !residual) return NLGPU_ERR_ARG;
-    return guarded([&] {
-        cg_solve_noalloc(static_cast<cudaStream_t>(stream), n, d_rowptr, d_col, d_val, d_b, d_x, tolerance,
-                         max_iterations, iterations, residual);
+    int conv_status = NLGPU_OK;
+    const int rc = guarded([&] {
+        if (!cg_solve_noalloc(static_cast<cudaStream_t>(stream), n, d_rowptr, d_col, d_val, d_b, d_x, tolerance,
+                              max_iterations, iterations, residual))
+            conv_status = NLGPU_ERR_NO_CONVERGENCE;
     });
+    return rc != NLGPU_OK ? rc : conv_status;
 }
 
 int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value) {
     if (!ctx) return NLGPU_ERR_ARG;
     if (option == NLGPU_OPTION_GLOBAL_SWEEPS) { ctx->force_global_sweeps = value != 0; return NLGPU_OK; }
     if (option == NLGPU_OPTION_ORDERED_PAIRS) { ctx->ordered_pairs = value != 0; return NLGPU_OK; }
+    if (option == NLGPU_OPTION_FP32_SYMMETRIC) {
+        ctx->fp32_symmetric = value != 0;
+        ctx->full.up_ok = false;   // the next mixed solve or stage timing rebuilds the FP32 copy
+        ctx->full.val32.release();
+        return NLGPU_OK;
+    }
     if (option == NLGPU_OPTION_ASSEMBLY_PRECISION) {
         if (value < NLGPU_ASSEMBLY_AUTO || value > NLGPU_ASSEMBLY_FP64) return NLGPU_ERR_ARG;
         ctx->assembly_precision = value;
@@ -1208,7 +1220,8 @@ int nlgpu_time_stage(nlgpu_ctx* ctx, int stage, int reps, double* ms) {
             NL_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), c.stream));
             NL_CUDA(cudaMemsetAsync(x32.p, 0, x32.bytes(), c.stream));
             if (stage == 2 || stage >= 5) NL_REQUIRE(c.ilt.ok, NLGPU_ERR_STATE, "no ILLT factor");
-            if (stage == 4 && (c.full.val32.n != size_t(c.full.nnz) || !c.full.col16_ok)) matrix_to_f32(c, c.full);
+            if (stage == 4 && !c.full.up_ok && (c.full.val32.n != size_t(c.full.nnz) || !c.full.col16_ok))
+                matrix_to_f32(c, c.full, c.symmetric && c.fp32_symmetric ? &c.inner : nullptr);
         }
         if (stage == 1 || stage == 7)
             NL_REQUIRE(c.inner.nnz > 0 && c.model.nonlocal(), NLGPU_ERR_STATE, "no nonlocal pattern");

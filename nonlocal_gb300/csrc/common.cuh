@@ -151,6 +151,18 @@ struct Csr {
     dbuf<float> rowsum32;        // row sums of the FP64 values (difference-form FP32 SpMV)
     dbuf<int16_t> col16;         // column - row, when every entry's offset fits 16 bits
     bool col16_ok = false;
+    // the strictly upper part in FP32 for the symmetric FP32 SpMV (mixed.cu):
+    // row pointers, 16-bit offsets column - row and values; each CTA of that
+    // SpMV owns a contiguous row range and accumulates into a shared-memory
+    // window of the columns its rows reach
+    dbuf<i64> up_rp;
+    dbuf<uint16_t> up_off;
+    dbuf<float> up_val;
+    dbuf<int32_t> up_part;       // [up_blocks + 1] first row of each CTA's range
+    dbuf<int32_t> up_window;     // [up_blocks] columns from the range's first row to the farthest column
+    i64 up_nnz = 0;
+    int up_blocks = 0, up_window_max = 0;
+    bool up_ok = false;
 };
 
 struct BoundaryGroup {
@@ -377,6 +389,7 @@ struct Ctx {
     bool force_global_sweeps = false;   // use the global-memory sweeps (for comparison)
     int ilt_sweeps = NLGPU_DEFAULT_TRIANGULAR_SWEEPS;   // FP32 ILLT: Jacobi sweeps per triangle (0: exact)
     bool ordered_pairs = false;         // evaluate every ordered element pair (for comparison)
+    bool fp32_symmetric = false;        // FP32 SpMV from the strictly upper part (for comparison)
     int assembly_precision = NLGPU_ASSEMBLY_AUTO;
     bool ff_assembly = false;           // pair blocks in float-float on the FP32 pipes (mixed precision)
     bool ff_assembled = false;          // the last assembly ran in float-float
@@ -472,7 +485,10 @@ void jacobi_build(Ctx& ctx, IncompleteCholesky& ic, const std::vector<i64>& rp, 
 void jacobi_fill(Ctx& ctx, IncompleteCholesky& ic);
 void jacobi_apply32(Ctx& ctx, IncompleteCholesky& ic, int sweeps, const float* r, float* z, const double* flags);
 // mixed.cu
-void matrix_to_f32(Ctx& ctx, Csr& A);
+// FP32 copy of the solver matrix A (full rows) for the mixed solve; with the
+// upper storage of a symmetric A given, only its strictly upper part is copied
+// (symmetric FP32 SpMV) when every row's reach fits the SpMV's shared memory
+void matrix_to_f32(Ctx& ctx, Csr& A, const Csr* upper = nullptr);
 void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y);
 // sweeps 0: level-scheduled triangular solves; > 0: that many Jacobi sweeps per triangle
 void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, int sweeps = 0);
@@ -512,7 +528,7 @@ struct MpnnTrainResult {
 void mpnn_train(Ctx& ctx, const Csr& A, IncompleteCholesky& M, const double* b, const MpnnTrainOptions& o,
                 MpnnTrainResult& out);
 // noalloc.cu
-void cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, const double* val, const double* b,
+bool cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, const double* val, const double* b,
                       double* x, double tolerance, i64 max_iterations, i64* iterations, double* residual);
 // onedim.cu
 void stationary_1d(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight, int influence,

@@ -180,6 +180,174 @@ __global__ void __launch_bounds__(MX_THREADS) k_spmv32(i64 n, const i64* __restr
     }
 }
 
+// q = A32 p from the strictly upper part of the symmetric matrix (half the
+// bytes of the full rows; NLGPU_OPTION_FP32_SYMMETRIC).  Measured on the
+// 300x300 serendipity problem it is no faster than the full-row kernel (0.77
+// against 0.79 ms per product; one more launch for p.q): the shared-memory
+// atomics, not the bytes, bound it, so full rows stay the default.  In the same difference form, an upper entry a_rc
+// (c > r) gives t = a_rc (p_c - p_r) to row r and -t to row c.  Each CTA (one
+// per SM, so that the x values of its rows' reach stay in L1 beside the
+// window) owns a contiguous range of rows with equal entry counts and
+// accumulates every contribution with shared-memory atomics into a window of
+// the columns its rows reach (its first row up to the farthest column); the
+// window is then added to q with global atomics, so q must be zero before the
+// launch (the kernel that forms the next direction clears its slot).  Warp per
+// row, entry per lane, four entries in flight per lane.  Summation order is
+// not fixed (atomics); the flexible FP32 iteration absorbs that.  p.q is taken
+// afterwards from the finished q (k_pq32): alpha must match the q the residual
+// update uses, or the recurrence loses its local orthogonality.
+constexpr int UP_THREADS = 1024;
+
+__global__ void __launch_bounds__(UP_THREADS, 1) k_spmv32_up(const i64* __restrict__ rp, const uint16_t* __restrict__ off,
+                                                             const float* __restrict__ val,
+                                                             const float* __restrict__ rowsum,
+                                                             const int32_t* __restrict__ part_rows,
+                                                             const int32_t* __restrict__ window,
+                                                             const float* __restrict__ x, float* __restrict__ y,
+                                                             const double* __restrict__ flags, i64 ring) {
+    extern __shared__ float acc[];
+    if (flags && flags[S_DONE] != 0.0) return;
+    if (ring) {
+        const i64 slot = i64(flags[S_ITERS]) % MX_M;
+        x += slot * ring; y += slot * ring;
+    }
+    const int r0 = part_rows[blockIdx.x], r1 = part_rows[blockIdx.x + 1], W = window[blockIdx.x];
+    for (int k = threadIdx.x; k < W; k += blockDim.x) acc[k] = 0.0f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, nw = int(blockDim.x >> 5);
+    for (int r = r0 + int(threadIdx.x >> 5); r < r1; r += nw) {
+        const float xr = x[r];
+        const float* xo = x + r;
+        float* ao = acc + (r - r0);
+        const i64 b = rp[r];
+        const uint16_t* orow = off + b;
+        const float* vrow = val + b;
+        const int len = int(rp[r + 1] - b);
+        float s = 0.0f;
+        int q = lane;
+        for (; q + 96 < len; q += 128) {
+            const int o0 = __ldg(orow + q), o1 = __ldg(orow + q + 32), o2 = __ldg(orow + q + 64),
+                      o3 = __ldg(orow + q + 96);
+            const float v0 = __ldg(vrow + q), v1 = __ldg(vrow + q + 32), v2 = __ldg(vrow + q + 64),
+                        v3 = __ldg(vrow + q + 96);
+            const float t0 = v0 * (xo[o0] - xr), t1 = v1 * (xo[o1] - xr), t2 = v2 * (xo[o2] - xr),
+                        t3 = v3 * (xo[o3] - xr);
+            s += (t0 + t1) + (t2 + t3);
+            atomicAdd(ao + o0, -t0); atomicAdd(ao + o1, -t1); atomicAdd(ao + o2, -t2); atomicAdd(ao + o3, -t3);
+        }
+        for (; q < len; q += 32) {
+            const int o = __ldg(orow + q);
+            const float t = __ldg(vrow + q) * (xo[o] - xr);
+            s += t;
+            atomicAdd(ao + o, -t);
+        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) atomicAdd(ao, s + rowsum[r] * xr);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < W; k += blockDim.x) {
+        const float v = acc[k];
+        if (v != 0.0f) atomicAdd(y + r0 + k, v);
+    }
+}
+
+// p_j.q_j of the current direction slot j (after the symmetric SpMV); the last
+// block stores it and forms alpha = (p_j.r) / (p_j.q_j)
+__global__ void __launch_bounds__(MX_THREADS) k_pq32(i64 n, const float* __restrict__ pring,
+                                                     const float* __restrict__ qring, double* __restrict__ part,
+                                                     double* __restrict__ flags, unsigned* ticket) {
+    __shared__ double sh[40];
+    if (flags[S_DONE] != 0.0) return;
+    const i64 slot = i64(flags[S_ITERS]) % MX_M;
+    const float* p = pring + slot * n;
+    const float* q = qring + slot * n;
+    float s = 0.0f;   // a thread's one or two elements in FP32; block and global sums in FP64
+    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
+        s = fmaf(p[i], q[i], s);
+    double v[1] = {double(s)};
+    if (mx_reduce_last<1>(v, part, ticket, sh) && threadIdx.x == 0) {
+        flags[S_PQ + slot] = v[0];
+        flags[S_ALPHA] = flags[S_PR] / v[0];
+    }
+}
+
+// strictly upper entries per row of an upper-stored matrix (warp per row);
+// an entry below the diagonal marks the matrix unusable here
+__global__ void k_up_count(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col, i64* __restrict__ cnt,
+                           int* __restrict__ bad) {
+    const int lane = threadIdx.x & 31;
+    const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
+    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
+        int c = 0, below = 0;
+        for (i64 k = rp[r] + lane; k < rp[r + 1]; k += 32) {
+            c += col[k] > r;
+            below |= col[k] < r;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+            below |= __shfl_xor_sync(0xffffffffu, below, o);
+        }
+        if (lane == 0) {
+            cnt[r] = c;
+            if (below) *bad = 1;
+        }
+    }
+}
+
+// offsets column - row (16 bits) and FP32 values of the strictly upper entries,
+// which are the tail of each sorted upper row
+__global__ void k_up_fill(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col,
+                          const double* __restrict__ val, const i64* __restrict__ up_rp, uint16_t* __restrict__ off,
+                          float* __restrict__ v32, int* __restrict__ bad) {
+    const int lane = threadIdx.x & 31;
+    const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
+    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
+        const i64 len = up_rp[r + 1] - up_rp[r], src = rp[r + 1] - len;
+        int wide = 0;
+        for (i64 k = lane; k < len; k += 32) {
+            const i64 o = i64(col[src + k]) - r;
+            wide |= o > 65535;
+            off[up_rp[r] + k] = uint16_t(o);
+            v32[up_rp[r] + k] = float(val[src + k]);
+        }
+        if (__any_sync(0xffffffffu, wide) && lane == 0) *bad = 1;
+    }
+}
+
+// first row of each of `blocks` row ranges with equal entry counts
+__global__ void k_up_partition(i64 n, const i64* __restrict__ up_rp, int blocks, int32_t* __restrict__ part) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > blocks) return;
+    if (c == blocks) { part[c] = int32_t(n); return; }
+    const i64 target = i64(double(up_rp[n]) * c / blocks);
+    i64 lo = 0, hi = n;   // first row r with up_rp[r] >= target
+    while (lo < hi) {
+        const i64 mid = (lo + hi) / 2;
+        if (up_rp[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    part[c] = int32_t(lo);
+}
+
+// columns reached by each range: from its first row to the farthest column of its rows
+__global__ void k_up_window(const i64* __restrict__ up_rp, const uint16_t* __restrict__ off,
+                            const int32_t* __restrict__ part, int32_t* __restrict__ window, int* __restrict__ wmax) {
+    __shared__ int sh[32];
+    const int r0 = part[blockIdx.x], r1 = part[blockIdx.x + 1];
+    int far = r0 - 1;
+    for (int r = r0 + int(threadIdx.x); r < r1; r += blockDim.x) {
+        const i64 e = up_rp[r + 1];
+        far = max(far, e > up_rp[r] ? r + int(off[e - 1]) : r);
+    }
+    for (int o = 16; o > 0; o >>= 1) far = max(far, __shfl_xor_sync(0xffffffffu, far, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = far;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < int(blockDim.x >> 5); ++w) far = max(far, sh[w]);
+        window[blockIdx.x] = far - r0 + 1;
+        atomicMax(wmax, far - r0 + 1);
+    }
+}
+
 // FP64 outer kernels: partial of a.b; r = b - q with the partial of r.r
 __global__ void __launch_bounds__(MX_THREADS) k_dot_f64(i64 n, const double* __restrict__ a, const double* __restrict__ b,
                                                         double* __restrict__ partial) {
@@ -340,7 +508,8 @@ __global__ void __launch_bounds__(MX_THREADS) k_dotm32(i64 n, const float* __res
 // numerator, stored by the last block)
 __global__ void __launch_bounds__(MX_THREADS) k_update_pm32(i64 n, float* __restrict__ pring, const float* __restrict__ z,
                                                             const float* __restrict__ r, double* __restrict__ part,
-                                                            double* __restrict__ flags, unsigned* ticket) {
+                                                            double* __restrict__ flags, unsigned* ticket,
+                                                            float* __restrict__ qring_clear) {
     __shared__ double sh[40];
     if (flags[S_DONE] != 0.0) return;
     const i64 k = i64(flags[S_ITERS]);
@@ -349,8 +518,12 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_pm32(i64 n, float* __rest
 #pragma unroll
     for (int s = 0; s < MX_M; ++s) beta[s] = s < count ? float(flags[S_BETA + s]) : 0.0f;
     float* pn = pring + i64(next) * n;
+    // the symmetric SpMV accumulates q_k into its slot: clear it (its old
+    // direction was last read by k_dotm32 of this iteration)
+    float* qn = qring_clear ? qring_clear + i64(next) * n : nullptr;
     float pr = 0.0f;
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+        if (qn) qn[i] = 0.0f;
         float v = z[i];
 #pragma unroll
         for (int s = 0; s < MX_M; ++s)
@@ -387,7 +560,14 @@ void precondition32(Ctx& ctx, IncompleteCholesky* M, const float* r, float* z, c
 
 void launch_spmv32(Ctx& ctx, const Csr& A, const float* x, float* y, double* dot_partial, double* flags, i64 ring,
                    unsigned* ticket) {
-    if (A.col16_ok)
+    if (A.up_ok) {
+        NL_LAUNCH(k_spmv32_up, A.up_blocks, UP_THREADS, size_t(A.up_window_max) * sizeof(float), ctx.stream,
+                  A.up_rp.p, A.up_off.p, A.up_val.p, A.rowsum32.p, A.up_part.p, A.up_window.p, x, y, flags, ring);
+        if (dot_partial) {
+            const unsigned G = unsigned(std::min<i64>(RED_BLOCKS, std::max<i64>(1, (A.rows + MX_THREADS - 1) / MX_THREADS)));
+            NL_LAUNCH(k_pq32, G, MX_THREADS, 0, ctx.stream, A.rows, x, y, dot_partial, flags, ticket);
+        }
+    } else if (A.col16_ok)
         NL_LAUNCH(k_spmv32<int16_t>, SPMV_BLOCKS, MX_THREADS, 0, ctx.stream, A.rows, A.rowptr.p, A.col16.p, A.val32.p,
                   A.rowsum32.p, x, y, dot_partial, flags, ring, ticket);
     else
@@ -398,6 +578,7 @@ void launch_spmv32(Ctx& ctx, const Csr& A, const float* x, float* y, double* dot
 }  // namespace
 
 void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y) {
+    if (A.up_ok) NL_CUDA(cudaMemsetAsync(y, 0, size_t(A.rows) * sizeof(float), ctx.stream));
     launch_spmv32(ctx, A, x, y, nullptr, nullptr, 0, nullptr);
 }
 
@@ -407,13 +588,67 @@ void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, int
     precondition32(ctx, &ic, r, z, nullptr, nullptr, 0.0, sweeps);
 }
 
-// FP32 values and FP64 row sums of the solver matrix, and 16-bit column
-// offsets when the pattern's bandwidth allows
-void matrix_to_f32(Ctx& ctx, Csr& A) {
-    A.val32.resize(size_t(A.nnz));
+namespace {
+
+// The strictly upper part of `upper` in FP32 with 16-bit offsets and the row
+// ranges of the symmetric SpMV's CTAs (one per SM); false (full rows are used)
+// when an offset exceeds 16 bits or a window exceeds one CTA's shared memory.
+bool upper_to_f32(Ctx& ctx, Csr& A, const Csr& upper) {
+    const i64 n = upper.rows;
+    if (n <= 0 || n != A.rows || n >= (i64(1) << 31)) return false;
+    int dev = 0, sms = 0, smem_optin = 0, smem_sm = 0;
+    NL_CUDA(cudaGetDevice(&dev));
+    NL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    NL_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    NL_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    A.up_rp.resize(size_t(n) + 1);
+    dbuf<int> flags;   // [0] bad, [1] widest window
+    flags.resize(2);
+    flags.zero(ctx.stream);
+    NL_LAUNCH(k_up_count, RED_BLOCKS, 256, 0, ctx.stream, n, upper.rowptr.p, upper.col.p, A.up_rp.p, flags.p);
+    NL_CUDA(cudaMemsetAsync(A.up_rp.p + n, 0, sizeof(i64), ctx.stream));
+    i64 total = 0;
+    exclusive_scan(ctx, A.up_rp.p, A.up_rp.p, n + 1, &total);
+    A.up_nnz = total;
+    A.up_off.resize(size_t(std::max<i64>(total, 1)));
+    A.up_val.resize(size_t(std::max<i64>(total, 1)));
+    NL_LAUNCH(k_up_fill, RED_BLOCKS, 256, 0, ctx.stream, n, upper.rowptr.p, upper.col.p, upper.val.p, A.up_rp.p,
+              A.up_off.p, A.up_val.p, flags.p);
+    const int blocks = sms;
+    A.up_part.resize(size_t(blocks) + 1);
+    A.up_window.resize(size_t(blocks));
+    NL_LAUNCH(k_up_partition, grid_for(blocks + 1, 256), 256, 0, ctx.stream, n, A.up_rp.p, blocks, A.up_part.p);
+    NL_LAUNCH(k_up_window, blocks, 256, 0, ctx.stream, A.up_rp.p, A.up_off.p, A.up_part.p, A.up_window.p, flags.p + 1);
+    int h[2] = {0, 0};
+    flags.download(h, 2, ctx.stream);
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+    const size_t bytes = size_t(std::max(h[1], 1)) * sizeof(float);
+    if (h[0] || bytes + 2048 > size_t(std::min(smem_optin, smem_sm))) return false;
+    NL_CUDA(cudaFuncSetAttribute(k_spmv32_up, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+    A.up_blocks = blocks;
+    A.up_window_max = std::max(h[1], 1);
+    return true;
+}
+
+}  // namespace
+
+// FP64 row sums of the solver matrix in FP32, and FP32 values: the strictly
+// upper part of `upper` for the symmetric SpMV when it applies, else the full
+// rows with 16-bit column offsets when the pattern's bandwidth allows
+void matrix_to_f32(Ctx& ctx, Csr& A, const Csr* upper) {
     A.rowsum32.resize(size_t(A.rows));
-    NL_LAUNCH(k_to_f32, grid_for(A.nnz, 256), 256, 0, ctx.stream, A.nnz, A.val.p, A.val32.p);
     NL_LAUNCH(k_rowsum, grid_for(A.rows, 256), 256, 0, ctx.stream, A.rows, A.rowptr.p, A.val.p, A.rowsum32.p);
+    A.up_ok = upper && upper_to_f32(ctx, A, *upper);
+    if (A.up_ok) {
+        // the full-row FP32 copy is not needed (and not kept up to date)
+        A.val32.release();
+        A.col16.release();
+        A.col16_ok = false;
+        return;
+    }
+    A.up_rp.release(); A.up_off.release(); A.up_val.release();
+    A.val32.resize(size_t(A.nnz));
+    NL_LAUNCH(k_to_f32, grid_for(A.nnz, 256), 256, 0, ctx.stream, A.nnz, A.val.p, A.val32.p);
     dbuf<unsigned long long> widest;
     widest.resize(1);
     widest.zero(ctx.stream);
@@ -443,7 +678,7 @@ void matrix_to_f32(Ctx& ctx, Csr& A) {
 // with the learned correction, whose network runs outside graphs).
 CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double* b, double* x, double tolerance,
                      i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps) {
-    NL_REQUIRE(A.val32.n == size_t(A.nnz), NLGPU_ERR_STATE, "the FP32 copy of the matrix is missing");
+    NL_REQUIRE(A.up_ok || A.val32.n == size_t(A.nnz), NLGPU_ERR_STATE, "the FP32 copy of the matrix is missing");
     NL_REQUIRE(!learned || (M && ctx.mp.ready && ctx.mp.n == A.rows), NLGPU_ERR_STATE,
                "the learned correction needs ILLT and a prepared network");
     const i64 n = A.rows;
@@ -470,6 +705,10 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     NL_CUDA(cudaMemsetAsync(part, 0, size_t(M_SLOTS) * RED_BLOCKS * sizeof(double), ctx.stream));
     NL_CUDA(cudaMemsetAsync(outer_part, 0, size_t(2) * RED_BLOCKS * sizeof(double), ctx.stream));
     if (!x_is_initial_guess) NL_CUDA(cudaMemsetAsync(x, 0, size_t(n) * sizeof(double), ctx.stream));
+    // the symmetric SpMV adds into q's ring slot: slot 0 starts at zero, the
+    // later slots are cleared by the kernel that forms their direction
+    float* qclear = A.up_ok ? w.q.p : nullptr;
+    if (qclear) NL_CUDA(cudaMemsetAsync(w.q.p, 0, size_t(n) * sizeof(float), ctx.stream));
     const double eta2 = update_factor * update_factor;
     CgResult res;
     auto precondition = [&](const double* pt, const double* fl, double t2) {
@@ -516,7 +755,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
                   eta2, cap);
         precondition(part, flags, eta2);
         NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, part, flags, ticket);
-        NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags, ticket);
+        NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags, ticket, qclear);
     };
     bool eager_done = false, captured = false;
     auto run_chunk = [&] {
@@ -595,7 +834,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
             // the end of iteration k - 1 (the kernels read k from the count)
             precondition(nullptr, nullptr, 0.0);
             NL_LAUNCH(k_dotm32, G, MX_THREADS, 0, ctx.stream, n, w.z.p, w.q.p, part, flags, ticket);
-            NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags, ticket);
+            NL_LAUNCH(k_update_pm32, G, MX_THREADS, 0, ctx.stream, n, w.p.p, w.z.p, w.r.p, part, flags, ticket, qclear);
         }
     }
     timer.mark("remaining iterations");

@@ -191,7 +191,7 @@ double* scratch_for_current_device() {
 
 }  // namespace
 
-void cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, const double* val, const double* b,
+bool cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, const double* val, const double* b,
                       double* x, double tolerance, i64 max_iterations, i64* iterations, double* residual) {
     NL_REQUIRE(n > 0 && n <= NA_MAX_ROWS, NLGPU_ERR_ARG, "n must be in 1 .. NLGPU_NOALLOC_MAX_ROWS");
     NL_REQUIRE(rp && col && val && b && x && tolerance > 0.0 && max_iterations > 0, NLGPU_ERR_ARG, "invalid argument");
@@ -211,21 +211,28 @@ void cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, 
     double host[8];
     NL_CUDA(cudaMemcpyAsync(host, sc, sizeof host, cudaMemcpyDeviceToHost, s));
     NL_CUDA(cudaStreamSynchronize(s));
-    if (host[NA_BB_S] == 0.0 || host[NA_RR_S] <= tol2 * host[NA_BB_S]) {
-        *iterations = 0;
-        *residual = host[NA_BB_S] == 0.0 ? 0.0 : std::sqrt(host[NA_RR_S] / host[NA_BB_S]);
-        return;
-    }
-    for (;;) {
-        for (int it = 0; it < NA_ITERS; ++it) {   // NA_ITERS is even: every chunk starts at parity 0
-            const int parity = it & 1;
-            NL_LAUNCH(na_spmv, NA_BLOCKS, NA_THREADS, 0, s, n, rp, col, val, p, q, part + NA_PQ * NA_BLOCKS, sc);
-            NL_LAUNCH(na_update_xr, NA_BLOCKS, NA_THREADS, 0, s, n, x, r, p, q, part, sc, parity);
-            NL_LAUNCH(na_update_p, NA_BLOCKS, NA_THREADS, 0, s, n, p, r, part, sc, tol2, maxit, parity);
-        }
-        NL_CUDA(cudaMemcpyAsync(host, sc, sizeof host, cudaMemcpyDeviceToHost, s));
+    if (host[NA_BB_S] == 0.0) {
+        // b = 0: the solution is x = 0 whatever the starting guess held
+        NL_CUDA(cudaMemsetAsync(x, 0, size_t(n) * sizeof(double), s));
         NL_CUDA(cudaStreamSynchronize(s));
-        if (host[NA_DONE] != 0.0) break;
+        *iterations = 0;
+        *residual = 0.0;
+        return true;
+    }
+    // a starting guess that already meets the tolerance skips the iteration and
+    // goes straight to the recomputed residual below
+    if (host[NA_RR_S] > tol2 * host[NA_BB_S]) {
+        for (;;) {
+            for (int it = 0; it < NA_ITERS; ++it) {   // NA_ITERS is even: every chunk starts at parity 0
+                const int parity = it & 1;
+                NL_LAUNCH(na_spmv, NA_BLOCKS, NA_THREADS, 0, s, n, rp, col, val, p, q, part + NA_PQ * NA_BLOCKS, sc);
+                NL_LAUNCH(na_update_xr, NA_BLOCKS, NA_THREADS, 0, s, n, x, r, p, q, part, sc, parity);
+                NL_LAUNCH(na_update_p, NA_BLOCKS, NA_THREADS, 0, s, n, p, r, part, sc, tol2, maxit, parity);
+            }
+            NL_CUDA(cudaMemcpyAsync(host, sc, sizeof host, cudaMemcpyDeviceToHost, s));
+            NL_CUDA(cudaStreamSynchronize(s));
+            if (host[NA_DONE] != 0.0) break;
+        }
     }
     // |b - A x| / |b| recomputed from the final x
     NL_LAUNCH(na_spmv, NA_BLOCKS, NA_THREADS, 0, s, n, rp, col, val, x, q, static_cast<double*>(nullptr),
@@ -237,6 +244,9 @@ void cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, 
     *iterations = i64(host[NA_ITS]);
     *residual = std::sqrt(host[NA_RR_S] / host[NA_BB_S]);
     NL_REQUIRE(std::isfinite(*residual), NLGPU_ERR_NUMERICAL, "CG broke down (non-finite residual)");
+    // a stop before the iteration cap means the recurrence met the tolerance;
+    // at the cap, the residual recomputed from x decides
+    return !(host[NA_ITS] >= maxit && host[NA_RR_S] > tol2 * host[NA_BB_S]);
 }
 
 }  // namespace nlgpu

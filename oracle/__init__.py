@@ -59,6 +59,7 @@ def lib() -> ctypes.CDLL:
         L.orc_stationary_1d.restype = c_int
         L.orc_threads.restype = c_int
         L.orc_set_threads.argtypes = [c_int]
+        L.orc_set_record_tolerance.argtypes = [c_p, c_d]
         _lib = L
     return _lib
 
@@ -143,6 +144,11 @@ class Problem:
 
     def assemble_local(self):
         lib().orc_assemble_local(self.h)
+
+    def set_record_tolerance(self, tol: float) -> None:
+        """Record the CG time ("cg_to_record") and iterations ("record_iterations")
+        at which later solves first reach `tol` (0: off)."""
+        lib().orc_set_record_tolerance(self.h, tol)
 
     def solve(self, variant: int = 0, tol: float = 1e-10, maxit: int = 10000, true_residual: bool = True) -> bool:
         return bool(lib().orc_solve(self.h, variant, tol, maxit, int(true_residual)))

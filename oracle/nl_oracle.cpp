@@ -214,6 +214,10 @@ struct Problem {
     long nl_max_iterations = 100, nonlinear_iterations = 0;
     std::vector<double> initial;
     std::map<std::string, double> timings;
+    // optional checkpoint of a solve run past a looser tolerance: the CG time
+    // and iterations at which the stopping measure first reached record_tol
+    double record_tol = 0.0;
+    long record_iterations = -1;
 };
 
 bool nonlocal_model(const Problem& p) { return p.p1 < 0.999; }   // nonlocal_constants.hpp:274-280
@@ -785,6 +789,15 @@ void cg(Problem& p, const Csr& A, const std::vector<double>& b, std::vector<doub
     auto measure = [&](double rho_) { return stop_true_residual ? std::sqrt(dot(r, r)) / bnorm : std::sqrt(rho_) / bnorm; };
     p.iterations = 0;
     p.residual = measure(rho);
+    const double t_start = omp_get_wtime();
+    p.record_iterations = -1;
+    auto checkpoint = [&] {
+        if (p.record_tol > 0.0 && p.record_iterations < 0 && p.residual <= p.record_tol) {
+            p.record_iterations = p.iterations;
+            p.timings["cg_to_record"] = omp_get_wtime() - t_start;
+        }
+    };
+    checkpoint();
     while (p.iterations < maxit && p.residual > tol) {
         sym_spmv(A, pv, z);
         const double nu = rho / dot(pv, z);
@@ -796,6 +809,7 @@ void cg(Problem& p, const Csr& A, const std::vector<double>& b, std::vector<doub
         for (size_t i = 0; i < n; ++i) pv[i] = z[i] + mu * pv[i];
         ++p.iterations;
         p.residual = measure(rho);
+        checkpoint();
     }
     sym_spmv(A, x, tmp);
     double s = 0; for (size_t i = 0; i < n; ++i) s += (b[i] - tmp[i]) * (b[i] - tmp[i]);
@@ -1305,6 +1319,7 @@ double orc_scalar(void* h, const char* name) {
     if (s == "ilt_shift") return p.ilt_shift;
     if (s == "threads") return omp_get_max_threads();
     if (s == "nonlinear_iterations") return double(p.nonlinear_iterations);
+    if (s == "record_iterations") return double(p.record_iterations);
     const auto it = p.timings.find(s);
     return it == p.timings.end() ? -1.0 : it->second;
 }
@@ -1414,5 +1429,9 @@ int orc_stationary_1d(i64 elements, int order, double length, double r, double p
 
 int orc_threads() { return omp_get_max_threads(); }
 void orc_set_threads(int n) { omp_set_num_threads(n); }
+
+// records the CG time and iteration count at which the next solves' stopping
+// measure first reaches `tol` (0 switches it off)
+void orc_set_record_tolerance(void* h, double tol) { static_cast<Problem*>(h)->record_tol = tol; }
 
 } // extern "C"

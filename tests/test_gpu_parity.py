@@ -191,6 +191,27 @@ def test_mixed_precision_solution(golden):
 
 
 @pytest.mark.parametrize("name", ["b12_fastpoly", "s6_exp_ortho_jitter"])
+def test_symmetric_fp32_spmv(lib, name):
+    """The mixed solve with the FP32 SpMV reading only the strictly upper part
+    (NLGPU_OPTION_FP32_SYMMETRIC, shared-memory scatter of the transposed
+    entries) reaches the reference's solution like the full-row SpMV, with the
+    same iteration count up to the order of its atomic additions."""
+    fx = gc.load(name)
+    runs = []
+    for symmetric in (0, 1):
+        pb = gpu_problem(fx)
+        lib.check(lib.load().nlgpu_set_option(pb.handle, lib.OPTION_FP32_SYMMETRIC, symmetric))
+        if fx["config"].get("local_weight", 1) < 0.999:
+            pb.find_neighbours(fx["config"].get("strategy", "MAX"))
+        t, rep = pb.stationary(tolerance=1e-13, max_iterations=50000, precision="mixed")
+        assert rep.fp32_symmetric == symmetric
+        assert rep.nnz_fp32 == (rep.nnz_inner - pb.n_nodes if symmetric else rep.nnz_solver)
+        assert rel(t, fx["temperature"]) < SOLUTION_RTOL, symmetric
+        runs.append(rep.iterations)
+    assert abs(runs[0] - runs[1]) <= max(3, runs[0] // 20), runs
+
+
+@pytest.mark.parametrize("name", ["b12_fastpoly", "s6_exp_ortho_jitter"])
 def test_tma_sweeps_match_global_sweeps(lib, name):
     """The TMA-fed shared-memory triangular sweeps compute what the global-memory
     sweeps compute (same entries in the same order; the two assemblies differ
