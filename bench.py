@@ -57,7 +57,7 @@ METHODS = {"learned": ("mixed", "illt_learned", 0), "mixed": ("mixed", "illt", 0
            "mixed_exact": ("mixed", "illt", -1), "plain": ("fp64", "illt", 0)}
 METHOD_NAMES = {"learned": "mixed-precision FCG with ILLT + learned message-passing correction",
                 "mixed": "mixed-precision FCG with ILLT (learned correction gated off: it did not beat ILLT alone)"}
-LEARNED_TRAINING = dict(right_hand_sides=4, epochs=20, batch=4, learning_rate=2e-3, seed=0)
+LEARNED_TRAINING = dict(right_hand_sides=2, epochs=20, batch=4, learning_rate=2e-3, seed=0)
 METRIC_TOLERANCE = 1e-10      # the metric's residual
 REFERENCE_TOLERANCE = 1e-13   # the FP64 solve the nodal error is measured against
 NODAL_ERROR_BAR = 1e-9
@@ -207,9 +207,12 @@ def cpu_solve(w, mesh, tolerance: float, record_tolerance: float = 0.0):
     et = oracle.BILINEAR if w["element"] == "bilinear" else oracle.SERENDIPITY
     inf = {"fast_polynomial": oracle.INF_FAST_POLYNOMIAL, "exponential": oracle.INF_EXPONENTIAL}[w["model"]["influence"]]
     cond = tuple(w["model"]["conductivity"])
+    # the same kernel parameters as the GPU model (thermal.Model2D: n = p = 2, q = 1/2
+    # for the exponential kernel, 1 otherwise)
+    q = 0.5 if w["model"]["influence"] == "exponential" else 1.0
     t0 = time.perf_counter()
     p = oracle.Problem(et, mesh.nodes, mesh.elements)
-    p.set_model(influence=inf, radius=w["model"]["radius"], local_weight=w["model"]["local_weight"],
+    p.set_model(influence=inf, n=2, p=2, q=q, radius=w["model"]["radius"], local_weight=w["model"]["local_weight"],
                 cond_kind=len(cond) - 1, cond=cond + (0.0,) * (3 - len(cond)))
     for group, kind, value in w["bcs"]:
         p.add_boundary(oracle.BC_TEMPERATURE if kind == "temperature" else oracle.BC_FLUX, mesh.boundaries[group], value)

@@ -41,21 +41,21 @@ enum {
     NLGPU_ERR_TIMEOUT = 8       /* a bounded device-side wait gave up */
 };
 
-/* element_2d_t numbering (libraries/mesh/mesh_2d/elements_set.hpp:231-237) */
+/* element_2d_t numbering (libraries/mesh/mesh_2d/elements_set.hpp:22-28) */
 enum { NLGPU_BILINEAR = 2, NLGPU_QUADRATIC_SERENDIPITY = 3 };
 
 /* influence kinds (libraries/solvers/solver_2d/influence_functions_2d.hpp:39-148) */
 enum { NLGPU_INFLUENCE_CONSTANT = 0, NLGPU_INFLUENCE_POLYNOMIAL = 1,
        NLGPU_INFLUENCE_EXPONENTIAL = 2, NLGPU_INFLUENCE_FAST_POLYNOMIAL = 3 };
 
-/* conductivity kinds (libraries/solvers/solver_2d/thermal/thermal_parameters_2d.hpp:176-192);
- * anisotropic components are ordered XX, YY, XY (libraries/constants/nonlocal_constants.hpp:262) */
+/* conductivity kinds (libraries/solvers/solver_2d/thermal/thermal_parameters_2d.hpp:8-23);
+ * anisotropic components are ordered XX, YY, XY (libraries/constants/nonlocal_constants.hpp:9) */
 enum { NLGPU_CONDUCTIVITY_ISOTROPIC = 0, NLGPU_CONDUCTIVITY_ORTHOTROPIC = 1, NLGPU_CONDUCTIVITY_ANISOTROPIC = 2 };
 
-/* diameter_expanding_strategy (libraries/mesh/mesh_2d/find_neighbours.hpp:357) */
+/* diameter_expanding_strategy (libraries/mesh/mesh_2d/find_neighbours.hpp:7) */
 enum { NLGPU_EXPAND_NO = 0, NLGPU_EXPAND_MAX = 1, NLGPU_EXPAND_MIN = 2, NLGPU_EXPAND_MEAN = 3 };
 
-/* assemble_part (libraries/solvers/solver_2d/base/matrix_assembler_2d.hpp:301-305) */
+/* assemble_part (libraries/solvers/solver_2d/base/matrix_assembler_2d.hpp:15-19) */
 enum { NLGPU_PART_LOCAL = 0, NLGPU_PART_FULL = 2 };
 
 /* boundary condition kinds (thermal_boundary_conditions_2d.hpp:9-98): temperature_2d,
@@ -82,7 +82,7 @@ enum { NLGPU_PRECISION_FP64 = 0, NLGPU_PRECISION_MIXED = 1 };
 #define NLGPU_DEFAULT_TRIANGULAR_SWEEPS 6
 #define NLGPU_EXACT_TRIANGULAR_SWEEPS (-1)
 
-/* Nonlocal model of one material: model_parameters<2, T> (equation_parameters.hpp:251-257)
+/* Nonlocal model of one material: model_parameters<2, T> (equation_parameters.hpp:18-24)
  * plus its influence function and constant conductivity (parameter_2d). */
 typedef struct nlgpu_model_2d {
     int influence;            /* NLGPU_INFLUENCE_* */
@@ -149,7 +149,7 @@ int nlgpu_synchronize(nlgpu_ctx* ctx);
 int nlgpu_mesh_2d(nlgpu_ctx* ctx, int element_type, int64_t n_nodes, const double* nodes,
                   int64_t n_elements, const int64_t* elements);
 /* Quadrature data as mesh_2d stores it: coordinates [e][q][2], |J| [e][q],
- * derivatives dN.adj(J) [e][i][q][2] (mesh_container_2d_utils.hpp:385-408).
+ * derivatives dN.adj(J) [e][i][q][2] (mesh_container_2d_utils.hpp:101-123).
  * Any pointer may be NULL. */
 int nlgpu_get_quadrature(nlgpu_ctx* ctx, double* qcoords, double* jacobians, double* derivatives);
 /* Element basis tables: qN, qNxi, qNeta [i][q], weights [q], N_i(0,0) [i]
@@ -208,12 +208,12 @@ int nlgpu_renumbering(nlgpu_ctx* ctx, const int64_t* permutation);
 int nlgpu_set_model_2d(nlgpu_ctx* ctx, const nlgpu_model_2d* model);
 /* Spatially varying isotropic conductivity, one value per quadrature point
  * [e][q] (evaluate_conductivity.hpp:9-48).  With a nonlocal model this makes
- * the problem non-symmetric (problem_settings.hpp:252-254). */
+ * the problem non-symmetric (problem_settings.hpp:32-34). */
 int nlgpu_set_conductivity_field(nlgpu_ctx* ctx, const double* values);
 /* Heat capacity and density for the nonstationary solver (parameter_2d). */
 int nlgpu_set_capacity(nlgpu_ctx* ctx, double capacity, double density);
 
-/* ---- neighbours: mesh::find_neighbours (find_neighbours.hpp:469-510) ------- */
+/* ---- neighbours: mesh::find_neighbours (find_neighbours.hpp:120-160) ------- */
 /* Runs the bucketed centre-distance search with the widened radius.  Outputs
  * (may be NULL): the widened radii [2] and the total number of pairs. */
 int nlgpu_find_neighbours(nlgpu_ctx* ctx, int strategy, double* search_radius, int64_t* pairs);
@@ -224,7 +224,7 @@ int nlgpu_get_neighbours(nlgpu_ctx* ctx, int64_t* offsets, int64_t* list);
 /* One boundary group: n_edges line elements of nodes_per_edge (2 or 3) nodes,
  * local order (end, [middle,] end).  kind NLGPU_BC_TEMPERATURE with a constant
  * value (node_values may give one value per listed node instead), or
- * NLGPU_BC_FLUX with a constant flux (thermal_boundary_conditions_2d.hpp:271-301).
+ * NLGPU_BC_FLUX with a constant flux (thermal_boundary_conditions_2d.hpp:25-39).
  * Groups apply in the order added; a node in two temperature groups keeps the
  * first non-zero value (boundary_condition_first_kind_2d.hpp:16-26). */
 int nlgpu_add_boundary_2d(nlgpu_ctx* ctx, int kind, int64_t n_edges, int nodes_per_edge,
@@ -236,7 +236,7 @@ int nlgpu_add_boundary_2d(nlgpu_ctx* ctx, int kind, int64_t n_edges, int nodes_p
  *                           the matrix (convection_condition_2d.hpp:11-31);
  *   NLGPU_BC_RADIATION      emissivity eps: sigma eps T^4 leaves through the edges,
  *                           solved by the reference's fixed-point loop
- *                           (radiation_condition_2d.hpp:91-135,
+ *                           (radiation_condition_2d.hpp:59-104,
  *                           stationary_heat_equation_solver_2d.hpp:66-116);
  *   NLGPU_BC_COMBINED_FLUX  all three (combined_flux_2d).
  * A stationary problem whose groups are all NLGPU_BC_FLUX (or that has none) is
@@ -302,7 +302,7 @@ int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, do
 /* ---- slae::conjugate_gradient on caller matrices (conjugate_gradient.hpp:15-79)
  * A: upper CSR of a symmetric matrix with the diagonal first in each row;
  * optional ILLT preconditioner built from P (upper CSR, same size), the
- * eigen_ILLT_preconditioner of eigen_preconditioner.hpp:136-137.
+ * eigen_ILLT_preconditioner of eigen_preconditioner.hpp:57.
  * x0 may be NULL (zero start).  Stops when |b - Ax| / |b| <= tolerance. */
 int nlgpu_cg_solve(nlgpu_ctx* ctx, int64_t n, const int64_t* a_rowptr, const int64_t* a_col,
                    const double* a_val, const int64_t* p_rowptr, const int64_t* p_col,
@@ -398,6 +398,47 @@ int nlgpu_cg_solve_noalloc(void* stream, int64_t n, const int64_t* d_rowptr, con
                            const double* d_val, const double* d_b, double* d_x, double tolerance,
                            int64_t max_iterations, int64_t* iterations, double* residual);
 
+/* ---- equilibrium_equation (mechanical/equilibrium_equation_2d.hpp:19-60):
+ * nonlocal plane elasticity, two degrees of freedom per node.  The mesh,
+ * neighbours and the nonlocal model (influence, radii, p1 of
+ * nlgpu_set_model_2d; its conductivity is not used) are the context's.
+ * Rows and columns of the stiffness matrices are 2 node + component
+ * (component 0 = x, 1 = y), as matrix_assembler_2d<T, I, J, 2> numbers them.
+ *
+ * nlgpu_set_elastic_2d replaces raw_mechanical_parameters' elastic part with
+ * constant parameters and forms the Hooke matrix as elastic_parameters.hpp's
+ * hooke() does: NLGPU_ELASTIC_ISOTROPIC {E, nu}; NLGPU_ELASTIC_ORTHOTROPIC
+ * {E_x, E_y, nu_x, nu_y, G}; NLGPU_ELASTIC_ANISOTROPIC {E_x, E_y, nu_x, nu_y,
+ * G, angle} (the orthotropic matrix rotated by `angle`).  hooke_out (6
+ * values or NULL) receives h11, h12, h66, h22, h16, h26. */
+enum { NLGPU_ELASTIC_ISOTROPIC = 0, NLGPU_ELASTIC_ORTHOTROPIC = 1, NLGPU_ELASTIC_ANISOTROPIC = 2 };
+int nlgpu_set_elastic_2d(nlgpu_ctx* ctx, int kind, const double* parameters, double* hooke_out);
+/* mechanical_boundaries_conditions_2d: one boundary group (line elements as in
+ * nlgpu_add_boundary_2d) with a condition per component: NLGPU_MECH_NONE,
+ * NLGPU_MECH_DISPLACEMENT (displacement_2d, first kind) or
+ * NLGPU_MECH_PRESSURE (pressure_2d, second kind) with its constant value. */
+enum { NLGPU_MECH_NONE = 0, NLGPU_MECH_DISPLACEMENT = 1, NLGPU_MECH_PRESSURE = 2 };
+int nlgpu_add_mechanical_boundary_2d(nlgpu_ctx* ctx, int64_t n_edges, int nodes_per_edge, const int64_t* edges,
+                                     int kind_x, double value_x, int kind_y, double value_y);
+int nlgpu_clear_mechanical_boundaries(nlgpu_ctx* ctx);
+/* stiffness_matrix::compute (stiffness_matrix_2d.hpp:176-197) of NLGPU_PART_FULL
+ * (inner and bound, with the right-hand side: pressure integrals, then
+ * f -= K_bound u_D, f[D] = u_D) or NLGPU_PART_LOCAL (p1 x the local
+ * stiffness, the ILLT's matrix). */
+int nlgpu_stiffness_matrix_2d(nlgpu_ctx* ctx, int part, int64_t* nnz_inner, int64_t* nnz_bound);
+/* CSR of NLGPU_MATRIX_INNER / _BOUND / _LOCAL of the stiffness (2 n rows;
+ * rowptr [2n + 1], then col / val of rowptr[2n] entries; pass NULL for what is
+ * not wanted) and the right-hand side [2n] after / before the first kind. */
+int nlgpu_get_stiffness_matrix(nlgpu_ctx* ctx, int which, int64_t* rowptr, int64_t* col, double* val);
+int nlgpu_get_mechanical_rhs(nlgpu_ctx* ctx, double* rhs, double* rhs_init);
+/* equilibrium_equation: assembles (FULL), then solves with CG and the ILLT of
+ * the LOCAL stiffness (options->preconditioner NLGPU_PRECONDITIONER_ILLT; the
+ * reference uses it for a nonlocal model and the identity otherwise; an ILLT
+ * that fails falls back to the identity) in FP64 or the mixed precision of
+ * the thermal solve.  displacement [2 n]: u_x, u_y per node. */
+int nlgpu_equilibrium_equation_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* displacement,
+                                  nlgpu_solve_report* report);
+
 /* ---- nonstationary_heat_equation_solver_2d (nonstationary_heat_equation_solver_2d.hpp:16-106)
  * compute: assembles dt*K + C (unit Dirichlet diagonal) for the current mesh,
  * model and boundary groups; initial temperature [n_nodes] or NULL (zero).
@@ -438,6 +479,25 @@ int nlgpu_batch_temperature(nlgpu_batch* batch, int64_t index, double* temperatu
 int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double length, double radius,
                         double local_weight, int influence, double conductivity, double t_left,
                         double q_right, int sin_source, double* temperature);
+
+/* ---- nonstationary_heat_equation_solver_1d (nonstationary_heat_equation_solver_1d.hpp:24-259)
+ * compute: one segment [0, length] as nlgpu_stationary_1d, constant capacity
+ * and density, implicit Euler step time_step; left_kind / right_kind
+ * NLGPU_BC_TEMPERATURE or NLGPU_BC_FLUX; initial_temperature [n] or NULL
+ * (zero), n = elements * order + 1.  Assembles dt K + C (C the capacity
+ * matrix; a temperature end's row and column routed out with a unit
+ * diagonal, as the reference) and factors it once.
+ * step: calc_step with the ends' values (temperature or flux as set at
+ * compute) and the sin(pi x) source when sin_source; f = dt (flux + source) +
+ * C T_prev, first kind, solve; temperature [n] receives the new temperature
+ * (or NULL).  temperature: the current temperature. */
+int nlgpu_nonstationary_1d_compute(nlgpu_ctx* ctx, int64_t elements, int order, double length, double radius,
+                                   double local_weight, int influence, double conductivity, double capacity,
+                                   double density, double time_step, int left_kind, int right_kind,
+                                   const double* initial_temperature, int64_t* nodes);
+int nlgpu_nonstationary_1d_step(nlgpu_ctx* ctx, double left_value, double right_value, int sin_source,
+                                double* temperature);
+int nlgpu_nonstationary_1d_temperature(nlgpu_ctx* ctx, double* temperature);
 
 /* ---- measurement utilities (no counterpart in the reference) ---------------
  * Events recorded on the context's stream (slots 0..63) and the device time

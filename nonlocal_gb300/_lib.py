@@ -26,6 +26,9 @@ CONDUCTIVITY_KIND = {1: 0, 2: 1, 3: 2}
 EXPAND = {"NO": 0, "MAX": 1, "MIN": 2, "MEAN": 3}
 PART_LOCAL, PART_FULL = 0, 2
 BC_TEMPERATURE, BC_FLUX, BC_CONVECTION, BC_RADIATION, BC_COMBINED_FLUX = 0, 1, 2, 3, 4
+ELASTIC = {"isotropic": 0, "orthotropic": 1, "anisotropic": 2}
+MECH_NONE, MECH_DISPLACEMENT, MECH_PRESSURE = 0, 1, 2
+MECH_CONDITION = {None: MECH_NONE, "displacement": MECH_DISPLACEMENT, "pressure": MECH_PRESSURE}
 MATRIX_INNER, MATRIX_BOUND, MATRIX_LOCAL = 0, 1, 2
 PRECONDITIONER = {"identity": 0, "illt": 1, "illt_learned": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
@@ -137,6 +140,17 @@ SIGNATURES = {
     "nlgpu_nonstationary_2d_compute": (c_int, [c_p, c_d, c_p]),
     "nlgpu_nonstationary_2d_step": (c_int, [c_p, c_d, c_p, c_d, c_i64, c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),
+    "nlgpu_nonstationary_1d_compute": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_d, c_int,
+                                               c_int, c_p, ctypes.POINTER(c_i64)]),
+    "nlgpu_nonstationary_1d_step": (c_int, [c_p, c_d, c_d, c_int, c_p]),
+    "nlgpu_nonstationary_1d_temperature": (c_int, [c_p, c_p]),
+    "nlgpu_set_elastic_2d": (c_int, [c_p, c_int, c_p, c_p]),
+    "nlgpu_add_mechanical_boundary_2d": (c_int, [c_p, c_i64, c_int, c_p, c_int, c_d, c_int, c_d]),
+    "nlgpu_clear_mechanical_boundaries": (c_int, [c_p]),
+    "nlgpu_stiffness_matrix_2d": (c_int, [c_p, c_int, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)]),
+    "nlgpu_get_stiffness_matrix": (c_int, [c_p, c_int, c_p, c_p, c_p]),
+    "nlgpu_get_mechanical_rhs": (c_int, [c_p, c_p, c_p]),
+    "nlgpu_equilibrium_equation_2d": (c_int, [c_p, ctypes.POINTER(SolveOptions), c_p, ctypes.POINTER(SolveReport)]),
     "nlgpu_cg_solve_noalloc": (c_int, [c_p, c_i64, c_p, c_p, c_p, c_p, c_p, c_d, c_i64, ctypes.POINTER(c_i64),
                                        ctypes.POINTER(c_d)]),
     "nlgpu_set_option": (c_int, [c_p, c_int, c_int]),

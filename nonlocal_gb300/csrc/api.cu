@@ -95,7 +95,7 @@ void neumann_prepare(Ctx& c) {
 void build_inner(Ctx& c) {
     NL_REQUIRE(c.mesh_ready && c.model_ready, NLGPU_ERR_STATE, "mesh and model must be set before assembly");
     ensure_boundary(c);
-    c.symmetric = !(c.model.nonlocal() && c.cond_field.n);   // problem_settings::is_symmetric (problem_settings.hpp:252-254)
+    c.symmetric = !(c.model.nonlocal() && c.cond_field.n);   // problem_settings::is_symmetric (problem_settings.hpp:32-34)
     if (c.model.nonlocal()) ensure_neighbours(c);
     build_patterns(c, !c.model.nonlocal(), c.symmetric, c.inner, &c.bound, &c.full, &c.full_from_upper);
     c.ff_assembly = c.assembly_precision == NLGPU_ASSEMBLY_FF;
@@ -1131,6 +1131,170 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
         stationary_1d(*ctx, elements, order, length, radius, local_weight, influence, conductivity, t_left, q_right,
                       sin_source != 0, temperature);
     });
+}
+
+int nlgpu_nonstationary_1d_compute(nlgpu_ctx* ctx, int64_t elements, int order, double length, double radius,
+                                   double local_weight, int influence, double conductivity, double capacity,
+                                   double density, double time_step, int left_kind, int right_kind,
+                                   const double* initial_temperature, int64_t* nodes) {
+    if (!ctx || elements <= 0 || (order != 1 && order != 2) || !(length > 0.0) || !(time_step > 0.0))
+        return NLGPU_ERR_ARG;
+    return guarded([&] {
+        nonstationary_1d_compute(*ctx, elements, order, length, radius, local_weight, influence, conductivity,
+                                 capacity, density, time_step, left_kind, right_kind, initial_temperature);
+        if (nodes) *nodes = nonstationary_1d_nodes(*ctx);
+    });
+}
+
+int nlgpu_nonstationary_1d_step(nlgpu_ctx* ctx, double left_value, double right_value, int sin_source,
+                                double* temperature) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] { nonstationary_1d_step(*ctx, left_value, right_value, sin_source != 0, temperature); });
+}
+
+int nlgpu_nonstationary_1d_temperature(nlgpu_ctx* ctx, double* temperature) {
+    if (!ctx || !temperature) return NLGPU_ERR_ARG;
+    return guarded([&] { nonstationary_1d_temperature(*ctx, temperature); });
+}
+
+int nlgpu_set_elastic_2d(nlgpu_ctx* ctx, int kind, const double* prm, double* hooke_out) {
+    if (!ctx || !prm) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Elastic& el = ctx->el;
+        double h[6] = {0, 0, 0, 0, 0, 0};   // h11 h12 h66 h22 h16 h26
+        if (kind == NLGPU_ELASTIC_ISOTROPIC) {
+            // isotropic_elastic_parameters::hooke (elastic_parameters.hpp:64-70)
+            const double E = prm[0], nu = prm[1];
+            NL_REQUIRE(E > 0.0 && nu > -1.0 && nu < 1.0, NLGPU_ERR_ARG, "isotropic: E > 0, -1 < nu < 1");
+            const double v = E / (1.0 - nu * nu);
+            h[0] = v; h[1] = nu * v; h[2] = 0.5 * v * (1.0 - nu); h[3] = v;
+        } else if (kind == NLGPU_ELASTIC_ORTHOTROPIC || kind == NLGPU_ELASTIC_ANISOTROPIC) {
+            // orthotropic_elastic_parameters::hooke (elastic_parameters.hpp:84-90)
+            const double Ex = prm[0], Ey = prm[1], nux = prm[2], nuy = prm[3], G = prm[4];
+            NL_REQUIRE(Ex > 0.0 && Ey > 0.0 && G > 0.0 && nux * nuy < 1.0, NLGPU_ERR_ARG,
+                       "orthotropic: E_x, E_y, G > 0 and nu_x nu_y < 1");
+            const double v = 1.0 / (1.0 - nux * nuy);
+            const double o11 = Ex * v, o12 = Ex * nuy * v, o66 = G, o22 = Ey * v;
+            if (kind == NLGPU_ELASTIC_ORTHOTROPIC) {
+                h[0] = o11; h[1] = o12; h[2] = o66; h[3] = o22;
+            } else {
+                // anisotropic_elastic_parameters::rotate (elastic_parameters.hpp:100-122)
+                const double a2 = 2.0 * prm[5];
+                const double s2 = std::sin(a2), c2 = std::cos(a2);
+                const double c4 = 0.125 * (c2 * c2 - s2 * s2);
+                const double diff = o11 - o22, core = o11 + o22 - 2.0 * o12 - 4.0 * o66;
+                const double plus = core * (c4 + 0.125), minus = core * (0.125 - c4);
+                const double cdiff = diff * (c2 + 0.5), minor = core * c2, s2q = 0.25 * s2;
+                h[0] = plus + 0.5 * (o12 + o22 + cdiff) + o66;
+                h[1] = minus + o12;
+                h[2] = minus + o66;
+                h[3] = plus + 0.5 * (o12 + o11 - cdiff) + o66;
+                h[4] = s2q * (diff + minor);
+                h[5] = s2q * (diff - minor);
+            }
+        } else {
+            NL_REQUIRE(false, NLGPU_ERR_ARG, "unknown elastic parameters kind");
+        }
+        el.kind = kind;
+        for (int k = 0; k < 6; ++k) el.h[k] = h[k];
+        if (hooke_out) for (int k = 0; k < 6; ++k) hooke_out[k] = h[k];
+        el.hooke_set = true;
+        el.assembled = false;
+        el.local_ready = false;
+    });
+}
+
+int nlgpu_add_mechanical_boundary_2d(nlgpu_ctx* ctx, int64_t n_edges, int nodes_per_edge, const int64_t* edges,
+                                     int kind_x, double value_x, int kind_y, double value_y) {
+    if (!ctx || !edges || n_edges < 0) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.mesh_ready, NLGPU_ERR_STATE, "no mesh");
+        NL_REQUIRE(nodes_per_edge == 2 || nodes_per_edge == 3, NLGPU_ERR_UNSUPPORTED, "boundary edges have 2 or 3 nodes");
+        for (const int k : {kind_x, kind_y})
+            NL_REQUIRE(k >= NLGPU_MECH_NONE && k <= NLGPU_MECH_PRESSURE, NLGPU_ERR_ARG, "unknown mechanical condition");
+        MechanicalGroup g;
+        g.nen = nodes_per_edge; g.n_edges = n_edges;
+        g.kind[0] = kind_x; g.kind[1] = kind_y; g.value[0] = value_x; g.value[1] = value_y;
+        std::vector<int32_t> e(size_t(n_edges * nodes_per_edge));
+        for (size_t k = 0; k < e.size(); ++k) {
+            NL_REQUIRE(edges[k] >= 0 && edges[k] < c.n_nodes, NLGPU_ERR_ARG, "boundary node out of range");
+            e[k] = int32_t(edges[k]);
+        }
+        g.edges.upload(e.data(), e.size(), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        c.el.groups.push_back(std::move(g));
+        c.el.assembled = false;
+        c.el.local_ready = false;
+    });
+}
+
+int nlgpu_clear_mechanical_boundaries(nlgpu_ctx* ctx) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    ctx->el.groups.clear();
+    ctx->el.assembled = false;
+    ctx->el.local_ready = false;
+    return NLGPU_OK;
+}
+
+int nlgpu_stiffness_matrix_2d(nlgpu_ctx* ctx, int part, int64_t* nnz_inner, int64_t* nnz_bound) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(part == NLGPU_PART_FULL || part == NLGPU_PART_LOCAL, NLGPU_ERR_ARG, "part FULL or LOCAL");
+        if (part == NLGPU_PART_FULL && c.model.nonlocal()) ensure_neighbours(c);
+        elastic_assemble(c, part == NLGPU_PART_LOCAL);
+        const Csr& m = part == NLGPU_PART_LOCAL ? c.el.local : c.el.inner;
+        if (nnz_inner) *nnz_inner = m.nnz;
+        if (nnz_bound) *nnz_bound = part == NLGPU_PART_LOCAL ? 0 : c.el.bound.nnz;
+    });
+}
+
+int nlgpu_get_stiffness_matrix(nlgpu_ctx* ctx, int which, int64_t* rowptr, int64_t* col, double* val) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(which >= NLGPU_MATRIX_INNER && which <= NLGPU_MATRIX_LOCAL, NLGPU_ERR_ARG, "unknown matrix");
+        if (which == NLGPU_MATRIX_LOCAL) {
+            NL_REQUIRE(c.el.local_ready, NLGPU_ERR_STATE, "LOCAL stiffness not assembled");
+            download_csr(c, c.el.local, rowptr, col, val);
+        } else {
+            NL_REQUIRE(c.el.assembled, NLGPU_ERR_STATE, "FULL stiffness not assembled");
+            download_csr(c, which == NLGPU_MATRIX_INNER ? c.el.inner : c.el.bound, rowptr, col, val);
+        }
+    });
+}
+
+int nlgpu_get_mechanical_rhs(nlgpu_ctx* ctx, double* rhs, double* rhs_init) {
+    if (!ctx) return NLGPU_ERR_ARG;
+    return guarded([&] {
+        Ctx& c = *ctx;
+        NL_REQUIRE(c.el.assembled, NLGPU_ERR_STATE, "FULL stiffness not assembled");
+        const size_t rows = size_t(2 * c.n_nodes);
+        if (rhs) c.el.rhs.download(rhs, rows, c.stream);
+        if (rhs_init) c.el.rhs_init.download(rhs_init, rows, c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int nlgpu_equilibrium_equation_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* displacement,
+                                  nlgpu_solve_report* report) {
+    if (!ctx || !options || !displacement) return NLGPU_ERR_ARG;
+    int conv_status = NLGPU_OK;
+    const int rc = guarded([&] {
+        Ctx& c = *ctx;
+        const auto t0 = std::chrono::steady_clock::now();
+        if (report) *report = nlgpu_solve_report{};
+        if (c.model.nonlocal()) ensure_neighbours(c);
+        elastic_assemble(c, false);
+        if (report) report->seconds_assembly = seconds(t0);
+        const CgResult r = elastic_solve(c, *options, report);
+        c.el.displacement.download(displacement, size_t(2 * c.n_nodes), c.stream);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        if (report) report->seconds_total = seconds(t0);
+        if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
+    });
+    return rc != NLGPU_OK ? rc : conv_status;
 }
 
 int nlgpu_cg_solve_noalloc(void* stream, int64_t n, const int64_t* d_rowptr, const int32_t* d_col, const double* d_val,

@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
 
 // Local integrands, one thread per (e, i, j): conductivity
 // (integrate_local, conductivity_matrix_2d.hpp:106-130) or capacity
-// (integrate_basic_pair, heat_capacity_matrix_2d.hpp:137-144).
+// (integrate_basic_pair, heat_capacity_matrix_2d.hpp:30-37).
 __global__ void k_assemble_local(i64 E, int nen, int nq, const int32_t* __restrict__ elems,
                                  const double* __restrict__ jac, const double* __restrict__ deriv,
                                  const uint8_t* __restrict__ is_inner, const double* __restrict__ cond_field,

@@ -1,5 +1,5 @@
 // Boundary conditions and the right-hand side of the stationary problem:
-//   * is_inner: nodes of temperature groups are Dirichlet (solvers_utils.hpp:179-188);
+//   * is_inner: nodes of temperature groups are Dirichlet (solvers_utils.hpp:31-40);
 //   * Dirichlet values, first non-zero value wins (boundary_condition_first_kind_2d.hpp:16-26);
 //   * flux integrals over boundary line elements (boundary_condition_second_kind_2d.hpp:12-33);
 //   * volume source integrals (right_part_2d.hpp:10-35);
@@ -106,9 +106,10 @@ void boundary_vectors(Ctx& ctx) {
     ctx.bc_ready = true;
 }
 
-void apply_first_kind(Ctx& ctx, const Csr& bound, const double* rhs_in, double* rhs_out, const double* x_dirichlet) {
+void apply_first_kind(Ctx& ctx, const Csr& bound, const double* rhs_in, double* rhs_out, const double* x_dirichlet,
+                      const uint8_t* is_inner) {
     NL_LAUNCH(k_first_kind, grid_for(bound.rows * 32, 256, 152 * 64), 256, 0, ctx.stream, bound.rows, bound.rowptr.p,
-              bound.col.p, bound.val.p, rhs_in, x_dirichlet, ctx.is_inner.p, rhs_out);
+              bound.col.p, bound.val.p, rhs_in, x_dirichlet, is_inner ? is_inner : ctx.is_inner.p, rhs_out);
 }
 
 }  // namespace nlgpu

@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <array>
 #include <functional>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -124,7 +125,7 @@ struct Basis {
 Basis make_basis(int element_type);
 
 // Line elements of boundary groups: 2 nodes / Gauss-1, 3 nodes / Gauss-2
-// (vtk_elements_set.hpp:354-363).
+// (vtk_elements_set.hpp:43-52).
 struct Basis1d {
     int nen = 0, nq = 0;
     double qN[3 * 2], qNxi[3 * 2], w[2];
@@ -137,7 +138,7 @@ struct Model {
     double q = 1.0, r[2] = {0.1, 0.1}, inv_r[2] = {10.0, 10.0}, p1 = 1.0, norm = 1.0;
     int cond_kind = NLGPU_CONDUCTIVITY_ISOTROPIC;
     double cond[3] = {1.0, 0.0, 0.0};
-    bool nonlocal() const noexcept { return p1 < 0.999; }   // nonlocal_constants.hpp:274-280
+    bool nonlocal() const noexcept { return p1 < 0.999; }   // nonlocal_constants.hpp:22-37
 };
 Model make_model(const nlgpu_model_2d& m);
 
@@ -320,6 +321,31 @@ struct MixedWork {
     ~MixedWork() { if (chunk) cudaGraphExecDestroy(chunk); }
 };
 
+// Nonlocal plane elasticity, DoF = 2 (elastic.cu): Hooke coefficients, the
+// boundary groups per component, and the stiffness system over 2 n rows
+// (row 2 node + component, as the reference numbers them).
+struct MechanicalGroup {
+    int nen = 2;
+    i64 n_edges = 0;
+    dbuf<int32_t> edges;
+    int kind[2] = {0, 0};        // NLGPU_MECH_NONE / DISPLACEMENT / PRESSURE per component
+    double value[2] = {0.0, 0.0};
+};
+struct Elastic {
+    bool hooke_set = false;
+    int kind = 0;
+    double h[6] = {0, 0, 0, 0, 0, 0};   // h11 h12 h66 h22 h16 h26
+    std::vector<MechanicalGroup> groups;
+    dbuf<uint8_t> is_inner;      // [2n] per degree of freedom
+    dbuf<double> x_dirichlet, rhs_init, rhs, displacement;
+    Csr inner, bound, full, local;
+    dbuf<i64> full_from_upper;
+    IncompleteCholesky ilt;
+    bool assembled = false, local_ready = false;
+};
+
+struct OneDimState;   // nonstationary 1D solver state (onedim.cu)
+
 struct Ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -375,6 +401,8 @@ struct Ctx {
     IncompleteCholesky plugin_ilt;   // nlgpu_illt_compute / nlgpu_illt_solve
     bool plugin_ilt_ready = false;
     CgWork cg;
+    Elastic el;
+    std::shared_ptr<OneDimState> od;
     MixedWork mx;
     BicgWork bi;
     Mpnn mp;
@@ -418,10 +446,15 @@ void mesh_init(Ctx& ctx);
 void find_neighbours(Ctx& ctx, int strategy);
 // boundary.cu
 void boundary_vectors(Ctx& ctx);
-void apply_first_kind(Ctx& ctx, const Csr& bound, const double* rhs_in, double* rhs_out, const double* x_dirichlet);
+// is_inner: per-row inner flags (default ctx.is_inner)
+void apply_first_kind(Ctx& ctx, const Csr& bound, const double* rhs_in, double* rhs_out, const double* x_dirichlet,
+                      const uint8_t* is_inner = nullptr);
 // pattern.cu
+// is_inner: per-row inner flags (default ctx.is_inner)
 void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* bound, Csr* full,
-                    dbuf<i64>* full_from_upper);
+                    dbuf<i64>* full_from_upper, const uint8_t* is_inner = nullptr);
+// full-row entry -> entry of the same value in the upper storage (-1 for padding)
+void full_map(Ctx& ctx, const Csr& upper, const Csr& full, dbuf<i64>& map, bool symmetric);
 // assemble.cu
 void assemble_full(Ctx& ctx);
 void assemble_local(Ctx& ctx, Csr& m, double weight, int integrand);   // integrand 0 conductivity, 1 capacity
@@ -530,7 +563,17 @@ void mpnn_train(Ctx& ctx, const Csr& A, IncompleteCholesky& M, const double* b, 
 // noalloc.cu
 bool cg_solve_noalloc(cudaStream_t s, i64 n, const i64* rp, const int32_t* col, const double* val, const double* b,
                       double* x, double tolerance, i64 max_iterations, i64* iterations, double* residual);
+// elastic.cu: nonlocal plane elasticity (equilibrium_equation_2d.hpp:19-60)
+void elastic_boundaries(Ctx& ctx);
+void elastic_assemble(Ctx& ctx, bool local_part);
+CgResult elastic_solve(Ctx& ctx, const nlgpu_solve_options& o, nlgpu_solve_report* rep);
 // onedim.cu
+void nonstationary_1d_compute(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight,
+                              int influence, double conductivity, double capacity, double density, double time_step,
+                              int left_kind, int right_kind, const double* initial);
+void nonstationary_1d_step(Ctx& ctx, double left_value, double right_value, bool sin_source, double* temperature);
+void nonstationary_1d_temperature(Ctx& ctx, double* temperature);
+i64 nonstationary_1d_nodes(const Ctx& ctx);
 void stationary_1d(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight, int influence,
                    double conductivity, double t_left, double q_right, bool sin_source, double* temperature);
 

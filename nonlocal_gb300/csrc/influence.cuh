@@ -6,14 +6,14 @@
 
 namespace nlgpu {
 
-__device__ __forceinline__ double ipow(double x, int n) {   // power(T, integral) of metamath/functions/power.hpp:232-247
+__device__ __forceinline__ double ipow(double x, int n) {   // power(T, integral) of metamath/functions/power.hpp:25-40
     double r = 1.0;
     while (n > 0) { if (n & 1) { r *= x; --n; } else { x *= x; n >>= 1; } }
     return r;
 }
 
 // Influence function without its normalisation (influence_functions_2d.hpp:39-148),
-// over the powered distance of search_function.hpp:569-579 with the radii as
+// over the powered distance of search_function.hpp:29-73 with the radii as
 // inverse multipliers.
 template<int INF>
 __device__ __forceinline__ double shape(const Model& m, double dx, double dy) {

@@ -85,8 +85,8 @@ __global__ void k_quadrature(i64 E, int nen, int nq, const double* __restrict__ 
             J00 += x * dxi; J01 += x * deta; J10 += y * dxi; J11 += y * deta;
         }
         qcoord[2 * (e * nq + q)] = cx; qcoord[2 * (e * nq + q) + 1] = cy;
-        jac[e * nq + q] = fabs(J00 * J11 - J01 * J10);   // mesh_container_2d_utils.hpp:372-375
-        for (int i = 0; i < nen; ++i) {   // derivatives_in_quad (mesh_container_2d_utils.hpp:385-408)
+        jac[e * nq + q] = fabs(J00 * J11 - J01 * J10);   // mesh_container_2d_utils.hpp:88-91
+        for (int i = 0; i < nen; ++i) {   // derivatives_in_quad (mesh_container_2d_utils.hpp:101-123)
             const double dxi = b.qNxi[i * nq + q], deta = b.qNeta[i * nq + q];
             double* d = deriv + 2 * ((e * nen + i) * nq + q);
             d[0] = dxi * J11 - deta * J10;
@@ -123,7 +123,7 @@ __global__ void k_fill_node_elements(i64 E, int nen, const int32_t* __restrict__
 }
 
 // Orders each node's element list by element number (node_elements_2d,
-// mesh_container_2d_utils.hpp:302-311) and records the node's local index.
+// mesh_container_2d_utils.hpp:18-26) and records the node's local index.
 __global__ void k_sort_node_elements(i64 n, int nen, const int32_t* __restrict__ elems, const i64* __restrict__ off,
                                      int32_t* __restrict__ ne_elem, int8_t* __restrict__ ne_local) {
     for (i64 v = blockIdx.x * i64(blockDim.x) + threadIdx.x; v < n; v += i64(gridDim.x) * blockDim.x) {
@@ -151,7 +151,7 @@ Basis make_basis(int element_type) {
     Basis b{};
     b.type = element_type;
     b.nen = element_type == NLGPU_BILINEAR ? 4 : 8;
-    const int n1 = element_type == NLGPU_BILINEAR ? 2 : 3;   // vtk_elements_set.hpp:365-383
+    const int n1 = element_type == NLGPU_BILINEAR ? 2 : 3;   // vtk_elements_set.hpp:54-72
     b.nq = n1 * n1;
     double g[3], gw[3];
     gauss_rule(n1, g, gw);

@@ -1,4 +1,4 @@
-// Neighbour search of mesh::find_neighbours (libraries/mesh/mesh_2d/find_neighbours.hpp:469-510)
+// Neighbour search of mesh::find_neighbours (libraries/mesh/mesh_2d/find_neighbours.hpp:120-160)
 // for a mesh whose elements form one group.
 //
 //   1. radius widening by the element-centre distance between elements that

@@ -4,7 +4,7 @@
 //     added to the entries (row, col >= row) of the assembled matrix for every
 //     pair of nodes of a convection edge;
 //   * radiation: with the previous temperature T_q = sum_k N_k(q) T_k on the
-//     edge, stationary (radiation_condition_2d.hpp:91-135)
+//     edge, stationary (radiation_condition_2d.hpp:59-104)
 //     K(row, col >= row) -= 4 sigma eps int T_q^3 N_i N_j |J| and
 //     r_rad[row] -= sigma eps int T_q^4 N_i |J|; nonstationary
 //     (radiation_condition_2d.hpp:43-88) K += dt 4 sigma eps int T_q^3 N_i N_j |J|

@@ -3,7 +3,7 @@
 //   mesh: one segment [0, length], `elements` Lagrange elements of order 1 or 2,
 //     neighbours e +- round(r / h) inside the segment (mesh_1d.hpp:119-122, 221-232);
 //   assembly: p1 * local + (1 - p1) * nonlocal element blocks
-//     (thermal_conductivity_assembler.hpp:178-213, assebmler_base.hpp:360-404),
+//     (thermal_conductivity_assembler.hpp:64-125, assebmler_base.hpp:112-155),
 //     upper band, node 0 Dirichlet: its row goes to the bound vector, entries
 //     of column 0 in other rows are dropped, unit diagonal;
 //   right-hand side: flux at the right end, source integral, first-kind step;
@@ -13,6 +13,15 @@
 // Assembly: one thread per (element, neighbour element) pair computes the
 // (order+1)^2 block.  Factorisation: one CTA walks the diagonal; at step k
 // every thread updates part of the trailing (bandwidth x bandwidth) window.
+//
+// 1D nonstationary (nonstationary_heat_equation_solver_1d.hpp:24-259):
+// compute() assembles A = dt K + C (C the local capacity matrix c rho int N_i N_j,
+// heat_capacity_assembler.hpp:30-58) with either end a temperature (its row and
+// column routed out, unit diagonal, K's row kept as dt x bound) or a flux, and
+// factors A once (LDL^T of the band).  calc_step() forms
+// f = dt (flux + source) + C T_prev (inner entries of C only, as the
+// reference's product), applies the first kind and solves with the factor: the
+// solution the reference's ConjugateGradient reaches at machine tolerance.
 #include "common.cuh"
 
 #include <cmath>
@@ -52,6 +61,7 @@ struct Problem1d {
     int order;
     double h, jac, r, p1, lambda, norm;
     int kind;                  // 0 bell, 1 triangle, 2 normal, 3 constant
+    int fk0, fk1;              // temperature (first kind) at the left / right end
 };
 
 // influence_functions_1d.hpp:10-75
@@ -63,15 +73,26 @@ __device__ __forceinline__ double influence_1d(const Problem1d& P, double x, dou
     return d < P.r ? P.norm : 0.0;
 }
 
-__device__ __forceinline__ void band_add(const Problem1d& P, double* band, double* bound0, i64 row, i64 col, double v) {
-    if (row == 0 || col == 0) {
-        if (row == 0 && col != 0) atomicAdd(bound0 + col, v);
+// assembler_base_1d::calc_matrix (assebmler_base.hpp:121-154): entries in the
+// row or column of a first-kind end go to that end's bound vector (its row's
+// entries; the diagonal becomes 1 later) or are dropped; the rest fill the
+// upper band.  bound0 / boundN may be null (dropped).
+__device__ __forceinline__ void band_add(const Problem1d& P, double* band, double* bound0, double* boundN, i64 row,
+                                         i64 col, double v) {
+    const i64 last = P.n - 1;
+    if (P.fk0 && (row == 0 || col == 0)) {
+        if (row == 0 && col != 0 && bound0) atomicAdd(bound0 + col, v);
+        return;
+    }
+    if (P.fk1 && (row == last || col == last)) {
+        if (row == last && col != last && boundN) atomicAdd(boundN + col, v);
         return;
     }
     if (row <= col) atomicAdd(band + row * (P.bw + 1) + (col - row), v);
 }
 
-__global__ void k_assemble_1d(Problem1d P, Line L, double* __restrict__ band, double* __restrict__ bound0) {
+__global__ void k_assemble_1d(Problem1d P, Line L, double* __restrict__ band, double* __restrict__ bound0,
+                              double* __restrict__ boundN) {
     const i64 width = 2 * P.nb + 1;
     for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < P.E * width; t += i64(gridDim.x) * blockDim.x) {
         const i64 e = t / width, f = e - P.nb + t % width;
@@ -94,12 +115,12 @@ __global__ void k_assemble_1d(Problem1d P, Line L, double* __restrict__ band, do
                             inner += influence_1d(P, xl[qL], xn[qNL]) * P.lambda * L.w[qNL] * L.qNxi[j * L.nq + qNL];
                         integral += L.w[qL] * L.qNxi[i * L.nq + qL] * inner;
                     }
-                    band_add(P, band, bound0, row, col, (1.0 - P.p1) * integral);
+                    band_add(P, band, bound0, boundN, row, col, (1.0 - P.p1) * integral);
                 }
                 if (f == e) {
                     double integral = 0.0;
                     for (int q = 0; q < L.nq; ++q) integral += P.lambda * L.w[q] * L.qNxi[i * L.nq + q] * L.qNxi[j * L.nq + q];
-                    band_add(P, band, bound0, row, col, P.p1 * (integral / P.jac));
+                    band_add(P, band, bound0, boundN, row, col, P.p1 * (integral / P.jac));
                 }
             }
         }
@@ -127,11 +148,10 @@ __global__ void k_first_kind_1d(i64 n, const double* __restrict__ bound0, double
     }
 }
 
-// In-place band LDL^T (upper band: band[i*(bw+1) + (j-i)]) and the two
-// triangular solves, in one CTA.  Step k scales row k by 1/d_k after using it
-// to update the trailing window.
-__global__ void __launch_bounds__(1024) k_band_ldlt_solve(i64 n, i64 bw, double* __restrict__ band, double* __restrict__ f,
-                                                          int* __restrict__ failed) {
+// In-place band LDL^T (upper band: band[i*(bw+1) + (j-i)]) in one CTA.  Step
+// k scales row k by 1/d_k after using it to update the trailing window.
+// Returns false (and raises *failed) on a zero pivot.
+__device__ bool band_ldlt(i64 n, i64 bw, double* __restrict__ band, int* __restrict__ failed) {
     const i64 w = bw + 1;
     __shared__ double dk;
     for (i64 k = 0; k < n; ++k) {
@@ -140,7 +160,7 @@ __global__ void __launch_bounds__(1024) k_band_ldlt_solve(i64 n, i64 bw, double*
             if (dk == 0.0) *failed = 1;
         }
         __syncthreads();
-        if (dk == 0.0) return;
+        if (dk == 0.0) return false;
         const i64 m = min(bw, n - 1 - k);   // rows k+1 .. k+m
         for (i64 t = threadIdx.x; t < m * m; t += blockDim.x) {
             const i64 a = t / m + 1, b = t % m + 1;   // row k+a, col k+b
@@ -152,6 +172,107 @@ __global__ void __launch_bounds__(1024) k_band_ldlt_solve(i64 n, i64 bw, double*
         for (i64 t = threadIdx.x + 1; t <= m; t += blockDim.x) band[k * w + t] /= dk;
         __syncthreads();
     }
+    return true;
+}
+
+__global__ void __launch_bounds__(1024) k_band_ldlt(i64 n, i64 bw, double* __restrict__ band, int* __restrict__ failed) {
+    band_ldlt(n, bw, band, failed);
+}
+
+// U^T D U x = f with the factor of k_band_ldlt (unit upper U), by one warp:
+// forward U^T y = f, y /= d, backward U x = y.  Every row's dot product is
+// spread over the lanes and reduced by shuffles; __syncwarp orders each
+// solved value before the next row reads it.
+__global__ void __launch_bounds__(32) k_band_solve_warp(i64 n, i64 bw, const double* __restrict__ band,
+                                                        double* __restrict__ f) {
+    const i64 w = bw + 1;
+    const int lane = threadIdx.x;
+    for (i64 i = 1; i < n; ++i) {
+        double s = 0.0;
+        for (i64 k = max(i64(0), i - bw) + lane; k < i; k += 32) s += band[k * w + (i - k)] * f[k];
+        s = warp_sum(s);
+        if (lane == 0) f[i] -= s;
+        __syncwarp();
+    }
+    for (i64 i = lane; i < n; i += 32) f[i] /= band[i * w];
+    __syncwarp();
+    for (i64 i = n - 2; i >= 0; --i) {
+        double s = 0.0;
+        for (i64 j = i + 1 + lane; j <= min(n - 1, i + bw); j += 32) s += band[i * w + (j - i)] * f[j];
+        s = warp_sum(s);
+        if (lane == 0) f[i] -= s;
+        __syncwarp();
+    }
+}
+
+// heat_capacity_assembler_1d::integrate: c rho sum_q w_q N_i N_j |J| per
+// (element, i, j), routed as the conductivity (bound entries dropped)
+__global__ void k_capacity_1d(Problem1d P, Line L, double factor, double* __restrict__ band) {
+    for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < P.E * L.nen * L.nen; t += i64(gridDim.x) * blockDim.x) {
+        const i64 e = t / (L.nen * L.nen);
+        const int i = int(t / L.nen % L.nen), j = int(t % L.nen);
+        double integral = 0.0;
+        for (int q = 0; q < L.nq; ++q) integral += L.w[q] * L.qN[i * L.nq + q] * L.qN[j * L.nq + q];
+        band_add(P, band, nullptr, nullptr, e * P.order + i, e * P.order + j, factor * (integral * P.jac));
+    }
+}
+
+// A = dt K + C over the band, unit diagonal at first-kind ends (C too), bound vectors x dt
+__global__ void k_combine_1d(Problem1d P, double dt, double* __restrict__ a, double* __restrict__ c,
+                             double* __restrict__ bound0, double* __restrict__ boundN) {
+    const i64 w = P.bw + 1, last = P.n - 1;
+    for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < P.n * w; t += i64(gridDim.x) * blockDim.x) {
+        a[t] = dt * a[t] + c[t];
+        if (t < P.n) { bound0[t] *= dt; boundN[t] *= dt; }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (P.fk0) { a[0] = 1.0; c[0] = 1.0; }
+        if (P.fk1) { a[last * w] = 1.0; c[last * w] = 1.0; }
+    }
+}
+
+// f = second-kind ends + source integral (before the time step factor)
+__global__ void k_step_loads_1d(Problem1d P, Line L, double q_left, double q_right, bool sin_source,
+                                double* __restrict__ f) {
+    for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < P.E * L.nen; t += i64(gridDim.x) * blockDim.x) {
+        const i64 e = t / L.nen;
+        const int i = int(t % L.nen);
+        if (!sin_source) continue;
+        double integral = 0.0;
+        for (int q = 0; q < L.nq; ++q)
+            integral += L.w[q] * L.qN[i * L.nq + q] * sin(std::numbers::pi * (P.h * double(e) + (L.x[q] - (-1.0)) * P.jac));
+        atomicAdd(f + e * P.order + i, integral * P.jac);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!P.fk0) atomicAdd(f, q_left);
+        if (!P.fk1) atomicAdd(f + P.n - 1, q_right);
+    }
+}
+
+// f = dt f + C T_prev (symmetric band product), then the first kind of each
+// temperature end: f -= bound T_end, f[end] = T_end (boundary_condition_first_kind_1d.hpp)
+__global__ void k_step_rhs_1d(Problem1d P, double dt, const double* __restrict__ c, const double* __restrict__ t_prev,
+                              const double* __restrict__ bound0, const double* __restrict__ boundN, double t_left,
+                              double t_right, double* __restrict__ f) {
+    const i64 w = P.bw + 1, last = P.n - 1;
+    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < P.n; i += i64(gridDim.x) * blockDim.x) {
+        double s = 0.0;
+        for (i64 j = max(i64(0), i - P.bw); j < i; ++j) s += c[j * w + (i - j)] * t_prev[j];
+        for (i64 j = i; j <= min(last, i + P.bw); ++j) s += c[i * w + (j - i)] * t_prev[j];
+        double v = dt * f[i] + s;
+        if (P.fk0) v -= bound0[i] * t_left;
+        if (P.fk1) v -= boundN[i] * t_right;
+        if (P.fk0 && i == 0) v = t_left;
+        if (P.fk1 && i == last) v = t_right;
+        f[i] = v;
+    }
+}
+
+// One CTA: band LDL^T and both triangular solves (the stationary solve).
+__global__ void __launch_bounds__(1024) k_band_ldlt_solve(i64 n, i64 bw, double* __restrict__ band, double* __restrict__ f,
+                                                          int* __restrict__ failed) {
+    const i64 w = bw + 1;
+    if (!band_ldlt(n, bw, band, failed)) return;
     // U^T D U x = f with unit upper U: forward U^T y = f
     for (i64 i = 1; i < n; ++i) {
         double s = 0.0;
@@ -177,12 +298,10 @@ __global__ void __launch_bounds__(1024) k_band_ldlt_solve(i64 n, i64 bw, double*
     }
 }
 
-}  // namespace
-
-void stationary_1d(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight, int influence,
-                   double conductivity, double t_left, double q_right, bool sin_source, double* temperature) {
+// mesh, model and band geometry of one segment [0, length]
+Problem1d make_problem_1d(i64 elements, int order, double length, double radius, double local_weight, int influence,
+                          double conductivity) {
     NL_REQUIRE(influence >= 0 && influence <= 3, NLGPU_ERR_ARG, "unknown 1D influence kind");
-    const Line L = make_line(order);
     Problem1d P{};
     P.E = elements; P.order = order; P.n = elements * order + 1;
     P.h = length / double(elements);
@@ -197,13 +316,96 @@ void stationary_1d(Ctx& ctx, i64 elements, int order, double length, double radi
     else if (influence == 2) P.norm = 1.0 / (radius * std::sqrt(2 * std::numbers::pi));
     else P.norm = 0.5 / radius;
     NL_REQUIRE(double(P.n) * double(P.bw + 1) * 8.0 < 64e9, NLGPU_ERR_UNSUPPORTED, "1D band too large");
+    return P;
+}
+
+}  // namespace
+
+// Device state of nonstationary_heat_equation_solver_1d between compute and the steps.
+struct OneDimState {
+    Problem1d P{};
+    Line L{};
+    double dt = 0.0;
+    dbuf<double> a, c, bound0, boundN, t, f;
+};
+
+void nonstationary_1d_compute(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight,
+                              int influence, double conductivity, double capacity, double density, double time_step,
+                              int left_kind, int right_kind, const double* initial) {
+    NL_REQUIRE(elements > 0 && (order == 1 || order == 2) && length > 0.0 && time_step > 0.0, NLGPU_ERR_ARG,
+               "invalid 1D mesh or time step");
+    for (const int k : {left_kind, right_kind})
+        NL_REQUIRE(k == NLGPU_BC_TEMPERATURE || k == NLGPU_BC_FLUX, NLGPU_ERR_UNSUPPORTED,
+                   "1D ends take a temperature or a flux");
+    auto st = std::make_shared<OneDimState>();
+    Problem1d& P = st->P;
+    P = make_problem_1d(elements, order, length, radius, local_weight, influence, conductivity);
+    P.fk0 = left_kind == NLGPU_BC_TEMPERATURE;
+    P.fk1 = right_kind == NLGPU_BC_TEMPERATURE;
+    st->L = make_line(order);
+    st->dt = time_step;
+    const size_t n = size_t(P.n), nb = size_t(P.n * (P.bw + 1));
+    st->a.resize(nb); st->a.zero(ctx.stream);
+    st->c.resize(nb); st->c.zero(ctx.stream);
+    st->bound0.resize(n); st->bound0.zero(ctx.stream);
+    st->boundN.resize(n); st->boundN.zero(ctx.stream);
+    st->t.resize(n);
+    st->f.resize(n);
+    if (initial) st->t.upload(initial, n, ctx.stream);
+    else st->t.zero(ctx.stream);
+    dbuf<int> failed;
+    failed.resize(1); failed.zero(ctx.stream);
+    NL_LAUNCH(k_assemble_1d, grid_for(P.E * (2 * P.nb + 1), 128), 128, 0, ctx.stream, P, st->L, st->a.p, st->bound0.p,
+              st->boundN.p);
+    NL_LAUNCH(k_capacity_1d, grid_for(P.E * st->L.nen * st->L.nen, 256), 256, 0, ctx.stream, P, st->L,
+              capacity * density, st->c.p);
+    NL_LAUNCH(k_combine_1d, grid_for(i64(nb), 256), 256, 0, ctx.stream, P, time_step, st->a.p, st->c.p, st->bound0.p,
+              st->boundN.p);
+    NL_LAUNCH(k_band_ldlt, 1, 1024, 0, ctx.stream, P.n, P.bw, st->a.p, failed.p);
+    int hf = 0;
+    NL_CUDA(cudaMemcpyAsync(&hf, failed.p, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+    NL_REQUIRE(!hf, NLGPU_ERR_NUMERICAL, "zero pivot in the 1D LDL^T factorisation");
+    ctx.od = st;
+}
+
+void nonstationary_1d_step(Ctx& ctx, double left_value, double right_value, bool sin_source, double* temperature) {
+    NL_REQUIRE(ctx.od, NLGPU_ERR_STATE, "call nlgpu_nonstationary_1d_compute first");
+    OneDimState& st = *ctx.od;
+    const Problem1d& P = st.P;
+    const size_t n = size_t(P.n);
+    st.f.zero(ctx.stream);
+    NL_LAUNCH(k_step_loads_1d, grid_for(P.E * st.L.nen, 256), 256, 0, ctx.stream, P, st.L, left_value, right_value,
+              sin_source, st.f.p);
+    NL_LAUNCH(k_step_rhs_1d, grid_for(P.n, 256), 256, 0, ctx.stream, P, st.dt, st.c.p, st.t.p, st.bound0.p,
+              st.boundN.p, left_value, right_value, st.f.p);
+    NL_LAUNCH(k_band_solve_warp, 1, 32, 0, ctx.stream, P.n, P.bw, st.a.p, st.f.p);
+    std::swap(st.t, st.f);
+    if (temperature) st.t.download(temperature, n, ctx.stream);
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+void nonstationary_1d_temperature(Ctx& ctx, double* temperature) {
+    NL_REQUIRE(ctx.od, NLGPU_ERR_STATE, "call nlgpu_nonstationary_1d_compute first");
+    ctx.od->t.download(temperature, size_t(ctx.od->P.n), ctx.stream);
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+i64 nonstationary_1d_nodes(const Ctx& ctx) { return ctx.od ? ctx.od->P.n : 0; }
+
+void stationary_1d(Ctx& ctx, i64 elements, int order, double length, double radius, double local_weight, int influence,
+                   double conductivity, double t_left, double q_right, bool sin_source, double* temperature) {
+    const Line L = make_line(order);
+    Problem1d P = make_problem_1d(elements, order, length, radius, local_weight, influence, conductivity);
+    P.fk0 = 1; P.fk1 = 0;   // temperature on the left, flux on the right
     dbuf<double> band, bound0, f;
     dbuf<int> failed;
     band.resize(size_t(P.n * (P.bw + 1))); band.zero(ctx.stream);
     bound0.resize(size_t(P.n)); bound0.zero(ctx.stream);
     f.resize(size_t(P.n)); f.zero(ctx.stream);
     failed.resize(1); failed.zero(ctx.stream);
-    NL_LAUNCH(k_assemble_1d, grid_for(P.E * (2 * P.nb + 1), 128), 128, 0, ctx.stream, P, L, band.p, bound0.p);
+    NL_LAUNCH(k_assemble_1d, grid_for(P.E * (2 * P.nb + 1), 128), 128, 0, ctx.stream, P, L, band.p, bound0.p,
+              static_cast<double*>(nullptr));
     NL_LAUNCH(k_rhs_1d, grid_for(P.E * L.nen, 256), 256, 0, ctx.stream, P, L, q_right, sin_source, f.p);
     NL_LAUNCH(k_first_kind_1d, grid_for(P.n, 256), 256, 0, ctx.stream, P.n, bound0.p, t_left, f.p, band.p);
     NL_LAUNCH(k_band_ldlt_solve, 1, 1024, 0, ctx.stream, P.n, P.bw, band.p, f.p, failed.p);

@@ -2,7 +2,7 @@
 //
 // The reference builds them in two mesh_run sweeps (shift_initializer counts
 // distinct columns per row, matrix_index_initializer writes them, then
-// sort_indices; matrix_assembler_2d.hpp:430-461, conductivity_matrix_2d.hpp:39-72)
+// sort_indices; matrix_assembler_2d.hpp:144-176, conductivity_matrix_2d.hpp:39-72)
 // with the split of matrix_separator_base::part (matrix_separator_base.hpp:51-58):
 //   INNER  column and row inner, and row <= column when symmetric;
 //   BOUND  column Dirichlet and row != column (full rows);
@@ -261,8 +261,14 @@ __global__ void k_full_map(i64 n, const i64* __restrict__ up_rp, const int32_t* 
 
 }  // namespace
 
+void full_map(Ctx& ctx, const Csr& upper, const Csr& full, dbuf<i64>& map, bool symmetric) {
+    map.resize(size_t(full.nnz));
+    NL_LAUNCH(k_full_map, grid_for(full.rows * 32, 256, 152 * 64), 256, 0, ctx.stream, full.rows, upper.rowptr.p,
+              upper.col.p, full.rowptr.p, full.col.p, static_cast<const uint8_t*>(nullptr), symmetric, map.p);
+}
+
 void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* bound, Csr* full,
-                    dbuf<i64>* full_from_upper) {
+                    dbuf<i64>* full_from_upper, const uint8_t* is_inner) {
     const i64 n = ctx.n_nodes;
     NL_REQUIRE(local_only || ctx.neighbours_ready, NLGPU_ERR_STATE, "neighbour search must run before a nonlocal assembly");
     for (Csr* m : {&inner, bound, full})   // 16-bit column offsets belong to the old pattern
@@ -276,7 +282,7 @@ void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* 
     a.n = n; a.nen = ctx.basis.nen; a.local_only = local_only; a.symmetric = symmetric;
     a.elems = ctx.elems.p; a.ne_off = ctx.ne_off.p; a.ne_elem = ctx.ne_elem.p;
     a.noff = local_only ? nullptr : ctx.noff.p; a.nlist = local_only ? nullptr : ctx.nlist.p;
-    a.is_inner = ctx.is_inner.p;
+    a.is_inner = is_inner ? is_inner : ctx.is_inner.p;
     a.emin = ctx.elem_minnode.p; a.emax = ctx.elem_maxnode.p;
     a.cnt_inner = ci.p; a.cnt_bound = cb.p; a.cnt_full = cf.p; a.error = err.p;
     const unsigned grid = unsigned(std::min<i64>(n, 152 * 8));
@@ -305,7 +311,7 @@ void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* 
     if (full && full_from_upper) {
         full_from_upper->resize(size_t(nnz_f));
         NL_LAUNCH(k_full_map, grid_for(n * 32, 256, 152 * 64), 256, 0, ctx.stream, n, inner.rowptr.p, inner.col.p,
-                  F.rowptr.p, F.col.p, ctx.is_inner.p, symmetric, full_from_upper->p);
+                  F.rowptr.p, F.col.p, a.is_inner, symmetric, full_from_upper->p);
         F.val.resize(size_t(nnz_f));
     }
     NL_CUDA(cudaStreamSynchronize(ctx.stream));

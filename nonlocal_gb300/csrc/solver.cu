@@ -3,7 +3,7 @@
 // Reference: slae::conjugate_gradient::solve (conjugate_gradient.hpp:48-79) with
 // the symmetric product of independent_symmetric_matrix_vector_product.hpp:55-79,
 // and eigen_ILLT_preconditioner = Eigen::IncompleteCholesky<T, Upper,
-// NaturalOrdering> (eigen_preconditioner.hpp:136-137) built from p1*K_local
+// NaturalOrdering> (eigen_preconditioner.hpp:57) built from p1*K_local
 // (stationary_heat_equation_solver_2d.hpp:91-101).
 //
 // GB300 form:

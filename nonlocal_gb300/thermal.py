@@ -5,14 +5,16 @@ Names and argument meaning follow the reference:
 * ``Problem2D`` holds what the reference spreads over ``mesh::mesh_2d``,
   ``parameters_2d`` and ``thermal_boundaries_conditions_2d``: one device
   context (``nlgpu_ctx``) per problem;
-* ``find_neighbours`` -- ``mesh::find_neighbours`` (find_neighbours.hpp:469-510);
+* ``find_neighbours`` -- ``mesh::find_neighbours`` (find_neighbours.hpp:120-160);
 * ``Problem2D.conductivity_matrix`` -- ``conductivity_matrix_2d::compute``
   (conductivity_matrix_2d.hpp:166-193);
 * ``stationary_heat_equation_solver_2d`` (stationary_heat_equation_solver_2d.hpp:46-120);
 * ``NonstationaryHeatEquationSolver2D`` (nonstationary_heat_equation_solver_2d.hpp:16-106);
 * ``conjugate_gradient`` -- ``slae::conjugate_gradient`` with the ILLT
-  preconditioner (conjugate_gradient.hpp:15-79, eigen_preconditioner.hpp:136-137);
-* ``stationary_heat_equation_solver_1d`` (stationary_heat_equation_solver_1d.hpp:43-122).
+  preconditioner (conjugate_gradient.hpp:15-79, eigen_preconditioner.hpp:57);
+* ``stationary_heat_equation_solver_1d`` (stationary_heat_equation_solver_1d.hpp:43-122);
+* ``equilibrium_equation`` / ``MechanicalProblem2D`` -- nonlocal plane elasticity
+  (mechanical/equilibrium_equation_2d.hpp:19-60, stiffness_matrix_2d.hpp).
 
 Errors raise ``NlgpuError`` (the reference throws std::domain_error /
 std::logic_error); every compute call runs on the GPU.
@@ -424,6 +426,111 @@ class Problem2D(Context):
         return z, p, loss.value, g
 
 
+@dataclass
+class ElasticParameters:
+    """elastic_parameters_t (elastic_parameters.hpp): constant isotropic (E, nu),
+    orthotropic (E_x, E_y, nu_x, nu_y, G) or anisotropic (the orthotropic ones
+    and a rotation angle)."""
+
+    kind: str = "isotropic"
+    young_modulus: tuple[float, ...] = (210.0,)
+    poissons_ratio: tuple[float, ...] = (0.3,)
+    shear_modulus: float = 210.0 / 13.0
+    angle: float = 0.0
+
+    def values(self) -> np.ndarray:
+        if self.kind == "isotropic":
+            return np.array([self.young_modulus[0], self.poissons_ratio[0]], dtype=np.float64)
+        v = [*self.young_modulus[:2], *self.poissons_ratio[:2], self.shear_modulus]
+        if self.kind == "anisotropic":
+            v.append(self.angle)
+        return np.array(v, dtype=np.float64)
+
+
+@dataclass
+class MechanicalBoundary:
+    """mechanical_boundary_conditions_2d of one group: per component None,
+    ("displacement", value) (displacement_2d) or ("pressure", value) (pressure_2d)."""
+
+    edges: np.ndarray
+    x: tuple | None = None
+    y: tuple | None = None
+
+
+class MechanicalProblem2D(Problem2D):
+    """A plane-elasticity problem on the GPU (DoF = 2, rows 2 node + component):
+    the mesh, neighbours and nonlocal model of Problem2D, Hooke parameters and
+    displacement / pressure boundaries."""
+
+    def set_elastic(self, parameters: ElasticParameters) -> np.ndarray:
+        """Sets the Hooke matrix; returns h11, h12, h66, h22, h16, h26."""
+        v = parameters.values()
+        h = np.empty(6)
+        L.check(self._lib.nlgpu_set_elastic_2d(self._h, L.ELASTIC[parameters.kind], L.ptr(v), L.ptr(h)))
+        self.elastic = parameters
+        return h
+
+    def add_mechanical_boundary(self, b: MechanicalBoundary) -> None:
+        edges = L.i64(b.edges)
+        kx, vx = (None, 0.0) if b.x is None else b.x
+        ky, vy = (None, 0.0) if b.y is None else b.y
+        L.check(self._lib.nlgpu_add_mechanical_boundary_2d(self._h, edges.shape[0], edges.shape[1], L.ptr(edges),
+                                                           L.MECH_CONDITION[kx], float(vx), L.MECH_CONDITION[ky],
+                                                           float(vy)))
+
+    def clear_mechanical_boundaries(self) -> None:
+        L.check(self._lib.nlgpu_clear_mechanical_boundaries(self._h))
+
+    def stiffness_matrix(self, part: str = "FULL") -> tuple[int, int]:
+        """stiffness_matrix::compute of the FULL or LOCAL part."""
+        ni, nb = ctypes.c_int64(), ctypes.c_int64()
+        L.check(self._lib.nlgpu_stiffness_matrix_2d(self._h, L.PART_FULL if part == "FULL" else L.PART_LOCAL,
+                                                    ctypes.byref(ni), ctypes.byref(nb)))
+        return int(ni.value), int(nb.value)
+
+    def stiffness(self, which: str = "inner") -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        code = {"inner": L.MATRIX_INNER, "bound": L.MATRIX_BOUND, "local": L.MATRIX_LOCAL}[which]
+        rp = np.empty(2 * self.n_nodes + 1, dtype=np.int64)
+        L.check(self._lib.nlgpu_get_stiffness_matrix(self._h, code, L.ptr(rp), None, None))
+        col = np.empty(int(rp[-1]), dtype=np.int64)
+        val = np.empty(int(rp[-1]))
+        L.check(self._lib.nlgpu_get_stiffness_matrix(self._h, code, None, L.ptr(col), L.ptr(val)))
+        return rp, col, val
+
+    def mechanical_rhs(self) -> tuple[np.ndarray, np.ndarray]:
+        f, f0 = np.empty(2 * self.n_nodes), np.empty(2 * self.n_nodes)
+        L.check(self._lib.nlgpu_get_mechanical_rhs(self._h, L.ptr(f), L.ptr(f0)))
+        return f, f0
+
+    def equilibrium(self, tolerance=1e-10, max_iterations=10000, preconditioner=None, precision="fp64",
+                    triangular_sweeps=0):
+        """equilibrium_equation: assembly, boundary conditions and the CG solve
+        (ILLT of the LOCAL stiffness for a nonlocal model, identity for a local
+        one, unless `preconditioner` says otherwise).  Returns the displacement
+        as [n][2] and the report."""
+        if preconditioner is None:
+            preconditioner = "illt" if self.model.local_weight < 0.999 else "identity"
+        o = self._options(tolerance, max_iterations, preconditioner, precision, 0.0, triangular_sweeps)
+        u = np.empty(2 * self.n_nodes)
+        rep = L.SolveReport()
+        L.check(self._lib.nlgpu_equilibrium_equation_2d(self._h, ctypes.byref(o), L.ptr(u), ctypes.byref(rep)))
+        return u.reshape(-1, 2), SolveReport(rep.as_dict())
+
+
+def equilibrium_equation(problem: MechanicalProblem2D, model: Model2D, elastic: ElasticParameters,
+                         boundaries: list[MechanicalBoundary], tolerance=1e-10, **kw):
+    """mechanical::equilibrium_equation (equilibrium_equation_2d.hpp:19-60): the
+    displacement [n][2] of a plane-elasticity problem and the solve report."""
+    problem.set_model(model)
+    problem.set_elastic(elastic)
+    problem.clear_mechanical_boundaries()
+    for b in boundaries:
+        problem.add_mechanical_boundary(b)
+    if model.local_weight < 0.999:
+        problem.find_neighbours()
+    return problem.equilibrium(tolerance=tolerance, **kw)
+
+
 def unpack_learned_weights(w) -> dict:
     """Packed parameters -> {w1 4x64, w2 128x64, w3 128x64, w4 128x1} (input x output)."""
     w = np.asarray(w, dtype=np.float64)
@@ -600,3 +707,51 @@ def stationary_heat_equation_solver_1d(context: Context | None = None, elements:
                                              float(local_weight), kinds[influence], float(conductivity), float(t_left),
                                              float(q_right), int(bool(sin_source)), L.ptr(t)))
     return t
+
+
+INFLUENCE_1D = {"bell": 0, "triangle": 1, "normal": 2, "constant": 3}
+
+
+class NonstationaryHeatEquationSolver1D:
+    """nonstationary_heat_equation_solver_1d<T, I> on one segment [0, length]:
+    ``compute(left, right, initial)`` with each end ("temperature", value) or
+    ("flux", value) (the kinds are fixed by compute, as the reference's matrix
+    portrait), then ``calc_step(left_value, right_value, sin_source)`` per
+    implicit Euler step; ``temperature`` is the current temperature."""
+
+    def __init__(self, context: Context | None = None, elements: int = 200, order: int = 2, length: float = 1.0,
+                 radius: float = 0.1, local_weight: float = 0.5, influence: str = "bell", conductivity: float = 1.0,
+                 capacity: float = 1.0, density: float = 1.0, time_step: float = 1e-3):
+        self.ctx = context if context is not None else Context()
+        self.args = (int(elements), int(order), float(length), float(radius), float(local_weight),
+                     INFLUENCE_1D[influence], float(conductivity), float(capacity), float(density), float(time_step))
+        self.n = int(elements) * int(order) + 1
+        self.time_step = float(time_step)
+        self.time = 0.0
+
+    def compute(self, left=("temperature", 0.0), right=("flux", 0.0), initial=None) -> None:
+        kinds = {"temperature": L.BC_TEMPERATURE, "flux": L.BC_FLUX}
+        t0 = None if initial is None else L.f64(initial)
+        if t0 is not None and t0.shape != (self.n,):
+            raise ValueError(f"the initial temperature needs {self.n} nodal values")
+        nodes = ctypes.c_int64()
+        L.check(self.ctx._lib.nlgpu_nonstationary_1d_compute(self.ctx.handle, *self.args, kinds[left[0]],
+                                                             kinds[right[0]], L.ptr(t0), ctypes.byref(nodes)))
+        assert nodes.value == self.n
+        self.left, self.right = left, right
+
+    def calc_step(self, left_value: float | None = None, right_value: float | None = None,
+                  sin_source: bool = False) -> np.ndarray:
+        lv = self.left[1] if left_value is None else left_value
+        rv = self.right[1] if right_value is None else right_value
+        t = np.empty(self.n)
+        L.check(self.ctx._lib.nlgpu_nonstationary_1d_step(self.ctx.handle, float(lv), float(rv), int(bool(sin_source)),
+                                                          L.ptr(t)))
+        self.time += self.time_step
+        return t
+
+    @property
+    def temperature(self) -> np.ndarray:
+        t = np.empty(self.n)
+        L.check(self.ctx._lib.nlgpu_nonstationary_1d_temperature(self.ctx.handle, L.ptr(t)))
+        return t

@@ -15,7 +15,7 @@
 //     on breakdown (at most 10 attempts), left-looking column factorisation that
 //     keeps, per column, as many off-diagonal entries as the input column had
 //     (the largest in magnitude).  Used by the reference as its "ILLT"
-//     preconditioner (libraries/solvers/slae/eigen_preconditioner.hpp:136-137).
+//     preconditioner (libraries/solvers/slae/eigen_preconditioner.hpp:57).
 //   * SimplicialCholesky<..., Upper, NaturalOrdering>: a band LDL^T
 //     factorisation (used by the 1D stationary solver,
 //     libraries/solvers/solver_1d/thermal/stationary_heat_equation_solver_1d.hpp:99-105).

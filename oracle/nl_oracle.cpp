@@ -36,7 +36,7 @@ namespace {
 using i64 = int64_t;
 using vec2 = std::array<double, 2>;
 
-enum { ORC_BILINEAR = 2, ORC_SERENDIPITY = 3 };   // element_2d_t numbering (elements_set.hpp:231-237)
+enum { ORC_BILINEAR = 2, ORC_SERENDIPITY = 3 };   // element_2d_t numbering (elements_set.hpp:22-28)
 enum { INF_CONSTANT = 0, INF_POLYNOMIAL = 1, INF_EXPONENTIAL = 2, INF_FAST_POLYNOMIAL = 3 };
 enum { COND_ISO = 0, COND_ORTHO = 1, COND_ANISO = 2 };
 // temperature_2d, flux_2d, convection_2d, radiation_2d, combined_flux_2d
@@ -103,7 +103,7 @@ struct Element2d {
 };
 
 // element_2d_integrate::set_quadrature (element_2d_integrate.hpp:69-106) on the
-// rectangle [-1,1]^2 with the element's Gauss rule (vtk_elements_set.hpp:365-383).
+// rectangle [-1,1]^2 with the element's Gauss rule (vtk_elements_set.hpp:54-72).
 Element2d make_element2d(int type) {
     Element2d el;
     el.type = type;
@@ -135,7 +135,7 @@ Element2d make_element2d(int type) {
 }
 
 // 1D boundary elements: lagrangian order 1 with Gauss-1, order 2 with Gauss-2
-// (vtk_elements_set.hpp:354-363, element_1d_integrate.hpp:60-80).
+// (vtk_elements_set.hpp:43-52, element_1d_integrate.hpp:60-80).
 struct Element1d { int nen = 2, nq = 1; std::vector<double> qN, qNxi, w; };
 Element1d make_element1d(int nen) {
     Element1d el; el.nen = nen;
@@ -220,16 +220,16 @@ struct Problem {
     long record_iterations = -1;
 };
 
-bool nonlocal_model(const Problem& p) { return p.p1 < 0.999; }   // nonlocal_constants.hpp:274-280
+bool nonlocal_model(const Problem& p) { return p.p1 < 0.999; }   // nonlocal_constants.hpp:22-37
 
-// influence_functions_2d.hpp:39-148 with powered_distance (search_function.hpp:569-579)
+// influence_functions_2d.hpp:39-148 with powered_distance (search_function.hpp:29-73)
 double powered_dist(const Problem& p, const vec2& a, const vec2& b, const double* r) {
     const double z0 = (a[0] - b[0]) / r[0], z1 = (a[1] - b[1]) / r[1];
     if (p.inf_n == 2) return z0 * z0 + z1 * z1;
     if (p.inf_n == 1) return std::abs(z0) + std::abs(z1);
     return std::pow(std::abs(z0), p.inf_n) + std::pow(std::abs(z1), p.inf_n);
 }
-double ipow(double x, int n) {   // power.hpp:232-247
+double ipow(double x, int n) {   // power.hpp:25-40
     double res = 1.0;
     while (n > 0) { if (n & 1) { res *= x; --n; } else { x *= x; n >>= 1; } }
     return res;
@@ -268,7 +268,7 @@ const double* dN(const Problem& p, i64 e, int i, int q) { return &p.deriv[size_t
 i64 node_of(const Problem& p, i64 e, int i) { return p.elems[size_t(e * p.el.nen + i)]; }
 
 // mesh_2d::init (mesh_2d.hpp:97-108): node_elements_2d, quad coords, Jacobi
-// matrices, |J| and derivatives_in_quad (mesh_container_2d_utils.hpp:302-408).
+// matrices, |J| and derivatives_in_quad (mesh_container_2d_utils.hpp:18-123).
 void mesh_init(Problem& p) {
     const int nen = p.el.nen, nq = p.el.nq;
     p.node_elements.assign(size_t(p.n_nodes), {});
@@ -405,7 +405,7 @@ int part(const Problem& p, i64 row, i64 col, bool symmetric) {
     return 2;
 }
 
-// Portrait (shift_initializer/matrix_index_initializer, matrix_assembler_2d.hpp:430-461)
+// Portrait (shift_initializer/matrix_index_initializer, matrix_assembler_2d.hpp:144-176)
 // and values (integrator, integrator.hpp:62-91; calc_coeffs :463-475) of
 // conductivity_matrix_2d::compute (conductivity_matrix_2d.hpp:166-193).
 // The three mesh_run passes (mesh_2d_utils.hpp:13-37) run over node rows with
@@ -499,7 +499,7 @@ void boundary_vectors(Problem& p) {
     const i64 n = p.n_nodes;
     p.is_inner.assign(size_t(n), 1);
     p.x_dirichlet.assign(size_t(n), 0.0);
-    for (const Boundary& b : p.bnds)   // inner_nodes (solvers_utils.hpp:179-188)
+    for (const Boundary& b : p.bnds)   // inner_nodes (solvers_utils.hpp:31-40)
         if (b.kind == BC_TEMPERATURE)
             for (const i64 v : b.edges) p.is_inner[size_t(v)] = 0;
     p.rhs_init.assign(size_t(n), 0.0);
@@ -604,7 +604,7 @@ void convection_condition(const Problem& p, Csr& K) {
         });
 }
 
-// radiation_condition_2d, stationary overload (radiation_condition_2d.hpp:91-135):
+// radiation_condition_2d, stationary overload (radiation_condition_2d.hpp:59-104):
 // K(row, col >= row) -= 4 sigma eps int T^3 N_i N_j |J|, r[row] -= sigma eps int T^4 N_i |J|
 // with T the previous temperature at the edge's quadrature points
 void radiation_condition(const Problem& p, Csr& K, std::vector<double>& r, const std::vector<double>& T) {
@@ -849,7 +849,7 @@ void orc_set_model(void* h, int influence, int n, int pp, double q, double r1, d
 void orc_set_conductivity_field(void* h, const double* values) {   // isotropic, per quadrature point [e][q]
     auto& p = *static_cast<Problem*>(h);
     p.cond_q.assign(values, values + p.n_elems * p.el.nq);
-    p.symmetric = !nonlocal_model(p);   // problem_settings::is_symmetric (problem_settings.hpp:252-254)
+    p.symmetric = !nonlocal_model(p);   // problem_settings::is_symmetric (problem_settings.hpp:32-34)
 }
 
 void orc_set_capacity(void* h, double capacity, double density) {
@@ -1331,7 +1331,7 @@ double orc_scalar(void* h, const char* name) {
 // right end, source sin(pi x) when sin_source != 0, influence kind
 // 0 = polynomial_1d<2,1> (bell), 1 = polynomial_1d<1,1>, 2 = normal, 3 = constant
 // (influence_functions_1d.hpp:10-75).  Mesh: mesh_1d.hpp:119-300; assembly:
-// thermal_conductivity_assembler.hpp:178-248 and assebmler_base.hpp:360-404;
+// thermal_conductivity_assembler.hpp:64-125 and assebmler_base.hpp:112-155;
 // direct LDL^T solve (the restated SimplicialCholesky).
 int orc_stationary_1d(i64 elements, int order, double length, double r, double p1, int kind, double conductivity,
                       double t_left, double q_right, int sin_source, double* temperature_out) {

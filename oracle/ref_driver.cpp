@@ -8,7 +8,7 @@
 // product.
 //
 // Usage: ref_driver key=value ...   (see parse() below)
-//   mode=stationary2d | nonstationary2d | stationary1d | mechanical2d
+//   mode=stationary2d | nonstationary2d | stationary1d | nonstationary1d | mechanical2d
 //
 // The stationary 2D branch restates the ten driver lines of
 // libraries/solvers/solver_2d/thermal/stationary_heat_equation_solver_2d.hpp:72-103
@@ -23,6 +23,7 @@
 #include <solvers/solver_2d/mechanical/equilibrium_equation_2d.hpp>
 #include <solvers/solver_1d/influence_functions_1d.hpp>
 #include <solvers/solver_1d/thermal/stationary_heat_equation_solver_1d.hpp>
+#include <solvers/solver_1d/thermal/nonstationary_heat_equation_solver_1d.hpp>
 #include <metamath/finite_elements/finite_elements_1d/element/element_1d_integrate.hpp>
 #include <map>            // cuthill_mckee.hpp uses std::multimap without including <map>
 #include <unordered_set>
@@ -549,6 +550,65 @@ int stationary1d() {
     return 0;
 }
 
+// nonstationary_heat_equation_solver_1d (nonstationary_heat_equation_solver_1d.hpp:24-259):
+// one segment [0, 1], constant conductivity, capacity and density; each end a
+// temperature or a flux (left=t:<v> | f:<v>, right=...), source sin(pi x) or
+// none, initial temperature 0 or sin(pi x); `steps` calls of calc_step, the
+// temperature after each dumped as history (steps x n).
+int nonstationary1d() {
+    using namespace nonlocal;
+    using namespace nonlocal::solver_1d;
+    using namespace nonlocal::solver_1d::thermal;
+    const size_t elements = size_t(getd("elements", 200));
+    const size_t order = size_t(getd("order", 2));
+    const T r = getd("radius", 0.1);
+    const T p1 = getd("local_weight", 0.5);
+    using metamath::finite_element::element_1d_integrate;
+    using metamath::finite_element::element_1d;
+    using metamath::finite_element::lagrangian_element_1d;
+    using metamath::finite_element::quadrature_1d;
+    using metamath::finite_element::gauss;
+    std::unique_ptr<element_1d_integrate<T>> element;
+    if (order == 1) element = std::make_unique<element_1d_integrate<T>>(std::make_unique<element_1d<T, lagrangian_element_1d, 1>>(), quadrature_1d<T, gauss, 2>{});
+    else if (order == 2) element = std::make_unique<element_1d_integrate<T>>(std::make_unique<element_1d<T, lagrangian_element_1d, 2>>(), quadrature_1d<T, gauss, 3>{});
+    else throw std::domain_error{"unsupported 1D element"};
+    auto mesh = std::make_shared<mesh::mesh_1d<T>>(std::move(element), std::vector<mesh::segment_data<T>>{{.length = 1, .search_radius = r, .elements = elements}});
+    parameters_1d<T> parameters(1);
+    parameters[0].model.local_weight = p1;
+    const std::string kind = get("influence", "bell");
+    if (kind == "bell") parameters[0].model.influence = influence::polynomial_1d<T, 2, 1>{r};
+    else if (kind == "triangle") parameters[0].model.influence = influence::polynomial_1d<T, 1, 1>{r};
+    else if (kind == "normal") parameters[0].model.influence = influence::normal_distribution_1d<T>{r};
+    else parameters[0].model.influence = influence::constant_1d<T>{r};
+    parameters[0].physical.conductivity = getd("conductivity", 1.0);
+    parameters[0].physical.capacity = getd("capacity", 1.0);
+    parameters[0].physical.density = getd("density", 1.0);
+    const auto side = [](const std::string& spec) -> std::unique_ptr<thermal_boundary_condition_1d<T>> {
+        const T v = std::stod(spec.substr(2));
+        if (spec[0] == 't') return std::make_unique<temperature_1d<T>>(v);
+        return std::make_unique<flux_1d<T>>(v);
+    };
+    thermal_boundaries_conditions_1d<T> bcs;
+    bcs.front() = side(get("left", "t:0"));
+    bcs.back() = side(get("right", "f:1"));
+    const T dt = getd("dt", 1e-3);
+    nonstationary_heat_equation_solver_1d<T, J> solver{mesh, parameters, dt};
+    if (get("initial", "zero") == "sin")
+        solver.initialize_temperature(std::function<T(const T)>{[](const T x) { return std::sin(std::numbers::pi_v<T> * x); }});
+    solver.compute(bcs);
+    std::optional<std::function<T(const T)>> source;
+    if (get("source", "sin") == "sin") source = [](const T x) { return std::sin(std::numbers::pi_v<T> * x); };
+    const size_t steps = size_t(getd("steps", 5));
+    std::vector<double> history;
+    for (size_t s = 0; s < steps; ++s) {
+        solver.calc_step(bcs, source);
+        const auto& t = solver.temperature();
+        history.insert(history.end(), t.begin(), t.end());
+    }
+    dump("history", history.data(), history.size(), std::to_string(steps) + "," + std::to_string(mesh->nodes_count()));
+    return 0;
+}
+
 } // namespace
 
 int main(int argc, char** argv) {
@@ -566,6 +626,7 @@ int main(int argc, char** argv) {
         if (mode == "nonstationary2d") return nonstationary2d();
         if (mode == "mechanical2d") return mechanical2d();
         if (mode == "stationary1d") return stationary1d();
+        if (mode == "nonstationary1d") return nonstationary1d();
         std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     } catch (const std::exception& e) {
         std::fprintf(stderr, "ref_driver: %s\n", e.what());

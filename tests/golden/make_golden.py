@@ -133,6 +133,17 @@ CASES = {
                           {"mode": "stationary1d", "elements": 1000, "order": 2, "radius": 0.1, "local_weight": 0.5,
                            "influence": "bell", "conductivity": 1, "left_temperature": 0, "right_flux": 1,
                            "source": "sin"}),
+    # 1D nonstationary (nonstationary_heat_equation_solver_1d): 5 implicit Euler steps
+    "d1_nonstationary_quadratic": ({"none": True},
+                                   {"mode": "nonstationary1d", "elements": 200, "order": 2, "radius": 0.1,
+                                    "local_weight": 0.5, "influence": "bell", "conductivity": 1, "capacity": 1,
+                                    "density": 1, "dt": 1e-2, "steps": 5, "left": "t:0", "right": "f:1",
+                                    "source": "sin", "initial": "zero"}),
+    "d1_nonstationary_linear": ({"none": True},
+                                {"mode": "nonstationary1d", "elements": 40, "order": 1, "radius": 0.1,
+                                 "local_weight": 0.3, "influence": "triangle", "conductivity": 2, "capacity": 1.5,
+                                 "density": 2, "dt": 5e-3, "steps": 4, "left": "f:-0.5", "right": "t:1",
+                                 "source": "none", "initial": "sin"}),
     "d1_linear_40_triangle": ({"none": True},
                               {"mode": "stationary1d", "elements": 40, "order": 1, "quadrature": 2, "radius": 0.1,
                                "local_weight": 0.3, "influence": "triangle", "conductivity": 2,
