@@ -52,11 +52,18 @@ sys.path.insert(0, ROOT)
 METRIC = ("time to 1e-10 relative residual, nonlocal stationary 2D solve (full pipeline): learned mixed-precision "
           "FCG vs plain FP64 ILLT-CG")
 # method -> (precision, preconditioner, triangular sweeps of the FP32 ILLT: 0 the library's
-# default Jacobi sweeps, -1 exact level-scheduled substitution)
-METHODS = {"learned": ("mixed", "illt_learned", 0), "mixed": ("mixed", "illt", 0),
-           "mixed_exact": ("mixed", "illt", -1), "plain": ("fp64", "illt", 0)}
+# default Jacobi sweeps, -1 exact level-scheduled substitution; coarse-space correction)
+METHODS = {"learned": ("mixed", "illt_learned", 0, False), "mixed": ("mixed", "illt", 0, False),
+           "coarse": ("mixed", "illt", 0, True), "mixed_exact": ("mixed", "illt", -1, False),
+           "plain": ("fp64", "illt", 0, False)}
 METHOD_NAMES = {"learned": "mixed-precision FCG with ILLT + learned message-passing correction",
-                "mixed": "mixed-precision FCG with ILLT (learned correction gated off: it did not beat ILLT alone)"}
+                "coarse": "mixed-precision FCG with ILLT + coarse-space (aggregation deflation) correction; the "
+                          "learned message-passing correction gated off (it did not beat ILLT alone)"}
+
+
+def coarse_target(n_nodes: int) -> int:
+    """Aggregates of the coarse-space correction: about 128 nodes each, 64 .. 2048."""
+    return int(min(2048, max(64, n_nodes // 128)))
 LEARNED_TRAINING = dict(right_hand_sides=2, epochs=20, batch=4, learning_rate=2e-3, seed=0)
 METRIC_TOLERANCE = 1e-10      # the metric's residual
 REFERENCE_TOLERANCE = 1e-13   # the FP64 solve the nodal error is measured against
@@ -338,11 +345,14 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     h = pb.handle
     stop_tol = w["stop_tolerance"]
 
+    coarse = coarse_target(pb.n_nodes)
+
     def step(method, tol):
-        precision, pre, sweeps = METHODS[method]
+        precision, pre, sweeps, with_coarse = METHODS[method]
         pb.find_neighbours()
         return pb.stationary(tolerance=tol, max_iterations=100000, precision=precision, preconditioner=pre,
-                             triangular_sweeps=sweeps, check_convergence=tol >= 1e-12)
+                             triangular_sweeps=sweeps, check_convergence=tol >= 1e-12,
+                             coarse_aggregates=coarse if with_coarse else 0)
 
     def timed(method, tol, count):
         """count device-timed solves (CUDA events on the library's stream), L2 flushed before each."""
@@ -361,17 +371,15 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     few = max(1, min(args.steps, 3))
     step("plain", METRIC_TOLERANCE)
     step("mixed_exact", stop_tol)
-    for _ in range(args.warmup):
-        step("mixed", stop_tol)
+    step("mixed", stop_tol)
     # the learned correction is trained once per operator, on pairs the plain
     # solver harvests from this system (not timed as part of a solve); its
     # validation gate decides whether the timed method uses it
     train = pb.train_learned_preconditioner(**LEARNED_TRAINING)
     learned_weights = pb.learned_weights()
-    primary = "learned" if train["learned_enabled"] else "mixed"
-    if primary == "learned":
-        for _ in range(args.warmup):
-            step("learned", stop_tol)
+    primary = "learned" if train["learned_enabled"] else "coarse"
+    for _ in range(args.warmup):
+        step(primary, stop_tol)
     # -------- timed region: the primary method, then the comparisons
     sampler = ClockSampler(local)
     launches0 = L.kernel_launches()
@@ -384,7 +392,7 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
     plain_ms, rep_plain, temp_plain = timed("plain", METRIC_TOLERANCE, max(1, min(args.steps, 5)))
     plain_same_ms, rep_plain_same, _ = timed("plain", stop_tol, few)
     exact_ms, rep_exact, _ = timed("mixed_exact", stop_tol, few)
-    mixed_ms, rep_mixed = (mean_ms, rep) if primary == "mixed" else timed("mixed", stop_tol, args.steps)[:2]
+    mixed_ms, rep_mixed, _ = timed("mixed", stop_tol, few)
     L.check(lib.nlgpu_synchronize(h))
     clocks = sampler.stop()
     barrier(dist)
@@ -470,7 +478,8 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
         if primary == "learned":
             pe.set_learned_weights(learned_weights, enabled=True)
         te, _ = pe.stationary(tolerance=stop_tol, max_iterations=100000, precision=METHODS[primary][0],
-                              preconditioner=METHODS[primary][1])
+                              preconditioner=METHODS[primary][1],
+                              coarse_aggregates=coarse if METHODS[primary][3] else 0)
         e2e_s.append(time.perf_counter() - t0)
         pe.close()
     e2e = max_over_ranks(dist, sum(e2e_s) / len(e2e_s))
@@ -506,9 +515,11 @@ def run_gpu(args, w, mesh, world, rank, local, dist):
                                ["neighbours", "pattern", "assembly", "boundary", "preconditioner", "solve"]},
                   "stage_ms": stage_ms},
         "learned_training": dict(train, **{"config": LEARNED_TRAINING}),
+        "coarse_aggregates": coarse if METHODS[primary][3] else 0,
         "mixed_illt": {"ms_per_step": mixed_ms, "cg_iterations": rep_mixed.iterations,
                        "reliable_updates": rep_mixed.outer_iterations, "residual": rep_mixed.residual,
-                       "triangular_sweeps": L.DEFAULT_TRIANGULAR_SWEEPS},
+                       "triangular_sweeps": L.DEFAULT_TRIANGULAR_SWEEPS,
+                       "note": "the same mixed-precision FCG without the coarse-space correction (ILLT alone)"},
         "mixed_illt_exact_sweeps": {"ms_per_step": exact_ms, "cg_iterations": rep_exact.iterations,
                                     "reliable_updates": rep_exact.outer_iterations, "residual": rep_exact.residual},
         "plain_fp64": {"ms_per_step": plain_ms, "cg_iterations": rep_plain.iterations, "residual": rep_plain.residual,
@@ -545,7 +556,7 @@ def renumbering_report(w, mesh, T, L, lib, steps: int) -> dict:
     shuffled = relabel_nodes(mesh, np.random.default_rng(1).permutation(mesh.n_nodes))
     pb = make_problem(w, T, shuffled)
     h = pb.handle
-    precision, pre, sweeps = METHODS["mixed"]
+    precision, pre, sweeps, _ = METHODS["mixed"]
 
     def solve_ms():
         out = []

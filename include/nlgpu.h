@@ -102,6 +102,9 @@ typedef struct nlgpu_solve_options {
     int precision;            /* NLGPU_PRECISION_* */
     double inner_tolerance;   /* MIXED: relative reduction of each FP32 inner solve (<= 0: 1e-2) */
     int triangular_sweeps;    /* MIXED: see NLGPU_DEFAULT_TRIANGULAR_SWEEPS (0: the default) */
+    int coarse_aggregates;    /* MIXED with ILLT: 0 none; > 0 adds a coarse-space correction over about
+                                 that many node aggregates (no counterpart in the reference, whose
+                                 preconditioner is ILLT alone) */
 } nlgpu_solve_options;
 
 typedef struct nlgpu_solve_report {

@@ -49,7 +49,7 @@ class Model2D(ctypes.Structure):
 
 class SolveOptions(ctypes.Structure):
     _fields_ = [("tolerance", c_d), ("max_iterations", c_i64), ("preconditioner", c_int), ("precision", c_int),
-                ("inner_tolerance", c_d), ("triangular_sweeps", c_int)]
+                ("inner_tolerance", c_d), ("triangular_sweeps", c_int), ("coarse_aggregates", c_int)]
 
 
 DEFAULT_TRIANGULAR_SWEEPS = 6   # NLGPU_DEFAULT_TRIANGULAR_SWEEPS

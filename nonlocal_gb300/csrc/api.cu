@@ -221,10 +221,14 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     if (mixed) {
         matrix_to_f32(c, c.full, c.symmetric && c.fp32_symmetric ? &c.inner : nullptr);
         timer.mark("FP32 matrix");
+        NL_REQUIRE(o.coarse_aggregates >= 0, NLGPU_ERR_ARG, "coarse_aggregates must be >= 0");
+        const bool coarse = o.coarse_aggregates > 0 && M && !c.neumann;
+        if (coarse) coarse_build(c, c.full, o.coarse_aggregates);
+        timer.mark("coarse correction");
         c.ilt_sweeps = sweeps;
         r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, b, c.temperature.p, o.tolerance, o.max_iterations,
                         o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M && c.mp.use,
-                        c.ilt_sweeps);
+                        c.ilt_sweeps, coarse && c.co.ready);
         if (learned && M && c.mp.use) mpnn_check(c);
         if (learned && !(M && c.mp.use)) r.learned_fallback = true;   // gated off: ILLT alone
     } else {

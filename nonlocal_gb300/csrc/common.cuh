@@ -301,6 +301,21 @@ struct Mpnn {
     dbuf<int> error;
 };
 
+// Coarse-space correction of the mixed solve (coarse.cu): aggregates, AP,
+// the FP32 inverse of A_c = P^T A P and the application's work vectors.
+struct Coarse {
+    bool ready = false;
+    i64 nc = 0, ap_nnz = 0;
+    dbuf<int32_t> agg;           // [n] aggregate of each node (-1: none)
+    dbuf<i64> ptr;               // [nc + 1] node lists of the aggregates
+    dbuf<int32_t> nodes;
+    dbuf<i64> ap_rp;             // AP: per row (aggregate, sum of the row's entries over it)
+    dbuf<int32_t> ap_col;
+    dbuf<float> ap_val;
+    dbuf<float> ainv;            // [nc][nc]
+    dbuf<float> rc, ec, w, y;
+};
+
 // Device state of BiCGSTAB (bicgstab.cu).
 struct BicgWork {
     dbuf<double> r, r0, p, v, s, t, y, z, dinv, part, sc;
@@ -401,6 +416,7 @@ struct Ctx {
     IncompleteCholesky plugin_ilt;   // nlgpu_illt_compute / nlgpu_illt_solve
     bool plugin_ilt_ready = false;
     CgWork cg;
+    Coarse co;
     Elastic el;
     std::shared_ptr<OneDimState> od;
     MixedWork mx;
@@ -526,7 +542,12 @@ void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y);
 // sweeps 0: level-scheduled triangular solves; > 0: that many Jacobi sweeps per triangle
 void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, int sweeps = 0);
 CgResult mixed_solve(Ctx& ctx, const Csr& A_full, IncompleteCholesky* M, const double* b, double* x, double tolerance,
-                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps);
+                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps,
+                     bool coarse = false);
+// coarse.cu: the coarse-space correction around the FP32 ILLT application
+void coarse_build(Ctx& ctx, const Csr& A_full, int target);
+void coarse_before(Ctx& ctx, const float* r, const double* flags);   // ctx.co.w = r - A Q r, ctx.co.y = Q r
+void coarse_after(Ctx& ctx, float* z, const double* flags);          // z += Q r
 // batch.cu: many nonstationary instances stepped together (block-diagonal system)
 struct Batch;
 Batch* batch_create(const std::vector<Ctx*>& instances);

@@ -677,7 +677,9 @@ void matrix_to_f32(Ctx& ctx, Csr& A, const Csr* upper) {
 // iterations is captured once per solve and replayed as one CUDA graph (not
 // with the learned correction, whose network runs outside graphs).
 CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double* b, double* x, double tolerance,
-                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps) {
+                     i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps,
+                     bool coarse) {
+    NL_REQUIRE(!coarse || ctx.co.ready, NLGPU_ERR_STATE, "the coarse correction is not built");
     NL_REQUIRE(A.up_ok || A.val32.n == size_t(A.nnz), NLGPU_ERR_STATE, "the FP32 copy of the matrix is missing");
     NL_REQUIRE(!learned || (M && ctx.mp.ready && ctx.mp.n == A.rows), NLGPU_ERR_STATE,
                "the learned correction needs ILLT and a prepared network");
@@ -712,7 +714,13 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     const double eta2 = update_factor * update_factor;
     CgResult res;
     auto precondition = [&](const double* pt, const double* fl, double t2) {
-        precondition32(ctx, M, w.r.p, w.z.p, pt, fl, t2, sweeps);
+        if (coarse) {   // z = M^-1 (r - A Q r) + Q r
+            coarse_before(ctx, w.r.p, fl);
+            precondition32(ctx, M, ctx.co.w.p, w.z.p, pt, fl, t2, sweeps);
+            coarse_after(ctx, w.z.p, fl);
+        } else {
+            precondition32(ctx, M, w.r.p, w.z.p, pt, fl, t2, sweeps);
+        }
         if (learned) mpnn_apply(ctx, w.r.p, w.z.p, w.z.p, false);
     };
     // |b|^2 and the first residual

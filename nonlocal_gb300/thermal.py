@@ -361,21 +361,24 @@ class Problem2D(Context):
     # ---- solves -----------------------------------------------------------------
     @staticmethod
     def _options(tolerance, max_iterations, preconditioner, precision, inner_tolerance=0.0,
-                 triangular_sweeps=0) -> L.SolveOptions:
+                 triangular_sweeps=0, coarse_aggregates=0) -> L.SolveOptions:
         o = L.SolveOptions()
         o.tolerance, o.max_iterations = float(tolerance), int(max_iterations)
         o.preconditioner, o.precision = L.PRECONDITIONER[preconditioner], L.PRECISION[precision]
         o.inner_tolerance = float(inner_tolerance)
         o.triangular_sweeps = int(triangular_sweeps)
+        o.coarse_aggregates = int(coarse_aggregates)
         return o
 
     def stationary(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64",
-                   check_convergence=True, inner_tolerance=0.0, triangular_sweeps=0):
+                   check_convergence=True, inner_tolerance=0.0, triangular_sweeps=0, coarse_aggregates=0):
         """stationary_heat_equation_solver_2d; precision "mixed" runs the FP32 inner
         solve with FP64 refinement (inner_tolerance: reduction per inner solve;
         triangular_sweeps: Jacobi sweeps per triangle of the FP32 ILLT application,
-        0 the default, -1 exact level-scheduled substitution)."""
-        o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance, triangular_sweeps)
+        0 the default, -1 exact level-scheduled substitution; coarse_aggregates > 0
+        adds a coarse-space correction over about that many node aggregates)."""
+        o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance, triangular_sweeps,
+                          coarse_aggregates)
         t = np.empty(self.n_nodes)
         rep = L.SolveReport()
         rc = self._lib.nlgpu_stationary_2d(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep))
