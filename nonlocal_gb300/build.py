@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "libnlgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = ["util.cu", "mesh.cu", "neighbours.cu", "boundary.cu", "pattern.cu", "assemble.cu", "solver.cu",
          "onedim.cu", "sweep.cu", "jacobi.cu", "mixed.cu", "flux.cu", "renumber.cu", "su2.cu", "nonlinear.cu",
-         "bicgstab.cu", "elastic.cu", "coarse.cu",
+         "bicgstab.cu", "elastic.cu", "coarse.cu", "iltbuild.cu",
          "batch.cu", "tc_gemm.cu",
          "mpnn.cu", "noalloc.cu", "api.cu"]
 HEADERS = ["common.cuh", "ff.cuh", "influence.cuh"]

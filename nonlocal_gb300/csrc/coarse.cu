@@ -12,7 +12,7 @@
 //   AP          per row the sums of the row's entries by column aggregate
 //               (segmented warp sums over the row's sorted columns; a row may
 //               hold an aggregate more than once, only the sum matters)
-//   A_c = P^T A P  from AP (atomics over AP's few entries), FP64
+//   A_c = P^T A P  from AP, a row per aggregate summed in shared memory, FP64
 //   A_c^-1      Gauss-Jordan in FP64 (A_c is SPD, no pivoting), one launch per
 //               pivot ping-ponging two copies; stored in FP32 for the solve
 //   apply       Q r = P A_c^-1 P^T r, then z = M^-1 (r - A Q r) + Q r with
@@ -173,16 +173,26 @@ __global__ void k_ap(i64 n, const i64* __restrict__ rp, const int32_t* __restric
     }
 }
 
-// A_c[I][J] += AP[r][J] for I = agg(r)
-__global__ void k_coarse_matrix(i64 n, const i64* __restrict__ ap_rp, const int32_t* __restrict__ ap_col,
-                                const double* __restrict__ ap_val, const int32_t* __restrict__ agg, i64 nc,
-                                double* __restrict__ ac) {
-    const int lane = threadIdx.x & 31;
-    const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
-    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
-        const i64 I = agg[r];
-        if (I < 0) continue;
-        for (i64 k = ap_rp[r] + lane; k < ap_rp[r + 1]; k += 32) atomicAdd(ac + I * nc + ap_col[k], ap_val[k]);
+// Row I of A_c = sum over the nodes r of aggregate I of AP row r: a CTA per
+// aggregate accumulates the row in shared memory (nc doubles), then writes it
+// whole.  Dynamic shared memory: nc doubles.
+__global__ void __launch_bounds__(CO_THREADS) k_coarse_rows(i64 nc, const i64* __restrict__ ptr,
+                                                            const int32_t* __restrict__ nodes,
+                                                            const i64* __restrict__ ap_rp,
+                                                            const int32_t* __restrict__ ap_col,
+                                                            const double* __restrict__ ap_val, double* __restrict__ ac) {
+    extern __shared__ double row[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = int(blockDim.x >> 5);
+    for (i64 I = blockIdx.x; I < nc; I += gridDim.x) {
+        for (i64 j = threadIdx.x; j < nc; j += blockDim.x) row[j] = 0.0;
+        __syncthreads();
+        for (i64 t = ptr[I] + warp; t < ptr[I + 1]; t += nw) {
+            const int32_t r = nodes[t];
+            for (i64 k = ap_rp[r] + lane; k < ap_rp[r + 1]; k += 32) atomicAdd(row + ap_col[k], ap_val[k]);
+        }
+        __syncthreads();
+        for (i64 j = threadIdx.x; j < nc; j += blockDim.x) ac[I * nc + j] = row[j];
+        __syncthreads();
     }
 }
 
@@ -307,7 +317,8 @@ void coarse_build(Ctx& ctx, const Csr& A, int target) {
     co.nc = nc;
     // a mesh whose nodes leave most cells empty (strongly graded or elongated)
     // may still give far more aggregates than asked for: no coarse correction
-    if (nc < 1 || nc > 2 * i64(target) + 64) return;
+    // (the coarse rows are accumulated in shared memory: at most 24 Ki aggregates)
+    if (nc < 1 || nc > std::min<i64>(2 * i64(target) + 64, 24 * 1024)) return;
     dbuf<unsigned long long> count;
     count.resize(size_t(nc) + 1);
     count.zero(ctx.stream);
@@ -346,8 +357,10 @@ void coarse_build(Ctx& ctx, const Csr& A, int target) {
     dbuf<double> m0, m1;
     m0.resize(size_t(nc * nc));
     m1.resize(size_t(nc * nc));
-    m0.zero(ctx.stream);
-    NL_LAUNCH(k_coarse_matrix, gw, CO_THREADS, 0, ctx.stream, n, co.ap_rp.p, co.ap_col.p, ap64.p, co.agg.p, nc, m0.p);
+    const size_t row_bytes = size_t(nc) * sizeof(double);
+    NL_CUDA(cudaFuncSetAttribute(k_coarse_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, int(row_bytes)));
+    NL_LAUNCH(k_coarse_rows, unsigned(std::min<i64>(nc, 152 * 8)), CO_THREADS, row_bytes, ctx.stream, nc, co.ptr.p,
+              co.nodes.p, co.ap_rp.p, co.ap_col.p, ap64.p, m0.p);
     timer.mark("AP and A_c");
     // ---- A_c^-1 by Gauss-Jordan (ping-pong), then FP32
     double* src = m0.p;

@@ -528,9 +528,10 @@ void subtract3(Ctx& ctx, const double* a, const double* b, const double* d, doub
 std::array<double, 3> step_norms(Ctx& ctx, const double* residual, const double* prev, double* x);
 void add_scaled(Ctx& ctx, double a, const double* x, double* y);
 void add_constant(Ctx& ctx, double a, double* y);
+// iltbuild.cu: U pattern copies, U^T, the factorisation's levels (offsets on the
+// host too) and the Jacobi sweeps' layouts, built on the device
+void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, std::vector<i64>& lev_ptr);
 // jacobi.cu: the factor applied by Jacobi sweeps on its two triangles
-void jacobi_build(Ctx& ctx, IncompleteCholesky& ic, const std::vector<i64>& rp, const std::vector<int32_t>& col,
-                  const std::vector<i64>& lrp, const std::vector<int32_t>& lcol, const std::vector<i64>& l_to_u);
 void jacobi_fill(Ctx& ctx, IncompleteCholesky& ic);
 void jacobi_apply32(Ctx& ctx, IncompleteCholesky& ic, int sweeps, const float* r, float* z, const double* flags);
 // mixed.cu

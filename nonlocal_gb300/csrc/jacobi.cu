@@ -32,42 +32,8 @@ namespace {
 
 constexpr int JB_THREADS = 256;
 
-// sliced ELL layout of per-row entry lists: columns and factor positions
-void build_slab(Ctx& ctx, i64 n, const std::vector<i64>& first, const std::vector<i64>& last,
-                const std::vector<int32_t>& cols, const std::vector<i64>* src_of, JacobiSlab& s) {
-    const i64 slices = (n + 31) / 32;
-    std::vector<i64> slice(size_t(slices + 1), 0);
-    for (i64 sl = 0; sl < slices; ++sl) {
-        i64 w = 0;
-        for (i64 r = sl * 32; r < std::min(n, sl * 32 + 32); ++r) w = std::max(w, last[size_t(r)] - first[size_t(r)]);
-        slice[size_t(sl) + 1] = slice[size_t(sl)] + 32 * w;
-    }
-    s.entries = slice[size_t(slices)];
-    const size_t m = size_t(std::max<i64>(s.entries, 1));
-    std::vector<int32_t> col(m, 0);
-    std::vector<i64> src(m, -1);
-    for (i64 r = 0; r < n; ++r) {
-        const i64 sl = r / 32, lane = r % 32, w = (slice[size_t(sl) + 1] - slice[size_t(sl)]) / 32;
-        for (i64 k = 0; k < w; ++k) {
-            const size_t e = size_t(slice[size_t(sl)] + 32 * k + lane);
-            const i64 pos = first[size_t(r)] + k;
-            if (pos < last[size_t(r)]) {
-                col[e] = cols[size_t(pos)];
-                src[e] = src_of ? (*src_of)[size_t(pos)] : pos;
-            } else {
-                col[e] = int32_t(r);
-            }
-        }
-    }
-    // padding rows of the last slice (r >= n) point at row 0 with value 0
-    s.slice.upload(slice.data(), slice.size(), ctx.stream);
-    s.col.upload(col.data(), col.size(), ctx.stream);
-    s.src.upload(src.data(), src.size(), ctx.stream);
-    s.val.resize(m);
-    s.val.zero(ctx.stream);
-}
-
-// val = u[src] / u_ii of the entry's row (0 for padding)
+// val = u[src] / u_ii of the entry's row (0 for padding); the sliced-ELL
+// layouts themselves are built by iltbuild.cu
 __global__ void k_jacobi_values(i64 n, const i64* __restrict__ slice, const i64* __restrict__ src,
                                 const i64* __restrict__ u_rp, const double* __restrict__ u, float* __restrict__ val) {
     for (i64 r = blockIdx.x * i64(blockDim.x) + threadIdx.x; r < n; r += i64(gridDim.x) * blockDim.x) {
@@ -130,23 +96,6 @@ void sweep(Ctx& ctx, i64 n, const JacobiSlab& s, const float* base, const float*
 }
 
 }  // namespace
-
-void jacobi_build(Ctx& ctx, IncompleteCholesky& ic, const std::vector<i64>& rp, const std::vector<int32_t>& col,
-                  const std::vector<i64>& lrp, const std::vector<int32_t>& lcol, const std::vector<i64>& l_to_u) {
-    const i64 n = ic.n;
-    // U^T rows: the diagonal is the last entry; U rows: the diagonal is the first
-    const size_t rows = static_cast<size_t>(n);
-    std::vector<i64> lo_first(lrp.begin(), lrp.end() - 1), lo_last(rows), up_first(rows), up_last(rows);
-    for (i64 r = 0; r < n; ++r) {
-        lo_last[size_t(r)] = lrp[size_t(r) + 1] - 1;
-        up_first[size_t(r)] = rp[size_t(r)] + 1;
-        up_last[size_t(r)] = rp[size_t(r) + 1];
-    }
-    build_slab(ctx, n, lo_first, lo_last, lcol, &l_to_u, ic.jlo);
-    build_slab(ctx, n, up_first, up_last, col, nullptr, ic.jup);
-    ic.jc.resize(size_t(n)); ic.jdinv.resize(size_t(n));
-    ic.jt0.resize(size_t(n)); ic.jt1.resize(size_t(n)); ic.jy.resize(size_t(n));
-}
 
 void jacobi_fill(Ctx& ctx, IncompleteCholesky& ic) {
     const i64 n = ic.n;

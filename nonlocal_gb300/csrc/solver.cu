@@ -510,58 +510,39 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
     const i64 n = upper.rows, nnz = upper.nnz;
     ic.n = n; ic.nnz = nnz;
     PhaseTimer timer(ctx.stream, "ilt_build");
-    std::vector<i64> rp(size_t(n + 1));
-    std::vector<int32_t> col(static_cast<size_t>(nnz));
-    upper.rowptr.download(rp.data(), rp.size(), ctx.stream);
-    upper.col.download(col.data(), col.size(), ctx.stream);
-    NL_CUDA(cudaStreamSynchronize(ctx.stream));
-    for (i64 r = 0; r < n; ++r)
-        NL_REQUIRE(rp[size_t(r) + 1] > rp[size_t(r)] && col[size_t(rp[size_t(r)])] == int32_t(r), NLGPU_ERR_ARG,
-                   "every row of the preconditioner matrix needs its diagonal first");
-    timer.mark("download");
-    // U^T as lower CSR with the diagonal last, and the U position of each entry
-    std::vector<i64> lrp(size_t(n + 1), 0);
-    for (i64 k = 0; k < nnz; ++k) ++lrp[size_t(col[size_t(k)]) + 1];
-    for (i64 r = 0; r < n; ++r) lrp[size_t(r) + 1] += lrp[size_t(r)];
-    std::vector<int32_t> lcol(static_cast<size_t>(nnz));
-    std::vector<i64> l_to_u(static_cast<size_t>(nnz));
-    {
-        std::vector<i64> cur(lrp.begin(), lrp.end() - 1);
-        for (i64 r = 0; r < n; ++r)
-            for (i64 k = rp[size_t(r)]; k < rp[size_t(r) + 1]; ++k) {
-                const i64 pos = cur[size_t(col[size_t(k)])]++;
-                lcol[size_t(pos)] = int32_t(r);
-                l_to_u[size_t(pos)] = k;
-            }
-    }
-    std::vector<i64> ident(static_cast<size_t>(nnz)), u_diag(static_cast<size_t>(n)), l_diag(static_cast<size_t>(n));
-    std::iota(ident.begin(), ident.end(), i64(0));
-    for (i64 r = 0; r < n; ++r) { u_diag[size_t(r)] = rp[size_t(r)]; l_diag[size_t(r)] = lrp[size_t(r) + 1] - 1; }
-    std::vector<i64> ic_lev_ptr, bwd_lev_ptr;
-    std::vector<int32_t> ic_rows, bwd_rows;
-    build_slab(ctx, lrp, lcol, l_to_u, l_diag, true, ic.fwd, &ic_lev_ptr, &ic_rows);
-    build_slab(ctx, rp, col, ident, u_diag, false, ic.bwd, &bwd_lev_ptr, &bwd_rows);
-    timer.mark("transpose, levels, slabs");
-    // TMA-fed shared-memory sweeps when every dependency fits the ring
+    // U^T, the factorisation's levels and the Jacobi layouts on the device
+    std::vector<i64> ic_lev_ptr;
+    ilt_structure_gpu(ctx, upper, ic, ic_lev_ptr);
+    timer.mark("structure");
     ctx.sweep_error.resize(1);
     ctx.sweep_error.zero(ctx.stream);
     ic.fwd_plan = SweepPlan{};
     ic.bwd_plan = SweepPlan{};
-    if (tma_plans && sweep_plan_build(ctx, ic_lev_ptr, ic_rows, lrp, lcol, l_to_u, l_diag, ic.fwd_plan))
-        sweep_plan_build(ctx, bwd_lev_ptr, bwd_rows, rp, col, ident, u_diag, ic.bwd_plan);
-    timer.mark("sweep plans");
-    ic.ic_levels = i64(ic_lev_ptr.size()) - 1;
-    ic.ic_lev_ptr.upload(ic_lev_ptr.data(), ic_lev_ptr.size(), ctx.stream);
-    ic.ic_rows.upload(ic_rows.data(), ic_rows.size(), ctx.stream);
-    ic.lrp.upload(lrp.data(), lrp.size(), ctx.stream);
-    ic.lcol.upload(lcol.data(), lcol.size(), ctx.stream);
-    ic.l_to_u.upload(l_to_u.data(), l_to_u.size(), ctx.stream);
-    ic.rp.upload(rp.data(), rp.size(), ctx.stream);
-    ic.col.upload(col.data(), col.size(), ctx.stream);
+    for (TriSlab* sl : {&ic.fwd, &ic.bwd}) { sl->n_levels = 0; sl->entries = 0; }
+    if (tma_plans) {
+        // the exact level-scheduled sweeps' layouts (host): level-ELL slabs of both
+        // triangles and the TMA-fed shared-memory plans when every dependency fits the ring
+        std::vector<i64> rp(size_t(n + 1)), lrp(size_t(n + 1)), l_to_u(static_cast<size_t>(nnz));
+        std::vector<int32_t> col(static_cast<size_t>(nnz)), lcol(static_cast<size_t>(nnz));
+        ic.rp.download(rp.data(), rp.size(), ctx.stream);
+        ic.col.download(col.data(), col.size(), ctx.stream);
+        ic.lrp.download(lrp.data(), lrp.size(), ctx.stream);
+        ic.lcol.download(lcol.data(), lcol.size(), ctx.stream);
+        ic.l_to_u.download(l_to_u.data(), l_to_u.size(), ctx.stream);
+        NL_CUDA(cudaStreamSynchronize(ctx.stream));
+        std::vector<i64> ident(static_cast<size_t>(nnz)), u_diag(static_cast<size_t>(n)), l_diag(static_cast<size_t>(n));
+        std::iota(ident.begin(), ident.end(), i64(0));
+        for (i64 r = 0; r < n; ++r) { u_diag[size_t(r)] = rp[size_t(r)]; l_diag[size_t(r)] = lrp[size_t(r) + 1] - 1; }
+        std::vector<i64> fwd_lev_ptr, bwd_lev_ptr;
+        std::vector<int32_t> fwd_rows, bwd_rows;
+        build_slab(ctx, lrp, lcol, l_to_u, l_diag, true, ic.fwd, &fwd_lev_ptr, &fwd_rows);
+        build_slab(ctx, rp, col, ident, u_diag, false, ic.bwd, &bwd_lev_ptr, &bwd_rows);
+        if (sweep_plan_build(ctx, fwd_lev_ptr, fwd_rows, lrp, lcol, l_to_u, l_diag, ic.fwd_plan))
+            sweep_plan_build(ctx, bwd_lev_ptr, bwd_rows, rp, col, ident, u_diag, ic.bwd_plan);
+        timer.mark("exact sweep layouts");
+    }
     ic.y.resize(size_t(n + 1)); ic.w.resize(size_t(n + 1));
     ic.y32.resize(size_t(n + 1)); ic.w32.resize(size_t(n + 1));
-    jacobi_build(ctx, ic, rp, col, lrp, lcol, l_to_u);
-    timer.mark("uploads, jacobi layout");
     // Lin-More scaling and the shifted factorisation
     ic.scale.resize(size_t(n)); ic.scale.zero(ctx.stream);
     ic.scale32.resize(size_t(n));
@@ -608,6 +589,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
         sweep_plan_fill(ctx, ic.bwd_plan, ic.u.p);
     }
     for (TriSlab* s : {&ic.fwd, &ic.bwd}) {
+        if (!s->n_levels) continue;   // no exact-sweep layout in this build
         if (s->entries)
             NL_LAUNCH(k_slab_values, grid_for(s->entries, 256), 256, 0, ctx.stream, s->entries, s->src.p, ic.u.p,
                       s->val.p, s->val32.p);
