@@ -658,6 +658,26 @@ def run_batch(args, world, rank, local, dist):
     total = max_over_ranks(dist, total)
     its = np.array(its)
     nodes = sum((e + 1) ** 2 for e, _ in specs)
+    # roofline of the step: the block-diagonal SpMV of every CG iteration (full
+    # rows, 8 + 4 bytes per entry, row pointers, x read and y written once), summed
+    # over the instances' iterations, against the measured copy bandwidth
+    spmv_bytes = []
+    for s_ in solvers:
+        n_i = s_.problem.n_nodes
+        rp = np.empty(n_i + 1, dtype=np.int64)
+        L.check(lib.nlgpu_get_matrix(s_.problem.handle, L.MATRIX_INNER, L.ptr(rp), None, None))
+        full = 2 * int(rp[-1]) - n_i
+        spmv_bytes.append(full * 12 + (n_i + 1) * 8 + 2 * n_i * 8)
+    step_bytes = float((its * np.array(spmv_bytes)[None, :]).sum()) / args.steps
+    pk, pk_kind = peaks()
+    achieved = step_bytes / (total / args.steps) / 1e9
+    roof = {"kernel": "k_batch_spmv (block-diagonal CG SpMV)", "bound": "hbm", "achieved": achieved,
+            "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+            "traffic": None, "algorithmic_bytes_per_step": step_bytes,
+            "note": "SpMV bytes only, over the whole step time (right-hand sides and vector updates not counted)"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = batch_cpu_baseline(specs[:4], dt, tol)
     if rank != 0:
         return 0
     value = len(specs) * args.steps * world / total
@@ -674,20 +694,46 @@ def run_batch(args, world, rank, local, dist):
         "setup_s": setup_s, "clocks": clocks, "gpu_launches": int(launches),
         "e2e": {"value": value, "unit": "instance-steps/s", "h2d_bytes_per_step": 8 * len(specs),
                 "d2h_bytes_per_step": 8 * len(specs)},
-        "roofline": None, "cpu_baseline": None,
+        "roofline": roof, "cpu_baseline": cpu,
     }
     print(json.dumps(line))
     batch.close()
     return 0
 
 
-ONCE_STAGES = ("assembly_fp64", "assembly_ff", "solve_mixed", "solve_fp64", "gemm_bf16")
+def batch_cpu_baseline(specs, dt: float, tol: float, steps: int = 3) -> dict:
+    """The CPU restatement steps a sample of the batched workload's instances
+    (the reference steps one problem at a time: identity CG per step), all host
+    threads; instance-steps per second over the step loops (set-up excluded,
+    as in the GPU figure)."""
+    import oracle
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    oracle.build.build()
+    oracle.set_threads(os.cpu_count() or 1)
+    secs = 0.0
+    for edges, r in specs:
+        mesh = structured_quad_mesh(edges, edges, "bilinear")
+        p = oracle.Problem(oracle.BILINEAR, mesh.nodes, mesh.elements)
+        p.set_model(influence=oracle.INF_FAST_POLYNOMIAL, radius=(r, r), local_weight=0.5)
+        p.add_boundary(oracle.BC_TEMPERATURE, mesh.boundaries["left"], 0.0)
+        p.find_neighbours()
+        p.nonstationary(dt, steps, 10.0, tol=tol, maxit=10000)
+        secs += p.scalar("steps")
+    return {"value": len(specs) * steps / secs, "unit": "instance-steps/s", "cores": os.cpu_count() or 1,
+            "kind": "port",
+            "sample": f"{len(specs)} instances of the workload ({', '.join(f'{e}x{e} r={r:.3f}' for e, r in specs)}), "
+                      f"{steps} implicit Euler steps each (identity CG to {tol:g}, the reference's choice) by the CPU "
+                      "restatement on all host threads; step loops timed, set-up excluded"}
+
+
+ONCE_STAGES = ("assembly_fp64", "assembly_ff", "solve_mixed", "solve_coarse", "solve_fp64", "gemm_bf16")
 
 
 def run_once(args) -> int:
     """One stage of one workload, once, for ncu captures of a single kernel on a
     case of the benchmark's shape: the pair assembly in FP64 or float-float, a
-    whole stationary solve (mixed-precision or plain FP64), or the learned
+    whole stationary solve (mixed-precision without or with the coarse-space
+    correction, or plain FP64), or the learned
     correction's tensor-core GEMM at one message-passing layer's shape (rows =
     the workload's nodes, 128 inputs, 64 outputs)."""
     from nonlocal_gb300 import build as nbuild
@@ -718,8 +764,10 @@ def run_once(args) -> int:
         pb.conductivity_matrix("FULL")
         print(json.dumps({"once": args.once, "workload": args.workload, "scale": s, "element_pairs": pb.pairs}))
     else:
-        _, rep = pb.stationary(tolerance=w["stop_tolerance"] if args.once == "solve_mixed" else METRIC_TOLERANCE,
-                               max_iterations=100000, precision="mixed" if args.once == "solve_mixed" else "fp64")
+        mixed = args.once in ("solve_mixed", "solve_coarse")
+        _, rep = pb.stationary(tolerance=w["stop_tolerance"] if mixed else METRIC_TOLERANCE, max_iterations=100000,
+                               precision="mixed" if mixed else "fp64",
+                               coarse_aggregates=coarse_target(pb.n_nodes) if args.once == "solve_coarse" else 0)
         print(json.dumps({"once": args.once, "workload": args.workload, "scale": s, "iterations": rep.iterations,
                           "residual": rep.residual}))
     return 0

@@ -28,6 +28,8 @@
 #include "ff.cuh"
 #include "influence.cuh"
 
+#include <cmath>
+
 namespace nlgpu {
 
 namespace {
@@ -244,6 +246,7 @@ struct FFArgs {
     const float4* deriv;    // [e][i][q]: (gx.h, gx.l, gy.h, gy.l)
     const float4* qcoord;   // [e][q]: (x.h, x.l, y.h, y.l)
     const float2* cw;       // [e][q]: c_q = w_q norm (1 - p1) [lambda_q]
+    FFExpTable exp_table;   // exp(k / 64), copied to shared memory by each CTA
 };
 
 __global__ void k_ff_stage(i64 E, int nen, int nq, const double* __restrict__ deriv, const double* __restrict__ qcoord,
@@ -277,7 +280,7 @@ struct PairFF {
 // shape<INF> in float-float (fast polynomial, polynomial and exponential with
 // p divisible by n; the host sends the other kinds to the FP64 kernel)
 template<int INF>
-__device__ __forceinline__ ff shape_ff(const Model& m, ff dx, ff dy, ff ir0, ff ir1, ff q) {
+__device__ __forceinline__ ff shape_ff(const Model& m, ff dx, ff dy, ff ir0, ff ir1, ff q, const ff* exp_table) {
     const ff z0 = ff_mul(dx, ir0), z1 = ff_mul(dy, ir1);
     ff d;
     if (m.n == 2) d = ff_add(ff_mul(z0, z0), ff_mul(z1, z1));
@@ -290,7 +293,7 @@ __device__ __forceinline__ ff shape_ff(const Model& m, ff dx, ff dy, ff ir0, ff 
         if constexpr (INF == NLGPU_INFLUENCE_POLYNOMIAL)
             return ff_lt(d, 1.0f) ? ff_ipow(ff_sub(ff_make(1.0f), dp), int(m.q)) : ff_make(0.0f);
         else
-            return ff_exp_nonpositive(ff_neg(ff_mul(q, dp)));
+            return ff_exp_nonpositive(ff_neg(ff_mul(q, dp)), exp_table);
     }
 }
 
@@ -303,6 +306,9 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
     __shared__ i64 row_start[NEN];
     __shared__ int row_len[NEN], row_off[NEN + 1];
     __shared__ int use_smem;
+    __shared__ ff etab[2 * FF_EXP_K + 1];
+    for (int t = threadIdx.x; t < 2 * FF_EXP_K + 1; t += blockDim.x)
+        etab[t] = ff{f.exp_table.v[t].x, f.exp_table.v[t].y};
 
     auto* pairs = reinterpret_cast<PairFF<NEN, NQ>*>(smem_raw);
     double* acc = reinterpret_cast<double*>(smem_raw + sizeof(PairFF<NEN, NQ>) * AS_FF_WARPS);
@@ -380,24 +386,25 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
             for (int t = lane; t < NQ * NQ; t += 32) {
                 const int qL = t / NQ, qNL = t % NQ;
                 ps.phi[t] = ff_mul(ps.c[qNL], shape_ff<INF>(m, ff_sub(eqx[qL], ps.qx[qNL]), ff_sub(eqy[qL], ps.qy[qNL]),
-                                                             ir0, ir1, qf));
+                                                             ir0, ir1, qf, etab));
             }
             __syncwarp();
             for (int t = lane; t < NQ * NEN; t += 32) {
                 const int qL = t / NEN, j = t % NEN;
-                ff h0 = ff_make(0.0f), h1 = ff_make(0.0f);
+                ffdot d0, d1;
 #pragma unroll
                 for (int qNL = 0; qNL < NQ; ++qNL) {
                     const ff fq = ps.phi[qL * NQ + qNL];
                     const ff gx = ps.gx[j * NQ + qNL], gy = ps.gy[j * NQ + qNL];
                     if (m.cond_kind != NLGPU_CONDUCTIVITY_ANISOTROPIC) {
-                        h0 = ff_fma(h0, fq, gx);
-                        h1 = ff_fma(h1, fq, gy);
+                        ffdot_add(d0, fq, gx);
+                        ffdot_add(d1, fq, gy);
                     } else {
-                        h0 = ff_fma(h0, fq, ff_add(ff_mul(k0, gx), ff_mul(k2, gy)));
-                        h1 = ff_fma(h1, fq, ff_add(ff_mul(k2, gx), ff_mul(k1, gy)));
+                        ffdot_add(d0, fq, ff_add(ff_mul(k0, gx), ff_mul(k2, gy)));
+                        ffdot_add(d1, fq, ff_add(ff_mul(k2, gx), ff_mul(k1, gy)));
                     }
                 }
+                ff h0 = ffdot_value(d0), h1 = ffdot_value(d1);
                 if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) { h0 = ff_mul(h0, k0); h1 = ff_mul(h1, k1); }
                 ps.hx[t] = h0;
                 ps.hy[t] = h1;
@@ -414,11 +421,13 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
                 const bool bwd_inner = tr && c_in && r_in && c <= r;
                 const bool bwd_bound = tr && !r_in && c != r;
                 if (!fwd_inner && !fwd_bound && !bwd_inner && !bwd_bound) continue;
-                ff vf = ff_make(0.0f);
+                ffdot dv;
 #pragma unroll
-                for (int qL = 0; qL < NQ; ++qL)
-                    vf = ff_fma(ff_fma(vf, ewx[i * NQ + qL], ps.hx[qL * NEN + j]), ewy[i * NQ + qL], ps.hy[qL * NEN + j]);
-                double v = ff_to(vf);
+                for (int qL = 0; qL < NQ; ++qL) {
+                    ffdot_add(dv, ewx[i * NQ + qL], ps.hx[qL * NEN + j]);
+                    ffdot_add(dv, ewy[i * NQ + qL], ps.hy[qL * NEN + j]);
+                }
+                double v = ff_to(ffdot_value(dv));
                 if (self) {
                     double loc = 0.0;
 #pragma unroll
@@ -614,7 +623,12 @@ void assemble_full(Ctx& ctx) {
         NL_LAUNCH(k_ff_stage, grid_for(ctx.n_elems * nen * nq, 256), 256, 0, ctx.stream, ctx.n_elems, nen, nq,
                   ctx.deriv.p, ctx.qcoord.p, a.cond_field, ctx.model, ctx.basis, ctx.deriv_ff.p, ctx.qcoord_ff.p,
                   ctx.cw_ff.p);
-        const FFArgs f{ctx.deriv_ff.p, ctx.qcoord_ff.p, ctx.cw_ff.p};
+        FFArgs f{ctx.deriv_ff.p, ctx.qcoord_ff.p, ctx.cw_ff.p, {}};
+        for (int k = -FF_EXP_K; k <= FF_EXP_K; ++k) {
+            const double x = std::exp(double(k) / 64.0);
+            const float hi = float(x);
+            f.exp_table.v[k + FF_EXP_K] = make_float2(hi, float(x - double(hi)));
+        }
         if (nen == 4) dispatch_influence_ff<4, 4>(ctx, a, f, sym);
         else dispatch_influence_ff<8, 9>(ctx, a, f, sym);
     } else if (ctx.basis.nen == 4) {

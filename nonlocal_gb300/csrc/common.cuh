@@ -262,6 +262,7 @@ struct IncompleteCholesky {
     dbuf<float> jc, jdinv;       // s_i / u_ii and 1 / u_ii
     dbuf<float> jt0, jt1, jy;    // Jacobi iterates and the scaled forward result
     bool ok = false;
+    bool exact_ready = false;    // fwd / bwd slabs and plans built and filled (ilt_exact_layouts)
     int attempts = 0;
     double shift = 0.0;
 };
@@ -485,6 +486,8 @@ void spmv_full(Ctx& ctx, const Csr& A, const double* x, double* y);
 // triangular solves (without them exact solves use the global-memory sweeps)
 void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plans = true);
 void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* z);
+// the exact sweeps' layouts of a factorised ILLT (once; before any stream capture)
+void ilt_exact_layouts(Ctx& ctx, IncompleteCholesky& ic);
 struct CgResult {
     i64 iterations = 0, outer_iterations = 0;
     double residual = 0, reference_residual = 0;

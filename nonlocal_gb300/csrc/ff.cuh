@@ -80,32 +80,61 @@ __device__ __forceinline__ ff ff_ipow(ff x, int n) {
     return r;
 }
 
-// exp(t) for t <= 0 from the mathematics of the exponential: t = m ln2 + f
-// with |f| <= ln2 / 2, exp(f) = exp(f / 16)^16, and exp(g) for |g| <= 0.0217
-// by its Taylor series through g^9 (remainder below 1e-20 relative), every
-// step in float-float.  Results below 1e-37 are flushed to zero.  ln2 and 1/k!
-// are split into two floats each (hi = float(x), lo = float(x - hi)).
-__device__ __forceinline__ ff ff_exp_nonpositive(ff t) {
+// Compensated dot product of float-float operands (the Dot2 scheme of Ogita,
+// Rump and Oishi, 2005, with float-float inputs): each product's high part
+// goes into a running float sum through TwoSum, and every rounding error --
+// the product's (FMA-exact, with the two cross terms of the low parts) and the
+// sum's -- into one float compensation, folded in once at the end.  12
+// FP32 operations per term instead of the 17 of a renormalised float-float
+// multiply-add; the result is as accurate as float-float arithmetic (errors
+// of order n^2 2^-48 of the terms' magnitudes).
+struct ffdot {
+    float s = 0.0f, c = 0.0f;
+};
+
+__device__ __forceinline__ void ffdot_add(ffdot& acc, ff a, ff b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    const ff t = two_sum(acc.s, p);
+    acc.s = t.h;
+    acc.c = __fadd_rn(acc.c, __fadd_rn(t.l, e));
+}
+
+__device__ __forceinline__ ff ffdot_value(const ffdot& acc) { return quick_two_sum(acc.s, acc.c); }
+
+// exp(k / 64) for k = -FF_EXP_K .. FF_EXP_K as float-float pairs, filled on the
+// host (exp of a double, split hi = float(x), lo = float(x - hi))
+constexpr int FF_EXP_K = 23;
+struct FFExpTable {
+    float2 v[2 * FF_EXP_K + 1];
+};
+
+// exp(t) for t <= 0 from the mathematics of the exponential: t = m ln2 + f with
+// |f| <= ln2 / 2, f = k / 64 + g with |g| <= 1/128, exp(f) = exp(k / 64) exp(g)
+// with exp(k / 64) from the table and exp(g) by its Taylor series through g^6
+// (remainder below 4e-19), every step in float-float.  Results below 1e-37
+// are flushed to zero.  ln2 and 1/k! are split into two floats each.
+__device__ __forceinline__ ff ff_exp_nonpositive(ff t, const ff* table) {
     if (t.h < -85.0f) return ff_make(0.0f);
     const ff ln2{0.6931471824645996f, -1.9046542121259336e-09f};
     const float m = rintf(t.h * 1.4426950216293335f);
     const ff f = ff_sub(t, ff_mul_f(ln2, m));
-    const ff g{f.h * 0.0625f, f.l * 0.0625f};
-    const ff inv_fact[10] = {{1.0f, 0.0f},
-                             {1.0f, 0.0f},
-                             {0.5f, 0.0f},
-                             {0.1666666716337204f, -4.967053879312289e-09f},
-                             {0.0416666679084301f, -1.2417634698280722e-09f},
-                             {0.008333333767950535f, -4.34617203337595e-10f},
-                             {0.0013888889225199819f, -3.3631094437103215e-11f},
-                             {0.00019841270113829523f, -2.725596874933456e-12f},
-                             {2.4801587642286904e-05f, -3.40699609366682e-13f},
-                             {2.7557318844628753e-06f, 3.793571224297229e-14f}};
-    ff p = inv_fact[9];
+    const float k = rintf(f.h * 64.0f);
+    const ff g = ff_sub(f, ff_make(k * 0.015625f));
+    const ff inv_fact[7] = {{1.0f, 0.0f},
+                            {1.0f, 0.0f},
+                            {0.5f, 0.0f},
+                            {0.1666666716337204f, -4.967053879312289e-09f},
+                            {0.0416666679084301f, -1.2417634698280722e-09f},
+                            {0.008333333767950535f, -4.34617203337595e-10f},
+                            {0.0013888889225199819f, -3.3631094437103215e-11f}};
+    ff p = inv_fact[6];
 #pragma unroll
-    for (int k = 8; k >= 0; --k) p = ff_add(ff_mul(p, g), inv_fact[k]);
-#pragma unroll
-    for (int s = 0; s < 4; ++s) p = ff_mul(p, p);
+    for (int j = 5; j >= 0; --j) p = ff_add(ff_mul(p, g), inv_fact[j]);
+    const int ki = min(FF_EXP_K, max(-FF_EXP_K, int(k)));
+    p = ff_mul(p, table[ki + FF_EXP_K]);
     const int e = int(m);
     return ff{ldexpf(p.h, e), ldexpf(p.l, e)};
 }

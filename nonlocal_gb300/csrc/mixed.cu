@@ -583,6 +583,7 @@ void spmv32(Ctx& ctx, const Csr& A, const float* x, float* y) {
 }
 
 void ilt_apply32(Ctx& ctx, IncompleteCholesky& ic, const float* r, float* z, int sweeps) {
+    if (sweeps <= 0) ilt_exact_layouts(ctx, ic);
     ctx.mx.n = ic.n;
     ctx.mx.r64.reserve(size_t(ic.n)); ctx.mx.q64.reserve(size_t(ic.n));
     precondition32(ctx, &ic, r, z, nullptr, nullptr, 0.0, sweeps);
@@ -680,6 +681,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
                      i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps,
                      bool coarse) {
     NL_REQUIRE(!coarse || ctx.co.ready, NLGPU_ERR_STATE, "the coarse correction is not built");
+    if (M && sweeps <= 0) ilt_exact_layouts(ctx, *M);   // exact FP32 sweeps (before any capture)
     NL_REQUIRE(A.up_ok || A.val32.n == size_t(A.nnz), NLGPU_ERR_STATE, "the FP32 copy of the matrix is missing");
     NL_REQUIRE(!learned || (M && ctx.mp.ready && ctx.mp.n == A.rows), NLGPU_ERR_STATE,
                "the learned correction needs ILLT and a prepared network");

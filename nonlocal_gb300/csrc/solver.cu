@@ -506,6 +506,49 @@ void spmv_full(Ctx& ctx, const Csr& A, const double* x, double* y) {
               static_cast<double*>(nullptr), static_cast<const double*>(nullptr));
 }
 
+// The exact level-scheduled sweeps' layouts from the factor's structure (host):
+// level-ELL slabs of both triangles and the TMA-fed shared-memory plans when
+// every dependency fits the ring, with the factor's values.  Built once per
+// factorisation, the first time a solve uses exact sweeps (FP64 ILLT-CG, or
+// the mixed solve with exact FP32 sweeps); not inside a stream capture.
+void ilt_exact_layouts(Ctx& ctx, IncompleteCholesky& ic) {
+    if (ic.exact_ready || !ic.ok) return;
+    const i64 n = ic.n, nnz = ic.nnz;
+    PhaseTimer timer(ctx.stream, "ilt_exact_layouts");
+    std::vector<i64> rp(size_t(n + 1)), lrp(size_t(n + 1)), l_to_u(static_cast<size_t>(nnz));
+    std::vector<int32_t> col(static_cast<size_t>(nnz)), lcol(static_cast<size_t>(nnz));
+    ic.rp.download(rp.data(), rp.size(), ctx.stream);
+    ic.col.download(col.data(), col.size(), ctx.stream);
+    ic.lrp.download(lrp.data(), lrp.size(), ctx.stream);
+    ic.lcol.download(lcol.data(), lcol.size(), ctx.stream);
+    ic.l_to_u.download(l_to_u.data(), l_to_u.size(), ctx.stream);
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+    std::vector<i64> ident(static_cast<size_t>(nnz)), u_diag(static_cast<size_t>(n)), l_diag(static_cast<size_t>(n));
+    std::iota(ident.begin(), ident.end(), i64(0));
+    for (i64 r = 0; r < n; ++r) { u_diag[size_t(r)] = rp[size_t(r)]; l_diag[size_t(r)] = lrp[size_t(r) + 1] - 1; }
+    std::vector<i64> fwd_lev_ptr, bwd_lev_ptr;
+    std::vector<int32_t> fwd_rows, bwd_rows;
+    build_slab(ctx, lrp, lcol, l_to_u, l_diag, true, ic.fwd, &fwd_lev_ptr, &fwd_rows);
+    build_slab(ctx, rp, col, ident, u_diag, false, ic.bwd, &bwd_lev_ptr, &bwd_rows);
+    if (sweep_plan_build(ctx, fwd_lev_ptr, fwd_rows, lrp, lcol, l_to_u, l_diag, ic.fwd_plan))
+        sweep_plan_build(ctx, bwd_lev_ptr, bwd_rows, rp, col, ident, u_diag, ic.bwd_plan);
+    timer.mark("layouts");
+    if (ic.fwd_plan.ok && ic.bwd_plan.ok) {
+        sweep_plan_fill(ctx, ic.fwd_plan, ic.u.p);
+        sweep_plan_fill(ctx, ic.bwd_plan, ic.u.p);
+    }
+    for (TriSlab* sl : {&ic.fwd, &ic.bwd}) {
+        if (sl->entries)
+            NL_LAUNCH(k_slab_values, grid_for(sl->entries, 256), 256, 0, ctx.stream, sl->entries, sl->src.p, ic.u.p,
+                      sl->val.p, sl->val32.p);
+        NL_LAUNCH(k_slab_diag, grid_for(n, 256), 256, 0, ctx.stream, n, sl->diag_src.p, ic.u.p, sl->inv_diag.p,
+                  sl->inv_diag32.p);
+    }
+    NL_CUDA(cudaStreamSynchronize(ctx.stream));
+    ic.exact_ready = true;
+    timer.mark("value fills");
+}
+
 void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plans) {
     const i64 n = upper.rows, nnz = upper.nnz;
     ic.n = n; ic.nnz = nnz;
@@ -519,28 +562,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
     ic.fwd_plan = SweepPlan{};
     ic.bwd_plan = SweepPlan{};
     for (TriSlab* sl : {&ic.fwd, &ic.bwd}) { sl->n_levels = 0; sl->entries = 0; }
-    if (tma_plans) {
-        // the exact level-scheduled sweeps' layouts (host): level-ELL slabs of both
-        // triangles and the TMA-fed shared-memory plans when every dependency fits the ring
-        std::vector<i64> rp(size_t(n + 1)), lrp(size_t(n + 1)), l_to_u(static_cast<size_t>(nnz));
-        std::vector<int32_t> col(static_cast<size_t>(nnz)), lcol(static_cast<size_t>(nnz));
-        ic.rp.download(rp.data(), rp.size(), ctx.stream);
-        ic.col.download(col.data(), col.size(), ctx.stream);
-        ic.lrp.download(lrp.data(), lrp.size(), ctx.stream);
-        ic.lcol.download(lcol.data(), lcol.size(), ctx.stream);
-        ic.l_to_u.download(l_to_u.data(), l_to_u.size(), ctx.stream);
-        NL_CUDA(cudaStreamSynchronize(ctx.stream));
-        std::vector<i64> ident(static_cast<size_t>(nnz)), u_diag(static_cast<size_t>(n)), l_diag(static_cast<size_t>(n));
-        std::iota(ident.begin(), ident.end(), i64(0));
-        for (i64 r = 0; r < n; ++r) { u_diag[size_t(r)] = rp[size_t(r)]; l_diag[size_t(r)] = lrp[size_t(r) + 1] - 1; }
-        std::vector<i64> fwd_lev_ptr, bwd_lev_ptr;
-        std::vector<int32_t> fwd_rows, bwd_rows;
-        build_slab(ctx, lrp, lcol, l_to_u, l_diag, true, ic.fwd, &fwd_lev_ptr, &fwd_rows);
-        build_slab(ctx, rp, col, ident, u_diag, false, ic.bwd, &bwd_lev_ptr, &bwd_rows);
-        if (sweep_plan_build(ctx, fwd_lev_ptr, fwd_rows, lrp, lcol, l_to_u, l_diag, ic.fwd_plan))
-            sweep_plan_build(ctx, bwd_lev_ptr, bwd_rows, rp, col, ident, u_diag, ic.bwd_plan);
-        timer.mark("exact sweep layouts");
-    }
+    ic.exact_ready = false;
     ic.y.resize(size_t(n + 1)); ic.w.resize(size_t(n + 1));
     ic.y32.resize(size_t(n + 1)); ic.w32.resize(size_t(n + 1));
     // Lin-More scaling and the shifted factorisation
@@ -584,28 +606,19 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
     timer.mark("scaling, factorisation");
     if (!ic.ok) return;
     jacobi_fill(ctx, ic);
-    if (ic.fwd_plan.ok && ic.bwd_plan.ok) {
-        sweep_plan_fill(ctx, ic.fwd_plan, ic.u.p);
-        sweep_plan_fill(ctx, ic.bwd_plan, ic.u.p);
-    }
-    for (TriSlab* s : {&ic.fwd, &ic.bwd}) {
-        if (!s->n_levels) continue;   // no exact-sweep layout in this build
-        if (s->entries)
-            NL_LAUNCH(k_slab_values, grid_for(s->entries, 256), 256, 0, ctx.stream, s->entries, s->src.p, ic.u.p,
-                      s->val.p, s->val32.p);
-        NL_LAUNCH(k_slab_diag, grid_for(n, 256), 256, 0, ctx.stream, n, s->diag_src.p, ic.u.p, s->inv_diag.p,
-                  s->inv_diag32.p);
-    }
     timer.mark("value fills");
+    if (tma_plans) ilt_exact_layouts(ctx, ic);
 }
 
 void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* z) {
+    ilt_exact_layouts(ctx, const_cast<IncompleteCholesky&>(ic));
     ctx.cg.n = ic.n;
     precondition(ctx, &ic, r, z, nullptr, nullptr, 0.0);
 }
 
 CgResult cg_solve(Ctx& ctx, const Csr& A, const IncompleteCholesky* M, const double* b, double* x,
                   double tolerance, i64 max_iterations, bool x_is_initial_guess, const CgChunkHook& on_chunk) {
+    if (M) ilt_exact_layouts(ctx, const_cast<IncompleteCholesky&>(*M));
     const i64 n = A.rows;
     CgWork& w = ctx.cg;
     w.n = n;

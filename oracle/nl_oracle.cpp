@@ -1154,6 +1154,7 @@ void orc_nonstationary(void* h, double dt, long steps, double omega, double tol,
     std::vector<double> T(static_cast<size_t>(p.n_nodes), 0.0), f, CT;
     p.history.clear();
     long total_it = 0;
+    const double t_steps = now();
     for (long s = 1; s <= steps; ++s) {
         const double value = std::sin(omega * double(s) * dt);
         f = p.rhs_init;
@@ -1168,6 +1169,7 @@ void orc_nonstationary(void* h, double dt, long steps, double omega, double tol,
         T = x;
         p.history.insert(p.history.end(), T.begin(), T.end());
     }
+    p.timings["steps"] = now() - t_steps;
     p.iterations = total_it;
     p.solution = T;
 }
