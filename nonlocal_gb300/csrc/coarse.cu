@@ -129,47 +129,119 @@ __global__ void __launch_bounds__(CO_THREADS) k_agg_sort(i64 nc, const i64* __re
     }
 }
 
-// Segmented sums of one row's entries by column aggregate: lanes hold 32
-// consecutive entries; a segment is a run of equal aggregates over
-// neighbouring lanes (head flags, segmented inclusive scan), its last lane
-// holds the sum.  Count pass (ap_col null): segments per row; fill pass:
-// (J, sum) in row order.  Rows outside every aggregate get none.
-__global__ void k_ap(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col, const double* __restrict__ val,
-                     const int32_t* __restrict__ agg, i64* __restrict__ cnt, const i64* __restrict__ ap_rp,
-                     int32_t* __restrict__ ap_col, double* __restrict__ ap_val) {
-    const int lane = threadIdx.x & 31;
-    const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
-    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
-        i64 out = ap_col ? ap_rp[r] : 0, count = 0;
-        if (agg[r] >= 0) {
-            for (i64 k0 = rp[r]; k0 < rp[r + 1]; k0 += 32) {
+// AP = A P: entry (r, J) = sum of row r's entries over the columns in
+// aggregate J (Dirichlet columns belong to none).  Warp per row.  A first
+// sweep over the row marks its aggregates in the warp's shared-memory bitmap
+// (nc bits) and counts the runs of equal aggregates in column order; a row
+// with at most AP_MAXD distinct aggregates gets one entry per aggregate, in
+// increasing order, each the sum of its runs in column order (a run's sum by a
+// segmented warp scan, the runs added one after another by lane 0, so the
+// result does not depend on the schedule); a row with more keeps one entry
+// per run.  The count pass (FILL = false) makes the same choice.
+constexpr int AP_WARPS = 8;
+constexpr int AP_MAXD = 128;
+
+inline size_t ap_smem_bytes(i64 nc) {
+    const size_t words = size_t((nc + 31) / 32);
+    return size_t(AP_WARPS) * (2 * words * sizeof(uint32_t) + AP_MAXD * sizeof(double));
+}
+
+template<bool FILL>
+__global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* __restrict__ rp,
+                                                      const int32_t* __restrict__ col, const double* __restrict__ val,
+                                                      const int32_t* __restrict__ agg, i64* __restrict__ cnt,
+                                                      const i64* __restrict__ ap_rp, int32_t* __restrict__ ap_col,
+                                                      double* __restrict__ ap_val) {
+    extern __shared__ __align__(8) unsigned char ap_smem[];
+    const unsigned full = 0xffffffffu;
+    const int words = (nc + 31) >> 5;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double* slot = reinterpret_cast<double*>(ap_smem) + wid * AP_MAXD;
+    uint32_t* bm = reinterpret_cast<uint32_t*>(ap_smem + AP_WARPS * AP_MAXD * sizeof(double)) + wid * 2 * words;
+    int* pre = reinterpret_cast<int*>(bm + words);
+    const i64 warps = i64(gridDim.x) * AP_WARPS;
+    for (i64 r = i64(blockIdx.x) * AP_WARPS + wid; r < n; r += warps) {
+        if (agg[r] < 0) {
+            if (!FILL && lane == 0) cnt[r] = 0;
+            continue;
+        }
+        const i64 rb = rp[r], re = rp[r + 1];
+        for (int w = lane; w < words; w += 32) bm[w] = 0u;
+        __syncwarp();
+        int runs = 0;
+        for (i64 k0 = rb; k0 < re; k0 += 32) {
+            const i64 k = k0 + lane;
+            const int32_t J = k < re ? agg[col[k]] : -1;
+            if (J >= 0) atomicOr(&bm[J >> 5], 1u << (J & 31));
+            const int32_t Jn = __shfl_down_sync(full, J, 1);
+            runs += __popc(__ballot_sync(full, J >= 0 && (lane == 31 || Jn != J)));
+        }
+        __syncwarp();
+        int D = 0;   // distinct aggregates; pre[w] = set bits before word w
+        for (int w0 = 0; w0 < words; w0 += 32) {
+            const int w = w0 + lane;
+            const int c = w < words ? __popc(bm[w]) : 0;
+            int incl = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(full, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (w < words) pre[w] = D + incl - c;
+            D += __shfl_sync(full, incl, 31);
+        }
+        const bool merge = D <= AP_MAXD;
+        if constexpr (!FILL) {
+            if (lane == 0) cnt[r] = merge ? D : runs;
+        } else {
+            for (int t = lane; t < AP_MAXD; t += 32) slot[t] = 0.0;
+            __syncwarp();
+            i64 out = ap_rp[r];
+            for (i64 k0 = rb; k0 < re; k0 += 32) {
                 const i64 k = k0 + lane;
-                const bool valid = k < rp[r + 1];
-                const int32_t J = valid ? agg[col[k]] : -1;   // Dirichlet columns: no aggregate
-                double v = J >= 0 ? val[k] : 0.0;
-                const int32_t Jp = __shfl_up_sync(0xffffffffu, J, 1);
+                const bool valid = k < re;
+                const int32_t J = valid ? agg[col[k]] : -1;
+                const double a = valid ? val[k] : 0.0;
+                double v = J >= 0 ? a : 0.0;
+                const int32_t Jp = __shfl_up_sync(full, J, 1);
                 bool head = lane == 0 || Jp != J;
                 for (int o = 1; o < 32; o <<= 1) {
-                    const double vu = __shfl_up_sync(0xffffffffu, v, o);
-                    const bool hu = __shfl_up_sync(0xffffffffu, head, o);
+                    const double vu = __shfl_up_sync(full, v, o);
+                    const bool hu = __shfl_up_sync(full, head, o);
                     if (lane >= o) {
                         if (!head) v += vu;
                         head = head || hu;
                     }
                 }
-                const int32_t Jn = __shfl_down_sync(0xffffffffu, J, 1);
+                const int32_t Jn = __shfl_down_sync(full, J, 1);
                 const bool end = J >= 0 && (lane == 31 || Jn != J);
-                const unsigned ends = __ballot_sync(0xffffffffu, end);
-                if (ap_col && end) {
-                    const i64 pos = out + __popc(ends & ((1u << lane) - 1u));
-                    ap_col[pos] = J;
-                    ap_val[pos] = v;
+                const unsigned ends = __ballot_sync(full, end);
+                if (merge) {
+                    for (unsigned m = ends; m; m &= m - 1) {
+                        const int src = __ffs(m) - 1;
+                        const double vs = __shfl_sync(full, v, src);
+                        const int32_t Js = __shfl_sync(full, J, src);
+                        if (lane == 0) slot[pre[Js >> 5] + __popc(bm[Js >> 5] & ((1u << (Js & 31)) - 1u))] += vs;
+                    }
+                } else {
+                    if (end) {
+                        const i64 pos = out + __popc(ends & ((1u << lane) - 1u));
+                        ap_col[pos] = J;
+                        ap_val[pos] = v;
+                    }
+                    out += __popc(ends);
                 }
-                out += __popc(ends);
-                count += __popc(ends);
             }
+            __syncwarp();
+            if (merge)
+                for (int w = lane; w < words; w += 32) {
+                    int p = pre[w];
+                    for (uint32_t m = bm[w]; m; m &= m - 1, ++p) {
+                        ap_col[out + p] = w * 32 + __ffs(m) - 1;
+                        ap_val[out + p] = slot[p];
+                    }
+                }
         }
-        if (!ap_col && lane == 0) cnt[r] = count;
+        __syncwarp();
     }
 }
 
@@ -196,28 +268,88 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse_rows(i64 nc, const i64* _
     }
 }
 
-// one Gauss-Jordan step at pivot k, from src into dst (in-place inversion
-// without pivoting for an SPD matrix); block (32, 8): a warp covers 32
-// columns of one row, so the row's pivot-column entry is a broadcast load
-// The pivot's reciprocal comes from pinv[k & 1] (one FP64 division per step,
-// not per entry): the thread that writes the next pivot's entry also stores
-// its reciprocal in the other slot.
-constexpr int GJ_X = 32, GJ_Y = 8;
-__global__ void __launch_bounds__(GJ_X * GJ_Y) k_gauss_jordan(int nc, int k, const double* __restrict__ src,
-                                                              double* __restrict__ dst, double* __restrict__ pinv) {
-    const int j = blockIdx.x * GJ_X + threadIdx.x, i = blockIdx.y * GJ_Y + threadIdx.y;
-    if (i >= nc || j >= nc) return;
-    const double inv_p = pinv[k & 1];
-    const i64 t = i64(i) * nc + j;
-    double v;
-    if (i == k) v = j == k ? inv_p : src[i64(k) * nc + j] * inv_p;
-    else if (j == k) v = -src[i64(i) * nc + k] * inv_p;
-    else v = src[t] - src[i64(i) * nc + k] * (src[i64(k) * nc + j] * inv_p);
-    dst[t] = v;
-    if (i == k + 1 && j == k + 1) pinv[(k + 1) & 1] = 1.0 / v;
+// A_c^-1 by blocked Gauss-Jordan without pivoting (A_c is SPD), in panels of
+// GJ_B pivots on a copy padded to a multiple of GJ_B with an identity block
+// (blockdiag(A_c, I)^-1 = blockdiag(A_c^-1, I)).  For panel P, with
+// D = src[P][P]^-1 and R = D src[P][:], one out-of-place pass writes
+//   dst[P][P] = D,   dst[P][j] = R[j],   dst[i][P] = -src[i][P] D,
+//   dst[i][j] = src[i][j] - src[i][P] R[j]      (i, j outside P),
+// the Gauss-Jordan step of a whole panel: three launches per panel instead
+// of one per pivot, the rank-GJ_B update run as 32x32 tiles from shared memory.
+constexpr int GJ_B = 32;
+
+__global__ void k_gj_pad(int nc, int ncp, const double* __restrict__ a, double* __restrict__ dst) {
+    for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < i64(ncp) * ncp; t += i64(gridDim.x) * blockDim.x) {
+        const int i = int(t / ncp), j = int(t % ncp);
+        dst[t] = (i < nc && j < nc) ? a[i64(i) * nc + j] : (i == j ? 1.0 : 0.0);
+    }
 }
 
-__global__ void k_first_pivot(const double* __restrict__ a, double* __restrict__ pinv) { pinv[0] = 1.0 / a[0]; }
+// D = src[P][P]^-1 by unblocked Gauss-Jordan in shared memory (one CTA, 32x32)
+__global__ void __launch_bounds__(GJ_B * GJ_B) k_gj_diag(int ncp, int k0, const double* __restrict__ src,
+                                                         double* __restrict__ dinv) {
+    __shared__ double d[GJ_B][GJ_B + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    d[ty][tx] = src[i64(k0 + ty) * ncp + k0 + tx];
+    __syncthreads();
+    for (int k = 0; k < GJ_B; ++k) {
+        const double inv = 1.0 / d[k][k];
+        const double dik = d[ty][k], dkj = d[k][tx];
+        double v;
+        if (ty == k) v = tx == k ? inv : dkj * inv;
+        else if (tx == k) v = -dik * inv;
+        else v = d[ty][tx] - dik * (dkj * inv);
+        __syncthreads();
+        d[ty][tx] = v;
+        __syncthreads();
+    }
+    dinv[ty * GJ_B + tx] = d[ty][tx];
+}
+
+// R = D src[P][:] (GJ_B x ncp), a 32-column tile per CTA
+__global__ void __launch_bounds__(GJ_B * GJ_B) k_gj_rows(int ncp, int k0, const double* __restrict__ src,
+                                                         const double* __restrict__ dinv, double* __restrict__ R) {
+    __shared__ double D[GJ_B][GJ_B + 1], S[GJ_B][GJ_B + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y, j = blockIdx.x * GJ_B + tx;
+    D[ty][tx] = dinv[ty * GJ_B + tx];
+    S[ty][tx] = src[i64(k0 + ty) * ncp + j];
+    __syncthreads();
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < GJ_B; ++q) s = fma(D[ty][q], S[q][tx], s);
+    R[i64(ty) * ncp + j] = s;
+}
+
+// one 32x32 tile of dst per CTA
+__global__ void __launch_bounds__(GJ_B * GJ_B) k_gj_update(int ncp, int k0, const double* __restrict__ src,
+                                                           const double* __restrict__ dinv,
+                                                           const double* __restrict__ R, double* __restrict__ dst) {
+    __shared__ double C[GJ_B][GJ_B + 1], T[GJ_B][GJ_B + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.y * GJ_B, j0 = blockIdx.x * GJ_B, i = i0 + ty, j = j0 + tx;
+    const bool pj = j0 == k0;
+    if (i0 == k0) {   // the panel's rows (uniform over the CTA)
+        dst[i64(i) * ncp + j] = pj ? dinv[ty * GJ_B + tx] : R[i64(ty) * ncp + j];
+        return;
+    }
+    C[ty][tx] = src[i64(i) * ncp + k0 + tx];
+    T[ty][tx] = pj ? dinv[ty * GJ_B + tx] : R[i64(ty) * ncp + j];
+    __syncthreads();
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < GJ_B; ++q) s = fma(C[ty][q], T[q][tx], s);
+    dst[i64(i) * ncp + j] = pj ? -s : src[i64(i) * ncp + j] - s;
+}
+
+// the nc x nc part of the padded inverse as FP32
+__global__ void k_inverse_to_f32(int nc, int ncp, const double* __restrict__ a, float* __restrict__ b,
+                                 int* __restrict__ bad) {
+    for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < i64(nc) * nc; t += i64(gridDim.x) * blockDim.x) {
+        const double v = a[(t / nc) * ncp + t % nc];
+        if (!isfinite(v)) *bad = 1;
+        b[t] = float(v);
+    }
+}
 
 __global__ void k_to_f32_co(i64 n, const double* __restrict__ a, float* __restrict__ b, int* __restrict__ bad) {
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
@@ -337,9 +469,12 @@ void coarse_build(Ctx& ctx, const Csr& A, int target) {
     dbuf<i64> cnt;
     cnt.resize(size_t(n) + 1);
     NL_CUDA(cudaMemsetAsync(cnt.p + n, 0, sizeof(i64), ctx.stream));
-    const unsigned gw = grid_for(n * 32, CO_THREADS, 152 * 64);
-    NL_LAUNCH(k_ap, gw, CO_THREADS, 0, ctx.stream, n, A.rowptr.p, A.col.p, A.val.p, co.agg.p, cnt.p,
-              static_cast<const i64*>(nullptr), static_cast<int32_t*>(nullptr), static_cast<double*>(nullptr));
+    const unsigned gw = unsigned(std::max<i64>(1, std::min<i64>((n + AP_WARPS - 1) / AP_WARPS, 152 * 8)));
+    const size_t ap_smem = ap_smem_bytes(nc);
+    NL_CUDA(cudaFuncSetAttribute(k_ap<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ap_smem)));
+    NL_CUDA(cudaFuncSetAttribute(k_ap<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ap_smem)));
+    NL_LAUNCH(k_ap<false>, gw, AP_WARPS * 32, ap_smem, ctx.stream, n, int(nc), A.rowptr.p, A.col.p, A.val.p, co.agg.p,
+              cnt.p, static_cast<const i64*>(nullptr), static_cast<int32_t*>(nullptr), static_cast<double*>(nullptr));
     co.ap_rp.resize(size_t(n) + 1);
     i64 nap = 0;
     exclusive_scan(ctx, cnt.p, co.ap_rp.p, n + 1, &nap);
@@ -347,34 +482,40 @@ void coarse_build(Ctx& ctx, const Csr& A, int target) {
     co.ap_col.resize(size_t(std::max<i64>(nap, 1)));
     dbuf<double> ap64;
     ap64.resize(size_t(std::max<i64>(nap, 1)));
-    NL_LAUNCH(k_ap, gw, CO_THREADS, 0, ctx.stream, n, A.rowptr.p, A.col.p, A.val.p, co.agg.p, cnt.p, co.ap_rp.p,
-              co.ap_col.p, ap64.p);
+    NL_LAUNCH(k_ap<true>, gw, AP_WARPS * 32, ap_smem, ctx.stream, n, int(nc), A.rowptr.p, A.col.p, A.val.p, co.agg.p,
+              cnt.p, co.ap_rp.p, co.ap_col.p, ap64.p);
     co.ap_val.resize(size_t(std::max<i64>(nap, 1)));
     dbuf<int> bad;
     bad.resize(1);
     bad.zero(ctx.stream);
     NL_LAUNCH(k_to_f32_co, grid_for(nap, CO_THREADS), CO_THREADS, 0, ctx.stream, nap, ap64.p, co.ap_val.p, bad.p);
-    dbuf<double> m0, m1;
+    dbuf<double> m0;
     m0.resize(size_t(nc * nc));
-    m1.resize(size_t(nc * nc));
     const size_t row_bytes = size_t(nc) * sizeof(double);
     NL_CUDA(cudaFuncSetAttribute(k_coarse_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, int(row_bytes)));
     NL_LAUNCH(k_coarse_rows, unsigned(std::min<i64>(nc, 152 * 8)), CO_THREADS, row_bytes, ctx.stream, nc, co.ptr.p,
               co.nodes.p, co.ap_rp.p, co.ap_col.p, ap64.p, m0.p);
     timer.mark("AP and A_c");
-    // ---- A_c^-1 by Gauss-Jordan (ping-pong), then FP32
-    double* src = m0.p;
-    double* dst = m1.p;
-    const dim3 gb(unsigned((nc + GJ_X - 1) / GJ_X), unsigned((nc + GJ_Y - 1) / GJ_Y)), tb(GJ_X, GJ_Y);
-    dbuf<double> pinv;
-    pinv.resize(2);
-    NL_LAUNCH(k_first_pivot, 1, 1, 0, ctx.stream, src, pinv.p);
-    for (int k = 0; k < int(nc); ++k) {
-        NL_LAUNCH(k_gauss_jordan, gb, tb, 0, ctx.stream, int(nc), k, src, dst, pinv.p);
+    // ---- A_c^-1 by blocked Gauss-Jordan (ping-pong), then FP32
+    const int ncp = int((nc + GJ_B - 1) / GJ_B * GJ_B);
+    dbuf<double> p0, p1, dinv, R;
+    p0.resize(size_t(ncp) * ncp);
+    p1.resize(size_t(ncp) * ncp);
+    dinv.resize(size_t(GJ_B) * GJ_B);
+    R.resize(size_t(GJ_B) * ncp);
+    NL_LAUNCH(k_gj_pad, grid_for(i64(ncp) * ncp, CO_THREADS), CO_THREADS, 0, ctx.stream, int(nc), ncp, m0.p, p0.p);
+    double* src = p0.p;
+    double* dst = p1.p;
+    const dim3 tb(GJ_B, GJ_B), gr(unsigned(ncp / GJ_B)), gt(unsigned(ncp / GJ_B), unsigned(ncp / GJ_B));
+    for (int k0 = 0; k0 < ncp; k0 += GJ_B) {
+        NL_LAUNCH(k_gj_diag, 1, tb, 0, ctx.stream, ncp, k0, src, dinv.p);
+        NL_LAUNCH(k_gj_rows, gr, tb, 0, ctx.stream, ncp, k0, src, dinv.p, R.p);
+        NL_LAUNCH(k_gj_update, gt, tb, 0, ctx.stream, ncp, k0, src, dinv.p, R.p, dst);
         std::swap(src, dst);
     }
     co.ainv.resize(size_t(nc * nc));
-    NL_LAUNCH(k_to_f32_co, grid_for(nc * nc, CO_THREADS), CO_THREADS, 0, ctx.stream, nc * nc, src, co.ainv.p, bad.p);
+    NL_LAUNCH(k_inverse_to_f32, grid_for(nc * nc, CO_THREADS), CO_THREADS, 0, ctx.stream, int(nc), ncp, src, co.ainv.p,
+              bad.p);
     int hbad = 0;
     NL_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof hbad, cudaMemcpyDeviceToHost, ctx.stream));
     NL_CUDA(cudaStreamSynchronize(ctx.stream));

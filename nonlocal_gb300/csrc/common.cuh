@@ -533,7 +533,7 @@ void add_scaled(Ctx& ctx, double a, const double* x, double* y);
 void add_constant(Ctx& ctx, double a, double* y);
 // iltbuild.cu: U pattern copies, U^T, the factorisation's levels (offsets on the
 // host too) and the Jacobi sweeps' layouts, built on the device
-void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, std::vector<i64>& lev_ptr);
+void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic);
 // jacobi.cu: the factor applied by Jacobi sweeps on its two triangles
 void jacobi_fill(Ctx& ctx, IncompleteCholesky& ic);
 void jacobi_apply32(Ctx& ctx, IncompleteCholesky& ic, int sweeps, const float* r, float* z, const double* flags);

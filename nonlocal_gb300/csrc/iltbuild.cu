@@ -66,9 +66,13 @@ __global__ void k_sort_rows(i64 n, const i64* __restrict__ lrp, int32_t* __restr
 
 // Kahn's algorithm in one CTA: in-degree of row i = off-diagonal entries of
 // its lower row; a finished row releases the rows of its U row.  rows[] holds
-// the levels one after another; lev_ptr[L] their starts.  Every row is
-// finished once and each level finishes at least one row, so the loop ends
-// after at most n levels.
+// the levels one after another; lev_ptr[L] their starts.  LV_SUB threads share
+// a frontier row, so the releases of a whole level (about a hundred rows of a
+// dozen entries on an 8-node mesh) go out as one round of independent
+// atomics.  Every row is finished once and each level finishes at least one
+// row, so the loop ends after at most n levels.  The order of the rows inside
+// a level is that of the atomics; nothing downstream depends on it.
+constexpr int LV_SUB = 8;
 __global__ void __launch_bounds__(IB_LEVEL_THREADS) k_levels(i64 n, const i64* __restrict__ lrp,
                                                              const i64* __restrict__ rp, const int32_t* __restrict__ col,
                                                              int* __restrict__ indeg, int32_t* __restrict__ rows,
@@ -82,14 +86,15 @@ __global__ void __launch_bounds__(IB_LEVEL_THREADS) k_levels(i64 n, const i64* _
         if (d == 0) rows[atomicAdd(&count, 1)] = int32_t(i);
     }
     __syncthreads();
-    int s = 0, e = count;
+    i64 s = 0, e = count;
     i64 L = 0;
     if (threadIdx.x == 0) lev_ptr[0] = 0;
     while (e > s) {
         if (threadIdx.x == 0) lev_ptr[L + 1] = e;
-        for (int t = s + int(threadIdx.x); t < e; t += blockDim.x) {
-            const int32_t i = rows[t];
-            for (i64 k = rp[i] + 1; k < rp[i + 1]; ++k) {
+        for (i64 t = s * LV_SUB + threadIdx.x; t < e * LV_SUB; t += blockDim.x) {
+            const int32_t i = rows[t / LV_SUB];
+            const i64 re = rp[i + 1];
+            for (i64 k = rp[i] + 1 + t % LV_SUB; k < re; k += LV_SUB) {
                 const int32_t c = col[k];
                 if (atomicSub(indeg + c, 1) == 1) rows[atomicAdd(&count, 1)] = c;
             }
@@ -164,9 +169,9 @@ void jacobi_slab_gpu(Ctx& ctx, i64 n, TriRows tr, const int32_t* cols, const i64
 
 }  // namespace
 
-// U pattern copies, U^T, the factorisation's levels (lev_ptr on the host for
-// the per-level launches) and the Jacobi layouts, all on the device
-void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, std::vector<i64>& lev_ptr) {
+// U pattern copies, U^T, the factorisation's rows in level order and the
+// Jacobi layouts, all on the device
+void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     const i64 n = upper.rows, nnz = upper.nnz;
     dbuf<int> bad;
     bad.resize(1);
@@ -208,8 +213,6 @@ void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, std::
     NL_REQUIRE(!hbad, NLGPU_ERR_ARG, "every row of the preconditioner matrix needs its diagonal first");
     NL_REQUIRE(ho[1] == n, NLGPU_ERR_STATE, "the factor's dependency graph does not reach every row");
     ic.ic_levels = ho[0];
-    lev_ptr.resize(size_t(ho[0] + 1));
-    ic.ic_lev_ptr.download(lev_ptr.data(), lev_ptr.size(), ctx.stream);
     // Jacobi layouts of U^T (values u[l_to_u]) and U
     jacobi_slab_gpu(ctx, n, TriRows{ic.lrp.p, true}, ic.lcol.p, ic.l_to_u.p, ic.jlo);
     jacobi_slab_gpu(ctx, n, TriRows{ic.rp.p, false}, ic.col.p, nullptr, ic.jup);

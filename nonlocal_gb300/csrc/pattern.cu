@@ -10,11 +10,12 @@
 // The candidate columns of row r are the nodes of every neighbour eNL of every
 // element eL containing r (nodes of eL itself for the local part).
 //
-// Here one CTA owns a row.  Candidates are OR-ed into a shared-memory bitmap
-// over a window of node numbers (windows repeat when the row spans more
-// nodes than a window holds, so any numbering works), then the set bits are
-// classified and emitted in increasing order with per-thread counts and block
-// scans: the result is the reference's sorted column list without any sort.
+// Here one warp owns a row.  Candidates are OR-ed into the warp's
+// shared-memory bitmap over a window of node numbers (windows repeat when the
+// row spans more nodes than a window holds, so any numbering works), then the
+// set bits are classified a word at a time and emitted in increasing order
+// with warp scans: the result is the reference's sorted column list without
+// any sort.
 // Three lists come out at once: the inner part (upper or full), the bound
 // part, and the full-row inner pattern the solver's SpMV reads (rows padded
 // to a multiple of 4 entries).
@@ -24,15 +25,16 @@ namespace nlgpu {
 
 namespace {
 
-constexpr int PT_THREADS = 256;
-constexpr int PT_WORDS = 10048;                // 321536 node numbers per window (39.3 KB)
-constexpr i64 PT_WINDOW = i64(PT_WORDS) * 32;
-constexpr int PT_ELEM_WORDS = 2048;            // 65536 element numbers for the element bitmap (8 KB)
 constexpr int PT_MAX_ELEMS = 16;               // elements sharing one node
+constexpr int PW_WARPS = 8;                    // rows (warps) per CTA
+constexpr int PW_WORDS = 1024;                 // node bitmap per warp: 32768 node numbers (4 KB)
+constexpr i64 PW_WINDOW = i64(PW_WORDS) * 32;
+constexpr int PW_EWORDS = 512;                 // element bitmap per warp: 16384 element numbers (2 KB)
+constexpr int PW_UNROLL = 4;                   // candidate elements in flight per lane
+constexpr size_t PW_SMEM = size_t(PW_WARPS) * (PW_WORDS + PW_EWORDS) * sizeof(uint32_t);
 
 struct PatternArgs {
     i64 n;
-    int nen;
     bool local_only, symmetric;
     const int32_t* elems;
     const i64* ne_off;
@@ -40,8 +42,10 @@ struct PatternArgs {
     const i64* noff;
     const int32_t* nlist;
     const uint8_t* is_inner;
-    const int32_t* emin;   // smallest / largest node number of every element
+    const uint32_t* inner_bits;   // is_inner as a bitmap (bit c of word c / 32)
+    const int32_t* emin;          // smallest / largest node number of every element
     const int32_t* emax;
+    const int4* nb_range;         // per element: the extreme node and element numbers of its neighbours
     // count pass outputs
     i64* cnt_inner;
     i64* cnt_bound;
@@ -56,178 +60,214 @@ struct PatternArgs {
     int* error;
 };
 
-__device__ __forceinline__ i64 block_scan_excl(i64 v, i64* sh, i64* total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    i64 incl = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        const i64 t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
+__global__ void k_inner_bits(i64 n, const uint8_t* __restrict__ is_inner, uint32_t* __restrict__ bits) {
+    const i64 words = (n + 31) / 32;
+    for (i64 w = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; w < words; w += (i64(gridDim.x) * blockDim.x) >> 5) {
+        const i64 c = w * 32 + (threadIdx.x & 31);
+        const unsigned b = __ballot_sync(0xffffffffu, c < n && is_inner[c]);
+        if ((threadIdx.x & 31) == 0) bits[w] = b;
     }
-    if (lane == 31) sh[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        i64 s = lane < PT_THREADS / 32 ? sh[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-            const i64 t = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += t;
-        }
-        if (lane < PT_THREADS / 32) sh[lane] = s;
-    }
-    __syncthreads();
-    const i64 off = warp ? sh[warp - 1] : 0;
-    *total = sh[PT_THREADS / 32 - 1];
-    __syncthreads();
-    return off + incl - v;
 }
 
-// One CTA per row.  Every candidate column goes into one shared-memory
-// bitmap over a window of node numbers; the set bits are then classified
-// (inner / bound / full) and emitted in increasing order with per-thread
-// counts and block scans.  The window's node range comes from the candidate
-// elements' smallest and largest node numbers, and NEN is a template
-// parameter, so a candidate costs two loads and one shared-memory OR.
-// The elements of a node share most of their neighbours: each candidate
-// element is expanded into its nodes once per row, the first time it is met
-// (an element bitmap over a window of element numbers from the smallest
-// candidate; candidates beyond the window are expanded every time).
-template<int NEN>
-__global__ void __launch_bounds__(PT_THREADS) k_pattern(PatternArgs a) {
-    __shared__ uint32_t bm[PT_WORDS];
-    __shared__ uint32_t ebm[PT_ELEM_WORDS];
-    __shared__ int32_t seg_elem[PT_MAX_ELEMS];
-    __shared__ i64 seg_noff[PT_MAX_ELEMS], seg_len[PT_MAX_ELEMS];
-    __shared__ i64 sh_scan[PT_THREADS / 32];
-    __shared__ int red_min[PT_THREADS / 32], red_max[PT_THREADS / 32], red_emin[PT_THREADS / 32],
-        red_emax[PT_THREADS / 32];
-    const bool fill = a.col_inner != nullptr;
-
-    for (i64 r = blockIdx.x; r < a.n; r += gridDim.x) {
-        const i64 eb = a.ne_off[r], ee = a.ne_off[r + 1];
-        const int ne = int(ee - eb);
-        if (ne > PT_MAX_ELEMS) { if (threadIdx.x == 0) atomicExch(a.error, 1); continue; }
-        if (threadIdx.x < ne) {
-            const int32_t e = a.ne_elem[eb + threadIdx.x];
-            seg_elem[threadIdx.x] = e;
-            seg_noff[threadIdx.x] = a.local_only ? 0 : a.noff[e];
-            seg_len[threadIdx.x] = a.local_only ? 1 : a.noff[e + 1] - a.noff[e];
-        }
-        __syncthreads();
-        const bool row_inner = a.is_inner[r];
-        auto cand_elem = [&](int s, i64 k) -> int32_t {
-            return a.local_only ? seg_elem[s] : a.nlist[seg_noff[s] + k];
-        };
-
-        // node range of the candidates from their elements' extreme nodes, and
-        // the smallest candidate element
+// per element e: (smallest node, largest node, smallest element, largest
+// element) over its neighbour list (warp per element)
+__global__ void k_neighbour_range(i64 E, const i64* __restrict__ noff, const int32_t* __restrict__ nlist,
+                                  const int32_t* __restrict__ emin, const int32_t* __restrict__ emax,
+                                  int4* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const i64 warps = (i64(gridDim.x) * blockDim.x) >> 5;
+    for (i64 e = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; e < E; e += warps) {
         int lo = 0x7fffffff, hi = -1, elo = 0x7fffffff, ehi = -1;
-        for (int s = 0; s < ne; ++s)
-            for (i64 k = threadIdx.x; k < seg_len[s]; k += PT_THREADS) {
-                const int32_t e = cand_elem(s, k);
-                lo = min(lo, a.emin[e]);
-                hi = max(hi, a.emax[e]);
-                elo = min(elo, e);
-                ehi = max(ehi, e);
-            }
+        for (i64 k = noff[e] + lane; k < noff[e + 1]; k += 32) {
+            const int32_t f = nlist[k];
+            lo = min(lo, emin[f]); hi = max(hi, emax[f]);
+            elo = min(elo, f); ehi = max(ehi, f);
+        }
         for (int o = 16; o > 0; o >>= 1) {
             lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
             hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
             elo = min(elo, __shfl_xor_sync(0xffffffffu, elo, o));
             ehi = max(ehi, __shfl_xor_sync(0xffffffffu, ehi, o));
         }
-        if ((threadIdx.x & 31) == 0) {
-            red_min[threadIdx.x >> 5] = lo; red_max[threadIdx.x >> 5] = hi;
-            red_emin[threadIdx.x >> 5] = elo; red_emax[threadIdx.x >> 5] = ehi;
-        }
-        __syncthreads();
-        lo = red_min[0]; hi = red_max[0]; elo = red_emin[0]; ehi = red_emax[0];
-        for (int w = 1; w < PT_THREADS / 32; ++w) {
-            lo = min(lo, red_min[w]); hi = max(hi, red_max[w]); elo = min(elo, red_emin[w]); ehi = max(ehi, red_emax[w]);
-        }
-        __syncthreads();
-
-        i64 n_inner = 0, n_bound = 0, n_full = 0;
-        if (!row_inner) {   // Dirichlet row: unit diagonal only in the inner parts
-            n_inner = 1; n_full = 1;
-            if (fill && threadIdx.x == 0) { a.col_inner[a.rp_inner[r]] = int32_t(r); a.col_full[a.rp_full[r]] = int32_t(r); }
-        }
-        for (i64 base = lo; hi >= 0 && base <= hi; base += PT_WINDOW) {
-            // clear only the words the candidates can reach
-            const int node_words = int(min(i64(hi) - base, PT_WINDOW - 1) >> 5) + 1;
-            for (int w = threadIdx.x; w < node_words; w += PT_THREADS) bm[w] = 0u;
-            if (ne > 1) {
-                const int elem_words = int(min(i64(ehi) - elo, i64(PT_ELEM_WORDS) * 32 - 1) >> 5) + 1;
-                for (int w = threadIdx.x; w < elem_words; w += PT_THREADS) ebm[w] = 0u;
-            }
-            __syncthreads();
-            for (int s = 0; s < ne; ++s)
-                for (i64 k = threadIdx.x; k < seg_len[s]; k += PT_THREADS) {
-                    const int32_t e = cand_elem(s, k);
-                    if (ne > 1) {   // an element met before in this row adds nothing new
-                        const i64 eo = i64(e) - elo;
-                        if (eo < i64(PT_ELEM_WORDS) * 32) {
-                            const uint32_t bit = 1u << (eo & 31);
-                            if (atomicOr(&ebm[eo >> 5], bit) & bit) continue;
-                        }
-                    }
-#pragma unroll
-                    for (int j = 0; j < NEN; ++j) {
-                        const i64 off = i64(a.elems[i64(e) * NEN + j]) - base;
-                        if (off < 0 || off >= PT_WINDOW) continue;
-                        atomicOr(&bm[off >> 5], 1u << (off & 31));
-                    }
-                }
-            __syncthreads();
-            const i64 span = min(i64(hi) - base + 1, PT_WINDOW);
-            const int words = int((span + 31) >> 5);
-            const int per = (words + PT_THREADS - 1) / PT_THREADS;
-            const int w0 = threadIdx.x * per, w1 = min(words, w0 + per);
-            // matrix_separator_base::part on every distinct candidate column
-            auto classify = [&](int32_t c, bool& in_inner, bool& in_bound, bool& in_full) {
-                const bool c_in = a.is_inner[c];
-                in_full = c_in && row_inner;
-                in_inner = in_full && (!a.symmetric || r <= c);
-                in_bound = !c_in && c != r;
-            };
-            i64 ci = 0, cb = 0, cf = 0;
-            for (int w = w0; w < w1; ++w)
-                for (uint32_t m = bm[w]; m; m &= m - 1) {
-                    bool ii, bb, ff;
-                    classify(int32_t(base + i64(w) * 32 + __ffs(m) - 1), ii, bb, ff);
-                    ci += ii; cb += bb; cf += ff;
-                }
-            i64 ti, tb, tf;
-            const i64 oi = block_scan_excl(ci, sh_scan, &ti);
-            const i64 ob = block_scan_excl(cb, sh_scan, &tb);
-            const i64 of = block_scan_excl(cf, sh_scan, &tf);
-            if (fill) {
-                i64 pi = a.rp_inner[r] + n_inner + oi, pb = a.rp_bound[r] + n_bound + ob, pf = a.rp_full[r] + n_full + of;
-                for (int w = w0; w < w1; ++w)
-                    for (uint32_t m = bm[w]; m; m &= m - 1) {
-                        const int32_t c = int32_t(base + i64(w) * 32 + __ffs(m) - 1);
-                        bool ii, bb, ff;
-                        classify(c, ii, bb, ff);
-                        if (ii) a.col_inner[pi++] = c;
-                        if (bb) a.col_bound[pb++] = c;
-                        if (ff) a.col_full[pf++] = c;
-                    }
-            }
-            n_inner += ti; n_bound += tb; n_full += tf;
-            __syncthreads();
-        }
-        if (!fill) {
-            if (threadIdx.x == 0) { a.cnt_inner[r] = n_inner; a.cnt_bound[r] = n_bound; a.cnt_full[r] = (n_full + 3) & ~i64(3); }
-        } else {   // pad the solver row to a multiple of 4 with (r, 0) entries
-            const i64 end = a.rp_full[r + 1];
-            for (i64 k = a.rp_full[r] + n_full + threadIdx.x; k < end; k += PT_THREADS) a.col_full[k] = int32_t(r);
-        }
-        __syncthreads();
+        if (lane == 0) out[e] = make_int4(lo, hi, elo, ehi);
     }
 }
 
-void launch_pattern(Ctx& ctx, unsigned grid, const PatternArgs& a) {
-    if (a.nen == 4) NL_LAUNCH(k_pattern<4>, grid, PT_THREADS, 0, ctx.stream, a);
-    else if (a.nen == 8) NL_LAUNCH(k_pattern<8>, grid, PT_THREADS, 0, ctx.stream, a);
-    else NL_REQUIRE(false, NLGPU_ERR_UNSUPPORTED, "elements of 4 or 8 nodes");
+// bits b of the word of node numbers [nb, nb + 32) with nb + b >= r
+__device__ __forceinline__ uint32_t mask_from(i64 r, i64 nb) {
+    if (r <= nb) return 0xffffffffu;
+    if (r >= nb + 32) return 0u;
+    return ~((1u << unsigned(r - nb)) - 1u);
+}
+
+__device__ __forceinline__ uint32_t bit_of(i64 r, i64 nb) {
+    return (r >= nb && r < nb + 32) ? (1u << unsigned(r - nb)) : 0u;
+}
+
+template<int NEN>
+__device__ __forceinline__ void load_nodes(const int32_t* __restrict__ elems, int32_t e, int32_t (&v)[NEN]) {
+    const int4* p = reinterpret_cast<const int4*>(elems + i64(e) * NEN);
+#pragma unroll
+    for (int h = 0; h < NEN / 4; ++h) {
+        const int4 q = __ldg(p + h);
+        v[4 * h] = q.x; v[4 * h + 1] = q.y; v[4 * h + 2] = q.z; v[4 * h + 3] = q.w;
+    }
+}
+
+// One warp per row.  The candidate columns go into the warp's shared-memory
+// bitmap over a window of node numbers (from the precomputed extreme node
+// numbers of the row's elements' neighbours; rows spanning more than one
+// window take several, so any numbering works).  The elements of a node share
+// most of their neighbours: a second bitmap over element numbers lets each
+// candidate element be expanded into its nodes once per row (candidates
+// beyond that window are expanded every time).  The set bits are then
+// classified a word at a time against the inner-node bitmap and emitted in
+// increasing order, 32 words per round with a warp scan of the counts: the
+// reference's sorted column list without a sort.
+template<int NEN>
+__global__ void __launch_bounds__(PW_WARPS * 32) k_pattern(PatternArgs a) {
+    extern __shared__ uint32_t pw_smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t* bm = pw_smem + wid * PW_WORDS;
+    uint32_t* ebm = pw_smem + PW_WARPS * PW_WORDS + wid * PW_EWORDS;
+    const unsigned full = 0xffffffffu;
+    const bool fill = a.col_inner != nullptr;
+    const i64 warps = i64(gridDim.x) * PW_WARPS;
+
+    for (i64 r = i64(blockIdx.x) * PW_WARPS + wid; r < a.n; r += warps) {
+        const i64 eb = a.ne_off[r];
+        const int ne = int(a.ne_off[r + 1] - eb);
+        if (ne > PT_MAX_ELEMS) { if (lane == 0) atomicExch(a.error, 1); continue; }
+        int32_t my_e = -1;
+        i64 my_off = 0;
+        int my_len = 0, lo = 0x7fffffff, hi = -1, elo = 0x7fffffff, ehi = -1;
+        if (lane < ne) {
+            my_e = a.ne_elem[eb + lane];
+            if (a.local_only) {
+                lo = a.emin[my_e]; hi = a.emax[my_e];
+            } else {
+                my_off = a.noff[my_e];
+                my_len = int(a.noff[my_e + 1] - my_off);
+                const int4 g = a.nb_range[my_e];
+                lo = g.x; hi = g.y; elo = g.z; ehi = g.w;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(full, lo, o));
+            hi = max(hi, __shfl_xor_sync(full, hi, o));
+            elo = min(elo, __shfl_xor_sync(full, elo, o));
+            ehi = max(ehi, __shfl_xor_sync(full, ehi, o));
+        }
+        const bool row_inner = a.is_inner[r];
+        i64 n_inner = 0, n_bound = 0, n_full = 0;
+        if (!row_inner) {   // Dirichlet row: unit diagonal only in the inner parts
+            n_inner = 1; n_full = 1;
+            if (fill && lane == 0) { a.col_inner[a.rp_inner[r]] = int32_t(r); a.col_full[a.rp_full[r]] = int32_t(r); }
+        }
+        const bool dedupe = !a.local_only && ne > 1;
+        const i64 elem_span = min(i64(ehi) - elo, i64(PW_EWORDS) * 32 - 1);
+        for (i64 base = i64(lo) & ~i64(31); hi >= 0 && base <= hi; base += PW_WINDOW) {
+            const int nw = int(min(i64(hi) - base, PW_WINDOW - 1) >> 5) + 1;
+            for (int w = lane; w < nw; w += 32) bm[w] = 0u;
+            if (dedupe)
+                for (int w = lane; w <= int(elem_span >> 5); w += 32) ebm[w] = 0u;
+            __syncwarp();
+            auto expand = [&](int32_t e) {
+                int32_t v[NEN];
+                load_nodes<NEN>(a.elems, e, v);
+#pragma unroll
+                for (int j = 0; j < NEN; ++j) {
+                    const i64 off = i64(v[j]) - base;
+                    if (off >= 0 && off < PW_WINDOW) atomicOr(&bm[off >> 5], 1u << (off & 31));
+                }
+            };
+            if (a.local_only) {
+                if (lane < ne) expand(my_e);
+            } else {
+                for (int s = 0; s < ne; ++s) {
+                    const i64 off = __shfl_sync(full, my_off, s);
+                    const int len = __shfl_sync(full, my_len, s);
+                    for (int k0 = 0; k0 < len; k0 += 32 * PW_UNROLL) {
+                        int32_t e[PW_UNROLL];
+#pragma unroll
+                        for (int u = 0; u < PW_UNROLL; ++u) {
+                            const int k = k0 + u * 32 + lane;
+                            e[u] = k < len ? a.nlist[off + k] : -1;
+                        }
+                        if (dedupe) {   // an element met before in this row adds nothing new
+#pragma unroll
+                            for (int u = 0; u < PW_UNROLL; ++u) {
+                                const i64 eo = i64(e[u]) - elo;
+                                if (e[u] >= 0 && eo < i64(PW_EWORDS) * 32) {
+                                    const uint32_t bit = 1u << (eo & 31);
+                                    if (atomicOr(&ebm[eo >> 5], bit) & bit) e[u] = -1;
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < PW_UNROLL; ++u)
+                            if (e[u] >= 0) expand(e[u]);
+                    }
+                }
+            }
+            __syncwarp();
+            // matrix_separator_base::part a word at a time, 32 words per round
+            for (int w0 = 0; w0 < nw; w0 += 32) {
+                const int w = w0 + lane;
+                const i64 nb = base + i64(w) * 32;
+                uint32_t m = 0u, iw = 0u;
+                if (w < nw) {
+                    m = bm[w];
+                    if (m) iw = a.inner_bits[nb >> 5];
+                }
+                const uint32_t mf = row_inner ? (m & iw) : 0u;
+                const uint32_t mi = a.symmetric ? (mf & mask_from(r, nb)) : mf;
+                const uint32_t mb = m & ~iw & ~bit_of(r, nb);
+                // three counts (each <= 1024 per round) packed in 21-bit fields
+                const unsigned long long c = (unsigned long long)__popc(mi) |
+                                             ((unsigned long long)__popc(mb) << 21) |
+                                             ((unsigned long long)__popc(mf) << 42);
+                unsigned long long incl = c;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned long long t = __shfl_up_sync(full, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const unsigned long long tot = __shfl_sync(full, incl, 31);
+                if (fill) {
+                    const unsigned long long ex = incl - c;
+                    const unsigned long long f21 = (1ull << 21) - 1;
+                    i64 pi = a.rp_inner[r] + n_inner + i64(ex & f21);
+                    i64 pb = a.rp_bound[r] + n_bound + i64((ex >> 21) & f21);
+                    i64 pf = a.rp_full[r] + n_full + i64(ex >> 42);
+                    for (uint32_t t = mi; t; t &= t - 1) a.col_inner[pi++] = int32_t(nb + __ffs(t) - 1);
+                    for (uint32_t t = mb; t; t &= t - 1) a.col_bound[pb++] = int32_t(nb + __ffs(t) - 1);
+                    for (uint32_t t = mf; t; t &= t - 1) a.col_full[pf++] = int32_t(nb + __ffs(t) - 1);
+                }
+                n_inner += i64(tot & ((1ull << 21) - 1));
+                n_bound += i64((tot >> 21) & ((1ull << 21) - 1));
+                n_full += i64(tot >> 42);
+            }
+            __syncwarp();
+        }
+        if (!fill) {
+            if (lane == 0) { a.cnt_inner[r] = n_inner; a.cnt_bound[r] = n_bound; a.cnt_full[r] = (n_full + 3) & ~i64(3); }
+        } else {   // pad the solver row to a multiple of 4 with (r, 0) entries
+            const i64 end = a.rp_full[r + 1];
+            for (i64 k = a.rp_full[r] + n_full + lane; k < end; k += 32) a.col_full[k] = int32_t(r);
+        }
+    }
+}
+
+void launch_pattern(Ctx& ctx, int nen, unsigned grid, const PatternArgs& a) {
+    if (nen == 4) {
+        NL_CUDA(cudaFuncSetAttribute(k_pattern<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(PW_SMEM)));
+        NL_LAUNCH(k_pattern<4>, grid, PW_WARPS * 32, PW_SMEM, ctx.stream, a);
+    } else if (nen == 8) {
+        NL_CUDA(cudaFuncSetAttribute(k_pattern<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(PW_SMEM)));
+        NL_LAUNCH(k_pattern<8>, grid, PW_WARPS * 32, PW_SMEM, ctx.stream, a);
+    } else {
+        NL_REQUIRE(false, NLGPU_ERR_UNSUPPORTED, "elements of 4 or 8 nodes");
+    }
 }
 
 // full-row entry -> index of the same value in the upper storage (or -1 for padding)
@@ -279,14 +319,27 @@ void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* 
     dbuf<int> err;
     err.resize(1); err.zero(ctx.stream);
     PatternArgs a{};
-    a.n = n; a.nen = ctx.basis.nen; a.local_only = local_only; a.symmetric = symmetric;
+    a.n = n; a.local_only = local_only; a.symmetric = symmetric;
     a.elems = ctx.elems.p; a.ne_off = ctx.ne_off.p; a.ne_elem = ctx.ne_elem.p;
     a.noff = local_only ? nullptr : ctx.noff.p; a.nlist = local_only ? nullptr : ctx.nlist.p;
     a.is_inner = is_inner ? is_inner : ctx.is_inner.p;
     a.emin = ctx.elem_minnode.p; a.emax = ctx.elem_maxnode.p;
     a.cnt_inner = ci.p; a.cnt_bound = cb.p; a.cnt_full = cf.p; a.error = err.p;
-    const unsigned grid = unsigned(std::min<i64>(n, 152 * 8));
-    launch_pattern(ctx, grid, a);
+    dbuf<uint32_t> bits;
+    bits.resize(size_t((n + 31) / 32 + 1));
+    NL_LAUNCH(k_inner_bits, grid_for((n + 31) / 32 * 32, 256), 256, 0, ctx.stream, n, a.is_inner, bits.p);
+    a.inner_bits = bits.p;
+    dbuf<int4> range;
+    if (!local_only) {
+        const i64 E = ctx.n_elems;
+        range.resize(size_t(std::max<i64>(E, 1)));
+        NL_LAUNCH(k_neighbour_range, grid_for(E * 32, 256, 152 * 64), 256, 0, ctx.stream, E, ctx.noff.p, ctx.nlist.p,
+                  ctx.elem_minnode.p, ctx.elem_maxnode.p, range.p);
+        a.nb_range = range.p;
+    }
+    const int nen = ctx.basis.nen;
+    const unsigned grid = unsigned(std::max<i64>(1, std::min<i64>((n + PW_WARPS - 1) / PW_WARPS, 152 * 4 * 8)));
+    launch_pattern(ctx, nen, grid, a);
     int herr = 0;
     NL_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof herr, cudaMemcpyDeviceToHost, ctx.stream));
     i64 nnz_i = 0, nnz_b = 0, nnz_f = 0;
@@ -305,7 +358,7 @@ void build_patterns(Ctx& ctx, bool local_only, bool symmetric, Csr& inner, Csr* 
     a.rp_inner = inner.rowptr.p; a.rp_bound = B.rowptr.p; a.rp_full = F.rowptr.p;
     a.col_inner = inner.col.p; a.col_bound = B.col.p; a.col_full = F.col.p;
     // count pointers stay set but are not written in the fill pass
-    launch_pattern(ctx, grid, a);
+    launch_pattern(ctx, nen, grid, a);
     inner.val.resize(size_t(nnz_i)); inner.val.zero(ctx.stream);
     B.val.resize(size_t(nnz_b)); B.val.zero(ctx.stream);
     if (full && full_from_upper) {

@@ -209,37 +209,69 @@ __global__ void k_scaled(i64 n, const i64* __restrict__ rp, const int32_t* __res
 
 // Up-looking IC(0): U has the pattern of the upper matrix; row i subtracts
 // u_ki * row k for every k < i with u_ki != 0 (L row i, with its U position in
-// l_to_u), then divides by the root of its pivot.  One launch per level, one
-// warp per row of the level (rows of one level only read rows of earlier
-// levels).  Lane y owns entry y of row i (rows of up to 32 entries; longer
-// rows run the sequential merge on lane 0).  For up to IC_MAXS rows k of L row i at a time,
-// the warp's lanes spread over the entries of those rows' segments (columns
-// >= i), each finds its column among row i's (binary search in shared memory)
-// and stores u_ki u_kj in a table; lane y then subtracts the table's column y
-// in the order of k, as the sequential form does (product and subtraction
-// rounded separately).  The chain of dependent global loads per row is a few
-// instead of one per merge step.
+// l_to_u), then divides by the root of its pivot.
+//
+// Synchronisation-free schedule (after Liu, Li, Hou and Vinter, "A
+// synchronization-free algorithm for parallel sparse triangular solves",
+// Euro-Par 2016): one launch for the whole factorisation; each warp takes the
+// next row from a ticket counter over the rows in dependency-level order,
+// loads the row's structure, waits until every row k of L row i has
+// published its U row (done[k], stored with release semantics after the
+// row's values; the wait is bounded by %globaltimer and reports a timeout),
+// reads those rows through L2, computes and publishes its own.  A row's
+// dependencies come earlier in the level order, so their tickets went to
+// warps that are already running: the oldest unfinished row can always
+// proceed, and rows of consecutive levels overlap instead of waiting for a
+// launch boundary.
+//
+// Inside a row: lane y owns entry y of row i (rows of up to 32 entries;
+// longer rows run the sequential merge on lane 0).  For up to IC_MAXS rows k
+// of L row i at a time, the lanes spread over the entries of those rows'
+// segments (columns >= i), each finds its column among row i's (binary search
+// in shared memory) and stores u_ki u_kj in a table; lane y then subtracts
+// the table's column y in the order of k, as the sequential form does
+// (product and subtraction rounded separately), so the result does not depend
+// on the schedule.
 constexpr int IC_WARPS = 8;
 constexpr int IC_MAXS = 16;
+constexpr unsigned long long IC_WAIT_LIMIT_NS = 2000000000ull;
 
+__device__ __forceinline__ unsigned long long ic_globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// rows of other warps are read through L2 (__ldcg): they were written after
+// this SM may have cached the lines
 __device__ void ic0_row_sequential(int32_t i, const i64* __restrict__ rp, const int32_t* __restrict__ col,
                                    const double* __restrict__ a, double shift, const i64* __restrict__ lrp,
-                                   const int32_t* __restrict__ lcol, const i64* __restrict__ l_to_u,
-                                   double* __restrict__ u, int* __restrict__ failed) {
+                                   const int32_t* __restrict__ lcol, const i64* __restrict__ l_to_u, double* u,
+                                   int* __restrict__ failed) {
     const i64 b = rp[i], e = rp[i + 1];
     for (i64 s = b; s < e; ++s) u[s] = a[s];
     u[b] += shift;
     for (i64 s = lrp[i]; s < lrp[i + 1] - 1; ++s) {
         const int32_t k = lcol[s];
         const i64 pk = l_to_u[s];
-        const double uki = u[pk];
+        const double uki = __ldcg(u + pk);
         i64 x = pk, y = b;
         const i64 ke = rp[k + 1];
         while (x < ke && y < e) {
             const int32_t cx = col[x], cy = col[y];
             if (cx < cy) ++x;
             else if (cx > cy) ++y;
-            else { u[y] = __dsub_rn(u[y], __dmul_rn(uki, u[x])); ++x; ++y; }
+            else { u[y] = __dsub_rn(u[y], __dmul_rn(uki, __ldcg(u + x))); ++x; ++y; }
         }
     }
     const double d = u[b];
@@ -249,80 +281,107 @@ __device__ void ic0_row_sequential(int32_t i, const i64* __restrict__ rp, const 
     for (i64 s = b + 1; s < e; ++s) u[s] /= rd;
 }
 
-__global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_level(i64 t0, i64 t1, const int32_t* __restrict__ lev_rows,
-                                                             const i64* __restrict__ rp, const int32_t* __restrict__ col,
-                                                             const double* __restrict__ a, double shift,
-                                                             const i64* __restrict__ lrp,
-                                                             const int32_t* __restrict__ lcol,
-                                                             const i64* __restrict__ l_to_u, double* __restrict__ u,
-                                                             int* __restrict__ failed) {
+__global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t* __restrict__ order,
+                                                            const i64* __restrict__ rp, const int32_t* __restrict__ col,
+                                                            const double* __restrict__ a, double shift,
+                                                            const i64* __restrict__ lrp,
+                                                            const int32_t* __restrict__ lcol,
+                                                            const i64* __restrict__ l_to_u, double* u,
+                                                            int* __restrict__ ticket, int* done,
+                                                            int* __restrict__ failed, int* __restrict__ timed_out) {
     __shared__ double table[IC_WARPS][IC_MAXS][32];
     __shared__ int32_t rowcol[IC_WARPS][32];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
-    const i64 t = t0 + i64(blockIdx.x) * IC_WARPS + wb;
-    if (t >= t1) return;   // whole warps
-    const int32_t i = lev_rows[t];
-    const i64 b = rp[i], e = rp[i + 1];
-    const int m = int(e - b);
-    if (m > 32) {
-        if (lane == 0) ic0_row_sequential(i, rp, col, a, shift, lrp, lcol, l_to_u, u, failed);
-        return;
-    }
-    const bool own = lane < m;
-    rowcol[wb][lane] = own ? col[b + lane] : 0x7fffffff;
-    double acc = own ? a[b + lane] : 0.0;
-    if (lane == 0) acc += shift;
-    const i64 lb = lrp[i], le = lrp[i + 1] - 1;   // L row i without its diagonal (its last entry)
-    for (i64 s0 = lb; s0 < le; s0 += IC_MAXS) {
-        const int ns = le - s0 < IC_MAXS ? int(le - s0) : IC_MAXS;
-        i64 pk = 0;
-        double uki = 0.0;
-        int len = 0;
-        if (lane < ns) {
-            pk = l_to_u[s0 + lane];   // (k, i) in U: row k's segment from column i on
-            len = int(rp[lcol[s0 + lane] + 1] - pk);
-            uki = u[pk];
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(ticket, 1);
+        t = __shfl_sync(full, t, 0);
+        if (t >= n) break;
+        const int32_t i = order[t];
+        const i64 b = rp[i], e = rp[i + 1];
+        const int m = int(e - b);
+        const i64 lb = lrp[i], le = lrp[i + 1] - 1;   // L row i without its diagonal (its last entry)
+        const bool own = lane < m;
+        double acc = 0.0;
+        if (m <= 32) {
+            rowcol[wb][lane] = own ? col[b + lane] : 0x7fffffff;
+            acc = own ? a[b + lane] : 0.0;
+            if (lane == 0) acc += shift;
         }
-        int incl = len;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(full, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const int total = __shfl_sync(full, incl, 31);
-        for (int q = 0; q < ns; ++q) table[wb][q][lane] = 0.0;
-        __syncwarp();
-        for (int base = 0; base < total; base += 32) {
-            const int idx = base + lane;
-            int s = 0;
-            for (int q = 0; q < ns; ++q) s += __shfl_sync(full, incl, q) <= idx ? 1 : 0;
-            const int sc = min(s, ns - 1);
-            const int start = __shfl_sync(full, incl, max(sc - 1, 0)) * (sc > 0 ? 1 : 0);
-            const i64 pks = __shfl_sync(full, pk, sc);
-            const double ukis = __shfl_sync(full, uki, sc);
-            if (idx < total) {
-                const i64 x = pks + (idx - start);
-                const int32_t cx = col[x];
-                int lo = 0, hi = m;   // column cx among row i's
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (rowcol[wb][mid] < cx) lo = mid + 1; else hi = mid;
+        // wait for the rows this row reads
+        bool gave_up = false;
+        for (i64 s = lb + lane; s < le && !gave_up; s += 32) {
+            const int* flag = done + lcol[s];
+            if (ld_acquire_gpu(flag) == 0) {
+                const unsigned long long t0 = ic_globaltimer();
+                while (ld_acquire_gpu(flag) == 0) {
+                    if (ic_globaltimer() - t0 > IC_WAIT_LIMIT_NS) { gave_up = true; break; }
+                    __nanosleep(32);
                 }
-                if (lo < m && rowcol[wb][lo] == cx) table[wb][s][lo] = __dmul_rn(ukis, u[x]);
             }
         }
+        if (__any_sync(full, gave_up) && lane == 0) atomicExch(timed_out, 1);
         __syncwarp();
-        for (int q = 0; q < ns; ++q) acc = __dsub_rn(acc, table[wb][q][lane]);
+        if (m > 32) {
+            if (lane == 0) ic0_row_sequential(i, rp, col, a, shift, lrp, lcol, l_to_u, u, failed);
+        } else {
+            for (i64 s0 = lb; s0 < le; s0 += IC_MAXS) {
+                const int ns = le - s0 < IC_MAXS ? int(le - s0) : IC_MAXS;
+                i64 pk = 0;
+                double uki = 0.0;
+                int len = 0;
+                if (lane < ns) {
+                    pk = l_to_u[s0 + lane];   // (k, i) in U: row k's segment from column i on
+                    len = int(rp[lcol[s0 + lane] + 1] - pk);
+                    uki = __ldcg(u + pk);
+                }
+                int incl = len;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(full, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const int total = __shfl_sync(full, incl, 31);
+                for (int q = 0; q < ns; ++q) table[wb][q][lane] = 0.0;
+                __syncwarp();
+                for (int base = 0; base < total; base += 32) {
+                    const int idx = base + lane;
+                    int s = 0;
+                    for (int q = 0; q < ns; ++q) s += __shfl_sync(full, incl, q) <= idx ? 1 : 0;
+                    const int sc = min(s, ns - 1);
+                    const int start = __shfl_sync(full, incl, max(sc - 1, 0)) * (sc > 0 ? 1 : 0);
+                    const i64 pks = __shfl_sync(full, pk, sc);
+                    const double ukis = __shfl_sync(full, uki, sc);
+                    if (idx < total) {
+                        const i64 x = pks + (idx - start);
+                        const int32_t cx = col[x];
+                        int lo = 0, hi = m;   // column cx among row i's
+                        while (lo < hi) {
+                            const int mid = (lo + hi) >> 1;
+                            if (rowcol[wb][mid] < cx) lo = mid + 1; else hi = mid;
+                        }
+                        if (lo < m && rowcol[wb][lo] == cx) table[wb][s][lo] = __dmul_rn(ukis, __ldcg(u + x));
+                    }
+                }
+                __syncwarp();
+                for (int q = 0; q < ns; ++q) acc = __dsub_rn(acc, table[wb][q][lane]);
+                __syncwarp();
+            }
+            const double d = __shfl_sync(full, acc, 0);
+            if (!(d > 0.0)) {
+                if (lane == 0) atomicExch(failed, 1);
+            } else {
+                const double rd = sqrt(d);
+                if (lane == 0) u[b] = rd;
+                else if (own) u[b + lane] = acc / rd;
+            }
+        }
+        // publish row i (a failed pivot publishes too: the attempt is retried
+        // with a larger shift, and no row may wait for ever)
+        __threadfence();
         __syncwarp();
+        if (lane == 0) st_release_gpu(done + i, 1);
     }
-    const double d = __shfl_sync(full, acc, 0);
-    if (!(d > 0.0)) {
-        if (lane == 0) atomicExch(failed, 1);
-        return;
-    }
-    const double rd = sqrt(d);
-    if (lane == 0) u[b] = rd;
-    else if (own) u[b + lane] = acc / rd;
 }
 
 __global__ void k_slab_values(i64 count, const i64* __restrict__ src, const double* __restrict__ u,
@@ -554,8 +613,7 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
     ic.n = n; ic.nnz = nnz;
     PhaseTimer timer(ctx.stream, "ilt_build");
     // U^T, the factorisation's levels and the Jacobi layouts on the device
-    std::vector<i64> ic_lev_ptr;
-    ilt_structure_gpu(ctx, upper, ic, ic_lev_ptr);
+    ilt_structure_gpu(ctx, upper, ic);
     timer.mark("structure");
     ctx.sweep_error.resize(1);
     ctx.sweep_error.zero(ctx.stream);
@@ -573,8 +631,11 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
     NL_LAUNCH(k_to_float, grid_for(n, 256), 256, 0, ctx.stream, n, ic.scale.p, ic.scale32.p);
     ic.a_scaled.resize(size_t(nnz)); ic.u.resize(size_t(nnz));
     dbuf<unsigned long long> mind;
-    dbuf<int> failed;
-    mind.resize(1); failed.resize(1);
+    dbuf<int> failed, sync;   // failed: [pivot, timeout]; sync: [ticket, done flags per row]
+    mind.resize(1); failed.resize(2); sync.resize(size_t(n + 1));
+    // resident warps well above the widest level, so the rows of the next
+    // levels are taken while the current one finishes
+    const unsigned ic_grid = unsigned(std::max<i64>(1, std::min<i64>((n + IC_WARPS - 1) / IC_WARPS, 152 * 2)));
     const unsigned long long init = ~0ull;
     NL_CUDA(cudaMemcpyAsync(mind.p, &init, sizeof init, cudaMemcpyHostToDevice, ctx.stream));
     NL_LAUNCH(k_scaled, grid_for(n, 256), 256, 0, ctx.stream, n, upper.rowptr.p, upper.col.p, upper.val.p, ic.scale.p,
@@ -590,16 +651,15 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
     ic.ok = false;
     for (ic.attempts = 1; ic.attempts <= 10; ++ic.attempts) {
         failed.zero(ctx.stream);
-        for (i64 l = 0; l < ic.ic_levels; ++l) {
-            const i64 t0 = ic_lev_ptr[size_t(l)], t1 = ic_lev_ptr[size_t(l) + 1];
-            NL_LAUNCH(k_ic0_level, unsigned((t1 - t0 + IC_WARPS - 1) / IC_WARPS), IC_WARPS * 32, 0, ctx.stream, t0, t1,
-                      ic.ic_rows.p, ic.rp.p, ic.col.p, ic.a_scaled.p, shift, ic.lrp.p, ic.lcol.p, ic.l_to_u.p, ic.u.p,
-                      failed.p);
-        }
-        int hf = 0;
-        NL_CUDA(cudaMemcpyAsync(&hf, failed.p, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
+        sync.zero(ctx.stream);
+        NL_LAUNCH(k_ic0_rows, ic_grid, IC_WARPS * 32, 0, ctx.stream, n, ic.ic_rows.p, ic.rp.p, ic.col.p,
+                  ic.a_scaled.p, shift, ic.lrp.p, ic.lcol.p, ic.l_to_u.p, ic.u.p, sync.p, sync.p + 1, failed.p,
+                  failed.p + 1);
+        int hf[2] = {0, 0};
+        NL_CUDA(cudaMemcpyAsync(hf, failed.p, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
         NL_CUDA(cudaStreamSynchronize(ctx.stream));
-        if (!hf) { ic.ok = true; break; }
+        NL_REQUIRE(!hf[1], NLGPU_ERR_TIMEOUT, "the factorisation's wait for a dependency row timed out");
+        if (!hf[0]) { ic.ok = true; break; }
         shift = std::max(initial_shift, 2.0 * shift);
     }
     ic.shift = shift;
