@@ -526,11 +526,18 @@ int nlgpu_nonstationary_1d_temperature(nlgpu_ctx* ctx, double* temperature);
  * NLGPU_OPTION_FP32_SYMMETRIC = 1 makes the mixed solve's FP32 SpMV read only
  * the strictly upper part of a symmetric solver matrix (half the entries,
  * transposed contributions added with shared-memory atomics) instead of its
- * full rows (the default; for comparison). */
+ * full rows (the default; for comparison).
+ * NLGPU_OPTION_ASSEMBLY_WARPS sets the warps per CTA of the float-float pair
+ * assembly: 16 or 32, or 0 (default) to time both on a sample of elements at
+ * the first float-float assembly of each (element type, influence kind, pair
+ * mode) and keep the faster; nlgpu_assembly_tuning reports the choice. */
 enum { NLGPU_OPTION_GLOBAL_SWEEPS = 0, NLGPU_OPTION_ORDERED_PAIRS = 1, NLGPU_OPTION_ASSEMBLY_PRECISION = 2,
-       NLGPU_OPTION_FP32_SYMMETRIC = 3 };
+       NLGPU_OPTION_FP32_SYMMETRIC = 3, NLGPU_OPTION_ASSEMBLY_WARPS = 4 };
 enum { NLGPU_ASSEMBLY_AUTO = 0, NLGPU_ASSEMBLY_FF = 1, NLGPU_ASSEMBLY_FP64 = 2 };
 int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value);
+/* Warps per CTA of the last float-float pair assembly (0 before any) and the
+ * sample times (ms) of the last tuning with 16 and 32 warps (0 when none ran). */
+int nlgpu_assembly_tuning(nlgpu_ctx* ctx, int* warps, double* sample_ms);
 int nlgpu_event_record(nlgpu_ctx* ctx, int slot);
 int nlgpu_event_elapsed(nlgpu_ctx* ctx, int start_slot, int stop_slot, double* milliseconds);
 int nlgpu_flush_l2(nlgpu_ctx* ctx, int64_t bytes);

@@ -33,6 +33,7 @@ MATRIX_INNER, MATRIX_BOUND, MATRIX_LOCAL = 0, 1, 2
 PRECONDITIONER = {"identity": 0, "illt": 1, "illt_learned": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
 OPTION_GLOBAL_SWEEPS, OPTION_ORDERED_PAIRS, OPTION_ASSEMBLY_PRECISION, OPTION_FP32_SYMMETRIC = 0, 1, 2, 3
+OPTION_ASSEMBLY_WARPS = 4
 ASSEMBLY = {"auto": 0, "ff": 1, "fp64": 2}
 
 
@@ -154,6 +155,7 @@ SIGNATURES = {
     "nlgpu_cg_solve_noalloc": (c_int, [c_p, c_i64, c_p, c_p, c_p, c_p, c_p, c_d, c_i64, ctypes.POINTER(c_i64),
                                        ctypes.POINTER(c_d)]),
     "nlgpu_set_option": (c_int, [c_p, c_int, c_int]),
+    "nlgpu_assembly_tuning": (c_int, [c_p, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_double)]),
     "nlgpu_event_record": (c_int, [c_p, c_int]),
     "nlgpu_event_elapsed": (c_int, [c_p, c_int, c_int, ctypes.POINTER(c_d)]),
     "nlgpu_flush_l2": (c_int, [c_p, c_i64]),

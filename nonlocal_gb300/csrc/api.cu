@@ -1324,6 +1324,11 @@ int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value) {
         ctx->full.val32.release();
         return NLGPU_OK;
     }
+    if (option == NLGPU_OPTION_ASSEMBLY_WARPS) {
+        if (value != 0 && value != 16 && value != 32) return NLGPU_ERR_ARG;
+        ctx->ff_warps_option = value;
+        return NLGPU_OK;
+    }
     if (option == NLGPU_OPTION_ASSEMBLY_PRECISION) {
         if (value < NLGPU_ASSEMBLY_AUTO || value > NLGPU_ASSEMBLY_FP64) return NLGPU_ERR_ARG;
         ctx->assembly_precision = value;
@@ -1331,6 +1336,14 @@ int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value) {
         return NLGPU_OK;
     }
     return NLGPU_ERR_ARG;
+}
+
+int nlgpu_assembly_tuning(nlgpu_ctx* ctx, int* warps, double* sample_ms) {
+    if (!ctx || !warps || !sample_ms) return NLGPU_ERR_ARG;
+    *warps = ctx->ff_warps_used;
+    sample_ms[0] = ctx->ff_tune_ms[0];
+    sample_ms[1] = ctx->ff_tune_ms[1];
+    return NLGPU_OK;
 }
 
 int nlgpu_event_record(nlgpu_ctx* ctx, int slot) {

@@ -39,6 +39,7 @@ constexpr int AS_WARPS = AS_THREADS / 32;
 
 struct AssembleArgs {
     i64 E;
+    i64 e0;                   // first element (the float-float kernel's tuning samples start later)
     const int32_t* elems;
     const double* qcoord;     // [e][q][2]
     const double* jac;        // [e][q]
@@ -238,15 +239,14 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, M
 // to the FP64 solution.  Only the rows' accumulators, the rare self term and
 // the index work stay FP64 / integer.  Element data is staged once per
 // assembly as float-float (k_ff_stage), so the pair loop converts nothing.
-// 16 warps per CTA (the FP64 kernel's 8 leave the FP32 pipes idle).
-constexpr int AS_FF_THREADS = 512;
-constexpr int AS_FF_WARPS = AS_FF_THREADS / 32;
+// 16 or 32 warps per CTA (the FP64 kernel's 8 leave the FP32 pipes idle),
+// chosen per problem by timing both on a sample of elements (ff_warps).
 
 struct FFArgs {
     const float4* deriv;    // [e][i][q]: (gx.h, gx.l, gy.h, gy.l)
-    const float4* qcoord;   // [e][q]: (x.h, x.l, y.h, y.l)
+    const float4* qcoord;   // [e][q]: (x/r0 .h, .l, y/r1 .h, .l), coordinates in units of the radii
     const float2* cw;       // [e][q]: c_q = w_q norm (1 - p1) [lambda_q]
-    FFExpTable exp_table;   // exp(k / 64), copied to shared memory by each CTA
+    FFExpTable exp_table;   // exp(k / 256), copied to shared memory by each CTA
 };
 
 __global__ void k_ff_stage(i64 E, int nen, int nq, const double* __restrict__ deriv, const double* __restrict__ qcoord,
@@ -258,7 +258,7 @@ __global__ void k_ff_stage(i64 E, int nen, int nq, const double* __restrict__ de
         const ff gx = ff_from(deriv[2 * t]), gy = ff_from(deriv[2 * t + 1]);
         dff[t] = make_float4(gx.h, gx.l, gy.h, gy.l);
         if (t < E * nq) {
-            const ff x = ff_from(qcoord[2 * t]), y = ff_from(qcoord[2 * t + 1]);
+            const ff x = ff_from(qcoord[2 * t] * m.inv_r[0]), y = ff_from(qcoord[2 * t + 1] * m.inv_r[1]);
             qff[t] = make_float4(x.h, x.l, y.h, y.l);
             const double lam = cond_field ? cond_field[t] : m.cond[0];
             const ff c = ff_from(b.w[t % nq] * cnl * (iso ? lam : 1.0));
@@ -267,21 +267,23 @@ __global__ void k_ff_stage(i64 E, int nen, int nq, const double* __restrict__ de
     }
 }
 
+// per warp: eNL's data; g holds eNL's gradients (x then y) for H = Phi (Lambda
+// G) and then H itself (x then y), which the lanes keep in registers until
+// every lane has read G
 template<int NEN, int NQ>
 struct PairFF {
     ff qx[NQ], qy[NQ];
-    ff gx[NEN * NQ], gy[NEN * NQ];
+    ff g[2 * NEN * NQ];
     ff phi[NQ * NQ];
-    ff hx[NQ * NEN], hy[NQ * NEN];
     ff c[NQ];
     int32_t nodes[NEN];
 };
 
 // shape<INF> in float-float (fast polynomial, polynomial and exponential with
 // p divisible by n; the host sends the other kinds to the FP64 kernel)
+// z0, z1: the coordinate differences in units of the radii
 template<int INF>
-__device__ __forceinline__ ff shape_ff(const Model& m, ff dx, ff dy, ff ir0, ff ir1, ff q, const ff* exp_table) {
-    const ff z0 = ff_mul(dx, ir0), z1 = ff_mul(dy, ir1);
+__device__ __forceinline__ ff shape_ff(const Model& m, ff z0, ff z1, ff q, const ff* exp_table) {
     ff d;
     if (m.n == 2) d = ff_add(ff_mul(z0, z0), ff_mul(z1, z1));
     else if (m.n == 1) d = ff_add(ff_abs(z0), ff_abs(z1));
@@ -297,8 +299,10 @@ __device__ __forceinline__ ff shape_ff(const Model& m, ff dx, ff dy, ff ir0, ff 
     }
 }
 
-template<int NEN, int NQ, int INF, bool SYM>
-__global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArgs a, FFArgs f, Model m, Basis b) {
+template<int NEN, int NQ, int INF, bool SYM, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_assemble_pairs_ff(AssembleArgs a, FFArgs f, Model m, Basis b) {
+    constexpr int THREADS = WARPS * 32;
+    constexpr int HN = 2 * NQ * NEN, HR = (HN + 31) / 32;   // H outputs and lane rounds
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ ff eqx[NQ], eqy[NQ], ewx[NEN * NQ], ewy[NEN * NQ];
     __shared__ double egx[NEN * NQ], egy[NEN * NQ], ejac[NQ], elam[NQ];   // the self term stays FP64
@@ -311,17 +315,17 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
         etab[t] = ff{f.exp_table.v[t].x, f.exp_table.v[t].y};
 
     auto* pairs = reinterpret_cast<PairFF<NEN, NQ>*>(smem_raw);
-    double* acc = reinterpret_cast<double*>(smem_raw + sizeof(PairFF<NEN, NQ>) * AS_FF_WARPS);
+    double* acc = reinterpret_cast<double*>(smem_raw + sizeof(PairFF<NEN, NQ>) * WARPS);
     int32_t* cols = reinterpret_cast<int32_t*>(acc + a.cap);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     PairFF<NEN, NQ>& ps = pairs[warp];
     const bool iso = m.cond_kind == NLGPU_CONDUCTIVITY_ISOTROPIC;
-    const ff ir0 = ff_from(m.inv_r[0]), ir1 = ff_from(m.inv_r[1]), qf = ff_from(m.q);
+    const ff qf = ff_from(m.q);
     const ff k0 = ff_from(m.cond[0]), k1 = ff_from(m.cond[1]), k2 = ff_from(m.cond[2]);
 
-    for (i64 eL = blockIdx.x; eL < a.E; eL += gridDim.x) {
+    for (i64 eL = a.e0 + blockIdx.x; eL < a.E; eL += gridDim.x) {
         // ---- element eL: quadrature data, weighted gradients and its node rows
-        for (int t = threadIdx.x; t < NEN * NQ; t += AS_FF_THREADS) {
+        for (int t = threadIdx.x; t < NEN * NQ; t += THREADS) {
             egx[t] = a.deriv[2 * (eL * NEN * NQ + t)];
             egy[t] = a.deriv[2 * (eL * NEN * NQ + t) + 1];
             const float4 g = f.deriv[eL * NEN * NQ + t];
@@ -329,7 +333,7 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
             ewx[t] = ff_mul(w, ff{g.x, g.y});
             ewy[t] = ff_mul(w, ff{g.z, g.w});
         }
-        for (int t = threadIdx.x; t < NQ; t += AS_FF_THREADS) {
+        for (int t = threadIdx.x; t < NQ; t += THREADS) {
             const float4 q = f.qcoord[eL * NQ + t];
             eqx[t] = ff{q.x, q.y};
             eqy[t] = ff{q.z, q.w};
@@ -353,7 +357,7 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
         const bool smem_rows = use_smem;
         if (smem_rows) {
             for (int i = 0; i < NEN; ++i)
-                for (int t = threadIdx.x; t < row_len[i]; t += AS_FF_THREADS) {
+                for (int t = threadIdx.x; t < row_len[i]; t += THREADS) {
                     cols[row_off[i] + t] = a.in_col[row_start[i] + t];
                     acc[row_off[i] + t] = 0.0;
                 }
@@ -363,7 +367,7 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
 
         // ---- pairs (eL, eNL): one warp each
         const i64 kb = a.noff[eL], ke = a.noff[eL + 1];
-        for (i64 k = kb + warp; k < ke; k += AS_FF_WARPS) {
+        for (i64 k = kb + warp; k < ke; k += WARPS) {
             const int32_t eNL = a.nlist[k];
             if constexpr (SYM) {   // the pair belongs to the element with the smaller key
                 const int32_t key_n = a.minnode[eNL];
@@ -371,8 +375,8 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
             }
             for (int t = lane; t < NEN * NQ; t += 32) {
                 const float4 g = f.deriv[i64(eNL) * NEN * NQ + t];
-                ps.gx[t] = ff{g.x, g.y};
-                ps.gy[t] = ff{g.z, g.w};
+                ps.g[t] = ff{g.x, g.y};
+                ps.g[NEN * NQ + t] = ff{g.z, g.w};
             }
             if (lane < NQ) {
                 const float4 q = f.qcoord[i64(eNL) * NQ + lane];
@@ -386,29 +390,40 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
             for (int t = lane; t < NQ * NQ; t += 32) {
                 const int qL = t / NQ, qNL = t % NQ;
                 ps.phi[t] = ff_mul(ps.c[qNL], shape_ff<INF>(m, ff_sub(eqx[qL], ps.qx[qNL]), ff_sub(eqy[qL], ps.qy[qNL]),
-                                                             ir0, ir1, qf, etab));
+                                                             qf, etab));
             }
             __syncwarp();
-            for (int t = lane; t < NQ * NEN; t += 32) {
-                const int qL = t / NEN, j = t % NEN;
-                ffdot d0, d1;
+            // one lane per (direction, qL, j): 2 NQ NEN dots of NQ terms fill
+            // the lanes better than NQ NEN pairs of dots (144 = 4.5 rounds of
+            // 32 against 72 = 2.25 rounds of double work for the 8-node element)
+            ff hv[HR];
 #pragma unroll
-                for (int qNL = 0; qNL < NQ; ++qNL) {
-                    const ff fq = ps.phi[qL * NQ + qNL];
-                    const ff gx = ps.gx[j * NQ + qNL], gy = ps.gy[j * NQ + qNL];
-                    if (m.cond_kind != NLGPU_CONDUCTIVITY_ANISOTROPIC) {
-                        ffdot_add(d0, fq, gx);
-                        ffdot_add(d1, fq, gy);
-                    } else {
-                        ffdot_add(d0, fq, ff_add(ff_mul(k0, gx), ff_mul(k2, gy)));
-                        ffdot_add(d1, fq, ff_add(ff_mul(k2, gx), ff_mul(k1, gy)));
+            for (int rnd = 0; rnd < HR; ++rnd) {
+                const int t = lane + 32 * rnd;
+                if (t < HN) {
+                    const int dir = t >= NQ * NEN, u = dir ? t - NQ * NEN : t;
+                    const int qL = u / NEN, j = u % NEN;
+                    const ff* gd = ps.g + dir * NEN * NQ;
+                    ffdot d;
+#pragma unroll
+                    for (int qNL = 0; qNL < NQ; ++qNL) {
+                        const ff fq = ps.phi[qL * NQ + qNL];
+                        if (m.cond_kind != NLGPU_CONDUCTIVITY_ANISOTROPIC) {
+                            ffdot_add(d, fq, gd[j * NQ + qNL]);
+                        } else {
+                            const ff gx = ps.g[j * NQ + qNL], gy = ps.g[NEN * NQ + j * NQ + qNL];
+                            ffdot_add(d, fq, dir ? ff_add(ff_mul(k2, gx), ff_mul(k1, gy))
+                                                 : ff_add(ff_mul(k0, gx), ff_mul(k2, gy)));
+                        }
                     }
+                    hv[rnd] = ffdot_value(d);
+                    if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) hv[rnd] = ff_mul(hv[rnd], dir ? k1 : k0);
                 }
-                ff h0 = ffdot_value(d0), h1 = ffdot_value(d1);
-                if (m.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC) { h0 = ff_mul(h0, k0); h1 = ff_mul(h1, k1); }
-                ps.hx[t] = h0;
-                ps.hy[t] = h1;
             }
+            __syncwarp();   // every lane has read G: H (x then y, [qL][j]) replaces it
+#pragma unroll
+            for (int rnd = 0; rnd < HR; ++rnd)
+                if (lane + 32 * rnd < HN) ps.g[lane + 32 * rnd] = hv[rnd];
             __syncwarp();
             const bool self = eNL == int32_t(eL);
             for (int t = lane; t < NEN * NEN; t += 32) {
@@ -424,8 +439,8 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
                 ffdot dv;
 #pragma unroll
                 for (int qL = 0; qL < NQ; ++qL) {
-                    ffdot_add(dv, ewx[i * NQ + qL], ps.hx[qL * NEN + j]);
-                    ffdot_add(dv, ewy[i * NQ + qL], ps.hy[qL * NEN + j]);
+                    ffdot_add(dv, ewx[i * NQ + qL], ps.g[qL * NEN + j]);
+                    ffdot_add(dv, ewy[i * NQ + qL], ps.g[NQ * NEN + qL * NEN + j]);
                 }
                 double v = ff_to(ffdot_value(dv));
                 if (self) {
@@ -460,7 +475,7 @@ __global__ void __launch_bounds__(AS_FF_THREADS) k_assemble_pairs_ff(AssembleArg
         __syncthreads();
         if (smem_rows)
             for (int i = 0; i < NEN; ++i)
-                for (int t = threadIdx.x; t < row_len[i]; t += AS_FF_THREADS) {
+                for (int t = threadIdx.x; t < row_len[i]; t += THREADS) {
                     const double v = acc[row_off[i] + t];
                     if (v != 0.0) atomicAdd(a.in_val + row_start[i] + t, v);
                 }
@@ -552,21 +567,70 @@ void dispatch_influence(Ctx& ctx, const AssembleArgs& a, bool sym) {
     }
 }
 
+template<int NEN, int NQ, int INF, int WARPS>
+void launch_pairs_ff_w(Ctx& ctx, AssembleArgs a, const FFArgs& f, bool sym) {
+    auto kernel = sym ? k_assemble_pairs_ff<NEN, NQ, INF, true, WARPS> : k_assemble_pairs_ff<NEN, NQ, INF, false, WARPS>;
+    // the row accumulators take what shared memory the per-warp blocks leave
+    int dev = 0, optin = 0;
+    NL_CUDA(cudaGetDevice(&dev));
+    NL_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa{};
+    NL_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    const size_t fixed = sizeof(PairFF<NEN, NQ>) * WARPS;
+    const size_t avail = size_t(optin) - fa.sharedSizeBytes;
+    NL_REQUIRE(avail > fixed + 4096, NLGPU_ERR_UNSUPPORTED, "not enough shared memory for the pair assembly");
+    a.cap = int((avail - fixed) / 12);
+    const size_t dyn = fixed + size_t(a.cap) * (sizeof(double) + sizeof(int32_t));
+    const unsigned grid = unsigned(std::max<i64>(1, std::min<i64>(a.E - a.e0, 152 * 16)));
+    NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
+    NL_LAUNCH(kernel, grid, WARPS * 32, dyn, ctx.stream, a, f, ctx.model, ctx.basis);
+}
+
+// Warps per CTA: forced by NLGPU_OPTION_ASSEMBLY_WARPS, else tuned once per
+// (element type, influence kind, pair mode) and context by timing both forms
+// on the same sample of elements from the middle of the mesh (their
+// contributions are cleared afterwards: the matrices are zeroed again).
 template<int NEN, int NQ, int INF>
 void launch_pairs_ff(Ctx& ctx, AssembleArgs a, const FFArgs& f, bool sym) {
-    const size_t fixed = sizeof(PairFF<NEN, NQ>) * AS_FF_WARPS;
-    a.cap = int((200 * 1024 - fixed) / 12);
-    const size_t dyn = fixed + size_t(a.cap) * (sizeof(double) + sizeof(int32_t));
-    const unsigned grid = unsigned(std::min<i64>(a.E, 152 * 16));
-    if (sym) {
-        auto kernel = k_assemble_pairs_ff<NEN, NQ, INF, true>;
-        NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
-        NL_LAUNCH(kernel, grid, AS_FF_THREADS, dyn, ctx.stream, a, f, ctx.model, ctx.basis);
-    } else {
-        auto kernel = k_assemble_pairs_ff<NEN, NQ, INF, false>;
-        NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn)));
-        NL_LAUNCH(kernel, grid, AS_FF_THREADS, dyn, ctx.stream, a, f, ctx.model, ctx.basis);
+    int warps = ctx.ff_warps_option;
+    if (warps == 0) {
+        const int key = NEN * 1000 + INF * 10 + (sym ? 1 : 0);
+        auto it = ctx.ff_warps_tuned.find(key);
+        if (it != ctx.ff_warps_tuned.end()) {
+            warps = it->second;
+        } else {
+            const i64 sample = std::min<i64>(a.E, 152 * 8);
+            AssembleArgs s = a;
+            s.e0 = (a.E - sample) / 2;
+            s.E = s.e0 + sample;
+            double ms[2] = {0.0, 0.0};
+            cudaEvent_t ev[2] = {};
+            NL_CUDA(cudaEventCreate(&ev[0]));
+            NL_CUDA(cudaEventCreate(&ev[1]));
+            for (int rep = 0; rep < 2; ++rep)   // the first round warms up
+                for (int v = 0; v < 2; ++v) {
+                    NL_CUDA(cudaEventRecord(ev[0], ctx.stream));
+                    if (v == 0) launch_pairs_ff_w<NEN, NQ, INF, 16>(ctx, s, f, sym);
+                    else launch_pairs_ff_w<NEN, NQ, INF, 32>(ctx, s, f, sym);
+                    NL_CUDA(cudaEventRecord(ev[1], ctx.stream));
+                    NL_CUDA(cudaEventSynchronize(ev[1]));
+                    float t = 0.0f;
+                    NL_CUDA(cudaEventElapsedTime(&t, ev[0], ev[1]));
+                    ms[v] = double(t);
+                }
+            cudaEventDestroy(ev[0]);
+            cudaEventDestroy(ev[1]);
+            ctx.inner.val.zero(ctx.stream);
+            ctx.bound.val.zero(ctx.stream);
+            warps = ms[1] < ms[0] ? 32 : 16;
+            ctx.ff_warps_tuned[key] = warps;
+            ctx.ff_tune_ms[0] = ms[0];
+            ctx.ff_tune_ms[1] = ms[1];
+        }
     }
+    ctx.ff_warps_used = warps;
+    if (warps == 32) launch_pairs_ff_w<NEN, NQ, INF, 32>(ctx, a, f, sym);
+    else launch_pairs_ff_w<NEN, NQ, INF, 16>(ctx, a, f, sym);
 }
 
 template<int NEN, int NQ>
@@ -625,7 +689,7 @@ void assemble_full(Ctx& ctx) {
                   ctx.cw_ff.p);
         FFArgs f{ctx.deriv_ff.p, ctx.qcoord_ff.p, ctx.cw_ff.p, {}};
         for (int k = -FF_EXP_K; k <= FF_EXP_K; ++k) {
-            const double x = std::exp(double(k) / 64.0);
+            const double x = std::exp(double(k) / double(FF_EXP_STEPS));
             const float hi = float(x);
             f.exp_table.v[k + FF_EXP_K] = make_float2(hi, float(x - double(hi)));
         }

@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <array>
 #include <functional>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -438,6 +439,10 @@ struct Ctx {
     int assembly_precision = NLGPU_ASSEMBLY_AUTO;
     bool ff_assembly = false;           // pair blocks in float-float on the FP32 pipes (mixed precision)
     bool ff_assembled = false;          // the last assembly ran in float-float
+    int ff_warps_option = 0;            // warps per CTA of the float-float pair assembly (0: tuned)
+    int ff_warps_used = 0;              // ... of its last launch
+    double ff_tune_ms[2] = {0.0, 0.0};  // the last tuning's sample times with 16 and 32 warps
+    std::map<int, int> ff_warps_tuned;  // tuned choice per (element type, influence kind, pair mode)
     dbuf<float4> deriv_ff, qcoord_ff;   // float-float copies: (gx, gy) / (x, y) as (hi, lo, hi, lo)
     dbuf<float2> cw_ff;                 // w_q norm (1 - p1) [lambda_q] per element and point
     // measurement

@@ -104,39 +104,44 @@ __device__ __forceinline__ void ffdot_add(ffdot& acc, ff a, ff b) {
 
 __device__ __forceinline__ ff ffdot_value(const ffdot& acc) { return quick_two_sum(acc.s, acc.c); }
 
-// exp(k / 64) for k = -FF_EXP_K .. FF_EXP_K as float-float pairs, filled on the
-// host (exp of a double, split hi = float(x), lo = float(x - hi))
-constexpr int FF_EXP_K = 23;
+// exp(k / 256) for k = -FF_EXP_K .. FF_EXP_K as float-float pairs, filled on
+// the host (exp of a double, split hi = float(x), lo = float(x - hi))
+constexpr int FF_EXP_K = 89;
+constexpr float FF_EXP_STEPS = 256.0f;
 struct FFExpTable {
     float2 v[2 * FF_EXP_K + 1];
 };
 
-// exp(t) for t <= 0 from the mathematics of the exponential: t = m ln2 + f with
-// |f| <= ln2 / 2, f = k / 64 + g with |g| <= 1/128, exp(f) = exp(k / 64) exp(g)
-// with exp(k / 64) from the table and exp(g) by its Taylor series through g^6
-// (remainder below 4e-19), every step in float-float.  Results below 1e-37
-// are flushed to zero.  ln2 and 1/k! are split into two floats each.
+// exp(t) for t <= 0 from the mathematics of the exponential:
+//   t = m ln2 + f, |f| <= ln2 / 2 (ln2 split into two floats);
+//   f = k / 256 + g, |g| <= 1/512 (f.h - k/256 is exact by Sterbenz's lemma);
+//   exp(f) = exp(k / 256) exp(g), exp(k / 256) from the table and
+//   exp(g) = 1 + g + g^2/2 + g^3 (1/6 + g/24 + g^2/120) + O(g^6),
+// the first three terms in float-float (g^2 by the FMA exact product), the
+// bracket in FP32: its term is below 2^-27 and needs only 2^-21 relative
+// accuracy for a result good to about 2^-48, and the omitted g^6 / 720 is
+// below 2^-63.  The scaling by 2^m builds the power of two from its exponent
+// bits (m >= -123 here).  Results below 1e-37 are flushed to zero.
 __device__ __forceinline__ ff ff_exp_nonpositive(ff t, const ff* table) {
     if (t.h < -85.0f) return ff_make(0.0f);
     const ff ln2{0.6931471824645996f, -1.9046542121259336e-09f};
     const float m = rintf(t.h * 1.4426950216293335f);
     const ff f = ff_sub(t, ff_mul_f(ln2, m));
-    const float k = rintf(f.h * 64.0f);
-    const ff g = ff_sub(f, ff_make(k * 0.015625f));
-    const ff inv_fact[7] = {{1.0f, 0.0f},
-                            {1.0f, 0.0f},
-                            {0.5f, 0.0f},
-                            {0.1666666716337204f, -4.967053879312289e-09f},
-                            {0.0416666679084301f, -1.2417634698280722e-09f},
-                            {0.008333333767950535f, -4.34617203337595e-10f},
-                            {0.0013888889225199819f, -3.3631094437103215e-11f}};
-    ff p = inv_fact[6];
-#pragma unroll
-    for (int j = 5; j >= 0; --j) p = ff_add(ff_mul(p, g), inv_fact[j]);
+    const float k = rintf(f.h * FF_EXP_STEPS);
+    const ff g = quick_two_sum(__fsub_rn(f.h, k * (1.0f / FF_EXP_STEPS)), f.l);
+    const float p2 = __fmul_rn(g.h, g.h);
+    const float e2 = __fmaf_rn(2.0f * g.h, g.l, __fmaf_rn(g.h, g.h, -p2));   // g^2 = p2 + e2
+    const float q = __fmul_rn(__fmul_rn(p2, g.h),
+                              __fmaf_rn(g.h, __fmaf_rn(g.h, 0.008333333767950535f, 0.0416666679084301f),
+                                        0.1666666716337204f));
+    const float low = __fadd_rn(__fadd_rn(g.l, 0.5f * e2), q);
+    const ff u = quick_two_sum(g.h, 0.5f * p2);       // |g| >= g^2 / 2
+    const ff v = quick_two_sum(1.0f, u.h);
+    ff p = quick_two_sum(v.h, __fadd_rn(v.l, __fadd_rn(u.l, low)));
     const int ki = min(FF_EXP_K, max(-FF_EXP_K, int(k)));
     p = ff_mul(p, table[ki + FF_EXP_K]);
-    const int e = int(m);
-    return ff{ldexpf(p.h, e), ldexpf(p.l, e)};
+    const float scale = __int_as_float((127 + int(m)) << 23);
+    return ff{__fmul_rn(p.h, scale), __fmul_rn(p.l, scale)};
 }
 
 }  // namespace nlgpu

@@ -302,6 +302,20 @@ class Problem2D(Context):
         pipes for mixed-precision solves, FP64 otherwise), "ff" or "fp64" always."""
         L.check(self._lib.nlgpu_set_option(self._h, L.OPTION_ASSEMBLY_PRECISION, L.ASSEMBLY[kind]))
 
+    def set_assembly_warps(self, warps: int = 0) -> None:
+        """Warps per CTA of the float-float pair assembly: 16 or 32, or 0 to time
+        both on a sample of elements at the first float-float assembly and keep
+        the faster."""
+        L.check(self._lib.nlgpu_set_option(self._h, L.OPTION_ASSEMBLY_WARPS, int(warps)))
+
+    def assembly_tuning(self) -> dict:
+        """Warps per CTA of the last float-float assembly and the last tuning's
+        sample times (ms) with 16 and 32 warps."""
+        w = ctypes.c_int()
+        ms = (ctypes.c_double * 2)()
+        L.check(self._lib.nlgpu_assembly_tuning(self._h, ctypes.byref(w), ms))
+        return {"warps": w.value, "sample_ms_16": ms[0], "sample_ms_32": ms[1]}
+
     # ---- neighbours -----------------------------------------------------------
     def find_neighbours(self, strategy: str = "MAX") -> tuple[np.ndarray, int]:
         r = np.empty(2)

@@ -123,6 +123,31 @@ def test_float_float_assembly_matrices(golden):
         pb.set_assembly_precision("auto")
 
 
+@pytest.mark.parametrize("warps", [16, 32])
+def test_float_float_assembly_warps(golden, warps):
+    """Both CTA shapes of the float-float pair assembly (16 and 32 warps, which
+    the tuner chooses between) meet the FP64 bar against the reference's
+    matrices, and the tuner reports one of them."""
+    _, fx, pb = golden
+    if fx["config"].get("local_weight", 1) < 0.999:
+        pb.find_neighbours(fx["config"].get("strategy", "MAX"))
+    pb.set_assembly_precision("ff")
+    try:
+        pb.set_assembly_warps(warps)
+        pb.conductivity_matrix("FULL")
+        assert_csr_equal(pb.matrix("inner"), fx, "K_inner")
+        assert_csr_equal(pb.matrix("bound"), fx, "K_bound")
+        tuning = pb.assembly_tuning()
+        assert tuning["warps"] in (0, warps)   # 0: the model runs the FP64 kernel
+        pb.set_assembly_warps(0)
+        pb.conductivity_matrix("FULL")
+        assert_csr_equal(pb.matrix("inner"), fx, "K_inner")
+        assert pb.assembly_tuning()["warps"] in (0, 16, 32)
+    finally:
+        pb.set_assembly_warps(0)
+        pb.set_assembly_precision("auto")
+
+
 def test_stationary_solution(golden):
     _, fx, pb = golden
     if fx["config"].get("local_weight", 1) < 0.999:
