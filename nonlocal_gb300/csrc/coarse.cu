@@ -22,6 +22,7 @@
 // nc x nc, one pass over AP and r before the ILLT application and one add
 // after it.
 #include "common.cuh"
+#include "ff.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -137,7 +138,10 @@ __global__ void __launch_bounds__(CO_THREADS) k_agg_sort(i64 nc, const i64* __re
 // increasing order, each the sum of its runs in column order (a run's sum by a
 // segmented warp scan, the runs added one after another by lane 0, so the
 // result does not depend on the schedule); a row with more keeps one entry
-// per run.  The count pass (FILL = false) makes the same choice.
+// per run.  The count pass (FILL = false) makes the same choice.  The sums run
+// in float-float on the FP32 pipes (each FP64 entry split by integer
+// operations): a warp-wide FP64 add occupies GB300's FP64 pipe for 16 cycles,
+// and five of them per entry made this kernel FP64-bound.
 constexpr int AP_WARPS = 8;
 constexpr int AP_MAXD = 128;
 
@@ -156,7 +160,7 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
     const unsigned full = 0xffffffffu;
     const int words = (nc + 31) >> 5;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double* slot = reinterpret_cast<double*>(ap_smem) + wid * AP_MAXD;
+    ff* slot = reinterpret_cast<ff*>(ap_smem) + wid * AP_MAXD;
     uint32_t* bm = reinterpret_cast<uint32_t*>(ap_smem + AP_WARPS * AP_MAXD * sizeof(double)) + wid * 2 * words;
     int* pre = reinterpret_cast<int*>(bm + words);
     const i64 warps = i64(gridDim.x) * AP_WARPS;
@@ -193,7 +197,7 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
         if constexpr (!FILL) {
             if (lane == 0) cnt[r] = merge ? D : runs;
         } else {
-            for (int t = lane; t < AP_MAXD; t += 32) slot[t] = 0.0;
+            for (int t = lane; t < AP_MAXD; t += 32) slot[t] = ff{0.0f, 0.0f};
             __syncwarp();
             i64 out = ap_rp[r];
             for (i64 k0 = rb; k0 < re; k0 += 32) {
@@ -201,14 +205,14 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
                 const bool valid = k < re;
                 const int32_t J = valid ? agg[col[k]] : -1;
                 const double a = valid ? val[k] : 0.0;
-                double v = J >= 0 ? a : 0.0;
+                ff v = J >= 0 ? ff_split(a) : ff{0.0f, 0.0f};
                 const int32_t Jp = __shfl_up_sync(full, J, 1);
                 bool head = lane == 0 || Jp != J;
                 for (int o = 1; o < 32; o <<= 1) {
-                    const double vu = __shfl_up_sync(full, v, o);
+                    const ff vu{__shfl_up_sync(full, v.h, o), __shfl_up_sync(full, v.l, o)};
                     const bool hu = __shfl_up_sync(full, head, o);
                     if (lane >= o) {
-                        if (!head) v += vu;
+                        if (!head) v = ff_add(v, vu);
                         head = head || hu;
                     }
                 }
@@ -218,15 +222,18 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
                 if (merge) {
                     for (unsigned m = ends; m; m &= m - 1) {
                         const int src = __ffs(m) - 1;
-                        const double vs = __shfl_sync(full, v, src);
+                        const ff vs{__shfl_sync(full, v.h, src), __shfl_sync(full, v.l, src)};
                         const int32_t Js = __shfl_sync(full, J, src);
-                        if (lane == 0) slot[pre[Js >> 5] + __popc(bm[Js >> 5] & ((1u << (Js & 31)) - 1u))] += vs;
+                        if (lane == 0) {
+                            ff& t = slot[pre[Js >> 5] + __popc(bm[Js >> 5] & ((1u << (Js & 31)) - 1u))];
+                            t = ff_add(t, vs);
+                        }
                     }
                 } else {
                     if (end) {
                         const i64 pos = out + __popc(ends & ((1u << lane) - 1u));
                         ap_col[pos] = J;
-                        ap_val[pos] = v;
+                        ap_val[pos] = ff_to(v);
                     }
                     out += __popc(ends);
                 }
@@ -237,7 +244,7 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
                     int p = pre[w];
                     for (uint32_t m = bm[w]; m; m &= m - 1, ++p) {
                         ap_col[out + p] = w * 32 + __ffs(m) - 1;
-                        ap_val[out + p] = slot[p];
+                        ap_val[out + p] = ff_to(slot[p]);
                     }
                 }
         }

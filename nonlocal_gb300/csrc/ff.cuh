@@ -27,6 +27,28 @@ __device__ __forceinline__ ff ff_from(double x) {
 
 __device__ __forceinline__ double ff_to(ff a) { return double(a.h) + double(a.l); }
 
+// float-float of a double by integer operations only (no FP64 instruction):
+// h = the double truncated to 24 significant bits, l = the remaining 29 bits
+// rounded to a float, so h + l carries about 48 bits; |x| outside
+// [2^-100, 2^127] gives (0, 0) (or h = +-inf for a too large or non-finite x)
+__device__ __forceinline__ ff ff_split(double x) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const unsigned sign = unsigned(b >> 32) & 0x80000000u;
+    const int e = int((b >> 52) & 0x7ff) - 1023;
+    if (e < -100) return ff{0.0f, 0.0f};
+    if (e > 127) return ff{__uint_as_float(sign | 0x7f800000u), 0.0f};
+    const unsigned long long mant = b & 0xfffffffffffffull;
+    const float h = __uint_as_float(sign | (unsigned(e + 127) << 23) | unsigned(mant >> 29));
+    const unsigned rest = unsigned(mant & 0x1fffffffull);   // 29 bits below h's last
+    // rest * 2^(e - 52), e - 52 in [-152, 75]: below 2^-126 the power of two is
+    // built as 2^(e - 52 + 64) * 2^-64
+    const int s = e - 52;
+    const float r = __uint2float_rn(rest);
+    const float l = s >= -126 ? __fmul_rn(r, __uint_as_float(unsigned(s + 127) << 23))
+                              : __fmul_rn(__fmul_rn(r, __uint_as_float(unsigned(s + 64 + 127) << 23)), 5.421010862427522e-20f);
+    return ff{h, sign ? -l : l};
+}
+
 // s + e = a + b exactly (any a, b)
 __device__ __forceinline__ ff two_sum(float a, float b) {
     const float s = __fadd_rn(a, b);
