@@ -92,9 +92,10 @@ L2_FLUSH_BYTES = 256 << 20
 # the measured-peaks file holds no FP32 figure
 FP32_PEAK_TFLOPS = 74.0
 FP32_PEAK_KIND = "measured FP32 FMA loop (CUDA events) on GB300, 74.0 TFLOP/s; nominal 80.5"
-# instructions per float-float multiply-add (exact product 4, renormalisation 3,
-# TwoSum and renormalisation 11): the float-float kernel's own issue cost
-FF_INSTRUCTIONS = 18
+# FP32 instructions per float-float multiply-add of the kernel's compensated
+# dot products (exact product with the cross terms 4, TwoSum 6, compensation 2):
+# the float-float kernel's own issue cost per algorithmic multiply-add
+FF_INSTRUCTIONS = 12
 # CPU arm: stop taking further full solves once this much time has gone
 REFERENCE_BUDGET_S = 150.0
 

@@ -9,12 +9,13 @@
 //               that are not inner (Dirichlet) belong to none.  P is the
 //               n x nc indicator matrix of the aggregates; each aggregate's
 //               node list is kept sorted (deterministic restriction).
-//   AP          per row the sums of the row's entries by column aggregate
-//               (segmented warp sums over the row's sorted columns; a row may
-//               hold an aggregate more than once, only the sum matters)
+//   AP          per row the sums of the row's entries by column aggregate,
+//               one entry per aggregate in increasing order (float-float
+//               segmented warp sums over the row's sorted columns)
 //   A_c = P^T A P  from AP, a row per aggregate summed in shared memory, FP64
-//   A_c^-1      Gauss-Jordan in FP64 (A_c is SPD, no pivoting), one launch per
-//               pivot ping-ponging two copies; stored in FP32 for the solve
+//   A_c^-1      blocked Gauss-Jordan in FP64 (A_c is SPD, no pivoting), 32
+//               pivots per panel, three launches per panel ping-ponging two
+//               copies; stored in FP32 for the solve
 //   apply       Q r = P A_c^-1 P^T r, then z = M^-1 (r - A Q r) + Q r with
 //               A Q r = AP (A_c^-1 P^T r)  (A-DEF1 of Tang, Nabben, Vuik and
 //               Erlangga 2009); flexible CG absorbs its non-symmetry.
@@ -176,9 +177,12 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
         for (i64 k0 = rb; k0 < re; k0 += 32) {
             const i64 k = k0 + lane;
             const int32_t J = k < re ? agg[col[k]] : -1;
-            if (J >= 0) atomicOr(&bm[J >> 5], 1u << (J & 31));
             const int32_t Jn = __shfl_down_sync(full, J, 1);
-            runs += __popc(__ballot_sync(full, J >= 0 && (lane == 31 || Jn != J)));
+            const bool end = J >= 0 && (lane == 31 || Jn != J);
+            // one mark per run: neighbouring lanes mostly share an aggregate,
+            // and their atomics on one word would serialise
+            if (end) atomicOr(&bm[J >> 5], 1u << (J & 31));
+            runs += __popc(__ballot_sync(full, end));
         }
         __syncwarp();
         int D = 0;   // distinct aggregates; pre[w] = set bits before word w
