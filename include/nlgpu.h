@@ -105,6 +105,8 @@ typedef struct nlgpu_solve_options {
     int coarse_aggregates;    /* MIXED with ILLT: 0 none; > 0 adds a coarse-space correction over about
                                  that many node aggregates (no counterpart in the reference, whose
                                  preconditioner is ILLT alone) */
+    double coarse_aspect;     /* width / height of the aggregates' grid cells; <= 0: sqrt(lambda_x /
+                                 lambda_y) for an orthotropic conductivity, 1 otherwise */
 } nlgpu_solve_options;
 
 typedef struct nlgpu_solve_report {
@@ -457,8 +459,10 @@ int nlgpu_nonstationary_2d_step(nlgpu_ctx* ctx, double dirichlet_value, const do
  * batches calls of nonstationary_heat_equation_solver_2d::calc_step)
  * create: instances already set up by nlgpu_nonstationary_2d_compute (each with
  * its own mesh, model, time step and boundaries; their sizes may differ); the
- * batch copies their matrices and current temperatures and leaves the
- * contexts unchanged.  step: one implicit-Euler step of every instance, the
+ * batch copies their matrices and current temperatures and releases the
+ * contexts' upper-storage copies of dt K + C and their full -> upper maps, which
+ * only a radiation update reads (batches take no radiation edges); the
+ * contexts still step on their own.  step: one implicit-Euler step of every instance, the
  * Dirichlet nodes of instance k set to dirichlet_values[k]; CG with the
  * identity preconditioner from the previous temperature, as calc_step, on the
  * block-diagonal system of all instances (one launch per stage for all of
@@ -471,6 +475,21 @@ int nlgpu_batch_destroy(nlgpu_batch* batch);
 int nlgpu_batch_step(nlgpu_batch* batch, const double* dirichlet_values, double tolerance, int64_t max_iterations,
                      int64_t* iterations);
 int nlgpu_batch_temperature(nlgpu_batch* batch, int64_t index, double* temperature);
+/* Per instance: rows and the entries the batched step's SpMV reads (the
+ * system matrix C + dt K in full padded rows), arrays of `count` values. */
+int nlgpu_batch_sizes(nlgpu_batch* batch, int64_t* rows, int64_t* system_entries);
+/* The batched step's solver: NLGPU_BATCH_IDENTITY_FP64 (default; the
+ * reference's identity-preconditioned FP64 CG per instance, each with its own
+ * scalars and stop) or NLGPU_BATCH_MIXED_ILLT (mixed-precision FCG on the whole
+ * block-diagonal system with the ILLT of every instance's C + dt p1 K_local,
+ * FP64 reliable updates, every instance held to |b_k - A_k x_k| <= tol |b_k|,
+ * FP64 ILLT-CG as its fallback; the iteration counts it reports are those of
+ * the whole system). */
+enum { NLGPU_BATCH_IDENTITY_FP64 = 0, NLGPU_BATCH_MIXED_ILLT = 1 };
+int nlgpu_batch_set_method(nlgpu_batch* batch, int method);
+/* NLGPU_BATCH_MIXED_ILLT: the last step's FCG iterations, FP64 refinement
+ * steps and whether the FP64 ILLT-CG fallback ran (zeros for the identity CG). */
+int nlgpu_batch_last_solve(nlgpu_batch* batch, int64_t* inner_iterations, int64_t* outer_iterations, int* fallback);
 
 /* ---- stationary_heat_equation_solver_1d (stationary_heat_equation_solver_1d.hpp:43-122)
  * One segment [0, length] of `elements` Lagrange elements of `order` 1

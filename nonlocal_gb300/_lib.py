@@ -34,6 +34,7 @@ PRECONDITIONER = {"identity": 0, "illt": 1, "illt_learned": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
 OPTION_GLOBAL_SWEEPS, OPTION_ORDERED_PAIRS, OPTION_ASSEMBLY_PRECISION, OPTION_FP32_SYMMETRIC = 0, 1, 2, 3
 OPTION_ASSEMBLY_WARPS = 4
+BATCH_METHOD = {"identity_fp64": 0, "mixed_illt": 1}
 ASSEMBLY = {"auto": 0, "ff": 1, "fp64": 2}
 
 
@@ -50,7 +51,8 @@ class Model2D(ctypes.Structure):
 
 class SolveOptions(ctypes.Structure):
     _fields_ = [("tolerance", c_d), ("max_iterations", c_i64), ("preconditioner", c_int), ("precision", c_int),
-                ("inner_tolerance", c_d), ("triangular_sweeps", c_int), ("coarse_aggregates", c_int)]
+                ("inner_tolerance", c_d), ("triangular_sweeps", c_int), ("coarse_aggregates", c_int),
+                ("coarse_aspect", c_d)]
 
 
 DEFAULT_TRIANGULAR_SWEEPS = 6   # NLGPU_DEFAULT_TRIANGULAR_SWEEPS
@@ -138,6 +140,9 @@ SIGNATURES = {
     "nlgpu_batch_destroy": (c_int, [c_p]),
     "nlgpu_batch_step": (c_int, [c_p, c_p, c_d, c_i64, c_p]),
     "nlgpu_batch_temperature": (c_int, [c_p, c_i64, c_p]),
+    "nlgpu_batch_sizes": (c_int, [c_p, c_p, c_p]),
+    "nlgpu_batch_set_method": (c_int, [c_p, c_int]),
+    "nlgpu_batch_last_solve": (c_int, [c_p, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)]),
     "nlgpu_nonstationary_2d_compute": (c_int, [c_p, c_d, c_p]),
     "nlgpu_nonstationary_2d_step": (c_int, [c_p, c_d, c_p, c_d, c_i64, c_p, ctypes.POINTER(c_i64)]),
     "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),

@@ -223,7 +223,13 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
         timer.mark("FP32 matrix");
         NL_REQUIRE(o.coarse_aggregates >= 0, NLGPU_ERR_ARG, "coarse_aggregates must be >= 0");
         const bool coarse = o.coarse_aggregates > 0 && M && !c.neumann;
-        if (coarse) coarse_build(c, c.full, o.coarse_aggregates);
+        if (coarse) {
+            double aspect = o.coarse_aspect;
+            if (!(aspect > 0.0))
+                aspect = c.model.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC && c.model.cond[0] > 0.0 && c.model.cond[1] > 0.0
+                             ? std::sqrt(c.model.cond[0] / c.model.cond[1]) : 1.0;
+            coarse_build(c, c.full, o.coarse_aggregates, aspect);
+        }
         timer.mark("coarse correction");
         c.ilt_sweeps = sweeps;
         r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, b, c.temperature.p, o.tolerance, o.max_iterations,
@@ -1125,6 +1131,21 @@ int nlgpu_batch_step(nlgpu_batch* batch, const double* dirichlet_values, double 
 int nlgpu_batch_temperature(nlgpu_batch* batch, int64_t index, double* temperature) {
     if (!batch || !temperature) return NLGPU_ERR_ARG;
     return guarded([&] { batch_temperature(*batch->impl, index, temperature); });
+}
+
+int nlgpu_batch_last_solve(nlgpu_batch* batch, int64_t* inner_iterations, int64_t* outer_iterations, int* fallback) {
+    if (!batch || !inner_iterations || !outer_iterations || !fallback) return NLGPU_ERR_ARG;
+    return guarded([&] { batch_last_solve(*batch->impl, inner_iterations, outer_iterations, fallback); });
+}
+
+int nlgpu_batch_set_method(nlgpu_batch* batch, int method) {
+    if (!batch) return NLGPU_ERR_ARG;
+    return guarded([&] { batch_set_method(*batch->impl, method); });
+}
+
+int nlgpu_batch_sizes(nlgpu_batch* batch, int64_t* rows, int64_t* system_entries) {
+    if (!batch || !rows || !system_entries) return NLGPU_ERR_ARG;
+    return guarded([&] { batch_sizes(*batch->impl, rows, system_entries); });
 }
 
 int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double length, double radius, double local_weight,

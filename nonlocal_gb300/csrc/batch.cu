@@ -17,8 +17,17 @@
 //   * a chunk of CG_ITERS iterations is captured once as a CUDA graph and
 //     replayed; the host reads how many instances are still running once per
 //     chunk.
+// That identity FP64 CG is the reference's per-step solve.  The other method
+// (NLGPU_BATCH_MIXED_ILLT) solves the whole block-diagonal system with the
+// single-system mixed-precision FCG (FP32 difference-form SpMV, FP32 ILLT by
+// Jacobi sweeps, FP64 reliable updates) preconditioned by the ILLT of
+// C + dt p1 K_local of every instance (the block-diagonal local part, factored
+// once), to a global tolerance tol sqrt(min_k |b_k|^2 / sum_k |b_k|^2) that
+// gives every instance |b_k - A_k x_k| <= tol |b_k|; the FP64 ILLT-CG is its
+// fallback when the FCG does not converge.
 #include "common.cuh"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 
@@ -57,39 +66,70 @@ __global__ void k_bt_axpy(i64 n, const double* __restrict__ a, double* __restric
     BT_ROWS(i) y[i] += a[i];
 }
 
-// y = A x, warp per padded full row; running instances only.  Optional
-// per-instance partials of x.y.
-__global__ void __launch_bounds__(BT_THREADS) k_bt_spmv(i64 n, const i64* __restrict__ rp, const int4* __restrict__ col4,
+// y = A x over padded full rows in row blocks: a block holds 32 / g
+// consecutive rows of one instance, each taken by g lanes (g a power of two
+// from the instance's mean row length, so that every lane reads a few int4
+// groups), and the warps take blocks in turn (grid stride).  The instances'
+// rows differ in length by two orders of magnitude (r/h from 2 to 26): a
+// whole warp per short row left most lanes idle and spent a five-step FP64
+// warp reduction per row, which on GB300's two-lane FP64 pipe cost more than
+// the row.  Blocks of stopped instances are skipped.  Optional per-instance
+// partials of x.y: one warp sum per block, kept by lane 0 while its blocks stay
+// in one instance and added with one FP64 atomic when the instance changes.
+// desc: first row (bits 0-31), log2 g (bits 32-34), rows in the block (35-40).
+__global__ void __launch_bounds__(BT_THREADS) k_bt_spmv(i64 nblocks, const unsigned long long* __restrict__ desc,
+                                                        const i64* __restrict__ rp, const int4* __restrict__ col4,
                                                         const double2* __restrict__ val2, const double* __restrict__ x,
                                                         double* __restrict__ y, const int32_t* __restrict__ inst,
                                                         const double* __restrict__ sc, i64 K, double* __restrict__ dot) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
-    // contiguous row ranges per warp keep a warp inside one instance most of the time
-    const i64 per = (n + warps - 1) / warps;
-    const i64 w = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5;
-    const i64 r0 = w * per, r1 = r0 + per < n ? r0 + per : n;
-    for (i64 base = r0; base < r1; base += 32) {
-        // lane l computes nothing itself; the warp walks the 32 rows of this slice
-        double mine = 0.0;
-        int my_inst = -1;
-        for (int j = 0; j < 32 && base + j < r1; ++j) {
-            const i64 r = base + j;
-            const int k = inst[r];
-            if (sc[BS_DONE * K + k] != 0.0) continue;
+    double acc = 0.0;
+    int acc_inst = -1;
+    for (i64 bk = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; bk < nblocks; bk += warps) {
+        const unsigned long long d = desc[bk];
+        const i64 first = i64(d & 0xffffffffull);
+        const int lg = int((d >> 32) & 7), cnt = int((d >> 35) & 63);
+        const int k = inst[first];
+        if (sc[BS_DONE * K + k] != 0.0) continue;
+        const int g = 1 << lg, sub = lane & (g - 1), slot = lane >> lg;
+        const i64 r = first + slot;
+        const bool active = slot < cnt;
+        double s = 0.0;
+        if (active) {
             const i64 b4 = rp[r] >> 2, e4 = rp[r + 1] >> 2;
-            double s = 0.0;
-            for (i64 q = b4 + lane; q < e4; q += 32) {
+            for (i64 q = b4 + sub; q < e4; q += g) {
                 const int4 c = __ldg(col4 + q);
                 const double2 v0 = __ldg(val2 + 2 * q), v1 = __ldg(val2 + 2 * q + 1);
                 s += v0.x * x[c.x] + v0.y * x[c.y] + v1.x * x[c.z] + v1.y * x[c.w];
             }
-            s = warp_sum(s);
-            if (lane == j) { mine = s * x[r]; my_inst = k; }
-            if (lane == 0) y[r] = s;
         }
-        if (dot) seg_add(my_inst >= 0 ? mine : 0.0, my_inst, dot);
+        for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(full, s, o);   // within the lane group
+        double contrib = 0.0;
+        if (active && sub == 0) {
+            y[r] = s;
+            contrib = s * x[r];
+        }
+        if (dot) {
+            contrib = warp_sum(contrib);
+            if (lane == 0) {
+                if (k != acc_inst) {
+                    if (acc_inst >= 0) atomicAdd(dot + acc_inst, acc);
+                    acc = 0.0;
+                    acc_inst = k;
+                }
+                acc += contrib;
+            }
+        }
     }
+    if (dot && lane == 0 && acc_inst >= 0) atomicAdd(dot + acc_inst, acc);
+}
+
+// per-instance |v|^2 into acc (zeroed by the caller)
+__global__ void __launch_bounds__(BT_THREADS) k_bt_norm2(i64 n, const double* __restrict__ v,
+                                                         const int32_t* __restrict__ inst, double* __restrict__ acc) {
+    BT_ROWS(i) seg_add(v[i] * v[i], inst[i], acc);
 }
 
 // out = in - B x_D on inner rows, x_D on Dirichlet rows (warp per row of the
@@ -212,12 +252,24 @@ struct Batch {
     std::vector<i64> row_off;
     dbuf<int32_t> inst_of_row;
     Csr A, C, B;
+    dbuf<unsigned long long> blocks_A, blocks_C;   // SpMV row blocks (k_bt_spmv)
+    i64 nblocks_A = 0, nblocks_C = 0;
     dbuf<double> rhs_dt, x, b, r, p, q, tmp, xd, dval, sc;
     dbuf<uint8_t> is_inner;
     dbuf<int> running;
     cudaGraphExec_t chunk = nullptr;
     double chunk_tol2 = -1.0, chunk_cap = -1.0;
     int chunk_kernels = 0;
+    // NLGPU_BATCH_MIXED_ILLT: the single-system solvers' work buffers on this
+    // stream, the block-diagonal local matrix and its ILLT (built at the first
+    // mixed step)
+    int method = NLGPU_BATCH_IDENTITY_FP64;
+    Ctx solver;
+    Csr M;
+    IncompleteCholesky ic;
+    bool mixed_ready = false;
+    i64 last_inner = 0, last_outer = 0;
+    bool last_fallback = false;
 };
 
 namespace {
@@ -245,10 +297,37 @@ void concat(Batch& bt, Csr& out, Sel sel, bool with_inst) {
     }
 }
 
+// row blocks of a concatenated matrix for k_bt_spmv: per instance g lanes per
+// row, g the smallest power of two (2 .. 32) with g * 12 >= the mean padded
+// row length (about three int4 groups per lane)
+void row_blocks(Batch& bt, const Csr& M, dbuf<unsigned long long>& out, i64& count) {
+    std::vector<i64> rp(size_t(bt.N + 1));
+    M.rowptr.download(rp.data(), rp.size(), bt.stream);
+    NL_CUDA(cudaStreamSynchronize(bt.stream));
+    std::vector<unsigned long long> desc;
+    for (i64 k = 0; k < bt.K; ++k) {
+        const i64 r0 = bt.row_off[size_t(k)], r1 = bt.row_off[size_t(k) + 1];
+        if (r1 <= r0) continue;
+        const double mean = double(rp[size_t(r1)] - rp[size_t(r0)]) / double(r1 - r0);
+        int lg = 1;
+        while (lg < 5 && double(1 << lg) * 12.0 < mean) ++lg;
+        const i64 per = 32 >> lg;
+        for (i64 r = r0; r < r1; r += per)
+            desc.push_back((unsigned long long)r | ((unsigned long long)lg << 32) |
+                           ((unsigned long long)std::min<i64>(per, r1 - r) << 35));
+    }
+    count = i64(desc.size());
+    out.resize(std::max<size_t>(desc.size(), 1));
+    if (!desc.empty()) out.upload(desc.data(), desc.size(), bt.stream);
+}
+
 // y = M x over every row; with skip_done the rows of stopped instances are left
 // alone (the second half of the scalar array stays zero: "nothing stopped")
 void bt_spmv(Batch& bt, const Csr& M, const double* x, double* y, double* dot, bool skip_done) {
-    NL_LAUNCH(k_bt_spmv, RED_BLOCKS, BT_THREADS, 0, bt.stream, bt.N, M.rowptr.p, reinterpret_cast<const int4*>(M.col.p),
+    const bool is_a = &M == &bt.A;
+    const i64 nb = is_a ? bt.nblocks_A : bt.nblocks_C;
+    NL_LAUNCH(k_bt_spmv, grid_for(nb * 32, BT_THREADS, 152 * 8), BT_THREADS, 0, bt.stream, nb,
+              (is_a ? bt.blocks_A : bt.blocks_C).p, M.rowptr.p, reinterpret_cast<const int4*>(M.col.p),
               reinterpret_cast<const double2*>(M.val.p), x, y, bt.inst_of_row.p,
               skip_done ? bt.sc.p : bt.sc.p + bt.K * BS_COUNT, bt.K, dot);
 }
@@ -274,6 +353,19 @@ Batch* batch_create(const std::vector<Ctx*>& instances) {
         concat(*bt, bt->A, [](Ctx& c) -> const Csr& { return c.full; }, true);
         concat(*bt, bt->C, [](Ctx& c) -> const Csr& { return c.capacity_full; }, false);
         concat(*bt, bt->B, [](Ctx& c) -> const Csr& { return c.bound; }, false);
+        row_blocks(*bt, bt->A, bt->blocks_A, bt->nblocks_A);
+        row_blocks(*bt, bt->C, bt->blocks_C, bt->nblocks_C);
+        // the instances' upper-storage copies of dt K + C and their full -> upper
+        // maps are read again only by the radiation update of a single-instance
+        // step, and batches hold no radiation: release them (a third of the
+        // memory of a large batch)
+        NL_CUDA(cudaStreamSynchronize(bt->stream));
+        for (Ctx* c : instances) {
+            c->full_from_upper.release();
+            c->inner.col.release();
+            c->inner.val.release();
+            c->inner.nnz = 0;
+        }
         for (auto* v : {&bt->rhs_dt, &bt->x, &bt->b, &bt->r, &bt->p, &bt->q, &bt->tmp, &bt->xd}) v->resize(size_t(bt->N));
         bt->is_inner.resize(size_t(bt->N));
         for (i64 k = 0; k < bt->K; ++k) {
@@ -306,6 +398,79 @@ void batch_destroy(Batch* bt) {
     delete bt;
 }
 
+namespace {
+
+// the block-diagonal local matrix C + dt p1 K_local (upper, Dirichlet rows a
+// unit diagonal), its ILLT and the FP32 copy of the system matrix
+void batch_prepare_mixed(Batch& bt) {
+    if (bt.mixed_ready) return;
+    std::vector<Csr> local(bt.inst.size());
+    for (size_t k = 0; k < bt.inst.size(); ++k) {
+        Ctx& c = *bt.inst[k];
+        build_patterns(c, true, true, local[k], nullptr, nullptr, nullptr);
+        assemble_local(c, local[k], c.capacity * c.density, 1);
+        assemble_local(c, local[k], c.time_step * c.model.p1, 0);
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    concat(bt, bt.M, [&](Ctx& c) -> const Csr& {
+        const size_t k = size_t(std::find(bt.inst.begin(), bt.inst.end(), &c) - bt.inst.begin());
+        return local[k];
+    }, false);
+    bt.solver.stream = bt.stream;
+    bt.solver.n_nodes = bt.N;
+    ilt_build(bt.solver, bt.M, bt.ic, false);
+    NL_REQUIRE(bt.ic.ok, NLGPU_ERR_NUMERICAL, "the ILLT of the batched local matrix failed");
+    matrix_to_f32(bt.solver, bt.A, nullptr);
+    NL_REQUIRE(bt.A.col16_ok, NLGPU_ERR_UNSUPPORTED, "an instance's band is wider than 16-bit column offsets");
+    NL_CUDA(cudaStreamSynchronize(bt.stream));
+    bt.mixed_ready = true;
+}
+
+i64 batch_solve_mixed(Batch& bt, double tolerance, i64 max_iterations, i64* iterations) {
+    const i64 N = bt.N, K = bt.K;
+    batch_prepare_mixed(bt);
+    double* bb = bt.sc.p + BS_BB * K;
+    NL_CUDA(cudaMemsetAsync(bb, 0, size_t(K) * sizeof(double), bt.stream));
+    NL_LAUNCH(k_bt_norm2, RED_BLOCKS, BT_THREADS, 0, bt.stream, N, bt.b.p, bt.inst_of_row.p, bb);
+    std::vector<double> h(static_cast<size_t>(K));
+    NL_CUDA(cudaMemcpyAsync(h.data(), bb, size_t(K) * sizeof(double), cudaMemcpyDeviceToHost, bt.stream));
+    NL_CUDA(cudaStreamSynchronize(bt.stream));
+    double total = 0.0, smallest = 0.0;
+    for (double v : h) {
+        total += v;
+        if (v > 0.0 && (smallest == 0.0 || v < smallest)) smallest = v;
+    }
+    if (total == 0.0) {   // every right-hand side zero: x = 0 everywhere
+        NL_CUDA(cudaMemsetAsync(bt.x.p, 0, size_t(N) * sizeof(double), bt.stream));
+        if (iterations) for (i64 k = 0; k < K; ++k) iterations[k] = 0;
+        return 0;
+    }
+    const double tol_g = tolerance * std::sqrt(smallest / total);
+    CgResult r = mixed_solve(bt.solver, bt.A, &bt.ic, bt.b.p, bt.x.p, tol_g, max_iterations, 1e-2, true, false,
+                             NLGPU_DEFAULT_TRIANGULAR_SWEEPS, false);
+    bt.last_fallback = !r.converged;
+    if (!r.converged) r = cg_solve(bt.solver, bt.A, &bt.ic, bt.b.p, bt.x.p, tol_g, max_iterations, true);
+    bt.last_inner = r.iterations;
+    bt.last_outer = r.outer_iterations;
+    NL_REQUIRE(r.converged, NLGPU_ERR_NO_CONVERGENCE, "the batched step did not converge");
+    if (iterations) for (i64 k = 0; k < K; ++k) iterations[k] = r.iterations;
+    return r.iterations;
+}
+
+}  // namespace
+
+void batch_last_solve(const Batch& bt, i64* inner, i64* outer, int* fallback) {
+    *inner = bt.method == NLGPU_BATCH_MIXED_ILLT ? bt.last_inner : 0;
+    *outer = bt.method == NLGPU_BATCH_MIXED_ILLT ? bt.last_outer : 0;
+    *fallback = bt.method == NLGPU_BATCH_MIXED_ILLT && bt.last_fallback ? 1 : 0;
+}
+
+void batch_set_method(Batch& bt, int method) {
+    NL_REQUIRE(method == NLGPU_BATCH_IDENTITY_FP64 || method == NLGPU_BATCH_MIXED_ILLT, NLGPU_ERR_ARG,
+               "batch method: NLGPU_BATCH_IDENTITY_FP64 or NLGPU_BATCH_MIXED_ILLT");
+    bt.method = method;
+}
+
 // one implicit-Euler step of every instance; returns the largest iteration count
 i64 batch_step(Batch& bt, const double* dirichlet_values, double tolerance, i64 max_iterations, i64* iterations) {
     const i64 N = bt.N, K = bt.K;
@@ -319,6 +484,7 @@ i64 batch_step(Batch& bt, const double* dirichlet_values, double tolerance, i64 
     NL_LAUNCH(k_bt_axpy, grid_for(N, 256), 256, 0, bt.stream, N, bt.rhs_dt.p, bt.tmp.p);
     NL_LAUNCH(k_bt_first_kind, grid_for(N * 32, 256, 152 * 64), 256, 0, bt.stream, N, bt.B.rowptr.p, bt.B.col.p,
               bt.B.val.p, bt.tmp.p, bt.xd.p, bt.is_inner.p, bt.b.p);
+    if (bt.method == NLGPU_BATCH_MIXED_ILLT) return batch_solve_mixed(bt, tolerance, max_iterations, iterations);
     // CG from x0 = T_prev: r = b - A x, p = r, |r|^2 and |b|^2 per instance
     NL_CUDA(cudaMemsetAsync(sc, 0, size_t(K) * BS_COUNT * sizeof(double), bt.stream));
     bt_spmv(bt, bt.A, bt.x.p, bt.q.p, nullptr, false);
@@ -377,5 +543,12 @@ void batch_temperature(Batch& bt, i64 index, double* out) {
 }
 
 cudaStream_t batch_stream(Batch& bt) { return bt.stream; }
+
+void batch_sizes(const Batch& bt, i64* rows, i64* system_entries) {
+    for (size_t k = 0; k < bt.inst.size(); ++k) {
+        rows[k] = bt.row_off[k + 1] - bt.row_off[k];
+        system_entries[k] = bt.inst[k]->full.nnz;
+    }
+}
 
 }  // namespace nlgpu

@@ -73,12 +73,12 @@ __global__ void k_bbox(i64 n, const double* __restrict__ xy, const uint8_t* __re
 
 // aggregate cell of every node (-1 for rows that are not inner)
 __global__ void k_cell_of_node(i64 n, const double* __restrict__ xy, const uint8_t* __restrict__ is_inner, double x0,
-                               double y0, double inv_h, int cx, int cy, int32_t* __restrict__ cell,
+                               double y0, double inv_hx, double inv_hy, int cx, int cy, int32_t* __restrict__ cell,
                                i64* __restrict__ used) {
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         if (is_inner && !is_inner[i]) { cell[i] = -1; continue; }
-        const int a = min(cx - 1, max(0, int((xy[2 * i] - x0) * inv_h)));
-        const int b = min(cy - 1, max(0, int((xy[2 * i + 1] - y0) * inv_h)));
+        const int a = min(cx - 1, max(0, int((xy[2 * i] - x0) * inv_hx)));
+        const int b = min(cy - 1, max(0, int((xy[2 * i + 1] - y0) * inv_hy)));
         const int c = b * cx + a;
         cell[i] = c;
         used[c] = 1;
@@ -425,7 +425,7 @@ __global__ void k_add_coarse(i64 n, const float* __restrict__ y, float* __restri
 
 }  // namespace
 
-void coarse_build(Ctx& ctx, const Csr& A, int target) {
+void coarse_build(Ctx& ctx, const Csr& A, int target, double aspect) {
     Coarse& co = ctx.co;
     const i64 n = A.rows;
     NL_REQUIRE(n == ctx.n_nodes && ctx.is_inner.n == size_t(n), NLGPU_ERR_STATE,
@@ -446,15 +446,19 @@ void coarse_build(Ctx& ctx, const Csr& A, int target) {
     if (hb[0] == ~0ull) return;   // no inner node
     const double x0 = from_key(hb[0]), y0 = from_key(hb[1]), x1 = from_key(hb[2]), y1 = from_key(hb[3]);
     const double wx = std::max(x1 - x0, 1e-300), wy = std::max(y1 - y0, 1e-300);
+    // cells of area wx wy / target, `aspect` times wider than high (elongated
+    // along the stronger conductivity, where the error is smoothest)
+    const double a = std::min(std::max(aspect > 0.0 ? aspect : 1.0, 1.0 / 64.0), 64.0);
     const double h = std::max(std::sqrt(wx * wy / double(target)), std::max(wx, wy) / 4096.0);
-    const int cx = std::max(1, int(std::ceil(wx / h * (1.0 + 1e-12)))), cy = std::max(1, int(std::ceil(wy / h * (1.0 + 1e-12))));
+    const double hx = h * std::sqrt(a), hy = h / std::sqrt(a);
+    const int cx = std::max(1, int(std::ceil(wx / hx * (1.0 + 1e-12)))), cy = std::max(1, int(std::ceil(wy / hy * (1.0 + 1e-12))));
     const i64 cells = i64(cx) * cy;
     co.agg.resize(size_t(n));
     dbuf<i64> used;
     used.resize(size_t(cells) + 1);
     used.zero(ctx.stream);
     NL_LAUNCH(k_cell_of_node, grid_for(n, CO_THREADS), CO_THREADS, 0, ctx.stream, n, ctx.nodes.p, ctx.is_inner.p, x0, y0,
-              1.0 / h, cx, cy, co.agg.p, used.p);
+              1.0 / hx, 1.0 / hy, cx, cy, co.agg.p, used.p);
     i64 nc = 0;
     exclusive_scan(ctx, used.p, used.p, cells + 1, &nc);
     co.nc = nc;

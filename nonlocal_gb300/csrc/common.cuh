@@ -554,7 +554,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A_full, IncompleteCholesky* M, const d
                      i64 max_iterations, double update_factor, bool x_is_initial_guess, bool learned, int sweeps,
                      bool coarse = false);
 // coarse.cu: the coarse-space correction around the FP32 ILLT application
-void coarse_build(Ctx& ctx, const Csr& A_full, int target);
+void coarse_build(Ctx& ctx, const Csr& A_full, int target, double aspect = 1.0);
 void coarse_before(Ctx& ctx, const float* r, const double* flags);   // ctx.co.w = r - A Q r, ctx.co.y = Q r
 void coarse_after(Ctx& ctx, float* z, const double* flags);          // z += Q r
 // batch.cu: many nonstationary instances stepped together (block-diagonal system)
@@ -564,6 +564,9 @@ void batch_destroy(Batch* bt);
 i64 batch_step(Batch& bt, const double* dirichlet_values, double tolerance, i64 max_iterations, i64* iterations);
 void batch_temperature(Batch& bt, i64 index, double* out);
 cudaStream_t batch_stream(Batch& bt);
+void batch_sizes(const Batch& bt, i64* rows, i64* system_entries);
+void batch_set_method(Batch& bt, int method);
+void batch_last_solve(const Batch& bt, i64* inner, i64* outer, int* fallback);
 // bicgstab.cu: Jacobi-preconditioned BiCGSTAB on a full-row (non-symmetric) matrix, zero start
 CgResult bicgstab_solve(Ctx& ctx, const Csr& A_full, const double* b, double* x, double tolerance, i64 max_iterations);
 // mpnn.cu

@@ -13,7 +13,10 @@
 
 namespace nlgpu {
 
-struct ff {
+// 8-byte aligned, so that a float-float moves as one 64-bit access wherever it
+// lives (a 4-byte aligned array of them, after a 4-byte shared variable, gave
+// misaligned 64-bit shared-memory loads)
+struct __align__(8) ff {
     float h, l;
 };
 

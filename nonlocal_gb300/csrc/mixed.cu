@@ -728,8 +728,11 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     // |b|^2 and the first residual
     NL_LAUNCH(k_dot_f64, G, MX_THREADS, 0, ctx.stream, n, b, b, outer_part);
     NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, outer_part, outer_sc);
+    bool x_zero = !x_is_initial_guess;   // A 0 = 0: the first residual needs no product
     auto true_residual = [&](double* hs) {
-        spmv_full(ctx, A, x, w.q64.p);
+        if (x_zero) NL_CUDA(cudaMemsetAsync(w.q64.p, 0, size_t(n) * sizeof(double), ctx.stream));
+        else spmv_full(ctx, A, x, w.q64.p);
+        x_zero = false;
         NL_LAUNCH(k_residual_f64, G, MX_THREADS, 0, ctx.stream, n, b, w.q64.p, w.r64.p, outer_part + RED_BLOCKS);
         NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, outer_part + RED_BLOCKS, outer_sc + 1);
         NL_CUDA(cudaMemcpyAsync(hs, outer_sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));

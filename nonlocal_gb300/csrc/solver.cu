@@ -309,6 +309,15 @@ __global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t
             acc = own ? a[b + lane] : 0.0;
             if (lane == 0) acc += shift;
         }
+        // the first chunk's structure does not depend on other rows: load it
+        // before waiting, so only the values are read after the wait
+        const int ns_first = le - lb < IC_MAXS ? int(le - lb) : IC_MAXS;
+        i64 pk_first = 0;
+        int len_first = 0;
+        if (m <= 32 && lane < ns_first) {
+            pk_first = l_to_u[lb + lane];
+            len_first = int(rp[lcol[lb + lane] + 1] - pk_first);
+        }
         // wait for the rows this row reads
         bool gave_up = false;
         for (i64 s = lb + lane; s < le && !gave_up; s += 32) {
@@ -328,14 +337,15 @@ __global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t
         } else {
             for (i64 s0 = lb; s0 < le; s0 += IC_MAXS) {
                 const int ns = le - s0 < IC_MAXS ? int(le - s0) : IC_MAXS;
-                i64 pk = 0;
+                const bool first_chunk = s0 == lb;
+                i64 pk = first_chunk ? pk_first : 0;
                 double uki = 0.0;
-                int len = 0;
-                if (lane < ns) {
+                int len = first_chunk ? len_first : 0;
+                if (!first_chunk && lane < ns) {
                     pk = l_to_u[s0 + lane];   // (k, i) in U: row k's segment from column i on
                     len = int(rp[lcol[s0 + lane] + 1] - pk);
-                    uki = __ldcg(u + pk);
                 }
+                if (lane < ns) uki = __ldcg(u + pk);
                 int incl = len;
                 for (int o = 1; o < 32; o <<= 1) {
                     const int v = __shfl_up_sync(full, incl, o);

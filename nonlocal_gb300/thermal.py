@@ -375,24 +375,28 @@ class Problem2D(Context):
     # ---- solves -----------------------------------------------------------------
     @staticmethod
     def _options(tolerance, max_iterations, preconditioner, precision, inner_tolerance=0.0,
-                 triangular_sweeps=0, coarse_aggregates=0) -> L.SolveOptions:
+                 triangular_sweeps=0, coarse_aggregates=0, coarse_aspect=0.0) -> L.SolveOptions:
         o = L.SolveOptions()
         o.tolerance, o.max_iterations = float(tolerance), int(max_iterations)
         o.preconditioner, o.precision = L.PRECONDITIONER[preconditioner], L.PRECISION[precision]
         o.inner_tolerance = float(inner_tolerance)
         o.triangular_sweeps = int(triangular_sweeps)
         o.coarse_aggregates = int(coarse_aggregates)
+        o.coarse_aspect = float(coarse_aspect)
         return o
 
     def stationary(self, tolerance=1e-10, max_iterations=10000, preconditioner="illt", precision="fp64",
-                   check_convergence=True, inner_tolerance=0.0, triangular_sweeps=0, coarse_aggregates=0):
+                   check_convergence=True, inner_tolerance=0.0, triangular_sweeps=0, coarse_aggregates=0,
+                   coarse_aspect=0.0):
         """stationary_heat_equation_solver_2d; precision "mixed" runs the FP32 inner
         solve with FP64 refinement (inner_tolerance: reduction per inner solve;
         triangular_sweeps: Jacobi sweeps per triangle of the FP32 ILLT application,
         0 the default, -1 exact level-scheduled substitution; coarse_aggregates > 0
-        adds a coarse-space correction over about that many node aggregates)."""
+        adds a coarse-space correction over about that many node aggregates, whose
+        grid cells are coarse_aspect times wider than high (0: from the
+        conductivity))."""
         o = self._options(tolerance, max_iterations, preconditioner, precision, inner_tolerance, triangular_sweeps,
-                          coarse_aggregates)
+                          coarse_aggregates, coarse_aspect)
         t = np.empty(self.n_nodes)
         rep = L.SolveReport()
         rc = self._lib.nlgpu_stationary_2d(self._h, ctypes.byref(o), L.ptr(t), ctypes.byref(rep))
@@ -613,6 +617,27 @@ class BatchNonstationary:
         t = np.empty(self.solvers[index].problem.n_nodes)
         L.check(self._lib.nlgpu_batch_temperature(self._h, int(index), L.ptr(t)))
         return t
+
+    def set_method(self, method: str = "identity_fp64") -> None:
+        """The step's solver: "identity_fp64" (the reference's identity CG per
+        instance) or "mixed_illt" (mixed-precision FCG with ILLT on the whole
+        block-diagonal system, FP64 ILLT-CG fallback)."""
+        L.check(self._lib.nlgpu_batch_set_method(self._h, L.BATCH_METHOD[method]))
+
+    def last_solve(self) -> dict:
+        """mixed_illt: the last step's FCG iterations, FP64 refinement steps and
+        whether the FP64 ILLT-CG fallback ran."""
+        inner, outer = ctypes.c_int64(), ctypes.c_int64()
+        fb = ctypes.c_int()
+        L.check(self._lib.nlgpu_batch_last_solve(self._h, ctypes.byref(inner), ctypes.byref(outer), ctypes.byref(fb)))
+        return {"inner": inner.value, "outer": outer.value, "fallback": bool(fb.value)}
+
+    def sizes(self) -> tuple[np.ndarray, np.ndarray]:
+        """Per instance: rows and the system entries each step's SpMV reads."""
+        rows = np.empty(len(self.solvers), dtype=np.int64)
+        nnz = np.empty(len(self.solvers), dtype=np.int64)
+        L.check(self._lib.nlgpu_batch_sizes(self._h, L.ptr(rows), L.ptr(nnz)))
+        return rows, nnz
 
 
 class NonstationaryHeatEquationSolver2D:

@@ -412,6 +412,38 @@ def test_batched_nonstationary_matches_single_instances(lib):
     batch.close()
 
 
+def test_batched_mixed_illt_matches_single_instances(lib):
+    """The batched step's mixed-precision ILLT method (FCG on the whole
+    block-diagonal system, FP64 reliable updates, every instance held to its own
+    relative residual) reaches the temperatures of the reference's identity FP64
+    CG stepping each instance on its own, in fewer iterations."""
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    specs = [(12, 0.25, 1e-3), (20, 0.15, 1e-3), (9, 0.3, 2e-3), (16, 0.2, 5e-4)]
+
+    def build(nx, r, dt):
+        mesh = structured_quad_mesh(nx, nx, "bilinear")
+        pb = T.Problem2D.from_mesh(mesh)
+        pb.set_model(T.Model2D(influence="fast_polynomial", radius=(r, r), local_weight=0.5))
+        pb.add_boundary(T.Boundary(edges=mesh.boundaries["left"], kind="temperature", value=0.0))
+        pb.add_boundary(T.Boundary(edges=mesh.boundaries["right"], kind="flux", value=1.0))
+        s = T.NonstationaryHeatEquationSolver2D(pb, dt)
+        s.compute()
+        return s
+
+    singles = [build(*sp) for sp in specs]
+    batch = T.BatchNonstationary([build(*sp) for sp in specs])
+    batch.set_method("mixed_illt")
+    for step in range(1, 6):
+        values = [np.sin(10.0 * step * sp[2]) for sp in specs]
+        its = batch.step(values, tolerance=1e-13, max_iterations=5000)
+        for k, s in enumerate(singles):
+            t = s.calc_step(values[k], tolerance=1e-13, max_iterations=5000)
+            assert rel(batch.temperature(k), t) < SOLUTION_RTOL, (step, k)
+        assert int(its.max()) < max(s.iterations[-1] for s in singles), (step, its, [s.iterations[-1] for s in singles])
+    batch.close()
+
+
 @pytest.mark.parametrize("name", ["d1_quadratic_1000", "d1_linear_40_triangle"])
 def test_stationary_1d(lib, name):
     from nonlocal_gb300 import thermal as T
