@@ -105,8 +105,8 @@ typedef struct nlgpu_solve_options {
     int coarse_aggregates;    /* MIXED with ILLT: 0 none; > 0 adds a coarse-space correction over about
                                  that many node aggregates (no counterpart in the reference, whose
                                  preconditioner is ILLT alone) */
-    double coarse_aspect;     /* width / height of the aggregates' grid cells; <= 0: sqrt(lambda_x /
-                                 lambda_y) for an orthotropic conductivity, 1 otherwise */
+    double coarse_aspect;     /* width / height of the aggregates' grid cells; <= 0: (lambda_x /
+                                 lambda_y)^0.7 for an orthotropic conductivity, 1 otherwise */
 } nlgpu_solve_options;
 
 typedef struct nlgpu_solve_report {

@@ -225,9 +225,12 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
         const bool coarse = o.coarse_aggregates > 0 && M && !c.neumann;
         if (coarse) {
             double aspect = o.coarse_aspect;
+            // (lambda_x / lambda_y)^0.7: on the 300x300 orthotropic (1, 0.1) problem the
+            // FCG took 87 iterations with square cells, 67 at ratio^0.5, 62 at
+            // ratio^0.7 (aspect 5), 72 at the ratio itself
             if (!(aspect > 0.0))
                 aspect = c.model.cond_kind == NLGPU_CONDUCTIVITY_ORTHOTROPIC && c.model.cond[0] > 0.0 && c.model.cond[1] > 0.0
-                             ? std::sqrt(c.model.cond[0] / c.model.cond[1]) : 1.0;
+                             ? std::pow(c.model.cond[0] / c.model.cond[1], 0.7) : 1.0;
             coarse_build(c, c.full, o.coarse_aggregates, aspect);
         }
         timer.mark("coarse correction");

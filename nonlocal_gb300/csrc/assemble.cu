@@ -277,6 +277,7 @@ struct PairFF {
     ff phi[NQ * NQ];
     ff c[NQ];
     int32_t nodes[NEN];
+    int32_t inner[NEN];   // whether each of eNL's nodes is inner (read once per pair, not per entry)
 };
 
 // shape<INF> in float-float (fast polynomial, polynomial and exponential with
@@ -306,7 +307,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_assemble_pairs_ff(AssembleArgs a
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ ff eqx[NQ], eqy[NQ], ewx[NEN * NQ], ewy[NEN * NQ];
     __shared__ double egx[NEN * NQ], egy[NEN * NQ], ejac[NQ], elam[NQ];   // the self term stays FP64
-    __shared__ int32_t enodes[NEN];
+    __shared__ int32_t enodes[NEN], einner[NEN];   // eL's nodes and whether each is inner
     __shared__ i64 row_start[NEN];
     __shared__ int row_len[NEN], row_off[NEN + 1];
     __shared__ int use_smem;
@@ -342,9 +343,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_assemble_pairs_ff(AssembleArgs a
         }
         if (threadIdx.x < NEN) {
             const int32_t r = a.elems[eL * NEN + threadIdx.x];
+            const bool r_in = a.is_inner[r];
             enodes[threadIdx.x] = r;
+            einner[threadIdx.x] = r_in;
             row_start[threadIdx.x] = a.in_rp[r];
-            row_len[threadIdx.x] = a.is_inner[r] ? int(a.in_rp[r + 1] - a.in_rp[r]) : 0;
+            row_len[threadIdx.x] = r_in ? int(a.in_rp[r + 1] - a.in_rp[r]) : 0;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -385,7 +388,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_assemble_pairs_ff(AssembleArgs a
                 const float2 c = f.cw[i64(eNL) * NQ + lane];
                 ps.c[lane] = ff{c.x, c.y};
             }
-            if (lane < NEN) ps.nodes[lane] = a.elems[i64(eNL) * NEN + lane];
+            if (lane < NEN) {
+                const int32_t c = a.elems[i64(eNL) * NEN + lane];
+                ps.nodes[lane] = c;
+                ps.inner[lane] = a.is_inner[c];
+            }
             __syncwarp();
             for (int t = lane; t < NQ * NQ; t += 32) {
                 const int qL = t / NQ, qNL = t % NQ;
@@ -429,7 +436,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_assemble_pairs_ff(AssembleArgs a
             for (int t = lane; t < NEN * NEN; t += 32) {
                 const int i = t / NEN, j = t % NEN;
                 const int32_t r = enodes[i], c = ps.nodes[j];
-                const bool r_in = a.is_inner[r], c_in = a.is_inner[c];
+                const bool r_in = einner[i] != 0, c_in = ps.inner[j] != 0;
                 const bool fwd_inner = c_in && r_in && (!a.symmetric || r <= c);
                 const bool fwd_bound = !c_in && r != c;
                 const bool tr = SYM && !self;
