@@ -612,6 +612,139 @@ def batch_instances(count: int, seed: int = 0):
     return [(int(rng.integers(64, 257)), float(rng.uniform(0.03, 0.1))) for _ in range(count)]
 
 
+def config4_instances(count: int, seed: int = 0):
+    """Variable-conductivity workload: 128x128 bilinear meshes, r ~ U[0.02, 0.08],
+    p1 ~ U[0.2, 0.8], a log-normal conductivity exp(g) with g a Gaussian random
+    field (correlation length 0.1, std 0.5), one field seed per instance."""
+    import numpy as np
+    rng = np.random.default_rng(seed + 4)
+    return [(float(rng.uniform(0.02, 0.08)), float(rng.uniform(0.2, 0.8)), int(rng.integers(1 << 31)))
+            for _ in range(count)]
+
+
+def run_config4(args, world, rank, local, dist):
+    """--workload config4: many variable-conductivity stationary problems.  A
+    conductivity field with a nonlocal model makes the reference's system
+    non-symmetric (evaluate_conductivity.hpp:9-48, stationary_heat_equation_solver_2d.hpp:105-108):
+    full storage, ordered-pair assembly and Jacobi-preconditioned BiCGSTAB, as
+    the reference; the instances' contexts run on their own streams from host
+    threads, so their solves overlap on the GPU."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    from nonlocal_gb300 import _lib as L
+    from nonlocal_gb300 import build as nbuild
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.fields import lognormal_conductivity
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    nbuild.build()
+    lib = L.load()
+    L.check(lib.nlgpu_set_device(local))
+    tol, edges = 1e-10, 128
+    specs = config4_instances(args.instances4, seed=rank)
+    mesh = structured_quad_mesh(edges, edges, "bilinear")
+
+    def make(spec):
+        r, p1, seed = spec
+        pb = T.Problem2D.from_mesh(mesh)
+        pb.set_model(T.Model2D(influence="fast_polynomial", radius=(r, r), local_weight=p1))
+        qc = pb.quadrature()[0]
+        pb.set_conductivity_field(lognormal_conductivity(qc, 0.1, 0.5, seed=seed))
+        pb.add_boundary(T.Boundary(edges=mesh.boundaries["left"], kind="temperature", value=0.0))
+        pb.add_boundary(T.Boundary(edges=mesh.boundaries["right"], kind="flux", value=1.0))
+        pb.find_neighbours()
+        return pb
+
+    def solve(pb):
+        _, rep = pb.stationary(tolerance=tol, max_iterations=100000, precision="fp64")
+        return rep
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=SETUP_THREADS) as pool:
+        problems = list(pool.map(make, specs))
+        setup_s = time.perf_counter() - t0
+        for _ in range(args.warmup):
+            list(pool.map(solve, problems))
+        sampler = ClockSampler(local)
+        barrier(dist)
+        launches0 = L.kernel_launches()
+        sampler.start()
+        t_all = time.perf_counter()
+        reps = []
+        for _ in range(args.steps):
+            reps.append(list(pool.map(solve, problems)))
+        total = time.perf_counter() - t_all
+        clocks = sampler.stop()
+    launches = L.kernel_launches() - launches0
+    barrier(dist)
+    total = max_over_ranks(dist, total)
+    last = reps[-1]
+    its = np.array([r.iterations for r in last])
+    per = np.array([r.seconds_total for r in last])
+    pairs = int(sum(r.element_pairs for r in last))
+    # BiCGSTAB reads the full-row FP64 matrix twice per iteration
+    spmv = sum(2 * int(r.iterations) * (int(r.nnz_solver) * 12 + (pb.n_nodes + 1) * 8 + 2 * pb.n_nodes * 8)
+               for r, pb in zip(last, problems))
+    pk, pk_kind = peaks()
+    achieved = spmv / (total / args.steps) / 1e9
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle
+        oracle.build.build()
+        oracle.set_threads(os.cpu_count() or 1)
+        sample = specs[:2]
+        secs = 0.0
+        for r, p1, seed in sample:
+            pbq = make((r, p1, seed))
+            qc = pbq.quadrature()[0]
+            pbq.close()
+            o = oracle.Problem(oracle.BILINEAR, mesh.nodes, mesh.elements)
+            o.set_model(influence=oracle.INF_FAST_POLYNOMIAL, radius=(r, r), local_weight=p1)
+            o.set_conductivity_field(lognormal_conductivity(qc, 0.1, 0.5, seed=seed))
+            o.add_boundary(oracle.BC_TEMPERATURE, mesh.boundaries["left"], 0.0)
+            o.add_flux_boundary(oracle.BC_FLUX, mesh.boundaries["right"], flux=1.0)
+            t1 = time.perf_counter()
+            o.find_neighbours()
+            o.assemble()
+            o.solve(tol=tol, maxit=100000)
+            secs += time.perf_counter() - t1
+        cpu = {"value": len(sample) / secs, "unit": "instance-solves/s", "cores": os.cpu_count() or 1,
+               "kind": "port",
+               "sample": f"{len(sample)} instances of the workload (neighbours, assembly, BiCGSTAB to {tol:g}) by the "
+                         "CPU restatement of the reference on all host threads"}
+    if rank != 0:
+        for pb in problems:
+            pb.close()
+        return 0
+    value = len(specs) * args.steps * world / total
+    line = {
+        "metric": "variable-conductivity nonlocal stationary solves: instance-solves per second (full pipeline "
+                  "from the resident mesh, BiCGSTAB to |b - Ax| <= 1e-10 |b|)",
+        "value": value, "unit": "instance-solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{len(specs)} instances, {edges}x{edges} bilinear, log-normal conductivity exp(g), "
+                               "g a Gaussian random field (correlation length 0.1, std 0.5), r ~ U[0.02, 0.08], "
+                               "p1 ~ U[0.2, 0.8], fast polynomial kernel, left T = 0, unit flux right",
+                   "instances": len(specs), "parallelism": f"replicas x{world}, {SETUP_THREADS} host threads"},
+        "solve_s": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
+        "bicgstab_iterations": {"mean": float(its.mean()), "max": int(its.max())},
+        "element_pairs_per_s": pairs * len(specs) / len(last) * world / (total / args.steps) / len(specs),
+        "setup_s": setup_s, "clocks": clocks, "gpu_launches": int(launches),
+        "e2e": {"value": value, "unit": "instance-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "roofline": {"kernel": "k_spmv (BiCGSTAB, full-row FP64)", "bound": "hbm", "achieved": achieved,
+                     "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                     "traffic": None, "algorithmic_bytes_per_step": spmv,
+                     "note": "SpMV bytes only over the whole round (assembly and vector updates not counted)"},
+        "cpu_baseline": cpu,
+        "learned": "not applied: the variable-conductivity operator is non-symmetric (the reference's semantics), "
+                   "and the learned correction runs inside flexible CG on a symmetric operator",
+    }
+    print(json.dumps(line))
+    for pb in problems:
+        pb.close()
+    return 0
+
+
 def run_batch(args, world, rank, local, dist):
     """--workload config5: many nonstationary instances stepped together."""
     import numpy as np
@@ -806,7 +939,8 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["nlgpu", "reference"], default="nlgpu")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["config5"], default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["config4", "config5"], default=DEFAULT_WORKLOAD)
+    ap.add_argument("--instances4", type=int, default=64, help="config4: number of instances")
     ap.add_argument("--instances", type=int, default=256, help="config5: number of instances")
     ap.add_argument("--batch-method", choices=["mixed_illt", "identity_fp64"], default="mixed_illt",
                     help="config5: the per-step solver")
@@ -819,6 +953,17 @@ def main() -> int:
     if args.once:
         return run_once(args)
     world, rank, local, dist = dist_setup()
+    if args.workload == "config4":
+        try:
+            if args.impl == "reference":
+                if rank == 0:
+                    print(json.dumps({"impl": "reference", "unavailable": "the variable-conductivity workload has no "
+                                      "CPU arm here; its line carries a CPU-port sample as cpu_baseline"}))
+                return 0
+            return run_config4(args, world, rank, local, dist)
+        finally:
+            if dist is not None:
+                dist.destroy_process_group()
     if args.workload == "config5":
         try:
             if args.impl == "reference":

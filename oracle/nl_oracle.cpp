@@ -816,6 +816,75 @@ void cg(Problem& p, const Csr& A, const std::vector<double>& b, std::vector<doub
     p.true_residual = std::sqrt(s) / bnorm;
 }
 
+// y = A x over full (non-symmetric) rows
+void full_spmv(const Csr& A, const std::vector<double>& x, std::vector<double>& y) {
+    const i64 n = A.rows;
+    y.assign(size_t(n), 0.0);
+    #pragma omp parallel for schedule(static)
+    for (i64 r = 0; r < n; ++r) {
+        double s = 0.0;
+        for (i64 k = A.rowptr[size_t(r)]; k < A.rowptr[size_t(r) + 1]; ++k) s += A.val[size_t(k)] * x[size_t(A.col[size_t(k)])];
+        y[size_t(r)] = s;
+    }
+}
+
+// Jacobi-preconditioned BiCGSTAB (van der Vorst 1992, right preconditioning by
+// the diagonal, as Eigen's BiCGSTAB with its default diagonal preconditioner)
+// from x = 0 for the reference's non-symmetric systems (a conductivity field
+// with a nonlocal model, stationary_heat_equation_solver_2d.hpp:105-108);
+// restarts with r0^ = r when (r0^, r) vanishes; stops on |b - A x| / |b|.
+void bicgstab(Problem& p, const Csr& A, const std::vector<double>& b, std::vector<double>& x, double tol, long maxit) {
+    const size_t n = size_t(A.rows);
+    auto dot = [n](const std::vector<double>& u, const std::vector<double>& w) {
+        double s = 0.0;
+        for (size_t i = 0; i < n; ++i) s += u[i] * w[i];
+        return s;
+    };
+    std::vector<double> dinv(n, 1.0);
+    for (size_t r = 0; r < n; ++r) {
+        const double* d = const_cast<Csr&>(A).find(i64(r), i64(r));
+        if (d && *d != 0.0) dinv[r] = 1.0 / *d;
+    }
+    x.assign(n, 0.0);
+    const double bnorm = std::sqrt(dot(b, b));
+    p.iterations = 0;
+    if (bnorm == 0.0) { p.residual = p.true_residual = 0.0; return; }
+    std::vector<double> r = b, rhat = b, pv(n, 0.0), v(n, 0.0), y(n), sv(n), z(n), t(n);
+    double rho = 1.0, alpha = 1.0, omega = 1.0;
+    p.residual = 1.0;
+    while (p.iterations < maxit && p.residual > tol) {
+        const double rho_new = dot(rhat, r);
+        if (rho_new == 0.0) {   // breakdown: restart the shadow residual
+            rhat = r;
+            rho = alpha = omega = 1.0;
+            std::fill(pv.begin(), pv.end(), 0.0);
+            std::fill(v.begin(), v.end(), 0.0);
+            continue;
+        }
+        const double beta = (rho_new / rho) * (alpha / omega);
+        rho = rho_new;
+        for (size_t i = 0; i < n; ++i) pv[i] = r[i] + beta * (pv[i] - omega * v[i]);
+        for (size_t i = 0; i < n; ++i) y[i] = dinv[i] * pv[i];
+        full_spmv(A, y, v);
+        alpha = rho / dot(rhat, v);
+        for (size_t i = 0; i < n; ++i) sv[i] = r[i] - alpha * v[i];
+        for (size_t i = 0; i < n; ++i) z[i] = dinv[i] * sv[i];
+        full_spmv(A, z, t);
+        const double tt = dot(t, t);
+        omega = tt > 0.0 ? dot(t, sv) / tt : 0.0;
+        for (size_t i = 0; i < n; ++i) {
+            x[i] += alpha * y[i] + omega * z[i];
+            r[i] = sv[i] - omega * t[i];
+        }
+        ++p.iterations;
+        p.residual = std::sqrt(dot(r, r)) / bnorm;
+    }
+    full_spmv(A, x, t);
+    double s = 0.0;
+    for (size_t i = 0; i < n; ++i) s += (b[i] - t[i]) * (b[i] - t[i]);
+    p.true_residual = std::sqrt(s) / bnorm;
+}
+
 double now() { return omp_get_wtime(); }
 
 } // namespace
@@ -1001,6 +1070,12 @@ int orc_solve(void* h, int variant, double tol, long maxit, int stop_true_residu
     if (pure_neumann(p)) return solve_neumann(p, tol, maxit, stop_true_residual);
     double t0 = now();
     std::vector<double> x;
+    if (!p.symmetric) {   // full storage: BiCGSTAB, as the reference
+        bicgstab(p, p.K_inner, p.rhs, x, tol, maxit);
+        p.timings["cg"] = now() - t0;
+        p.solution = x;
+        return 1;
+    }
     if (variant == 0) {
         const auto Kl = to_eigen(p.K_local);
         Eigen::IncompleteCholesky<double, Eigen::Upper, Eigen::NaturalOrdering<i64>> ilt(Kl);

@@ -162,6 +162,10 @@ def test_nonsymmetric_field_matrices():
     a = gc.csr_to_dense(fx["K_inner_rowptr"], fx["K_inner_col"], fx["K_inner_val"], n, n)
     assert not np.allclose(a, a.T)
     assert np.linalg.norm(a @ fx["temperature"] - fx["rhs"]) <= 1e-12 * np.linalg.norm(fx["rhs"])
+    # the oracle's own BiCGSTAB reaches the reference's solution
+    prob.solve(tol=1e-13, maxit=20000)
+    t = prob.get("solution")
+    assert np.linalg.norm(t - fx["temperature"]) <= 1e-10 * np.linalg.norm(fx["temperature"])
 
 
 def test_known_answers():
