@@ -303,6 +303,19 @@ int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, doub
 /* Only the solve stage on the already assembled system (for timing it alone). */
 int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* temperature,
                           nlgpu_solve_report* report);
+/* The solve stage of many contexts at once, each with its system assembled
+ * (nlgpu_conductivity_matrix_2d(FULL)).  The non-symmetric systems (a
+ * conductivity field with a nonlocal model; the reference solves each with
+ * Jacobi-preconditioned BiCGSTAB, stationary_heat_equation_solver_2d.hpp:105-108)
+ * run as one block-diagonal BiCGSTAB, every instance with its own scalars
+ * and stop test |b - A x| <= tolerance |b|; an instance whose recurrence
+ * breaks down is solved again alone.  Symmetric instances are solved one
+ * after another as by nlgpu_solve_assembled.  temperatures[k]: [n_nodes of
+ * instance k]; reports may be NULL, else [count].  Returns
+ * NLGPU_ERR_NO_CONVERGENCE when an instance did not converge (every output is
+ * still written). */
+int nlgpu_solve_assembled_batch(int64_t count, nlgpu_ctx* const* instances, const nlgpu_solve_options* options,
+                                double* const* temperatures, nlgpu_solve_report* reports);
 
 /* ---- slae::conjugate_gradient on caller matrices (conjugate_gradient.hpp:15-79)
  * A: upper CSR of a symmetric matrix with the diagonal first in each row;

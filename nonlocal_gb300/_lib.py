@@ -130,6 +130,7 @@ SIGNATURES = {
     "nlgpu_get_rhs": (c_int, [c_p, c_p, c_p]),
     "nlgpu_stationary_2d": (c_int, [c_p, ctypes.POINTER(SolveOptions), c_p, ctypes.POINTER(SolveReport)]),
     "nlgpu_solve_assembled": (c_int, [c_p, ctypes.POINTER(SolveOptions), c_p, ctypes.POINTER(SolveReport)]),
+    "nlgpu_solve_assembled_batch": (c_int, [c_i64, c_p, ctypes.POINTER(SolveOptions), c_p, c_p]),
     "nlgpu_cg_solve": (c_int, [c_p, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_d, c_i64, c_p,
                                ctypes.POINTER(SolveReport)]),
     "nlgpu_illt_compute": (c_int, [c_p, c_i64, c_p, c_p, c_p, ctypes.POINTER(c_int)]),

@@ -746,6 +746,50 @@ int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, do
     return rc != NLGPU_OK ? rc : conv_status;
 }
 
+int nlgpu_solve_assembled_batch(int64_t count, nlgpu_ctx* const* instances, const nlgpu_solve_options* options,
+                                double* const* temperatures, nlgpu_solve_report* reports) {
+    if (count < 0 || (count > 0 && (!instances || !temperatures)) || !options) return NLGPU_ERR_ARG;
+    for (int64_t k = 0; k < count; ++k)
+        if (!instances[k] || !temperatures[k]) return NLGPU_ERR_ARG;
+    int conv_status = NLGPU_OK;
+    const int rc = guarded([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<Ctx*> batched;
+        std::vector<int64_t> index;
+        for (int64_t k = 0; k < count; ++k) {
+            Ctx& c = *instances[k];
+            NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "the system must be assembled first");
+            if (!c.symmetric && !has_radiation(c) && !c.neumann) {
+                batched.push_back(&c);
+                index.push_back(k);
+            }
+        }
+        std::vector<CgResult> res;
+        if (!batched.empty()) res = batch_bicgstab(batched, options->tolerance, options->max_iterations);
+        const double batch_seconds = seconds(t0);
+        size_t next = 0;
+        for (int64_t k = 0; k < count; ++k) {
+            Ctx& c = *instances[k];
+            nlgpu_solve_report* rep = reports ? reports + k : nullptr;
+            if (rep) std::memset(rep, 0, sizeof *rep);
+            CgResult r;
+            const auto t1 = std::chrono::steady_clock::now();
+            if (next < index.size() && index[next] == k) {
+                r = res[next++];
+                fill_report(c, rep, r);
+                if (rep) rep->seconds_solve = batch_seconds;
+            } else {
+                r = stationary_solve(c, *options, rep);
+            }
+            c.temperature.download(temperatures[k], size_t(c.n_nodes), c.stream);
+            NL_CUDA(cudaStreamSynchronize(c.stream));
+            if (rep) rep->seconds_total = (rep->seconds_solve > 0.0 ? rep->seconds_solve : 0.0) + seconds(t1);
+            if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
+        }
+    });
+    return rc != NLGPU_OK ? rc : conv_status;
+}
+
 int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* temperature,
                         nlgpu_solve_report* report) {
     if (!ctx || !options || !temperature) return NLGPU_ERR_ARG;
@@ -768,7 +812,8 @@ int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, doub
         t0 = std::chrono::steady_clock::now();
         c.symmetric = !(c.model.nonlocal() && c.cond_field.n);
         build_patterns(c, !c.model.nonlocal(), c.symmetric, c.inner, &c.bound, &c.full, &c.full_from_upper);
-        build_patterns(c, true, true, c.local, nullptr, nullptr, nullptr);
+        // the local matrix feeds the ILLT; the non-symmetric systems' BiCGSTAB uses the diagonal
+        if (c.symmetric) build_patterns(c, true, true, c.local, nullptr, nullptr, nullptr);
         NL_CUDA(cudaStreamSynchronize(c.stream));
         rep->seconds_pattern = seconds(t0);
         t0 = std::chrono::steady_clock::now();
@@ -780,8 +825,10 @@ int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, doub
         assemble_full(c);
         boundary_matrix_terms(c);
         fill_full_from_upper(c, c.inner, c.full, c.full_from_upper);
-        assemble_local(c, c.local, c.model.p1, 0);
-        c.local_ready = true;
+        if (c.symmetric) {
+            assemble_local(c, c.local, c.model.p1, 0);
+            c.local_ready = true;
+        }
         NL_CUDA(cudaStreamSynchronize(c.stream));
         rep->seconds_assembly = seconds(t0);
         t0 = std::chrono::steady_clock::now();

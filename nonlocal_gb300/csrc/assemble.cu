@@ -653,7 +653,7 @@ void dispatch_influence_ff(Ctx& ctx, const AssembleArgs& a, const FFArgs& f, boo
 // p / n and constant conductivity; the rest runs the FP64 kernel
 bool ff_supported(const Ctx& ctx) {
     const Model& m = ctx.model;
-    if (ctx.cond_field.n || m.n < 1) return false;
+    if (m.n < 1) return false;
     if (m.influence == NLGPU_INFLUENCE_FAST_POLYNOMIAL) return true;
     if (m.influence == NLGPU_INFLUENCE_POLYNOMIAL || m.influence == NLGPU_INFLUENCE_EXPONENTIAL)
         return m.p >= 0 && m.p % m.n == 0;

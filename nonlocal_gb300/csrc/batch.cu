@@ -55,6 +55,12 @@ __device__ __forceinline__ void seg_add(double v, int inst, double* acc) {
 }
 
 #define BT_ROWS(i) for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
+// the same rows, but every lane of a warp stays in the loop while any lane has
+// a row (i - lane is the warp's first row): for loops that call seg_add, whose
+// shuffles need the whole warp; lanes past the end pass instance -1
+#define BT_WARP_ROWS(i)                                                                          \
+    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i - i64(threadIdx.x & 31) < n; \
+         i += i64(gridDim.x) * blockDim.x)
 
 // x_D: the instance's Dirichlet value on Dirichlet rows, 0 elsewhere
 __global__ void k_bt_xd(i64 n, const int32_t* __restrict__ inst, const uint8_t* __restrict__ is_inner,
@@ -68,31 +74,49 @@ __global__ void k_bt_axpy(i64 n, const double* __restrict__ a, double* __restric
 
 // y = A x over padded full rows in row blocks: a block holds 32 / g
 // consecutive rows of one instance, each taken by g lanes (g a power of two
-// from the instance's mean row length, so that every lane reads a few int4
-// groups), and the warps take blocks in turn (grid stride).  The instances'
-// rows differ in length by two orders of magnitude (r/h from 2 to 26): a
-// whole warp per short row left most lanes idle and spent a five-step FP64
-// warp reduction per row, which on GB300's two-lane FP64 pipe cost more than
-// the row.  Blocks of stopped instances are skipped.  Optional per-instance
-// partials of x.y: one warp sum per block, kept by lane 0 while its blocks stay
-// in one instance and added with one FP64 atomic when the instance changes.
+// from the instance's mean row length, so that every lane reads about twelve
+// int4 groups), and the warps take blocks in turn (grid stride).  The
+// instances' rows differ in length by two orders of magnitude (r/h from 2 to
+// 26).  On GB300's two-lane FP64 pipe every warp-wide FP64 add costs as much
+// as a warp of FMAs, so the reductions are kept rare: a row's g partial sums
+// meet in log2 g shuffle steps, and the optional per-instance products w.y
+// (w = x when w is null) and y.y (dot2) stay in the lanes' registers while a
+// warp's blocks belong to one instance; one warp sum and one FP64 atomic each
+// when the instance changes (with one FP64 add per row in the loop, the
+// pipe spent more on the sums than on the products).  Blocks of stopped
+// instances (done[k] != 0) are skipped.
 // desc: first row (bits 0-31), log2 g (bits 32-34), rows in the block (35-40).
 __global__ void __launch_bounds__(BT_THREADS) k_bt_spmv(i64 nblocks, const unsigned long long* __restrict__ desc,
                                                         const i64* __restrict__ rp, const int4* __restrict__ col4,
                                                         const double2* __restrict__ val2, const double* __restrict__ x,
                                                         double* __restrict__ y, const int32_t* __restrict__ inst,
-                                                        const double* __restrict__ sc, i64 K, double* __restrict__ dot) {
+                                                        const double* __restrict__ done, double* __restrict__ dot,
+                                                        const double* __restrict__ w, double* __restrict__ dot2) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
-    double acc = 0.0;
+    const double* wv = w ? w : x;
+    double acc = 0.0, acc2 = 0.0;
     int acc_inst = -1;
+    auto flush = [&]() {   // warp-uniform: called by every lane
+        const double a = warp_sum(acc);
+        const double a2 = dot2 ? warp_sum(acc2) : 0.0;
+        if (lane == 0 && acc_inst >= 0) {
+            atomicAdd(dot + acc_inst, a);
+            if (dot2) atomicAdd(dot2 + acc_inst, a2);
+        }
+        acc = acc2 = 0.0;
+    };
     for (i64 bk = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; bk < nblocks; bk += warps) {
         const unsigned long long d = desc[bk];
         const i64 first = i64(d & 0xffffffffull);
         const int lg = int((d >> 32) & 7), cnt = int((d >> 35) & 63);
         const int k = inst[first];
-        if (sc[BS_DONE * K + k] != 0.0) continue;
+        if (done[k] != 0.0) continue;
+        if (dot && k != acc_inst) {
+            flush();
+            acc_inst = k;
+        }
         const int g = 1 << lg, sub = lane & (g - 1), slot = lane >> lg;
         const i64 r = first + slot;
         const bool active = slot < cnt;
@@ -106,30 +130,21 @@ __global__ void __launch_bounds__(BT_THREADS) k_bt_spmv(i64 nblocks, const unsig
             }
         }
         for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(full, s, o);   // within the lane group
-        double contrib = 0.0;
         if (active && sub == 0) {
             y[r] = s;
-            contrib = s * x[r];
-        }
-        if (dot) {
-            contrib = warp_sum(contrib);
-            if (lane == 0) {
-                if (k != acc_inst) {
-                    if (acc_inst >= 0) atomicAdd(dot + acc_inst, acc);
-                    acc = 0.0;
-                    acc_inst = k;
-                }
-                acc += contrib;
+            if (dot) {
+                acc += s * wv[r];
+                acc2 += s * s;
             }
         }
     }
-    if (dot && lane == 0 && acc_inst >= 0) atomicAdd(dot + acc_inst, acc);
+    if (dot) flush();
 }
 
 // per-instance |v|^2 into acc (zeroed by the caller)
 __global__ void __launch_bounds__(BT_THREADS) k_bt_norm2(i64 n, const double* __restrict__ v,
                                                          const int32_t* __restrict__ inst, double* __restrict__ acc) {
-    BT_ROWS(i) seg_add(v[i] * v[i], inst[i], acc);
+    BT_WARP_ROWS(i) seg_add(i < n ? v[i] * v[i] : 0.0, i < n ? inst[i] : -1, acc);
 }
 
 // out = in - B x_D on inner rows, x_D on Dirichlet rows (warp per row of the
@@ -157,11 +172,17 @@ __global__ void k_bt_scale(i64 n, double h, double* __restrict__ v) {
 __global__ void __launch_bounds__(BT_THREADS) k_bt_start(i64 n, const double* __restrict__ b, const double* __restrict__ q,
                                                          double* __restrict__ r, double* __restrict__ p,
                                                          const int32_t* __restrict__ inst, double* __restrict__ sc, i64 K) {
-    BT_ROWS(i) {
-        const double v = b[i] - q[i];
-        r[i] = v; p[i] = v;
-        seg_add(v * v, inst[i], sc + BS_RR0 * K);
-        seg_add(b[i] * b[i], inst[i], sc + BS_BB * K);
+    BT_WARP_ROWS(i) {
+        double v = 0.0, bi = 0.0;
+        int k = -1;
+        if (i < n) {
+            bi = b[i];
+            v = bi - q[i];
+            r[i] = v; p[i] = v;
+            k = inst[i];
+        }
+        seg_add(v * v, k, sc + BS_RR0 * K);
+        seg_add(bi * bi, k, sc + BS_BB * K);
     }
 }
 
@@ -172,11 +193,11 @@ __global__ void __launch_bounds__(BT_THREADS) k_bt_update_xr(i64 n, double* __re
                                                              i64 K, int parity) {
     const double* rr_cur = sc + (parity ? BS_RR1 : BS_RR0) * K;
     double* rr_new = sc + (parity ? BS_RR0 : BS_RR1) * K;
-    BT_ROWS(i) {
-        const int k = inst[i];
+    BT_WARP_ROWS(i) {
+        const int k = i < n ? inst[i] : -1;
         double v2 = 0.0;
         int kk = -1;
-        if (sc[BS_DONE * K + k] == 0.0) {
+        if (k >= 0 && sc[BS_DONE * K + k] == 0.0) {
             const double alpha = rr_cur[k] / sc[BS_PQ * K + k];
             x[i] += alpha * p[i];
             const double v = r[i] - alpha * q[i];
@@ -298,8 +319,8 @@ void concat(Batch& bt, Csr& out, Sel sel, bool with_inst) {
 }
 
 // row blocks of a concatenated matrix for k_bt_spmv: per instance g lanes per
-// row, g the smallest power of two (2 .. 32) with g * 12 >= the mean padded
-// row length (about three int4 groups per lane)
+// row, g the smallest power of two (1 .. 32) with g * 48 >= the mean padded
+// row length (about twelve int4 groups per lane)
 void row_blocks(Batch& bt, const Csr& M, dbuf<unsigned long long>& out, i64& count) {
     std::vector<i64> rp(size_t(bt.N + 1));
     M.rowptr.download(rp.data(), rp.size(), bt.stream);
@@ -309,8 +330,8 @@ void row_blocks(Batch& bt, const Csr& M, dbuf<unsigned long long>& out, i64& cou
         const i64 r0 = bt.row_off[size_t(k)], r1 = bt.row_off[size_t(k) + 1];
         if (r1 <= r0) continue;
         const double mean = double(rp[size_t(r1)] - rp[size_t(r0)]) / double(r1 - r0);
-        int lg = 1;
-        while (lg < 5 && double(1 << lg) * 12.0 < mean) ++lg;
+        int lg = 0;
+        while (lg < 5 && double(1 << lg) * 48.0 < mean) ++lg;
         const i64 per = 32 >> lg;
         for (i64 r = r0; r < r1; r += per)
             desc.push_back((unsigned long long)r | ((unsigned long long)lg << 32) |
@@ -329,7 +350,8 @@ void bt_spmv(Batch& bt, const Csr& M, const double* x, double* y, double* dot, b
     NL_LAUNCH(k_bt_spmv, grid_for(nb * 32, BT_THREADS, 152 * 8), BT_THREADS, 0, bt.stream, nb,
               (is_a ? bt.blocks_A : bt.blocks_C).p, M.rowptr.p, reinterpret_cast<const int4*>(M.col.p),
               reinterpret_cast<const double2*>(M.val.p), x, y, bt.inst_of_row.p,
-              skip_done ? bt.sc.p : bt.sc.p + bt.K * BS_COUNT, bt.K, dot);
+              (skip_done ? bt.sc.p : bt.sc.p + bt.K * BS_COUNT) + BS_DONE * bt.K, dot, static_cast<const double*>(nullptr),
+              static_cast<double*>(nullptr));
 }
 
 }  // namespace
@@ -494,7 +516,7 @@ i64 batch_step(Batch& bt, const double* dirichlet_values, double tolerance, i64 
     if (!bt.chunk || bt.chunk_tol2 != tol2 || bt.chunk_cap != cap) {
         if (bt.chunk) { cudaGraphExecDestroy(bt.chunk); bt.chunk = nullptr; }
         cudaGraph_t g = nullptr;
-        const i64 before = g_launches.load();
+        CountCaptured counted;
         NL_CUDA(cudaStreamBeginCapture(bt.stream, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < BT_ITERS; ++it) {
             const int parity = it & 1;
@@ -506,8 +528,7 @@ i64 batch_step(Batch& bt, const double* dirichlet_values, double tolerance, i64 
             NL_LAUNCH(k_bt_check, 1, 256, 0, bt.stream, K, sc, parity, tol2, cap, bt.running.p);
         }
         NL_CUDA(cudaStreamEndCapture(bt.stream, &g));
-        bt.chunk_kernels = int(g_launches.load() - before);
-        g_launches.fetch_sub(bt.chunk_kernels);   // counted when the graph is launched
+        bt.chunk_kernels = int(counted.kernels);   // counted when the graph is launched
         const cudaError_t e = cudaGraphInstantiate(&bt.chunk, g, 0);
         cudaGraphDestroy(g);
         NL_CUDA(e);
@@ -549,6 +570,315 @@ void batch_sizes(const Batch& bt, i64* rows, i64* system_entries) {
         rows[k] = bt.row_off[k + 1] - bt.row_off[k];
         system_entries[k] = bt.inst[k]->full.nnz;
     }
+}
+
+// ------------------------------------------------------------ stationary batch
+// The stationary solves of many assembled non-symmetric systems (variable
+// conductivity with a nonlocal model) at once.  The reference solves each with
+// Eigen's BiCGSTAB and its diagonal preconditioner
+// (stationary_heat_equation_solver_2d.hpp:105-108); here the instances' full
+// matrices are concatenated into one block-diagonal system and every
+// instance runs the right-preconditioned BiCGSTAB of the single-system solver
+// (van der Vorst 1992) with its own scalars, from x0 = 0:
+//   beta = (rho / rho_old)(alpha / omega);  p = r + beta (p - omega v);  y = D^-1 p
+//   v = A y                      (one SpMV over all rows; r0.v per instance)
+//   alpha = rho / r0.v;  s = r - alpha v;  z = D^-1 s
+//   t = A z                      (one SpMV; t.s and t.t per instance)
+//   omega = t.s / t.t;  x += alpha y + omega z;  r = s - omega t   (|r|^2, r0.r)
+// Six launches an iteration for all instances, captured as CUDA-graph chunks;
+// a stopped instance's rows are skipped.  An instance stops when its
+// recurrence residual meets the tolerance, at the iteration cap, or when the
+// recurrence breaks down (rho or omega vanishing, a non-finite scalar); then
+// the true residuals decide, and the instances that miss the tolerance start
+// again from their x with r0 = b - A x (at most 16 rounds), as the
+// single-system solver does.
+
+namespace {
+
+constexpr int BB_ITERS = 16;   // iterations per captured chunk (even)
+constexpr int BB_ROUNDS = 16;  // starts from the true residual
+// per-instance scalars (double [K] each); RHO0 / RHO1 alternate with the parity;
+// FIN marks an instance whose true residual met the tolerance (or the cap)
+enum { BB_BB = 0, BB_RHO0, BB_RHO1, BB_R0V, BB_TS, BB_TT, BB_RR, BB_ALPHA, BB_OMEGA, BB_DONE, BB_ITERS_S, BB_FIN,
+       BB_COUNT };
+
+// r = r0 = b - q (q = A x); p = v = 0; r0.r per instance into RHO0 (zeroed
+// by the caller), and |b|^2 into BB on the first start
+__global__ void __launch_bounds__(BT_THREADS) k_bb_start(i64 n, const double* __restrict__ b, const double* __restrict__ q,
+                                                         double* __restrict__ r, double* __restrict__ r0,
+                                                         double* __restrict__ p, double* __restrict__ v,
+                                                         const int32_t* __restrict__ inst, double* __restrict__ sc, i64 K,
+                                                         int first) {
+    BT_WARP_ROWS(i) {
+        double bi = 0.0, ri = 0.0;
+        int k = -1;
+        if (i < n) {
+            bi = b[i];
+            ri = bi - q[i];
+            r[i] = ri; r0[i] = ri; p[i] = 0.0; v[i] = 0.0;
+            k = inst[i];
+        }
+        seg_add(ri * ri, k, sc + BB_RHO0 * K);
+        if (first) seg_add(bi * bi, k, sc + BB_BB * K);
+    }
+}
+
+// the scalars of a start: rho = r0.r, |r|^2 = rho, rho_old = alpha = omega = 1;
+// the instances marked final stay stopped (on the first start: b = 0)
+__global__ void k_bb_first(i64 K, double* __restrict__ sc, int first) {
+    for (i64 k = threadIdx.x; k < K; k += blockDim.x) {
+        if (first) {
+            sc[BB_ITERS_S * K + k] = 0.0;
+            sc[BB_FIN * K + k] = sc[BB_BB * K + k] == 0.0 ? 1.0 : 0.0;
+        }
+        sc[BB_RR * K + k] = sc[BB_RHO0 * K + k];
+        sc[BB_RHO1 * K + k] = 1.0;
+        sc[BB_ALPHA * K + k] = 1.0;
+        sc[BB_OMEGA * K + k] = 1.0;
+        sc[BB_R0V * K + k] = 0.0;
+        sc[BB_TS * K + k] = 0.0;
+        sc[BB_TT * K + k] = 0.0;
+        sc[BB_DONE * K + k] = sc[BB_FIN * K + k];
+    }
+}
+
+// dinv = 1 / diagonal (1 where it is zero) of the concatenated full rows
+__global__ void k_bb_jacobi(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col,
+                            const double* __restrict__ val, double* __restrict__ dinv) {
+    BT_ROWS(r) {
+        double d = 0.0;
+        for (i64 k = rp[r]; k < rp[r + 1]; ++k)
+            if (col[k] == int32_t(r)) d += val[k];
+        dinv[r] = d != 0.0 ? 1.0 / d : 1.0;
+    }
+}
+
+// p = r + beta (p - omega v); y = dinv p
+__global__ void k_bb_p(i64 n, const double* __restrict__ r, double* __restrict__ p, const double* __restrict__ v,
+                       const double* __restrict__ dinv, double* __restrict__ y, const int32_t* __restrict__ inst,
+                       const double* __restrict__ sc, i64 K, int q) {
+    const double* rho = sc + (q ? BB_RHO1 : BB_RHO0) * K;
+    const double* rho_old = sc + (q ? BB_RHO0 : BB_RHO1) * K;
+    BT_ROWS(i) {
+        const int k = inst[i];
+        if (sc[BB_DONE * K + k] != 0.0) continue;
+        const double w = sc[BB_OMEGA * K + k];
+        const double beta = (rho[k] / rho_old[k]) * (sc[BB_ALPHA * K + k] / w);
+        const double pi = r[i] + beta * (p[i] - w * v[i]);
+        p[i] = pi;
+        y[i] = dinv[i] * pi;
+    }
+}
+
+// alpha = rho / r0.v; s = r - alpha v; z = dinv s.  Block 0 clears the
+// accumulators the x / r update adds into (nothing reads them here).
+__global__ void k_bb_s(i64 n, const double* __restrict__ r, const double* __restrict__ v, const double* __restrict__ dinv,
+                       double* __restrict__ s, double* __restrict__ z, const int32_t* __restrict__ inst,
+                       double* __restrict__ sc, i64 K, int q) {
+    const double* rho = sc + (q ? BB_RHO1 : BB_RHO0) * K;
+    BT_ROWS(i) {
+        const int k = inst[i];
+        if (sc[BB_DONE * K + k] != 0.0) continue;
+        const double alpha = rho[k] / sc[BB_R0V * K + k];
+        const double si = r[i] - alpha * v[i];
+        s[i] = si;
+        z[i] = dinv[i] * si;
+    }
+    if (blockIdx.x == 0)
+        for (i64 k = threadIdx.x; k < K; k += blockDim.x) {
+            sc[(q ? BB_RHO0 : BB_RHO1) * K + k] = 0.0;
+            sc[BB_RR * K + k] = 0.0;
+        }
+}
+
+// omega = t.s / t.t; x += alpha y + omega z; r = s - omega t; |r|^2 and r0.r per instance
+__global__ void __launch_bounds__(BT_THREADS) k_bb_xr(i64 n, double* __restrict__ x, const double* __restrict__ y,
+                                                      const double* __restrict__ z, const double* __restrict__ s,
+                                                      const double* __restrict__ t, double* __restrict__ r,
+                                                      const double* __restrict__ r0, const int32_t* __restrict__ inst,
+                                                      double* __restrict__ sc, i64 K, int q) {
+    const double* rho = sc + (q ? BB_RHO1 : BB_RHO0) * K;
+    double* rho_new = sc + (q ? BB_RHO0 : BB_RHO1) * K;
+    BT_WARP_ROWS(i) {
+        const int k = i < n ? inst[i] : -1;
+        double rr = 0.0, r0r = 0.0;
+        int kk = -1;
+        if (k >= 0 && sc[BB_DONE * K + k] == 0.0) {
+            const double alpha = rho[k] / sc[BB_R0V * K + k];
+            const double tt = sc[BB_TT * K + k];
+            const double omega = tt > 0.0 ? sc[BB_TS * K + k] / tt : 0.0;
+            x[i] += alpha * y[i] + omega * z[i];
+            const double ri = s[i] - omega * t[i];
+            r[i] = ri;
+            rr = ri * ri;
+            r0r = r0[i] * ri;
+            kk = k;
+        }
+        seg_add(rr, kk, sc + BB_RR * K);
+        seg_add(r0r, kk, rho_new);
+    }
+}
+
+// per instance: keep alpha and omega, count the iteration, stop on
+// |r| <= tol |b|, the cap or a breakdown; clear the SpMV accumulators and
+// count the running instances
+__global__ void k_bb_check(i64 K, double* __restrict__ sc, int q, double tol2, double max_iterations,
+                           int* __restrict__ running) {
+    __shared__ int cnt;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    for (i64 k = threadIdx.x; k < K; k += blockDim.x) {
+        if (sc[BB_DONE * K + k] == 0.0) {
+            const double rho_new = sc[(q ? BB_RHO0 : BB_RHO1) * K + k];
+            const double alpha = sc[(q ? BB_RHO1 : BB_RHO0) * K + k] / sc[BB_R0V * K + k];
+            const double tt = sc[BB_TT * K + k];
+            const double omega = tt > 0.0 ? sc[BB_TS * K + k] / tt : 0.0;
+            const double rr = sc[BB_RR * K + k], bb = sc[BB_BB * K + k];
+            sc[BB_ALPHA * K + k] = alpha;
+            sc[BB_OMEGA * K + k] = omega;
+            sc[BB_ITERS_S * K + k] += 1.0;
+            const bool broke = !isfinite(alpha) || !isfinite(omega) || omega == 0.0 || !isfinite(rr) ||
+                               !(fabs(rho_new) >= 1e-30 * bb);
+            if (rr <= tol2 * bb || broke || sc[BB_ITERS_S * K + k] >= max_iterations) sc[BB_DONE * K + k] = 1.0;
+            else atomicAdd(&cnt, 1);
+        }
+        sc[BB_R0V * K + k] = 0.0;
+        sc[BB_TS * K + k] = 0.0;
+        sc[BB_TT * K + k] = 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) running[BT_RUN_SLOT] = cnt;
+}
+
+// per instance |b - q|^2 into acc (zeroed by the caller)
+__global__ void __launch_bounds__(BT_THREADS) k_bb_residual(i64 n, const double* __restrict__ b, const double* __restrict__ q,
+                                                            const int32_t* __restrict__ inst, double* __restrict__ acc) {
+    BT_WARP_ROWS(i) {
+        const double d = i < n ? b[i] - q[i] : 0.0;
+        seg_add(d * d, i < n ? inst[i] : -1, acc);
+    }
+}
+
+}  // namespace
+
+std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double tolerance, i64 max_iterations) {
+    Batch bt;
+    NL_CUDA(cudaStreamCreateWithFlags(&bt.stream, cudaStreamNonBlocking));
+    struct StreamGuard {
+        Batch& b;
+        ~StreamGuard() {
+            if (b.chunk) cudaGraphExecDestroy(b.chunk);
+            cudaStreamSynchronize(b.stream);
+            cudaStreamDestroy(b.stream);
+        }
+    } guard{bt};
+    bt.inst = instances;
+    bt.K = i64(instances.size());
+    bt.row_off.assign(size_t(bt.K + 1), 0);
+    for (i64 k = 0; k < bt.K; ++k) {
+        Ctx& c = *instances[size_t(k)];
+        NL_REQUIRE(c.inner_ready && !c.symmetric && c.full.rows == c.n_nodes, NLGPU_ERR_STATE,
+                   "every instance needs its assembled non-symmetric system");
+        NL_CUDA(cudaStreamSynchronize(c.stream));
+        bt.row_off[size_t(k) + 1] = bt.row_off[size_t(k)] + c.n_nodes;
+    }
+    const i64 N = bt.row_off.back(), K = bt.K;
+    bt.N = N;
+    NL_REQUIRE(N < (i64(1) << 31), NLGPU_ERR_UNSUPPORTED, "more than 2^31 rows in one batch");
+    bt.inst_of_row.resize(size_t(N));
+    concat(bt, bt.A, [](Ctx& c) -> const Csr& { return c.full; }, true);
+    row_blocks(bt, bt.A, bt.blocks_A, bt.nblocks_A);
+    dbuf<double> r0, v, s, t, y, z, dinv, acc;
+    for (auto* b : {&bt.x, &bt.b, &bt.r, &bt.p, &r0, &v, &s, &t, &y, &z, &dinv}) b->resize(size_t(N));
+    for (i64 k = 0; k < K; ++k) {
+        Ctx& c = *instances[size_t(k)];
+        NL_CUDA(cudaMemcpyAsync(bt.b.p + bt.row_off[size_t(k)], c.rhs.p, size_t(c.n_nodes) * sizeof(double),
+                                cudaMemcpyDeviceToDevice, bt.stream));
+    }
+    bt.sc.resize(size_t(K) * BB_COUNT);
+    bt.sc.zero(bt.stream);
+    bt.running.resize(1);
+    acc.resize(size_t(K));
+    double* sc = bt.sc.p;
+    const double tol2 = tolerance * tolerance;
+    const double cap = double(std::min<i64>(max_iterations, i64(1) << 40));
+    NL_LAUNCH(k_bb_jacobi, grid_for(N, 256), 256, 0, bt.stream, N, bt.A.rowptr.p, bt.A.col.p, bt.A.val.p, dinv.p);
+    NL_CUDA(cudaMemsetAsync(bt.x.p, 0, size_t(N) * sizeof(double), bt.stream));
+    NL_CUDA(cudaMemsetAsync(t.p, 0, size_t(N) * sizeof(double), bt.stream));   // A x for x = 0
+    auto spmv = [&](const double* in, double* out, double* dot, const double* w, double* dot2) {
+        NL_LAUNCH(k_bt_spmv, grid_for(bt.nblocks_A * 32, BT_THREADS, 152 * 8), BT_THREADS, 0, bt.stream, bt.nblocks_A,
+                  bt.blocks_A.p, bt.A.rowptr.p, reinterpret_cast<const int4*>(bt.A.col.p),
+                  reinterpret_cast<const double2*>(bt.A.val.p), in, out, bt.inst_of_row.p, sc + BB_DONE * K, dot, w,
+                  dot2);
+    };
+    std::vector<double> h(size_t(K) * BB_COUNT), res2(static_cast<size_t>(K)), fin(static_cast<size_t>(K));
+    std::vector<CgResult> out(static_cast<size_t>(K));
+    for (int round = 0; round < BB_ROUNDS; ++round) {
+        const int first = round == 0 ? 1 : 0;
+        NL_CUDA(cudaMemsetAsync(sc + BB_RHO0 * K, 0, size_t(K) * sizeof(double), bt.stream));
+        NL_LAUNCH(k_bb_start, RED_BLOCKS, BT_THREADS, 0, bt.stream, N, bt.b.p, t.p, bt.r.p, r0.p, bt.p.p, v.p,
+                  bt.inst_of_row.p, sc, K, first);
+        NL_LAUNCH(k_bb_first, 1, 256, 0, bt.stream, K, sc, first);
+        if (!bt.chunk) {
+            cudaGraph_t g = nullptr;
+            CountCaptured counted;
+            NL_CUDA(cudaStreamBeginCapture(bt.stream, cudaStreamCaptureModeThreadLocal));
+            for (int it = 0; it < BB_ITERS; ++it) {
+                const int q = it & 1;
+                NL_LAUNCH(k_bb_p, grid_for(N, 256, RED_BLOCKS * 4), 256, 0, bt.stream, N, bt.r.p, bt.p.p, v.p, dinv.p,
+                          y.p, bt.inst_of_row.p, sc, K, q);
+                spmv(y.p, v.p, sc + BB_R0V * K, r0.p, static_cast<double*>(nullptr));
+                NL_LAUNCH(k_bb_s, grid_for(N, 256, RED_BLOCKS * 4), 256, 0, bt.stream, N, bt.r.p, v.p, dinv.p, s.p, z.p,
+                          bt.inst_of_row.p, sc, K, q);
+                spmv(z.p, t.p, sc + BB_TS * K, s.p, sc + BB_TT * K);
+                NL_LAUNCH(k_bb_xr, RED_BLOCKS, BT_THREADS, 0, bt.stream, N, bt.x.p, y.p, z.p, s.p, t.p, bt.r.p, r0.p,
+                          bt.inst_of_row.p, sc, K, q);
+                NL_LAUNCH(k_bb_check, 1, 256, 0, bt.stream, K, sc, q, tol2, cap, bt.running.p);
+            }
+            NL_CUDA(cudaStreamEndCapture(bt.stream, &g));
+            bt.chunk_kernels = int(counted.kernels);   // counted when the graph is launched
+            const cudaError_t e = cudaGraphInstantiate(&bt.chunk, g, 0);
+            cudaGraphDestroy(g);
+            NL_CUDA(e);
+        }
+        for (i64 chunks = 1;; ++chunks) {
+            NL_CUDA(cudaGraphLaunch(bt.chunk, bt.stream));
+            g_launches.fetch_add(bt.chunk_kernels);
+            int running = 0;
+            NL_CUDA(cudaMemcpyAsync(&running, bt.running.p, sizeof running, cudaMemcpyDeviceToHost, bt.stream));
+            NL_CUDA(cudaStreamSynchronize(bt.stream));
+            if (running == 0 || double(chunks * BB_ITERS) >= cap + BB_ITERS) break;
+        }
+        // the true residual of every instance decides (t = A x over every row)
+        acc.zero(bt.stream);
+        NL_CUDA(cudaMemsetAsync(sc + BB_DONE * K, 0, size_t(K) * sizeof(double), bt.stream));
+        spmv(bt.x.p, t.p, nullptr, nullptr, nullptr);
+        NL_LAUNCH(k_bb_residual, RED_BLOCKS, BT_THREADS, 0, bt.stream, N, bt.b.p, t.p, bt.inst_of_row.p, acc.p);
+        NL_CUDA(cudaMemcpyAsync(h.data(), sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost, bt.stream));
+        NL_CUDA(cudaMemcpyAsync(res2.data(), acc.p, res2.size() * sizeof(double), cudaMemcpyDeviceToHost, bt.stream));
+        NL_CUDA(cudaStreamSynchronize(bt.stream));
+        bool all = true;
+        for (i64 k = 0; k < K; ++k) {
+            CgResult& r = out[size_t(k)];
+            const double bb = h[size_t(BB_BB * K + k)];
+            r.iterations = i64(h[size_t(BB_ITERS_S * K + k)]);
+            r.residual = bb > 0.0 ? std::sqrt(res2[size_t(k)] / bb) : 0.0;
+            r.converged = r.residual <= tolerance;
+            const bool final = r.converged || r.iterations >= max_iterations || !std::isfinite(r.residual);
+            fin[size_t(k)] = final ? 1.0 : 0.0;
+            all = all && final;
+        }
+        if (all) break;
+        NL_CUDA(cudaMemcpyAsync(sc + BB_FIN * K, fin.data(), size_t(K) * sizeof(double), cudaMemcpyHostToDevice, bt.stream));
+    }
+    for (i64 k = 0; k < K; ++k) {
+        Ctx& c = *instances[size_t(k)];
+        c.temperature.resize(size_t(c.n_nodes));
+        NL_CUDA(cudaMemcpyAsync(c.temperature.p, bt.x.p + bt.row_off[size_t(k)], size_t(c.n_nodes) * sizeof(double),
+                                cudaMemcpyDeviceToDevice, bt.stream));
+    }
+    NL_CUDA(cudaStreamSynchronize(bt.stream));
+    return out;
 }
 
 }  // namespace nlgpu

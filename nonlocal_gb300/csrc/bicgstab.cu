@@ -10,7 +10,10 @@
 // device in slots alternating with the iteration parity (a kernel never
 // overwrites a scalar that other blocks of the same kernel still read); every
 // reduction writes one partial per block, re-summed in a fixed order by the
-// consumers.  The host checks the done flag every BI_ITERS iterations and
+// consumers, so every iteration launches the same kernels with the same
+// arguments: BI_ITERS iterations are captured once per solve and replayed as
+// one CUDA graph (eight launches an iteration made small systems
+// launch-bound).  The host checks the done flag every BI_ITERS iterations and
 // restarts from the true residual when the shadow residual becomes orthogonal
 // to the residual (rho ~ 0), as the documented Eigen solver does.
 #include "common.cuh"
@@ -38,9 +41,11 @@ __device__ __forceinline__ double bi_block_sum(double v, double* sh) {
     return s;
 }
 
-__device__ __forceinline__ double bi_partials(const double* part, double* sh) {
+// sum of the partials of a reduction made by a launch of gridDim.x blocks
+// (every reducing kernel of one solve runs with the same grid)
+__device__ __forceinline__ double bi_partials(const double* part, double* sh, int nb) {
     double v = 0.0;
-    for (int k = threadIdx.x; k < RED_BLOCKS; k += blockDim.x) v += part[k];
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) v += part[k];
     v = bi_block_sum(v, sh);
     if (threadIdx.x == 0) sh[32] = v;
     __syncthreads();
@@ -84,7 +89,7 @@ __global__ void __launch_bounds__(BI_THREADS) k_bi_rho(i64 n, const double* __re
                                                        double max_iterations) {
     __shared__ double sh[40];
     if (sc[SB_DONE] != 0.0) return;
-    const double rr = bi_partials(part + B_RR * RED_BLOCKS, sh);
+    const double rr = bi_partials(part + B_RR * RED_BLOCKS, sh, gridDim.x);
     if (rr <= tol2 * sc[SB_BB] || sc[SB_ITERS] >= max_iterations || !(rr == rr)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) { sc[SB_DONE] = 1.0; sc[SB_RR] = rr; }
         return;
@@ -103,7 +108,7 @@ __global__ void __launch_bounds__(BI_THREADS) k_bi_p(i64 n, const double* __rest
     __shared__ double sh[40];
     if (sc[SB_DONE] != 0.0) return;
     const int o = q ^ 1;
-    const double rho = bi_partials(part + B_RHO * RED_BLOCKS, sh);
+    const double rho = bi_partials(part + B_RHO * RED_BLOCKS, sh, gridDim.x);
     const double beta = (rho / sc[SB_RHO + o]) * (sc[SB_ALPHA + o] / sc[SB_OMEGA + o]);
     const double w = sc[SB_OMEGA + o];
     BI_LOOP(i) {
@@ -132,7 +137,7 @@ __global__ void __launch_bounds__(BI_THREADS) k_bi_s(i64 n, const double* __rest
                                                      double* __restrict__ sc, int q) {
     __shared__ double sh[40];
     if (sc[SB_DONE] != 0.0) return;
-    const double alpha = sc[SB_RHO + q] / bi_partials(part + B_R0V * RED_BLOCKS, sh);
+    const double alpha = sc[SB_RHO + q] / bi_partials(part + B_R0V * RED_BLOCKS, sh, gridDim.x);
     BI_LOOP(i) {
         const double si = r[i] - alpha * v[i];
         s[i] = si;
@@ -159,7 +164,8 @@ __global__ void __launch_bounds__(BI_THREADS) k_bi_x(i64 n, double* __restrict__
                                                      double* __restrict__ part, double* __restrict__ sc, int q) {
     __shared__ double sh[40];
     if (sc[SB_DONE] != 0.0) return;
-    const double ts = bi_partials(part + B_TS * RED_BLOCKS, sh), tt = bi_partials(part + B_TT * RED_BLOCKS, sh);
+    const double ts = bi_partials(part + B_TS * RED_BLOCKS, sh, gridDim.x);
+    const double tt = bi_partials(part + B_TT * RED_BLOCKS, sh, gridDim.x);
     const double omega = tt > 0.0 ? ts / tt : 0.0;
     const double alpha = sc[SB_ALPHA + q];
     double acc = 0.0;
@@ -174,9 +180,9 @@ __global__ void __launch_bounds__(BI_THREADS) k_bi_x(i64 n, double* __restrict__
     if (blockIdx.x == 0 && threadIdx.x == 0) { sc[SB_OMEGA + q] = omega; sc[SB_ITERS] += 1.0; }
 }
 
-__global__ void __launch_bounds__(BI_THREADS) k_bi_sum(const double* __restrict__ part, double* __restrict__ dst) {
+__global__ void __launch_bounds__(BI_THREADS) k_bi_sum(const double* __restrict__ part, int nb, double* __restrict__ dst) {
     __shared__ double sh[40];
-    const double s = bi_partials(part, sh);
+    const double s = bi_partials(part, sh, nb);
     if (threadIdx.x == 0) *dst = s;
 }
 
@@ -190,15 +196,64 @@ CgResult bicgstab_solve(Ctx& ctx, const Csr& A, const double* b, double* x, doub
     w.sc.reserve(SB_COUNT);
     double* part = w.part.p;
     double* sc = w.sc.p;
-    const unsigned G = RED_BLOCKS;
+    // one block per 256 rows up to RED_BLOCKS: small systems leave the GPU to
+    // the solves of other contexts on other streams
+    const unsigned G = unsigned(std::min<i64>(RED_BLOCKS, std::max<i64>(1, (n + BI_THREADS - 1) / BI_THREADS)));
     NL_LAUNCH(k_bi_jacobi, grid_for(n, 256), 256, 0, ctx.stream, n, A.rowptr.p, A.col.p, A.val.p, w.dinv.p);
     NL_CUDA(cudaMemsetAsync(x, 0, size_t(n) * sizeof(double), ctx.stream));
     NL_CUDA(cudaMemsetAsync(sc, 0, SB_COUNT * sizeof(double), ctx.stream));
     NL_LAUNCH(k_bi_dot, G, BI_THREADS, 0, ctx.stream, n, b, b, part + B_RR * RED_BLOCKS, sc);
-    NL_LAUNCH(k_bi_sum, 1, BI_THREADS, 0, ctx.stream, part + B_RR * RED_BLOCKS, sc + SB_BB);
+    NL_LAUNCH(k_bi_sum, 1, BI_THREADS, 0, ctx.stream, part + B_RR * RED_BLOCKS, int(G), sc + SB_BB);
     const double tol2 = tolerance * tolerance;
     const double cap = double(std::min<i64>(max_iterations, i64(1) << 40));
     CgResult res;
+    auto chunk = [&] {
+        for (int it = 0; it < BI_ITERS; ++it) {
+            const int q = it & 1;
+            NL_LAUNCH(k_bi_rho, G, BI_THREADS, 0, ctx.stream, n, w.r0.p, w.r.p, part, sc, tol2, cap);
+            NL_LAUNCH(k_bi_p, G, BI_THREADS, 0, ctx.stream, n, w.r.p, w.p.p, w.v.p, w.dinv.p, w.y.p, part, sc, q);
+            spmv_full(ctx, A, w.y.p, w.v.p);
+            NL_LAUNCH(k_bi_dot, G, BI_THREADS, 0, ctx.stream, n, w.r0.p, w.v.p, part + B_R0V * RED_BLOCKS, sc);
+            NL_LAUNCH(k_bi_s, G, BI_THREADS, 0, ctx.stream, n, w.r.p, w.v.p, w.dinv.p, w.s.p, w.z.p, part, sc, q);
+            spmv_full(ctx, A, w.z.p, w.t.p);
+            NL_LAUNCH(k_bi_ts, G, BI_THREADS, 0, ctx.stream, n, w.t.p, w.s.p, part, sc);
+            NL_LAUNCH(k_bi_x, G, BI_THREADS, 0, ctx.stream, n, x, w.y.p, w.z.p, w.s.p, w.t.p, w.r.p, part, sc, q);
+        }
+    };
+    bool eager_done = false, captured = false;
+    auto run_chunk = [&] {
+        if (!eager_done) {   // the first chunk runs eagerly (the SpMV's lazy set-up happens outside a capture)
+            chunk();
+            eager_done = true;
+            return;
+        }
+        if (!captured) {
+            cudaGraph_t g = nullptr;
+            {
+                CountCaptured counted;
+                NL_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+                chunk();
+                NL_CUDA(cudaStreamEndCapture(ctx.stream, &g));
+                w.chunk_kernels = int(counted.kernels);   // counted when the graph is launched
+            }
+            cudaError_t e = cudaErrorGraphExecUpdateFailure;
+            if (w.chunk) {
+                cudaGraphExecUpdateResultInfo info;
+                e = cudaGraphExecUpdate(w.chunk, g, &info);
+                if (e != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    cudaGraphExecDestroy(w.chunk);
+                    w.chunk = nullptr;
+                }
+            }
+            if (e != cudaSuccess) e = cudaGraphInstantiate(&w.chunk, g, 0);
+            cudaGraphDestroy(g);
+            NL_CUDA(e);
+            captured = true;
+        }
+        NL_CUDA(cudaGraphLaunch(w.chunk, ctx.stream));
+        g_launches.fetch_add(w.chunk_kernels);
+    };
     for (int restart = 0; restart < 16; ++restart) {
         // r = r0 = b - A x, p = v = 0, rho_old = alpha = omega = 1 (the slots iteration 0 reads)
         spmv_full(ctx, A, x, w.t.p);
@@ -209,19 +264,8 @@ CgResult bicgstab_solve(Ctx& ctx, const Csr& A, const double* b, double* x, doub
         NL_CUDA(cudaMemcpyAsync(sc + SB_OMEGA + 1, &ones[2], sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
         NL_CUDA(cudaMemsetAsync(sc + SB_DONE, 0, sizeof(double), ctx.stream));
         double h[SB_COUNT];
-        bool breakdown = false;
         for (;;) {
-            for (int it = 0; it < BI_ITERS; ++it) {
-                const int q = it & 1;
-                NL_LAUNCH(k_bi_rho, G, BI_THREADS, 0, ctx.stream, n, w.r0.p, w.r.p, part, sc, tol2, cap);
-                NL_LAUNCH(k_bi_p, G, BI_THREADS, 0, ctx.stream, n, w.r.p, w.p.p, w.v.p, w.dinv.p, w.y.p, part, sc, q);
-                spmv_full(ctx, A, w.y.p, w.v.p);
-                NL_LAUNCH(k_bi_dot, G, BI_THREADS, 0, ctx.stream, n, w.r0.p, w.v.p, part + B_R0V * RED_BLOCKS, sc);
-                NL_LAUNCH(k_bi_s, G, BI_THREADS, 0, ctx.stream, n, w.r.p, w.v.p, w.dinv.p, w.s.p, w.z.p, part, sc, q);
-                spmv_full(ctx, A, w.z.p, w.t.p);
-                NL_LAUNCH(k_bi_ts, G, BI_THREADS, 0, ctx.stream, n, w.t.p, w.s.p, part, sc);
-                NL_LAUNCH(k_bi_x, G, BI_THREADS, 0, ctx.stream, n, x, w.y.p, w.z.p, w.s.p, w.t.p, w.r.p, part, sc, q);
-            }
+            run_chunk();
             NL_CUDA(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
             NL_CUDA(cudaStreamSynchronize(ctx.stream));
             res.iterations = i64(h[SB_ITERS]);
@@ -229,18 +273,18 @@ CgResult bicgstab_solve(Ctx& ctx, const Csr& A, const double* b, double* x, doub
             // shadow residual orthogonal to the residual, or a non-finite scalar: restart
             const double rho = h[SB_RHO + 1], rr_b = h[SB_BB];
             if (!std::isfinite(h[SB_ALPHA]) || !std::isfinite(h[SB_ALPHA + 1]) || !std::isfinite(h[SB_OMEGA + 1]) ||
-                std::fabs(rho) < 1e-30 * rr_b) { breakdown = true; break; }
+                std::fabs(rho) < 1e-30 * rr_b)
+                break;
         }
         // the true residual decides
         spmv_full(ctx, A, x, w.t.p);
         NL_LAUNCH(k_bi_start, G, BI_THREADS, 0, ctx.stream, n, b, w.t.p, w.s.p, w.z.p, w.y.p, w.y.p, part);
-        NL_LAUNCH(k_bi_sum, 1, BI_THREADS, 0, ctx.stream, part + B_RR * RED_BLOCKS, sc + SB_RR);
+        NL_LAUNCH(k_bi_sum, 1, BI_THREADS, 0, ctx.stream, part + B_RR * RED_BLOCKS, int(G), sc + SB_RR);
         NL_CUDA(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
         NL_CUDA(cudaStreamSynchronize(ctx.stream));
         res.residual = h[SB_BB] > 0.0 ? std::sqrt(h[SB_RR] / h[SB_BB]) : 0.0;
         res.converged = res.residual <= tolerance;
         if (res.converged || res.iterations >= max_iterations || !std::isfinite(res.residual)) break;
-        (void)breakdown;
     }
     return res;
 }

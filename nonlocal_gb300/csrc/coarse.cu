@@ -11,7 +11,9 @@
 //               node list is kept sorted (deterministic restriction).
 //   AP          per row the sums of the row's entries by column aggregate,
 //               one entry per aggregate in increasing order (float-float
-//               segmented warp sums over the row's sorted columns)
+//               segmented warp sums over the row's sorted columns), from the
+//               FP32 rows the inner iteration applies, the own aggregate's
+//               entry completing the FP64 row sum
 //   A_c = P^T A P  from AP, a row per aggregate summed in shared memory, FP64
 //   A_c^-1      blocked Gauss-Jordan in FP64 (A_c is SPD, no pivoting), 32
 //               pivots per panel, three launches per panel ping-ponging two
@@ -151,12 +153,36 @@ inline size_t ap_smem_bytes(i64 nc) {
     return size_t(AP_WARPS) * (2 * words * sizeof(uint32_t) + AP_MAXD * sizeof(double));
 }
 
-template<bool FILL>
-__global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* __restrict__ rp,
-                                                      const int32_t* __restrict__ col, const double* __restrict__ val,
-                                                      const int32_t* __restrict__ agg, i64* __restrict__ cnt,
-                                                      const i64* __restrict__ ap_rp, int32_t* __restrict__ ap_col,
-                                                      double* __restrict__ ap_val) {
+// The matrix rows AP reads: the FP32 copy of the mixed-precision solve (float
+// values, 16-bit column offsets, FP64 row sums), so that AP is that of the
+// difference-form operator the FP32 iteration applies (its entries sum to the
+// row sum: the own aggregate takes s_r minus the others), or the FP64 rows
+// (values split into float-float by integer operations).
+struct ApInput {
+    const i64* rp;
+    const int32_t* col;     // FP64 form
+    const double* val;
+    const int16_t* off;     // FP32 form: column - row
+    const float* val32;
+    const float* rowsum;
+};
+
+template<bool F32>
+__device__ __forceinline__ int32_t ap_col_of(const ApInput& in, i64 r, i64 k) {
+    if constexpr (F32) return int32_t(r + in.off[k]);
+    else return in.col[k];
+}
+
+template<bool F32>
+__device__ __forceinline__ ff ap_val_of(const ApInput& in, i64 k) {
+    if constexpr (F32) return ff{in.val32[k], 0.0f};
+    else return ff_split(in.val[k]);
+}
+
+template<bool FILL, bool F32>
+__global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, ApInput in, const int32_t* __restrict__ agg,
+                                                      i64* __restrict__ cnt, const i64* __restrict__ ap_rp,
+                                                      int32_t* __restrict__ ap_col, double* __restrict__ ap_val) {
     extern __shared__ __align__(8) unsigned char ap_smem[];
     const unsigned full = 0xffffffffu;
     const int words = (nc + 31) >> 5;
@@ -166,17 +192,18 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
     int* pre = reinterpret_cast<int*>(bm + words);
     const i64 warps = i64(gridDim.x) * AP_WARPS;
     for (i64 r = i64(blockIdx.x) * AP_WARPS + wid; r < n; r += warps) {
-        if (agg[r] < 0) {
+        const int32_t own = agg[r];
+        if (own < 0) {
             if (!FILL && lane == 0) cnt[r] = 0;
             continue;
         }
-        const i64 rb = rp[r], re = rp[r + 1];
+        const i64 rb = in.rp[r], re = in.rp[r + 1];
         for (int w = lane; w < words; w += 32) bm[w] = 0u;
         __syncwarp();
         int runs = 0;
         for (i64 k0 = rb; k0 < re; k0 += 32) {
             const i64 k = k0 + lane;
-            const int32_t J = k < re ? agg[col[k]] : -1;
+            const int32_t J = k < re ? agg[ap_col_of<F32>(in, r, k)] : -1;
             const int32_t Jn = __shfl_down_sync(full, J, 1);
             const bool end = J >= 0 && (lane == 31 || Jn != J);
             // one mark per run: neighbouring lanes mostly share an aggregate,
@@ -203,13 +230,14 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
         } else {
             for (int t = lane; t < AP_MAXD; t += 32) slot[t] = ff{0.0f, 0.0f};
             __syncwarp();
-            i64 out = ap_rp[r];
+            i64 out = ap_rp[r], own_pos = -1;
+            ff lane_total{0.0f, 0.0f};   // this lane's entries (FP32 form: the row-sum correction)
             for (i64 k0 = rb; k0 < re; k0 += 32) {
                 const i64 k = k0 + lane;
                 const bool valid = k < re;
-                const int32_t J = valid ? agg[col[k]] : -1;
-                const double a = valid ? val[k] : 0.0;
-                ff v = J >= 0 ? ff_split(a) : ff{0.0f, 0.0f};
+                const int32_t J = valid ? agg[ap_col_of<F32>(in, r, k)] : -1;
+                ff v = J >= 0 ? ap_val_of<F32>(in, k) : ff{0.0f, 0.0f};
+                if constexpr (F32) lane_total = ff_add(lane_total, v);
                 const int32_t Jp = __shfl_up_sync(full, J, 1);
                 bool head = lane == 0 || Jp != J;
                 for (int o = 1; o < 32; o <<= 1) {
@@ -239,10 +267,27 @@ __global__ void __launch_bounds__(AP_WARPS * 32) k_ap(i64 n, int nc, const i64* 
                         ap_col[pos] = J;
                         ap_val[pos] = ff_to(v);
                     }
+                    const unsigned owns = __ballot_sync(full, end && J == own);
+                    if (own_pos < 0 && owns) own_pos = out + __popc(ends & ((1u << (__ffs(owns) - 1)) - 1u));
                     out += __popc(ends);
                 }
             }
             __syncwarp();
+            if constexpr (F32) {   // the own aggregate takes s_r - (everything else)
+                for (int o = 16; o > 0; o >>= 1)
+                    lane_total = ff_add(lane_total, ff{__shfl_xor_sync(full, lane_total.h, o),
+                                                       __shfl_xor_sync(full, lane_total.l, o)});
+                if (lane == 0) {
+                    const ff d = ff_sub(ff{in.rowsum[r], 0.0f}, lane_total);
+                    if (merge) {
+                        ff& t = slot[pre[own >> 5] + __popc(bm[own >> 5] & ((1u << (own & 31)) - 1u))];
+                        t = ff_add(t, d);
+                    } else if (own_pos >= 0) {
+                        ap_val[own_pos] += ff_to(d);
+                    }
+                }
+                __syncwarp();
+            }
             if (merge)
                 for (int w = lane; w < words; w += 32) {
                     int p = pre[w];
@@ -486,10 +531,17 @@ void coarse_build(Ctx& ctx, const Csr& A, int target, double aspect) {
     NL_CUDA(cudaMemsetAsync(cnt.p + n, 0, sizeof(i64), ctx.stream));
     const unsigned gw = unsigned(std::max<i64>(1, std::min<i64>((n + AP_WARPS - 1) / AP_WARPS, 152 * 8)));
     const size_t ap_smem = ap_smem_bytes(nc);
-    NL_CUDA(cudaFuncSetAttribute(k_ap<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ap_smem)));
-    NL_CUDA(cudaFuncSetAttribute(k_ap<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ap_smem)));
-    NL_LAUNCH(k_ap<false>, gw, AP_WARPS * 32, ap_smem, ctx.stream, n, int(nc), A.rowptr.p, A.col.p, A.val.p, co.agg.p,
-              cnt.p, static_cast<const i64*>(nullptr), static_cast<int32_t*>(nullptr), static_cast<double*>(nullptr));
+    // the FP32 rows of the mixed-precision solve when they are there
+    const bool f32 = A.col16_ok && A.col16.n == size_t(A.nnz) && A.val32.n == size_t(A.nnz) &&
+                     A.rowsum32.n == size_t(A.rows);
+    const ApInput in{A.rowptr.p, A.col.p, A.val.p, A.col16.p, A.val32.p, A.rowsum32.p};
+    auto launch_ap = [&](bool fill, const i64* rp_out, int32_t* col_out, double* val_out) {
+        auto kernel = fill ? (f32 ? k_ap<true, true> : k_ap<true, false>) : (f32 ? k_ap<false, true> : k_ap<false, false>);
+        NL_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ap_smem)));
+        NL_LAUNCH(kernel, gw, AP_WARPS * 32, ap_smem, ctx.stream, n, int(nc), in, co.agg.p, cnt.p, rp_out, col_out,
+                  val_out);
+    };
+    launch_ap(false, nullptr, nullptr, nullptr);
     co.ap_rp.resize(size_t(n) + 1);
     i64 nap = 0;
     exclusive_scan(ctx, cnt.p, co.ap_rp.p, n + 1, &nap);
@@ -497,8 +549,7 @@ void coarse_build(Ctx& ctx, const Csr& A, int target, double aspect) {
     co.ap_col.resize(size_t(std::max<i64>(nap, 1)));
     dbuf<double> ap64;
     ap64.resize(size_t(std::max<i64>(nap, 1)));
-    NL_LAUNCH(k_ap<true>, gw, AP_WARPS * 32, ap_smem, ctx.stream, n, int(nc), A.rowptr.p, A.col.p, A.val.p, co.agg.p,
-              cnt.p, co.ap_rp.p, co.ap_col.p, ap64.p);
+    launch_ap(true, co.ap_rp.p, co.ap_col.p, ap64.p);
     co.ap_val.resize(size_t(std::max<i64>(nap, 1)));
     dbuf<int> bad;
     bad.resize(1);

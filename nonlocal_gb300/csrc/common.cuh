@@ -45,12 +45,30 @@ struct error : std::runtime_error {
         if (!(cond)) throw ::nlgpu::error{(code), (msg)};                      \
     } while (0)
 
+// Kernel launches issued by the library (all host threads).  A launch made
+// while this thread captures a stream into a graph counts into the capture's
+// own counter instead, and the graph's kernels count when the graph launches.
 extern std::atomic<int64_t> g_launches;
+extern thread_local int64_t* t_capture_sink;
+
+struct CountCaptured {
+    int64_t kernels = 0;
+    int64_t* prev;
+    CountCaptured() : prev{t_capture_sink} { t_capture_sink = &kernels; }
+    ~CountCaptured() { t_capture_sink = prev; }
+    CountCaptured(const CountCaptured&) = delete;
+    CountCaptured& operator=(const CountCaptured&) = delete;
+};
+
+inline void count_launch() {
+    if (t_capture_sink) ++*t_capture_sink;
+    else g_launches.fetch_add(1, std::memory_order_relaxed);
+}
 
 #define NL_LAUNCH(kernel, grid, block, smem, stream, ...)                      \
     do {                                                                       \
         kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);            \
-        ::nlgpu::g_launches.fetch_add(1, std::memory_order_relaxed);           \
+        ::nlgpu::count_launch();                                               \
         NL_CUDA(cudaGetLastError());                                           \
     } while (0)
 
@@ -321,6 +339,9 @@ struct Coarse {
 // Device state of BiCGSTAB (bicgstab.cu).
 struct BicgWork {
     dbuf<double> r, r0, p, v, s, t, y, z, dinv, part, sc;
+    cudaGraphExec_t chunk = nullptr;   // BI_ITERS iterations, captured per solve
+    int chunk_kernels = 0;
+    ~BicgWork() { if (chunk) cudaGraphExecDestroy(chunk); }
 };
 
 // Device state of the mixed-precision solve (mixed.cu).
@@ -567,6 +588,7 @@ cudaStream_t batch_stream(Batch& bt);
 void batch_sizes(const Batch& bt, i64* rows, i64* system_entries);
 void batch_set_method(Batch& bt, int method);
 void batch_last_solve(const Batch& bt, i64* inner, i64* outer, int* fallback);
+std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double tolerance, i64 max_iterations);
 // bicgstab.cu: Jacobi-preconditioned BiCGSTAB on a full-row (non-symmetric) matrix, zero start
 CgResult bicgstab_solve(Ctx& ctx, const Csr& A_full, const double* b, double* x, double tolerance, i64 max_iterations);
 // mpnn.cu

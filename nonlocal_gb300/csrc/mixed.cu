@@ -384,28 +384,30 @@ __global__ void k_to_f32(i64 n, const double* __restrict__ a, float* __restrict_
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) b[i] = float(a[i]);
 }
 
-// largest |column - row| of the matrix (warp per row)
-__global__ void k_max_offset(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col,
-                             unsigned long long* __restrict__ out) {
+// The FP32 copy in one pass over the FP64 rows (warp per row): float values,
+// 16-bit offsets column - row (written clamped; kept only when the widest
+// offset fits), the row sums of the FP64 values and the widest offset.
+__global__ void k_fp32_copy(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col,
+                            const double* __restrict__ val, float* __restrict__ val32, int16_t* __restrict__ col16,
+                            float* __restrict__ rowsum, unsigned long long* __restrict__ widest) {
     const int lane = threadIdx.x & 31;
     const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
     unsigned long long m = 0;
-    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps)
+    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
+        double s = 0.0;
         for (i64 k = rp[r] + lane; k < rp[r + 1]; k += 32) {
+            const double v = val[k];
             const i64 d = i64(col[k]) - r;
+            s += v;
+            val32[k] = float(v);
+            col16[k] = int16_t(d < -32768 ? -32768 : (d > 32767 ? 32767 : d));
             m = max(m, static_cast<unsigned long long>(d < 0 ? -d : d));
         }
+        s = warp_sum(s);
+        if (lane == 0) rowsum[r] = float(s);
+    }
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0 && m) atomicMax(out, m);
-}
-
-// col16 = column - row (offsets checked to fit 16 bits)
-__global__ void k_col_offsets(i64 n, const i64* __restrict__ rp, const int32_t* __restrict__ col,
-                              int16_t* __restrict__ col16) {
-    const int lane = threadIdx.x & 31;
-    const i64 warps = i64(gridDim.x) * (blockDim.x >> 5);
-    for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps)
-        for (i64 k = rp[r] + lane; k < rp[r + 1]; k += 32) col16[k] = int16_t(i64(col[k]) - r);
+    if (lane == 0 && m) atomicMax(widest, m);
 }
 
 // partial of a.b
@@ -638,9 +640,9 @@ bool upper_to_f32(Ctx& ctx, Csr& A, const Csr& upper) {
 // rows with 16-bit column offsets when the pattern's bandwidth allows
 void matrix_to_f32(Ctx& ctx, Csr& A, const Csr* upper) {
     A.rowsum32.resize(size_t(A.rows));
-    NL_LAUNCH(k_rowsum, grid_for(A.rows, 256), 256, 0, ctx.stream, A.rows, A.rowptr.p, A.val.p, A.rowsum32.p);
     A.up_ok = upper && upper_to_f32(ctx, A, *upper);
     if (A.up_ok) {
+        NL_LAUNCH(k_rowsum, grid_for(A.rows, 256), 256, 0, ctx.stream, A.rows, A.rowptr.p, A.val.p, A.rowsum32.p);
         // the full-row FP32 copy is not needed (and not kept up to date)
         A.val32.release();
         A.col16.release();
@@ -649,21 +651,17 @@ void matrix_to_f32(Ctx& ctx, Csr& A, const Csr* upper) {
     }
     A.up_rp.release(); A.up_off.release(); A.up_val.release();
     A.val32.resize(size_t(A.nnz));
-    NL_LAUNCH(k_to_f32, grid_for(A.nnz, 256), 256, 0, ctx.stream, A.nnz, A.val.p, A.val32.p);
+    A.col16.resize(size_t(A.nnz));
     dbuf<unsigned long long> widest;
     widest.resize(1);
     widest.zero(ctx.stream);
-    NL_LAUNCH(k_max_offset, RED_BLOCKS, 256, 0, ctx.stream, A.rows, A.rowptr.p, A.col.p, widest.p);
+    NL_LAUNCH(k_fp32_copy, grid_for(A.rows * 32, 256, 152 * 64), 256, 0, ctx.stream, A.rows, A.rowptr.p, A.col.p,
+              A.val.p, A.val32.p, A.col16.p, A.rowsum32.p, widest.p);
     unsigned long long w = 0;
     widest.download(&w, 1, ctx.stream);
     NL_CUDA(cudaStreamSynchronize(ctx.stream));
     A.col16_ok = w <= 32767;
-    if (A.col16_ok) {
-        A.col16.resize(size_t(A.nnz));
-        NL_LAUNCH(k_col_offsets, RED_BLOCKS, 256, 0, ctx.stream, A.rows, A.rowptr.p, A.col.p, A.col16.p);
-    } else {
-        A.col16.release();
-    }
+    if (!A.col16_ok) A.col16.release();
 }
 
 // One flexible CG in FP32 with reliable updates: the FP32 recurrence runs
@@ -779,13 +777,14 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
         }
         if (!captured) {
             cudaGraph_t g = nullptr;
-            const i64 before = g_launches.load();
-            NL_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
-            for (int it = 0; it < MX_ITERS; ++it) iteration();
-            NL_CUDA(cudaStreamEndCapture(ctx.stream, &g));
+            {
+                CountCaptured counted;
+                NL_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+                for (int it = 0; it < MX_ITERS; ++it) iteration();
+                NL_CUDA(cudaStreamEndCapture(ctx.stream, &g));
+                w.chunk_kernels = int(counted.kernels);   // counted when the graph is launched
+            }
             timer.mark("first chunk, capture");
-            w.chunk_kernels = int(g_launches.load() - before);
-            g_launches.fetch_sub(w.chunk_kernels);   // counted when the graph is launched
             cudaError_t e = cudaErrorGraphExecUpdateFailure;
             if (w.chunk) {
                 cudaGraphExecUpdateResultInfo info;

@@ -5,6 +5,7 @@
 namespace nlgpu {
 
 std::atomic<int64_t> g_launches{0};
+thread_local int64_t* t_capture_sink = nullptr;
 
 namespace {
 

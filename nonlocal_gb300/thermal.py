@@ -572,6 +572,28 @@ def find_neighbours(problem: Problem2D, strategy: str = "MAX"):
     return r, off, lst
 
 
+def solve_assembled_batch(problems: list, tolerance: float = 1e-10, max_iterations: int = 10000,
+                          check_convergence: bool = True):
+    """The solve stage of many assembled problems in one call
+    (nlgpu_solve_assembled_batch): the non-symmetric systems (a conductivity
+    field with a nonlocal model) run as one block-diagonal BiCGSTAB with
+    per-instance scalars and stop tests, the others one after another.
+    Returns the temperatures and reports, in the problems' order."""
+    count = len(problems)
+    if count == 0:
+        return [], []
+    lib = problems[0]._lib
+    temps = [np.empty(pb.n_nodes) for pb in problems]
+    handles = (ctypes.c_void_p * count)(*[pb._h for pb in problems])
+    outs = (ctypes.c_void_p * count)(*[t.ctypes.data for t in temps])
+    reps = (L.SolveReport * count)()
+    o = problems[0]._options(tolerance, max_iterations, "illt", "fp64", 0.0, 0)
+    rc = lib.nlgpu_solve_assembled_batch(count, handles, ctypes.byref(o), outs, reps)
+    if rc != L.OK and (check_convergence or rc != 6):
+        L.check(rc)
+    return temps, [SolveReport(r.as_dict()) for r in reps]
+
+
 def stationary_heat_equation_solver_2d(problem: Problem2D, model: Model2D, boundaries: list[Boundary],
                                        source: float = 0.0, tolerance: float = 1e-10, max_iterations: int = 10000,
                                        preconditioner: str = "illt", precision: str = "fp64"):

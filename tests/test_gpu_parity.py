@@ -179,6 +179,61 @@ def test_nonsymmetric_variable_conductivity(lib):
     assert rep.residual <= 1e-13
     assert rel(t, fx["temperature"]) < SOLUTION_RTOL
     assert_flux(pb.calc_flux(fx["temperature"]), fx)
+    # the ordered pairs in float-float on the FP32 pipes meet the same bar
+    pb.set_assembly_precision("ff")
+    try:
+        pb.conductivity_matrix("FULL")
+        assert pb.assembly_tuning()["warps"] in (16, 32)
+        assert_csr_equal(pb.matrix("inner"), fx, "K_inner")
+        assert_csr_equal(pb.matrix("bound"), fx, "K_bound")
+        t, rep = pb.solve_assembled(tolerance=1e-13, max_iterations=20000)
+        assert rel(t, fx["temperature"]) < SOLUTION_RTOL
+    finally:
+        pb.set_assembly_precision("auto")
+
+
+def test_batched_nonsymmetric_solves_match_single_instances(lib):
+    """nlgpu_solve_assembled_batch: the reference's variable-conductivity
+    fixture and log-normal-conductivity instances of uneven size, radius and
+    p1 solved as one block-diagonal BiCGSTAB reach the fixture's temperature
+    and each instance's single-system BiCGSTAB solution; a symmetric instance
+    in the same call is solved on its own."""
+    from nonlocal_gb300 import thermal as T
+    from nonlocal_gb300.fields import lognormal_conductivity
+    from nonlocal_gb300.meshgen import structured_quad_mesh
+    fx = gc.load("b10_field_nonsym")
+    problems = []
+    pb = gpu_problem(fx)
+    pb.set_conductivity_field(fx["conductivity_q"])
+    pb.find_neighbours(fx["config"].get("strategy", "MAX"))
+    problems.append(pb)
+    for k, (nx, r, p1) in enumerate([(12, 0.2, 0.3), (20, 0.08, 0.7), (16, 0.12, 0.5)]):
+        mesh = structured_quad_mesh(nx, nx, "bilinear")
+        q = T.Problem2D.from_mesh(mesh)
+        q.set_model(T.Model2D(influence="fast_polynomial", radius=(r, r), local_weight=p1))
+        q.set_conductivity_field(lognormal_conductivity(q.quadrature()[0], 0.1, 0.5, seed=k))
+        q.add_boundary(T.Boundary(edges=mesh.boundaries["left"], kind="temperature", value=0.0))
+        q.add_boundary(T.Boundary(edges=mesh.boundaries["right"], kind="flux", value=1.0))
+        q.find_neighbours()
+        problems.append(q)
+    mesh = structured_quad_mesh(10, 10, "bilinear")
+    sym = T.Problem2D.from_mesh(mesh)
+    sym.set_model(T.Model2D(influence="fast_polynomial", radius=(0.2, 0.2), local_weight=0.5))
+    sym.add_boundary(T.Boundary(edges=mesh.boundaries["left"], kind="temperature", value=0.0))
+    sym.add_boundary(T.Boundary(edges=mesh.boundaries["right"], kind="flux", value=1.0))
+    sym.find_neighbours()
+    problems.insert(2, sym)
+    for q in problems:
+        q.conductivity_matrix("FULL")
+    temps, reps = T.solve_assembled_batch(problems, tolerance=1e-13, max_iterations=20000)
+    for t, rep in zip(temps, reps):
+        assert rep.residual <= 1e-13 and rep.iterations > 0
+    assert rel(temps[0], fx["temperature"]) < SOLUTION_RTOL
+    for q, t in zip(problems, temps):
+        single, rep = q.solve_assembled(tolerance=1e-13, max_iterations=20000)
+        assert rel(t, single) < 1e-9   # two solutions with |b - Ax| <= 1e-13 |b| each
+    for q in problems:
+        q.close()
 
 
 FLUX_RTOL = 1e-12
