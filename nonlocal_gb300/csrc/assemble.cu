@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_pairs(AssembleArgs a, M
                 double v = 0.0;
                 #pragma unroll
                 for (int qL = 0; qL < NQ; ++qL)
-                    v += ewx[i * NQ + qL] * ps.hx[qL * NEN + j] + ewy[i * NQ + qL] * ps.hy[qL * NEN + j];
+                    v = fma(ewy[i * NQ + qL], ps.hy[qL * NEN + j], fma(ewx[i * NQ + qL], ps.hx[qL * NEN + j], v));
                 if (self) {
                     double loc = 0.0;
                     #pragma unroll

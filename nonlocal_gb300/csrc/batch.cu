@@ -120,14 +120,20 @@ __global__ void __launch_bounds__(BT_THREADS) k_bt_spmv(i64 nblocks, const unsig
         const int g = 1 << lg, sub = lane & (g - 1), slot = lane >> lg;
         const i64 r = first + slot;
         const bool active = slot < cnt;
-        double s = 0.0;
+        double s = 0.0, s2 = 0.0;
         if (active) {
             const i64 b4 = rp[r] >> 2, e4 = rp[r + 1] >> 2;
             for (i64 q = b4 + sub; q < e4; q += g) {
                 const int4 c = __ldg(col4 + q);
                 const double2 v0 = __ldg(val2 + 2 * q), v1 = __ldg(val2 + 2 * q + 1);
-                s += v0.x * x[c.x] + v0.y * x[c.y] + v1.x * x[c.z] + v1.y * x[c.w];
+                // two FMA chains: written as one sum of products the group cost a multiply
+                // and an add besides its FMAs on the FP64 pipe, which bounds this product
+                s = fma(v0.x, x[c.x], s);
+                s2 = fma(v0.y, x[c.y], s2);
+                s = fma(v1.x, x[c.z], s);
+                s2 = fma(v1.y, x[c.w], s2);
             }
+            s += s2;
         }
         for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(full, s, o);   // within the lane group
         if (active && sub == 0) {

@@ -74,13 +74,18 @@ __global__ void __launch_bounds__(RED_THREADS) k_spmv(i64 n, const i64* __restri
     double dot = 0.0;
     for (i64 r = (blockIdx.x * i64(blockDim.x) + threadIdx.x) >> 5; r < n; r += warps) {
         const i64 b4 = rp[r] >> 2, e4 = rp[r + 1] >> 2;
-        double s = 0.0;
+        double s = 0.0, s2 = 0.0;
         for (i64 k = b4 + lane; k < e4; k += 32) {
             const int4 c = __ldg(col4 + k);
             const double2 v0 = __ldg(val2 + 2 * k), v1 = __ldg(val2 + 2 * k + 1);
-            s += v0.x * x[c.x] + v0.y * x[c.y] + v1.x * x[c.z] + v1.y * x[c.w];
+            // two FMA chains: written as one sum of products the group cost a multiply
+            // and an add besides its FMAs on the FP64 pipe, which bounds this product
+            s = fma(v0.x, x[c.x], s);
+            s2 = fma(v0.y, x[c.y], s2);
+            s = fma(v1.x, x[c.z], s);
+            s2 = fma(v1.y, x[c.w], s2);
         }
-        s = warp_sum(s);
+        s = warp_sum(s + s2);
         if (lane == 0) { y[r] = s; dot += s * x[r]; }
     }
     if (dot_partial) {
