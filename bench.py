@@ -657,8 +657,10 @@ def run_config4(args, world, rank, local, dist):
         pb.find_neighbours()
         return pb
 
+    precision = "mixed" if args.precond4 == "illt" else "fp64"
+
     def solve(pb):
-        _, rep = pb.stationary(tolerance=tol, max_iterations=100000, precision="fp64")
+        _, rep = pb.stationary(tolerance=tol, max_iterations=100000, precision=precision)
         return rep
 
     def assemble(pb):
@@ -666,12 +668,13 @@ def run_config4(args, world, rank, local, dist):
 
     solve_seconds = []
 
-    def step(pool):
+    def step(pool, prec=None):
         if args.solve4 == "single":
             return list(pool.map(solve, problems))
         list(pool.map(assemble, problems))
         t1 = time.perf_counter()
-        _, reps_b = T.solve_assembled_batch(problems, tolerance=tol, max_iterations=100000, check_convergence=False)
+        _, reps_b = T.solve_assembled_batch(problems, tolerance=tol, max_iterations=100000, check_convergence=False,
+                                            precision=prec or precision)
         solve_seconds.append(time.perf_counter() - t1)
         return reps_b
 
@@ -692,12 +695,28 @@ def run_config4(args, world, rank, local, dist):
             reps.append(step(pool))
         total = time.perf_counter() - t_all
         clocks = sampler.stop()
-    launches = L.kernel_launches() - launches0
+        launches = L.kernel_launches() - launches0
+        per = np.array(solve_seconds) if solve_seconds else None
+        other = None
+        if args.solve4 == "batch":   # the other preconditioner, a few steps
+            other_prec = "fp64" if precision == "mixed" else "mixed"
+            step(pool, other_prec)
+            solve_seconds.clear()
+            t2 = time.perf_counter()
+            o_reps = [step(pool, other_prec) for _ in range(3)]
+            o_total = time.perf_counter() - t2
+            o_its = np.array([r.iterations for r in o_reps[-1]])
+            other = {"preconditioner": "diagonal (the reference's)" if other_prec == "fp64" else "FP32 ILLT of the local parts",
+                     "instance_solves_per_s": len(specs) * 3 / o_total, "batched_solve_s": float(np.mean(solve_seconds)),
+                     "iterations": {"mean": float(o_its.mean()), "max": int(o_its.max())},
+                     "converged": int(sum(r.residual <= tol for r in o_reps[-1]))}
     barrier(dist)
     total = max_over_ranks(dist, total)
     last = reps[-1]
     its = np.array([r.iterations for r in last])
-    per = np.array(solve_seconds) if solve_seconds else np.array([r.seconds_total for r in last])
+    if per is None:
+        per = np.array([r.seconds_total for r in last])
+    solve_seconds = list(per) if args.solve4 == "batch" else []
     pairs = int(sum(r.element_pairs for r in last))
     # BiCGSTAB reads the full-row FP64 matrix twice per iteration
     spmv = sum(2 * int(r.iterations) * (int(r.nnz_solver) * 12 + (pb.n_nodes + 1) * 8 + 2 * pb.n_nodes * 8)
@@ -748,11 +767,15 @@ def run_config4(args, world, rank, local, dist):
                                "g a Gaussian random field (correlation length 0.1, std 0.5), r ~ U[0.02, 0.08], "
                                "p1 ~ U[0.2, 0.8], fast polynomial kernel, left T = 0, unit flux right",
                    "instances": len(specs), "solve": args.solve4, "assembly": args.assembly4,
+                   "preconditioner": args.precond4,
                    "parallelism": f"replicas x{world}, {SETUP_THREADS} host threads"},
         "solve_s": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                     "what": "the batched solve of all instances per step" if args.solve4 == "batch"
                             else "one instance's assembly and solve, overlapping the others'"},
+        "preconditioner": "FP32 ILLT of each instance's p1 K_local (this library's)" if precision == "mixed"
+                          else "diagonal (the reference's)",
         "bicgstab_iterations": {"mean": float(its.mean()), "max": int(its.max())},
+        "other_preconditioner": other,
         "residual_max": float(max(r.residual for r in last)),
         "converged": int(sum(r.residual <= tol for r in last)),
         "element_pairs_per_s": pairs * world / (total / args.steps),
@@ -974,6 +997,9 @@ def main() -> int:
     ap.add_argument("--instances4", type=int, default=64, help="config4: number of instances")
     ap.add_argument("--assembly4", choices=["ff", "fp64"], default="ff",
                     help="config4: pair blocks in float-float on the FP32 pipes, or in FP64")
+    ap.add_argument("--precond4", choices=["illt", "jacobi"], default="illt",
+                    help="config4: BiCGSTAB preconditioned by the FP32 ILLT of the local parts, or by the "
+                         "diagonal (the reference's)")
     ap.add_argument("--solve4", choices=["batch", "single"], default="batch",
                     help="config4: one block-diagonal BiCGSTAB over all instances, or one solve per instance")
     ap.add_argument("--instances", type=int, default=256, help="config5: number of instances")

@@ -309,8 +309,12 @@ int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, do
  * Jacobi-preconditioned BiCGSTAB, stationary_heat_equation_solver_2d.hpp:105-108)
  * run as one block-diagonal BiCGSTAB, every instance with its own scalars
  * and stop test |b - A x| <= tolerance |b|; an instance whose recurrence
- * breaks down is solved again alone.  Symmetric instances are solved one
- * after another as by nlgpu_solve_assembled.  temperatures[k]: [n_nodes of
+ * breaks down or drifts starts again from its x.  precision FP64: the
+ * reference's diagonal preconditioner; MIXED: the ILLT of every instance's
+ * p1 K_local applied in FP32 (products and vectors stay FP64; the same
+ * choice applies to a single non-symmetric nlgpu_solve_assembled /
+ * nlgpu_stationary_2d).  Symmetric instances are solved one after another as
+ * by nlgpu_solve_assembled.  temperatures[k]: [n_nodes of
  * instance k]; reports may be NULL, else [count].  Returns
  * NLGPU_ERR_NO_CONVERGENCE when an instance did not converge (every output is
  * still written). */

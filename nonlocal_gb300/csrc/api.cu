@@ -182,10 +182,13 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
     const double* b = rhs ? rhs : c.rhs.p;
     if (!c.symmetric) {
         // variable conductivity with a nonlocal model: full storage, BiCGSTAB with
-        // the diagonal preconditioner (stationary_heat_equation_solver_2d.hpp:105-108)
+        // the diagonal preconditioner (stationary_heat_equation_solver_2d.hpp:105-108);
+        // MIXED: preconditioned by the FP32 ILLT of the local part instead
         const auto t0 = std::chrono::steady_clock::now();
         c.temperature.resize(size_t(c.n_nodes));
-        CgResult r = bicgstab_solve(c, c.full, b, c.temperature.p, o.tolerance, o.max_iterations);
+        CgResult r = o.precision == NLGPU_PRECISION_MIXED && !rhs
+                         ? batch_bicgstab({&c}, o.tolerance, o.max_iterations, true).front()
+                         : bicgstab_solve(c, c.full, b, c.temperature.p, o.tolerance, o.max_iterations);
         if (rep) rep->seconds_solve = seconds(t0);
         fill_report(c, rep, r);
         return r;
@@ -765,7 +768,9 @@ int nlgpu_solve_assembled_batch(int64_t count, nlgpu_ctx* const* instances, cons
             }
         }
         std::vector<CgResult> res;
-        if (!batched.empty()) res = batch_bicgstab(batched, options->tolerance, options->max_iterations);
+        if (!batched.empty())
+            res = batch_bicgstab(batched, options->tolerance, options->max_iterations,
+                                 options->precision == NLGPU_PRECISION_MIXED);
         const double batch_seconds = seconds(t0);
         size_t next = 0;
         for (int64_t k = 0; k < count; ++k) {

@@ -597,7 +597,11 @@ void batch_sizes(const Batch& bt, i64* rows, i64* system_entries) {
 // recurrence breaks down (rho or omega vanishing, a non-finite scalar); then
 // the true residuals decide, and the instances that miss the tolerance start
 // again from their x with r0 = b - A x (at most 16 rounds), as the
-// single-system solver does.
+// single-system solver does.  With `illt` the preconditioner is instead the
+// ILLT of every instance's p1 K_local (this library's addition: the local
+// part is symmetric also with a conductivity field), applied in FP32 by the
+// single-system Jacobi sweeps and widened; the products, vectors and scalars
+// stay FP64.
 
 namespace {
 
@@ -659,10 +663,10 @@ __global__ void k_bb_jacobi(i64 n, const i64* __restrict__ rp, const int32_t* __
     }
 }
 
-// p = r + beta (p - omega v); y = dinv p
+// p = r + beta (p - omega v); y = dinv p, or p32 = p for the ILLT (which then writes y)
 __global__ void k_bb_p(i64 n, const double* __restrict__ r, double* __restrict__ p, const double* __restrict__ v,
-                       const double* __restrict__ dinv, double* __restrict__ y, const int32_t* __restrict__ inst,
-                       const double* __restrict__ sc, i64 K, int q) {
+                       const double* __restrict__ dinv, double* __restrict__ y, float* __restrict__ p32,
+                       const int32_t* __restrict__ inst, const double* __restrict__ sc, i64 K, int q) {
     const double* rho = sc + (q ? BB_RHO1 : BB_RHO0) * K;
     const double* rho_old = sc + (q ? BB_RHO0 : BB_RHO1) * K;
     BT_ROWS(i) {
@@ -672,15 +676,17 @@ __global__ void k_bb_p(i64 n, const double* __restrict__ r, double* __restrict__
         const double beta = (rho[k] / rho_old[k]) * (sc[BB_ALPHA * K + k] / w);
         const double pi = r[i] + beta * (p[i] - w * v[i]);
         p[i] = pi;
-        y[i] = dinv[i] * pi;
+        if (p32) p32[i] = float(pi);
+        else y[i] = dinv[i] * pi;
     }
 }
 
-// alpha = rho / r0.v; s = r - alpha v; z = dinv s.  Block 0 clears the
-// accumulators the x / r update adds into (nothing reads them here).
+// alpha = rho / r0.v; s = r - alpha v; z = dinv s, or s32 = s for the ILLT.
+// Block 0 clears the accumulators the x / r update adds into (nothing reads
+// them here).
 __global__ void k_bb_s(i64 n, const double* __restrict__ r, const double* __restrict__ v, const double* __restrict__ dinv,
-                       double* __restrict__ s, double* __restrict__ z, const int32_t* __restrict__ inst,
-                       double* __restrict__ sc, i64 K, int q) {
+                       double* __restrict__ s, double* __restrict__ z, float* __restrict__ s32,
+                       const int32_t* __restrict__ inst, double* __restrict__ sc, i64 K, int q) {
     const double* rho = sc + (q ? BB_RHO1 : BB_RHO0) * K;
     BT_ROWS(i) {
         const int k = inst[i];
@@ -688,7 +694,8 @@ __global__ void k_bb_s(i64 n, const double* __restrict__ r, const double* __rest
         const double alpha = rho[k] / sc[BB_R0V * K + k];
         const double si = r[i] - alpha * v[i];
         s[i] = si;
-        z[i] = dinv[i] * si;
+        if (s32) s32[i] = float(si);
+        else z[i] = dinv[i] * si;
     }
     if (blockIdx.x == 0)
         for (i64 k = threadIdx.x; k < K; k += blockDim.x) {
@@ -756,6 +763,11 @@ __global__ void k_bb_check(i64 K, double* __restrict__ sc, int q, double tol2, d
     if (threadIdx.x == 0) running[BT_RUN_SLOT] = cnt;
 }
 
+// y = the FP32 preconditioner output, widened
+__global__ void k_bb_widen(i64 n, const float* __restrict__ a, double* __restrict__ y) {
+    BT_ROWS(i) y[i] = double(a[i]);
+}
+
 // per instance |b - q|^2 into acc (zeroed by the caller)
 __global__ void __launch_bounds__(BT_THREADS) k_bb_residual(i64 n, const double* __restrict__ b, const double* __restrict__ q,
                                                             const int32_t* __restrict__ inst, double* __restrict__ acc) {
@@ -767,7 +779,8 @@ __global__ void __launch_bounds__(BT_THREADS) k_bb_residual(i64 n, const double*
 
 }  // namespace
 
-std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double tolerance, i64 max_iterations) {
+std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double tolerance, i64 max_iterations,
+                                     bool illt) {
     Batch bt;
     NL_CUDA(cudaStreamCreateWithFlags(&bt.stream, cudaStreamNonBlocking));
     struct StreamGuard {
@@ -794,8 +807,42 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
     bt.inst_of_row.resize(size_t(N));
     concat(bt, bt.A, [](Ctx& c) -> const Csr& { return c.full; }, true);
     row_blocks(bt, bt.A, bt.blocks_A, bt.nblocks_A);
+    // the local ILLT preconditioner: p1 K_local of every instance (symmetric also with a
+    // conductivity field: the field enters at the element's own quadrature points),
+    // block-diagonal, factored by the single-system IC(0) and applied by FP32 Jacobi sweeps
+    if (illt) {
+        std::vector<Csr> local(instances.size());
+        for (size_t k = 0; k < instances.size(); ++k) {
+            Ctx& c = *instances[k];
+            build_patterns(c, true, true, local[k], nullptr, nullptr, nullptr);
+            assemble_local(c, local[k], c.model.p1, 0);
+            NL_CUDA(cudaStreamSynchronize(c.stream));
+        }
+        concat(bt, bt.M, [&](Ctx& c) -> const Csr& {
+            const size_t k = size_t(std::find(bt.inst.begin(), bt.inst.end(), &c) - bt.inst.begin());
+            return local[k];
+        }, false);
+        bt.solver.stream = bt.stream;
+        bt.solver.n_nodes = N;
+        ilt_build(bt.solver, bt.M, bt.ic, false);
+        illt = bt.ic.ok;   // the diagonal otherwise (as the reference)
+    }
     dbuf<double> r0, v, s, t, y, z, dinv, acc;
+    dbuf<float> in32, out32;
     for (auto* b : {&bt.x, &bt.b, &bt.r, &bt.p, &r0, &v, &s, &t, &y, &z, &dinv}) b->resize(size_t(N));
+    if (illt) {
+        in32.resize(size_t(N));
+        out32.resize(size_t(N));
+    }
+    const int sweeps = NLGPU_DEFAULT_TRIANGULAR_SWEEPS;
+    auto precondition = [&](double* out) {   // out = M^-1 in32 (FP32 sweeps), widened
+        ilt_apply32(bt.solver, bt.ic, in32.p, out32.p, sweeps);
+        NL_LAUNCH(k_bb_widen, grid_for(N, 256), 256, 0, bt.stream, N, out32.p, out);
+    };
+    if (illt) {   // the first application outside the capture (lazy set-up)
+        in32.zero(bt.stream);
+        precondition(y.p);
+    }
     for (i64 k = 0; k < K; ++k) {
         Ctx& c = *instances[size_t(k)];
         NL_CUDA(cudaMemcpyAsync(bt.b.p + bt.row_off[size_t(k)], c.rhs.p, size_t(c.n_nodes) * sizeof(double),
@@ -832,10 +879,12 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
             for (int it = 0; it < BB_ITERS; ++it) {
                 const int q = it & 1;
                 NL_LAUNCH(k_bb_p, grid_for(N, 256, RED_BLOCKS * 4), 256, 0, bt.stream, N, bt.r.p, bt.p.p, v.p, dinv.p,
-                          y.p, bt.inst_of_row.p, sc, K, q);
+                          y.p, illt ? in32.p : nullptr, bt.inst_of_row.p, sc, K, q);
+                if (illt) precondition(y.p);
                 spmv(y.p, v.p, sc + BB_R0V * K, r0.p, static_cast<double*>(nullptr));
                 NL_LAUNCH(k_bb_s, grid_for(N, 256, RED_BLOCKS * 4), 256, 0, bt.stream, N, bt.r.p, v.p, dinv.p, s.p, z.p,
-                          bt.inst_of_row.p, sc, K, q);
+                          illt ? in32.p : nullptr, bt.inst_of_row.p, sc, K, q);
+                if (illt) precondition(z.p);
                 spmv(z.p, t.p, sc + BB_TS * K, s.p, sc + BB_TT * K);
                 NL_LAUNCH(k_bb_xr, RED_BLOCKS, BT_THREADS, 0, bt.stream, N, bt.x.p, y.p, z.p, s.p, t.p, bt.r.p, r0.p,
                           bt.inst_of_row.p, sc, K, q);

@@ -588,7 +588,8 @@ cudaStream_t batch_stream(Batch& bt);
 void batch_sizes(const Batch& bt, i64* rows, i64* system_entries);
 void batch_set_method(Batch& bt, int method);
 void batch_last_solve(const Batch& bt, i64* inner, i64* outer, int* fallback);
-std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double tolerance, i64 max_iterations);
+std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double tolerance, i64 max_iterations,
+                                     bool illt);
 // bicgstab.cu: Jacobi-preconditioned BiCGSTAB on a full-row (non-symmetric) matrix, zero start
 CgResult bicgstab_solve(Ctx& ctx, const Csr& A_full, const double* b, double* x, double tolerance, i64 max_iterations);
 // mpnn.cu

@@ -573,12 +573,14 @@ def find_neighbours(problem: Problem2D, strategy: str = "MAX"):
 
 
 def solve_assembled_batch(problems: list, tolerance: float = 1e-10, max_iterations: int = 10000,
-                          check_convergence: bool = True):
+                          check_convergence: bool = True, precision: str = "fp64"):
     """The solve stage of many assembled problems in one call
     (nlgpu_solve_assembled_batch): the non-symmetric systems (a conductivity
     field with a nonlocal model) run as one block-diagonal BiCGSTAB with
-    per-instance scalars and stop tests, the others one after another.
-    Returns the temperatures and reports, in the problems' order."""
+    per-instance scalars and stop tests (precision "fp64": the reference's
+    diagonal preconditioner; "mixed": the FP32 ILLT of each local part), the
+    others one after another.  Returns the temperatures and reports, in the
+    problems' order."""
     count = len(problems)
     if count == 0:
         return [], []
@@ -587,7 +589,7 @@ def solve_assembled_batch(problems: list, tolerance: float = 1e-10, max_iteratio
     handles = (ctypes.c_void_p * count)(*[pb._h for pb in problems])
     outs = (ctypes.c_void_p * count)(*[t.ctypes.data for t in temps])
     reps = (L.SolveReport * count)()
-    o = problems[0]._options(tolerance, max_iterations, "illt", "fp64", 0.0, 0)
+    o = problems[0]._options(tolerance, max_iterations, "illt", precision, 0.0, 0)
     rc = lib.nlgpu_solve_assembled_batch(count, handles, ctypes.byref(o), outs, reps)
     if rc != L.OK and (check_convergence or rc != 6):
         L.check(rc)

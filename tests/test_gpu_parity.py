@@ -232,6 +232,16 @@ def test_batched_nonsymmetric_solves_match_single_instances(lib):
     for q, t in zip(problems, temps):
         single, rep = q.solve_assembled(tolerance=1e-13, max_iterations=20000)
         assert rel(t, single) < 1e-9   # two solutions with |b - Ax| <= 1e-13 |b| each
+    # MIXED: the FP32 ILLT of each local part instead of the diagonal, batched and alone
+    temps_m, reps_m = T.solve_assembled_batch(problems, tolerance=1e-13, max_iterations=20000, precision="mixed")
+    assert rel(temps_m[0], fx["temperature"]) < SOLUTION_RTOL
+    for k, (q, t, tm, rep, rep_m) in enumerate(zip(problems, temps, temps_m, reps, reps_m)):
+        assert rep_m.residual <= 1e-13
+        assert rel(tm, t) < 1e-9, k
+        if k != 2:   # the non-symmetric ones: fewer iterations than with the diagonal
+            assert rep_m.iterations < rep.iterations, (k, rep_m.iterations, rep.iterations)
+            single, rep_s = q.solve_assembled(tolerance=1e-13, max_iterations=20000, precision="mixed")
+            assert rel(single, t) < 1e-9 and rep_s.residual <= 1e-13
     for q in problems:
         q.close()
 
