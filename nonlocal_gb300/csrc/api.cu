@@ -209,7 +209,7 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
         if (!c.local_ready) build_local(c);
         timer.mark("local matrix");
         // the exact sweeps' shared-memory plans only when this solve uses them
-        if (!keep_preconditioner) ilt_build(c, c.local, c.ilt, !(mixed && sweeps > 0));
+        if (!keep_preconditioner) ilt_build(c, c.local, c.ilt, !(mixed && sweeps > 0), mixed && sweeps > 0);
         timer.mark("preconditioner");
         if (c.ilt.ok) M = &c.ilt;   // identity fallback (stationary_heat_equation_solver_2d.hpp:97-101)
         if (learned && M && !(c.mp.ready && c.mp.n == c.local.rows)) mpnn_prepare(c, c.local);
@@ -996,7 +996,7 @@ void ensure_learning_state(Ctx& c) {
     NL_REQUIRE(c.inner_ready, NLGPU_ERR_STATE, "assemble the system first (nlgpu_conductivity_matrix_2d)");
     NL_REQUIRE(c.symmetric, NLGPU_ERR_UNSUPPORTED, "the learned correction needs a symmetric system");
     if (!c.local_ready) build_local(c);
-    if (!c.ilt.ok || c.ilt.n != c.local.rows) ilt_build(c, c.local, c.ilt);
+    if (!c.ilt.ok || c.ilt.n != c.local.rows || c.ilt.approximate) ilt_build(c, c.local, c.ilt);
     NL_REQUIRE(c.ilt.ok, NLGPU_ERR_NUMERICAL, "ILLT failed on the local matrix");
     if (!c.full.up_ok && c.full.val32.n != size_t(c.full.nnz))
         matrix_to_f32(c, c.full, c.fp32_symmetric ? &c.inner : nullptr);

@@ -446,7 +446,7 @@ void batch_prepare_mixed(Batch& bt) {
     }, false);
     bt.solver.stream = bt.stream;
     bt.solver.n_nodes = bt.N;
-    ilt_build(bt.solver, bt.M, bt.ic, false);
+    ilt_build(bt.solver, bt.M, bt.ic, false, true);
     NL_REQUIRE(bt.ic.ok, NLGPU_ERR_NUMERICAL, "the ILLT of the batched local matrix failed");
     matrix_to_f32(bt.solver, bt.A, nullptr);
     NL_REQUIRE(bt.A.col16_ok, NLGPU_ERR_UNSUPPORTED, "an instance's band is wider than 16-bit column offsets");
@@ -824,7 +824,7 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
         }, false);
         bt.solver.stream = bt.stream;
         bt.solver.n_nodes = N;
-        ilt_build(bt.solver, bt.M, bt.ic, false);
+        ilt_build(bt.solver, bt.M, bt.ic, false, true);
         illt = bt.ic.ok;   // the diagonal otherwise (as the reference)
     }
     dbuf<double> r0, v, s, t, y, z, dinv, acc;

@@ -281,6 +281,7 @@ struct IncompleteCholesky {
     dbuf<float> jc, jdinv;       // s_i / u_ii and 1 / u_ii
     dbuf<float> jt0, jt1, jy;    // Jacobi iterates and the scaled forward result
     bool ok = false;
+    bool approximate = false;    // factor from the fixed-point sweeps (ilt_build), not the exact IC(0)
     bool exact_ready = false;    // fwd / bwd slabs and plans built and filled (ilt_exact_layouts)
     int attempts = 0;
     double shift = 0.0;
@@ -510,7 +511,8 @@ void nonstationary_rhs(Ctx& ctx, double dirichlet_value, bool per_node_values, c
 void spmv_full(Ctx& ctx, const Csr& A, const double* x, double* y);
 // tma_plans: also build the TMA-fed shared-memory sweep plans of the exact
 // triangular solves (without them exact solves use the global-memory sweeps)
-void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plans = true);
+// approximate: the factor from a few fixed-point sweeps (for the FP32 Jacobi-sweep application)
+void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plans = true, bool approximate = false);
 void ilt_apply(Ctx& ctx, const IncompleteCholesky& ic, const double* r, double* z);
 // the exact sweeps' layouts of a factorised ILLT (once; before any stream capture)
 void ilt_exact_layouts(Ctx& ctx, IncompleteCholesky& ic);
@@ -559,7 +561,7 @@ void add_scaled(Ctx& ctx, double a, const double* x, double* y);
 void add_constant(Ctx& ctx, double a, double* y);
 // iltbuild.cu: U pattern copies, U^T, the factorisation's levels (offsets on the
 // host too) and the Jacobi sweeps' layouts, built on the device
-void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic);
+void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool levels = true);
 // jacobi.cu: the factor applied by Jacobi sweeps on its two triangles
 void jacobi_fill(Ctx& ctx, IncompleteCholesky& ic);
 void jacobi_apply32(Ctx& ctx, IncompleteCholesky& ic, int sweeps, const float* r, float* z, const double* flags);

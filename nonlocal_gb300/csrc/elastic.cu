@@ -462,7 +462,7 @@ CgResult elastic_solve(Ctx& ctx, const nlgpu_solve_options& o, nlgpu_solve_repor
     const int sweeps = o.triangular_sweeps == 0 ? NLGPU_DEFAULT_TRIANGULAR_SWEEPS : std::max(o.triangular_sweeps, 0);
     if (o.preconditioner == NLGPU_PRECONDITIONER_ILLT) {
         if (!el.local_ready) elastic_assemble(ctx, true);
-        ilt_build(ctx, el.local, el.ilt, !(mixed && sweeps > 0));
+        ilt_build(ctx, el.local, el.ilt, !(mixed && sweeps > 0), mixed && sweeps > 0);
         if (el.ilt.ok) M = &el.ilt;
     } else {
         el.ilt.ok = false;

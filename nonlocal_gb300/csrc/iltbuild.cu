@@ -171,7 +171,7 @@ void jacobi_slab_gpu(Ctx& ctx, i64 n, TriRows tr, const int32_t* cols, const i64
 
 // U pattern copies, U^T, the factorisation's rows in level order and the
 // Jacobi layouts, all on the device
-void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
+void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool levels) {
     const i64 n = upper.rows, nnz = upper.nnz;
     dbuf<int> bad;
     bad.resize(1);
@@ -196,23 +196,25 @@ void ilt_structure_gpu(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic) {
     NL_LAUNCH(k_transpose_place, grid_for(n, IB_THREADS), IB_THREADS, 0, ctx.stream, n, upper.rowptr.p, upper.col.p,
               ic.lrp.p, cursor.p, ic.lcol.p, ic.l_to_u.p);
     NL_LAUNCH(k_sort_rows, grid_for(n, IB_THREADS), IB_THREADS, 0, ctx.stream, n, ic.lrp.p, ic.lcol.p, ic.l_to_u.p);
-    // levels
-    dbuf<int> indeg;
-    indeg.resize(size_t(n));
-    ic.ic_rows.resize(size_t(n));
-    ic.ic_lev_ptr.resize(size_t(n + 1));
-    dbuf<i64> out;
-    out.resize(2);
-    NL_LAUNCH(k_levels, 1, IB_LEVEL_THREADS, 0, ctx.stream, n, ic.lrp.p, upper.rowptr.p, upper.col.p, indeg.p,
-              ic.ic_rows.p, ic.ic_lev_ptr.p, out.p);
-    i64 ho[2] = {0, 0};
+    // levels of the exact factorisation's schedule
+    i64 ho[2] = {0, n};
     int hbad = 0;
-    out.download(ho, 2, ctx.stream);
+    dbuf<int> indeg;
+    dbuf<i64> out;
+    if (levels) {
+        indeg.resize(size_t(n));
+        ic.ic_rows.resize(size_t(n));
+        ic.ic_lev_ptr.resize(size_t(n + 1));
+        out.resize(2);
+        NL_LAUNCH(k_levels, 1, IB_LEVEL_THREADS, 0, ctx.stream, n, ic.lrp.p, upper.rowptr.p, upper.col.p, indeg.p,
+                  ic.ic_rows.p, ic.ic_lev_ptr.p, out.p);
+        out.download(ho, 2, ctx.stream);
+    }
     NL_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof hbad, cudaMemcpyDeviceToHost, ctx.stream));
     NL_CUDA(cudaStreamSynchronize(ctx.stream));
     NL_REQUIRE(!hbad, NLGPU_ERR_ARG, "every row of the preconditioner matrix needs its diagonal first");
     NL_REQUIRE(ho[1] == n, NLGPU_ERR_STATE, "the factor's dependency graph does not reach every row");
-    ic.ic_levels = ho[0];
+    ic.ic_levels = levels ? ho[0] : 0;
     // Jacobi layouts of U^T (values u[l_to_u]) and U
     jacobi_slab_gpu(ctx, n, TriRows{ic.lrp.p, true}, ic.lcol.p, ic.l_to_u.p, ic.jlo);
     jacobi_slab_gpu(ctx, n, TriRows{ic.rp.p, false}, ic.col.p, nullptr, ic.jup);

@@ -237,7 +237,17 @@ __global__ void k_scaled(i64 n, const i64* __restrict__ rp, const int32_t* __res
 // the table's column y in the order of k, as the sequential form does
 // (product and subtraction rounded separately), so the result does not depend
 // on the schedule.
+//
+// SWEEP: one sweep of the fixed-point form of the same equations (Chow and
+// Patel, "Fine-grained parallel incomplete LU factorization", SISC 2015): every
+// row at once, reading the other rows' values of the previous sweep (uin) and
+// writing its own (u), with no order and no waits.  Started from the scaled
+// matrix's rows divided by the root of their diagonal, a few sweeps give a
+// factor that serves the FP32 Jacobi-sweep application as well as the exact
+// one, without the exact form's dependency chain (2 401 levels on the
+// 300x300 serendipity mesh, at a few microseconds each).
 constexpr int IC_WARPS = 8;
+constexpr int IC_SWEEPS = 3;
 constexpr int IC_MAXS = 16;
 constexpr unsigned long long IC_WAIT_LIMIT_NS = 2000000000ull;
 
@@ -261,22 +271,22 @@ __device__ __forceinline__ void st_release_gpu(int* p, int v) {
 // this SM may have cached the lines
 __device__ void ic0_row_sequential(int32_t i, const i64* __restrict__ rp, const int32_t* __restrict__ col,
                                    const double* __restrict__ a, double shift, const i64* __restrict__ lrp,
-                                   const int32_t* __restrict__ lcol, const i64* __restrict__ l_to_u, double* u,
-                                   int* __restrict__ failed) {
+                                   const int32_t* __restrict__ lcol, const i64* __restrict__ l_to_u,
+                                   const double* uin, double* u, int* __restrict__ failed) {
     const i64 b = rp[i], e = rp[i + 1];
     for (i64 s = b; s < e; ++s) u[s] = a[s];
     u[b] += shift;
     for (i64 s = lrp[i]; s < lrp[i + 1] - 1; ++s) {
         const int32_t k = lcol[s];
         const i64 pk = l_to_u[s];
-        const double uki = __ldcg(u + pk);
+        const double uki = __ldcg(uin + pk);
         i64 x = pk, y = b;
         const i64 ke = rp[k + 1];
         while (x < ke && y < e) {
             const int32_t cx = col[x], cy = col[y];
             if (cx < cy) ++x;
             else if (cx > cy) ++y;
-            else { u[y] = __dsub_rn(u[y], __dmul_rn(uki, __ldcg(u + x))); ++x; ++y; }
+            else { u[y] = __dsub_rn(u[y], __dmul_rn(uki, __ldcg(uin + x))); ++x; ++y; }
         }
     }
     const double d = u[b];
@@ -286,13 +296,14 @@ __device__ void ic0_row_sequential(int32_t i, const i64* __restrict__ rp, const 
     for (i64 s = b + 1; s < e; ++s) u[s] /= rd;
 }
 
+template<bool SWEEP>
 __global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t* __restrict__ order,
                                                             const i64* __restrict__ rp, const int32_t* __restrict__ col,
                                                             const double* __restrict__ a, double shift,
                                                             const i64* __restrict__ lrp,
                                                             const int32_t* __restrict__ lcol,
-                                                            const i64* __restrict__ l_to_u, double* u,
-                                                            int* __restrict__ ticket, int* done,
+                                                            const i64* __restrict__ l_to_u, const double* uin,
+                                                            double* u, int* __restrict__ ticket, int* done,
                                                             int* __restrict__ failed, int* __restrict__ timed_out) {
     __shared__ double table[IC_WARPS][IC_MAXS][32];
     __shared__ int32_t rowcol[IC_WARPS][32];
@@ -303,7 +314,7 @@ __global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t
         if (lane == 0) t = atomicAdd(ticket, 1);
         t = __shfl_sync(full, t, 0);
         if (t >= n) break;
-        const int32_t i = order[t];
+        const int32_t i = SWEEP ? int32_t(t) : order[t];
         const i64 b = rp[i], e = rp[i + 1];
         const int m = int(e - b);
         const i64 lb = lrp[i], le = lrp[i + 1] - 1;   // L row i without its diagonal (its last entry)
@@ -323,22 +334,23 @@ __global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t
             pk_first = l_to_u[lb + lane];
             len_first = int(rp[lcol[lb + lane] + 1] - pk_first);
         }
-        // wait for the rows this row reads
-        bool gave_up = false;
-        for (i64 s = lb + lane; s < le && !gave_up; s += 32) {
-            const int* flag = done + lcol[s];
-            if (ld_acquire_gpu(flag) == 0) {
-                const unsigned long long t0 = ic_globaltimer();
-                while (ld_acquire_gpu(flag) == 0) {
-                    if (ic_globaltimer() - t0 > IC_WAIT_LIMIT_NS) { gave_up = true; break; }
-                    __nanosleep(32);
+        if constexpr (!SWEEP) {   // wait for the rows this row reads
+            bool gave_up = false;
+            for (i64 s = lb + lane; s < le && !gave_up; s += 32) {
+                const int* flag = done + lcol[s];
+                if (ld_acquire_gpu(flag) == 0) {
+                    const unsigned long long t0 = ic_globaltimer();
+                    while (ld_acquire_gpu(flag) == 0) {
+                        if (ic_globaltimer() - t0 > IC_WAIT_LIMIT_NS) { gave_up = true; break; }
+                        __nanosleep(32);
+                    }
                 }
             }
+            if (__any_sync(full, gave_up) && lane == 0) atomicExch(timed_out, 1);
         }
-        if (__any_sync(full, gave_up) && lane == 0) atomicExch(timed_out, 1);
         __syncwarp();
         if (m > 32) {
-            if (lane == 0) ic0_row_sequential(i, rp, col, a, shift, lrp, lcol, l_to_u, u, failed);
+            if (lane == 0) ic0_row_sequential(i, rp, col, a, shift, lrp, lcol, l_to_u, uin, u, failed);
         } else {
             for (i64 s0 = lb; s0 < le; s0 += IC_MAXS) {
                 const int ns = le - s0 < IC_MAXS ? int(le - s0) : IC_MAXS;
@@ -350,7 +362,7 @@ __global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t
                     pk = l_to_u[s0 + lane];   // (k, i) in U: row k's segment from column i on
                     len = int(rp[lcol[s0 + lane] + 1] - pk);
                 }
-                if (lane < ns) uki = __ldcg(u + pk);
+                if (lane < ns) uki = __ldcg(uin + pk);
                 int incl = len;
                 for (int o = 1; o < 32; o <<= 1) {
                     const int v = __shfl_up_sync(full, incl, o);
@@ -375,7 +387,7 @@ __global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t
                             const int mid = (lo + hi) >> 1;
                             if (rowcol[wb][mid] < cx) lo = mid + 1; else hi = mid;
                         }
-                        if (lo < m && rowcol[wb][lo] == cx) table[wb][s][lo] = __dmul_rn(ukis, __ldcg(u + x));
+                        if (lo < m && rowcol[wb][lo] == cx) table[wb][s][lo] = __dmul_rn(ukis, __ldcg(uin + x));
                     }
                 }
                 __syncwarp();
@@ -393,9 +405,24 @@ __global__ void __launch_bounds__(IC_WARPS * 32) k_ic0_rows(i64 n, const int32_t
         }
         // publish row i (a failed pivot publishes too: the attempt is retried
         // with a larger shift, and no row may wait for ever)
-        __threadfence();
-        __syncwarp();
-        if (lane == 0) st_release_gpu(done + i, 1);
+        if constexpr (!SWEEP) {
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) st_release_gpu(done + i, 1);
+        }
+    }
+}
+
+// Starting factor of the fixed-point form: row i of the scaled matrix divided
+// by the root of its (shifted) diagonal
+__global__ void k_ic0_start(i64 n, const i64* __restrict__ rp, const double* __restrict__ a, double shift,
+                            double* __restrict__ u, int* __restrict__ failed) {
+    for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+        const double d = a[rp[i]] + shift;
+        if (!(d > 0.0)) { atomicExch(failed, 1); continue; }
+        const double rd = sqrt(d);
+        u[rp[i]] = rd;
+        for (i64 k = rp[i] + 1; k < rp[i + 1]; ++k) u[k] = a[k] / rd;
     }
 }
 
@@ -623,12 +650,13 @@ void ilt_exact_layouts(Ctx& ctx, IncompleteCholesky& ic) {
     timer.mark("value fills");
 }
 
-void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plans) {
+void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plans, bool approximate) {
     const i64 n = upper.rows, nnz = upper.nnz;
     ic.n = n; ic.nnz = nnz;
+    ic.approximate = approximate;
     PhaseTimer timer(ctx.stream, "ilt_build");
-    // U^T, the factorisation's levels and the Jacobi layouts on the device
-    ilt_structure_gpu(ctx, upper, ic);
+    // U^T, the factorisation's levels (exact form) and the Jacobi layouts on the device
+    ilt_structure_gpu(ctx, upper, ic, !approximate);
     timer.mark("structure");
     ctx.sweep_error.resize(1);
     ctx.sweep_error.zero(ctx.stream);
@@ -664,12 +692,29 @@ void ilt_build(Ctx& ctx, const Csr& upper, IncompleteCholesky& ic, bool tma_plan
     const double initial_shift = 1e-3;
     double shift = mindiag <= 0.0 ? initial_shift - mindiag : 0.0;
     ic.ok = false;
+    dbuf<double> u_prev;
+    if (approximate) u_prev.resize(size_t(nnz));
     for (ic.attempts = 1; ic.attempts <= 10; ++ic.attempts) {
         failed.zero(ctx.stream);
-        sync.zero(ctx.stream);
-        NL_LAUNCH(k_ic0_rows, ic_grid, IC_WARPS * 32, 0, ctx.stream, n, ic.ic_rows.p, ic.rp.p, ic.col.p,
-                  ic.a_scaled.p, shift, ic.lrp.p, ic.lcol.p, ic.l_to_u.p, ic.u.p, sync.p, sync.p + 1, failed.p,
-                  failed.p + 1);
+        if (approximate) {
+            // the sweeps alternate between the two buffers and end in ic.u
+            double* buf[2] = {IC_SWEEPS % 2 ? u_prev.p : ic.u.p, IC_SWEEPS % 2 ? ic.u.p : u_prev.p};
+            NL_LAUNCH(k_ic0_start, grid_for(n, 256), 256, 0, ctx.stream, n, ic.rp.p, ic.a_scaled.p, shift, buf[0],
+                      failed.p);
+            const unsigned sweep_grid = unsigned(std::max<i64>(1, std::min<i64>((n + IC_WARPS - 1) / IC_WARPS, 152 * 16)));
+            for (int sw = 0; sw < IC_SWEEPS; ++sw) {
+                sync.zero(ctx.stream);   // the sweep's row ticket
+                NL_LAUNCH(k_ic0_rows<true>, sweep_grid, IC_WARPS * 32, 0, ctx.stream, n,
+                          static_cast<const int32_t*>(nullptr), ic.rp.p, ic.col.p, ic.a_scaled.p, shift, ic.lrp.p,
+                          ic.lcol.p, ic.l_to_u.p, buf[sw & 1], buf[(sw + 1) & 1], sync.p, sync.p + 1, failed.p,
+                          failed.p + 1);
+            }
+        } else {
+            sync.zero(ctx.stream);
+            NL_LAUNCH(k_ic0_rows<false>, ic_grid, IC_WARPS * 32, 0, ctx.stream, n, ic.ic_rows.p, ic.rp.p, ic.col.p,
+                      ic.a_scaled.p, shift, ic.lrp.p, ic.lcol.p, ic.l_to_u.p, ic.u.p, ic.u.p, sync.p, sync.p + 1,
+                      failed.p, failed.p + 1);
+        }
         int hf[2] = {0, 0};
         NL_CUDA(cudaMemcpyAsync(hf, failed.p, sizeof hf, cudaMemcpyDeviceToHost, ctx.stream));
         NL_CUDA(cudaStreamSynchronize(ctx.stream));
