@@ -3,22 +3,29 @@
 //
 //   C[M x N] = A[M x K] . B[N x K]^T      A, B: BF16, K contiguous (K-major)
 //
-// One CTA (128 threads) owns a 128-row tile of C and all N <= 128 columns:
-//   * the A tile (128 x 64) and B tile (N x 64) of each K step are copied by
-//     the threads (16-byte loads) into shared memory in the canonical
-//     no-swizzle K-major layout: 8x8 "core matrices" of 128 contiguous bytes,
-//     K-adjacent core matrices 128 B apart (LBO), 8-row groups 1024 B apart
-//     (SBO);
+// A CTA (128 threads) takes 128-row tiles of C (all N <= 128 columns) in
+// turn, and each tile's K steps of 64:
+//   * the A tile (128 x 64) and B tile (N x 64) of a step are copied by the
+//     threads with 16-byte cp.async (asynchronous, zero-filled past the ends)
+//     into shared memory in the canonical no-swizzle K-major layout: 8x8 "core
+//     matrices" of 128 contiguous bytes, K-adjacent core matrices 128 B apart
+//     (LBO), 8-row groups 1024 B apart (SBO); consecutive threads fill
+//     consecutive 16-byte rows of a core matrix, so the stores do not collide
+//     in the banks.  Two stages: the copies of the next step are in flight
+//     while the tensor cores run the current one;
 //   * one thread issues four tcgen05.mma.cta_group::1.kind::f16 (M = 128,
 //     N, K = 16 each) accumulating in FP32 in tensor memory, and commits them
 //     to an mbarrier that every thread waits on (bounded by %globaltimer);
-//   * the epilogue reads the accumulator with tcgen05.ld (warp w reads lanes
-//     32w..32w+31, i.e. rows) and applies one of the epilogues below.
-// Rows beyond M and K beyond the end are loaded as zeros.  Split-K launches
-// (gridDim.y > 1) add their partial products with FP32 atomics.
+//   * after a tile's last step the epilogue reads the accumulator with
+//     tcgen05.ld (warp w reads lanes 32w..32w+31, i.e. rows) and applies one
+//     of the epilogues below.
+// Split-K launches (gridDim.y > 1) add their partial products with FP32
+// atomics.
 #include "common.cuh"
 
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 namespace nlgpu {
 
@@ -60,23 +67,22 @@ __device__ __forceinline__ bool tg_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// copies rows [row0, row0 + rows) x K range [k0, k0 + 64) of a K-major BF16
-// matrix (leading dimension ld elements) into the core-matrix layout; zeros
-// outside [0, nrows) x [0, kmax)
+// starts the copies of rows [row0, row0 + rows) x K range [k0, k0 + 64) of a
+// K-major BF16 matrix (leading dimension ld elements) into the core-matrix
+// layout; zeros outside [0, nrows) x [0, kmax) (cp.async zero-fills what its
+// source size leaves out)
 __device__ __forceinline__ void tg_load_tile(unsigned char* dst, const __nv_bfloat16* __restrict__ src, i64 ld,
                                              i64 row0, int rows, i64 nrows, i64 k0, i64 kmax) {
     const int chunks = rows * (TG_KT / 8);
     for (int c = threadIdx.x; c < chunks; c += TG_THREADS) {
-        const int r = c >> 3, kg = c & 7;
+        const int rl = c & 7, kg = (c >> 3) & 7, rh = c >> 6;   // row rh * 8 + rl, K group kg
+        const int r = rh * 8 + rl;
         const i64 gr = row0 + r, gk = k0 + kg * 8;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (gr < nrows && gk + 8 <= kmax) v = *reinterpret_cast<const uint4*>(src + gr * ld + gk);
-        else if (gr < nrows && gk < kmax) {
-            __nv_bfloat16 tmp[8];
-            for (int e = 0; e < 8; ++e) tmp[e] = gk + e < kmax ? src[gr * ld + gk + e] : __float2bfloat16(0.0f);
-            v = *reinterpret_cast<const uint4*>(tmp);
-        }
-        *reinterpret_cast<uint4*>(dst + (r >> 3) * TG_SBO + kg * TG_LBO + (r & 7) * 16) = v;
+        int bytes = 0;
+        if (gr < nrows && gk < kmax) bytes = int(kmax - gk >= 8 ? 16 : (kmax - gk) * 2);
+        const __nv_bfloat16* g = bytes ? src + gr * ld + gk : src;
+        const uint32_t d = tg_smem(dst + rh * TG_SBO + kg * TG_LBO + rl * 16);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(g), "r"(bytes) : "memory");
     }
 }
 
@@ -101,9 +107,8 @@ struct TgArgs {
 template<int N, int EPI>
 __global__ void __launch_bounds__(TG_THREADS) k_tc_gemm(TgArgs a) {
     static_assert(N % 16 == 0 && N >= 16 && N <= 128, "N");
+    constexpr int STAGE = (128 + N) * TG_KT * 2;          // A tile then B tile
     extern __shared__ __align__(1024) unsigned char tg_smem_buf[];
-    unsigned char* tileA = tg_smem_buf;                    // 16 KB
-    unsigned char* tileB = tg_smem_buf + 128 * TG_KT * 2;  // N x 64 x 2 B
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_base_slot;
     __shared__ int failed;
@@ -123,24 +128,41 @@ __global__ void __launch_bounds__(TG_THREADS) k_tc_gemm(TgArgs a) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_slot;
-    const i64 row0 = i64(blockIdx.x) * 128;
     const i64 kbeg = i64(blockIdx.y) * a.k_per_split;
     const i64 kend = kbeg + a.k_per_split < a.K ? kbeg + a.k_per_split : a.K;
+    const i64 steps = kend > kbeg ? (kend - kbeg + TG_KT - 1) / TG_KT : 0;
+    const i64 tiles = (a.M + 127) / 128;
+    const i64 my_tiles = i64(blockIdx.x) < tiles ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const i64 items = my_tiles * steps;   // (tile, step) pairs of this CTA, tile-major
+    auto load = [&](i64 item) {
+        const i64 tile = i64(blockIdx.x) + (item / steps) * gridDim.x;
+        const i64 k0 = kbeg + (item % steps) * TG_KT;
+        unsigned char* st = tg_smem_buf + (item & 1) * STAGE;
+        tg_load_tile(st, a.A, a.lda, tile * 128, 128, a.M, k0, kend);
+        tg_load_tile(st + 128 * TG_KT * 2, a.B, a.ldb, 0, N, N, k0, kend);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
     uint32_t phase = 0;
-    bool first = true;
-    for (i64 k0 = kbeg; k0 < kend; k0 += TG_KT) {
-        tg_load_tile(tileA, a.A, a.lda, row0, 128, a.M, k0, kend);
-        tg_load_tile(tileB, a.B, a.ldb, 0, N, N, k0, kend);
+    if (items > 0) load(0);
+    for (i64 it = 0; it < items && !failed; ++it) {
+        // the next step's copies go out before this step's wait
+        if (it + 1 < items) {
+            load(it + 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        const i64 step = it % steps;
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa = tg_smem(tileA), sb = tg_smem(tileB);
+            const uint32_t sa = tg_smem(tg_smem_buf + (it & 1) * STAGE), sb = sa + 128 * TG_KT * 2;
 #pragma unroll
             for (int j = 0; j < TG_KT / 16; ++j) {
                 const uint64_t da = tg_desc(sa + uint32_t(j) * 2 * TG_LBO);
                 const uint64_t db = tg_desc(sb + uint32_t(j) * 2 * TG_LBO);
-                const uint32_t acc = (first && j == 0) ? 0u : 1u;
+                const uint32_t acc = (step == 0 && j == 0) ? 0u : 1u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
                     "setp.ne.b32 p, %4, 0;\n\t"
@@ -151,8 +173,7 @@ __global__ void __launch_bounds__(TG_THREADS) k_tc_gemm(TgArgs a) {
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          ::"r"(tg_smem(&bar)) : "memory");
         }
-        first = false;
-        // every thread waits for the MMAs (the tiles are rewritten next step)
+        // every thread waits for the MMAs: their stage is refilled two steps on
         if (!tg_try_wait(&bar, phase)) {
             const unsigned long long t0 = tg_time();
             while (!tg_try_wait(&bar, phase)) {
@@ -162,10 +183,11 @@ __global__ void __launch_bounds__(TG_THREADS) k_tc_gemm(TgArgs a) {
         phase ^= 1u;
         __syncthreads();
         if (failed) break;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!failed && kend > kbeg) {
-        const i64 row = row0 + warp * 32 + lane;
+        if (step != steps - 1) continue;
+        // the tile's epilogue
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const i64 tile = i64(blockIdx.x) + (it / steps) * gridDim.x;
+        const i64 row = tile * 128 + warp * 32 + lane;
 #pragma unroll
         for (int c0 = 0; c0 < N; c0 += 16) {
             uint32_t v[16];
@@ -194,7 +216,11 @@ __global__ void __launch_bounds__(TG_THREADS) k_tc_gemm(TgArgs a) {
                 }
             }
         }
+        // the accumulator is read before the next tile's first MMA overwrites it
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -204,13 +230,15 @@ __global__ void __launch_bounds__(TG_THREADS) k_tc_gemm(TgArgs a) {
 
 template<int N, int EPI>
 static void launch_tc_gemm(Ctx& ctx, const TgArgs& a, int splits) {
-    const size_t smem = size_t(128 + N) * TG_KT * 2;
+    const size_t smem = 2 * size_t(128 + N) * TG_KT * 2;   // two stages
     static bool attr = false;
     if (!attr) {
         NL_CUDA(cudaFuncSetAttribute(k_tc_gemm<N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         attr = true;
     }
-    const dim3 grid(unsigned((a.M + 127) / 128), unsigned(splits));
+    // at most four CTAs per SM (tensor memory and shared memory), taking the tiles in turn
+    const i64 tiles = (a.M + 127) / 128;
+    const dim3 grid(unsigned(std::min<i64>(tiles, i64(152) * 4 / std::max(1, splits) + 1)), unsigned(splits));
     NL_LAUNCH((k_tc_gemm<N, EPI>), grid, TG_THREADS, smem, ctx.stream, a);
 }
 
