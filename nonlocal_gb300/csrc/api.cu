@@ -18,6 +18,7 @@ thread_local std::string g_last_error;
 
 template<class F>
 int guarded(F&& f) {
+    g_last_error.clear();
     try {
         f();
         return NLGPU_OK;
@@ -31,6 +32,15 @@ int guarded(F&& f) {
         g_last_error = e.what();
         return NLGPU_ERR_ARG;
     }
+}
+
+// the status of a solve entry: its error, else NLGPU_ERR_NO_CONVERGENCE (with a
+// message) when the solve ended before the tolerance
+int solve_status(int rc, int conv_status) {
+    if (rc != NLGPU_OK) return rc;
+    if (conv_status == NLGPU_ERR_NO_CONVERGENCE)
+        g_last_error = "the solve stopped before the tolerance (iteration limit or a stalled recurrence)";
+    return conv_status;
 }
 
 double ipow_host(double x, int n) {
@@ -239,7 +249,7 @@ CgResult solve_system(Ctx& c, const nlgpu_solve_options& o, nlgpu_solve_report* 
         timer.mark("coarse correction");
         c.ilt_sweeps = sweeps;
         r = mixed_solve(c, c.full, M ? &c.ilt : nullptr, b, c.temperature.p, o.tolerance, o.max_iterations,
-                        o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, learned && M && c.mp.use,
+                        o.inner_tolerance > 0.0 ? o.inner_tolerance : MIXED_UPDATE_FACTOR, false, learned && M && c.mp.use,
                         c.ilt_sweeps, coarse && c.co.ready);
         if (learned && M && c.mp.use) mpnn_check(c);
         if (learned && !(M && c.mp.use)) r.learned_fallback = true;   // gated off: ILLT alone
@@ -746,7 +756,7 @@ int nlgpu_solve_assembled(nlgpu_ctx* ctx, const nlgpu_solve_options* options, do
         if (report) report->seconds_total = seconds(t0);
         if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
     });
-    return rc != NLGPU_OK ? rc : conv_status;
+    return solve_status(rc, conv_status);
 }
 
 int nlgpu_solve_assembled_batch(int64_t count, nlgpu_ctx* const* instances, const nlgpu_solve_options* options,
@@ -792,7 +802,7 @@ int nlgpu_solve_assembled_batch(int64_t count, nlgpu_ctx* const* instances, cons
             if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
         }
     });
-    return rc != NLGPU_OK ? rc : conv_status;
+    return solve_status(rc, conv_status);
 }
 
 int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, double* temperature,
@@ -849,7 +859,7 @@ int nlgpu_stationary_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* options, doub
         rep->seconds_total = seconds(t_all);
         if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
     });
-    return rc != NLGPU_OK ? rc : conv_status;
+    return solve_status(rc, conv_status);
 }
 
 int nlgpu_cg_solve(nlgpu_ctx* ctx, int64_t n, const int64_t* a_rowptr, const int64_t* a_col, const double* a_val,
@@ -921,7 +931,7 @@ int nlgpu_cg_solve(nlgpu_ctx* ctx, int64_t n, const int64_t* a_rowptr, const int
         }
         if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
     });
-    return rc != NLGPU_OK ? rc : conv_status;
+    return solve_status(rc, conv_status);
 }
 
 int nlgpu_illt_compute(nlgpu_ctx* ctx, int64_t n, const int64_t* rowptr, const int64_t* col, const double* val,
@@ -1139,7 +1149,7 @@ int nlgpu_nonstationary_2d_step(nlgpu_ctx* ctx, double dirichlet_value, const do
         if (iterations) *iterations = r.iterations;
         if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
     });
-    return rc != NLGPU_OK ? rc : conv_status;
+    return solve_status(rc, conv_status);
 }
 
 struct nlgpu_batch {
@@ -1374,7 +1384,7 @@ int nlgpu_equilibrium_equation_2d(nlgpu_ctx* ctx, const nlgpu_solve_options* opt
         if (report) report->seconds_total = seconds(t0);
         if (!r.converged) conv_status = NLGPU_ERR_NO_CONVERGENCE;
     });
-    return rc != NLGPU_OK ? rc : conv_status;
+    return solve_status(rc, conv_status);
 }
 
 int nlgpu_cg_solve_noalloc(void* stream, int64_t n, const int64_t* d_rowptr, const int32_t* d_col, const double* d_val,
@@ -1387,7 +1397,7 @@ int nlgpu_cg_solve_noalloc(void* stream, int64_t n, const int64_t* d_rowptr, con
                               max_iterations, iterations, residual))
             conv_status = NLGPU_ERR_NO_CONVERGENCE;
     });
-    return rc != NLGPU_OK ? rc : conv_status;
+    return solve_status(rc, conv_status);
 }
 
 int nlgpu_set_option(nlgpu_ctx* ctx, int option, int value) {

@@ -474,7 +474,7 @@ i64 batch_solve_mixed(Batch& bt, double tolerance, i64 max_iterations, i64* iter
         return 0;
     }
     const double tol_g = tolerance * std::sqrt(smallest / total);
-    CgResult r = mixed_solve(bt.solver, bt.A, &bt.ic, bt.b.p, bt.x.p, tol_g, max_iterations, 1e-2, true, false,
+    CgResult r = mixed_solve(bt.solver, bt.A, &bt.ic, bt.b.p, bt.x.p, tol_g, max_iterations, MIXED_UPDATE_FACTOR, true, false,
                              NLGPU_DEFAULT_TRIANGULAR_SWEEPS, false);
     bt.last_fallback = !r.converged;
     if (!r.converged) r = cg_solve(bt.solver, bt.A, &bt.ic, bt.b.p, bt.x.p, tol_g, max_iterations, true);

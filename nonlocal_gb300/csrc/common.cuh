@@ -257,6 +257,10 @@ struct SweepPlan {
 
 // CG reduction layout shared by the solver kernels
 constexpr int RED_BLOCKS = 152 * 4;   // blocks of every reducing kernel (one partial each)
+// default drop of the FP32 residual between the mixed solve's FP64 reliable updates
+// (1e-3 saved two updates and 5 ms on the 300x300 serendipity problem but
+// stalled the FP32 recurrence of a pure Neumann problem)
+constexpr double MIXED_UPDATE_FACTOR = 1e-2;
 enum { S_BB = 0, S_RZ0 = 1, S_DONE = 2, S_ITERS = 3, S_RR_FINAL = 4 };   // scalar slots
 enum { P_PQ = 0, P_RR = 1, P_RZ_A = 2, P_RZ_B = 3, P_BB = 4, P_COUNT = 5 };   // partial buffers
 

@@ -473,7 +473,7 @@ CgResult elastic_solve(Ctx& ctx, const nlgpu_solve_options& o, nlgpu_solve_repor
     if (mixed) {
         matrix_to_f32(ctx, el.full);
         r = mixed_solve(ctx, el.full, M ? &el.ilt : nullptr, el.rhs.p, el.displacement.p, o.tolerance,
-                        o.max_iterations, o.inner_tolerance > 0.0 ? o.inner_tolerance : 1e-2, false, false, sweeps);
+                        o.max_iterations, o.inner_tolerance > 0.0 ? o.inner_tolerance : MIXED_UPDATE_FACTOR, false, false, sweeps);
     } else {
         r = cg_solve(ctx, el.full, M, el.rhs.p, el.displacement.p, o.tolerance, o.max_iterations, false);
     }

@@ -469,6 +469,10 @@ __global__ void __launch_bounds__(MX_THREADS) k_update_dr32(i64 n, float* __rest
     p += slot * n;
     q += slot * n;
     const float alpha = float(flags[S_ALPHA]);
+    if (!isfinite(alpha)) {   // p.q vanished in FP32 (breakdown): end the cycle, the reliable update restarts it
+        if (blockIdx.x == 0 && threadIdx.x == 0) flags[S_DONE] = 1.0;
+        return;
+    }
     float s = 0.0f;   // a thread's one or two elements in FP32; block and global sums in FP64
     for (i64 i = blockIdx.x * i64(blockDim.x) + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
         d[i] += alpha * p[i];
@@ -755,6 +759,7 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
     NL_LAUNCH(k_sum_to, 1, MX_THREADS, 0, ctx.stream, part + P_RZ_B * RED_BLOCKS, flags + S_PR);
     const double cap = double(std::min<i64>(max_iterations, i64(1) << 40));
     double last_rr = hs[1];
+    int stalled = 0;
     i64 k = 0;
     i64 iters_at_update = 0;
     // one iteration k (k read on the device): q_j = A p_j (j = k mod MX_M) and
@@ -826,6 +831,9 @@ CgResult mixed_solve(Ctx& ctx, const Csr& A, IncompleteCholesky* M, const double
         res.residual = std::sqrt(hs[1] / hs[0]);
         if (hs[1] <= tolerance * tolerance * hs[0]) { res.converged = true; break; }
         if (res.iterations >= max_iterations || !std::isfinite(hs[1])) break;
+        // five updates in a row without progress: the recurrence has stalled
+        stalled = hs[1] >= last_rr ? stalled + 1 : 0;
+        if (stalled >= 5) break;
         // the learned correction must buy at least a factor 10 per update interval,
         // or the rest of the solve runs with ILLT alone
         if (learned && hs[1] > 1e-2 * last_rr) { learned = false; res.learned_fallback = true; }
