@@ -58,3 +58,20 @@ def test_no_device_is_reported_cleanly(built):
     assert lib.nlgpu_create(ctypes.byref(h), None) == 2   # NLGPU_ERR_CUDA
     assert lib.nlgpu_status_string(2) == b"CUDA error"
     assert lib.nlgpu_mesh_2d(None, 2, 0, None, 0, None) == 1   # NLGPU_ERR_ARG
+
+
+def test_batched_solve_checks_its_arguments(built):
+    """nlgpu_solve_assembled_batch rejects a negative count and missing arrays
+    before touching a device, and an empty batch is a no-op."""
+    import ctypes
+    from nonlocal_gb300 import _lib
+    lib = _lib.load(built)
+    opts = _lib.SolveOptions()
+    opts.tolerance, opts.max_iterations = 1e-10, 100
+    assert lib.nlgpu_solve_assembled_batch(-1, None, ctypes.byref(opts), None, None) == 1   # NLGPU_ERR_ARG
+    assert lib.nlgpu_solve_assembled_batch(2, None, ctypes.byref(opts), None, None) == 1
+    handles = (ctypes.c_void_p * 1)(None)
+    outs = (ctypes.c_void_p * 1)(None)
+    assert lib.nlgpu_solve_assembled_batch(1, handles, ctypes.byref(opts), outs, None) == 1   # null context
+    assert lib.nlgpu_solve_assembled_batch(0, None, ctypes.byref(opts), None, None) == 0
+    assert lib.nlgpu_solve_assembled_batch(0, None, None, None, None) == 1   # options are required
