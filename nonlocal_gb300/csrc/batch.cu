@@ -811,7 +811,8 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
     row_blocks(bt, bt.A, bt.blocks_A, bt.nblocks_A);
     // the local ILLT preconditioner: p1 K_local of every instance (symmetric also with a
     // conductivity field: the field enters at the element's own quadrature points),
-    // block-diagonal, factored by the single-system IC(0) and applied by FP32 Jacobi sweeps
+    // block-diagonal, factored by the fixed-point form of IC(0) (rebuilt with every
+    // batch) and applied by FP32 Jacobi sweeps
     if (illt) {
         std::vector<Csr> local(instances.size());
         for (size_t k = 0; k < instances.size(); ++k) {
