@@ -796,6 +796,7 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
     bt.inst = instances;
     bt.K = i64(instances.size());
     bt.row_off.assign(size_t(bt.K + 1), 0);
+    PhaseTimer timer(bt.stream, "batch_bicgstab");
     for (i64 k = 0; k < bt.K; ++k) {
         Ctx& c = *instances[size_t(k)];
         NL_REQUIRE(c.inner_ready && !c.symmetric && c.full.rows == c.n_nodes, NLGPU_ERR_STATE,
@@ -809,6 +810,7 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
     bt.inst_of_row.resize(size_t(N));
     concat(bt, bt.A, [](Ctx& c) -> const Csr& { return c.full; }, true);
     row_blocks(bt, bt.A, bt.blocks_A, bt.nblocks_A);
+    timer.mark("concatenation, row blocks");
     // the local ILLT preconditioner: p1 K_local of every instance (symmetric also with a
     // conductivity field: the field enters at the element's own quadrature points),
     // block-diagonal, factored by the fixed-point form of IC(0) (rebuilt with every
@@ -829,6 +831,7 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
         bt.solver.n_nodes = N;
         ilt_build(bt.solver, bt.M, bt.ic, false, true);
         illt = bt.ic.ok;   // the diagonal otherwise (as the reference)
+        timer.mark("local matrices, ILLT");
     }
     dbuf<double> r0, v, s, t, y, z, dinv, acc;
     dbuf<float> in32, out32;
@@ -846,6 +849,7 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
         in32.zero(bt.stream);
         precondition(y.p);
     }
+    timer.mark("vectors");
     for (i64 k = 0; k < K; ++k) {
         Ctx& c = *instances[size_t(k)];
         NL_CUDA(cudaMemcpyAsync(bt.b.p + bt.row_off[size_t(k)], c.rhs.p, size_t(c.n_nodes) * sizeof(double),
@@ -926,6 +930,7 @@ std::vector<CgResult> batch_bicgstab(const std::vector<Ctx*>& instances, double 
             fin[size_t(k)] = final ? 1.0 : 0.0;
             all = all && final;
         }
+        timer.mark("round");
         if (all) break;
         NL_CUDA(cudaMemcpyAsync(sc + BB_FIN * K, fin.data(), size_t(K) * sizeof(double), cudaMemcpyHostToDevice, bt.stream));
     }
