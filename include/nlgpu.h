@@ -522,14 +522,19 @@ int nlgpu_stationary_1d(nlgpu_ctx* ctx, int64_t elements, int order, double leng
 /* ---- nonstationary_heat_equation_solver_1d (nonstationary_heat_equation_solver_1d.hpp:24-259)
  * compute: one segment [0, length] as nlgpu_stationary_1d, constant capacity
  * and density, implicit Euler step time_step; left_kind / right_kind
- * NLGPU_BC_TEMPERATURE or NLGPU_BC_FLUX; initial_temperature [n] or NULL
- * (zero), n = elements * order + 1.  Assembles dt K + C (C the capacity
+ * NLGPU_BC_TEMPERATURE, NLGPU_BC_FLUX or NLGPU_BC_CONVECTION (convection_1d,
+ * thermal_boundary_conditions_1d.hpp:36-55: its heat transfer coefficient set
+ * before by nlgpu_nonstationary_1d_convection); initial_temperature [n] or
+ * NULL (zero), n = elements * order + 1.  Assembles dt K + C (C the capacity
  * matrix; a temperature end's row and column routed out with a unit
- * diagonal, as the reference) and factors it once.
- * step: calc_step with the ends' values (temperature or flux as set at
- * compute) and the sin(pi x) source when sin_source; f = dt (flux + source) +
- * C T_prev, first kind, solve; temperature [n] receives the new temperature
- * (or NULL).  temperature: the current temperature. */
+ * diagonal, a convection end's diagonal + dt h, as the reference) and factors
+ * it once.
+ * step: calc_step with the ends' values (temperature, flux, or a convection
+ * end's ambient temperature, as set at compute) and the sin(pi x) source when
+ * sin_source; f = dt (flux or h T_ambient + source) + C T_prev, first kind,
+ * solve; temperature [n] receives the new temperature (or NULL).
+ * temperature: the current temperature. */
+int nlgpu_nonstationary_1d_convection(nlgpu_ctx* ctx, double heat_transfer_left, double heat_transfer_right);
 int nlgpu_nonstationary_1d_compute(nlgpu_ctx* ctx, int64_t elements, int order, double length, double radius,
                                    double local_weight, int influence, double conductivity, double capacity,
                                    double density, double time_step, int left_kind, int right_kind,

@@ -149,6 +149,7 @@ SIGNATURES = {
     "nlgpu_stationary_1d": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_int, c_p]),
     "nlgpu_nonstationary_1d_compute": (c_int, [c_p, c_i64, c_int, c_d, c_d, c_d, c_int, c_d, c_d, c_d, c_d, c_int,
                                                c_int, c_p, ctypes.POINTER(c_i64)]),
+    "nlgpu_nonstationary_1d_convection": (c_int, [c_p, c_d, c_d]),
     "nlgpu_nonstationary_1d_step": (c_int, [c_p, c_d, c_d, c_int, c_p]),
     "nlgpu_nonstationary_1d_temperature": (c_int, [c_p, c_p]),
     "nlgpu_set_elastic_2d": (c_int, [c_p, c_int, c_p, c_p]),

@@ -1236,6 +1236,13 @@ int nlgpu_nonstationary_1d_compute(nlgpu_ctx* ctx, int64_t elements, int order, 
     });
 }
 
+int nlgpu_nonstationary_1d_convection(nlgpu_ctx* ctx, double heat_transfer_left, double heat_transfer_right) {
+    if (!ctx || !(heat_transfer_left >= 0.0) || !(heat_transfer_right >= 0.0)) return NLGPU_ERR_ARG;
+    ctx->od_heat_transfer[0] = heat_transfer_left;
+    ctx->od_heat_transfer[1] = heat_transfer_right;
+    return NLGPU_OK;
+}
+
 int nlgpu_nonstationary_1d_step(nlgpu_ctx* ctx, double left_value, double right_value, int sin_source,
                                 double* temperature) {
     if (!ctx) return NLGPU_ERR_ARG;

@@ -447,6 +447,7 @@ struct Ctx {
     Coarse co;
     Elastic el;
     std::shared_ptr<OneDimState> od;
+    double od_heat_transfer[2] = {0.0, 0.0};   // 1D convection ends (nlgpu_nonstationary_1d_convection)
     MixedWork mx;
     BicgWork bi;
     Mpnn mp;

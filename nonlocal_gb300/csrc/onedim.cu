@@ -62,6 +62,8 @@ struct Problem1d {
     double h, jac, r, p1, lambda, norm;
     int kind;                  // 0 bell, 1 triangle, 2 normal, 3 constant
     int fk0, fk1;              // temperature (first kind) at the left / right end
+    int cv0, cv1;              // convection at the left / right end
+    double h0, h1;             // their heat transfer coefficients
 };
 
 // influence_functions_1d.hpp:10-75
@@ -217,17 +219,26 @@ __global__ void k_capacity_1d(Problem1d P, Line L, double factor, double* __rest
     }
 }
 
-// A = dt K + C over the band, unit diagonal at first-kind ends (C too), bound vectors x dt
+// A = dt K + C over the band, unit diagonal at first-kind ends (C too), bound
+// vectors x dt; a convection end adds dt h to its diagonal (K gets h before the
+// time step factor: convection_condition_1d.hpp:10-14,
+// nonstationary_heat_equation_solver_1d.hpp:167-178).  The ends' diagonals are
+// set by the thread of their band element.
 __global__ void k_combine_1d(Problem1d P, double dt, double* __restrict__ a, double* __restrict__ c,
                              double* __restrict__ bound0, double* __restrict__ boundN) {
     const i64 w = P.bw + 1, last = P.n - 1;
     for (i64 t = blockIdx.x * i64(blockDim.x) + threadIdx.x; t < P.n * w; t += i64(gridDim.x) * blockDim.x) {
-        a[t] = dt * a[t] + c[t];
+        double v = dt * a[t] + c[t];
+        if (t == 0) {
+            if (P.fk0) { v = 1.0; c[0] = 1.0; }
+            else if (P.cv0) v += dt * P.h0;
+        }
+        if (t == last * w) {
+            if (P.fk1) { v = 1.0; c[t] = 1.0; }
+            else if (P.cv1) v += dt * P.h1;
+        }
+        a[t] = v;
         if (t < P.n) { bound0[t] *= dt; boundN[t] *= dt; }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (P.fk0) { a[0] = 1.0; c[0] = 1.0; }
-        if (P.fk1) { a[last * w] = 1.0; c[last * w] = 1.0; }
     }
 }
 
@@ -243,9 +254,9 @@ __global__ void k_step_loads_1d(Problem1d P, Line L, double q_left, double q_rig
             integral += L.w[q] * L.qN[i * L.nq + q] * sin(std::numbers::pi * (P.h * double(e) + (L.x[q] - (-1.0)) * P.jac));
         atomicAdd(f + e * P.order + i, integral * P.jac);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (!P.fk0) atomicAdd(f, q_left);
-        if (!P.fk1) atomicAdd(f + P.n - 1, q_right);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // a convection end's value is its ambient temperature
+        if (!P.fk0) atomicAdd(f, P.cv0 ? P.h0 * q_left : q_left);
+        if (!P.fk1) atomicAdd(f + P.n - 1, P.cv1 ? P.h1 * q_right : q_right);
     }
 }
 
@@ -335,13 +346,17 @@ void nonstationary_1d_compute(Ctx& ctx, i64 elements, int order, double length, 
     NL_REQUIRE(elements > 0 && (order == 1 || order == 2) && length > 0.0 && time_step > 0.0, NLGPU_ERR_ARG,
                "invalid 1D mesh or time step");
     for (const int k : {left_kind, right_kind})
-        NL_REQUIRE(k == NLGPU_BC_TEMPERATURE || k == NLGPU_BC_FLUX, NLGPU_ERR_UNSUPPORTED,
-                   "1D ends take a temperature or a flux");
+        NL_REQUIRE(k == NLGPU_BC_TEMPERATURE || k == NLGPU_BC_FLUX || k == NLGPU_BC_CONVECTION, NLGPU_ERR_UNSUPPORTED,
+                   "1D ends take a temperature, a flux or a convection");
     auto st = std::make_shared<OneDimState>();
     Problem1d& P = st->P;
     P = make_problem_1d(elements, order, length, radius, local_weight, influence, conductivity);
     P.fk0 = left_kind == NLGPU_BC_TEMPERATURE;
     P.fk1 = right_kind == NLGPU_BC_TEMPERATURE;
+    P.cv0 = left_kind == NLGPU_BC_CONVECTION;
+    P.cv1 = right_kind == NLGPU_BC_CONVECTION;
+    P.h0 = P.cv0 ? ctx.od_heat_transfer[0] : 0.0;
+    P.h1 = P.cv1 ? ctx.od_heat_transfer[1] : 0.0;
     st->L = make_line(order);
     st->dt = time_step;
     const size_t n = size_t(P.n), nb = size_t(P.n * (P.bw + 1));

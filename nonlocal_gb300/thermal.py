@@ -780,10 +780,12 @@ INFLUENCE_1D = {"bell": 0, "triangle": 1, "normal": 2, "constant": 3}
 
 class NonstationaryHeatEquationSolver1D:
     """nonstationary_heat_equation_solver_1d<T, I> on one segment [0, length]:
-    ``compute(left, right, initial)`` with each end ("temperature", value) or
-    ("flux", value) (the kinds are fixed by compute, as the reference's matrix
-    portrait), then ``calc_step(left_value, right_value, sin_source)`` per
-    implicit Euler step; ``temperature`` is the current temperature."""
+    ``compute(left, right, initial)`` with each end ("temperature", value),
+    ("flux", value) or ("convection", (heat_transfer, ambient_temperature))
+    (the kinds are fixed by compute, as the reference's matrix portrait), then
+    ``calc_step(left_value, right_value, sin_source)`` per implicit Euler step
+    (a convection end's value is its ambient temperature); ``temperature`` is
+    the current temperature."""
 
     def __init__(self, context: Context | None = None, elements: int = 200, order: int = 2, length: float = 1.0,
                  radius: float = 0.1, local_weight: float = 0.5, influence: str = "bell", conductivity: float = 1.0,
@@ -796,15 +798,18 @@ class NonstationaryHeatEquationSolver1D:
         self.time = 0.0
 
     def compute(self, left=("temperature", 0.0), right=("flux", 0.0), initial=None) -> None:
-        kinds = {"temperature": L.BC_TEMPERATURE, "flux": L.BC_FLUX}
+        kinds = {"temperature": L.BC_TEMPERATURE, "flux": L.BC_FLUX, "convection": L.BC_CONVECTION}
         t0 = None if initial is None else L.f64(initial)
         if t0 is not None and t0.shape != (self.n,):
             raise ValueError(f"the initial temperature needs {self.n} nodal values")
+        # a convection end: (heat transfer, ambient temperature); the step value is the ambient temperature
+        heat = [float(e[1][0]) if e[0] == "convection" else 0.0 for e in (left, right)]
+        L.check(self.ctx._lib.nlgpu_nonstationary_1d_convection(self.ctx.handle, heat[0], heat[1]))
         nodes = ctypes.c_int64()
         L.check(self.ctx._lib.nlgpu_nonstationary_1d_compute(self.ctx.handle, *self.args, kinds[left[0]],
                                                              kinds[right[0]], L.ptr(t0), ctypes.byref(nodes)))
         assert nodes.value == self.n
-        self.left, self.right = left, right
+        self.left, self.right = [(e[0], float(e[1][1])) if e[0] == "convection" else e for e in (left, right)]
 
     def calc_step(self, left_value: float | None = None, right_value: float | None = None,
                   sin_source: bool = False) -> np.ndarray:

@@ -552,7 +552,8 @@ int stationary1d() {
 
 // nonstationary_heat_equation_solver_1d (nonstationary_heat_equation_solver_1d.hpp:24-259):
 // one segment [0, 1], constant conductivity, capacity and density; each end a
-// temperature or a flux (left=t:<v> | f:<v>, right=...), source sin(pi x) or
+// temperature, a flux or a convection (left=t:<v> | f:<v> | c:<h>,<T_ambient>,
+// right=...), source sin(pi x) or
 // none, initial temperature 0 or sin(pi x); `steps` calls of calc_step, the
 // temperature after each dumped as history (steps x n).
 int nonstationary1d() {
@@ -586,6 +587,10 @@ int nonstationary1d() {
     const auto side = [](const std::string& spec) -> std::unique_ptr<thermal_boundary_condition_1d<T>> {
         const T v = std::stod(spec.substr(2));
         if (spec[0] == 't') return std::make_unique<temperature_1d<T>>(v);
+        if (spec[0] == 'c') {   // c:<heat transfer>,<ambient temperature>
+            const size_t comma = spec.find(',');
+            return std::make_unique<convection_1d<T>>(v, std::stod(spec.substr(comma + 1)));
+        }
         return std::make_unique<flux_1d<T>>(v);
     };
     thermal_boundaries_conditions_1d<T> bcs;

@@ -144,6 +144,11 @@ CASES = {
                                  "local_weight": 0.3, "influence": "triangle", "conductivity": 2, "capacity": 1.5,
                                  "density": 2, "dt": 5e-3, "steps": 4, "left": "f:-0.5", "right": "t:1",
                                  "source": "none", "initial": "sin"}),
+    "d1_nonstationary_convection": ({"none": True},
+                                    {"mode": "nonstationary1d", "elements": 60, "order": 2, "radius": 0.15,
+                                     "local_weight": 0.4, "influence": "bell", "conductivity": 1.5, "capacity": 1,
+                                     "density": 1, "dt": 1e-2, "steps": 5, "left": "c:2,1", "right": "c:0.5,-0.5",
+                                     "source": "sin", "initial": "sin"}),
     "d1_linear_40_triangle": ({"none": True},
                               {"mode": "stationary1d", "elements": 40, "order": 1, "quadrature": 2, "radius": 0.1,
                                "local_weight": 0.3, "influence": "triangle", "conductivity": 2,

@@ -3,7 +3,9 @@ nonstationary_heat_equation_solver_1d (tests/golden/d1_nonstationary_*: the
 temperature after every calc_step): quadratic elements with a bell kernel,
 left temperature / right flux and a sin(pi x) source from zero; linear
 elements with a triangle kernel, left flux / right temperature and a sin(pi x)
-initial temperature.  History within 1e-10 relative L2 per step."""
+initial temperature; quadratic elements with a convection at both ends
+(convection_1d: heat transfer and ambient temperature).  History within 1e-10
+relative L2 per step."""
 import numpy as np
 import pytest
 
@@ -25,11 +27,15 @@ def lib():
 
 
 def end(spec):
-    kind = {"t": "temperature", "f": "flux"}[spec[0]]
+    kind = {"t": "temperature", "f": "flux", "c": "convection"}[spec[0]]
+    if kind == "convection":   # c:<heat transfer>,<ambient temperature>
+        h, t = spec[2:].split(",")
+        return kind, (float(h), float(t))
     return kind, float(spec[2:])
 
 
-@pytest.mark.parametrize("name", ["d1_nonstationary_quadratic", "d1_nonstationary_linear"])
+@pytest.mark.parametrize("name", ["d1_nonstationary_quadratic", "d1_nonstationary_linear",
+                                  "d1_nonstationary_convection"])
 def test_nonstationary_1d_history(lib, name):
     from nonlocal_gb300 import thermal as T
     fx = gc.load(name)
@@ -56,8 +62,8 @@ def test_nonstationary_1d_rejects_other_ends(lib):
     from nonlocal_gb300 import _lib as L
     from nonlocal_gb300 import thermal as T
     s = T.NonstationaryHeatEquationSolver1D(elements=10, order=1)
-    with pytest.raises(L.NlgpuError):
-        L.check(s.ctx._lib.nlgpu_nonstationary_1d_compute(s.ctx.handle, *s.args, L.BC_CONVECTION, L.BC_FLUX, None,
+    with pytest.raises(L.NlgpuError):   # radiation ends are not built
+        L.check(s.ctx._lib.nlgpu_nonstationary_1d_compute(s.ctx.handle, *s.args, L.BC_RADIATION, L.BC_FLUX, None,
                                                           None))
     with pytest.raises(L.NlgpuError):   # no compute yet
         s.calc_step(0.0, 0.0)
